@@ -1,0 +1,192 @@
+/*
+ * tpm.h - C ABI of the GB300-native RK4 substep of the triply-periodic,
+ * low-Mach, particle-laden turbulence solver (libtpm.so).
+ *
+ * The library replaces the reference's per-operator C++ classes on the hot
+ * path: grid's substep sequence (grid.cpp:595-900), the field algebra of
+ * tensor0/tensor1 (tensor0.cpp, tensor1.cpp), the Lagrangian particle stage
+ * (particle.cpp:58-654) and the FFT pressure projection (poisson.cpp:391-462).
+ * One context owns one periodic box resident on one GPU; the reference's MPI
+ * halo exchange and particle migration (communicator.cpp:157-373,
+ * particle.cpp:150-297,772-846) become periodic index wrap inside the kernels.
+ *
+ * Conventions
+ *  - Every call returns an int status (TPM_OK = 0, negative on error) and
+ *    never exits or traps; tpm_last_error() describes the last failure.
+ *  - Fields cross the boundary in the reference's file layout
+ *    (communicator.cpp:114-155): unghosted global FP64 arrays, C order
+ *    [Nz][Ny][Nx] (x fastest); a vector field (tensor1) is the x, y and z
+ *    blocks back to back (3*Nx*Ny*Nz doubles).
+ *  - Particles cross as SoA host arrays of length np, like the restart files
+ *    Restart_Part_{x,y,z,u,v,w,T}.bin (FP64) and Restart_Part_flag.bin (int32)
+ *    (particle.cpp:939-989).
+ *  - A context is used from one host thread at a time.  Work is queued on
+ *    the context's CUDA stream; downloads synchronise.
+ */
+#ifndef TPM_H
+#define TPM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TPM_ABI_VERSION 1
+
+/* ---- status codes (the reference has none: void + std::cout + exit(1)) ---- */
+enum {
+  TPM_OK = 0,
+  TPM_ERR_ARG = -1,         /* bad argument / size / id */
+  TPM_ERR_CUDA = -2,        /* a CUDA runtime error */
+  TPM_ERR_TIMEOUT = -3,     /* a bounded device wait ran out */
+  TPM_ERR_NONFINITE = -4,   /* NaN/Inf detected in the state */
+  TPM_ERR_UNSUPPORTED = -5, /* option outside the ported path */
+  TPM_ERR_STATE = -6,       /* call out of order (e.g. step before initialize) */
+  TPM_ERR_NOMEM = -7        /* device allocation failed */
+};
+
+/* ---- arithmetic of the substep ---- */
+enum {
+  TPM_PREC_FP64 = 0,  /* plain FP64 path, parity with the reference */
+  TPM_PREC_MIXED = 1  /* FP32 stencils/FFT/particles, FP64 state, means and
+                         one FP64 defect-correction projection */
+};
+
+/*
+ * Run parameters: the fields of the reference's parameter deck
+ * (params.h:9-59, read in the token order of params.cpp:23-63) that the
+ * substep uses.  Derived constants are computed inside exactly as
+ * params.cpp:70-77 does: R=Cp-Cv, P0=Rho0*T0*R, Tp=Rhop*Dp*Dp/(18*Mu0),
+ * mp=Rhop*pi*Dp^3/6, N0=(int)(np0*Lx*Ly*Lz).  The "...1"/"...2" pairs switch
+ * at T_cur > threshold (params.cpp:80-86).
+ */
+typedef struct tpm_params {
+  int32_t Nx, Ny, Nz;       /* global grid, each a product of 2,3,5; Nx even */
+  int32_t precision;        /* TPM_PREC_* */
+  double Lx, Ly, Lz;        /* box size */
+  double dt, threshold;
+  int32_t cooling;          /* params.cpp:35 */
+  int32_t Iteration1, Iteration2;
+  int32_t TWC;              /* two-way momentum coupling */
+  double epsilon;           /* Poisson stop criterion on max|dp| */
+  int32_t ParticleGravity;
+  int32_t elongated_box;    /* must be 0 (outside the ported path) */
+  int32_t solve_for_scalar; /* must be 0 */
+  int32_t solve_for_vector; /* must be 0 */
+  double A1, A2;            /* linear forcing coefficient */
+  double Rho0;
+  double U0, V0, W0;        /* mean momentum target per component / Rho0 */
+  double T0;
+  double Mu0, k;            /* viscosity, conductivity */
+  double gx1, gy1, gz1, gx2, gy2, gz2;
+  double Cp, Cv;
+  double np0;               /* particle number density */
+  double Dp, Rhop, Cvp, epsilonp, Nu;
+  double I01, I02;          /* radiative intensity */
+} tpm_params;
+
+/* Field identifiers for upload/download.  Vector fields are 3*N doubles. */
+enum {
+  TPM_FIELD_RU = 0,      /* grid.h:57  rho*u on faces (vector)                 */
+  TPM_FIELD_RU_INT,      /* grid.h:58  stage value (vector)                    */
+  TPM_FIELD_RU_NEW,      /* grid.h:59  next stage value (vector)               */
+  TPM_FIELD_RU_NP1,      /* grid.h:60  next step accumulator (vector)          */
+  TPM_FIELD_RHO,         /* grid.h:85  density at centres                      */
+  TPM_FIELD_RHO_INT,
+  TPM_FIELD_RHO_NEW,
+  TPM_FIELD_RHO_NP1,
+  TPM_FIELD_P,           /* grid.h:72  hydrodynamic pressure                   */
+  TPM_FIELD_C,           /* grid.h:78  particle concentration                  */
+  TPM_FIELD_Q,           /* grid.h:98  RHS_Part_Temp, particle heat per cell   */
+  TPM_FIELD_FP,          /* part2gas_velocity output: two-way momentum source
+                            before the -mp/Vcell factor (vector)               */
+  TPM_FIELD_RHS_POIS,    /* grid.h:76  Poisson right-hand side (mean removed)  */
+  TPM_FIELD_DIVERGENCE,  /* grid.h:97  thermodynamic divergence constraint     */
+  TPM_FIELD_COUNT
+};
+
+/* Particle copies (particle.h:61-113). */
+enum { TPM_PSET_BASE = 0, TPM_PSET_INT = 1, TPM_PSET_NEW = 2, TPM_PSET_NP1 = 3 };
+
+typedef struct tpm_scalars {
+  double P0, P0_int, P0_new, P0_np1; /* grid.h:100-103 */
+  double T_cur;                      /* grid.h:106 */
+  int64_t num_timestep;              /* grid.h:107 */
+  int32_t last_poisson_iterations;   /* poisson.h:74 num_iteration_ */
+  int32_t total_poisson_iterations;  /* sum over all solves since create */
+  double last_poisson_error;         /* max|dp| of the last iteration */
+  double max_abs_div;                /* FP64 post-projection max|div u - divergence|
+                                        of the last stage (mixed path only; else -1) */
+} tpm_scalars;
+
+typedef struct tpm_ctx tpm_ctx;
+
+int tpm_abi_version(void);
+
+/* Create a context for one box with np particles on the current CUDA device.
+ * Rejects options outside the ported path (HYPRE solvers, passive scalar,
+ * passive vector, elongated box) with TPM_ERR_UNSUPPORTED. */
+int tpm_create(const tpm_params *params, int64_t np, tpm_ctx **out);
+int tpm_destroy(tpm_ctx *ctx);
+const char *tpm_last_error(const tpm_ctx *ctx);
+
+/* Fields (reference file layout, see above). */
+int tpm_upload_field(tpm_ctx *ctx, int field, const double *host);
+int tpm_download_field(tpm_ctx *ctx, int field, double *host);
+
+/* Particles: any pointer may be NULL to skip that quantity (flag too). */
+int tpm_upload_particles(tpm_ctx *ctx, int set, const double *x, const double *y,
+                         const double *z, const double *u, const double *v, const double *w,
+                         const double *T, const int32_t *flag);
+int tpm_download_particles(tpm_ctx *ctx, int set, double *x, double *y, double *z, double *u,
+                           double *v, double *w, double *T, int32_t *flag);
+/* particle.h:113 RHS_T (heat exchange rate, W) */
+int tpm_download_particle_rhs_t(tpm_ctx *ctx, double *rhs_t);
+/* Optional per-particle momentum relaxation time (extension: the reference has
+ * one global Tp, particle.cpp:365).  NULL restores the global Tp. */
+int tpm_set_particle_tau(tpm_ctx *ctx, const double *tau);
+
+/* Thermodynamic pressure, time and step counter (Restart_numbers.dat,
+ * grid.cpp:232-236). */
+int tpm_set_scalars(tpm_ctx *ctx, double P0, double T_cur, int64_t num_timestep);
+int tpm_get_scalars(tpm_ctx *ctx, tpm_scalars *out);
+
+/* grid::Initialize tail (grid.cpp:461-484): stage copies, face density and
+ * the initial particle heat coupling.  Call after uploading RU, Rho, P,
+ * particles and scalars. */
+int tpm_initialize(tpm_ctx *ctx);
+
+/* One RK4 substep (simulation.cpp:62-77 with Update_Particle enabled):
+ * Update_Rho, Update_P0, Update_Particle, Update_RU_WOP, Compute_Div_U_new,
+ * Compute_RHS_Pois, Solve_Poisson, Update_RU_WP, TimeAdvance_RK4. */
+int tpm_substep(tpm_ctx *ctx, int rk_stage);
+/* End of a time step (simulation.cpp:80,91): RU_np1.make_mean_U0, TimeAdvance. */
+int tpm_end_step(tpm_ctx *ctx);
+/* PARAM.update(T_cur) + 4 substeps + end of step (simulation.cpp:58-91). */
+int tpm_step(tpm_ctx *ctx);
+int tpm_run(tpm_ctx *ctx, int nsteps);
+int tpm_sync(tpm_ctx *ctx);
+
+/* poisson::Solve with Solver==0 (poisson.h:79, poisson.cpp:391-462) on host
+ * buffers: div(C grad P) = RHS by Richardson iteration preconditioned with
+ * the FFT constant-coefficient solve.  C is a vector field (3N), P holds the
+ * initial guess and receives the result.  Uses the context's grid. */
+int tpm_poisson_solve(tpm_ctx *ctx, const double *C3, double *P, const double *RHS,
+                      int max_iterations, double epsilon, int *iterations_out,
+                      double *error_out);
+
+/* Per-kernel timing with CUDA events on the context stream (for the bench). */
+int tpm_profile_enable(tpm_ctx *ctx, int on);
+/* Fills names (NUL separated, up to cap bytes), launches and total ms per
+ * kernel; returns the number of kernels (or a negative status). */
+int tpm_profile_report(tpm_ctx *ctx, char *names, int cap, int *launches, double *total_ms,
+                       int max_kernels);
+int tpm_profile_reset(tpm_ctx *ctx);
+/* Number of kernel launches issued by this context since create. */
+int64_t tpm_launch_count(const tpm_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TPM_H */
