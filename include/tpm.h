@@ -176,6 +176,13 @@ int tpm_poisson_solve(tpm_ctx *ctx, const double *C3, double *P, const double *R
                       int max_iterations, double epsilon, int *iterations_out,
                       double *error_out);
 
+/* Options (tpm_set_option). */
+enum {
+  TPM_OPT_STORE_DIVERGENCE = 1 /* keep the divergence constraint field for download
+                                  (grid.h:97); off by default to save bandwidth */
+};
+int tpm_set_option(tpm_ctx *ctx, int option, int value);
+
 /* Per-kernel timing with CUDA events on the context stream (for the bench). */
 int tpm_profile_enable(tpm_ctx *ctx, int on);
 /* Fills names (NUL separated, up to cap bytes), launches and total ms per

@@ -1,0 +1,629 @@
+// Context and C ABI of libtpm.so (declared in include/tpm.h).
+//
+// The context plays the part of the reference's grid object (grid.h:14-137)
+// for one box resident on one GPU: it owns every field and particle array,
+// one CUDA stream, and runs the substep sequence of simulation.cpp:60-78
+// (with the particle stage of simulation.cpp:64 enabled) as a fixed series of
+// kernel launches with no host round trip, except that a Poisson solve with
+// a positive stopping tolerance reads max|dp| back after each iteration, as
+// poisson.cpp:397 decides on it.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <utility>
+
+#include "tpm_internal.cuh"
+#include "tpm_reduce.cuh"
+
+using tpm::Grid;
+
+namespace {
+
+const double kPreH[4] = {0.5, 0.5, 1., 1. / 6.};  // grid.cpp:18-21
+
+bool factorable(int n) {
+  if (n < 1) return false;
+  for (int f : {2, 3, 5})
+    while (n % f == 0) n /= f;
+  return n == 1;
+}
+
+template <typename T>
+T *dalloc(tpm_ctx *c, size_t count) {
+  void *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw std::make_pair(TPM_ERR_NOMEM, std::string("cudaMalloc of ") +
+                                            std::to_string(count * sizeof(T)) + " bytes failed");
+  }
+  c->allocs.push_back(p);
+  return reinterpret_cast<T *>(p);
+}
+
+int fail(tpm_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+// Runs f, mapping exceptions to status codes (the library never exits).
+template <typename F>
+int guarded(tpm_ctx *c, F &&f) {
+  if (!c) return TPM_ERR_ARG;
+  try {
+    return f();
+  } catch (const std::pair<int, std::string> &e) {
+    return fail(c, e.first, e.second);
+  } catch (const std::string &s) {
+    return fail(c, TPM_ERR_CUDA, s);
+  } catch (const std::bad_alloc &) {
+    return fail(c, TPM_ERR_NOMEM, "host allocation failed");
+  }
+}
+
+void push_scalars(tpm_ctx *c) {
+  TPM_CUDA_TRY(cudaMemcpyAsync(c->dsc, c->hsc, sizeof(tpm::DevScalars), cudaMemcpyHostToDevice,
+                               c->stream));
+  TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+}
+
+void pull_scalars(tpm_ctx *c) {
+  TPM_CUDA_TRY(cudaMemcpyAsync(c->hsc, c->dsc, sizeof(tpm::DevScalars), cudaMemcpyDeviceToHost,
+                               c->stream));
+  TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+}
+
+// device field pointer and its length in doubles
+double *field_ptr(tpm_ctx *c, int f, long long *len, bool for_download) {
+  const long long n = c->g.n;
+  *len = n;
+  bool nb = c->np1_is_base && for_download;
+  switch (f) {
+    case TPM_FIELD_RU: *len = 3 * n; return c->RU;
+    case TPM_FIELD_RU_INT: *len = 3 * n; return c->RU_int;
+    case TPM_FIELD_RU_NEW: *len = 3 * n; return c->RU_new;
+    case TPM_FIELD_RU_NP1: *len = 3 * n; return nb ? c->RU : c->RU_np1;
+    case TPM_FIELD_RHO: return c->Rho;
+    case TPM_FIELD_RHO_INT: return c->Rho_int;
+    case TPM_FIELD_RHO_NEW: return c->Rho_new;
+    case TPM_FIELD_RHO_NP1: return nb ? c->Rho : c->Rho_np1;
+    case TPM_FIELD_P: return c->P;
+    case TPM_FIELD_C: return c->C;
+    case TPM_FIELD_Q: return c->Q;
+    case TPM_FIELD_FP: *len = 3 * n; return c->Fp;
+    case TPM_FIELD_RHS_POIS: return c->RHS;
+    case TPM_FIELD_DIVERGENCE: return c->divg;
+    default: return nullptr;
+  }
+}
+
+// np1 copies alias the base copies after initialize / end of step; make
+// them real before a caller overwrites either side.
+void materialize_np1(tpm_ctx *c) {
+  if (!c->np1_is_base) return;
+  const long long n = c->g.n;
+  TPM_CUDA_TRY(cudaMemcpyAsync(c->RU_np1, c->RU, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, c->stream));
+  TPM_CUDA_TRY(cudaMemcpyAsync(c->Rho_np1, c->Rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+  for (int q = 0; q < 7 && c->np > 0; ++q)
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->pq[3][q], c->pq[0][q], sizeof(double) * c->np,
+                                 cudaMemcpyDeviceToDevice, c->stream));
+  TPM_CUDA_TRY(cudaMemcpyAsync(&c->dsc->P0_np1, &c->dsc->P0, sizeof(double), cudaMemcpyDeviceToDevice,
+                               c->stream));
+  c->np1_is_base = false;
+}
+
+// PARAM.update (params.cpp:80-86)
+void param_update(tpm_ctx *c) {
+  if (c->T_cur > c->p.threshold) {
+    c->Iteration = c->p.Iteration2;
+    c->A = c->p.A2;
+    c->gx = c->p.gx2;
+    c->gy = c->p.gy2;
+    c->gz = c->p.gz2;
+    c->I0 = c->p.I02;
+  }
+}
+
+// poisson::FFT iteration control (poisson.cpp:395-410)
+void poisson_loop(tpm_ctx *c, int max_it, double eps) {
+  int it = 0;
+  double error = 100;
+  const bool need_err = eps > 0;
+  while ((it < max_it) && (error > eps)) {
+    tpm::poisson_iteration(c);
+    it++;
+    if (need_err) {
+      TPM_CUDA_TRY(cudaMemcpyAsync(&c->hsc->err, &c->dsc->err, sizeof(double),
+                                   cudaMemcpyDeviceToHost, c->stream));
+      TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+      error = c->hsc->err;
+    }
+  }
+  c->last_it = it;
+  c->total_it += it;
+  if (need_err) c->last_err = error;
+}
+
+void swap_stage(tpm_ctx *c) {
+  // grid::TimeAdvance_RK4 (grid.cpp:890-900): int = new
+  std::swap(c->RU_int, c->RU_new);
+  std::swap(c->Rho_int, c->Rho_new);
+  for (int q = 0; q < 7; ++q) std::swap(c->pq[1][q], c->pq[2][q]);
+  TPM_CUDA_TRY(cudaMemcpyAsync(&c->dsc->P0_int, &c->dsc->P0_new, sizeof(double),
+                               cudaMemcpyDeviceToDevice, c->stream));
+}
+
+void substep(tpm_ctx *c, int s) {
+  const bool nb = c->np1_is_base;
+  tpm::launch_p0_update(c, s);
+  tpm::launch_rho_update(c, s, nb);
+  tpm::launch_face_velocity(c);
+  tpm::launch_particle_push(c, s, nb);
+  tpm::particle_deposit_momentum(c);
+  tpm::particle_deposit_concentration(c);
+  tpm::particle_heat(c);
+  tpm::launch_rhs_momentum(c, s, nb);
+  tpm::launch_poisson_rhs(c, s, c->store_div);
+  poisson_loop(c, c->Iteration, c->p.epsilon);
+  tpm::launch_project(c, s);
+  swap_stage(c);
+  c->np1_is_base = false;
+}
+
+void end_step(tpm_ctx *c) {
+  // simulation.cpp:80 then grid::TimeAdvance (grid.cpp:595-606)
+  tpm::launch_mean_reset(c);
+  std::swap(c->Rho, c->Rho_np1);
+  for (int q = 0; q < 7; ++q) std::swap(c->pq[0][q], c->pq[3][q]);
+  TPM_CUDA_TRY(cudaMemcpyAsync(&c->dsc->P0, &c->dsc->P0_np1, sizeof(double),
+                               cudaMemcpyDeviceToDevice, c->stream));
+  c->T_cur += c->p.dt;
+  c->num_timestep++;
+  c->np1_is_base = true;
+}
+
+}  // namespace
+
+namespace tpm {
+
+void prof_begin(tpm_ctx *c, const char *, cudaEvent_t *ev0) {
+  cudaEventCreate(ev0);
+  cudaEventRecord(*ev0, c->stream);
+}
+
+void prof_end(tpm_ctx *c, const char *name, cudaEvent_t ev0) {
+  cudaEvent_t ev1;
+  cudaEventCreate(&ev1);
+  cudaEventRecord(ev1, c->stream);
+  for (auto &e : c->prof) {
+    if (e.name == name) {
+      e.pending.emplace_back(ev0, ev1);
+      return;
+    }
+  }
+  ProfEntry e;
+  e.name = name;
+  e.pending.emplace_back(ev0, ev1);
+  c->prof.push_back(std::move(e));
+}
+
+}  // namespace tpm
+
+extern "C" {
+
+int tpm_abi_version(void) { return TPM_ABI_VERSION; }
+
+const char *tpm_last_error(const tpm_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
+  if (!p || !out) return TPM_ERR_ARG;
+  *out = nullptr;
+  tpm_ctx *c = new (std::nothrow) tpm_ctx();
+  if (!c) return TPM_ERR_NOMEM;
+  c->p = *p;
+  *out = c;
+  if (p->elongated_box || p->solve_for_scalar || p->solve_for_vector)
+    return fail(c, TPM_ERR_UNSUPPORTED,
+                "elongated box, passive scalar and passive vector are outside the ported path");
+  if (p->precision != TPM_PREC_FP64 && p->precision != TPM_PREC_MIXED)
+    return fail(c, TPM_ERR_ARG, "unknown precision");
+  if (!factorable(p->Nx) || !factorable(p->Ny) || !factorable(p->Nz) || (p->Nx % 2) ||
+      p->Nx < 4 || p->Ny < 2 || p->Nz < 2)
+    return fail(c, TPM_ERR_ARG, "grid sizes must be products of 2, 3, 5 with Nx even and >= 4");
+  if (p->Nx / 2 > 2048 || p->Ny > 2048 || p->Nz > 2048)
+    return fail(c, TPM_ERR_ARG, "FFT pencils are limited to 2048 points (Nx <= 4096, Ny, Nz <= 2048)");
+  long long n = (long long)p->Nx * p->Ny * p->Nz;
+  if (n >= (1LL << 31) - 1 || np < 0 || np >= (1LL << 31) - 1)
+    return fail(c, TPM_ERR_ARG, "grid or particle count exceeds 2^31");
+  if (!(p->dt > 0) || !(p->Lx > 0) || !(p->Ly > 0) || !(p->Lz > 0) || !(p->Mu0 > 0))
+    return fail(c, TPM_ERR_ARG, "dt, box lengths and Mu0 must be positive");
+  if (p->Iteration1 < 0 || p->Iteration2 < 0)
+    return fail(c, TPM_ERR_ARG, "iteration counts must be >= 0");
+  return guarded(c, [&]() -> int {
+    TPM_CUDA_TRY(cudaGetDevice(&c->dev));
+    Grid &g = c->g;
+    g.nx = p->Nx; g.ny = p->Ny; g.nz = p->Nz; g.nxh = p->Nx / 2 + 1; g.n = n;
+    g.Lx = p->Lx; g.Ly = p->Ly; g.Lz = p->Lz;
+    g.dx = p->Lx / p->Nx; g.dy = p->Ly / p->Ny; g.dz = p->Lz / p->Nz;  // gridsize.cpp:25-27
+    g.inv_dx = 1. / g.dx; g.inv_dy = 1. / g.dy; g.inv_dz = 1. / g.dz;  // tensor0.cpp:17-22
+    g.inv_dx2 = 1. / (g.dx * g.dx); g.inv_dy2 = 1. / (g.dy * g.dy); g.inv_dz2 = 1. / (g.dz * g.dz);
+    g.idx = 1. / g.dx; g.idy = 1. / g.dy; g.idz = 1. / g.dz;          // particle.cpp:19-21
+    g.xh = p->Nx * g.dx; g.yh = p->Ny * g.dy; g.zh = p->Nz * g.dz;    // gridsize.cpp:72-77
+    // params.cpp:70-77
+    c->R = p->Cp - p->Cv;
+    c->P0ref = p->Rho0 * p->T0 * c->R;
+    c->Tp = p->Rhop * p->Dp * p->Dp / (18 * p->Mu0);
+    c->mp = p->Rhop * tpm::kPi * p->Dp * p->Dp * p->Dp / 6.;
+    c->Vcell = g.dx * g.dy * g.dz;  // gridsize.h:43
+    c->Iteration = p->Iteration1;
+    c->A = p->A1; c->gx = p->gx1; c->gy = p->gy1; c->gz = p->gz1; c->I0 = p->I01;
+    c->np = np;
+    TPM_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    // fields
+    c->RU = dalloc<double>(c, 3 * n); c->RU_int = dalloc<double>(c, 3 * n);
+    c->RU_new = dalloc<double>(c, 3 * n); c->RU_np1 = dalloc<double>(c, 3 * n);
+    c->Rho = dalloc<double>(c, n); c->Rho_int = dalloc<double>(c, n);
+    c->Rho_new = dalloc<double>(c, n); c->Rho_np1 = dalloc<double>(c, n);
+    c->P = dalloc<double>(c, n); c->C = dalloc<double>(c, n); c->Q = dalloc<double>(c, n);
+    c->Fp = dalloc<double>(c, 3 * n); c->U = dalloc<double>(c, 3 * n);
+    c->RHS = dalloc<double>(c, n); c->divg = dalloc<double>(c, n);
+    c->inv_rho = dalloc<double>(c, n); c->Tgas = dalloc<double>(c, n);
+    c->Cface = dalloc<double>(c, 3 * n); c->cc = dalloc<double>(c, n);
+    c->spec = dalloc<double2>(c, (size_t)g.nxh * g.ny * g.nz);
+    c->partials = dalloc<double>(c, (size_t)tpm::kPartRegions * tpm::kRedBlocks);
+    c->dsc = dalloc<tpm::DevScalars>(c, 1);
+    TPM_CUDA_TRY(cudaMallocHost(&c->hsc, sizeof(tpm::DevScalars)));
+    std::memset(c->hsc, 0, sizeof(tpm::DevScalars));
+    const long long zero_fields[] = {0};
+    (void)zero_fields;
+    for (double *f : {c->RU, c->RU_int, c->RU_new, c->RU_np1, c->Fp, c->U, c->Cface})
+      TPM_CUDA_TRY(cudaMemsetAsync(f, 0, sizeof(double) * 3 * n, c->stream));
+    for (double *f : {c->Rho, c->Rho_int, c->Rho_new, c->Rho_np1, c->P, c->C, c->Q, c->RHS,
+                      c->divg, c->inv_rho, c->Tgas, c->cc})
+      TPM_CUDA_TRY(cudaMemsetAsync(f, 0, sizeof(double) * n, c->stream));
+    TPM_CUDA_TRY(cudaMemsetAsync(c->partials, 0, sizeof(double) * tpm::kPartRegions * tpm::kRedBlocks,
+                                 c->stream));
+    c->hsc->P0 = c->hsc->P0_int = c->hsc->P0_np1 = c->hsc->P0_new = c->P0ref;
+    push_scalars(c);
+    tpm::fft_plans_create(c);
+    c->x_blocks = tpm::fft_x_blocks(c);
+    c->err_parts = dalloc<double>(c, c->x_blocks);
+    // particles
+    for (int s = 0; s < 4; ++s)
+      for (int q = 0; q < 7; ++q) {
+        c->pq[s][q] = dalloc<double>(c, np);
+        TPM_CUDA_TRY(cudaMemsetAsync(c->pq[s][q], 0, sizeof(double) * (np ? np : 1), c->stream));
+      }
+    c->rhs_t = dalloc<double>(c, np);
+    TPM_CUDA_TRY(cudaMemsetAsync(c->rhs_t, 0, sizeof(double) * (np ? np : 1), c->stream));
+    c->flag = dalloc<int32_t>(c, np);
+    c->key_t = dalloc<int32_t>(c, np);
+    c->key_r = dalloc<int32_t>(c, np);
+    c->perm_t = dalloc<int32_t>(c, np);
+    c->perm_r[0] = dalloc<int32_t>(c, np);
+    c->perm_r[1] = dalloc<int32_t>(c, np);
+    c->starts_t = dalloc<int32_t>(c, n + 1);
+    c->starts_r[0] = dalloc<int32_t>(c, n + 1);
+    c->starts_r[1] = dalloc<int32_t>(c, n + 1);
+    c->counts = dalloc<int32_t>(c, n);
+    c->scan_blocks = dalloc<int32_t>(c, (size_t)(n / 4096 + 2));
+    c->pay_t = dalloc<double>(c, 6 * (size_t)np);
+    c->pay_t_s = dalloc<double>(c, 6 * (size_t)np);
+    c->pay_r = dalloc<double>(c, 4 * (size_t)np);
+    c->pay_r_s[0] = dalloc<double>(c, 4 * (size_t)np);
+    c->pay_r_s[1] = dalloc<double>(c, 4 * (size_t)np);
+    TPM_CUDA_TRY(cudaMemsetAsync(c->starts_r[0], 0, sizeof(int32_t) * (n + 1), c->stream));
+    TPM_CUDA_TRY(cudaMemsetAsync(c->starts_r[1], 0, sizeof(int32_t) * (n + 1), c->stream));
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return TPM_OK;
+  });
+}
+
+int tpm_destroy(tpm_ctx *c) {
+  if (!c) return TPM_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto &e : c->prof)
+    for (auto &ev : e.pending) {
+      cudaEventDestroy(ev.first);
+      cudaEventDestroy(ev.second);
+    }
+  for (void *p : c->allocs) cudaFree(p);
+  if (c->fft_mem) cudaFree(c->fft_mem);
+  if (c->hsc) cudaFreeHost(c->hsc);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return TPM_OK;
+}
+
+int tpm_set_option(tpm_ctx *c, int option, int value) {
+  return guarded(c, [&]() -> int {
+    if (option == TPM_OPT_STORE_DIVERGENCE) {
+      c->store_div = value != 0;
+      return TPM_OK;
+    }
+    return fail(c, TPM_ERR_ARG, "unknown option");
+  });
+}
+
+int tpm_upload_field(tpm_ctx *c, int field, const double *host) {
+  return guarded(c, [&]() -> int {
+    if (!host) return fail(c, TPM_ERR_ARG, "null host buffer");
+    if (field == TPM_FIELD_RU_NP1 || field == TPM_FIELD_RHO_NP1 || field == TPM_FIELD_RU ||
+        field == TPM_FIELD_RHO)
+      materialize_np1(c);
+    long long len;
+    double *d = field_ptr(c, field, &len, false);
+    if (!d) return fail(c, TPM_ERR_ARG, "unknown field id");
+    TPM_CUDA_TRY(cudaMemcpyAsync(d, host, sizeof(double) * len, cudaMemcpyHostToDevice, c->stream));
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return TPM_OK;
+  });
+}
+
+int tpm_download_field(tpm_ctx *c, int field, double *host) {
+  return guarded(c, [&]() -> int {
+    if (!host) return fail(c, TPM_ERR_ARG, "null host buffer");
+    long long len;
+    double *d = field_ptr(c, field, &len, true);
+    if (!d) return fail(c, TPM_ERR_ARG, "unknown field id");
+    TPM_CUDA_TRY(cudaMemcpyAsync(host, d, sizeof(double) * len, cudaMemcpyDeviceToHost, c->stream));
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (field == TPM_FIELD_RHS_POIS) {
+      // the kernels keep RHS_Pois un-normalised and subtract its mean where
+      // they read it; apply make_mean_zero (grid.cpp:848) for the caller
+      pull_scalars(c);
+      const double m = c->hsc->mean_rhs;
+      for (long long i = 0; i < len; ++i) host[i] -= m;
+    }
+    return TPM_OK;
+  });
+}
+
+int tpm_upload_particles(tpm_ctx *c, int set, const double *x, const double *y, const double *z,
+                         const double *u, const double *v, const double *w, const double *T,
+                         const int32_t *flag) {
+  return guarded(c, [&]() -> int {
+    if (set < 0 || set > 3) return fail(c, TPM_ERR_ARG, "bad particle set");
+    if (set == TPM_PSET_BASE || set == TPM_PSET_NP1) materialize_np1(c);
+    const double *src[7] = {x, y, z, u, v, w, T};
+    for (int q = 0; q < 7; ++q)
+      if (src[q] && c->np)
+        TPM_CUDA_TRY(cudaMemcpyAsync(c->pq[set][q], src[q], sizeof(double) * c->np,
+                                     cudaMemcpyHostToDevice, c->stream));
+    if (flag && c->np)
+      TPM_CUDA_TRY(cudaMemcpyAsync(c->flag, flag, sizeof(int32_t) * c->np, cudaMemcpyHostToDevice,
+                                   c->stream));
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return TPM_OK;
+  });
+}
+
+int tpm_download_particles(tpm_ctx *c, int set, double *x, double *y, double *z, double *u,
+                           double *v, double *w, double *T, int32_t *flag) {
+  return guarded(c, [&]() -> int {
+    if (set < 0 || set > 3) return fail(c, TPM_ERR_ARG, "bad particle set");
+    int s = (set == TPM_PSET_NP1 && c->np1_is_base) ? TPM_PSET_BASE : set;
+    double *dst[7] = {x, y, z, u, v, w, T};
+    for (int q = 0; q < 7; ++q)
+      if (dst[q] && c->np)
+        TPM_CUDA_TRY(cudaMemcpyAsync(dst[q], c->pq[s][q], sizeof(double) * c->np,
+                                     cudaMemcpyDeviceToHost, c->stream));
+    if (flag && c->np)
+      TPM_CUDA_TRY(cudaMemcpyAsync(flag, c->flag, sizeof(int32_t) * c->np, cudaMemcpyDeviceToHost,
+                                   c->stream));
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return TPM_OK;
+  });
+}
+
+int tpm_download_particle_rhs_t(tpm_ctx *c, double *rhs_t) {
+  return guarded(c, [&]() -> int {
+    if (!rhs_t) return fail(c, TPM_ERR_ARG, "null host buffer");
+    if (c->np)
+      TPM_CUDA_TRY(cudaMemcpyAsync(rhs_t, c->rhs_t, sizeof(double) * c->np, cudaMemcpyDeviceToHost,
+                                   c->stream));
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return TPM_OK;
+  });
+}
+
+int tpm_set_particle_tau(tpm_ctx *c, const double *tau) {
+  return guarded(c, [&]() -> int {
+    if (!tau) {
+      c->tau = nullptr;
+      return TPM_OK;
+    }
+    for (int64_t i = 0; i < c->np; ++i)
+      if (!(tau[i] > 0)) return fail(c, TPM_ERR_ARG, "particle relaxation times must be > 0");
+    if (!c->tau_buf) c->tau_buf = dalloc<double>(c, c->np);
+    if (c->np)
+      TPM_CUDA_TRY(cudaMemcpyAsync(c->tau_buf, tau, sizeof(double) * c->np, cudaMemcpyHostToDevice,
+                                   c->stream));
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->tau = c->tau_buf;
+    return TPM_OK;
+  });
+}
+
+int tpm_set_scalars(tpm_ctx *c, double P0, double T_cur, int64_t num_timestep) {
+  return guarded(c, [&]() -> int {
+    pull_scalars(c);
+    c->hsc->P0 = P0;
+    push_scalars(c);
+    c->T_cur = T_cur;
+    c->num_timestep = num_timestep;
+    return TPM_OK;
+  });
+}
+
+int tpm_get_scalars(tpm_ctx *c, tpm_scalars *out) {
+  return guarded(c, [&]() -> int {
+    if (!out) return fail(c, TPM_ERR_ARG, "null output");
+    pull_scalars(c);
+    out->P0 = c->hsc->P0;
+    out->P0_int = c->hsc->P0_int;
+    out->P0_new = c->hsc->P0_new;
+    out->P0_np1 = c->np1_is_base ? c->hsc->P0 : c->hsc->P0_np1;
+    out->T_cur = c->T_cur;
+    out->num_timestep = c->num_timestep;
+    out->last_poisson_iterations = c->last_it;
+    out->total_poisson_iterations = c->total_it;
+    out->last_poisson_error = c->p.epsilon > 0 ? c->last_err : c->hsc->err;
+    out->max_abs_div = c->p.precision == TPM_PREC_MIXED ? c->hsc->max_div : -1.0;
+    if (!std::isfinite(c->hsc->mean_ru[0]) || !std::isfinite(c->hsc->mean_ru[1]) ||
+        !std::isfinite(c->hsc->mean_ru[2]) || !std::isfinite(c->hsc->P0))
+      return fail(c, TPM_ERR_NONFINITE, "non-finite momentum or pressure in the state");
+    return TPM_OK;
+  });
+}
+
+int tpm_initialize(tpm_ctx *c) {
+  return guarded(c, [&]() -> int {
+    const long long n = c->g.n;
+    // grid.cpp:461-472: stage and step copies
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->RU_int, c->RU, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, c->stream));
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->Rho_int, c->Rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+    for (int q = 0; q < 7 && c->np > 0; ++q)
+      TPM_CUDA_TRY(cudaMemcpyAsync(c->pq[1][q], c->pq[0][q], sizeof(double) * c->np,
+                                   cudaMemcpyDeviceToDevice, c->stream));
+    pull_scalars(c);
+    c->hsc->P0_int = c->hsc->P0;
+    c->hsc->P0_np1 = c->hsc->P0;
+    push_scalars(c);
+    c->np1_is_base = true;
+    // grid.cpp:474 (Rho_face is recomputed from Rho_int where it is needed)
+    // grid.cpp:481-484: initial particle heat coupling
+    tpm::particle_zero_fields(c);
+    tpm::particle_init_heat(c);
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->initialized = true;
+    return TPM_OK;
+  });
+}
+
+int tpm_substep(tpm_ctx *c, int rk_stage) {
+  return guarded(c, [&]() -> int {
+    if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
+    if (rk_stage < 0 || rk_stage > 3) return fail(c, TPM_ERR_ARG, "rk_stage must be 0..3");
+    substep(c, rk_stage);
+    return TPM_OK;
+  });
+}
+
+int tpm_end_step(tpm_ctx *c) {
+  return guarded(c, [&]() -> int {
+    if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
+    end_step(c);
+    return TPM_OK;
+  });
+}
+
+int tpm_step(tpm_ctx *c) {
+  return guarded(c, [&]() -> int {
+    if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
+    param_update(c);
+    for (int s = 0; s < 4; ++s) substep(c, s);
+    end_step(c);
+    return TPM_OK;
+  });
+}
+
+int tpm_run(tpm_ctx *c, int nsteps) {
+  return guarded(c, [&]() -> int {
+    if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
+    for (int k = 0; k < nsteps; ++k) {
+      param_update(c);
+      for (int s = 0; s < 4; ++s) substep(c, s);
+      end_step(c);
+    }
+    return TPM_OK;
+  });
+}
+
+int tpm_sync(tpm_ctx *c) {
+  return guarded(c, [&]() -> int {
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return TPM_OK;
+  });
+}
+
+int tpm_poisson_solve(tpm_ctx *c, const double *C3, double *P, const double *RHS,
+                      int max_iterations, double epsilon, int *iterations_out, double *error_out) {
+  return guarded(c, [&]() -> int {
+    if (!C3 || !P || !RHS) return fail(c, TPM_ERR_ARG, "null buffer");
+    const long long n = c->g.n;
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->Cface, C3, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, c->stream));
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->P, P, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->RHS, RHS, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+    pull_scalars(c);
+    c->hsc->mean_rhs = 0;  // poisson::Solve uses RHS as given
+    push_scalars(c);
+    tpm::launch_center_coeff_from_C(c);
+    const double eps_saved = c->last_err;
+    (void)eps_saved;
+    poisson_loop(c, max_iterations, epsilon);
+    TPM_CUDA_TRY(cudaMemcpyAsync(P, c->P, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    pull_scalars(c);
+    if (iterations_out) *iterations_out = c->last_it;
+    if (error_out) *error_out = c->hsc->err;
+    return TPM_OK;
+  });
+}
+
+int tpm_profile_enable(tpm_ctx *c, int on) {
+  return guarded(c, [&]() -> int {
+    c->prof_on = on != 0;
+    return TPM_OK;
+  });
+}
+
+int tpm_profile_reset(tpm_ctx *c) {
+  return guarded(c, [&]() -> int {
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    for (auto &e : c->prof)
+      for (auto &ev : e.pending) {
+        cudaEventDestroy(ev.first);
+        cudaEventDestroy(ev.second);
+      }
+    c->prof.clear();
+    return TPM_OK;
+  });
+}
+
+int tpm_profile_report(tpm_ctx *c, char *names, int cap, int *launches, double *total_ms,
+                       int max_kernels) {
+  return guarded(c, [&]() -> int {
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    for (auto &e : c->prof) {
+      for (auto &ev : e.pending) {
+        float ms = 0;
+        TPM_CUDA_TRY(cudaEventElapsedTime(&ms, ev.first, ev.second));
+        e.total_ms += ms;
+        e.launches++;
+        cudaEventDestroy(ev.first);
+        cudaEventDestroy(ev.second);
+      }
+      e.pending.clear();
+    }
+    int k = 0, off = 0;
+    for (auto &e : c->prof) {
+      if (k >= max_kernels) break;
+      int len = (int)e.name.size() + 1;
+      if (names && off + len <= cap) {
+        std::memcpy(names + off, e.name.c_str(), len);
+        off += len;
+      }
+      if (launches) launches[k] = e.launches;
+      if (total_ms) total_ms[k] = e.total_ms;
+      ++k;
+    }
+    return k;
+  });
+}
+
+int64_t tpm_launch_count(const tpm_ctx *c) { return c ? c->launches : 0; }
+
+}  // extern "C"

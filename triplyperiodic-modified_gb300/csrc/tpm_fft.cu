@@ -1,0 +1,503 @@
+// Pressure projection: poisson::FFT / poisson::CCP_FFT (poisson.cpp:391-462)
+// as hand-written pencil FFTs in shared memory.
+//
+// One Richardson iteration is five kernels over a half-complex spectrum
+// [Nz][Ny][Nx/2+1] (the reference transforms a full complex box whose input
+// is real, poisson.cpp:423-431; a real-to-complex transform is the same
+// transform at half the traffic):
+//   1. x-pass: residual r = cc*(div(C grad P) - RHS) of a block of x-rows,
+//      computed on the fly, packed as Nx/2 complex points, FFT, real-to-
+//      complex post-processing, written to the spectrum;
+//   2. y-pass forward;
+//   3. z-pass: forward FFT, divide by the modified wave number
+//      mwn = (2/dx^2)(1-cos kx dx) + ... except the zero mode
+//      (poisson.cpp:438-451), inverse FFT - all in shared memory;
+//   4. y-pass inverse;
+//   5. x-pass inverse: complex-to-real, dp = -x/N^3 (poisson.cpp:460),
+//      P += dp and a per-block max|dp| (poisson.cpp:405-407).
+// FFTs are mixed-radix (4, 2, 3, 5) Stockham auto-sort with twiddles from a
+// host table (cos/sin of 2 pi m/n).  Butterflies use explicit FMAs; the
+// residual and the update keep the reference's operation order.
+#include <cmath>
+#include <vector>
+
+#include "tpm_internal.cuh"
+#include "tpm_reduce.cuh"
+
+namespace tpm {
+namespace {
+
+constexpr int kFftThreads = 256;
+constexpr int kFftSmemPoints = 2048;  // complex points per ping-pong buffer
+
+template <typename T2>
+struct Cx;
+template <>
+struct Cx<double2> {
+  using T = double;
+  static __device__ __forceinline__ double2 mk(double a, double b) { return make_double2(a, b); }
+  static __device__ __forceinline__ double fma_(double a, double b, double c) {
+    return __fma_rn(a, b, c);
+  }
+  static __device__ __forceinline__ double2 tw(const FftPlan &p, int e) { return p.tw64[e]; }
+};
+template <>
+struct Cx<float2> {
+  using T = float;
+  static __device__ __forceinline__ float2 mk(float a, float b) { return make_float2(a, b); }
+  static __device__ __forceinline__ float fma_(float a, float b, float c) {
+    return __fmaf_rn(a, b, c);
+  }
+  static __device__ __forceinline__ float2 tw(const FftPlan &p, int e) { return p.tw32[e]; }
+};
+
+// (a) * (w or conj(w))
+template <typename T2>
+__device__ __forceinline__ T2 cmul(T2 a, T2 w, int sign) {
+  using C = Cx<T2>;
+  typename C::T wi = sign < 0 ? w.y : -w.y;
+  return C::mk(C::fma_(a.x, w.x, -a.y * wi), C::fma_(a.x, wi, a.y * w.x));
+}
+
+template <typename T2>
+__device__ __forceinline__ void dft_small(T2 *v, int R, int sign) {
+  using C = Cx<T2>;
+  using T = typename C::T;
+  if (R == 2) {
+    T2 a = v[0], b = v[1];
+    v[0] = C::mk(a.x + b.x, a.y + b.y);
+    v[1] = C::mk(a.x - b.x, a.y - b.y);
+  } else if (R == 4) {
+    T2 a = C::mk(v[0].x + v[2].x, v[0].y + v[2].y);
+    T2 b = C::mk(v[0].x - v[2].x, v[0].y - v[2].y);
+    T2 c = C::mk(v[1].x + v[3].x, v[1].y + v[3].y);
+    T2 d = C::mk(v[1].x - v[3].x, v[1].y - v[3].y);
+    T2 j = sign < 0 ? C::mk(d.y, -d.x) : C::mk(-d.y, d.x);  // d * (sign i)
+    v[0] = C::mk(a.x + c.x, a.y + c.y);
+    v[2] = C::mk(a.x - c.x, a.y - c.y);
+    v[1] = C::mk(b.x + j.x, b.y + j.y);
+    v[3] = C::mk(b.x - j.x, b.y - j.y);
+  } else if (R == 3) {
+    const T s3 = (T)0.86602540378443864676;
+    T s = sign < 0 ? -s3 : s3;
+    T2 sm = C::mk(v[1].x + v[2].x, v[1].y + v[2].y);
+    T2 df = C::mk(v[1].x - v[2].x, v[1].y - v[2].y);
+    T2 m = C::mk(C::fma_((T)-0.5, sm.x, v[0].x), C::fma_((T)-0.5, sm.y, v[0].y));
+    v[0] = C::mk(v[0].x + sm.x, v[0].y + sm.y);
+    v[1] = C::mk(C::fma_(-s, df.y, m.x), C::fma_(s, df.x, m.y));
+    v[2] = C::mk(C::fma_(s, df.y, m.x), C::fma_(-s, df.x, m.y));
+  } else {  // R == 5
+    const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;
+    const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;
+    T sa = sign < 0 ? -s1 : s1, sb = sign < 0 ? -s2 : s2;
+    T2 t1 = C::mk(v[1].x + v[4].x, v[1].y + v[4].y), t2 = C::mk(v[2].x + v[3].x, v[2].y + v[3].y);
+    T2 d1 = C::mk(v[1].x - v[4].x, v[1].y - v[4].y), d2 = C::mk(v[2].x - v[3].x, v[2].y - v[3].y);
+    T2 x0 = v[0];
+    T2 p1 = C::mk(C::fma_(c2, t2.x, C::fma_(c1, t1.x, x0.x)), C::fma_(c2, t2.y, C::fma_(c1, t1.y, x0.y)));
+    T2 p2 = C::mk(C::fma_(c1, t2.x, C::fma_(c2, t1.x, x0.x)), C::fma_(c1, t2.y, C::fma_(c2, t1.y, x0.y)));
+    T2 q1 = C::mk(C::fma_(sb, d2.x, sa * d1.x), C::fma_(sb, d2.y, sa * d1.y));
+    T2 q2 = C::mk(C::fma_(-sa, d2.x, sb * d1.x), C::fma_(-sa, d2.y, sb * d1.y));
+    v[0] = C::mk(x0.x + t1.x + t2.x, x0.y + t1.y + t2.y);
+    v[1] = C::mk(p1.x - q1.y, p1.y + q1.x);
+    v[4] = C::mk(p1.x + q1.y, p1.y - q1.x);
+    v[2] = C::mk(p2.x - q2.y, p2.y + q2.x);
+    v[3] = C::mk(p2.x + q2.y, p2.y - q2.x);
+  }
+}
+
+// One Stockham stage of radix R:  for i in [0, n/R): k = i mod p,
+//   v_t = a[i + t n/R] * w^(k t n/(p R)),  V = DFT_R(v),
+//   b[(i/p) p R + k + u p] = V_u.
+template <int R, typename T2>
+__device__ __forceinline__ void stockham_stage(const T2 *__restrict__ a, T2 *__restrict__ b,
+                                               int npen, const FftPlan &pl, int p, int sign) {
+  const int n = pl.n;
+  const int m = n / R;
+  const int step = n / (p * R);
+  const int total = m * npen;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int q = idx % npen;
+    const int i = idx / npen;
+    const int k = i % p;
+    T2 v[R];
+    v[0] = a[i * npen + q];
+#pragma unroll
+    for (int t = 1; t < R; ++t) v[t] = cmul(a[(i + t * m) * npen + q], Cx<T2>::tw(pl, k * t * step), sign);
+    dft_small(v, R, sign);
+    const int j = (i / p) * p * R + k;
+#pragma unroll
+    for (int u = 0; u < R; ++u) b[(j + u * p) * npen + q] = v[u];
+  }
+}
+
+// Batched Stockham FFT in shared memory.  Element t of pencil q lives at
+// a[t*npen + q]; consecutive threads take consecutive pencils.  Returns the
+// buffer (a or b) that holds the result.  Ends with __syncthreads().
+template <typename T2>
+__device__ T2 *smem_fft(T2 *a, T2 *b, int npen, const FftPlan &pl, int sign) {
+  int p = 1;
+  for (int s = 0; s < pl.nst; ++s) {
+    const int R = pl.radix[s];
+    switch (R) {
+      case 4: stockham_stage<4>(a, b, npen, pl, p, sign); break;
+      case 2: stockham_stage<2>(a, b, npen, pl, p, sign); break;
+      case 3: stockham_stage<3>(a, b, npen, pl, p, sign); break;
+      default: stockham_stage<5>(a, b, npen, pl, p, sign); break;
+    }
+    __syncthreads();
+    T2 *t = a;
+    a = b;
+    b = t;
+    p *= R;
+  }
+  return a;
+}
+
+__device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
+  return ((long long)k * g.ny + j) * g.nx + i;
+}
+
+// ------------------------------------------------- 1. residual + R2C along x
+// poisson.cpp:399-404 (residual) and the first third of fft_3d (:431).
+template <typename T2>
+__global__ void k_xfwd_resid(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
+                             const double *__restrict__ P, const double *__restrict__ Cf,
+                             const double *__restrict__ cc, const double *__restrict__ RHS,
+                             const DevScalars *__restrict__ s, T2 *__restrict__ spec, int npen) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using T = typename Cx<T2>::T;
+  T2 *a = reinterpret_cast<T2 *>(smem_raw);
+  const int M = pl.n;  // nx/2
+  T2 *b = a + M * npen;
+  const long long nrows = (long long)g.ny * g.nz;
+  const long long row0 = (long long)blockIdx.x * npen;
+  const double mean = s->mean_rhs;
+  const double *Cx_ = Cf, *Cy_ = Cf + g.n, *Cz_ = Cf + 2 * g.n;
+  // residual, written interleaved as z[m] = r[2m] + i r[2m+1]
+  for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
+    const int q = idx / g.nx, i = idx % g.nx;
+    const long long row = row0 + q;
+    double r = 0;
+    if (row < nrows) {
+      const int j = (int)(row % g.ny), k = (int)(row / g.ny);
+      const long long c = at(g, i, j, k);
+      const int ip = wrap_p(i, g.nx), im = wrap_m(i, g.nx);
+      const int jp = wrap_p(j, g.ny), jm = wrap_m(j, g.ny);
+      const int kp = wrap_p(k, g.nz), km = wrap_m(k, g.nz);
+      const long long cxp = at(g, ip, j, k), cyp = at(g, i, jp, k), czp = at(g, i, j, kp);
+      const double pc = P[c];
+      // dummy = grad_C2F(P) * C at the low and high faces
+      double gx_hi = (P[cxp] - pc) * g.inv_dx * Cx_[cxp];
+      double gx_lo = (pc - P[at(g, im, j, k)]) * g.inv_dx * Cx_[c];
+      double gy_hi = (P[cyp] - pc) * g.inv_dy * Cy_[cyp];
+      double gy_lo = (pc - P[at(g, i, jm, k)]) * g.inv_dy * Cy_[c];
+      double gz_hi = (P[czp] - pc) * g.inv_dz * Cz_[czp];
+      double gz_lo = (pc - P[at(g, i, j, km)]) * g.inv_dz * Cz_[c];
+      double rn = (gx_hi - gx_lo) * g.inv_dx + (gy_hi - gy_lo) * g.inv_dy +
+                  (gz_hi - gz_lo) * g.inv_dz;
+      rn -= (RHS[c] - mean);
+      rn *= cc[c];
+      r = rn;
+    }
+    T *slot = reinterpret_cast<T *>(&a[(i >> 1) * npen + q]);
+    slot[i & 1] = (T)r;
+  }
+  __syncthreads();
+  T2 *z = smem_fft(a, b, npen, pl, -1);
+  // real-to-complex post-processing: X[k] = Fe[k] + W^k Fo[k]
+  const int nxh = g.nxh;
+  for (int idx = threadIdx.x; idx < npen * nxh; idx += blockDim.x) {
+    const int q = idx / nxh, kx = idx % nxh;
+    const long long row = row0 + q;
+    if (row >= nrows) continue;
+    T2 Z = z[(kx % M) * npen + q];
+    T2 Zc = z[((M - kx) % M) * npen + q];
+    Zc.y = -Zc.y;
+    T fer = (Z.x + Zc.x) * (T)0.5, fei = (Z.y + Zc.y) * (T)0.5;
+    T dr = Z.x - Zc.x, di = Z.y - Zc.y;
+    T for_ = di * (T)0.5, foi = -dr * (T)0.5;  // (Z - Zc) / (2i)
+    T2 w = r2c_tw[kx];
+    T xr = Cx<T2>::fma_(w.x, for_, Cx<T2>::fma_(-w.y, foi, fer));
+    T xi = Cx<T2>::fma_(w.x, foi, Cx<T2>::fma_(w.y, for_, fei));
+    spec[row * nxh + kx] = Cx<T2>::mk(xr, xi);
+  }
+}
+
+// ------------------------------------------------------- 2./4. y pencils
+template <typename T2>
+__global__ void k_fft_y(Grid g, FftPlan pl, T2 *__restrict__ spec, int npen, int sign) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2 *a = reinterpret_cast<T2 *>(smem_raw);
+  T2 *b = a + pl.n * npen;
+  const int tiles = (g.nxh + npen - 1) / npen;
+  const int kz = blockIdx.x / tiles, kx0 = (blockIdx.x % tiles) * npen;
+  const long long base = (long long)kz * g.ny * g.nxh;
+  for (int idx = threadIdx.x; idx < npen * g.ny; idx += blockDim.x) {
+    const int q = idx % npen, ky = idx / npen;
+    a[ky * npen + q] = (kx0 + q < g.nxh) ? spec[base + (long long)ky * g.nxh + kx0 + q]
+                                         : Cx<T2>::mk(0, 0);
+  }
+  __syncthreads();
+  T2 *r = smem_fft(a, b, npen, pl, sign);
+  for (int idx = threadIdx.x; idx < npen * g.ny; idx += blockDim.x) {
+    const int q = idx % npen, ky = idx / npen;
+    if (kx0 + q < g.nxh) spec[base + (long long)ky * g.nxh + kx0 + q] = r[ky * npen + q];
+  }
+}
+
+// ------------------------------------------- 3. z pencils + wave-number solve
+template <typename T2>
+__global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const double *__restrict__ ax,
+                              const double *__restrict__ ay, const double *__restrict__ az,
+                              int npen) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using T = typename Cx<T2>::T;
+  T2 *a = reinterpret_cast<T2 *>(smem_raw);
+  T2 *b = a + pl.n * npen;
+  const int tiles = (g.nxh + npen - 1) / npen;
+  const int ky = blockIdx.x / tiles, kx0 = (blockIdx.x % tiles) * npen;
+  const long long plane = (long long)g.ny * g.nxh;
+  const long long base = (long long)ky * g.nxh + kx0;
+  for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
+    const int q = idx % npen, kz = idx / npen;
+    a[kz * npen + q] = (kx0 + q < g.nxh) ? spec[base + kz * plane + q] : Cx<T2>::mk(0, 0);
+  }
+  __syncthreads();
+  T2 *r = smem_fft(a, b, npen, pl, -1);
+  T2 *other = (r == a) ? b : a;
+  // divide by the modified wave number except the zero mode (poisson.cpp:442-449)
+  for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
+    const int q = idx % npen, kz = idx / npen;
+    const int kx = kx0 + q;
+    if (kx < g.nxh && (kx + ky + kz) > 0) {
+      const double mwn = ax[kx] + ay[ky] + az[kz];
+      T2 v = r[kz * npen + q];
+      v.y = (T)((double)v.y / mwn);
+      v.x = (T)((double)v.x / mwn);
+      r[kz * npen + q] = v;
+    }
+  }
+  __syncthreads();
+  T2 *o = smem_fft(r, other, npen, pl, +1);
+  for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
+    const int q = idx % npen, kz = idx / npen;
+    if (kx0 + q < g.nxh) spec[base + kz * plane + q] = o[kz * npen + q];
+  }
+}
+
+// ------------------------------------------- 5. C2R along x + P update
+template <typename T2>
+__global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
+                              const T2 *__restrict__ spec, double *__restrict__ P,
+                              double *__restrict__ partials, int npen) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double sh[32];
+  using T = typename Cx<T2>::T;
+  T2 *a = reinterpret_cast<T2 *>(smem_raw);
+  const int M = pl.n;
+  T2 *b = a + M * npen;
+  const long long nrows = (long long)g.ny * g.nz;
+  const long long row0 = (long long)blockIdx.x * npen;
+  const int nxh = g.nxh;
+  // Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) W^-k, k < M
+  for (int idx = threadIdx.x; idx < npen * M; idx += blockDim.x) {
+    const int q = idx / M, kx = idx % M;
+    const long long row = row0 + q;
+    T2 Z = Cx<T2>::mk(0, 0);
+    if (row < nrows) {
+      T2 X = spec[row * nxh + kx];
+      T2 Y = spec[row * nxh + (M - kx)];
+      Y.y = -Y.y;
+      T fer = X.x + Y.x, fei = X.y + Y.y;
+      T dr = X.x - Y.x, di = X.y - Y.y;
+      T2 w = r2c_tw[kx];  // exp(-2 pi i k / nx); use its conjugate
+      T for_ = Cx<T2>::fma_(dr, w.x, di * w.y);
+      T foi = Cx<T2>::fma_(di, w.x, -dr * w.y);
+      Z = Cx<T2>::mk(fer - foi, fei + for_);  // Fe + i Fo
+    }
+    a[kx * npen + q] = Z;
+  }
+  __syncthreads();
+  T2 *z = smem_fft(a, b, npen, pl, +1);
+  const double tot = (double)(g.nx * g.ny * g.nz);
+  double mx = 0;
+  for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
+    const int q = idx / g.nx, i = idx % g.nx;
+    const long long row = row0 + q;
+    if (row >= nrows) continue;
+    const T *zz = reinterpret_cast<const T *>(&z[(i >> 1) * npen + q]);
+    double x = (double)zz[i & 1];
+    double dp = (-1) * x / (tot);
+    const long long c = row * g.nx + i;
+    P[c] += dp;
+    double ad = fabs(dp);
+    mx = ad > mx ? ad : mx;
+  }
+  double bm = block_max(mx, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = bm;
+}
+
+__global__ void k_finish_max(const double *__restrict__ partials, int nparts, DevScalars *s) {
+  __shared__ double sh[32];
+  double v = 0;
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x) v = partials[b] > v ? partials[b] : v;
+  double m = block_max(v, sh);
+  if (threadIdx.x == 0) s->err = m;
+}
+
+int pens_for(int n) {
+  int p = kFftSmemPoints / n;
+  if (p < 1) p = 1;
+  if (p > 32) p = 32;
+  return p;
+}
+
+void factorize(int n, FftPlan &pl) {
+  pl.n = n;
+  pl.nst = 0;
+  int m = n;
+  while (m % 4 == 0) { pl.radix[pl.nst++] = 4; m /= 4; }
+  while (m % 2 == 0) { pl.radix[pl.nst++] = 2; m /= 2; }
+  while (m % 3 == 0) { pl.radix[pl.nst++] = 3; m /= 3; }
+  while (m % 5 == 0) { pl.radix[pl.nst++] = 5; m /= 5; }
+  if (m != 1) throw std::string("grid size must factor into 2, 3 and 5");
+}
+
+}  // namespace
+
+// modified wave number tables, evaluated with the host libm exactly as
+// poisson.cpp:433-447 writes them:  a_x[i] = (2/dx^2)*(1-cos(kk_i*dx)) with
+// kk_i = ((i<nx/2)?i:i-nx)*2pi/Lx.
+static void mwn_table(int n, double L, double d, std::vector<double> &t, int count) {
+  double TWO_PI(2 * 3.141592653589793);
+  double two_pi_over_L = TWO_PI / L;
+  double d2 = 2. / (d * d);
+  t.resize(count);
+  for (int i = 0; i < count; ++i) {
+    double kk = ((i < n / 2) ? i : i - n) * two_pi_over_L;
+    t[i] = (d2) * (1 - cos(kk * d));
+  }
+}
+
+void fft_plans_create(tpm_ctx *c) {
+  const Grid &g = c->g;
+  if (g.nx % 2) throw std::string("Nx must be even (real-to-complex x pass)");
+  factorize(g.nx / 2, c->fx);
+  factorize(g.ny, c->fy);
+  factorize(g.nz, c->fz);
+  // twiddles: one block of [n] double2 + [n] float2 per plan, plus the r2c table
+  auto table = [](int n, std::vector<double2> &d, std::vector<float2> &f) {
+    d.resize(n);
+    f.resize(n);
+    for (int m = 0; m < n; ++m) {
+      double a = 2.0 * 3.14159265358979323846 * (double)m / (double)n;
+      d[m] = make_double2(cos(a), -sin(a));
+      f[m] = make_float2((float)d[m].x, (float)d[m].y);
+    }
+  };
+  std::vector<double2> dx_, dy_, dz_, dr;
+  std::vector<float2> fx_, fy_, fz_, fr;
+  table(c->fx.n, dx_, fx_);
+  table(c->fy.n, dy_, fy_);
+  table(c->fz.n, dz_, fz_);
+  table(g.nx, dr, fr);  // r2c post-processing uses W^k, k <= nx/2
+  std::vector<double> ax, ay, az;
+  mwn_table(g.nx, g.Lx, g.dx, ax, g.nxh);
+  mwn_table(g.ny, g.Ly, g.dy, ay, g.ny);
+  mwn_table(g.nz, g.Lz, g.dz, az, g.nz);
+  size_t n64 = dx_.size() + dy_.size() + dz_.size() + dr.size();
+  size_t bytes = n64 * (sizeof(double2) + sizeof(float2)) + (ax.size() + ay.size() + az.size()) * 8;
+  char *mem = nullptr;
+  TPM_CUDA_TRY(cudaMalloc(&mem, bytes + 256));
+  c->fft_mem = mem;
+  double2 *d64 = reinterpret_cast<double2 *>(mem);
+  float2 *d32 = reinterpret_cast<float2 *>(d64 + n64);
+  double *tabs = reinterpret_cast<double *>(d32 + n64);
+  size_t o = 0;
+  auto put = [&](std::vector<double2> &d, std::vector<float2> &f, FftPlan *pl) -> size_t {
+    TPM_CUDA_TRY(cudaMemcpy(d64 + o, d.data(), d.size() * sizeof(double2), cudaMemcpyHostToDevice));
+    TPM_CUDA_TRY(cudaMemcpy(d32 + o, f.data(), f.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    if (pl) {
+      pl->tw64 = d64 + o;
+      pl->tw32 = d32 + o;
+    }
+    size_t at0 = o;
+    o += d.size();
+    return at0;
+  };
+  put(dx_, fx_, &c->fx);
+  put(dy_, fy_, &c->fy);
+  put(dz_, fz_, &c->fz);
+  size_t r0 = put(dr, fr, nullptr);
+  c->r2c64 = d64 + r0;
+  c->r2c32 = d32 + r0;
+  c->ax = tabs;
+  c->ay = tabs + ax.size();
+  c->az = tabs + ax.size() + ay.size();
+  TPM_CUDA_TRY(cudaMemcpy(c->ax, ax.data(), ax.size() * 8, cudaMemcpyHostToDevice));
+  TPM_CUDA_TRY(cudaMemcpy(c->ay, ay.data(), ay.size() * 8, cudaMemcpyHostToDevice));
+  TPM_CUDA_TRY(cudaMemcpy(c->az, az.data(), az.size() * 8, cudaMemcpyHostToDevice));
+  // dynamic shared memory above 48 KB
+  int smem64 = 2 * kFftSmemPoints * (int)sizeof(double2);
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_xfwd_resid<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_fft_y<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_fft_z_solve<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_xinv_update<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+}
+
+// One Richardson iteration of poisson::FFT (poisson.cpp:397-409).  Inputs:
+// P, c->Cface, c->cc, c->RHS and dsc->mean_rhs.  Output: P updated and
+// dsc->err = max|dp|.
+void poisson_iteration(tpm_ctx *c) {
+  const Grid &g = c->g;
+  using T2 = double2;
+  const long long nrows = (long long)g.ny * g.nz;
+  // x pass forward
+  {
+    int npen = pens_for(c->fx.n);
+    if (npen * c->fx.n < g.nx / 2) npen = 1;
+    int blocks = (int)((nrows + npen - 1) / npen);
+    size_t smem = 2 * (size_t)npen * c->fx.n * sizeof(T2);
+    TPM_LAUNCH(c, "fft_x_fwd_resid", k_xfwd_resid<T2>, blocks, kFftThreads, smem, g, c->fx,
+               c->r2c64, c->P, c->Cface, c->cc, c->RHS, c->dsc, c->spec, npen);
+  }
+  {
+    int npen = pens_for(c->fy.n);
+    int blocks = g.nz * ((g.nxh + npen - 1) / npen);
+    size_t smem = 2 * (size_t)npen * c->fy.n * sizeof(T2);
+    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, kFftThreads, smem, g, c->fy, c->spec, npen, -1);
+  }
+  {
+    int npen = pens_for(c->fz.n);
+    int blocks = g.ny * ((g.nxh + npen - 1) / npen);
+    size_t smem = 2 * (size_t)npen * c->fz.n * sizeof(T2);
+    TPM_LAUNCH(c, "fft_z_solve", k_fft_z_solve<T2>, blocks, kFftThreads, smem, g, c->fz, c->spec,
+               c->ax, c->ay, c->az, npen);
+  }
+  {
+    int npen = pens_for(c->fy.n);
+    int blocks = g.nz * ((g.nxh + npen - 1) / npen);
+    size_t smem = 2 * (size_t)npen * c->fy.n * sizeof(T2);
+    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, kFftThreads, smem, g, c->fy, c->spec, npen, +1);
+  }
+  {
+    int npen = pens_for(c->fx.n);
+    int blocks = (int)((nrows + npen - 1) / npen);
+    size_t smem = 2 * (size_t)npen * c->fx.n * sizeof(T2);
+    double *parts = c->err_parts;
+    int nparts = blocks;
+    TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, blocks, kFftThreads, smem, g, c->fx,
+               c->r2c64, c->spec, c->P, parts, npen);
+    TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 256, 0, parts, nparts, c->dsc);
+  }
+}
+
+}  // namespace tpm
+
+namespace tpm {
+int fft_x_blocks(const tpm_ctx *c) {
+  const long long nrows = (long long)c->g.ny * c->g.nz;
+  int npen = pens_for(c->g.nx / 2);
+  return (int)((nrows + npen - 1) / npen);
+}
+}  // namespace tpm

@@ -1,0 +1,444 @@
+// Grid-side kernels of the FP64 RK4 substep.
+//
+// Each kernel fuses a run of the reference's whole-field sweeps
+// (tensor0/tensor1 operators, grid.cpp:608-863) into one pass over the box.
+// Halo exchange becomes periodic index wrap.  Every expression keeps the
+// reference's floating-point operation order and the library is compiled
+// with --fmad=false, so apart from reductions and the FFT the results are
+// the reference's to the last bit.
+#include "tpm_internal.cuh"
+#include "tpm_reduce.cuh"
+
+namespace tpm {
+namespace {
+
+constexpr int kThreads = 256;
+
+struct Cell {
+  int i, j, k;
+  long long c;
+};
+
+__device__ __forceinline__ Cell cell_of(const Grid &g, long long c) {
+  Cell r;
+  r.c = c;
+  r.i = (int)(c % g.nx);
+  long long t = c / g.nx;
+  r.j = (int)(t % g.ny);
+  r.k = (int)(t / g.ny);
+  return r;
+}
+
+__device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
+  return ((long long)k * g.ny + j) * g.nx + i;
+}
+
+// ---------------------------------------------------------------- P0 update
+// grid::Update_P0, grid.cpp:816-830, with mean(RHS_Part_Temp) finished from
+// the heat deposit's per-block partial sums.
+__global__ void k_p0_update(const double *__restrict__ partials, int nparts, DevScalars *s,
+                            long long ntot, int cooling, double R, double Cv, double Cp,
+                            double Vcell, double dtpo, double dtpr, int stage, int np1_is_base) {
+  __shared__ double sh[kThreads];
+  double v = 0;
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x) v += partials[b];
+  double sum = block_sum(v, sh);
+  if (threadIdx.x == 0) {
+    double mean_energy_transferred = sum / (double)ntot;
+    double dP0_dt = cooling ? 0.0 : -R / Cv * mean_energy_transferred / Vcell;
+    double np1 = np1_is_base ? s->P0 : s->P0_np1;
+    np1 += dtpo * dP0_dt;
+    s->P0_np1 = np1;
+    s->P0_new = (stage != 3) ? s->P0 + dtpr * dP0_dt : np1;
+    s->T_scale = s->P0_new / R;
+    s->coef_div = -R / (Cp * s->P0_new * Vcell);
+    s->mean_Q = mean_energy_transferred;
+  }
+}
+
+// ---------------------------------------------------------------- density
+// grid::Update_Rho, grid.cpp:608-614, plus the two centre fields the rest of
+// the substep needs: 1/Rho_new (grid.cpp:834) and T = (P0_new/R)/Rho_new
+// (grid.cpp:882).
+__global__ void k_rho_update(Grid g, const double *__restrict__ RUi, const double *__restrict__ Rho,
+                             const double *__restrict__ np1_in, double *__restrict__ Rho_np1,
+                             double *__restrict__ Rho_new, double *__restrict__ inv_rho,
+                             double *__restrict__ Tgas, const DevScalars *__restrict__ s,
+                             double a_np1, double b_new, int stage) {
+  const double *RUx = RUi, *RUy = RUi + g.n, *RUz = RUi + 2 * g.n;
+  const double T_scale = s->T_scale;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    double D = (RUx[at(g, wrap_p(q.i, g.nx), q.j, q.k)] - RUx[c]) * g.inv_dx +
+               (RUy[at(g, q.i, wrap_p(q.j, g.ny), q.k)] - RUy[c]) * g.inv_dy +
+               (RUz[at(g, q.i, q.j, wrap_p(q.k, g.nz))] - RUz[c]) * g.inv_dz;
+    double np1 = np1_in[c] + a_np1 * D;
+    double nw = (stage != 3) ? 1 * Rho[c] + b_new * D : np1;
+    Rho_np1[c] = np1;
+    Rho_new[c] = nw;
+    inv_rho[c] = 1. / nw;
+    Tgas[c] = T_scale / nw;
+  }
+}
+
+// ------------------------------------------------------------ face velocity
+// U = RU_int / Rho_face with Rho_face = I_C2F(Rho_int) (grid.cpp:868,843).
+__global__ void k_face_velocity(Grid g, const double *__restrict__ RUi,
+                                const double *__restrict__ Rho_int, double *__restrict__ U) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    double r = Rho_int[c];
+    U[c] = RUi[c] / ((r + Rho_int[at(g, wrap_m(q.i, g.nx), q.j, q.k)]) * 0.5);
+    U[g.n + c] = RUi[g.n + c] / ((r + Rho_int[at(g, q.i, wrap_m(q.j, g.ny), q.k)]) * 0.5);
+    U[2 * g.n + c] = RUi[2 * g.n + c] / ((r + Rho_int[at(g, q.i, q.j, wrap_m(q.k, g.nz))]) * 0.5);
+  }
+}
+
+// ------------------------------------------------------- momentum RHS + RK
+struct RhsArgs {
+  double a_fp;   // -mp/Vcell
+  double b_gd;   // Mu0/3.
+  double c_lap;  // Mu0
+  double A, Rho0, g[3];
+  double dtpo, dtpr;
+  int stage, has_g;
+};
+
+// offsets of the neighbour in direction e (0,1,2) at +1 / -1, wrapped
+struct Nbr {
+  long long p[3], m[3];
+};
+__device__ __forceinline__ Nbr nbr_of(const Grid &g, const Cell &q) {
+  Nbr r;
+  r.p[0] = at(g, wrap_p(q.i, g.nx), q.j, q.k);
+  r.m[0] = at(g, wrap_m(q.i, g.nx), q.j, q.k);
+  r.p[1] = at(g, q.i, wrap_p(q.j, g.ny), q.k);
+  r.m[1] = at(g, q.i, wrap_m(q.j, g.ny), q.k);
+  r.p[2] = at(g, q.i, q.j, wrap_p(q.k, g.nz));
+  r.m[2] = at(g, q.i, q.j, wrap_m(q.k, g.nz));
+  return r;
+}
+
+// tensor0::Equal_Div_F2C of U at centre (i,j,k) (tensor0.cpp:249-256)
+__device__ __forceinline__ double divU_at(const Grid &g, const double *U, int i, int j, int k) {
+  long long c = at(g, i, j, k);
+  const double *Ux = U, *Uy = U + g.n, *Uz = U + 2 * g.n;
+  return (Ux[at(g, wrap_p(i, g.nx), j, k)] - Ux[c]) * g.inv_dx +
+         (Uy[at(g, i, wrap_p(j, g.ny), k)] - Uy[c]) * g.inv_dy +
+         (Uz[at(g, i, j, wrap_p(k, g.nz))] - Uz[c]) * g.inv_dz;
+}
+
+__device__ __forceinline__ long long shift(const Grid &g, int i, int j, int k, int dir, int s) {
+  if (dir == 0) return at(g, s > 0 ? wrap_p(i, g.nx) : wrap_m(i, g.nx), j, k);
+  if (dir == 1) return at(g, i, s > 0 ? wrap_p(j, g.ny) : wrap_m(j, g.ny), k);
+  return at(g, i, j, s > 0 ? wrap_p(k, g.nz) : wrap_m(k, g.nz));
+}
+
+// flux P_{d,e}(cell) = I_e,C2F(U_d) * I_d,C2F(RU_e)   (grid.cpp:785-800)
+__device__ __forceinline__ double flux_at(const Grid &g, const double *Ud, const double *RUe, int i,
+                                          int j, int k, int d, int e) {
+  long long c = at(g, i, j, k);
+  double iu = (Ud[c] + Ud[shift(g, i, j, k, e, -1)]) * 0.5;
+  double ir = (RUe[c] + RUe[shift(g, i, j, k, d, -1)]) * 0.5;
+  return iu * ir;
+}
+
+__global__ void k_rhs_momentum(Grid g, const double *__restrict__ U, const double *__restrict__ RUi,
+                               const double *__restrict__ Fp, const double *__restrict__ Rho_int,
+                               const double *__restrict__ RU, const double *__restrict__ np1_in,
+                               double *__restrict__ RU_np1, double *__restrict__ RU_new, RhsArgs a) {
+  const double inv_d[3] = {g.inv_dx, g.inv_dy, g.inv_dz};
+  const double inv_d2[3] = {g.inv_dx2, g.inv_dy2, g.inv_dz2};
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    Nbr nb = nbr_of(g, q);
+    const double div_c = divU_at(g, U, q.i, q.j, q.k);
+    const double div_m[3] = {divU_at(g, U, wrap_m(q.i, g.nx), q.j, q.k),
+                             divU_at(g, U, q.i, wrap_m(q.j, g.ny), q.k),
+                             divU_at(g, U, q.i, q.j, wrap_m(q.k, g.nz))};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double *Ud = U + d * g.n;
+      // dummy2 = grad_C2F(div U) (tensor1.cpp:259-270)
+      double gd = (div_c - div_m[d]) * inv_d[d];
+      // dummy = Del2(U_d) (tensor0.cpp:258-265)
+      double ud = Ud[c];
+      double lap = (Ud[nb.p[0]] - 2 * ud + Ud[nb.m[0]]) * inv_d2[0] +
+                   (Ud[nb.p[1]] - 2 * ud + Ud[nb.m[1]]) * inv_d2[1] +
+                   (Ud[nb.p[2]] - 2 * ud + Ud[nb.m[2]]) * inv_d2[2];
+      // RHS = -mp/Vcell*F_p + mu/3 grad(div U) + mu Del2 U  (grid.cpp:783)
+      double rhs = a.a_fp * Fp[d * g.n + c] + a.b_gd * gd + a.c_lap * lap;
+      // convection: Div_F2C(I_C2F(U_d) * I_d,C2F(RU_int))  (grid.cpp:785-801)
+      double conv = 0;
+      {
+        double t[3];
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+          const double *RUe = RUi + e * g.n;
+          int ip = e == 0 ? wrap_p(q.i, g.nx) : q.i;
+          int jp = e == 1 ? wrap_p(q.j, g.ny) : q.j;
+          int kp = e == 2 ? wrap_p(q.k, g.nz) : q.k;
+          t[e] = (flux_at(g, Ud, RUe, ip, jp, kp, d, e) - flux_at(g, Ud, RUe, q.i, q.j, q.k, d, e)) *
+                 inv_d[e];
+        }
+        conv = t[0] + t[1] + t[2];
+      }
+      rhs -= conv;
+      // artificial (linear) forcing A*RU_int (grid.cpp:803)
+      rhs += a.A * RUi[d * g.n + c];
+      // body force (Rho_face - Rho0)*g (grid.cpp:805-809)
+      if (a.has_g) {
+        double rf = (Rho_int[c] + Rho_int[d == 0 ? nb.m[0] : d == 1 ? nb.m[1] : nb.m[2]]) * 0.5;
+        rhs += (rf - a.Rho0) * a.g[d];
+      }
+      // RU_np1 += dt*post*RHS ; RU_new = RU + dt*pre*RHS  (grid.cpp:811-813)
+      double np1 = np1_in[d * g.n + c] + a.dtpo * rhs;
+      RU_np1[d * g.n + c] = np1;
+      RU_new[d * g.n + c] = (a.stage != 3) ? 1 * RU[d * g.n + c] + a.dtpr * rhs : np1;
+    }
+  }
+}
+
+// ---------------------------------------------------- Poisson right side
+// grid::Compute_Div_U_new (grid.cpp:832-839), grid::Compute_RHS_Pois
+// (grid.cpp:841-849) and the coefficient set-up of grid::Solve_Poisson /
+// poisson::FFT (grid.cpp:853, poisson.cpp:393-394) in one pass.  The mean of
+// RHS_Pois is reduced per block; it is subtracted where RHS_Pois is read.
+struct PoisArgs {
+  double kCp;        // k/Cp
+  double inv_dtpre;  // 1./(dt*pre)
+  int cooling, store_div;
+};
+
+__global__ void k_poisson_rhs(Grid g, const double *__restrict__ Rho_new,
+                              const double *__restrict__ inv_rho, const double *__restrict__ Q,
+                              const double *__restrict__ RUn, const DevScalars *__restrict__ s,
+                              double *__restrict__ RHS, double *__restrict__ divg,
+                              double *__restrict__ Cface, double *__restrict__ cc,
+                              double *__restrict__ partials, PoisArgs a) {
+  __shared__ double sh[kThreads];
+  const double coef = s->coef_div, meanQ = s->mean_Q;
+  const double OneThird = 1. / 3.;
+  double acc = 0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    Nbr nb = nbr_of(g, q);
+    // divergence = (k/Cp) Del2(1/Rho_new) - R/(Cp P0_new Vcell) Q
+    double ir = inv_rho[c];
+    double lap = (inv_rho[nb.p[0]] - 2 * ir + inv_rho[nb.m[0]]) * g.inv_dx2 +
+                 (inv_rho[nb.p[1]] - 2 * ir + inv_rho[nb.m[1]]) * g.inv_dy2 +
+                 (inv_rho[nb.p[2]] - 2 * ir + inv_rho[nb.m[2]]) * g.inv_dz2;
+    double Qc = a.cooling ? Q[c] - meanQ : Q[c];
+    double dv = a.kCp * lap + coef * Qc;
+    if (a.store_div) divg[c] = dv;
+    // Rho_face = I_C2F(Rho_new) on the 6 faces of the cell
+    double r = Rho_new[c];
+    double rf_lo[3] = {(r + Rho_new[nb.m[0]]) * 0.5, (r + Rho_new[nb.m[1]]) * 0.5,
+                       (r + Rho_new[nb.m[2]]) * 0.5};
+    double rf_hi[3] = {(Rho_new[nb.p[0]] + r) * 0.5, (Rho_new[nb.p[1]] + r) * 0.5,
+                       (Rho_new[nb.p[2]] + r) * 0.5};
+    // U = RU_new / Rho_face ; RHS = (div_F2C(U) - divergence) / (dt*pre)
+    double t[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double *R = RUn + d * g.n;
+      double u_hi = R[nb.p[d]] / rf_hi[d];
+      double u_lo = R[c] / rf_lo[d];
+      t[d] = (u_hi - u_lo) * (d == 0 ? g.inv_dx : d == 1 ? g.inv_dy : g.inv_dz);
+    }
+    double rhs = t[0] + t[1] + t[2];
+    rhs -= dv;
+    rhs *= a.inv_dtpre;
+    RHS[c] = rhs;
+    acc += rhs;
+    // C = 1/Rho_face ; center_coeff = -1/I_F2C(C)
+    double c_lo[3], c_hi[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      c_lo[d] = 1. / rf_lo[d];
+      c_hi[d] = 1. / rf_hi[d];
+      Cface[d * g.n + c] = c_lo[d];
+    }
+    double m = OneThird * ((c_lo[0] + c_hi[0]) * 0.5 + (c_lo[1] + c_hi[1]) * 0.5 +
+                           (c_lo[2] + c_hi[2]) * 0.5);
+    cc[c] = -1. / m;
+  }
+  double bs = block_sum(acc, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = bs;
+}
+
+// mean of a field from per-block partial sums, stored at *out
+__global__ void k_finish_mean(const double *__restrict__ partials, int nparts, long long ntot,
+                              double *out) {
+  __shared__ double sh[kThreads];
+  double v = 0;
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x) v += partials[b];
+  double sum = block_sum(v, sh);
+  if (threadIdx.x == 0) *out = sum / (double)ntot;
+}
+
+// ---------------------------------------------------------- projection
+// grid::Update_RU_WP, grid.cpp:857-863.  At the last stage the per-component
+// sums of RU_np1 for make_mean_U0 (simulation.cpp:80) are reduced too.
+__global__ void k_project(Grid g, const double *__restrict__ P, double *__restrict__ RU_np1,
+                          double *__restrict__ RU_new, double a_np1, double b_new, int stage,
+                          double *__restrict__ partials) {
+  __shared__ double sh[kThreads];
+  double acc[3] = {0, 0, 0};
+  const double inv_d[3] = {g.inv_dx, g.inv_dy, g.inv_dz};
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    Nbr nb = nbr_of(g, q);
+    double pc = P[c];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      double G = (pc - P[nb.m[d]]) * inv_d[d];
+      double np1 = RU_np1[d * g.n + c] + a_np1 * G;
+      RU_np1[d * g.n + c] = np1;
+      RU_new[d * g.n + c] = (stage != 3) ? RU_new[d * g.n + c] + b_new * G : np1;
+      acc[d] += np1;
+    }
+  }
+  if (stage == 3) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      double bs = block_sum(acc[d], sh);
+      if (threadIdx.x == 0) partials[d * kRedBlocks + blockIdx.x] = bs;
+    }
+  }
+}
+
+__global__ void k_finish_means3(const double *__restrict__ partials, int nparts, long long ntot,
+                                DevScalars *s) {
+  __shared__ double sh[kThreads];
+  for (int d = 0; d < 3; ++d) {
+    double v = 0;
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x) v += partials[d * kRedBlocks + b];
+    double sum = block_sum(v, sh);
+    if (threadIdx.x == 0) s->mean_ru[d] = sum / (double)ntot;
+    __syncthreads();
+  }
+}
+
+// tensor0::make_mean_U0 per component (tensor0.cpp:389-394) and
+// grid::TimeAdvance RU = RU_np1 (grid.cpp:599): the result goes to RU.
+__global__ void k_mean_reset(Grid g, const double *__restrict__ RU_np1, double *__restrict__ RU,
+                             const DevScalars *__restrict__ s, double r0, double r1, double r2) {
+  const double m[3] = {s->mean_ru[0], s->mean_ru[1], s->mean_ru[2]};
+  const double a[3] = {r0, r1, r2};
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      double v = RU_np1[d * g.n + c];
+      v -= m[d];
+      v += a[d];
+      RU[d * g.n + c] = v;
+    }
+  }
+}
+
+// grid::Initialize (grid.cpp:474): nothing to store on the device beyond the
+// copies done by the host; kept for the operator-level Poisson entry point:
+// center_coeff = -1/I_F2C(C) for a caller-supplied C (poisson.cpp:393-394).
+__global__ void k_center_coeff(Grid g, const double *__restrict__ Cf, double *__restrict__ cc) {
+  const double OneThird = 1. / 3.;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    Nbr nb = nbr_of(g, q);
+    double m = OneThird * ((Cf[c] + Cf[nb.p[0]]) * 0.5 + (Cf[g.n + c] + Cf[g.n + nb.p[1]]) * 0.5 +
+                           (Cf[2 * g.n + c] + Cf[2 * g.n + nb.p[2]]) * 0.5);
+    cc[c] = -1. / m;
+  }
+}
+
+}  // namespace
+
+int cell_blocks(const Grid &g) {
+  long long b = (g.n + kThreads - 1) / kThreads;
+  return (int)(b < kRedBlocks ? b : kRedBlocks);
+}
+
+static const double kPre[4] = {0.5, 0.5, 1., 1. / 6.};          // grid.cpp:18-21
+static const double kPost[4] = {1. / 6., 1. / 3., 1. / 3., 1. / 6.};  // grid.cpp:22-25
+
+void launch_p0_update(tpm_ctx *c, int s) {
+  TPM_LAUNCH(c, "p0_update", k_p0_update, 1, kThreads, 0, c->partials + kPartQ * kRedBlocks, c->q_parts, c->dsc, c->g.n,
+             c->p.cooling, c->R, c->p.Cv, c->p.Cp, c->Vcell, c->p.dt * kPost[s],
+             c->p.dt * kPre[s], s, (int)c->np1_is_base);
+}
+
+void launch_rho_update(tpm_ctx *c, int s, bool np1_in_base) {
+  TPM_LAUNCH(c, "rho_update", k_rho_update, cell_blocks(c->g), kThreads, 0, c->g, c->RU_int,
+             c->Rho, np1_in_base ? c->Rho : c->Rho_np1, c->Rho_np1, c->Rho_new, c->inv_rho,
+             c->Tgas, c->dsc, -(c->p.dt * kPost[s]), -c->p.dt * kPre[s], s);
+}
+
+void launch_face_velocity(tpm_ctx *c) {
+  TPM_LAUNCH(c, "face_velocity", k_face_velocity, cell_blocks(c->g), kThreads, 0, c->g,
+             c->RU_int, c->Rho_int, c->U);
+}
+
+void launch_rhs_momentum(tpm_ctx *c, int s, bool np1_in_base) {
+  RhsArgs a;
+  a.a_fp = -c->mp / c->Vcell;
+  a.b_gd = c->p.Mu0 / 3.;
+  a.c_lap = c->p.Mu0;
+  a.A = c->A;
+  a.Rho0 = c->p.Rho0;
+  a.g[0] = c->gx;
+  a.g[1] = c->gy;
+  a.g[2] = c->gz;
+  a.has_g = (c->gx != 0 || c->gy != 0 || c->gz != 0);
+  a.dtpo = c->p.dt * kPost[s];
+  a.dtpr = c->p.dt * kPre[s];
+  a.stage = s;
+  TPM_LAUNCH(c, "rhs_momentum", k_rhs_momentum, cell_blocks(c->g), kThreads, 0, c->g, c->U,
+             c->RU_int, c->Fp, c->Rho_int, c->RU, np1_in_base ? c->RU : c->RU_np1, c->RU_np1,
+             c->RU_new, a);
+}
+
+void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
+  PoisArgs a;
+  a.kCp = c->p.k / c->p.Cp;
+  a.inv_dtpre = (1. / (c->p.dt * kPre[s]));
+  a.cooling = c->p.cooling;
+  a.store_div = store_div;
+  int nb = cell_blocks(c->g);
+  TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs, nb, kThreads, 0, c->g, c->Rho_new, c->inv_rho,
+             c->Q, c->RU_new, c->dsc, c->RHS, c->divg, c->Cface, c->cc,
+             c->partials + kPartRhs * kRedBlocks, a);
+  TPM_LAUNCH(c, "finish_mean", k_finish_mean, 1, kThreads, 0, c->partials + kPartRhs * kRedBlocks,
+             nb, c->g.n,
+             &c->dsc->mean_rhs);
+}
+
+void launch_project(tpm_ctx *c, int s) {
+  int nb = cell_blocks(c->g);
+  TPM_LAUNCH(c, "project", k_project, nb, kThreads, 0, c->g, c->P, c->RU_np1, c->RU_new,
+             -(c->p.dt * kPost[s]), -(c->p.dt * kPre[s]), s, c->partials + kPartRu * kRedBlocks);
+  if (s == 3)
+    TPM_LAUNCH(c, "finish_means3", k_finish_means3, 1, kThreads, 0,
+               c->partials + kPartRu * kRedBlocks, nb, c->g.n,
+               c->dsc);
+}
+
+void launch_mean_reset(tpm_ctx *c) {
+  TPM_LAUNCH(c, "mean_reset", k_mean_reset, cell_blocks(c->g), kThreads, 0, c->g, c->RU_np1,
+             c->RU, c->dsc, c->p.U0 * c->p.Rho0, c->p.V0 * c->p.Rho0, c->p.W0 * c->p.Rho0);
+}
+
+void launch_center_coeff_from_C(tpm_ctx *c) {
+  TPM_LAUNCH(c, "center_coeff", k_center_coeff, cell_blocks(c->g), kThreads, 0, c->g, c->Cface,
+             c->cc);
+}
+
+void launch_init_fields(tpm_ctx *) {}
+
+}  // namespace tpm

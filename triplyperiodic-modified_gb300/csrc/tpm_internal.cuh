@@ -1,0 +1,193 @@
+// Internal declarations shared by the CUDA translation units of libtpm.so.
+//
+// Data layout in HBM (one context = one periodic box):
+//  * scalar fields: unghosted FP64 [Nz][Ny][Nx], x fastest, index
+//    c = (k*Ny + j)*Nx + i; a neighbour index wraps periodically (this is
+//    what the reference's ghost layers + halo exchange do on one rank);
+//  * vector (face) fields: the x, y, z components as three such blocks back
+//    to back, exactly the reference's tensor1 file layout;
+//  * spectrum: half-complex [Nz][Ny][Nx/2+1] (R2C along x);
+//  * particles: SoA, one array per quantity and per RK copy
+//    (base, int, new, np1 as in particle.h:61-113).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "tpm.h"
+
+namespace tpm {
+
+constexpr double kPi = 3.141592653589793;  // params.h:5
+
+struct Grid {
+  int nx, ny, nz, nxh;  // nxh = nx/2 + 1 (half spectrum)
+  long long n;          // cells
+  double dx, dy, dz;
+  double inv_dx, inv_dy, inv_dz, inv_dx2, inv_dy2, inv_dz2;  // tensor0.cpp:17-22
+  double idx, idy, idz;                                      // particle.cpp:19-21
+  double Lx, Ly, Lz, xh, yh, zh;                             // gridsize.cpp:72-77
+};
+
+__host__ __device__ __forceinline__ int wrap_p(int i, int n) { return i + 1 == n ? 0 : i + 1; }
+__host__ __device__ __forceinline__ int wrap_m(int i, int n) { return i == 0 ? n - 1 : i - 1; }
+__host__ __device__ __forceinline__ int wrap_any(int i, int n) {
+  i %= n;
+  return i < 0 ? i + n : i;
+}
+
+// Scalars that live on the device so a whole substep runs without host
+// round trips (grid.h:100-105).
+struct DevScalars {
+  double P0, P0_int, P0_new, P0_np1;
+  double T_scale;    // P0_new / R   (grid.cpp:882)
+  double coef_div;   // -R/(Cp*P0_new*Vcell)  (grid.cpp:838)
+  double mean_Q;     // mean(RHS_Part_Temp) of the current substep
+  double mean_rhs;   // mean(RHS_Pois) (grid.cpp:848)
+  double err;        // max|dp| of the last Poisson iteration (poisson.cpp:407)
+  double mean_ru[3]; // RU_np1 component means (simulation.cpp:80)
+  double max_div;    // FP64 post-projection residual (mixed path)
+  int nonfinite;
+  int pad;
+};
+
+// 1-D FFT plan in device memory: radices and exp(-2 pi i m / n) twiddles.
+struct FftPlan {
+  int n;
+  int nst;
+  int radix[16];
+  const double2 *tw64;  // n entries
+  const float2 *tw32;   // n entries
+};
+
+// Deterministic reductions: each reducing kernel writes one partial per
+// block; a one-block kernel finishes them in a fixed order.
+constexpr int kRedBlocks = 1024;
+
+struct ProfEntry {
+  std::string name;
+  int launches = 0;
+  double total_ms = 0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+};
+
+}  // namespace tpm
+
+// The context (opaque to callers, see tpm.h).
+struct tpm_ctx {
+  tpm_params p;
+  tpm::Grid g;
+  int64_t np = 0;
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int64_t launches = 0;
+
+  // derived constants (params.cpp:70-77)
+  double R = 0, Tp = 0, mp = 0, Vcell = 0, P0ref = 0;
+  // parameters switched at T_cur > threshold (params.cpp:80-86)
+  double A = 0, gx = 0, gy = 0, gz = 0, I0 = 0;
+  int Iteration = 0;
+
+  double T_cur = 0;
+  int64_t num_timestep = 0;
+  bool initialized = false;
+  bool np1_is_base = true;  // np1 copies equal base (after initialize / end of step)
+  int last_it = 0, total_it = 0;
+  double last_err = 0;
+
+  // ---- fields (device) ----
+  double *RU = nullptr, *RU_int = nullptr, *RU_new = nullptr, *RU_np1 = nullptr;  // 3n each
+  double *Rho = nullptr, *Rho_int = nullptr, *Rho_new = nullptr, *Rho_np1 = nullptr;
+  double *P = nullptr, *C = nullptr, *Q = nullptr, *Fp = nullptr /*3n*/, *U = nullptr /*3n*/;
+  double *RHS = nullptr, *divg = nullptr, *inv_rho = nullptr, *Tgas = nullptr;
+  double *Cface = nullptr /*3n*/, *cc = nullptr;
+  double2 *spec = nullptr;
+  double *partials = nullptr;  // kRedBlocks * 4
+  tpm::DevScalars *dsc = nullptr;
+  tpm::DevScalars *hsc = nullptr;  // pinned mirror
+  double *ax = nullptr, *ay = nullptr, *az = nullptr;  // modified wave number tables
+  tpm::FftPlan fx, fy, fz;
+  const double2 *r2c64 = nullptr;
+  const float2 *r2c32 = nullptr;
+  double *err_parts = nullptr;  // one max|dp| per x-pass block
+  int x_blocks = 0;
+  void *fft_mem = nullptr;
+
+  // ---- particles (device) ----
+  double *pq[4][7] = {};  // [set][quantity] set: base,int,new,np1; q: x,y,z,u,v,w,T
+  double *rhs_t = nullptr, *tau = nullptr, *tau_buf = nullptr;
+  int32_t *flag = nullptr;
+  int32_t *key_t = nullptr, *key_r = nullptr;
+  int32_t *perm_t = nullptr, *perm_r[2] = {nullptr, nullptr};
+  int32_t *starts_t = nullptr, *starts_r[2] = {nullptr, nullptr};
+  int32_t *counts = nullptr;
+  int32_t *scan_blocks = nullptr;
+  double *pay_t = nullptr, *pay_t_s = nullptr;          // 6*np
+  double *pay_r = nullptr, *pay_r_s[2] = {nullptr, nullptr};  // 4*np
+  int rcur = 0;  // which r-sorted buffer holds the latest x_new sort
+  int q_parts = 1;  // number of valid partial sums of Q (heat deposit blocks)
+
+  bool store_div = false;
+
+  // ---- profiling ----
+  bool prof_on = false;
+  std::vector<tpm::ProfEntry> prof;
+  std::vector<void *> allocs;
+};
+
+namespace tpm {
+
+// launch bookkeeping (tpm_ctx.cu)
+void prof_begin(tpm_ctx *c, const char *name, cudaEvent_t *ev0);
+void prof_end(tpm_ctx *c, const char *name, cudaEvent_t ev0);
+
+// ---- field kernels (tpm_fields.cu) ----
+void launch_p0_update(tpm_ctx *c, int stage);
+void launch_rho_update(tpm_ctx *c, int stage, bool np1_in_base);
+void launch_face_velocity(tpm_ctx *c);
+void launch_rhs_momentum(tpm_ctx *c, int stage, bool np1_in_base);
+void launch_poisson_rhs(tpm_ctx *c, int stage, bool store_div);
+void launch_project(tpm_ctx *c, int stage);
+void launch_mean_reset(tpm_ctx *c);
+void launch_init_fields(tpm_ctx *c);
+int cell_blocks(const Grid &g);
+void launch_center_coeff_from_C(tpm_ctx *c);  // operator-level Poisson entry
+
+// ---- Poisson / FFT (tpm_fft.cu) ----
+void fft_plans_create(tpm_ctx *c);
+int fft_x_blocks(const tpm_ctx *c);
+// one Richardson iteration; returns nothing (error lands in dsc->err)
+void poisson_iteration(tpm_ctx *c);
+
+// ---- particles (tpm_particles.cu) ----
+void launch_particle_push(tpm_ctx *c, int stage, bool np1_in_base);
+void particle_deposit_momentum(tpm_ctx *c);
+void particle_deposit_concentration(tpm_ctx *c);
+void particle_heat(tpm_ctx *c);
+void particle_init_heat(tpm_ctx *c);
+void particle_zero_fields(tpm_ctx *c);
+
+}  // namespace tpm
+
+#define TPM_CUDA_TRY(expr)                                                   \
+  do {                                                                       \
+    cudaError_t e_ = (expr);                                                 \
+    if (e_ != cudaSuccess) {                                                 \
+      throw std::string(#expr) + ": " + cudaGetErrorString(e_);              \
+    }                                                                        \
+  } while (0)
+
+// Launch with bookkeeping: counts launches, optionally times them.
+#define TPM_LAUNCH(ctx, name, kernel, grid, block, smem, ...)                \
+  do {                                                                       \
+    cudaEvent_t ev0_ = nullptr;                                              \
+    if ((ctx)->prof_on) tpm::prof_begin((ctx), (name), &ev0_);               \
+    kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);         \
+    (ctx)->launches++;                                                       \
+    TPM_CUDA_TRY(cudaGetLastError());                                        \
+    if ((ctx)->prof_on) tpm::prof_end((ctx), (name), ev0_);                  \
+  } while (0)

@@ -1,0 +1,518 @@
+// Lagrangian particle stage of the RK4 substep (grid::Update_Particle,
+// grid.cpp:865-888) on the GPU.
+//
+//  * k_push: one thread per particle does the whole per-particle chain of the
+//    reference - face-linear gas velocity at x_int (particle.cpp:340-360),
+//    position / velocity / temperature RK updates (:314-338, :362-399,
+//    :477-492), the periodic wrap that replaces migration (:58-104,
+//    :150-250), the trilinear gas temperature at x_new and the heat
+//    exchange rate (:430-474) - and emits each particle's deposit payload
+//    and its cell key.
+//  * deposits (part2gas_velocity :494-520, part2gas_concentration :522-555,
+//    part2gas_Temp_new :620-654) are deterministic: particles are counting-
+//    sorted by cell (ties ordered by particle index), then every target cell
+//    gathers the contributions of the particles in its neighbouring cells in
+//    a fixed order.  No floating-point atomics, so the sources are bit-
+//    reproducible run to run; they differ from the reference's particle-order
+//    sums only by FP64 reassociation.
+#include "tpm_internal.cuh"
+#include "tpm_reduce.cuh"
+
+namespace tpm {
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
+  return ((long long)k * g.ny + j) * g.nx + i;
+}
+
+struct PushArgs {
+  double dtpo, dtpr;       // dt*post, dt*pre
+  double iTp;              // 1/Tp (particle.cpp:365)
+  double gp[3];            // ParticleGravity*g (particle.cpp:376-378)
+  double alpha;            // particle.cpp:481
+  double iS;               // 1/(mp*Cvp), particle.cpp:483
+  double iTth;             // Nu*pi*Dp*k, particle.cpp:470
+  int stage, twc, has_tau;
+};
+
+struct PState {
+  const double *b[7];  // base (x is written back when wrapped)
+  double *bx[3];
+  const double *in[7];  // int
+  const double *np1_in[7];
+  double *np1[7];
+  double *nw[7];
+};
+
+__global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const double *__restrict__ U,
+                       const double *__restrict__ Tgas, double *__restrict__ rhs_t,
+                       const double *__restrict__ tau, int32_t *__restrict__ key_t,
+                       double *__restrict__ pay_t, int32_t *__restrict__ key_r,
+                       double *__restrict__ pay_r) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const double xi = ps.in[0][p], yi = ps.in[1][p], zi = ps.in[2][p];
+    const double ui = ps.in[3][p], vi = ps.in[4][p], wi = ps.in[5][p];
+    // ---- gas2part_velocity at x_int (particle.cpp:340-360) ----
+    const int tx = (int)(xi * g.idx), ty = (int)(yi * g.idy), tz = (int)(zi * g.idz);
+    const double xl = (xi * g.idx - ((int)(xi * g.idx)));
+    const double yl = (yi * g.idy - ((int)(yi * g.idy)));
+    const double zl = (zi * g.idz - ((int)(zi * g.idz)));
+    const int i0 = wrap_any(tx, g.nx), j0 = wrap_any(ty, g.ny), k0 = wrap_any(tz, g.nz);
+    const long long c0 = at(g, i0, j0, k0);
+    const double ug = xl * U[at(g, wrap_p(i0, g.nx), j0, k0)] + (1 - xl) * U[c0];
+    const double vg = yl * U[g.n + at(g, i0, wrap_p(j0, g.ny), k0)] + (1 - yl) * U[g.n + c0];
+    const double wg = zl * U[2 * g.n + at(g, i0, j0, wrap_p(k0, g.nz))] + (1 - zl) * U[2 * g.n + c0];
+    // ---- update_position (particle.cpp:314-338) ----
+    double xn[3], xp[3], xb[3];
+    const double uint_[3] = {ui, vi, wi};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      xb[d] = ps.b[d][p];
+      xp[d] = ps.np1_in[d][p] + a.dtpo * uint_[d];
+      xn[d] = (a.stage != 3) ? xb[d] + a.dtpr * uint_[d] : xp[d];
+    }
+    // ---- update_velocity (particle.cpp:362-399) ----
+    const double iTp = a.has_tau ? 1. / tau[p] : a.iTp;
+    const double rhs[3] = {(ug - ui) * iTp, (vg - vi) * iTp, (wg - wi) * iTp};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      double np1 = ps.np1_in[3 + d][p] + a.dtpo * (rhs[d] + a.gp[d]);
+      ps.np1[3 + d][p] = np1;
+      ps.nw[3 + d][p] = (a.stage != 3) ? ps.b[3 + d][p] + a.dtpr * (rhs[d] + a.gp[d]) : np1;
+    }
+    // ---- update_Temp with the previous heat rate (particle.cpp:477-492) ----
+    const double rt_old = rhs_t[p];
+    const double Tnp1 = ps.np1_in[6][p] + a.dtpo * a.iS * (rt_old + a.alpha);
+    const double Tnew = (a.stage != 3) ? ps.b[6][p] + a.dtpr * a.iS * (rt_old + a.alpha) : Tnp1;
+    ps.np1[6][p] = Tnp1;
+    ps.nw[6][p] = Tnew;
+    // ---- part2gas_velocity payload at x_int (particle.cpp:494-520) ----
+    if (a.twc) {
+      key_t[p] = (int32_t)c0;
+      pay_t[0 * np + p] = (1 - xl) * rhs[0];
+      pay_t[1 * np + p] = xl * rhs[0];
+      pay_t[2 * np + p] = (1 - yl) * rhs[1];
+      pay_t[3 * np + p] = yl * rhs[1];
+      pay_t[4 * np + p] = (1 - zl) * rhs[2];
+      pay_t[5 * np + p] = zl * rhs[2];
+    }
+    // ---- Send_Recv on one rank = periodic wrap (particle.cpp:58-104, 150-250) ----
+    const double L[3] = {g.Lx, g.Ly, g.Lz};
+    const double hi[3] = {g.xh, g.yh, g.zh};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (xn[d] > hi[d] || xn[d] < 0) {
+        if (xn[d] > L[d]) {
+          xn[d] -= L[d];
+          xb[d] -= L[d];
+          xp[d] -= L[d];
+          ps.bx[d][p] = xb[d];
+        } else if (xn[d] < 0) {
+          xn[d] += L[d];
+          xb[d] += L[d];
+          xp[d] += L[d];
+          ps.bx[d][p] = xb[d];
+        }
+      }
+      ps.np1[d][p] = xp[d];
+      ps.nw[d][p] = xn[d];
+    }
+    // ---- gas2part_Temp_new + Compute_RHS_Temp_new at x_new (particle.cpp:430-474) ----
+    const int ri = (int)(round(xn[0] * g.idx)), rj = (int)(round(xn[1] * g.idy)),
+              rk = (int)(round(xn[2] * g.idz));
+    const double x_l = xn[0] * g.idx - ri + 0.5;
+    const double y_l = xn[1] * g.idy - rj + 0.5;
+    const double z_l = xn[2] * g.idz - rk + 0.5;
+    const int i1 = wrap_any(ri, g.nx), im = wrap_any(ri - 1, g.nx);
+    const int j1 = wrap_any(rj, g.ny), jm = wrap_any(rj - 1, g.ny);
+    const int k1 = wrap_any(rk, g.nz), km = wrap_any(rk - 1, g.nz);
+    const double Tg = x_l * y_l * z_l * Tgas[at(g, i1, j1, k1)] +
+                      (1 - x_l) * y_l * z_l * Tgas[at(g, im, j1, k1)] +
+                      x_l * (1 - y_l) * z_l * Tgas[at(g, i1, jm, k1)] +
+                      x_l * y_l * (1 - z_l) * Tgas[at(g, i1, j1, km)] +
+                      (1 - x_l) * (1 - y_l) * z_l * Tgas[at(g, im, jm, k1)] +
+                      (1 - x_l) * y_l * (1 - z_l) * Tgas[at(g, im, j1, km)] +
+                      x_l * (y_l - 1) * (z_l - 1) * Tgas[at(g, i1, jm, km)] +
+                      (1 - x_l) * (1 - y_l) * (1 - z_l) * Tgas[at(g, im, jm, km)];
+    const double rt = (Tg - Tnew) * a.iTth;
+    rhs_t[p] = rt;
+    key_r[p] = (int32_t)at(g, i1, j1, k1);
+    pay_r[0 * np + p] = x_l;
+    pay_r[1 * np + p] = y_l;
+    pay_r[2 * np + p] = z_l;
+    pay_r[3 * np + p] = rt;
+  }
+}
+
+// round-indexed key and payload of the given particle set (used at
+// initialisation, at x_int: grid.cpp:481-484)
+__global__ void k_cic_payload(Grid g, const double *__restrict__ x, const double *__restrict__ y,
+                              const double *__restrict__ z, const double *__restrict__ Tp,
+                              const double *__restrict__ Tgas, double iTth, int64_t np,
+                              double *__restrict__ rhs_t, int32_t *__restrict__ key_r,
+                              double *__restrict__ pay_r) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const double xx = x[p], yy = y[p], zz = z[p];
+    const int ri = (int)(round(xx * g.idx)), rj = (int)(round(yy * g.idy)),
+              rk = (int)(round(zz * g.idz));
+    const double x_l = xx * g.idx - ri + 0.5;
+    const double y_l = yy * g.idy - rj + 0.5;
+    const double z_l = zz * g.idz - rk + 0.5;
+    const int i1 = wrap_any(ri, g.nx), im = wrap_any(ri - 1, g.nx);
+    const int j1 = wrap_any(rj, g.ny), jm = wrap_any(rj - 1, g.ny);
+    const int k1 = wrap_any(rk, g.nz), km = wrap_any(rk - 1, g.nz);
+    // gas2part_Temp_int + Compute_RHS_Temp_int (particle.cpp:402-466)
+    const double Tg = x_l * y_l * z_l * Tgas[at(g, i1, j1, k1)] +
+                      (1 - x_l) * y_l * z_l * Tgas[at(g, im, j1, k1)] +
+                      x_l * (1 - y_l) * z_l * Tgas[at(g, i1, jm, k1)] +
+                      x_l * y_l * (1 - z_l) * Tgas[at(g, i1, j1, km)] +
+                      (1 - x_l) * (1 - y_l) * z_l * Tgas[at(g, im, jm, k1)] +
+                      (1 - x_l) * y_l * (1 - z_l) * Tgas[at(g, im, j1, km)] +
+                      x_l * (y_l - 1) * (z_l - 1) * Tgas[at(g, i1, jm, km)] +
+                      (1 - x_l) * (1 - y_l) * (1 - z_l) * Tgas[at(g, im, jm, km)];
+    const double rt = (Tg - Tp[p]) * iTth;
+    rhs_t[p] = rt;
+    key_r[p] = (int32_t)at(g, i1, j1, k1);
+    pay_r[0 * np + p] = x_l;
+    pay_r[1 * np + p] = y_l;
+    pay_r[2 * np + p] = z_l;
+    pay_r[3 * np + p] = rt;
+  }
+}
+
+__global__ void k_fill_tgas(long long n, const double *__restrict__ Rho, double T_scale,
+                            double *__restrict__ Tgas) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x)
+    Tgas[c] = T_scale / Rho[c];
+}
+
+// ------------------------------------------------------------ counting sort
+__global__ void k_hist(const int32_t *__restrict__ key, int64_t np, int32_t *__restrict__ counts) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+       p += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&counts[key[p]], 1);
+}
+
+constexpr int kScanThreads = 512;
+constexpr int kScanPer = 8;
+constexpr int kScanChunk = kScanThreads * kScanPer;
+
+// exclusive scan, phase 1: per-chunk totals
+__global__ void k_scan_reduce(const int32_t *__restrict__ counts, long long n,
+                              int32_t *__restrict__ chunk_sums) {
+  __shared__ int32_t sh[32];
+  long long base = (long long)blockIdx.x * kScanChunk + threadIdx.x * kScanPer;
+  int32_t s = 0;
+#pragma unroll
+  for (int e = 0; e < kScanPer; ++e)
+    if (base + e < n) s += counts[base + e];
+  int32_t t = block_sum(s, sh);
+  if (threadIdx.x == 0) chunk_sums[blockIdx.x] = t;
+}
+
+// phase 2: one block turns chunk totals into chunk offsets (exclusive)
+__global__ void k_scan_chunks(int32_t *__restrict__ chunk_sums, int nchunks) {
+  __shared__ int32_t carry;
+  __shared__ int32_t sh[kScanThreads];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int b0 = 0; b0 < nchunks; b0 += kScanThreads) {
+    int i = b0 + threadIdx.x;
+    int32_t v = i < nchunks ? chunk_sums[i] : 0;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < kScanThreads; o <<= 1) {  // Hillis-Steele inclusive
+      int32_t w = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
+      __syncthreads();
+      sh[threadIdx.x] += w;
+      __syncthreads();
+    }
+    int32_t incl = sh[threadIdx.x];
+    if (i < nchunks) chunk_sums[i] = carry + incl - v;
+    __syncthreads();
+    if (threadIdx.x == kScanThreads - 1) carry += incl;
+    __syncthreads();
+  }
+}
+
+// phase 3: starts[c] = offset + exclusive scan within the chunk; counts
+// are cleared so the scatter can reuse them as cursors
+__global__ void k_scan_apply(int32_t *__restrict__ counts, long long n,
+                             const int32_t *__restrict__ chunk_off, int32_t *__restrict__ starts,
+                             int32_t total) {
+  __shared__ int32_t sh[kScanThreads];
+  long long base = (long long)blockIdx.x * kScanChunk + threadIdx.x * kScanPer;
+  int32_t v[kScanPer];
+  int32_t s = 0;
+#pragma unroll
+  for (int e = 0; e < kScanPer; ++e) {
+    v[e] = (base + e < n) ? counts[base + e] : 0;
+    s += v[e];
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 1; o < kScanThreads; o <<= 1) {
+    int32_t w = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
+    __syncthreads();
+    sh[threadIdx.x] += w;
+    __syncthreads();
+  }
+  int32_t run = chunk_off[blockIdx.x] + sh[threadIdx.x] - s;
+#pragma unroll
+  for (int e = 0; e < kScanPer; ++e) {
+    if (base + e < n) {
+      starts[base + e] = run;
+      counts[base + e] = 0;
+    }
+    run += v[e];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) starts[n] = total;
+}
+
+__global__ void k_scatter(const int32_t *__restrict__ key, int64_t np,
+                          const int32_t *__restrict__ starts, int32_t *__restrict__ cursor,
+                          int32_t *__restrict__ perm) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    int32_t k = key[p];
+    int32_t slot = starts[k] + atomicAdd(&cursor[k], 1);
+    perm[slot] = (int32_t)p;
+  }
+}
+
+// order each cell's particles by index: the deposit sums become independent
+// of the scatter's atomic order
+__global__ void k_segsort(long long n, const int32_t *__restrict__ starts,
+                          int32_t *__restrict__ perm) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x) {
+    int32_t s = starts[c], e = starts[c + 1];
+    for (int32_t a = s + 1; a < e; ++a) {
+      int32_t v = perm[a];
+      int32_t b = a - 1;
+      while (b >= s && perm[b] > v) {
+        perm[b + 1] = perm[b];
+        --b;
+      }
+      perm[b + 1] = v;
+    }
+  }
+}
+
+__global__ void k_gather_payload(int64_t np, int nf, const int32_t *__restrict__ perm,
+                                 const double *__restrict__ pay, double *__restrict__ sorted) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < np;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    int32_t p = perm[s];
+    for (int f = 0; f < nf; ++f) sorted[f * np + s] = pay[f * np + p];
+  }
+}
+
+// ------------------------------------------------------------------ deposits
+// part2gas_velocity (particle.cpp:494-520) + cumulative ghost fold: face d of
+// cell c collects the upper weight of the particles in cell c - e_d and the
+// lower weight of those in cell c.
+__global__ void k_dep_momentum(Grid g, const int32_t *__restrict__ starts,
+                               const double *__restrict__ pay, int64_t np, double *__restrict__ Fp) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % g.nx);
+    const long long t = c / g.nx;
+    const int j = (int)(t % g.ny), k = (int)(t / g.ny);
+    const long long m[3] = {at(g, wrap_m(i, g.nx), j, k), at(g, i, wrap_m(j, g.ny), k),
+                            at(g, i, j, wrap_m(k, g.nz))};
+    const int32_t s0 = starts[c], e0 = starts[c + 1];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      double acc = 0;
+      const int32_t s1 = starts[m[d]], e1 = starts[m[d] + 1];
+      for (int32_t s = s1; s < e1; ++s) acc += pay[(2 * d + 1) * np + s];
+      for (int32_t s = s0; s < e0; ++s) acc += pay[(2 * d) * np + s];
+      Fp[d * g.n + c] = acc;
+    }
+  }
+}
+
+// part2gas_concentration (particle.cpp:522-555) and part2gas_Temp_*
+// (:582-654): centre c collects from the particles whose round-indexed cell
+// is c + (dx,dy,dz), dx,dy,dz in {0,1}, with weight (fx*fy)*fz, fx = xl if
+// dx == 0 else (1-xl).  with_rhs multiplies by the particle heat rate and
+// reduces the block sums of the result (mean for grid::Update_P0).
+__global__ void k_dep_cic(Grid g, const int32_t *__restrict__ starts, const double *__restrict__ pay,
+                          int64_t np, int with_rhs, double *__restrict__ out,
+                          double *__restrict__ partials) {
+  __shared__ double sh[32];
+  double bsum = 0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % g.nx);
+    const long long t = c / g.nx;
+    const int j = (int)(t % g.ny), k = (int)(t / g.ny);
+    double acc = 0;
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+      for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+        for (int dx = 0; dx < 2; ++dx) {
+          const long long r = at(g, dx ? wrap_p(i, g.nx) : i, dy ? wrap_p(j, g.ny) : j,
+                                 dz ? wrap_p(k, g.nz) : k);
+          const int32_t s0 = starts[r], e0 = starts[r + 1];
+          for (int32_t s = s0; s < e0; ++s) {
+            const double xl = pay[s], yl = pay[np + s], zl = pay[2 * np + s];
+            const double fx = dx ? (1 - xl) : xl;
+            const double fy = dy ? (1 - yl) : yl;
+            const double fz = dz ? (1 - zl) : zl;
+            double w = fx * fy * fz;
+            if (with_rhs) w = w * pay[3 * np + s];
+            acc += w;
+          }
+        }
+    out[c] = acc;
+    bsum += acc;
+  }
+  if (with_rhs) {
+    double b = block_sum(bsum, sh);
+    if (threadIdx.x == 0) partials[blockIdx.x] = b;
+  }
+}
+
+int pblocks(int64_t np) {
+  int64_t b = (np + kThreads - 1) / kThreads;
+  if (b > 152 * 32) b = 152 * 32;
+  return (int)(b < 1 ? 1 : b);
+}
+
+// sort `key` into perm / starts (deterministic cell-major, index-minor order)
+void sort_by_cell(tpm_ctx *c, const int32_t *key, int32_t *perm, int32_t *starts) {
+  const long long n = c->g.n;
+  TPM_CUDA_TRY(cudaMemsetAsync(c->counts, 0, sizeof(int32_t) * n, c->stream));
+  TPM_LAUNCH(c, "sort_hist", k_hist, pblocks(c->np), kThreads, 0, key, c->np, c->counts);
+  const int nchunks = (int)((n + kScanChunk - 1) / kScanChunk);
+  TPM_LAUNCH(c, "sort_scan_reduce", k_scan_reduce, nchunks, kScanThreads, 0, c->counts, n,
+             c->scan_blocks);
+  TPM_LAUNCH(c, "sort_scan_chunks", k_scan_chunks, 1, kScanThreads, 0, c->scan_blocks, nchunks);
+  TPM_LAUNCH(c, "sort_scan_apply", k_scan_apply, nchunks, kScanThreads, 0, c->counts, n,
+             c->scan_blocks, starts, (int32_t)c->np);
+  TPM_LAUNCH(c, "sort_scatter", k_scatter, pblocks(c->np), kThreads, 0, key, c->np, starts,
+             c->counts, perm);
+  TPM_LAUNCH(c, "sort_segsort", k_segsort, cell_blocks(c->g), kThreads, 0, n, starts, perm);
+}
+
+PState pstate(tpm_ctx *c, bool np1_in_base) {
+  PState s;
+  for (int q = 0; q < 7; ++q) {
+    s.b[q] = c->pq[0][q];
+    s.in[q] = c->pq[1][q];
+    s.np1_in[q] = np1_in_base ? c->pq[0][q] : c->pq[3][q];
+    s.np1[q] = c->pq[3][q];
+    s.nw[q] = c->pq[2][q];
+  }
+  for (int d = 0; d < 3; ++d) s.bx[d] = c->pq[0][d];
+  return s;
+}
+
+}  // namespace
+
+static const double kPre[4] = {0.5, 0.5, 1., 1. / 6.};
+static const double kPost[4] = {1. / 6., 1. / 3., 1. / 3., 1. / 6.};
+
+void launch_particle_push(tpm_ctx *c, int s, bool np1_in_base) {
+  if (c->np == 0) return;
+  PushArgs a;
+  a.dtpo = c->p.dt * kPost[s];
+  a.dtpr = c->p.dt * kPre[s];
+  a.iTp = (c->Tp != 0) ? 1. / c->Tp : 0.0;
+  const double pg = (double)(c->p.ParticleGravity != 0);
+  a.gp[0] = pg * c->gx;
+  a.gp[1] = pg * c->gy;
+  a.gp[2] = pg * c->gz;
+  a.alpha = 0.25 * c->p.epsilonp * kPi * c->p.Dp * c->p.Dp * c->I0;
+  a.iS = 1. / (c->mp * c->p.Cvp);
+  a.iTth = c->p.Nu * kPi * c->p.Dp * c->p.k;
+  a.stage = s;
+  a.twc = c->p.TWC;
+  a.has_tau = c->tau != nullptr;
+  TPM_LAUNCH(c, "particle_push", k_push, pblocks(c->np), kThreads, 0, c->g,
+             pstate(c, np1_in_base), a, c->np, c->U, c->Tgas, c->rhs_t, c->tau, c->key_t,
+             c->pay_t, c->key_r, c->pay_r);
+}
+
+// two-way momentum source at x_int (grid.cpp:877)
+void particle_deposit_momentum(tpm_ctx *c) {
+  if (c->np == 0 || !c->p.TWC) {
+    TPM_CUDA_TRY(cudaMemsetAsync(c->Fp, 0, sizeof(double) * 3 * c->g.n, c->stream));
+    return;
+  }
+  sort_by_cell(c, c->key_t, c->perm_t, c->starts_t);
+  TPM_LAUNCH(c, "payload_gather_t", k_gather_payload, pblocks(c->np), kThreads, 0, c->np, 6,
+             c->perm_t, c->pay_t, c->pay_t_s);
+  TPM_LAUNCH(c, "deposit_momentum", k_dep_momentum, cell_blocks(c->g), kThreads, 0, c->g,
+             c->starts_t, c->pay_t_s, c->np, c->Fp);
+}
+
+// concentration at x_int (grid.cpp:876) from the round-indexed sort of the
+// previous x_new (= this x_int)
+void particle_deposit_concentration(tpm_ctx *c) {
+  if (c->np == 0) {
+    TPM_CUDA_TRY(cudaMemsetAsync(c->C, 0, sizeof(double) * c->g.n, c->stream));
+    return;
+  }
+  TPM_LAUNCH(c, "deposit_conc", k_dep_cic, cell_blocks(c->g), kThreads, 0, c->g,
+             c->starts_r[c->rcur], c->pay_r_s[c->rcur], c->np, 0, c->C, (double *)nullptr);
+}
+
+static void heat_deposit_from(tpm_ctx *c, int buf) {
+  int nb = cell_blocks(c->g);
+  sort_by_cell(c, c->key_r, c->perm_r[buf], c->starts_r[buf]);
+  TPM_LAUNCH(c, "payload_gather_r", k_gather_payload, pblocks(c->np), kThreads, 0, c->np, 4,
+             c->perm_r[buf], c->pay_r, c->pay_r_s[buf]);
+  TPM_LAUNCH(c, "deposit_heat", k_dep_cic, nb, kThreads, 0, c->g, c->starts_r[buf],
+             c->pay_r_s[buf], c->np, 1, c->Q, c->partials + kPartQ * kRedBlocks);
+  c->q_parts = nb;
+}
+
+// part2gas_Temp_new at x_new (grid.cpp:886)
+void particle_heat(tpm_ctx *c) {
+  if (c->np == 0) {
+    TPM_CUDA_TRY(cudaMemsetAsync(c->Q, 0, sizeof(double) * c->g.n, c->stream));
+    TPM_CUDA_TRY(cudaMemsetAsync(c->partials + kPartQ * kRedBlocks, 0, sizeof(double) * kRedBlocks,
+                                 c->stream));
+    return;
+  }
+  int buf = 1 - c->rcur;
+  heat_deposit_from(c, buf);
+  c->rcur = buf;
+}
+
+// grid::Initialize tail (grid.cpp:481-484): T = (P0_int/R)/Rho_int, heat rate
+// at x_int and its deposit; also leaves the round-indexed sort of x_int for
+// the first concentration deposit.
+void particle_init_heat(tpm_ctx *c) {
+  TPM_LAUNCH(c, "fill_tgas", k_fill_tgas, cell_blocks(c->g), kThreads, 0, c->g.n, c->Rho_int,
+             c->hsc->P0_int / c->R, c->Tgas);
+  if (c->np == 0) {
+    TPM_CUDA_TRY(cudaMemsetAsync(c->Q, 0, sizeof(double) * c->g.n, c->stream));
+    TPM_CUDA_TRY(cudaMemsetAsync(c->partials + kPartQ * kRedBlocks, 0, sizeof(double) * kRedBlocks,
+                                 c->stream));
+    return;
+  }
+  double iTth = c->p.Nu * kPi * c->p.Dp * c->p.k;
+  TPM_LAUNCH(c, "cic_payload", k_cic_payload, pblocks(c->np), kThreads, 0, c->g, c->pq[1][0],
+             c->pq[1][1], c->pq[1][2], c->pq[1][6], c->Tgas, iTth, c->np, c->rhs_t, c->key_r,
+             c->pay_r);
+  c->rcur = 0;
+  heat_deposit_from(c, 0);
+}
+
+void particle_zero_fields(tpm_ctx *c) {
+  TPM_CUDA_TRY(cudaMemsetAsync(c->Fp, 0, sizeof(double) * 3 * c->g.n, c->stream));
+  TPM_CUDA_TRY(cudaMemsetAsync(c->C, 0, sizeof(double) * c->g.n, c->stream));
+}
+
+}  // namespace tpm

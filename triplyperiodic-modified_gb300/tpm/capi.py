@@ -1,0 +1,285 @@
+"""ctypes binding of libtpm.so (include/tpm.h) and a ``Grid`` facade that
+mirrors the reference grid's public surface (grid.h:109-136): the same
+method names run the same steps on the GPU.
+
+There is no CPU fallback: constructing a context without the built library
+or without a CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import inputs
+from .params import Params, TpmParams, TpmScalars
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "lib", "libtpm.so")
+
+FIELD = dict(RU=0, RU_INT=1, RU_NEW=2, RU_NP1=3, RHO=4, RHO_INT=5, RHO_NEW=6, RHO_NP1=7, P=8,
+             C=9, Q=10, FP=11, RHS_POIS=12, DIVERGENCE=13)
+VECTOR = {"RU", "RU_INT", "RU_NEW", "RU_NP1", "FP"}
+PSET = dict(base=0, int=1, new=2, np1=3)
+OPT_STORE_DIVERGENCE = 1
+STATUS = {0: "TPM_OK", -1: "TPM_ERR_ARG", -2: "TPM_ERR_CUDA", -3: "TPM_ERR_TIMEOUT",
+          -4: "TPM_ERR_NONFINITE", -5: "TPM_ERR_UNSUPPORTED", -6: "TPM_ERR_STATE",
+          -7: "TPM_ERR_NOMEM"}
+
+# every entry point include/tpm.h declares: name -> (restype, argtypes)
+_vp, _dp, _ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int32)
+_i, _d, _i64 = ctypes.c_int, ctypes.c_double, ctypes.c_int64
+SIGNATURES = {
+    "tpm_abi_version": (_i, []),
+    "tpm_create": (_i, [_vp, _i64, ctypes.POINTER(_vp)]),
+    "tpm_destroy": (_i, [_vp]),
+    "tpm_last_error": (ctypes.c_char_p, [_vp]),
+    "tpm_upload_field": (_i, [_vp, _i, _dp]),
+    "tpm_download_field": (_i, [_vp, _i, _dp]),
+    "tpm_upload_particles": (_i, [_vp, _i] + [_dp] * 7 + [_ip]),
+    "tpm_download_particles": (_i, [_vp, _i] + [_dp] * 7 + [_ip]),
+    "tpm_download_particle_rhs_t": (_i, [_vp, _dp]),
+    "tpm_set_particle_tau": (_i, [_vp, _dp]),
+    "tpm_set_scalars": (_i, [_vp, _d, _d, _i64]),
+    "tpm_get_scalars": (_i, [_vp, _vp]),
+    "tpm_initialize": (_i, [_vp]),
+    "tpm_substep": (_i, [_vp, _i]),
+    "tpm_end_step": (_i, [_vp]),
+    "tpm_step": (_i, [_vp]),
+    "tpm_run": (_i, [_vp, _i]),
+    "tpm_sync": (_i, [_vp]),
+    "tpm_poisson_solve": (_i, [_vp, _dp, _dp, _dp, _i, _d, ctypes.POINTER(_i), _dp]),
+    "tpm_set_option": (_i, [_vp, _i, _i]),
+    "tpm_profile_enable": (_i, [_vp, _i]),
+    "tpm_profile_report": (_i, [_vp, ctypes.c_char_p, _i, ctypes.POINTER(_i), _dp, _i]),
+    "tpm_profile_reset": (_i, [_vp]),
+    "tpm_launch_count": (_i64, [_vp]),
+}
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """dlopen libtpm.so and declare every entry point (raises if absent)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is not built: run __graft_entry__.build() first")
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class TpmError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+class Context:
+    """One periodic box resident on the current CUDA device."""
+
+    def __init__(self, p: Params, npart: int):
+        self.L = load_library()
+        self.p = p
+        self.npart = int(npart)
+        self._cp = p.to_c()
+        h = _vp()
+        rc = self.L.tpm_create(ctypes.byref(self._cp), self.npart, ctypes.byref(h))
+        self.h = h
+        if rc != 0:
+            msg = self.L.tpm_last_error(h).decode() if h.value else "create failed"
+            self.L.tpm_destroy(h)
+            self.h = None
+            raise TpmError(rc, msg)
+
+    def _check(self, rc):
+        if rc != 0:
+            raise TpmError(rc, self.L.tpm_last_error(self.h).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.tpm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- fields ----
+    def _shape(self, name):
+        s = (self.p.Nz, self.p.Ny, self.p.Nx)
+        return ((3,) + s) if name in VECTOR else s
+
+    def upload_field(self, name, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if a.size != int(np.prod(self._shape(name))):
+            raise ValueError(f"{name}: expected {self._shape(name)}, got {a.shape}")
+        self._check(self.L.tpm_upload_field(self.h, FIELD[name], _dptr(a)))
+
+    def download_field(self, name):
+        a = np.empty(self._shape(name))
+        self._check(self.L.tpm_download_field(self.h, FIELD[name], _dptr(a)))
+        return a
+
+    # ---- particles ----
+    def upload_particles(self, part, pset="base"):
+        arrs = [np.ascontiguousarray(part[q], dtype=np.float64) for q in inputs.PQ]
+        flag = np.ascontiguousarray(part["flag"], dtype=np.int32)
+        self._check(self.L.tpm_upload_particles(self.h, PSET[pset], *[_dptr(a) for a in arrs],
+                                                flag.ctypes.data_as(_ip)))
+
+    def download_particles(self, pset="base"):
+        out = {q: np.empty(self.npart) for q in inputs.PQ}
+        out["flag"] = np.empty(self.npart, dtype=np.int32)
+        self._check(self.L.tpm_download_particles(self.h, PSET[pset],
+                                                  *[_dptr(out[q]) for q in inputs.PQ],
+                                                  out["flag"].ctypes.data_as(_ip)))
+        return out
+
+    def download_rhs_t(self):
+        a = np.empty(self.npart)
+        self._check(self.L.tpm_download_particle_rhs_t(self.h, _dptr(a)))
+        return a
+
+    def set_tau(self, tau):
+        if tau is None:
+            self._check(self.L.tpm_set_particle_tau(self.h, None))
+        else:
+            t = np.ascontiguousarray(tau, dtype=np.float64)
+            self._check(self.L.tpm_set_particle_tau(self.h, _dptr(t)))
+
+    # ---- scalars / control ----
+    def set_scalars(self, P0, T_cur=0.0, num_timestep=0):
+        self._check(self.L.tpm_set_scalars(self.h, P0, T_cur, num_timestep))
+
+    def scalars(self):
+        s = TpmScalars()
+        self._check(self.L.tpm_get_scalars(self.h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def set_option(self, opt, value):
+        self._check(self.L.tpm_set_option(self.h, opt, int(value)))
+
+    def load(self, s: inputs.State):
+        self.upload_field("RU", s.RU)
+        self.upload_field("RHO", s.Rho)
+        self.upload_field("P", s.P)
+        if self.npart:
+            self.upload_particles(s.part, "base")
+        self.set_scalars(s.P0, s.T_cur, s.num_timestep)
+        if s.tau is not None:
+            self.set_tau(s.tau)
+
+    def initialize(self):
+        self._check(self.L.tpm_initialize(self.h))
+
+    def substep(self, stage):
+        self._check(self.L.tpm_substep(self.h, stage))
+
+    def end_step(self):
+        self._check(self.L.tpm_end_step(self.h))
+
+    def step(self):
+        self._check(self.L.tpm_step(self.h))
+
+    def run(self, nsteps):
+        self._check(self.L.tpm_run(self.h, nsteps))
+
+    def sync(self):
+        self._check(self.L.tpm_sync(self.h))
+
+    def poisson_solve(self, C3, P, RHS, max_it, eps):
+        C3 = np.ascontiguousarray(C3, dtype=np.float64)
+        P = np.ascontiguousarray(P, dtype=np.float64).copy()
+        RHS = np.ascontiguousarray(RHS, dtype=np.float64)
+        it = ctypes.c_int(0)
+        err = ctypes.c_double(0)
+        self._check(self.L.tpm_poisson_solve(self.h, _dptr(C3), _dptr(P), _dptr(RHS), max_it,
+                                             eps, ctypes.byref(it), ctypes.byref(err)))
+        return P, it.value, err.value
+
+    # ---- profiling ----
+    def profile(self, on=True):
+        self._check(self.L.tpm_profile_enable(self.h, int(on)))
+
+    def profile_reset(self):
+        self._check(self.L.tpm_profile_reset(self.h))
+
+    def profile_report(self):
+        maxk, cap = 128, 8192
+        names = ctypes.create_string_buffer(cap)
+        launches = (ctypes.c_int * maxk)()
+        ms = (ctypes.c_double * maxk)()
+        k = self.L.tpm_profile_report(self.h, names, cap, launches, ms, maxk)
+        if k < 0:
+            self._check(k)
+        out, off = {}, 0
+        raw = names.raw
+        for i in range(k):
+            end = raw.index(b"\0", off)
+            out[raw[off:end].decode()] = (int(launches[i]), float(ms[i]))
+            off = end + 1
+        return out
+
+    def launch_count(self):
+        return int(self.L.tpm_launch_count(self.h))
+
+
+class Grid:
+    """The reference grid's time-stepping surface (grid.h:112-136) on the GPU.
+
+    ``Initialize``        -> grid::Initialize tail (grid.cpp:461-484)
+    ``substep(k)``        -> Update_Rho ... TimeAdvance_RK4 for RK4_count = k
+    ``TimeAdvance``       -> RU_np1.make_mean_U0 + grid::TimeAdvance
+    ``step``              -> PARAM.update + 4 substeps + TimeAdvance
+    """
+
+    def __init__(self, p: Params, state: inputs.State):
+        self.ctx = Context(p, state.npart)
+        self.ctx.load(state)
+
+    def Initialize(self):
+        self.ctx.initialize()
+
+    def substep(self, rk4_count):
+        self.ctx.substep(rk4_count)
+
+    def TimeAdvance(self):
+        self.ctx.end_step()
+
+    def step(self):
+        self.ctx.step()
+
+    @property
+    def T_cur(self):
+        return self.ctx.scalars()["T_cur"]
+
+    @property
+    def P0(self):
+        return self.ctx.scalars()["P0"]
+
+    def __getattr__(self, name):
+        # field access by reference names: RU, RU_int, Rho, P, C, RHS_Part_Temp ...
+        alias = {"RU": "RU", "RU_int": "RU_INT", "RU_new": "RU_NEW", "RU_np1": "RU_NP1",
+                 "Rho": "RHO", "Rho_int": "RHO_INT", "Rho_new": "RHO_NEW", "Rho_np1": "RHO_NP1",
+                 "P": "P", "C": "C", "RHS_Part_Temp": "Q", "RHS_Pois": "RHS_POIS",
+                 "divergence": "DIVERGENCE"}
+        if name in alias:
+            return self.ctx.download_field(alias[name])
+        raise AttributeError(name)
