@@ -1,0 +1,394 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 RK4 substep library on the 256^3 + 8M-particle
+heated, two-way-coupled workload (the headline configuration).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+One JSON line on stdout (rank 0).  `value` is whole-job Mcell-steps/s with the
+state resident in HBM; `e2e` is the same metric through the C ABI with the
+step-boundary state round-tripped every step between pinned host buffers and
+the device (tpm_upload_* / tpm_resume / tpm_step / tpm_download_*).  With
+--gpus N > 1 every rank runs an independent replica box (the path does not
+shard), and `value` sums the cells of all ranks over the slowest rank's time.
+`--impl reference` times the reference's CPU implementation of the path on
+this host instead (the reference build when it exists here, else the C
+restatement of it), on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "triplyperiodic-modified_gb300"))
+
+METRIC = "Mcell-steps/s at 256³+8M particles, mixed vs FP64 on 1 GB300; % HBM roofline"
+UNIT = "Mcell-steps/s"
+WORKLOAD = "box256_p8e6_heated"
+FALLBACK_HBM_GBS = 6800.0
+
+# Algorithmic bytes per launch of each kernel: (bytes per cell, bytes per
+# particle) for FP64 storage; the derivation is tabulated in the design doc.
+KERNEL_BYTES = {
+    "rhs_momentum": (21 * 8, 0),
+    "poisson_rhs": (11 * 8, 0),
+    "fft_x_fwd_resid": (6 * 8 + 8, 0),
+    "fft_y": (16, 0),
+    "fft_z_solve": (16, 0),
+    "fft_x_inv_update": (24, 0),
+    "deposit_heat": (4 + 8, 32),
+    "deposit_conc": (4 + 8, 24),
+    "deposit_momentum": (4 + 24, 48),
+    "particle_push": (0, 488),
+    "face_velocity": (7 * 8, 0),
+    "rho_update": (9 * 8, 0),
+    "project": (13 * 8, 0),
+}
+
+
+def peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        for k in ("hbm_gbs", "hbm_GBs", "copy_gbs"):
+            if k in d:
+                return float(d[k]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def algorithmic_bytes_per_step(ncell, npart, n_it, w=8, wp=8):
+    """Per RK4 step: N^3 (4 (61 + 15 (n_it-1)) + 9) w + Np 4 (37 wp + 16)."""
+    return ncell * (4 * (61 + 15 * (n_it - 1)) + 9) * w + npart * 4 * (37 * wp + 16)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- GPU arm
+def make_workload(name=WORKLOAD, precision=0, N=None, npart=None):
+    from tpm import inputs, params as P
+
+    w = dict(P.WORKLOADS[name])
+    N = N or w["N"]
+    npart = npart if npart is not None else w["npart"]
+    p = P.physical(N, npart, nu=w["nu"], A=w["A"], tau_p=w["tau_p"],
+                   mass_loading=w["mass_loading"], heating_Q=w["heating_Q"], iterations=20,
+                   epsilon=1e-13, precision=precision)
+    s = inputs.make_state(p, npart, seed=w["seed"])
+    p = p.replace(dt=inputs.cfl_dt(p, s.RU))
+    return p, s
+
+
+def time_gpu(p, s, steps, warmup, dist, device):
+    import torch
+    from tpm import capi
+
+    ctx = capi.Context(p, s.npart)
+    ctx.load(s)
+    ctx.initialize()
+    for _ in range(warmup):
+        ctx.step()
+    ctx.sync()
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=device)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    it0 = ctx.scalars()["total_poisson_iterations"]
+    l0 = ctx.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(device) as clk:
+        e0.record(stream)
+        ctx.run(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    sc = ctx.scalars()
+    n_it = (sc["total_poisson_iterations"] - it0) / (4.0 * steps)
+    launches = ctx.launch_count() - l0
+    # per-kernel durations (CUDA events around each launch on the same stream)
+    ctx.profile(True)
+    ctx.run(2)
+    prof = ctx.profile_report()
+    ctx.profile(False)
+    return ctx, ms, n_it, launches, prof, clk.summary()
+
+
+def time_e2e(ctx, steps):
+    """Same metric through the C ABI with host buffers: every step uploads the
+    step-boundary state from pinned host memory, resumes, steps, and reads the
+    state back."""
+    import numpy as np
+    import torch
+
+    st = ctx.download_state()
+
+    def pinned_like(a):
+        t = torch.empty(a.shape, dtype=torch.float64 if a.dtype == np.float64 else torch.int32,
+                        pin_memory=True)
+        v = t.numpy()
+        v[...] = a
+        return v
+
+    host = {k: pinned_like(st[k]) for k in ctx.STATE_FIELDS}
+    if ctx.npart:
+        host["part"] = {q: pinned_like(v) for q, v in st["part"].items()}
+        host["RHS_T"] = pinned_like(st["RHS_T"])
+    host["scalars"] = st["scalars"]
+    h2d = sum(host[k].nbytes for k in ctx.STATE_FIELDS)
+    if ctx.npart:
+        h2d += sum(v.nbytes for v in host["part"].values()) + host["RHS_T"].nbytes
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ctx.upload_state(host)
+        ctx.step()
+        st = ctx.download_state()
+        for k in ctx.STATE_FIELDS:
+            host[k][...] = st[k]
+        if ctx.npart:
+            for q, v in st["part"].items():
+                host["part"][q][...] = v
+            host["RHS_T"][...] = st["RHS_T"]
+        host["scalars"] = st["scalars"]
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) * 1e3 / steps, h2d, h2d
+
+
+def cpu_sample(workload, steps_total):
+    """A bounded CPU sample of the workload: a smaller box at the same particle
+    density and physics (128^3 unless that would take more than ~3 minutes)."""
+    from tpm import params as P
+
+    w = P.WORKLOADS[workload]
+    Ns = 128 if steps_total <= 16 else 96 if steps_total <= 40 else 64
+    Ns = min(Ns, w["N"])
+    nps = int(round(w["npart"] * (Ns / w["N"]) ** 3))
+    p, s = make_workload(workload, 0, N=Ns, npart=nps)
+    return Ns, nps, p, s
+
+
+def cpu_baseline_port(workload):
+    """The C restatement of the reference on one host core, one RK4 step of a
+    bounded sample of the workload (1 thread)."""
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import pyoracle
+
+    pyoracle.build()
+    Ns, nps, p, s = cpu_sample(workload, 1)
+    o = pyoracle.Oracle(p, s.npart)
+    o.load(s)
+    o.initialize()
+    t0 = time.perf_counter()
+    o.step()
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": round(p.ncell / dt / 1e6, 4), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"1 RK4 step of a {Ns}^3 box with {nps} particles (the workload's particle "
+                      f"density and physics), {dt:.1f} s on one core, C restatement of the "
+                      f"reference"}
+
+
+def gpu_main(args):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as td
+
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+        dist = td
+    prec = {"fp64": 0, "mixed": 1}[args.precision]
+    p, s = make_workload(args.workload, prec)
+    ctx, ms, n_it, launches, prof, clocks = time_gpu(p, s, args.steps, args.warmup, dist, local)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    value = world * p.ncell * args.steps / (ms * 1e-3) / 1e6
+    e2e_ms, h2d, d2h = time_e2e(ctx, max(1, min(args.steps, 3)))
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * p.ncell / (e2e_ms * 1e-3) / 1e6
+    peak, peak_kind = peaks()
+    # dominant kernel roofline
+    dom = max(prof.items(), key=lambda kv: kv[1][1])
+    name, (nl, tot_ms) = dom
+    bc, bp = KERNEL_BYTES.get(name, (0, 0))
+    per_launch = bc * p.ncell + bp * s.npart
+    avg_ms = tot_ms / nl
+    achieved = per_launch / (avg_ms * 1e-3) / 1e9
+    step_bytes = algorithmic_bytes_per_step(p.ncell, s.npart, n_it)
+    step_gbs = step_bytes / (ms_per_step * 1e-3) / 1e9
+    total_prof = sum(v[1] for v in prof.values())
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == 0 else "mixed(f32 compute, f64 state)",
+        "data": "synthetic (seeded solenoidal E(k)~k^4 exp(-2(k/4)^2) velocity, uniform particles)",
+        "config": {"workload": f"{args.workload}: {p.Nx}^3 cells, {s.npart} particles, heated, "
+                               f"two-way coupled, Poisson eps=1e-13 (mean {n_it:.2f} iterations)",
+                   "precision": args.precision, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (working set ~8 GB)"},
+        "roofline": {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": None, "peak_source": f"{peak_kind} HBM copy bandwidth",
+                     "kernel_share": round(tot_ms / total_prof, 4)},
+        "step_roofline": {"achieved_gbs": round(step_gbs, 1),
+                          "frac": round(step_gbs / peak, 4),
+                          "algorithmic_bytes_per_step": int(step_bytes)},
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "kernels_ms_per_step": {k: round(v[1] / 2, 3) for k, v in
+                                sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]},
+        "mparticle_steps_per_s": round(world * s.npart * args.steps / (ms * 1e-3) / 1e6, 3),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_port(args.workload)
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------- reference arm
+def reference_main(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import pyoracle
+
+    pyoracle.build()
+    # bounded sample: a smaller box at the workload's particle density and
+    # physics, one RK4 step per timed step
+    Ns, nps, p, s = cpu_sample(args.workload, args.steps + args.warmup)
+    kind = "port"
+    times = []
+    if pyoracle.have_reference():
+        ref = pyoracle.run_reference(p, s, args.steps)
+        kind = "reference"
+        secs = ref["seconds"]
+    else:
+        o = pyoracle.Oracle(p, s.npart)
+        o.load(s)
+        o.initialize()
+        for _ in range(args.warmup):
+            o.step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            o.step()
+        secs = time.perf_counter() - t0
+        o.close()
+    value = p.ncell * args.steps / secs / 1e6
+    sample = (f"{Ns}^3 box with {nps} particles (the workload's particle density and physics), "
+              f"{args.steps} RK4 steps on one host core")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(secs * 1e3 / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload} (sampled: {Ns}^3, {nps} particles)",
+                   "precision": "fp64", "parallelism": "1 host core"},
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": 1, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawTextHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    if args.impl == "reference":
+        reference_main(args)
+    else:
+        gpu_main(args)
+
+
+if __name__ == "__main__":
+    main()

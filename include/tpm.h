@@ -143,6 +143,7 @@ int tpm_download_particles(tpm_ctx *ctx, int set, double *x, double *y, double *
                            double *v, double *w, double *T, int32_t *flag);
 /* particle.h:113 RHS_T (heat exchange rate, W) */
 int tpm_download_particle_rhs_t(tpm_ctx *ctx, double *rhs_t);
+int tpm_upload_particle_rhs_t(tpm_ctx *ctx, const double *rhs_t);
 /* Optional per-particle momentum relaxation time (extension: the reference has
  * one global Tp, particle.cpp:365).  NULL restores the global Tp. */
 int tpm_set_particle_tau(tpm_ctx *ctx, const double *tau);
@@ -157,6 +158,15 @@ int tpm_get_scalars(tpm_ctx *ctx, tpm_scalars *out);
  * particles and scalars. */
 int tpm_initialize(tpm_ctx *ctx);
 
+/* Continue from a step-boundary state held by the caller: after uploading
+ * RU, RU_INT, RHO, P and Q (RHS_Part_Temp), the base particle set, the
+ * particle heat rates and the scalars, this restores the derived device state
+ * (stage copies, deposit sort) so the next tpm_step continues the run exactly
+ * where tpm_download_* took it.  (The reference's own restart, grid.cpp:221-238
+ * + :461-484, recomputes RU_int and RHS_Part_Temp instead and so does not
+ * continue a run bit for bit; tpm_initialize reproduces that.) */
+int tpm_resume(tpm_ctx *ctx);
+
 /* One RK4 substep (simulation.cpp:62-77 with Update_Particle enabled):
  * Update_Rho, Update_P0, Update_Particle, Update_RU_WOP, Compute_Div_U_new,
  * Compute_RHS_Pois, Solve_Poisson, Update_RU_WP, TimeAdvance_RK4. */
@@ -167,6 +177,8 @@ int tpm_end_step(tpm_ctx *ctx);
 int tpm_step(tpm_ctx *ctx);
 int tpm_run(tpm_ctx *ctx, int nsteps);
 int tpm_sync(tpm_ctx *ctx);
+/* The context's CUDA stream (cudaStream_t), e.g. to record timing events. */
+void *tpm_stream(tpm_ctx *ctx);
 
 /* poisson::Solve with Solver==0 (poisson.h:79, poisson.cpp:391-462) on host
  * buffers: div(C grad P) = RHS by Richardson iteration preconditioned with

@@ -33,6 +33,7 @@ struct orc {
   double R, Tp, mp, Vcell, xh, yh, zh;
   /* grid state (grid.h:57-98) */
   vec3 RU, RU_int, RU_new, RU_np1, RHS_RU, U, Rho_face, dummy, dummy2;
+  vec3 Fp; /* copy of the part2gas_velocity deposit, for inspection */
   double *Rho, *Rho_int, *Rho_new, *Rho_np1, *RHS_Rho, *P, *C, *T, *divergence, *RHS_Pois,
       *RHS_Part_Temp;
   /* poisson scratch (poisson.h:61-62) */
@@ -84,7 +85,7 @@ orc *orc_create(const tpm_params *p, int64_t np) {
   o->Vcell = o->dx * o->dy * o->dz; /* gridsize.h:43 */
   long n = o->n;
   o->RU = valloc(n); o->RU_int = valloc(n); o->RU_new = valloc(n); o->RU_np1 = valloc(n);
-  o->RHS_RU = valloc(n); o->U = valloc(n); o->Rho_face = valloc(n);
+  o->RHS_RU = valloc(n); o->U = valloc(n); o->Rho_face = valloc(n); o->Fp = valloc(n);
   o->dummy = valloc(n); o->dummy2 = valloc(n); o->pdummy = valloc(n);
   o->Rho = alloc(n); o->Rho_int = alloc(n); o->Rho_new = alloc(n); o->Rho_np1 = alloc(n);
   o->RHS_Rho = alloc(n); o->P = alloc(n); o->C = alloc(n); o->T = alloc(n);
@@ -107,7 +108,7 @@ orc *orc_create(const tpm_params *p, int64_t np) {
 
 void orc_destroy(orc *o) {
   if (!o) return;
-  vec3 *vs[] = {&o->RU, &o->RU_int, &o->RU_new, &o->RU_np1, &o->RHS_RU, &o->U, &o->Rho_face,
+  vec3 *vs[] = {&o->RU, &o->RU_int, &o->RU_new, &o->RU_np1, &o->RHS_RU, &o->U, &o->Rho_face, &o->Fp,
                 &o->dummy, &o->dummy2, &o->pdummy};
   for (size_t i = 0; i < sizeof(vs) / sizeof(vs[0]); ++i) vfree(*vs[i]);
   double *ss[] = {o->Rho, o->Rho_int, o->Rho_new, o->Rho_np1, o->RHS_Rho, o->P, o->C, o->T,
@@ -480,6 +481,8 @@ int orc_poisson_solve(orc *o, const double *C3, double *P, const double *RHS, in
   return poisson_fft(o, C, P, RHS, max_it, eps, err_out);
 }
 
+static void vcopy(orc *o, vec3 dst, vec3 src);
+
 /* --------------------------------------------------------- grid operators */
 /* grid::Update_Rho, grid.cpp:608-614 */
 static void update_rho(orc *o, int s) {
@@ -533,6 +536,7 @@ static void update_particle(orc *o, int s) {
     memset(o->RHS_RU.y, 0, sizeof(double) * (size_t)o->n);
     memset(o->RHS_RU.z, 0, sizeof(double) * (size_t)o->n);
   }
+  vcopy(o, o->Fp, o->RHS_RU);
   wrap_particles(o);
   double a = o->P0_new / o->R;
   for (long c = 0; c < o->n; ++c) o->T[c] = a / o->Rho_new[c];
@@ -768,7 +772,7 @@ static double *field_ptr(orc *o, int f, int *nvec) {
     case TPM_FIELD_RU_INT: v = &o->RU_int; break;
     case TPM_FIELD_RU_NEW: v = &o->RU_new; break;
     case TPM_FIELD_RU_NP1: v = &o->RU_np1; break;
-    case TPM_FIELD_FP: v = &o->RHS_RU; break;
+    case TPM_FIELD_FP: v = &o->Fp; break;
     case TPM_FIELD_RHO: return o->Rho;
     case TPM_FIELD_RHO_INT: return o->Rho_int;
     case TPM_FIELD_RHO_NEW: return o->Rho_new;

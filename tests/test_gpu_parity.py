@@ -278,3 +278,23 @@ def test_large_box_properties(capi):
     for q, L in (("x", p.Lx), ("y", p.Ly), ("z", p.Lz)):
         assert part[q].min() >= 0 and part[q].max() <= L
     assert np.all(np.isfinite(RU))
+
+
+def test_host_round_trip_resume_is_exact(capi):
+    """Downloading the step-boundary state and resuming from it in a fresh
+    context continues the run bit for bit (the e2e bench relies on this)."""
+    p, s = make_case(24, 2000, seed=12, heat=0.5)
+    a = gpu_run(capi, p, s, 2)
+    st = a.download_state()
+    a.run(2)
+    a.sync()
+    b = capi.Context(p, s.npart)
+    b.upload_state(st)
+    b.run(2)
+    b.sync()
+    for g in ("RU", "RU_INT", "RHO", "P", "Q", "C"):
+        assert np.array_equal(a.download_field(g), b.download_field(g)), g
+    pa, pb = a.download_particles("base"), b.download_particles("base")
+    for q in inputs.PQ:
+        assert np.array_equal(pa[q], pb[q]), q
+    assert a.scalars()["P0"] == b.scalars()["P0"]

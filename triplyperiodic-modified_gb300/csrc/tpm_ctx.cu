@@ -430,6 +430,17 @@ int tpm_download_particle_rhs_t(tpm_ctx *c, double *rhs_t) {
   });
 }
 
+int tpm_upload_particle_rhs_t(tpm_ctx *c, const double *rhs_t) {
+  return guarded(c, [&]() -> int {
+    if (!rhs_t) return fail(c, TPM_ERR_ARG, "null host buffer");
+    if (c->np)
+      TPM_CUDA_TRY(cudaMemcpyAsync(c->rhs_t, rhs_t, sizeof(double) * c->np, cudaMemcpyHostToDevice,
+                                   c->stream));
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return TPM_OK;
+  });
+}
+
 int tpm_set_particle_tau(tpm_ctx *c, const double *tau) {
   return guarded(c, [&]() -> int {
     if (!tau) {
@@ -498,6 +509,27 @@ int tpm_initialize(tpm_ctx *c) {
     // grid.cpp:481-484: initial particle heat coupling
     tpm::particle_zero_fields(c);
     tpm::particle_init_heat(c);
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->initialized = true;
+    return TPM_OK;
+  });
+}
+
+int tpm_resume(tpm_ctx *c) {
+  return guarded(c, [&]() -> int {
+    const long long n = c->g.n;
+    // at a step boundary Rho_int == Rho, x_int == x (all particle copies
+    // agree), P0_int == P0 and every np1 copy equals its base copy
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->Rho_int, c->Rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+    for (int q = 0; q < 7 && c->np > 0; ++q)
+      TPM_CUDA_TRY(cudaMemcpyAsync(c->pq[1][q], c->pq[0][q], sizeof(double) * c->np,
+                                   cudaMemcpyDeviceToDevice, c->stream));
+    pull_scalars(c);
+    c->hsc->P0_int = c->hsc->P0;
+    c->hsc->P0_np1 = c->hsc->P0;
+    push_scalars(c);
+    c->np1_is_base = true;
+    tpm::particle_resume(c);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->initialized = true;
     return TPM_OK;
@@ -625,5 +657,7 @@ int tpm_profile_report(tpm_ctx *c, char *names, int cap, int *launches, double *
 }
 
 int64_t tpm_launch_count(const tpm_ctx *c) { return c ? c->launches : 0; }
+
+void *tpm_stream(tpm_ctx *c) { return c ? (void *)c->stream : nullptr; }
 
 }  // extern "C"

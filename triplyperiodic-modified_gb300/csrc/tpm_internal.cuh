@@ -169,6 +169,7 @@ void particle_deposit_momentum(tpm_ctx *c);
 void particle_deposit_concentration(tpm_ctx *c);
 void particle_heat(tpm_ctx *c);
 void particle_init_heat(tpm_ctx *c);
+void particle_resume(tpm_ctx *c);
 void particle_zero_fields(tpm_ctx *c);
 
 }  // namespace tpm

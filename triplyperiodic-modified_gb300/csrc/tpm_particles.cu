@@ -153,7 +153,7 @@ __global__ void k_cic_payload(Grid g, const double *__restrict__ x, const double
                               const double *__restrict__ z, const double *__restrict__ Tp,
                               const double *__restrict__ Tgas, double iTth, int64_t np,
                               double *__restrict__ rhs_t, int32_t *__restrict__ key_r,
-                              double *__restrict__ pay_r) {
+                              double *__restrict__ pay_r, int compute_rhs) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
        p += (int64_t)gridDim.x * blockDim.x) {
     const double xx = x[p], yy = y[p], zz = z[p];
@@ -165,6 +165,14 @@ __global__ void k_cic_payload(Grid g, const double *__restrict__ x, const double
     const int i1 = wrap_any(ri, g.nx), im = wrap_any(ri - 1, g.nx);
     const int j1 = wrap_any(rj, g.ny), jm = wrap_any(rj - 1, g.ny);
     const int k1 = wrap_any(rk, g.nz), km = wrap_any(rk - 1, g.nz);
+    key_r[p] = (int32_t)at(g, i1, j1, k1);
+    pay_r[0 * np + p] = x_l;
+    pay_r[1 * np + p] = y_l;
+    pay_r[2 * np + p] = z_l;
+    if (!compute_rhs) {  // heat rate given (continuation of a run)
+      pay_r[3 * np + p] = rhs_t[p];
+      continue;
+    }
     // gas2part_Temp_int + Compute_RHS_Temp_int (particle.cpp:402-466)
     const double Tg = x_l * y_l * z_l * Tgas[at(g, i1, j1, k1)] +
                       (1 - x_l) * y_l * z_l * Tgas[at(g, im, j1, k1)] +
@@ -176,12 +184,20 @@ __global__ void k_cic_payload(Grid g, const double *__restrict__ x, const double
                       (1 - x_l) * (1 - y_l) * (1 - z_l) * Tgas[at(g, im, jm, km)];
     const double rt = (Tg - Tp[p]) * iTth;
     rhs_t[p] = rt;
-    key_r[p] = (int32_t)at(g, i1, j1, k1);
-    pay_r[0 * np + p] = x_l;
-    pay_r[1 * np + p] = y_l;
-    pay_r[2 * np + p] = z_l;
     pay_r[3 * np + p] = rt;
   }
+}
+
+// block partial sums of a centre field (mean for grid::Update_P0)
+__global__ void k_partial_sums(long long n, const double *__restrict__ f,
+                               double *__restrict__ partials) {
+  __shared__ double sh[32];
+  double acc = 0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x)
+    acc += f[c];
+  double b = block_sum(acc, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = b;
 }
 
 __global__ void k_fill_tgas(long long n, const double *__restrict__ Rho, double T_scale,
@@ -505,9 +521,27 @@ void particle_init_heat(tpm_ctx *c) {
   double iTth = c->p.Nu * kPi * c->p.Dp * c->p.k;
   TPM_LAUNCH(c, "cic_payload", k_cic_payload, pblocks(c->np), kThreads, 0, c->g, c->pq[1][0],
              c->pq[1][1], c->pq[1][2], c->pq[1][6], c->Tgas, iTth, c->np, c->rhs_t, c->key_r,
-             c->pay_r);
+             c->pay_r, 1);
   c->rcur = 0;
   heat_deposit_from(c, 0);
+}
+
+// Continuation from a caller-held state: rebuild the round-indexed sort of
+// x_int (first concentration deposit) from the given heat rates, and the
+// partial sums of the given RHS_Part_Temp (first Update_P0).
+void particle_resume(tpm_ctx *c) {
+  int nb = cell_blocks(c->g);
+  TPM_LAUNCH(c, "partial_sums", k_partial_sums, nb, kThreads, 0, c->g.n, c->Q,
+             c->partials + kPartQ * kRedBlocks);
+  c->q_parts = nb;
+  c->rcur = 0;
+  if (c->np == 0) return;
+  TPM_LAUNCH(c, "cic_payload", k_cic_payload, pblocks(c->np), kThreads, 0, c->g, c->pq[1][0],
+             c->pq[1][1], c->pq[1][2], c->pq[1][6], c->Tgas, 0.0, c->np, c->rhs_t, c->key_r,
+             c->pay_r, 0);
+  sort_by_cell(c, c->key_r, c->perm_r[0], c->starts_r[0]);
+  TPM_LAUNCH(c, "payload_gather_r", k_gather_payload, pblocks(c->np), kThreads, 0, c->np, 4,
+             c->perm_r[0], c->pay_r, c->pay_r_s[0]);
 }
 
 void particle_zero_fields(tpm_ctx *c) {

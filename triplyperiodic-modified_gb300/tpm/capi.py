@@ -40,7 +40,10 @@ SIGNATURES = {
     "tpm_upload_particles": (_i, [_vp, _i] + [_dp] * 7 + [_ip]),
     "tpm_download_particles": (_i, [_vp, _i] + [_dp] * 7 + [_ip]),
     "tpm_download_particle_rhs_t": (_i, [_vp, _dp]),
+    "tpm_upload_particle_rhs_t": (_i, [_vp, _dp]),
     "tpm_set_particle_tau": (_i, [_vp, _dp]),
+    "tpm_resume": (_i, [_vp]),
+    "tpm_stream": (_vp, [_vp]),
     "tpm_set_scalars": (_i, [_vp, _d, _d, _i64]),
     "tpm_get_scalars": (_i, [_vp, _vp]),
     "tpm_initialize": (_i, [_vp]),
@@ -156,6 +159,36 @@ class Context:
         a = np.empty(self.npart)
         self._check(self.L.tpm_download_particle_rhs_t(self.h, _dptr(a)))
         return a
+
+    def upload_rhs_t(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        self._check(self.L.tpm_upload_particle_rhs_t(self.h, _dptr(a)))
+
+    def resume(self):
+        self._check(self.L.tpm_resume(self.h))
+
+    def stream(self):
+        return self.L.tpm_stream(self.h)
+
+    # ---- exact step-boundary state (what tpm_resume needs) ----
+    STATE_FIELDS = ("RU", "RU_INT", "RHO", "P", "Q")
+
+    def download_state(self):
+        st = {f: self.download_field(f) for f in self.STATE_FIELDS}
+        st["part"] = self.download_particles("base") if self.npart else None
+        st["RHS_T"] = self.download_rhs_t() if self.npart else None
+        st["scalars"] = self.scalars()
+        return st
+
+    def upload_state(self, st):
+        for f in self.STATE_FIELDS:
+            self.upload_field(f, st[f])
+        if self.npart:
+            self.upload_particles(st["part"], "base")
+            self.upload_rhs_t(st["RHS_T"])
+        sc = st["scalars"]
+        self.set_scalars(sc["P0"], sc["T_cur"], sc["num_timestep"])
+        self.resume()
 
     def set_tau(self, tau):
         if tau is None:
