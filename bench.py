@@ -204,14 +204,7 @@ def time_e2e(ctx, steps):
     for _ in range(steps):
         ctx.upload_state(host)
         ctx.step()
-        st = ctx.download_state()
-        for k in ctx.STATE_FIELDS:
-            host[k][...] = st[k]
-        if ctx.npart:
-            for q, v in st["part"].items():
-                host["part"][q][...] = v
-            host["RHS_T"][...] = st["RHS_T"]
-        host["scalars"] = st["scalars"]
+        host = ctx.download_state(out=host)
     torch.cuda.synchronize()
     return (time.perf_counter() - t0) * 1e3 / steps, h2d, h2d
 

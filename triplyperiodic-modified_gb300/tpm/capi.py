@@ -135,8 +135,10 @@ class Context:
             raise ValueError(f"{name}: expected {self._shape(name)}, got {a.shape}")
         self._check(self.L.tpm_upload_field(self.h, FIELD[name], _dptr(a)))
 
-    def download_field(self, name):
-        a = np.empty(self._shape(name))
+    def download_field(self, name, out=None):
+        a = np.empty(self._shape(name)) if out is None else out
+        if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != np.prod(self._shape(name)):
+            raise ValueError(f"{name}: bad output buffer")
         self._check(self.L.tpm_download_field(self.h, FIELD[name], _dptr(a)))
         return a
 
@@ -147,16 +149,17 @@ class Context:
         self._check(self.L.tpm_upload_particles(self.h, PSET[pset], *[_dptr(a) for a in arrs],
                                                 flag.ctypes.data_as(_ip)))
 
-    def download_particles(self, pset="base"):
-        out = {q: np.empty(self.npart) for q in inputs.PQ}
-        out["flag"] = np.empty(self.npart, dtype=np.int32)
+    def download_particles(self, pset="base", out=None):
+        if out is None:
+            out = {q: np.empty(self.npart) for q in inputs.PQ}
+            out["flag"] = np.empty(self.npart, dtype=np.int32)
         self._check(self.L.tpm_download_particles(self.h, PSET[pset],
                                                   *[_dptr(out[q]) for q in inputs.PQ],
                                                   out["flag"].ctypes.data_as(_ip)))
         return out
 
-    def download_rhs_t(self):
-        a = np.empty(self.npart)
+    def download_rhs_t(self, out=None):
+        a = np.empty(self.npart) if out is None else out
         self._check(self.L.tpm_download_particle_rhs_t(self.h, _dptr(a)))
         return a
 
@@ -173,10 +176,13 @@ class Context:
     # ---- exact step-boundary state (what tpm_resume needs) ----
     STATE_FIELDS = ("RU", "RU_INT", "RHO", "P", "Q")
 
-    def download_state(self):
-        st = {f: self.download_field(f) for f in self.STATE_FIELDS}
-        st["part"] = self.download_particles("base") if self.npart else None
-        st["RHS_T"] = self.download_rhs_t() if self.npart else None
+    def download_state(self, out=None):
+        """Step-boundary state; with `out` (a previous result, e.g. in pinned
+        host memory) the arrays are filled in place."""
+        o = out or {}
+        st = {f: self.download_field(f, o.get(f)) for f in self.STATE_FIELDS}
+        st["part"] = self.download_particles("base", o.get("part")) if self.npart else None
+        st["RHS_T"] = self.download_rhs_t(o.get("RHS_T")) if self.npart else None
         st["scalars"] = self.scalars()
         return st
 
