@@ -59,9 +59,9 @@ def oracle_run(oracle_lib, p, s, nsteps=0, substeps=None, tau=None):
     return o
 
 
-def make_case(N, npart, seed, heat=0.3, iterations=3, eps=0.0, **extra):
-    p = P.physical(N, npart, nu=0.02, A=0.1, tau_p=0.1, mass_loading=0.5, heating_Q=heat,
-                   iterations=iterations, epsilon=eps)
+def make_case(N, npart, seed, heat=0.3, iterations=3, eps=0.0, mass_loading=0.5, **extra):
+    p = P.physical(N, npart, nu=0.02, A=0.1, tau_p=0.1, mass_loading=mass_loading,
+                   heating_Q=heat, iterations=iterations, epsilon=eps)
     s = inputs.make_state(p, npart, seed=seed)
     p = p.replace(dt=inputs.cfl_dt(p, s.RU), **extra)
     return p, s
@@ -70,12 +70,18 @@ def make_case(N, npart, seed, heat=0.3, iterations=3, eps=0.0, **extra):
 FIELDS = [("RU", "RU"), ("RU_INT", "RU_INT"), ("RHO", "RHO"), ("P", "P"), ("C", "C")]
 
 
-def assert_state_close(ctx, o, tol, check_rhs_t=True):
+def assert_state_close(ctx, o, tol, check_rhs_t=True, check_q=True):
+    """check_q / check_rhs_t: with heating off the particle heat exchange is
+    (Tg - T_p) of two temperatures equal up to roundoff, so it is roundoff
+    noise and has no meaningful relative error."""
     for g, r in FIELDS:
-        e = rel_err(ctx.download_field(g), o.get_field(r))
+        a = ctx.download_field(g)
+        assert np.all(np.isfinite(a)), g
+        e = rel_err(a, o.get_field(r))
         assert e <= tol, (g, e)
-    e = rel_err(ctx.download_field("Q"), o.get_field("Q"))
-    assert e <= 10 * tol, ("Q", e)
+    if check_q:
+        e = rel_err(ctx.download_field("Q"), o.get_field("Q"))
+        assert e <= 10 * tol, ("Q", e)
     a, b = ctx.download_particles("base"), o.get_particles(0)
     assert np.array_equal(a["flag"], b["flag"])
     for q in inputs.PQ:
@@ -138,12 +144,12 @@ def test_one_and_ten_steps_box32(capi, oracle_lib):
     p = p.replace(dt=inputs.cfl_dt(p, s.RU))
     ctx = gpu_run(capi, p, s, 1)
     o = oracle_run(oracle_lib, p, s, 1)
-    assert_state_close(ctx, o, TOL1, check_rhs_t=False)
+    assert_state_close(ctx, o, TOL1, check_rhs_t=False, check_q=False)
     ctx.run(9)
     ctx.sync()
     for _ in range(9):
         o.step()
-    assert_state_close(ctx, o, TOL10, check_rhs_t=False)
+    assert_state_close(ctx, o, TOL10, check_rhs_t=False, check_q=False)
     # particle cell indices identical (truncation and round indexing)
     a, b = ctx.download_particles("base"), o.get_particles(0)
     for q, L, N in (("x", p.Lx, p.Nx), ("y", p.Ly, p.Ny), ("z", p.Lz, p.Nz)):
@@ -193,8 +199,10 @@ def test_no_particles(capi, oracle_lib):
 
 
 def test_boundary_and_clustered_particles(capi, oracle_lib):
-    """Particles on cell faces, at 0, next to L, and many in one cell."""
-    p, s = make_case(16, 64, seed=4)
+    """Particles on cell faces, at 0, next to L, and many in one cell.  (Mass
+    loading small enough that 40 coincident particles do not make the coupled
+    system blow up - with 0.5 it diverges in the oracle as well.)"""
+    p, s = make_case(16, 64, seed=4, mass_loading=2e-3)
     L, dx = p.Lx, p.dx
     x = np.concatenate([np.zeros(8), np.full(8, np.nextafter(L, 0)), np.arange(8) * dx,
                         np.full(40, 3.3 * dx)])
@@ -212,7 +220,7 @@ def test_boundary_and_clustered_particles(capi, oracle_lib):
 
 
 def test_single_particle(capi, oracle_lib):
-    p, s = make_case(12, 1, seed=6)
+    p, s = make_case(12, 1, seed=6, mass_loading=1e-4)
     ctx = gpu_run(capi, p, s, 3)
     o = oracle_run(oracle_lib, p, s, 3)
     assert_state_close(ctx, o, TOL1)
