@@ -188,6 +188,32 @@ int tpm_poisson_solve(tpm_ctx *ctx, const double *C3, double *P, const double *R
                       int max_iterations, double epsilon, int *iterations_out,
                       double *error_out);
 
+/*
+ * Poisson solve that allocates nothing.  This entry point has no counterpart
+ * in the reference.  It is for callers that cannot call cudaMalloc: plug-ins
+ * handed device buffers by a host application, code issuing work while a
+ * stream is being captured, or runtimes whose memory pool forbids side
+ * allocations.  It solves the same problem as tpm_poisson_solve (the
+ * reference's poisson::Solve with Solver==0) on DEVICE pointers: C3 (3 face
+ * blocks), P (initial guess in, solution out) and RHS, for an Nx*Ny*Nz box of
+ * size Lx*Ly*Lz, on `stream` (a cudaStream_t; NULL = legacy default stream).
+ * It needs no context and never calls cudaMalloc, cudaFree or any allocating
+ * routine: its scratch is one file-scope device array of
+ * TPM_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until
+ * process exit, which bounds the grid to roughly 100^3 cells; larger grids
+ * return TPM_ERR_ARG.  The first call on a device looks up the array's
+ * device address and sets kernel attributes, so make that first call before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU (other streams, other host threads) race and must be serialised by the
+ * caller.  It synchronises `stream` once per call (and once per iteration
+ * when epsilon > 0, to test the stopping rule).
+ */
+#define TPM_NOALLOC_SCRATCH_BYTES (16u << 20)
+int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, double Ly, double Lz,
+                              const double *C3, double *P, const double *RHS,
+                              int max_iterations, double epsilon, void *stream,
+                              int *iterations_out, double *error_out);
+
 /* Options (tpm_set_option). */
 enum {
   TPM_OPT_STORE_DIVERGENCE = 1 /* keep the divergence constraint field for download

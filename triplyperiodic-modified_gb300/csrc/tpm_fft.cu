@@ -501,3 +501,213 @@ int fft_x_blocks(const tpm_ctx *c) {
   return (int)((nrows + npen - 1) / npen);
 }
 }  // namespace tpm
+
+// ===========================================================================
+// Allocation-free Poisson solve (tpm_poisson_solve_noalloc, include/tpm.h).
+//
+// Some callers cannot allocate device memory at all: a plug-in that only
+// receives buffers from its host application, code running while a stream is
+// being captured into a CUDA graph (cudaMalloc is illegal there), or a
+// runtime with its own pool that forbids side allocations.  This entry point
+// runs the same kernels as tpm_poisson_solve, but every byte of scratch it
+// needs (spectrum, centre coefficients, partial maxima, twiddle and
+// wave-number tables, device scalars) lives in the fixed array below, which
+// each GPU that loads the library holds until the process exits.  The caller
+// passes device pointers for the inputs and the output only.
+// ===========================================================================
+namespace tpm {
+namespace {
+
+constexpr size_t kStaticScratchBytes = (size_t)TPM_NOALLOC_SCRATCH_BYTES;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kStaticScratchBytes];
+
+// device address of g_noalloc_scratch, looked up once per device
+void *g_noalloc_ptr[kMaxDevices] = {};
+
+// host staging for the small tables (fixed size: no host allocation either)
+double2 g_tab_host[4 * 2048 + 8];
+double g_mwn_host[2048 + 2048 + 2048 + 8];
+
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+__global__ void k_center_coeff_noalloc(Grid g, const double *__restrict__ Cf, double *__restrict__ cc) {
+  const double OneThird = 1. / 3.;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % g.nx);
+    const long long t = c / g.nx;
+    const int j = (int)(t % g.ny), k = (int)(t / g.ny);
+    const long long cxp = at(g, wrap_p(i, g.nx), j, k), cyp = at(g, i, wrap_p(j, g.ny), k),
+                    czp = at(g, i, j, wrap_p(k, g.nz));
+    double m = OneThird * ((Cf[c] + Cf[cxp]) * 0.5 + (Cf[g.n + c] + Cf[g.n + cyp]) * 0.5 +
+                           (Cf[2 * g.n + c] + Cf[2 * g.n + czp]) * 0.5);
+    cc[c] = -1. / m;
+  }
+}
+
+}  // namespace
+}  // namespace tpm
+
+extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, double Ly, double Lz,
+                                         const double *C3, double *P, const double *RHS,
+                                         int max_iterations, double epsilon, void *stream,
+                                         int *iterations_out, double *error_out) {
+  using namespace tpm;
+  auto ok = [](int n) {
+    if (n < 1) return false;
+    for (int f : {2, 3, 5})
+      while (n % f == 0) n /= f;
+    return n == 1;
+  };
+  if (!C3 || !P || !RHS || max_iterations < 0) return TPM_ERR_ARG;
+  if (!ok(Nx) || !ok(Ny) || !ok(Nz) || (Nx % 2) || Nx < 4 || Ny < 2 || Nz < 2 ||
+      Nx / 2 > 2048 || Ny > 2048 || Nz > 2048 || !(Lx > 0) || !(Ly > 0) || !(Lz > 0))
+    return TPM_ERR_ARG;
+  Grid g;
+  g.nx = Nx; g.ny = Ny; g.nz = Nz; g.nxh = Nx / 2 + 1;
+  g.n = (long long)Nx * Ny * Nz;
+  g.Lx = Lx; g.Ly = Ly; g.Lz = Lz;
+  g.dx = Lx / Nx; g.dy = Ly / Ny; g.dz = Lz / Nz;
+  g.inv_dx = 1. / g.dx; g.inv_dy = 1. / g.dy; g.inv_dz = 1. / g.dz;
+  g.inv_dx2 = 1. / (g.dx * g.dx); g.inv_dy2 = 1. / (g.dy * g.dy); g.inv_dz2 = 1. / (g.dz * g.dz);
+  g.idx = g.inv_dx; g.idy = g.inv_dy; g.idz = g.inv_dz;
+  g.xh = Nx * g.dx; g.yh = Ny * g.dy; g.zh = Nz * g.dz;
+  const long long nrows = (long long)Ny * Nz;
+  const int npx = pens_for(Nx / 2);
+  const int xblocks = (int)((nrows + npx - 1) / npx);
+  const int ntab = Nx / 2 + Ny + Nz + Nx;
+  // scratch layout
+  const size_t o_sc = 0;
+  const size_t o_spec = o_sc + align256(sizeof(DevScalars));
+  const size_t o_cc = o_spec + align256((size_t)g.nxh * Ny * Nz * sizeof(double2));
+  const size_t o_err = o_cc + align256((size_t)g.n * sizeof(double));
+  const size_t o_tab = o_err + align256((size_t)xblocks * sizeof(double));
+  const size_t o_mwn = o_tab + align256((size_t)ntab * sizeof(double2));
+  const size_t need = o_mwn + align256((size_t)(g.nxh + Ny + Nz) * sizeof(double));
+  if (need > kStaticScratchBytes) return TPM_ERR_ARG;  // grid too large for the fixed scratch
+
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return TPM_ERR_CUDA;
+  if (!g_noalloc_ptr[dev]) {
+    // once per device, with that device current: resolve the array's device
+    // address (the host-side name is only a stand-in) and allow the FFT
+    // kernels their dynamic shared memory
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return TPM_ERR_CUDA;
+    int smem64 = 2 * kFftSmemPoints * (int)sizeof(double2);
+    if (cudaFuncSetAttribute(k_xfwd_resid<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_y<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_z_solve<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64) != cudaSuccess ||
+        cudaFuncSetAttribute(k_xinv_update<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64) != cudaSuccess)
+      return TPM_ERR_CUDA;
+    g_noalloc_ptr[dev] = p;
+  }
+  unsigned char *base = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
+  DevScalars *dsc = reinterpret_cast<DevScalars *>(base + o_sc);
+  double2 *spec = reinterpret_cast<double2 *>(base + o_spec);
+  double *cc = reinterpret_cast<double *>(base + o_cc);
+  double *errp = reinterpret_cast<double *>(base + o_err);
+  double2 *tab = reinterpret_cast<double2 *>(base + o_tab);
+  double *mwn = reinterpret_cast<double *>(base + o_mwn);
+
+  // plans and tables (twiddles exp(-2 pi i m/n); wave numbers as in
+  // poisson.cpp:433-447)
+  FftPlan fx, fy, fz;
+  try {
+    factorize(Nx / 2, fx);
+    factorize(Ny, fy);
+    factorize(Nz, fz);
+  } catch (const std::string &) {
+    return TPM_ERR_ARG;
+  }
+  int off = 0;
+  auto put_tw = [&](int n) {
+    for (int m = 0; m < n; ++m) {
+      double a = 2.0 * 3.14159265358979323846 * (double)m / (double)n;
+      g_tab_host[off + m] = make_double2(cos(a), -sin(a));
+    }
+    int at0 = off;
+    off += n;
+    return at0;
+  };
+  fx.tw64 = tab + put_tw(Nx / 2);
+  fy.tw64 = tab + put_tw(Ny);
+  fz.tw64 = tab + put_tw(Nz);
+  const double2 *r2c = tab + put_tw(Nx);
+  fx.tw32 = fy.tw32 = fz.tw32 = nullptr;
+  auto put_mwn = [](int n, double L, double d, double *t, int count) {
+    double TWO_PI(2 * 3.141592653589793);
+    double two_pi_over_L = TWO_PI / L;
+    double d2 = 2. / (d * d);
+    for (int i = 0; i < count; ++i) {
+      double kk = ((i < n / 2) ? i : i - n) * two_pi_over_L;
+      t[i] = (d2) * (1 - cos(kk * d));
+    }
+  };
+  put_mwn(Nx, Lx, g.dx, g_mwn_host, g.nxh);
+  put_mwn(Ny, Ly, g.dy, g_mwn_host + g.nxh, Ny);
+  put_mwn(Nz, Lz, g.dz, g_mwn_host + g.nxh + Ny, Nz);
+  const double *ax = mwn, *ay = mwn + g.nxh, *az = mwn + g.nxh + Ny;
+  if (cudaMemcpyAsync(tab, g_tab_host, sizeof(double2) * ntab, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(mwn, g_mwn_host, sizeof(double) * (g.nxh + Ny + Nz), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemsetAsync(dsc, 0, sizeof(DevScalars), st) != cudaSuccess)  // mean_rhs = 0: RHS used as given
+    return TPM_ERR_CUDA;
+  // table copies come from static host staging: finish them before a later
+  // call may rewrite it
+  if (cudaStreamSynchronize(st) != cudaSuccess) return TPM_ERR_CUDA;
+
+  int cb = (int)((g.n + 255) / 256);
+  if (cb > kRedBlocks) cb = kRedBlocks;
+  k_center_coeff_noalloc<<<cb, 256, 0, st>>>(g, C3, cc);
+  int it = 0;
+  double error = 100, host_err = 0;
+  const bool need_err = epsilon > 0;
+  while ((it < max_iterations) && (error > epsilon)) {
+    {
+      size_t smem = 2 * (size_t)npx * fx.n * sizeof(double2);
+      k_xfwd_resid<double2><<<xblocks, kFftThreads, smem, st>>>(g, fx, r2c, P, C3, cc, RHS, dsc, spec, npx);
+    }
+    {
+      int npen = pens_for(fy.n);
+      int blocks = Nz * ((g.nxh + npen - 1) / npen);
+      size_t smem = 2 * (size_t)npen * fy.n * sizeof(double2);
+      k_fft_y<double2><<<blocks, kFftThreads, smem, st>>>(g, fy, spec, npen, -1);
+    }
+    {
+      int npen = pens_for(fz.n);
+      int blocks = Ny * ((g.nxh + npen - 1) / npen);
+      size_t smem = 2 * (size_t)npen * fz.n * sizeof(double2);
+      k_fft_z_solve<double2><<<blocks, kFftThreads, smem, st>>>(g, fz, spec, ax, ay, az, npen);
+    }
+    {
+      int npen = pens_for(fy.n);
+      int blocks = Nz * ((g.nxh + npen - 1) / npen);
+      size_t smem = 2 * (size_t)npen * fy.n * sizeof(double2);
+      k_fft_y<double2><<<blocks, kFftThreads, smem, st>>>(g, fy, spec, npen, +1);
+    }
+    {
+      size_t smem = 2 * (size_t)npx * fx.n * sizeof(double2);
+      k_xinv_update<double2><<<xblocks, kFftThreads, smem, st>>>(g, fx, r2c, spec, P, errp, npx);
+      k_finish_max<<<1, 256, 0, st>>>(errp, xblocks, dsc);
+    }
+    if (cudaGetLastError() != cudaSuccess) return TPM_ERR_CUDA;
+    it++;
+    if (need_err) {
+      if (cudaMemcpyAsync(&host_err, &dsc->err, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        return TPM_ERR_CUDA;
+      error = host_err;
+    }
+  }
+  if (!need_err || error_out) {
+    if (cudaMemcpyAsync(&host_err, &dsc->err, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return TPM_ERR_CUDA;
+  }
+  if (iterations_out) *iterations_out = it;
+  if (error_out) *error_out = host_err;
+  return TPM_OK;
+}
