@@ -35,6 +35,8 @@ FALLBACK_HBM_GBS = 6800.0
 
 # Algorithmic bytes per launch of each kernel: (bytes per cell, bytes per
 # particle) for FP64 storage; the derivation is tabulated in the design doc.
+# `value` is the headline (mixed-precision) path; the FP64 path is reported
+# beside it under "fp64".
 KERNEL_BYTES = {
     "rhs_momentum": (21 * 8, 0),
     "poisson_rhs": (11 * 8, 0),
@@ -61,11 +63,6 @@ def peaks():
             if k in d:
                 return float(d[k]), "measured"
     return FALLBACK_HBM_GBS, "fallback"
-
-
-def algorithmic_bytes_per_step(ncell, npart, n_it, w=8, wp=8):
-    """Per RK4 step: N^3 (4 (61 + 15 (n_it-1)) + 9) w + Np 4 (37 wp + 16)."""
-    return ncell * (4 * (61 + 15 * (n_it - 1)) + 9) * w + npart * 4 * (37 * wp + 16)
 
 
 class ClockSampler:
@@ -243,7 +240,47 @@ def cpu_baseline_port(workload):
                       f"reference"}
 
 
+def kernel_bytes(name, ncell, npart, mixed):
+    bc, bp = KERNEL_BYTES.get(name, (0, 0))
+    if mixed:  # complex64 spectrum on the mixed path
+        bc = {"fft_y": 8, "fft_z_solve": 8, "fft_x_fwd_resid": 6 * 8 + 4,
+              "fft_x_inv_update": 4 + 16}.get(name, bc)
+    return bc * ncell + bp * npart
+
+
+def step_bytes(ncell, npart, n_it, mixed):
+    """Per RK4 step, SURVEY's fixed count with the FFT traffic at the spectrum's
+    width: N^3 [4 ((50 + 4 (n_it-1)) w + 11 n_it w_fft) + 9 w] + Np 4 (37 w_p + 16);
+    w = w_p = 8 (FP64 state on both paths), w_fft = 8 (FP64) or 4 (mixed)."""
+    w, wf = 8, (4 if mixed else 8)
+    per_cell = 4 * ((50 + 4 * (n_it - 1)) * w + 11 * n_it * wf) + 9 * w
+    return ncell * per_cell + npart * 4 * (37 * 8 + 16)
+
+
+def path_result(p, s, ms, steps, world, n_it, launches, prof, clocks, mixed, peak):
+    ms_per_step = ms / steps
+    dom_name, (nl, tot_ms) = max(prof.items(), key=lambda kv: kv[1][1])
+    per_launch = kernel_bytes(dom_name, p.ncell, s.npart, mixed)
+    achieved = per_launch / (tot_ms / nl * 1e-3) / 1e9
+    sb = step_bytes(p.ncell, s.npart, n_it, mixed)
+    sgbs = sb / (ms_per_step * 1e-3) / 1e9
+    total_prof = sum(v[1] for v in prof.values())
+    return {
+        "value": world * p.ncell * steps / (ms * 1e-3) / 1e6,
+        "ms_per_step": ms_per_step, "n_it": n_it, "launches": launches, "clocks": clocks,
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": None, "kernel_share": round(tot_ms / total_prof, 4)},
+        "step_roofline": {"achieved_gbs": round(sgbs, 1), "frac": round(sgbs / peak, 4),
+                          "algorithmic_bytes_per_step": int(sb)},
+        "kernels_ms_per_step": {k: round(v[1] / 2, 3) for k, v in
+                                sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]},
+        "mparticle_steps_per_s": world * s.npart * steps / (ms * 1e-3) / 1e6,
+    }
+
+
 def gpu_main(args):
+    import numpy as np
     import torch
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -256,60 +293,79 @@ def gpu_main(args):
 
         td.init_process_group("nccl", device_id=torch.device("cuda", local))
         dist = td
-    prec = {"fp64": 0, "mixed": 1}[args.precision]
-    p, s = make_workload(args.workload, prec)
-    ctx, ms, n_it, launches, prof, clocks = time_gpu(p, s, args.steps, args.warmup, dist, local)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_per_step = ms / args.steps
-    value = world * p.ncell * args.steps / (ms * 1e-3) / 1e6
-    e2e_ms, h2d, d2h = time_e2e(ctx, max(1, min(args.steps, 3)))
+    from tpm import params as P
+
+    p64, s = make_workload(args.workload, 0)
+    peak, peak_kind = peaks()
+    paths = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
+    res, ctxs = {}, {}
+    for name in paths:
+        p = p64.replace(precision=P.PREC_MIXED if name == "mixed" else P.PREC_FP64)
+        ctx, ms, n_it, launches, prof, clocks = time_gpu(p, s, args.steps, args.warmup, dist,
+                                                         local)
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        res[name] = path_result(p, s, ms, args.steps, world, n_it, launches, prof, clocks,
+                                name == "mixed", peak)
+        ctxs[name] = ctx
+    head = "mixed" if "mixed" in res else "fp64"
+    accuracy = None
+    if "mixed" in ctxs and "fp64" in ctxs:
+        # both paths ran the same steps from the same state
+        a, b = ctxs["mixed"], ctxs["fp64"]
+        accuracy = {}
+        for g in ("RU", "RHO", "P", "C", "Q"):
+            x, y = a.download_field(g), b.download_field(g)
+            accuracy[g] = float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300))
+        pa, pb = a.download_particles("base"), b.download_particles("base")
+        accuracy["particles"] = max(float(np.abs(pa[q] - pb[q]).max() / max(np.abs(pb[q]).max(),
+                                                                           1e-300))
+                                    for q in ("x", "y", "z", "u", "v", "w", "T"))
+        accuracy = {"rel_err_vs_fp64_per_field": accuracy,
+                    "max_abs_div_after_projection": a.scalars()["max_abs_div"]}
+        ctxs["fp64"].close()
+    hctx = ctxs[head]
+    e2e_ms, h2d, d2h = time_e2e(hctx, max(1, min(args.steps, 3)))
     if dist:
         t = torch.tensor([e2e_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    e2e_value = world * p.ncell / (e2e_ms * 1e-3) / 1e6
-    peak, peak_kind = peaks()
-    # dominant kernel roofline
-    dom = max(prof.items(), key=lambda kv: kv[1][1])
-    name, (nl, tot_ms) = dom
-    bc, bp = KERNEL_BYTES.get(name, (0, 0))
-    per_launch = bc * p.ncell + bp * s.npart
-    avg_ms = tot_ms / nl
-    achieved = per_launch / (avg_ms * 1e-3) / 1e9
-    step_bytes = algorithmic_bytes_per_step(p.ncell, s.npart, n_it)
-    step_gbs = step_bytes / (ms_per_step * 1e-3) / 1e9
-    total_prof = sum(v[1] for v in prof.values())
+    e2e_value = world * p64.ncell / (e2e_ms * 1e-3) / 1e6
+    r = res[head]
     line = {
-        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
+        "metric": METRIC, "value": round(r["value"], 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(r["ms_per_step"], 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if prec == 0 else "mixed(f32 compute, f64 state)",
+        "dtype": "f64" if head == "fp64" else "mixed (f32 compute, f64 state and residuals)",
         "data": "synthetic (seeded solenoidal E(k)~k^4 exp(-2(k/4)^2) velocity, uniform particles)",
-        "config": {"workload": f"{args.workload}: {p.Nx}^3 cells, {s.npart} particles, heated, "
-                               f"two-way coupled, Poisson eps=1e-13 (mean {n_it:.2f} iterations)",
-                   "precision": args.precision, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (working set ~8 GB)"},
-        "roofline": {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1),
-                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": None, "peak_source": f"{peak_kind} HBM copy bandwidth",
-                     "kernel_share": round(tot_ms / total_prof, 4)},
-        "step_roofline": {"achieved_gbs": round(step_gbs, 1),
-                          "frac": round(step_gbs / peak, 4),
-                          "algorithmic_bytes_per_step": int(step_bytes)},
+        "config": {"workload": f"{args.workload}: {p64.Nx}^3 cells, {s.npart} particles, heated, "
+                               f"two-way coupled, Poisson eps=1e-13 (mean {r['n_it']:.2f} "
+                               f"iterations)",
+                   "precision": head, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (working set ~8 GB per path)"},
+        "roofline": dict(r["roofline"], peak_source=f"{peak_kind} HBM copy bandwidth"),
+        "step_roofline": r["step_roofline"],
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": int(launches),
-        "clocks": clocks,
-        "kernels_ms_per_step": {k: round(v[1] / 2, 3) for k, v in
-                                sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]},
-        "mparticle_steps_per_s": round(world * s.npart * args.steps / (ms * 1e-3) / 1e6, 3),
+        "gpu_launches": int(r["launches"]),
+        "clocks": r["clocks"],
+        "kernels_ms_per_step": r["kernels_ms_per_step"],
+        "mparticle_steps_per_s": round(r["mparticle_steps_per_s"], 3),
     }
+    if "fp64" in res and head != "fp64":
+        f = res["fp64"]
+        line["fp64"] = {"value": round(f["value"], 3), "ms_per_step": round(f["ms_per_step"], 3),
+                        "n_it": f["n_it"], "roofline": f["roofline"],
+                        "step_roofline": f["step_roofline"], "clocks": f["clocks"],
+                        "kernels_ms_per_step": f["kernels_ms_per_step"]}
+        line["mixed_vs_fp64_speedup"] = round(r["value"] / f["value"], 3)
+    if accuracy:
+        line["mixed_accuracy"] = accuracy
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(args.workload)
-    ctx.close()
+    hctx.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
@@ -371,7 +427,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

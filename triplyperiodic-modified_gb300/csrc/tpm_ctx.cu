@@ -166,9 +166,10 @@ void substep(tpm_ctx *c, int s) {
   tpm::particle_deposit_concentration(c);
   tpm::particle_heat(c);
   tpm::launch_rhs_momentum(c, s, nb);
-  tpm::launch_poisson_rhs(c, s, c->store_div);
+  tpm::launch_poisson_rhs(c, s, c->store_div || c->p.precision == TPM_PREC_MIXED);
   poisson_loop(c, c->Iteration, c->p.epsilon);
   tpm::launch_project(c, s);
+  if (c->p.precision == TPM_PREC_MIXED) tpm::launch_div_residual(c, s);
   swap_stage(c);
   c->np1_is_base = false;
 }

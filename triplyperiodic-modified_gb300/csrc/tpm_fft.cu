@@ -270,10 +270,16 @@ __global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const d
     const int q = idx % npen, kz = idx / npen;
     const int kx = kx0 + q;
     if (kx < g.nxh && (kx + ky + kz) > 0) {
-      const double mwn = ax[kx] + ay[ky] + az[kz];
       T2 v = r[kz * npen + q];
-      v.y = (T)((double)v.y / mwn);
-      v.x = (T)((double)v.x / mwn);
+      if (sizeof(T) == sizeof(double)) {
+        const double inv = 1.0 / (ax[kx] + ay[ky] + az[kz]);
+        v.y = (T)((double)v.y * inv);
+        v.x = (T)((double)v.x * inv);
+      } else {  // FP32 correction solve of the mixed path
+        const float inv = 1.0f / ((float)ax[kx] + (float)ay[ky] + (float)az[kz]);
+        v.y = (T)((float)v.y * inv);
+        v.x = (T)((float)v.x * inv);
+      }
       r[kz * npen + q] = v;
     }
   }
@@ -319,7 +325,7 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   }
   __syncthreads();
   T2 *z = smem_fft(a, b, npen, pl, +1);
-  const double tot = (double)(g.nx * g.ny * g.nz);
+  const double inv_tot = 1.0 / (double)(g.nx * g.ny * g.nz);
   double mx = 0;
   for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
     const int q = idx / g.nx, i = idx % g.nx;
@@ -327,7 +333,7 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
     if (row >= nrows) continue;
     const T *zz = reinterpret_cast<const T *>(&z[(i >> 1) * npen + q]);
     double x = (double)zz[i & 1];
-    double dp = (-1) * x / (tot);
+    double dp = -(x * inv_tot);  // poisson.cpp:460, (-1)*re/N^3
     const long long c = row * g.nx + i;
     P[c] += dp;
     double ad = fabs(dp);
@@ -447,49 +453,59 @@ void fft_plans_create(tpm_ctx *c) {
 
 // One Richardson iteration of poisson::FFT (poisson.cpp:397-409).  Inputs:
 // P, c->Cface, c->cc, c->RHS and dsc->mean_rhs.  Output: P updated and
-// dsc->err = max|dp|.
-void poisson_iteration(tpm_ctx *c) {
+// dsc->err = max|dp|.  The residual and the update are FP64 on both paths;
+// T2 is the type of the constant-coefficient FFT solve (double2 on the FP64
+// path; float2 on the mixed path, where each iteration is one step of
+// iterative refinement: FP64 residual, FP32 correction, FP64 update).
+template <typename T2>
+static void poisson_iteration_t(tpm_ctx *c) {
   const Grid &g = c->g;
-  using T2 = double2;
   const long long nrows = (long long)g.ny * g.nz;
-  // x pass forward
+  T2 *spec = reinterpret_cast<T2 *>(c->spec);
+  const T2 *r2c = sizeof(T2) == sizeof(double2) ? reinterpret_cast<const T2 *>(c->r2c64)
+                                                : reinterpret_cast<const T2 *>(c->r2c32);
   {
     int npen = pens_for(c->fx.n);
-    if (npen * c->fx.n < g.nx / 2) npen = 1;
     int blocks = (int)((nrows + npen - 1) / npen);
     size_t smem = 2 * (size_t)npen * c->fx.n * sizeof(T2);
     TPM_LAUNCH(c, "fft_x_fwd_resid", k_xfwd_resid<T2>, blocks, kFftThreads, smem, g, c->fx,
-               c->r2c64, c->P, c->Cface, c->cc, c->RHS, c->dsc, c->spec, npen);
+               r2c, c->P, c->Cface, c->cc, c->RHS, c->dsc, spec, npen);
   }
   {
     int npen = pens_for(c->fy.n);
     int blocks = g.nz * ((g.nxh + npen - 1) / npen);
     size_t smem = 2 * (size_t)npen * c->fy.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, kFftThreads, smem, g, c->fy, c->spec, npen, -1);
+    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, kFftThreads, smem, g, c->fy, spec, npen, -1);
   }
   {
     int npen = pens_for(c->fz.n);
     int blocks = g.ny * ((g.nxh + npen - 1) / npen);
     size_t smem = 2 * (size_t)npen * c->fz.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_z_solve", k_fft_z_solve<T2>, blocks, kFftThreads, smem, g, c->fz, c->spec,
+    TPM_LAUNCH(c, "fft_z_solve", k_fft_z_solve<T2>, blocks, kFftThreads, smem, g, c->fz, spec,
                c->ax, c->ay, c->az, npen);
   }
   {
     int npen = pens_for(c->fy.n);
     int blocks = g.nz * ((g.nxh + npen - 1) / npen);
     size_t smem = 2 * (size_t)npen * c->fy.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, kFftThreads, smem, g, c->fy, c->spec, npen, +1);
+    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, kFftThreads, smem, g, c->fy, spec, npen, +1);
   }
   {
     int npen = pens_for(c->fx.n);
     int blocks = (int)((nrows + npen - 1) / npen);
     size_t smem = 2 * (size_t)npen * c->fx.n * sizeof(T2);
     double *parts = c->err_parts;
-    int nparts = blocks;
     TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, blocks, kFftThreads, smem, g, c->fx,
-               c->r2c64, c->spec, c->P, parts, npen);
-    TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 256, 0, parts, nparts, c->dsc);
+               r2c, spec, c->P, parts, npen);
+    TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 256, 0, parts, blocks, c->dsc);
   }
+}
+
+void poisson_iteration(tpm_ctx *c) {
+  if (c->p.precision == TPM_PREC_MIXED)
+    poisson_iteration_t<float2>(c);
+  else
+    poisson_iteration_t<double2>(c);
 }
 
 }  // namespace tpm

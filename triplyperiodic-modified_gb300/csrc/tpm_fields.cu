@@ -121,13 +121,16 @@ __device__ __forceinline__ Nbr nbr_of(const Grid &g, const Cell &q) {
   return r;
 }
 
-// tensor0::Equal_Div_F2C of U at centre (i,j,k) (tensor0.cpp:249-256)
-__device__ __forceinline__ double divU_at(const Grid &g, const double *U, int i, int j, int k) {
+// tensor0::Equal_Div_F2C of U at centre (i,j,k) (tensor0.cpp:249-256),
+// evaluated in the compute type TC (double on the FP64 path, float on the
+// mixed path; the loads convert)
+template <typename TC>
+__device__ __forceinline__ TC divU_at(const Grid &g, const double *U, int i, int j, int k) {
   long long c = at(g, i, j, k);
   const double *Ux = U, *Uy = U + g.n, *Uz = U + 2 * g.n;
-  return (Ux[at(g, wrap_p(i, g.nx), j, k)] - Ux[c]) * g.inv_dx +
-         (Uy[at(g, i, wrap_p(j, g.ny), k)] - Uy[c]) * g.inv_dy +
-         (Uz[at(g, i, j, wrap_p(k, g.nz))] - Uz[c]) * g.inv_dz;
+  return ((TC)Ux[at(g, wrap_p(i, g.nx), j, k)] - (TC)Ux[c]) * (TC)g.inv_dx +
+         ((TC)Uy[at(g, i, wrap_p(j, g.ny), k)] - (TC)Uy[c]) * (TC)g.inv_dy +
+         ((TC)Uz[at(g, i, j, wrap_p(k, g.nz))] - (TC)Uz[c]) * (TC)g.inv_dz;
 }
 
 __device__ __forceinline__ long long shift(const Grid &g, int i, int j, int k, int dir, int s) {
@@ -137,67 +140,74 @@ __device__ __forceinline__ long long shift(const Grid &g, int i, int j, int k, i
 }
 
 // flux P_{d,e}(cell) = I_e,C2F(U_d) * I_d,C2F(RU_e)   (grid.cpp:785-800)
-__device__ __forceinline__ double flux_at(const Grid &g, const double *Ud, const double *RUe, int i,
-                                          int j, int k, int d, int e) {
+template <typename TC>
+__device__ __forceinline__ TC flux_at(const Grid &g, const double *Ud, const double *RUe, int i,
+                                      int j, int k, int d, int e) {
   long long c = at(g, i, j, k);
-  double iu = (Ud[c] + Ud[shift(g, i, j, k, e, -1)]) * 0.5;
-  double ir = (RUe[c] + RUe[shift(g, i, j, k, d, -1)]) * 0.5;
+  TC iu = ((TC)Ud[c] + (TC)Ud[shift(g, i, j, k, e, -1)]) * (TC)0.5;
+  TC ir = ((TC)RUe[c] + (TC)RUe[shift(g, i, j, k, d, -1)]) * (TC)0.5;
   return iu * ir;
 }
 
+// grid::Update_RU_WOP (grid.cpp:776-814).  The right-hand side is evaluated
+// in TC; the RK combinations RU_np1 += dt*post*RHS, RU_new = RU + dt*pre*RHS
+// are always FP64.  With TC = double every operation is the reference's.
+template <typename TC>
 __global__ void k_rhs_momentum(Grid g, const double *__restrict__ U, const double *__restrict__ RUi,
                                const double *__restrict__ Fp, const double *__restrict__ Rho_int,
                                const double *__restrict__ RU, const double *__restrict__ np1_in,
                                double *__restrict__ RU_np1, double *__restrict__ RU_new, RhsArgs a) {
-  const double inv_d[3] = {g.inv_dx, g.inv_dy, g.inv_dz};
-  const double inv_d2[3] = {g.inv_dx2, g.inv_dy2, g.inv_dz2};
+  const TC inv_d[3] = {(TC)g.inv_dx, (TC)g.inv_dy, (TC)g.inv_dz};
+  const TC inv_d2[3] = {(TC)g.inv_dx2, (TC)g.inv_dy2, (TC)g.inv_dz2};
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
     Nbr nb = nbr_of(g, q);
-    const double div_c = divU_at(g, U, q.i, q.j, q.k);
-    const double div_m[3] = {divU_at(g, U, wrap_m(q.i, g.nx), q.j, q.k),
-                             divU_at(g, U, q.i, wrap_m(q.j, g.ny), q.k),
-                             divU_at(g, U, q.i, q.j, wrap_m(q.k, g.nz))};
+    const TC div_c = divU_at<TC>(g, U, q.i, q.j, q.k);
+    const TC div_m[3] = {divU_at<TC>(g, U, wrap_m(q.i, g.nx), q.j, q.k),
+                         divU_at<TC>(g, U, q.i, wrap_m(q.j, g.ny), q.k),
+                         divU_at<TC>(g, U, q.i, q.j, wrap_m(q.k, g.nz))};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const double *Ud = U + d * g.n;
       // dummy2 = grad_C2F(div U) (tensor1.cpp:259-270)
-      double gd = (div_c - div_m[d]) * inv_d[d];
+      TC gd = (div_c - div_m[d]) * inv_d[d];
       // dummy = Del2(U_d) (tensor0.cpp:258-265)
-      double ud = Ud[c];
-      double lap = (Ud[nb.p[0]] - 2 * ud + Ud[nb.m[0]]) * inv_d2[0] +
-                   (Ud[nb.p[1]] - 2 * ud + Ud[nb.m[1]]) * inv_d2[1] +
-                   (Ud[nb.p[2]] - 2 * ud + Ud[nb.m[2]]) * inv_d2[2];
+      TC ud = (TC)Ud[c];
+      TC lap = ((TC)Ud[nb.p[0]] - 2 * ud + (TC)Ud[nb.m[0]]) * inv_d2[0] +
+               ((TC)Ud[nb.p[1]] - 2 * ud + (TC)Ud[nb.m[1]]) * inv_d2[1] +
+               ((TC)Ud[nb.p[2]] - 2 * ud + (TC)Ud[nb.m[2]]) * inv_d2[2];
       // RHS = -mp/Vcell*F_p + mu/3 grad(div U) + mu Del2 U  (grid.cpp:783)
-      double rhs = a.a_fp * Fp[d * g.n + c] + a.b_gd * gd + a.c_lap * lap;
+      TC rhs = (TC)a.a_fp * (TC)Fp[d * g.n + c] + (TC)a.b_gd * gd + (TC)a.c_lap * lap;
       // convection: Div_F2C(I_C2F(U_d) * I_d,C2F(RU_int))  (grid.cpp:785-801)
-      double conv = 0;
+      TC conv = 0;
       {
-        double t[3];
+        TC t[3];
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
           const double *RUe = RUi + e * g.n;
           int ip = e == 0 ? wrap_p(q.i, g.nx) : q.i;
           int jp = e == 1 ? wrap_p(q.j, g.ny) : q.j;
           int kp = e == 2 ? wrap_p(q.k, g.nz) : q.k;
-          t[e] = (flux_at(g, Ud, RUe, ip, jp, kp, d, e) - flux_at(g, Ud, RUe, q.i, q.j, q.k, d, e)) *
-                 inv_d[e];
+          t[e] = (flux_at<TC>(g, Ud, RUe, ip, jp, kp, d, e) -
+                  flux_at<TC>(g, Ud, RUe, q.i, q.j, q.k, d, e)) * inv_d[e];
         }
         conv = t[0] + t[1] + t[2];
       }
       rhs -= conv;
       // artificial (linear) forcing A*RU_int (grid.cpp:803)
-      rhs += a.A * RUi[d * g.n + c];
+      rhs += (TC)a.A * (TC)RUi[d * g.n + c];
       // body force (Rho_face - Rho0)*g (grid.cpp:805-809)
       if (a.has_g) {
-        double rf = (Rho_int[c] + Rho_int[d == 0 ? nb.m[0] : d == 1 ? nb.m[1] : nb.m[2]]) * 0.5;
-        rhs += (rf - a.Rho0) * a.g[d];
+        TC rf = ((TC)Rho_int[c] + (TC)Rho_int[d == 0 ? nb.m[0] : d == 1 ? nb.m[1] : nb.m[2]]) *
+                (TC)0.5;
+        rhs += (rf - (TC)a.Rho0) * (TC)a.g[d];
       }
       // RU_np1 += dt*post*RHS ; RU_new = RU + dt*pre*RHS  (grid.cpp:811-813)
-      double np1 = np1_in[d * g.n + c] + a.dtpo * rhs;
+      const double r64 = (double)rhs;
+      double np1 = np1_in[d * g.n + c] + a.dtpo * r64;
       RU_np1[d * g.n + c] = np1;
-      RU_new[d * g.n + c] = (a.stage != 3) ? 1 * RU[d * g.n + c] + a.dtpr * rhs : np1;
+      RU_new[d * g.n + c] = (a.stage != 3) ? 1 * RU[d * g.n + c] + a.dtpr * r64 : np1;
     }
   }
 }
@@ -325,6 +335,42 @@ __global__ void k_finish_means3(const double *__restrict__ partials, int nparts,
   }
 }
 
+// FP64 post-projection divergence residual of the mixed path:
+// res = div_F2C(RU_new * C) - divergence - dt*pre*mean(RHS_Pois), with
+// C = 1/Rho_face(Rho_new) from k_poisson_rhs.  A converged projection gives
+// res = 0 (grid.cpp:841-863): div u_new = divergence + dt*pre*mean.
+__global__ void k_div_residual(Grid g, const double *__restrict__ RUn, const double *__restrict__ Cf,
+                               const double *__restrict__ divg, const DevScalars *__restrict__ s,
+                               double dtpre, double *__restrict__ partials) {
+  __shared__ double sh[kThreads];
+  const double off = dtpre * s->mean_rhs;
+  const double inv_d[3] = {g.inv_dx, g.inv_dy, g.inv_dz};
+  double mx = 0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    Nbr nb = nbr_of(g, q);
+    double dv = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double *R = RUn + d * g.n, *C = Cf + d * g.n;
+      dv += (R[nb.p[d]] * C[nb.p[d]] - R[c] * C[c]) * inv_d[d];
+    }
+    double r = fabs(dv - divg[c] - off);
+    mx = r > mx ? r : mx;
+  }
+  double b = block_max(mx, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = b;
+}
+
+__global__ void k_finish_max_div(const double *__restrict__ partials, int nparts, DevScalars *s) {
+  __shared__ double sh[kThreads];
+  double v = 0;
+  for (int b = threadIdx.x; b < nparts; b += blockDim.x) v = partials[b] > v ? partials[b] : v;
+  double m = block_max(v, sh);
+  if (threadIdx.x == 0) s->max_div = m;
+}
+
 // tensor0::make_mean_U0 per component (tensor0.cpp:389-394) and
 // grid::TimeAdvance RU = RU_np1 (grid.cpp:599): the result goes to RU.
 __global__ void k_mean_reset(Grid g, const double *__restrict__ RU_np1, double *__restrict__ RU,
@@ -399,9 +445,14 @@ void launch_rhs_momentum(tpm_ctx *c, int s, bool np1_in_base) {
   a.dtpo = c->p.dt * kPost[s];
   a.dtpr = c->p.dt * kPre[s];
   a.stage = s;
-  TPM_LAUNCH(c, "rhs_momentum", k_rhs_momentum, cell_blocks(c->g), kThreads, 0, c->g, c->U,
-             c->RU_int, c->Fp, c->Rho_int, c->RU, np1_in_base ? c->RU : c->RU_np1, c->RU_np1,
-             c->RU_new, a);
+  if (c->p.precision == TPM_PREC_MIXED)
+    TPM_LAUNCH(c, "rhs_momentum", k_rhs_momentum<float>, cell_blocks(c->g), kThreads, 0, c->g,
+               c->U, c->RU_int, c->Fp, c->Rho_int, c->RU, np1_in_base ? c->RU : c->RU_np1,
+               c->RU_np1, c->RU_new, a);
+  else
+    TPM_LAUNCH(c, "rhs_momentum", k_rhs_momentum<double>, cell_blocks(c->g), kThreads, 0, c->g,
+               c->U, c->RU_int, c->Fp, c->Rho_int, c->RU, np1_in_base ? c->RU : c->RU_np1,
+               c->RU_np1, c->RU_new, a);
 }
 
 void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
@@ -427,6 +478,14 @@ void launch_project(tpm_ctx *c, int s) {
     TPM_LAUNCH(c, "finish_means3", k_finish_means3, 1, kThreads, 0,
                c->partials + kPartRu * kRedBlocks, nb, c->g.n,
                c->dsc);
+}
+
+void launch_div_residual(tpm_ctx *c, int s) {
+  int nb = cell_blocks(c->g);
+  TPM_LAUNCH(c, "div_residual", k_div_residual, nb, kThreads, 0, c->g, c->RU_new, c->Cface,
+             c->divg, c->dsc, c->p.dt * kPre[s], c->partials + kPartDiv * kRedBlocks);
+  TPM_LAUNCH(c, "finish_max_div", k_finish_max_div, 1, kThreads, 0,
+             c->partials + kPartDiv * kRedBlocks, nb, c->dsc);
 }
 
 void launch_mean_reset(tpm_ctx *c) {

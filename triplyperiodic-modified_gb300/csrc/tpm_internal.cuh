@@ -152,6 +152,7 @@ void launch_face_velocity(tpm_ctx *c);
 void launch_rhs_momentum(tpm_ctx *c, int stage, bool np1_in_base);
 void launch_poisson_rhs(tpm_ctx *c, int stage, bool store_div);
 void launch_project(tpm_ctx *c, int stage);
+void launch_div_residual(tpm_ctx *c, int stage);
 void launch_mean_reset(tpm_ctx *c);
 void launch_init_fields(tpm_ctx *c);
 int cell_blocks(const Grid &g);
