@@ -316,6 +316,7 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->pay_r = dalloc<double>(c, 4 * (size_t)np);
     c->pay_r_s[0] = dalloc<double>(c, 4 * (size_t)np);
     c->pay_r_s[1] = dalloc<double>(c, 4 * (size_t)np);
+    c->w8 = dalloc<double>(c, 8 * (size_t)np);
     TPM_CUDA_TRY(cudaMemsetAsync(c->starts_r[0], 0, sizeof(int32_t) * (n + 1), c->stream));
     TPM_CUDA_TRY(cudaMemsetAsync(c->starts_r[1], 0, sizeof(int32_t) * (n + 1), c->stream));
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));

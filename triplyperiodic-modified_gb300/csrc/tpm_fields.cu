@@ -281,6 +281,105 @@ __global__ void k_poisson_rhs(Grid g, const double *__restrict__ Rho_new,
   if (threadIdx.x == 0) partials[blockIdx.x] = bs;
 }
 
+// ------------------------------------------------ mixed-path variants
+// 1/x to FP64 accuracy from an FP32 seed and two Newton steps (4 FMAs): on
+// GB300 an FP64 division costs several times that on the scarce FP64 pipe.
+__device__ __forceinline__ double rcp64(double x) {
+  double r = (double)__frcp_rn((float)x);
+  double e = __fma_rn(-x, r, 1.0);
+  r = __fma_rn(r, e, r);
+  e = __fma_rn(-x, r, 1.0);
+  return __fma_rn(r, e, r);
+}
+
+// k_rho_update of the mixed path: same FP64 density update, reciprocals
+// instead of divisions
+__global__ void k_rho_update_mixed(Grid g, const double *__restrict__ RUi,
+                                   const double *__restrict__ Rho, const double *__restrict__ np1_in,
+                                   double *__restrict__ Rho_np1, double *__restrict__ Rho_new,
+                                   double *__restrict__ inv_rho, double *__restrict__ Tgas,
+                                   const DevScalars *__restrict__ s, double a_np1, double b_new,
+                                   int stage) {
+  const double *RUx = RUi, *RUy = RUi + g.n, *RUz = RUi + 2 * g.n;
+  const double T_scale = s->T_scale;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    double D = (RUx[at(g, wrap_p(q.i, g.nx), q.j, q.k)] - RUx[c]) * g.inv_dx +
+               (RUy[at(g, q.i, wrap_p(q.j, g.ny), q.k)] - RUy[c]) * g.inv_dy +
+               (RUz[at(g, q.i, q.j, wrap_p(q.k, g.nz))] - RUz[c]) * g.inv_dz;
+    double np1 = np1_in[c] + a_np1 * D;
+    double nw = (stage != 3) ? Rho[c] + b_new * D : np1;
+    Rho_np1[c] = np1;
+    Rho_new[c] = nw;
+    double ir = rcp64(nw);
+    inv_rho[c] = ir;
+    Tgas[c] = T_scale * ir;
+  }
+}
+
+// k_poisson_rhs of the mixed path: FP64 throughout (the right-hand side
+// feeds the FP64 residual of the refinement), reciprocals for the 1/Rho_face
+// coefficients and U = RU*C instead of RU/Rho_face.
+__global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ Rho_new,
+                                    const double *__restrict__ inv_rho, const double *__restrict__ Q,
+                                    const double *__restrict__ RUn, const DevScalars *__restrict__ s,
+                                    double *__restrict__ RHS, double *__restrict__ divg,
+                                    double *__restrict__ Cface, double *__restrict__ cc,
+                                    double *__restrict__ partials, PoisArgs a) {
+  __shared__ double sh[kThreads];
+  const double coef = s->coef_div, meanQ = s->mean_Q;
+  const double OneThird = 1. / 3.;
+  double acc = 0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    Nbr nb = nbr_of(g, q);
+    double ir = inv_rho[c];
+    double lap = (inv_rho[nb.p[0]] - 2 * ir + inv_rho[nb.m[0]]) * g.inv_dx2 +
+                 (inv_rho[nb.p[1]] - 2 * ir + inv_rho[nb.m[1]]) * g.inv_dy2 +
+                 (inv_rho[nb.p[2]] - 2 * ir + inv_rho[nb.m[2]]) * g.inv_dz2;
+    double Qc = a.cooling ? Q[c] - meanQ : Q[c];
+    double dv = a.kCp * lap + coef * Qc;
+    divg[c] = dv;
+    double r = Rho_new[c];
+    double t[3], c_lo[3], c_hi[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      c_lo[d] = rcp64((r + Rho_new[nb.m[d]]) * 0.5);
+      c_hi[d] = rcp64((Rho_new[nb.p[d]] + r) * 0.5);
+      const double *R = RUn + d * g.n;
+      t[d] = (R[nb.p[d]] * c_hi[d] - R[c] * c_lo[d]) *
+             (d == 0 ? g.inv_dx : d == 1 ? g.inv_dy : g.inv_dz);
+      Cface[d * g.n + c] = c_lo[d];
+    }
+    double rhs = (t[0] + t[1] + t[2] - dv) * a.inv_dtpre;
+    RHS[c] = rhs;
+    acc += rhs;
+    double m = OneThird * ((c_lo[0] + c_hi[0]) * 0.5 + (c_lo[1] + c_hi[1]) * 0.5 +
+                           (c_lo[2] + c_hi[2]) * 0.5);
+    cc[c] = -rcp64(m);
+  }
+  double bs = block_sum(acc, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = bs;
+}
+
+// face velocity of the mixed path: only the FP32 stencil and the particle
+// gather read it, so it is formed in FP32
+__global__ void k_face_velocity_mixed(Grid g, const double *__restrict__ RUi,
+                                      const double *__restrict__ Rho_int, double *__restrict__ U) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    float r = (float)Rho_int[c];
+    U[c] = (double)((float)RUi[c] / ((r + (float)Rho_int[at(g, wrap_m(q.i, g.nx), q.j, q.k)]) * 0.5f));
+    U[g.n + c] = (double)((float)RUi[g.n + c] /
+                          ((r + (float)Rho_int[at(g, q.i, wrap_m(q.j, g.ny), q.k)]) * 0.5f));
+    U[2 * g.n + c] = (double)((float)RUi[2 * g.n + c] /
+                              ((r + (float)Rho_int[at(g, q.i, q.j, wrap_m(q.k, g.nz))]) * 0.5f));
+  }
+}
+
 // mean of a field from per-block partial sums, stored at *out
 __global__ void k_finish_mean(const double *__restrict__ partials, int nparts, long long ntot,
                               double *out) {
@@ -421,12 +520,23 @@ void launch_p0_update(tpm_ctx *c, int s) {
 }
 
 void launch_rho_update(tpm_ctx *c, int s, bool np1_in_base) {
+  if (c->p.precision == TPM_PREC_MIXED) {
+    TPM_LAUNCH(c, "rho_update", k_rho_update_mixed, cell_blocks(c->g), kThreads, 0, c->g,
+               c->RU_int, c->Rho, np1_in_base ? c->Rho : c->Rho_np1, c->Rho_np1, c->Rho_new,
+               c->inv_rho, c->Tgas, c->dsc, -(c->p.dt * kPost[s]), -c->p.dt * kPre[s], s);
+    return;
+  }
   TPM_LAUNCH(c, "rho_update", k_rho_update, cell_blocks(c->g), kThreads, 0, c->g, c->RU_int,
              c->Rho, np1_in_base ? c->Rho : c->Rho_np1, c->Rho_np1, c->Rho_new, c->inv_rho,
              c->Tgas, c->dsc, -(c->p.dt * kPost[s]), -c->p.dt * kPre[s], s);
 }
 
 void launch_face_velocity(tpm_ctx *c) {
+  if (c->p.precision == TPM_PREC_MIXED) {
+    TPM_LAUNCH(c, "face_velocity", k_face_velocity_mixed, cell_blocks(c->g), kThreads, 0, c->g,
+               c->RU_int, c->Rho_int, c->U);
+    return;
+  }
   TPM_LAUNCH(c, "face_velocity", k_face_velocity, cell_blocks(c->g), kThreads, 0, c->g,
              c->RU_int, c->Rho_int, c->U);
 }
@@ -462,6 +572,11 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
   a.cooling = c->p.cooling;
   a.store_div = store_div;
   int nb = cell_blocks(c->g);
+  if (c->p.precision == TPM_PREC_MIXED)
+    TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_mixed, nb, kThreads, 0, c->g, c->Rho_new,
+               c->inv_rho, c->Q, c->RU_new, c->dsc, c->RHS, c->divg, c->Cface, c->cc,
+               c->partials + kPartRhs * kRedBlocks, a);
+  else
   TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs, nb, kThreads, 0, c->g, c->Rho_new, c->inv_rho,
              c->Q, c->RU_new, c->dsc, c->RHS, c->divg, c->Cface, c->cc,
              c->partials + kPartRhs * kRedBlocks, a);

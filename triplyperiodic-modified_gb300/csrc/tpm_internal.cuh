@@ -128,6 +128,7 @@ struct tpm_ctx {
   int32_t *scan_blocks = nullptr;
   double *pay_t = nullptr, *pay_t_s = nullptr;          // 6*np
   double *pay_r = nullptr, *pay_r_s[2] = {nullptr, nullptr};  // 4*np
+  double *w8 = nullptr;  // 8*np corner weights (sorted order)
   int rcur = 0;  // which r-sorted buffer holds the latest x_new sort
   int q_parts = 1;  // number of valid partial sums of Q (heat deposit blocks)
 

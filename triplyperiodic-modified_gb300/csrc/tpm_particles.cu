@@ -354,14 +354,41 @@ __global__ void k_dep_momentum(Grid g, const int32_t *__restrict__ starts,
   }
 }
 
-// part2gas_concentration (particle.cpp:522-555) and part2gas_Temp_*
-// (:582-654): centre c collects from the particles whose round-indexed cell
-// is c + (dx,dy,dz), dx,dy,dz in {0,1}, with weight (fx*fy)*fz, fx = xl if
-// dx == 0 else (1-xl).  with_rhs multiplies by the particle heat rate and
-// reduces the block sums of the result (mean for grid::Update_P0).
-__global__ void k_dep_cic(Grid g, const int32_t *__restrict__ starts, const double *__restrict__ pay,
-                          int64_t np, int with_rhs, double *__restrict__ out,
-                          double *__restrict__ partials) {
+// part2gas_concentration (particle.cpp:522-555) and part2gas_Temp_* (:582-654).
+// Corner weights of the round-indexed linear stencil, once per particle in
+// sorted order (every lane busy): w[d][s] for d = (dz*2+dy)*2+dx is the
+// contribution of sorted particle s to the centre (its round cell) - (dx,dy,dz),
+// ((fx*fy)*fz)*rhs with fx = xl for dx = 0 and 1-xl for dx = 1 - the operation
+// order of particle.cpp:545-552 / :605-612 / :643-650.  TW is the weight type
+// (double on the FP64 path, float on the mixed path).
+template <typename TW>
+__global__ void k_cic_weights(int64_t np, const double *__restrict__ pay, int with_rhs,
+                              TW *__restrict__ w) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < np;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    const TW xl = (TW)pay[s], yl = (TW)pay[np + s], zl = (TW)pay[2 * np + s];
+    const TW fx[2] = {xl, 1 - xl}, fy[2] = {yl, 1 - yl}, fz[2] = {zl, 1 - zl};
+    const TW r = with_rhs ? (TW)pay[3 * np + s] : (TW)1;
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 2; ++dx) {
+        const TW fxy = fx[dx] * fy[dy];
+#pragma unroll
+        for (int dz = 0; dz < 2; ++dz) {
+          TW v = fxy * fz[dz];
+          if (with_rhs) v = v * r;
+          w[(size_t)((dz * 2 + dy) * 2 + dx) * np + s] = v;
+        }
+      }
+  }
+}
+
+// centre c sums, in a fixed order, the corner weights of the particles whose
+// round cell is c + (dx,dy,dz) (cumulative ghost fold included)
+template <typename TW>
+__global__ void k_dep_sum8(Grid g, const int32_t *__restrict__ starts, const TW *__restrict__ w,
+                           int64_t np, double *__restrict__ out, double *__restrict__ partials) {
   __shared__ double sh[32];
   double bsum = 0;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
@@ -369,7 +396,7 @@ __global__ void k_dep_cic(Grid g, const int32_t *__restrict__ starts, const doub
     const int i = (int)(c % g.nx);
     const long long t = c / g.nx;
     const int j = (int)(t % g.ny), k = (int)(t / g.ny);
-    double acc = 0;
+    TW acc = 0;
 #pragma unroll
     for (int dz = 0; dz < 2; ++dz)
 #pragma unroll
@@ -378,21 +405,14 @@ __global__ void k_dep_cic(Grid g, const int32_t *__restrict__ starts, const doub
         for (int dx = 0; dx < 2; ++dx) {
           const long long r = at(g, dx ? wrap_p(i, g.nx) : i, dy ? wrap_p(j, g.ny) : j,
                                  dz ? wrap_p(k, g.nz) : k);
+          const TW *wd = w + (size_t)((dz * 2 + dy) * 2 + dx) * np;
           const int32_t s0 = starts[r], e0 = starts[r + 1];
-          for (int32_t s = s0; s < e0; ++s) {
-            const double xl = pay[s], yl = pay[np + s], zl = pay[2 * np + s];
-            const double fx = dx ? (1 - xl) : xl;
-            const double fy = dy ? (1 - yl) : yl;
-            const double fz = dz ? (1 - zl) : zl;
-            double w = fx * fy * fz;
-            if (with_rhs) w = w * pay[3 * np + s];
-            acc += w;
-          }
+          for (int32_t s = s0; s < e0; ++s) acc += wd[s];
         }
-    out[c] = acc;
-    bsum += acc;
+    out[c] = (double)acc;
+    bsum += (double)acc;
   }
-  if (with_rhs) {
+  if (partials) {
     double b = block_sum(bsum, sh);
     if (threadIdx.x == 0) partials[blockIdx.x] = b;
   }
@@ -472,6 +492,9 @@ void particle_deposit_momentum(tpm_ctx *c) {
              c->starts_t, c->pay_t_s, c->np, c->Fp);
 }
 
+static void cic_deposit(tpm_ctx *c, int buf, bool with_rhs, double *out, double *partials,
+                        const char *tag);
+
 // concentration at x_int (grid.cpp:876) from the round-indexed sort of the
 // previous x_new (= this x_int)
 void particle_deposit_concentration(tpm_ctx *c) {
@@ -479,8 +502,27 @@ void particle_deposit_concentration(tpm_ctx *c) {
     TPM_CUDA_TRY(cudaMemsetAsync(c->C, 0, sizeof(double) * c->g.n, c->stream));
     return;
   }
-  TPM_LAUNCH(c, "deposit_conc", k_dep_cic, cell_blocks(c->g), kThreads, 0, c->g,
-             c->starts_r[c->rcur], c->pay_r_s[c->rcur], c->np, 0, c->C, (double *)nullptr);
+  cic_deposit(c, c->rcur, false, c->C, nullptr, "conc");
+}
+
+// linear-stencil deposit from the sorted payload of r-sort buffer `buf`
+static void cic_deposit(tpm_ctx *c, int buf, bool with_rhs, double *out, double *partials,
+                        const char *tag) {
+  const bool mixed = c->p.precision == TPM_PREC_MIXED;
+  const int nb = cell_blocks(c->g);
+  if (mixed) {
+    float *w = reinterpret_cast<float *>(c->w8);
+    TPM_LAUNCH(c, with_rhs ? "weights_heat" : "weights_conc", k_cic_weights<float>,
+               pblocks(c->np), kThreads, 0, c->np, c->pay_r_s[buf], (int)with_rhs, w);
+    TPM_LAUNCH(c, with_rhs ? "deposit_heat" : "deposit_conc", k_dep_sum8<float>, nb, kThreads, 0,
+               c->g, c->starts_r[buf], w, c->np, out, partials);
+  } else {
+    TPM_LAUNCH(c, with_rhs ? "weights_heat" : "weights_conc", k_cic_weights<double>,
+               pblocks(c->np), kThreads, 0, c->np, c->pay_r_s[buf], (int)with_rhs, c->w8);
+    TPM_LAUNCH(c, with_rhs ? "deposit_heat" : "deposit_conc", k_dep_sum8<double>, nb, kThreads, 0,
+               c->g, c->starts_r[buf], c->w8, c->np, out, partials);
+  }
+  (void)tag;
 }
 
 static void heat_deposit_from(tpm_ctx *c, int buf) {
@@ -488,8 +530,7 @@ static void heat_deposit_from(tpm_ctx *c, int buf) {
   sort_by_cell(c, c->key_r, c->perm_r[buf], c->starts_r[buf]);
   TPM_LAUNCH(c, "payload_gather_r", k_gather_payload, pblocks(c->np), kThreads, 0, c->np, 4,
              c->perm_r[buf], c->pay_r, c->pay_r_s[buf]);
-  TPM_LAUNCH(c, "deposit_heat", k_dep_cic, nb, kThreads, 0, c->g, c->starts_r[buf],
-             c->pay_r_s[buf], c->np, 1, c->Q, c->partials + kPartQ * kRedBlocks);
+  cic_deposit(c, buf, true, c->Q, c->partials + kPartQ * kRedBlocks, "heat");
   c->q_parts = nb;
 }
 
