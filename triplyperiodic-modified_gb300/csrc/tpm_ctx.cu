@@ -150,13 +150,22 @@ void poisson_loop(tpm_ctx *c, int max_it, double eps) {
 void swap_stage(tpm_ctx *c) {
   // grid::TimeAdvance_RK4 (grid.cpp:890-900): int = new
   std::swap(c->RU_int, c->RU_new);
+  std::swap(c->RUi32, c->RUn32);
   std::swap(c->Rho_int, c->Rho_new);
   for (int q = 0; q < 7; ++q) std::swap(c->pq[1][q], c->pq[2][q]);
   TPM_CUDA_TRY(cudaMemcpyAsync(&c->dsc->P0_int, &c->dsc->P0_new, sizeof(double),
                                cudaMemcpyDeviceToDevice, c->stream));
 }
 
+// FP32 copy of RU_int for the mixed path's stencils
+void refresh_rui32(tpm_ctx *c) {
+  if (c->p.precision != TPM_PREC_MIXED || !c->rui32_stale) return;
+  tpm::launch_to_float(c, c->RU_int, c->RUi32, 3 * c->g.n);
+  c->rui32_stale = false;
+}
+
 void substep(tpm_ctx *c, int s) {
+  refresh_rui32(c);
   const bool nb = c->np1_is_base;
   tpm::launch_p0_update(c, s);
   tpm::launch_rho_update(c, s, nb);
@@ -274,6 +283,14 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->inv_rho = dalloc<double>(c, n); c->Tgas = dalloc<double>(c, n);
     c->Cface = dalloc<double>(c, 3 * n); c->cc = dalloc<double>(c, n);
     c->spec = dalloc<double2>(c, (size_t)g.nxh * g.ny * g.nz);
+    if (p->precision == TPM_PREC_MIXED) {
+      c->U32 = dalloc<float>(c, 3 * n);
+      c->RUi32 = dalloc<float>(c, 3 * n);
+      c->RUn32 = dalloc<float>(c, 3 * n);
+      c->Fp32 = dalloc<float>(c, 3 * n);
+      for (float *f : {c->U32, c->RUi32, c->RUn32, c->Fp32})
+        TPM_CUDA_TRY(cudaMemsetAsync(f, 0, sizeof(float) * 3 * n, c->stream));
+    }
     c->partials = dalloc<double>(c, (size_t)tpm::kPartRegions * tpm::kRedBlocks);
     c->dsc = dalloc<tpm::DevScalars>(c, 1);
     TPM_CUDA_TRY(cudaMallocHost(&c->hsc, sizeof(tpm::DevScalars)));
@@ -359,6 +376,7 @@ int tpm_upload_field(tpm_ctx *c, int field, const double *host) {
     long long len;
     double *d = field_ptr(c, field, &len, false);
     if (!d) return fail(c, TPM_ERR_ARG, "unknown field id");
+    if (field == TPM_FIELD_RU_INT || field == TPM_FIELD_RU) c->rui32_stale = true;
     TPM_CUDA_TRY(cudaMemcpyAsync(d, host, sizeof(double) * len, cudaMemcpyHostToDevice, c->stream));
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return TPM_OK;
@@ -371,6 +389,8 @@ int tpm_download_field(tpm_ctx *c, int field, double *host) {
     long long len;
     double *d = field_ptr(c, field, &len, true);
     if (!d) return fail(c, TPM_ERR_ARG, "unknown field id");
+    if (field == TPM_FIELD_FP && c->p.precision == TPM_PREC_MIXED)
+      tpm::launch_to_double(c, c->Fp32, c->Fp, 3 * c->g.n);  // the mixed path keeps F_p in FP32
     TPM_CUDA_TRY(cudaMemcpyAsync(host, d, sizeof(double) * len, cudaMemcpyDeviceToHost, c->stream));
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     if (field == TPM_FIELD_RHS_POIS) {
@@ -507,6 +527,7 @@ int tpm_initialize(tpm_ctx *c) {
     c->hsc->P0_np1 = c->hsc->P0;
     push_scalars(c);
     c->np1_is_base = true;
+    c->rui32_stale = true;
     // grid.cpp:474 (Rho_face is recomputed from Rho_int where it is needed)
     // grid.cpp:481-484: initial particle heat coupling
     tpm::particle_zero_fields(c);
@@ -531,6 +552,7 @@ int tpm_resume(tpm_ctx *c) {
     c->hsc->P0_np1 = c->hsc->P0;
     push_scalars(c);
     c->np1_is_base = true;
+    c->rui32_stale = true;
     tpm::particle_resume(c);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->initialized = true;

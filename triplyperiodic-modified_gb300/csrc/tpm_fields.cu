@@ -124,10 +124,10 @@ __device__ __forceinline__ Nbr nbr_of(const Grid &g, const Cell &q) {
 // tensor0::Equal_Div_F2C of U at centre (i,j,k) (tensor0.cpp:249-256),
 // evaluated in the compute type TC (double on the FP64 path, float on the
 // mixed path; the loads convert)
-template <typename TC>
-__device__ __forceinline__ TC divU_at(const Grid &g, const double *U, int i, int j, int k) {
+template <typename TC, typename TIn>
+__device__ __forceinline__ TC divU_at(const Grid &g, const TIn *U, int i, int j, int k) {
   long long c = at(g, i, j, k);
-  const double *Ux = U, *Uy = U + g.n, *Uz = U + 2 * g.n;
+  const TIn *Ux = U, *Uy = U + g.n, *Uz = U + 2 * g.n;
   return ((TC)Ux[at(g, wrap_p(i, g.nx), j, k)] - (TC)Ux[c]) * (TC)g.inv_dx +
          ((TC)Uy[at(g, i, wrap_p(j, g.ny), k)] - (TC)Uy[c]) * (TC)g.inv_dy +
          ((TC)Uz[at(g, i, j, wrap_p(k, g.nz))] - (TC)Uz[c]) * (TC)g.inv_dz;
@@ -140,8 +140,8 @@ __device__ __forceinline__ long long shift(const Grid &g, int i, int j, int k, i
 }
 
 // flux P_{d,e}(cell) = I_e,C2F(U_d) * I_d,C2F(RU_e)   (grid.cpp:785-800)
-template <typename TC>
-__device__ __forceinline__ TC flux_at(const Grid &g, const double *Ud, const double *RUe, int i,
+template <typename TC, typename TIn>
+__device__ __forceinline__ TC flux_at(const Grid &g, const TIn *Ud, const TIn *RUe, int i,
                                       int j, int k, int d, int e) {
   long long c = at(g, i, j, k);
   TC iu = ((TC)Ud[c] + (TC)Ud[shift(g, i, j, k, e, -1)]) * (TC)0.5;
@@ -151,10 +151,11 @@ __device__ __forceinline__ TC flux_at(const Grid &g, const double *Ud, const dou
 
 // grid::Update_RU_WOP (grid.cpp:776-814).  The right-hand side is evaluated
 // in TC; the RK combinations RU_np1 += dt*post*RHS, RU_new = RU + dt*pre*RHS
-// are always FP64.  With TC = double every operation is the reference's.
-template <typename TC>
-__global__ void k_rhs_momentum(Grid g, const double *__restrict__ U, const double *__restrict__ RUi,
-                               const double *__restrict__ Fp, const double *__restrict__ Rho_int,
+// are always FP64.  With TC = TIn = double every operation is the reference's;
+// the mixed path reads FP32 copies of U, RU_int and F_p (TIn = float).
+template <typename TC, typename TIn>
+__global__ void k_rhs_momentum(Grid g, const TIn *__restrict__ U, const TIn *__restrict__ RUi,
+                               const TIn *__restrict__ Fp, const double *__restrict__ Rho_int,
                                const double *__restrict__ RU, const double *__restrict__ np1_in,
                                double *__restrict__ RU_np1, double *__restrict__ RU_new, RhsArgs a) {
   const TC inv_d[3] = {(TC)g.inv_dx, (TC)g.inv_dy, (TC)g.inv_dz};
@@ -163,13 +164,13 @@ __global__ void k_rhs_momentum(Grid g, const double *__restrict__ U, const doubl
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
     Nbr nb = nbr_of(g, q);
-    const TC div_c = divU_at<TC>(g, U, q.i, q.j, q.k);
-    const TC div_m[3] = {divU_at<TC>(g, U, wrap_m(q.i, g.nx), q.j, q.k),
-                         divU_at<TC>(g, U, q.i, wrap_m(q.j, g.ny), q.k),
-                         divU_at<TC>(g, U, q.i, q.j, wrap_m(q.k, g.nz))};
+    const TC div_c = divU_at<TC, TIn>(g, U, q.i, q.j, q.k);
+    const TC div_m[3] = {divU_at<TC, TIn>(g, U, wrap_m(q.i, g.nx), q.j, q.k),
+                         divU_at<TC, TIn>(g, U, q.i, wrap_m(q.j, g.ny), q.k),
+                         divU_at<TC, TIn>(g, U, q.i, q.j, wrap_m(q.k, g.nz))};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const double *Ud = U + d * g.n;
+      const TIn *Ud = U + d * g.n;
       // dummy2 = grad_C2F(div U) (tensor1.cpp:259-270)
       TC gd = (div_c - div_m[d]) * inv_d[d];
       // dummy = Del2(U_d) (tensor0.cpp:258-265)
@@ -185,12 +186,12 @@ __global__ void k_rhs_momentum(Grid g, const double *__restrict__ U, const doubl
         TC t[3];
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
-          const double *RUe = RUi + e * g.n;
+          const TIn *RUe = RUi + e * g.n;
           int ip = e == 0 ? wrap_p(q.i, g.nx) : q.i;
           int jp = e == 1 ? wrap_p(q.j, g.ny) : q.j;
           int kp = e == 2 ? wrap_p(q.k, g.nz) : q.k;
-          t[e] = (flux_at<TC>(g, Ud, RUe, ip, jp, kp, d, e) -
-                  flux_at<TC>(g, Ud, RUe, q.i, q.j, q.k, d, e)) * inv_d[e];
+          t[e] = (flux_at<TC, TIn>(g, Ud, RUe, ip, jp, kp, d, e) -
+                  flux_at<TC, TIn>(g, Ud, RUe, q.i, q.j, q.k, d, e)) * inv_d[e];
         }
         conv = t[0] + t[1] + t[2];
       }
@@ -366,18 +367,29 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ Rho_new,
 
 // face velocity of the mixed path: only the FP32 stencil and the particle
 // gather read it, so it is formed in FP32
-__global__ void k_face_velocity_mixed(Grid g, const double *__restrict__ RUi,
-                                      const double *__restrict__ Rho_int, double *__restrict__ U) {
+__global__ void k_face_velocity_mixed(Grid g, const float *__restrict__ RUi32,
+                                      const double *__restrict__ Rho_int, float *__restrict__ U) {
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
-    float r = (float)Rho_int[c];
-    U[c] = (double)((float)RUi[c] / ((r + (float)Rho_int[at(g, wrap_m(q.i, g.nx), q.j, q.k)]) * 0.5f));
-    U[g.n + c] = (double)((float)RUi[g.n + c] /
-                          ((r + (float)Rho_int[at(g, q.i, wrap_m(q.j, g.ny), q.k)]) * 0.5f));
-    U[2 * g.n + c] = (double)((float)RUi[2 * g.n + c] /
-                              ((r + (float)Rho_int[at(g, q.i, q.j, wrap_m(q.k, g.nz))]) * 0.5f));
+    const double r = Rho_int[c];
+    U[c] = RUi32[c] / (float)((r + Rho_int[at(g, wrap_m(q.i, g.nx), q.j, q.k)]) * 0.5);
+    U[g.n + c] = RUi32[g.n + c] / (float)((r + Rho_int[at(g, q.i, wrap_m(q.j, g.ny), q.k)]) * 0.5);
+    U[2 * g.n + c] =
+        RUi32[2 * g.n + c] / (float)((r + Rho_int[at(g, q.i, q.j, wrap_m(q.k, g.nz))]) * 0.5);
   }
+}
+
+__global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+__global__ void k_to_double(const float *__restrict__ a, double *__restrict__ b, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
 }
 
 // mean of a field from per-block partial sums, stored at *out
@@ -395,7 +407,7 @@ __global__ void k_finish_mean(const double *__restrict__ partials, int nparts, l
 // sums of RU_np1 for make_mean_U0 (simulation.cpp:80) are reduced too.
 __global__ void k_project(Grid g, const double *__restrict__ P, double *__restrict__ RU_np1,
                           double *__restrict__ RU_new, double a_np1, double b_new, int stage,
-                          double *__restrict__ partials) {
+                          double *__restrict__ partials, float *__restrict__ RUn32) {
   __shared__ double sh[kThreads];
   double acc[3] = {0, 0, 0};
   const double inv_d[3] = {g.inv_dx, g.inv_dy, g.inv_dz};
@@ -409,7 +421,9 @@ __global__ void k_project(Grid g, const double *__restrict__ P, double *__restri
       double G = (pc - P[nb.m[d]]) * inv_d[d];
       double np1 = RU_np1[d * g.n + c] + a_np1 * G;
       RU_np1[d * g.n + c] = np1;
-      RU_new[d * g.n + c] = (stage != 3) ? RU_new[d * g.n + c] + b_new * G : np1;
+      const double nw = (stage != 3) ? RU_new[d * g.n + c] + b_new * G : np1;
+      RU_new[d * g.n + c] = nw;
+      if (RUn32) RUn32[d * g.n + c] = (float)nw;
       acc[d] += np1;
     }
   }
@@ -534,7 +548,7 @@ void launch_rho_update(tpm_ctx *c, int s, bool np1_in_base) {
 void launch_face_velocity(tpm_ctx *c) {
   if (c->p.precision == TPM_PREC_MIXED) {
     TPM_LAUNCH(c, "face_velocity", k_face_velocity_mixed, cell_blocks(c->g), kThreads, 0, c->g,
-               c->RU_int, c->Rho_int, c->U);
+               c->RUi32, c->Rho_int, c->U32);
     return;
   }
   TPM_LAUNCH(c, "face_velocity", k_face_velocity, cell_blocks(c->g), kThreads, 0, c->g,
@@ -556,11 +570,11 @@ void launch_rhs_momentum(tpm_ctx *c, int s, bool np1_in_base) {
   a.dtpr = c->p.dt * kPre[s];
   a.stage = s;
   if (c->p.precision == TPM_PREC_MIXED)
-    TPM_LAUNCH(c, "rhs_momentum", k_rhs_momentum<float>, cell_blocks(c->g), kThreads, 0, c->g,
-               c->U, c->RU_int, c->Fp, c->Rho_int, c->RU, np1_in_base ? c->RU : c->RU_np1,
-               c->RU_np1, c->RU_new, a);
+    TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum<float, float>), cell_blocks(c->g), kThreads, 0,
+               c->g, c->U32, c->RUi32, c->Fp32, c->Rho_int, c->RU,
+               np1_in_base ? c->RU : c->RU_np1, c->RU_np1, c->RU_new, a);
   else
-    TPM_LAUNCH(c, "rhs_momentum", k_rhs_momentum<double>, cell_blocks(c->g), kThreads, 0, c->g,
+    TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum<double, double>), cell_blocks(c->g), kThreads, 0, c->g,
                c->U, c->RU_int, c->Fp, c->Rho_int, c->RU, np1_in_base ? c->RU : c->RU_np1,
                c->RU_np1, c->RU_new, a);
 }
@@ -588,7 +602,8 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
 void launch_project(tpm_ctx *c, int s) {
   int nb = cell_blocks(c->g);
   TPM_LAUNCH(c, "project", k_project, nb, kThreads, 0, c->g, c->P, c->RU_np1, c->RU_new,
-             -(c->p.dt * kPost[s]), -(c->p.dt * kPre[s]), s, c->partials + kPartRu * kRedBlocks);
+             -(c->p.dt * kPost[s]), -(c->p.dt * kPre[s]), s, c->partials + kPartRu * kRedBlocks,
+             c->p.precision == TPM_PREC_MIXED ? c->RUn32 : nullptr);
   if (s == 3)
     TPM_LAUNCH(c, "finish_means3", k_finish_means3, 1, kThreads, 0,
                c->partials + kPartRu * kRedBlocks, nb, c->g.n,
@@ -601,6 +616,14 @@ void launch_div_residual(tpm_ctx *c, int s) {
              c->divg, c->dsc, c->p.dt * kPre[s], c->partials + kPartDiv * kRedBlocks);
   TPM_LAUNCH(c, "finish_max_div", k_finish_max_div, 1, kThreads, 0,
              c->partials + kPartDiv * kRedBlocks, nb, c->dsc);
+}
+
+void launch_to_float(tpm_ctx *c, const double *src, float *dst, long long n) {
+  TPM_LAUNCH(c, "to_float", k_to_float, cell_blocks(c->g), kThreads, 0, src, dst, n);
+}
+
+void launch_to_double(tpm_ctx *c, const float *src, double *dst, long long n) {
+  TPM_LAUNCH(c, "to_double", k_to_double, cell_blocks(c->g), kThreads, 0, src, dst, n);
 }
 
 void launch_mean_reset(tpm_ctx *c) {

@@ -105,6 +105,10 @@ struct tpm_ctx {
   double *P = nullptr, *C = nullptr, *Q = nullptr, *Fp = nullptr /*3n*/, *U = nullptr /*3n*/;
   double *RHS = nullptr, *divg = nullptr, *inv_rho = nullptr, *Tgas = nullptr;
   double *Cface = nullptr /*3n*/, *cc = nullptr;
+  // FP32 copies read by the FP32 stencils of the mixed path (written once per
+  // value: FP64<->FP32 conversions issue on the FP64 pipe)
+  float *U32 = nullptr, *RUi32 = nullptr, *RUn32 = nullptr, *Fp32 = nullptr;  // 3n each
+  bool rui32_stale = true;
   double2 *spec = nullptr;
   double *partials = nullptr;  // kRedBlocks * 4
   tpm::DevScalars *dsc = nullptr;
@@ -158,6 +162,8 @@ void launch_mean_reset(tpm_ctx *c);
 void launch_init_fields(tpm_ctx *c);
 int cell_blocks(const Grid &g);
 void launch_center_coeff_from_C(tpm_ctx *c);  // operator-level Poisson entry
+void launch_to_float(tpm_ctx *c, const double *src, float *dst, long long n);
+void launch_to_double(tpm_ctx *c, const float *src, double *dst, long long n);
 
 // ---- Poisson / FFT (tpm_fft.cu) ----
 void fft_plans_create(tpm_ctx *c);

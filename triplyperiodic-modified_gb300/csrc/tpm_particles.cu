@@ -46,10 +46,13 @@ struct PState {
   double *nw[7];
 };
 
-__global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const double *__restrict__ U,
+// TU: element type of the face velocity (FP32 copy on the mixed path);
+// TP: type of the momentum-deposit payload.
+template <typename TU, typename TP>
+__global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__restrict__ U,
                        const double *__restrict__ Tgas, double *__restrict__ rhs_t,
                        const double *__restrict__ tau, int32_t *__restrict__ key_t,
-                       double *__restrict__ pay_t, int32_t *__restrict__ key_r,
+                       TP *__restrict__ pay_t, int32_t *__restrict__ key_r,
                        double *__restrict__ pay_r) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
        p += (int64_t)gridDim.x * blockDim.x) {
@@ -62,9 +65,20 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const double *
     const double zl = (zi * g.idz - ((int)(zi * g.idz)));
     const int i0 = wrap_any(tx, g.nx), j0 = wrap_any(ty, g.ny), k0 = wrap_any(tz, g.nz);
     const long long c0 = at(g, i0, j0, k0);
-    const double ug = xl * U[at(g, wrap_p(i0, g.nx), j0, k0)] + (1 - xl) * U[c0];
-    const double vg = yl * U[g.n + at(g, i0, wrap_p(j0, g.ny), k0)] + (1 - yl) * U[g.n + c0];
-    const double wg = zl * U[2 * g.n + at(g, i0, j0, wrap_p(k0, g.nz))] + (1 - zl) * U[2 * g.n + c0];
+    double ug, vg, wg;
+    if (sizeof(TU) == sizeof(double)) {
+      ug = xl * (double)U[at(g, wrap_p(i0, g.nx), j0, k0)] + (1 - xl) * (double)U[c0];
+      vg = yl * (double)U[g.n + at(g, i0, wrap_p(j0, g.ny), k0)] + (1 - yl) * (double)U[g.n + c0];
+      wg = zl * (double)U[2 * g.n + at(g, i0, j0, wrap_p(k0, g.nz))] +
+           (1 - zl) * (double)U[2 * g.n + c0];
+    } else {  // FP32 interpolation of the FP32 face velocity (mixed path)
+      const float xf = (float)xl, yf = (float)yl, zf = (float)zl;
+      ug = (double)(xf * (float)U[at(g, wrap_p(i0, g.nx), j0, k0)] + (1 - xf) * (float)U[c0]);
+      vg = (double)(yf * (float)U[g.n + at(g, i0, wrap_p(j0, g.ny), k0)] +
+                    (1 - yf) * (float)U[g.n + c0]);
+      wg = (double)(zf * (float)U[2 * g.n + at(g, i0, j0, wrap_p(k0, g.nz))] +
+                    (1 - zf) * (float)U[2 * g.n + c0]);
+    }
     // ---- update_position (particle.cpp:314-338) ----
     double xn[3], xp[3], xb[3];
     const double uint_[3] = {ui, vi, wi};
@@ -92,12 +106,12 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const double *
     // ---- part2gas_velocity payload at x_int (particle.cpp:494-520) ----
     if (a.twc) {
       key_t[p] = (int32_t)c0;
-      pay_t[0 * np + p] = (1 - xl) * rhs[0];
-      pay_t[1 * np + p] = xl * rhs[0];
-      pay_t[2 * np + p] = (1 - yl) * rhs[1];
-      pay_t[3 * np + p] = yl * rhs[1];
-      pay_t[4 * np + p] = (1 - zl) * rhs[2];
-      pay_t[5 * np + p] = zl * rhs[2];
+      pay_t[0 * np + p] = (TP)((1 - xl) * rhs[0]);
+      pay_t[1 * np + p] = (TP)(xl * rhs[0]);
+      pay_t[2 * np + p] = (TP)((1 - yl) * rhs[1]);
+      pay_t[3 * np + p] = (TP)(yl * rhs[1]);
+      pay_t[4 * np + p] = (TP)((1 - zl) * rhs[2]);
+      pay_t[5 * np + p] = (TP)(zl * rhs[2]);
     }
     // ---- Send_Recv on one rank = periodic wrap (particle.cpp:58-104, 150-250) ----
     const double L[3] = {g.Lx, g.Ly, g.Lz};
@@ -320,8 +334,9 @@ __global__ void k_segsort(long long n, const int32_t *__restrict__ starts,
   }
 }
 
+template <typename T>
 __global__ void k_gather_payload(int64_t np, int nf, const int32_t *__restrict__ perm,
-                                 const double *__restrict__ pay, double *__restrict__ sorted) {
+                                 const T *__restrict__ pay, T *__restrict__ sorted) {
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < np;
        s += (int64_t)gridDim.x * blockDim.x) {
     int32_t p = perm[s];
@@ -333,8 +348,9 @@ __global__ void k_gather_payload(int64_t np, int nf, const int32_t *__restrict__
 // part2gas_velocity (particle.cpp:494-520) + cumulative ghost fold: face d of
 // cell c collects the upper weight of the particles in cell c - e_d and the
 // lower weight of those in cell c.
+template <typename TP, typename TO>
 __global__ void k_dep_momentum(Grid g, const int32_t *__restrict__ starts,
-                               const double *__restrict__ pay, int64_t np, double *__restrict__ Fp) {
+                               const TP *__restrict__ pay, int64_t np, TO *__restrict__ Fp) {
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(c % g.nx);
@@ -345,11 +361,11 @@ __global__ void k_dep_momentum(Grid g, const int32_t *__restrict__ starts,
     const int32_t s0 = starts[c], e0 = starts[c + 1];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      double acc = 0;
+      TP acc = 0;
       const int32_t s1 = starts[m[d]], e1 = starts[m[d] + 1];
       for (int32_t s = s1; s < e1; ++s) acc += pay[(2 * d + 1) * np + s];
       for (int32_t s = s0; s < e0; ++s) acc += pay[(2 * d) * np + s];
-      Fp[d * g.n + c] = acc;
+      Fp[d * g.n + c] = (TO)acc;
     }
   }
 }
@@ -474,22 +490,39 @@ void launch_particle_push(tpm_ctx *c, int s, bool np1_in_base) {
   a.stage = s;
   a.twc = c->p.TWC;
   a.has_tau = c->tau != nullptr;
-  TPM_LAUNCH(c, "particle_push", k_push, pblocks(c->np), kThreads, 0, c->g,
-             pstate(c, np1_in_base), a, c->np, c->U, c->Tgas, c->rhs_t, c->tau, c->key_t,
-             c->pay_t, c->key_r, c->pay_r);
+  if (c->p.precision == TPM_PREC_MIXED)
+    TPM_LAUNCH(c, "particle_push", (k_push<float, float>), pblocks(c->np), kThreads, 0, c->g,
+               pstate(c, np1_in_base), a, c->np, c->U32, c->Tgas, c->rhs_t, c->tau, c->key_t,
+               reinterpret_cast<float *>(c->pay_t), c->key_r, c->pay_r);
+  else
+    TPM_LAUNCH(c, "particle_push", (k_push<double, double>), pblocks(c->np), kThreads, 0, c->g,
+               pstate(c, np1_in_base), a, c->np, c->U, c->Tgas, c->rhs_t, c->tau, c->key_t,
+               c->pay_t, c->key_r, c->pay_r);
 }
 
 // two-way momentum source at x_int (grid.cpp:877)
 void particle_deposit_momentum(tpm_ctx *c) {
+  const bool mixed = c->p.precision == TPM_PREC_MIXED;
   if (c->np == 0 || !c->p.TWC) {
-    TPM_CUDA_TRY(cudaMemsetAsync(c->Fp, 0, sizeof(double) * 3 * c->g.n, c->stream));
+    if (mixed)
+      TPM_CUDA_TRY(cudaMemsetAsync(c->Fp32, 0, sizeof(float) * 3 * c->g.n, c->stream));
+    else
+      TPM_CUDA_TRY(cudaMemsetAsync(c->Fp, 0, sizeof(double) * 3 * c->g.n, c->stream));
     return;
   }
   sort_by_cell(c, c->key_t, c->perm_t, c->starts_t);
-  TPM_LAUNCH(c, "payload_gather_t", k_gather_payload, pblocks(c->np), kThreads, 0, c->np, 6,
-             c->perm_t, c->pay_t, c->pay_t_s);
-  TPM_LAUNCH(c, "deposit_momentum", k_dep_momentum, cell_blocks(c->g), kThreads, 0, c->g,
-             c->starts_t, c->pay_t_s, c->np, c->Fp);
+  if (mixed) {
+    float *pt = reinterpret_cast<float *>(c->pay_t), *pts = reinterpret_cast<float *>(c->pay_t_s);
+    TPM_LAUNCH(c, "payload_gather_t", k_gather_payload<float>, pblocks(c->np), kThreads, 0, c->np,
+               6, c->perm_t, pt, pts);
+    TPM_LAUNCH(c, "deposit_momentum", (k_dep_momentum<float, float>), cell_blocks(c->g), kThreads,
+               0, c->g, c->starts_t, pts, c->np, c->Fp32);
+  } else {
+    TPM_LAUNCH(c, "payload_gather_t", k_gather_payload<double>, pblocks(c->np), kThreads, 0, c->np,
+               6, c->perm_t, c->pay_t, c->pay_t_s);
+    TPM_LAUNCH(c, "deposit_momentum", (k_dep_momentum<double, double>), cell_blocks(c->g),
+               kThreads, 0, c->g, c->starts_t, c->pay_t_s, c->np, c->Fp);
+  }
 }
 
 static void cic_deposit(tpm_ctx *c, int buf, bool with_rhs, double *out, double *partials,
@@ -528,7 +561,7 @@ static void cic_deposit(tpm_ctx *c, int buf, bool with_rhs, double *out, double 
 static void heat_deposit_from(tpm_ctx *c, int buf) {
   int nb = cell_blocks(c->g);
   sort_by_cell(c, c->key_r, c->perm_r[buf], c->starts_r[buf]);
-  TPM_LAUNCH(c, "payload_gather_r", k_gather_payload, pblocks(c->np), kThreads, 0, c->np, 4,
+  TPM_LAUNCH(c, "payload_gather_r", k_gather_payload<double>, pblocks(c->np), kThreads, 0, c->np, 4,
              c->perm_r[buf], c->pay_r, c->pay_r_s[buf]);
   cic_deposit(c, buf, true, c->Q, c->partials + kPartQ * kRedBlocks, "heat");
   c->q_parts = nb;
@@ -581,12 +614,13 @@ void particle_resume(tpm_ctx *c) {
              c->pq[1][1], c->pq[1][2], c->pq[1][6], c->Tgas, 0.0, c->np, c->rhs_t, c->key_r,
              c->pay_r, 0);
   sort_by_cell(c, c->key_r, c->perm_r[0], c->starts_r[0]);
-  TPM_LAUNCH(c, "payload_gather_r", k_gather_payload, pblocks(c->np), kThreads, 0, c->np, 4,
+  TPM_LAUNCH(c, "payload_gather_r", k_gather_payload<double>, pblocks(c->np), kThreads, 0, c->np, 4,
              c->perm_r[0], c->pay_r, c->pay_r_s[0]);
 }
 
 void particle_zero_fields(tpm_ctx *c) {
   TPM_CUDA_TRY(cudaMemsetAsync(c->Fp, 0, sizeof(double) * 3 * c->g.n, c->stream));
+  if (c->Fp32) TPM_CUDA_TRY(cudaMemsetAsync(c->Fp32, 0, sizeof(float) * 3 * c->g.n, c->stream));
   TPM_CUDA_TRY(cudaMemsetAsync(c->C, 0, sizeof(double) * c->g.n, c->stream));
 }
 
