@@ -216,8 +216,11 @@ int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, double Ly, doub
 
 /* Options (tpm_set_option). */
 enum {
-  TPM_OPT_STORE_DIVERGENCE = 1 /* keep the divergence constraint field for download
-                                  (grid.h:97); off by default to save bandwidth */
+  TPM_OPT_STORE_DIVERGENCE = 1, /* keep the divergence constraint field for download
+                                   (grid.h:97); off by default to save bandwidth */
+  TPM_OPT_DIV_RESIDUAL_EVERY_STAGE = 2 /* mixed path: evaluate the FP64 post-projection
+                                          divergence residual after every stage, not
+                                          only after the last one of each step */
 };
 int tpm_set_option(tpm_ctx *ctx, int option, int value);
 

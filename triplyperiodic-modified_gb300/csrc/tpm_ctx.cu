@@ -178,7 +178,8 @@ void substep(tpm_ctx *c, int s) {
   tpm::launch_poisson_rhs(c, s, c->store_div || c->p.precision == TPM_PREC_MIXED);
   poisson_loop(c, c->Iteration, c->p.epsilon);
   tpm::launch_project(c, s);
-  if (c->p.precision == TPM_PREC_MIXED) tpm::launch_div_residual(c, s);
+  if (c->p.precision == TPM_PREC_MIXED && (s == 3 || c->div_every_stage))
+    tpm::launch_div_residual(c, s);
   swap_stage(c);
   c->np1_is_base = false;
 }
@@ -290,6 +291,10 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
       c->Fp32 = dalloc<float>(c, 3 * n);
       for (float *f : {c->U32, c->RUi32, c->RUn32, c->Fp32})
         TPM_CUDA_TRY(cudaMemsetAsync(f, 0, sizeof(float) * 3 * n, c->stream));
+      c->Tgas32 = dalloc<float>(c, n);
+      TPM_CUDA_TRY(cudaMemsetAsync(c->Tgas32, 0, sizeof(float) * n, c->stream));
+      c->Cs = dalloc<double>(c, 3 * n);
+      TPM_CUDA_TRY(cudaMemsetAsync(c->Cs, 0, sizeof(double) * 3 * n, c->stream));
     }
     c->partials = dalloc<double>(c, (size_t)tpm::kPartRegions * tpm::kRedBlocks);
     c->dsc = dalloc<tpm::DevScalars>(c, 1);
@@ -361,6 +366,10 @@ int tpm_set_option(tpm_ctx *c, int option, int value) {
   return guarded(c, [&]() -> int {
     if (option == TPM_OPT_STORE_DIVERGENCE) {
       c->store_div = value != 0;
+      return TPM_OK;
+    }
+    if (option == TPM_OPT_DIV_RESIDUAL_EVERY_STAGE) {
+      c->div_every_stage = value != 0;
       return TPM_OK;
     }
     return fail(c, TPM_ERR_ARG, "unknown option");

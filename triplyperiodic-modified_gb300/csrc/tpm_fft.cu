@@ -159,7 +159,10 @@ __device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
 
 // ------------------------------------------------- 1. residual + R2C along x
 // poisson.cpp:399-404 (residual) and the first third of fft_3d (:431).
-template <typename T2>
+// kScaled (mixed path): Cf holds C*(1/d^2) per component, and the residual is
+// sum_d Cs_hi (P_hi - P) - Cs_lo (P - P_lo) - RHS, times cc: the same FP64
+// residual with a third fewer FP64 operations.
+template <typename T2, bool kScaled = false>
 __global__ void k_xfwd_resid(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
                              const double *__restrict__ P, const double *__restrict__ Cf,
                              const double *__restrict__ cc, const double *__restrict__ RHS,
@@ -186,15 +189,21 @@ __global__ void k_xfwd_resid(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
       const int kp = wrap_p(k, g.nz), km = wrap_m(k, g.nz);
       const long long cxp = at(g, ip, j, k), cyp = at(g, i, jp, k), czp = at(g, i, j, kp);
       const double pc = P[c];
-      // dummy = grad_C2F(P) * C at the low and high faces
-      double gx_hi = (P[cxp] - pc) * g.inv_dx * Cx_[cxp];
-      double gx_lo = (pc - P[at(g, im, j, k)]) * g.inv_dx * Cx_[c];
-      double gy_hi = (P[cyp] - pc) * g.inv_dy * Cy_[cyp];
-      double gy_lo = (pc - P[at(g, i, jm, k)]) * g.inv_dy * Cy_[c];
-      double gz_hi = (P[czp] - pc) * g.inv_dz * Cz_[czp];
-      double gz_lo = (pc - P[at(g, i, j, km)]) * g.inv_dz * Cz_[c];
-      double rn = (gx_hi - gx_lo) * g.inv_dx + (gy_hi - gy_lo) * g.inv_dy +
-                  (gz_hi - gz_lo) * g.inv_dz;
+      double rn;
+      if (kScaled) {
+        rn = (Cx_[cxp] * (P[cxp] - pc) - Cx_[c] * (pc - P[at(g, im, j, k)])) +
+             (Cy_[cyp] * (P[cyp] - pc) - Cy_[c] * (pc - P[at(g, i, jm, k)])) +
+             (Cz_[czp] * (P[czp] - pc) - Cz_[c] * (pc - P[at(g, i, j, km)]));
+      } else {
+        // dummy = grad_C2F(P) * C at the low and high faces
+        double gx_hi = (P[cxp] - pc) * g.inv_dx * Cx_[cxp];
+        double gx_lo = (pc - P[at(g, im, j, k)]) * g.inv_dx * Cx_[c];
+        double gy_hi = (P[cyp] - pc) * g.inv_dy * Cy_[cyp];
+        double gy_lo = (pc - P[at(g, i, jm, k)]) * g.inv_dy * Cy_[c];
+        double gz_hi = (P[czp] - pc) * g.inv_dz * Cz_[czp];
+        double gz_lo = (pc - P[at(g, i, j, km)]) * g.inv_dz * Cz_[c];
+        rn = (gx_hi - gx_lo) * g.inv_dx + (gy_hi - gy_lo) * g.inv_dy + (gz_hi - gz_lo) * g.inv_dz;
+      }
       rn -= (RHS[c] - mean);
       rn *= cc[c];
       r = rn;
@@ -468,8 +477,12 @@ static void poisson_iteration_t(tpm_ctx *c) {
     int npen = pens_for(c->fx.n);
     int blocks = (int)((nrows + npen - 1) / npen);
     size_t smem = 2 * (size_t)npen * c->fx.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_x_fwd_resid", k_xfwd_resid<T2>, blocks, kFftThreads, smem, g, c->fx,
-               r2c, c->P, c->Cface, c->cc, c->RHS, c->dsc, spec, npen);
+    if (c->p.precision == TPM_PREC_MIXED)
+      TPM_LAUNCH(c, "fft_x_fwd_resid", (k_xfwd_resid<T2, true>), blocks, kFftThreads, smem, g,
+                 c->fx, r2c, c->P, c->Cs, c->cc, c->RHS, c->dsc, spec, npen);
+    else
+      TPM_LAUNCH(c, "fft_x_fwd_resid", (k_xfwd_resid<T2, false>), blocks, kFftThreads, smem, g,
+                 c->fx, r2c, c->P, c->Cface, c->cc, c->RHS, c->dsc, spec, npen);
   }
   {
     int npen = pens_for(c->fy.n);

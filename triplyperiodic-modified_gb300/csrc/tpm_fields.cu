@@ -298,7 +298,7 @@ __device__ __forceinline__ double rcp64(double x) {
 __global__ void k_rho_update_mixed(Grid g, const double *__restrict__ RUi,
                                    const double *__restrict__ Rho, const double *__restrict__ np1_in,
                                    double *__restrict__ Rho_np1, double *__restrict__ Rho_new,
-                                   double *__restrict__ inv_rho, double *__restrict__ Tgas,
+                                   double *__restrict__ inv_rho, float *__restrict__ Tgas32,
                                    const DevScalars *__restrict__ s, double a_np1, double b_new,
                                    int stage) {
   const double *RUx = RUi, *RUy = RUi + g.n, *RUz = RUi + 2 * g.n;
@@ -315,22 +315,27 @@ __global__ void k_rho_update_mixed(Grid g, const double *__restrict__ RUi,
     Rho_new[c] = nw;
     double ir = rcp64(nw);
     inv_rho[c] = ir;
-    Tgas[c] = T_scale * ir;
+    Tgas32[c] = (float)(T_scale * ir);
   }
 }
 
-// k_poisson_rhs of the mixed path: FP64 throughout (the right-hand side
-// feeds the FP64 residual of the refinement), reciprocals for the 1/Rho_face
-// coefficients and U = RU*C instead of RU/Rho_face.
+// k_poisson_rhs of the mixed path.  The right-hand side is FP64 (it feeds the
+// FP64 residual of the refinement).  The face coefficients C ~ 1/Rho_face and
+// the preconditioner scale cc are FP32 reciprocals stored exactly as doubles:
+// the projection is consistent for any C used alike in U = RU*C, in
+// div(C grad P) and in the divergence check, and cc only sets the rate of the
+// Richardson iteration, not its fixed point.  Cs = C/d^2 feeds the residual.
 __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ Rho_new,
                                     const double *__restrict__ inv_rho, const double *__restrict__ Q,
                                     const double *__restrict__ RUn, const DevScalars *__restrict__ s,
                                     double *__restrict__ RHS, double *__restrict__ divg,
-                                    double *__restrict__ Cface, double *__restrict__ cc,
-                                    double *__restrict__ partials, PoisArgs a) {
+                                    double *__restrict__ Cface, double *__restrict__ Cs,
+                                    double *__restrict__ cc, double *__restrict__ partials,
+                                    PoisArgs a) {
   __shared__ double sh[kThreads];
   const double coef = s->coef_div, meanQ = s->mean_Q;
-  const double OneThird = 1. / 3.;
+  const double inv_d[3] = {g.inv_dx, g.inv_dy, g.inv_dz};
+  const double inv_d2[3] = {g.inv_dx2, g.inv_dy2, g.inv_dz2};
   double acc = 0;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
@@ -343,23 +348,23 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ Rho_new,
     double Qc = a.cooling ? Q[c] - meanQ : Q[c];
     double dv = a.kCp * lap + coef * Qc;
     divg[c] = dv;
-    double r = Rho_new[c];
-    double t[3], c_lo[3], c_hi[3];
+    const float r = (float)Rho_new[c];
+    double t[3];
+    float msum = 0.f;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      c_lo[d] = rcp64((r + Rho_new[nb.m[d]]) * 0.5);
-      c_hi[d] = rcp64((Rho_new[nb.p[d]] + r) * 0.5);
+      const float clo = 1.0f / ((r + (float)Rho_new[nb.m[d]]) * 0.5f);
+      const float chi = 1.0f / (((float)Rho_new[nb.p[d]] + r) * 0.5f);
       const double *R = RUn + d * g.n;
-      t[d] = (R[nb.p[d]] * c_hi[d] - R[c] * c_lo[d]) *
-             (d == 0 ? g.inv_dx : d == 1 ? g.inv_dy : g.inv_dz);
-      Cface[d * g.n + c] = c_lo[d];
+      t[d] = (R[nb.p[d]] * (double)chi - R[c] * (double)clo) * inv_d[d];
+      Cface[d * g.n + c] = (double)clo;
+      Cs[d * g.n + c] = (double)clo * inv_d2[d];
+      msum += (clo + chi) * 0.5f;
     }
     double rhs = (t[0] + t[1] + t[2] - dv) * a.inv_dtpre;
     RHS[c] = rhs;
     acc += rhs;
-    double m = OneThird * ((c_lo[0] + c_hi[0]) * 0.5 + (c_lo[1] + c_hi[1]) * 0.5 +
-                           (c_lo[2] + c_hi[2]) * 0.5);
-    cc[c] = -rcp64(m);
+    cc[c] = (double)(-3.0f / msum);
   }
   double bs = block_sum(acc, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = bs;
@@ -537,7 +542,7 @@ void launch_rho_update(tpm_ctx *c, int s, bool np1_in_base) {
   if (c->p.precision == TPM_PREC_MIXED) {
     TPM_LAUNCH(c, "rho_update", k_rho_update_mixed, cell_blocks(c->g), kThreads, 0, c->g,
                c->RU_int, c->Rho, np1_in_base ? c->Rho : c->Rho_np1, c->Rho_np1, c->Rho_new,
-               c->inv_rho, c->Tgas, c->dsc, -(c->p.dt * kPost[s]), -c->p.dt * kPre[s], s);
+               c->inv_rho, c->Tgas32, c->dsc, -(c->p.dt * kPost[s]), -c->p.dt * kPre[s], s);
     return;
   }
   TPM_LAUNCH(c, "rho_update", k_rho_update, cell_blocks(c->g), kThreads, 0, c->g, c->RU_int,
@@ -588,7 +593,7 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
   int nb = cell_blocks(c->g);
   if (c->p.precision == TPM_PREC_MIXED)
     TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_mixed, nb, kThreads, 0, c->g, c->Rho_new,
-               c->inv_rho, c->Q, c->RU_new, c->dsc, c->RHS, c->divg, c->Cface, c->cc,
+               c->inv_rho, c->Q, c->RU_new, c->dsc, c->RHS, c->divg, c->Cface, c->Cs, c->cc,
                c->partials + kPartRhs * kRedBlocks, a);
   else
   TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs, nb, kThreads, 0, c->g, c->Rho_new, c->inv_rho,

@@ -23,6 +23,7 @@ FIELD = dict(RU=0, RU_INT=1, RU_NEW=2, RU_NP1=3, RHO=4, RHO_INT=5, RHO_NEW=6, RH
 VECTOR = {"RU", "RU_INT", "RU_NEW", "RU_NP1", "FP"}
 PSET = dict(base=0, int=1, new=2, np1=3)
 OPT_STORE_DIVERGENCE = 1
+OPT_DIV_RESIDUAL_EVERY_STAGE = 2
 STATUS = {0: "TPM_OK", -1: "TPM_ERR_ARG", -2: "TPM_ERR_CUDA", -3: "TPM_ERR_TIMEOUT",
           -4: "TPM_ERR_NONFINITE", -5: "TPM_ERR_UNSUPPORTED", -6: "TPM_ERR_STATE",
           -7: "TPM_ERR_NOMEM"}
