@@ -274,7 +274,7 @@ def path_result(p, s, ms, steps, world, n_it, launches, prof, clocks, mixed, pea
         "step_roofline": {"achieved_gbs": round(sgbs, 1), "frac": round(sgbs / peak, 4),
                           "algorithmic_bytes_per_step": int(sb)},
         "kernels_ms_per_step": {k: round(v[1] / 2, 3) for k, v in
-                                sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]},
+                                sorted(prof.items(), key=lambda kv: -kv[1][1])},
         "mparticle_steps_per_s": world * s.npart * steps / (ms * 1e-3) / 1e6,
     }
 

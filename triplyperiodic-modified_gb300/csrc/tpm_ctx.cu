@@ -291,8 +291,6 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
       c->Fp32 = dalloc<float>(c, 3 * n);
       for (float *f : {c->U32, c->RUi32, c->RUn32, c->Fp32})
         TPM_CUDA_TRY(cudaMemsetAsync(f, 0, sizeof(float) * 3 * n, c->stream));
-      c->Tgas32 = dalloc<float>(c, n);
-      TPM_CUDA_TRY(cudaMemsetAsync(c->Tgas32, 0, sizeof(float) * n, c->stream));
       c->Cs = dalloc<double>(c, 3 * n);
       TPM_CUDA_TRY(cudaMemsetAsync(c->Cs, 0, sizeof(double) * 3 * n, c->stream));
     }

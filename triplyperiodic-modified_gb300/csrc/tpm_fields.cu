@@ -293,12 +293,19 @@ __device__ __forceinline__ double rcp64(double x) {
   return __fma_rn(r, e, r);
 }
 
+// 1/x to ~1e-14 relative: FP32 seed and one Newton step (2 FMAs)
+__device__ __forceinline__ double rcp64_1(double x) {
+  double r = (double)__frcp_rn((float)x);
+  double e = __fma_rn(-x, r, 1.0);
+  return __fma_rn(r, e, r);
+}
+
 // k_rho_update of the mixed path: same FP64 density update, reciprocals
 // instead of divisions
 __global__ void k_rho_update_mixed(Grid g, const double *__restrict__ RUi,
                                    const double *__restrict__ Rho, const double *__restrict__ np1_in,
                                    double *__restrict__ Rho_np1, double *__restrict__ Rho_new,
-                                   double *__restrict__ inv_rho, float *__restrict__ Tgas32,
+                                   double *__restrict__ inv_rho, double *__restrict__ Tgas,
                                    const DevScalars *__restrict__ s, double a_np1, double b_new,
                                    int stage) {
   const double *RUx = RUi, *RUy = RUi + g.n, *RUz = RUi + 2 * g.n;
@@ -315,16 +322,17 @@ __global__ void k_rho_update_mixed(Grid g, const double *__restrict__ RUi,
     Rho_new[c] = nw;
     double ir = rcp64(nw);
     inv_rho[c] = ir;
-    Tgas32[c] = (float)(T_scale * ir);
+    Tgas[c] = T_scale * ir;
   }
 }
 
 // k_poisson_rhs of the mixed path.  The right-hand side is FP64 (it feeds the
-// FP64 residual of the refinement).  The face coefficients C ~ 1/Rho_face and
-// the preconditioner scale cc are FP32 reciprocals stored exactly as doubles:
-// the projection is consistent for any C used alike in U = RU*C, in
-// div(C grad P) and in the divergence check, and cc only sets the rate of the
-// Richardson iteration, not its fixed point.  Cs = C/d^2 feeds the residual.
+// FP64 residual of the refinement).  The face coefficients C = 1/Rho_face
+// come from an FP32 seed and one FP64 Newton step (~1e-14 relative; an FP32
+// C would perturb the divergence constraint at 1e-7, which the nearly
+// divergence-free right-hand side amplifies in P).  The preconditioner scale
+// cc is FP32: it sets the rate of the Richardson iteration, not its fixed
+// point.  Cs = C/d^2 feeds the residual.
 __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ Rho_new,
                                     const double *__restrict__ inv_rho, const double *__restrict__ Q,
                                     const double *__restrict__ RUn, const DevScalars *__restrict__ s,
@@ -348,18 +356,18 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ Rho_new,
     double Qc = a.cooling ? Q[c] - meanQ : Q[c];
     double dv = a.kCp * lap + coef * Qc;
     divg[c] = dv;
-    const float r = (float)Rho_new[c];
+    const double r = Rho_new[c];
     double t[3];
     float msum = 0.f;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const float clo = 1.0f / ((r + (float)Rho_new[nb.m[d]]) * 0.5f);
-      const float chi = 1.0f / (((float)Rho_new[nb.p[d]] + r) * 0.5f);
+      const double clo = rcp64_1((r + Rho_new[nb.m[d]]) * 0.5);
+      const double chi = rcp64_1((Rho_new[nb.p[d]] + r) * 0.5);
       const double *R = RUn + d * g.n;
-      t[d] = (R[nb.p[d]] * (double)chi - R[c] * (double)clo) * inv_d[d];
-      Cface[d * g.n + c] = (double)clo;
-      Cs[d * g.n + c] = (double)clo * inv_d2[d];
-      msum += (clo + chi) * 0.5f;
+      t[d] = (R[nb.p[d]] * chi - R[c] * clo) * inv_d[d];
+      Cface[d * g.n + c] = clo;
+      Cs[d * g.n + c] = clo * inv_d2[d];
+      msum += ((float)clo + (float)chi) * 0.5f;
     }
     double rhs = (t[0] + t[1] + t[2] - dv) * a.inv_dtpre;
     RHS[c] = rhs;
@@ -542,7 +550,7 @@ void launch_rho_update(tpm_ctx *c, int s, bool np1_in_base) {
   if (c->p.precision == TPM_PREC_MIXED) {
     TPM_LAUNCH(c, "rho_update", k_rho_update_mixed, cell_blocks(c->g), kThreads, 0, c->g,
                c->RU_int, c->Rho, np1_in_base ? c->Rho : c->Rho_np1, c->Rho_np1, c->Rho_new,
-               c->inv_rho, c->Tgas32, c->dsc, -(c->p.dt * kPost[s]), -c->p.dt * kPre[s], s);
+               c->inv_rho, c->Tgas, c->dsc, -(c->p.dt * kPost[s]), -c->p.dt * kPre[s], s);
     return;
   }
   TPM_LAUNCH(c, "rho_update", k_rho_update, cell_blocks(c->g), kThreads, 0, c->g, c->RU_int,

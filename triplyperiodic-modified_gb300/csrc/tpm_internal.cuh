@@ -108,7 +108,6 @@ struct tpm_ctx {
   // FP32 copies read by the FP32 stencils of the mixed path (written once per
   // value: FP64<->FP32 conversions issue on the FP64 pipe)
   float *U32 = nullptr, *RUi32 = nullptr, *RUn32 = nullptr, *Fp32 = nullptr;  // 3n each
-  float *Tgas32 = nullptr;  // n
   double *Cs = nullptr;     // 3n: C/d^2 for the mixed residual
   bool rui32_stale = true;
   double2 *spec = nullptr;

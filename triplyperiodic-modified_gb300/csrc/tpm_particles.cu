@@ -50,7 +50,7 @@ struct PState {
 // TP: type of the momentum-deposit payload.
 template <typename TU, typename TP>
 __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__restrict__ U,
-                       const TU *__restrict__ Tgas, double *__restrict__ rhs_t,
+                       const double *__restrict__ Tgas, double *__restrict__ rhs_t,
                        const double *__restrict__ tau, int32_t *__restrict__ key_t,
                        TP *__restrict__ pay_t, int32_t *__restrict__ key_r,
                        double *__restrict__ pay_r) {
@@ -143,27 +143,16 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     const int i1 = wrap_any(ri, g.nx), im = wrap_any(ri - 1, g.nx);
     const int j1 = wrap_any(rj, g.ny), jm = wrap_any(rj - 1, g.ny);
     const int k1 = wrap_any(rk, g.nz), km = wrap_any(rk - 1, g.nz);
-    double Tg;
-    if (sizeof(TU) == sizeof(double)) {
-      Tg = x_l * y_l * z_l * (double)Tgas[at(g, i1, j1, k1)] +
-           (1 - x_l) * y_l * z_l * (double)Tgas[at(g, im, j1, k1)] +
-           x_l * (1 - y_l) * z_l * (double)Tgas[at(g, i1, jm, k1)] +
-           x_l * y_l * (1 - z_l) * (double)Tgas[at(g, i1, j1, km)] +
-           (1 - x_l) * (1 - y_l) * z_l * (double)Tgas[at(g, im, jm, k1)] +
-           (1 - x_l) * y_l * (1 - z_l) * (double)Tgas[at(g, im, j1, km)] +
-           x_l * (y_l - 1) * (z_l - 1) * (double)Tgas[at(g, i1, jm, km)] +
-           (1 - x_l) * (1 - y_l) * (1 - z_l) * (double)Tgas[at(g, im, jm, km)];
-    } else {  // FP32 trilinear gather of the FP32 gas temperature (mixed path)
-      const float xf = (float)x_l, yf = (float)y_l, zf = (float)z_l;
-      Tg = (double)(xf * yf * zf * (float)Tgas[at(g, i1, j1, k1)] +
-                    (1 - xf) * yf * zf * (float)Tgas[at(g, im, j1, k1)] +
-                    xf * (1 - yf) * zf * (float)Tgas[at(g, i1, jm, k1)] +
-                    xf * yf * (1 - zf) * (float)Tgas[at(g, i1, j1, km)] +
-                    (1 - xf) * (1 - yf) * zf * (float)Tgas[at(g, im, jm, k1)] +
-                    (1 - xf) * yf * (1 - zf) * (float)Tgas[at(g, im, j1, km)] +
-                    xf * (1 - yf) * (1 - zf) * (float)Tgas[at(g, i1, jm, km)] +
-                    (1 - xf) * (1 - yf) * (1 - zf) * (float)Tgas[at(g, im, jm, km)]);
-    }
+    // FP64 on both paths: the heat rate is a difference of nearly equal
+    // temperatures, which amplifies any rounding of Tg
+    const double Tg = x_l * y_l * z_l * Tgas[at(g, i1, j1, k1)] +
+                      (1 - x_l) * y_l * z_l * Tgas[at(g, im, j1, k1)] +
+                      x_l * (1 - y_l) * z_l * Tgas[at(g, i1, jm, k1)] +
+                      x_l * y_l * (1 - z_l) * Tgas[at(g, i1, j1, km)] +
+                      (1 - x_l) * (1 - y_l) * z_l * Tgas[at(g, im, jm, k1)] +
+                      (1 - x_l) * y_l * (1 - z_l) * Tgas[at(g, im, j1, km)] +
+                      x_l * (y_l - 1) * (z_l - 1) * Tgas[at(g, i1, jm, km)] +
+                      (1 - x_l) * (1 - y_l) * (1 - z_l) * Tgas[at(g, im, jm, km)];
     const double rt = (Tg - Tnew) * a.iTth;
     rhs_t[p] = rt;
     key_r[p] = (int32_t)at(g, i1, j1, k1);
@@ -505,7 +494,7 @@ void launch_particle_push(tpm_ctx *c, int s, bool np1_in_base) {
   a.has_tau = c->tau != nullptr;
   if (c->p.precision == TPM_PREC_MIXED)
     TPM_LAUNCH(c, "particle_push", (k_push<float, float>), pblocks(c->np), kThreads, 0, c->g,
-               pstate(c, np1_in_base), a, c->np, c->U32, c->Tgas32, c->rhs_t, c->tau, c->key_t,
+               pstate(c, np1_in_base), a, c->np, c->U32, c->Tgas, c->rhs_t, c->tau, c->key_t,
                reinterpret_cast<float *>(c->pay_t), c->key_r, c->pay_r);
   else
     TPM_LAUNCH(c, "particle_push", (k_push<double, double>), pblocks(c->np), kThreads, 0, c->g,
