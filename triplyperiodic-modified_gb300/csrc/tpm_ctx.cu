@@ -325,20 +325,17 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->key_r = dalloc<int32_t>(c, np);
     c->perm_t = dalloc<int32_t>(c, np);
     c->perm_r[0] = dalloc<int32_t>(c, np);
-    c->perm_r[1] = dalloc<int32_t>(c, np);
     c->starts_t = dalloc<int32_t>(c, n + 1);
     c->starts_r[0] = dalloc<int32_t>(c, n + 1);
-    c->starts_r[1] = dalloc<int32_t>(c, n + 1);
     c->counts = dalloc<int32_t>(c, n);
     c->scan_blocks = dalloc<int32_t>(c, (size_t)(n / 4096 + 2));
     c->pay_t = dalloc<double>(c, 6 * (size_t)np);
     c->pay_t_s = dalloc<double>(c, 6 * (size_t)np);
     c->pay_r = dalloc<double>(c, 4 * (size_t)np);
-    c->pay_r_s[0] = dalloc<double>(c, 4 * (size_t)np);
-    c->pay_r_s[1] = dalloc<double>(c, 4 * (size_t)np);
-    c->w8 = dalloc<double>(c, 8 * (size_t)np);
+    c->w8 = dalloc<double>(c, 16 * (size_t)np);
+    c->C_next = dalloc<double>(c, n);
+    TPM_CUDA_TRY(cudaMemsetAsync(c->C_next, 0, sizeof(double) * n, c->stream));
     TPM_CUDA_TRY(cudaMemsetAsync(c->starts_r[0], 0, sizeof(int32_t) * (n + 1), c->stream));
-    TPM_CUDA_TRY(cudaMemsetAsync(c->starts_r[1], 0, sizeof(int32_t) * (n + 1), c->stream));
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return TPM_OK;
   });

@@ -360,8 +360,9 @@ __global__ void k_finish_max(const double *__restrict__ partials, int nparts, De
   if (threadIdx.x == 0) s->err = m;
 }
 
-int pens_for(int n) {
-  int p = kFftSmemPoints / n;
+// pencils per block: two ping-pong buffers of 32 KB each
+int pens_for(int n, int elem_bytes = 16) {
+  int p = (kFftSmemPoints * 16 / elem_bytes) / n;
   if (p < 1) p = 1;
   if (p > 32) p = 32;
   return p;
@@ -458,6 +459,10 @@ void fft_plans_create(tpm_ctx *c) {
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_fft_y<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_fft_z_solve<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_xinv_update<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_xfwd_resid<float2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_fft_y<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_fft_z_solve<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_xinv_update<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
 }
 
 // One Richardson iteration of poisson::FFT (poisson.cpp:397-409).  Inputs:
@@ -468,6 +473,7 @@ void fft_plans_create(tpm_ctx *c) {
 // iterative refinement: FP64 residual, FP32 correction, FP64 update).
 template <typename T2>
 static void poisson_iteration_t(tpm_ctx *c) {
+  auto pens_for = [](int n) { return tpm::pens_for(n, (int)sizeof(T2)); };
   const Grid &g = c->g;
   const long long nrows = (long long)g.ny * g.nz;
   T2 *spec = reinterpret_cast<T2 *>(c->spec);

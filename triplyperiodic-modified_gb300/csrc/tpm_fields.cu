@@ -326,24 +326,41 @@ __global__ void k_rho_update_mixed(Grid g, const double *__restrict__ RUi,
   }
 }
 
-// k_poisson_rhs of the mixed path.  The right-hand side is FP64 (it feeds the
-// FP64 residual of the refinement).  The face coefficients C = 1/Rho_face
-// come from an FP32 seed and one FP64 Newton step (~1e-14 relative; an FP32
-// C would perturb the divergence constraint at 1e-7, which the nearly
-// divergence-free right-hand side amplifies in P).  The preconditioner scale
-// cc is FP32: it sets the rate of the Richardson iteration, not its fixed
-// point.  Cs = C/d^2 feeds the residual.
-__global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ Rho_new,
-                                    const double *__restrict__ inv_rho, const double *__restrict__ Q,
-                                    const double *__restrict__ RUn, const DevScalars *__restrict__ s,
-                                    double *__restrict__ RHS, double *__restrict__ divg,
-                                    double *__restrict__ Cface, double *__restrict__ Cs,
-                                    double *__restrict__ cc, double *__restrict__ partials,
-                                    PoisArgs a) {
+// Face coefficients of the mixed path, C = 1/Rho_face(Rho_new) on the three
+// lower faces of each cell (each face once), from an FP32 seed and one FP64
+// Newton step (~1e-14 relative; an FP32 C would perturb the divergence
+// constraint at 1e-7, which the nearly divergence-free right-hand side
+// amplifies in P).  Cs = C/d^2 feeds the FP64 residual of the refinement.
+__global__ void k_face_coeff_mixed(Grid g, const double *__restrict__ Rho_new,
+                                   double *__restrict__ Cface, double *__restrict__ Cs) {
+  const double inv_d2[3] = {g.inv_dx2, g.inv_dy2, g.inv_dz2};
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    Nbr nb = nbr_of(g, q);
+    const double r = Rho_new[c];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double clo = rcp64_1((r + Rho_new[nb.m[d]]) * 0.5);
+      Cface[d * g.n + c] = clo;
+      Cs[d * g.n + c] = clo * inv_d2[d];
+    }
+  }
+}
+
+// k_poisson_rhs of the mixed path: FP64 right-hand side (it feeds the FP64
+// residual), U = RU*C with the face coefficients above; the preconditioner
+// scale cc is FP32 (it sets the rate of the Richardson iteration, not its
+// fixed point).
+__global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
+                                    const double *__restrict__ Q, const double *__restrict__ RUn,
+                                    const double *__restrict__ Cface,
+                                    const DevScalars *__restrict__ s, double *__restrict__ RHS,
+                                    double *__restrict__ divg, double *__restrict__ cc,
+                                    double *__restrict__ partials, PoisArgs a) {
   __shared__ double sh[kThreads];
   const double coef = s->coef_div, meanQ = s->mean_Q;
   const double inv_d[3] = {g.inv_dx, g.inv_dy, g.inv_dz};
-  const double inv_d2[3] = {g.inv_dx2, g.inv_dy2, g.inv_dz2};
   double acc = 0;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
@@ -356,17 +373,13 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ Rho_new,
     double Qc = a.cooling ? Q[c] - meanQ : Q[c];
     double dv = a.kCp * lap + coef * Qc;
     divg[c] = dv;
-    const double r = Rho_new[c];
     double t[3];
     float msum = 0.f;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const double clo = rcp64_1((r + Rho_new[nb.m[d]]) * 0.5);
-      const double chi = rcp64_1((Rho_new[nb.p[d]] + r) * 0.5);
+      const double clo = Cface[d * g.n + c], chi = Cface[d * g.n + nb.p[d]];
       const double *R = RUn + d * g.n;
       t[d] = (R[nb.p[d]] * chi - R[c] * clo) * inv_d[d];
-      Cface[d * g.n + c] = clo;
-      Cs[d * g.n + c] = clo * inv_d2[d];
       msum += ((float)clo + (float)chi) * 0.5f;
     }
     double rhs = (t[0] + t[1] + t[2] - dv) * a.inv_dtpre;
@@ -599,11 +612,13 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
   a.cooling = c->p.cooling;
   a.store_div = store_div;
   int nb = cell_blocks(c->g);
-  if (c->p.precision == TPM_PREC_MIXED)
-    TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_mixed, nb, kThreads, 0, c->g, c->Rho_new,
-               c->inv_rho, c->Q, c->RU_new, c->dsc, c->RHS, c->divg, c->Cface, c->Cs, c->cc,
+  if (c->p.precision == TPM_PREC_MIXED) {
+    TPM_LAUNCH(c, "face_coeff", k_face_coeff_mixed, nb, kThreads, 0, c->g, c->Rho_new, c->Cface,
+               c->Cs);
+    TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_mixed, nb, kThreads, 0, c->g, c->inv_rho, c->Q,
+               c->RU_new, c->Cface, c->dsc, c->RHS, c->divg, c->cc,
                c->partials + kPartRhs * kRedBlocks, a);
-  else
+  } else
   TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs, nb, kThreads, 0, c->g, c->Rho_new, c->inv_rho,
              c->Q, c->RU_new, c->dsc, c->RHS, c->divg, c->Cface, c->cc,
              c->partials + kPartRhs * kRedBlocks, a);

@@ -127,14 +127,14 @@ struct tpm_ctx {
   double *rhs_t = nullptr, *tau = nullptr, *tau_buf = nullptr;
   int32_t *flag = nullptr;
   int32_t *key_t = nullptr, *key_r = nullptr;
-  int32_t *perm_t = nullptr, *perm_r[2] = {nullptr, nullptr};
-  int32_t *starts_t = nullptr, *starts_r[2] = {nullptr, nullptr};
+  int32_t *perm_t = nullptr, *perm_r[1] = {nullptr};
+  int32_t *starts_t = nullptr, *starts_r[1] = {nullptr};
   int32_t *counts = nullptr;
   int32_t *scan_blocks = nullptr;
   double *pay_t = nullptr, *pay_t_s = nullptr;          // 6*np
-  double *pay_r = nullptr, *pay_r_s[2] = {nullptr, nullptr};  // 4*np
-  double *w8 = nullptr;  // 8*np corner weights (sorted order)
-  int rcur = 0;  // which r-sorted buffer holds the latest x_new sort
+  double *pay_r = nullptr;  // 4*np: round-indexed fractions and heat rate, unsorted
+  double *w8 = nullptr;  // 16*np corner weights (heat, concentration; sorted order)
+  double *C_next = nullptr;  // concentration at this x_new = next substep's x_int
   int q_parts = 1;  // number of valid partial sums of Q (heat deposit blocks)
 
   bool store_div = false;

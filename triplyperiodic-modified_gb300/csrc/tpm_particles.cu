@@ -143,17 +143,37 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     const int i1 = wrap_any(ri, g.nx), im = wrap_any(ri - 1, g.nx);
     const int j1 = wrap_any(rj, g.ny), jm = wrap_any(rj - 1, g.ny);
     const int k1 = wrap_any(rk, g.nz), km = wrap_any(rk - 1, g.nz);
-    // FP64 on both paths: the heat rate is a difference of nearly equal
-    // temperatures, which amplifies any rounding of Tg
-    const double Tg = x_l * y_l * z_l * Tgas[at(g, i1, j1, k1)] +
-                      (1 - x_l) * y_l * z_l * Tgas[at(g, im, j1, k1)] +
-                      x_l * (1 - y_l) * z_l * Tgas[at(g, i1, jm, k1)] +
-                      x_l * y_l * (1 - z_l) * Tgas[at(g, i1, j1, km)] +
-                      (1 - x_l) * (1 - y_l) * z_l * Tgas[at(g, im, jm, k1)] +
-                      (1 - x_l) * y_l * (1 - z_l) * Tgas[at(g, im, j1, km)] +
-                      x_l * (y_l - 1) * (z_l - 1) * Tgas[at(g, i1, jm, km)] +
-                      (1 - x_l) * (1 - y_l) * (1 - z_l) * Tgas[at(g, im, jm, km)];
-    const double rt = (Tg - Tnew) * a.iTth;
+    double rt;
+    if (sizeof(TU) == sizeof(double)) {
+      const double Tg = x_l * y_l * z_l * Tgas[at(g, i1, j1, k1)] +
+                        (1 - x_l) * y_l * z_l * Tgas[at(g, im, j1, k1)] +
+                        x_l * (1 - y_l) * z_l * Tgas[at(g, i1, jm, k1)] +
+                        x_l * y_l * (1 - z_l) * Tgas[at(g, i1, j1, km)] +
+                        (1 - x_l) * (1 - y_l) * z_l * Tgas[at(g, im, jm, k1)] +
+                        (1 - x_l) * y_l * (1 - z_l) * Tgas[at(g, im, j1, km)] +
+                        x_l * (y_l - 1) * (z_l - 1) * Tgas[at(g, i1, jm, km)] +
+                        (1 - x_l) * (1 - y_l) * (1 - z_l) * Tgas[at(g, im, jm, km)];
+      rt = (Tg - Tnew) * a.iTth;
+    } else {
+      // mixed path: Tg - T_new = sum_k w_k (T_k - T_new) (the weights sum to
+      // one); the differences are FP64, the small weighted sum FP32, so the
+      // heat rate - a difference of nearly equal temperatures - keeps its
+      // relative accuracy
+      const float xf = (float)x_l, yf = (float)y_l, zf = (float)z_l;
+      const float d0 = (float)(Tgas[at(g, i1, j1, k1)] - Tnew);
+      const float d1 = (float)(Tgas[at(g, im, j1, k1)] - Tnew);
+      const float d2 = (float)(Tgas[at(g, i1, jm, k1)] - Tnew);
+      const float d3 = (float)(Tgas[at(g, i1, j1, km)] - Tnew);
+      const float d4 = (float)(Tgas[at(g, im, jm, k1)] - Tnew);
+      const float d5 = (float)(Tgas[at(g, im, j1, km)] - Tnew);
+      const float d6 = (float)(Tgas[at(g, i1, jm, km)] - Tnew);
+      const float d7 = (float)(Tgas[at(g, im, jm, km)] - Tnew);
+      const float sum = xf * yf * zf * d0 + (1 - xf) * yf * zf * d1 + xf * (1 - yf) * zf * d2 +
+                        xf * yf * (1 - zf) * d3 + (1 - xf) * (1 - yf) * zf * d4 +
+                        (1 - xf) * yf * (1 - zf) * d5 + xf * (1 - yf) * (1 - zf) * d6 +
+                        (1 - xf) * (1 - yf) * (1 - zf) * d7;
+      rt = (double)sum * a.iTth;
+    }
     rhs_t[p] = rt;
     key_r[p] = (int32_t)at(g, i1, j1, k1);
     pay_r[0 * np + p] = x_l;
@@ -372,21 +392,25 @@ __global__ void k_dep_momentum(Grid g, const int32_t *__restrict__ starts,
   }
 }
 
-// part2gas_concentration (particle.cpp:522-555) and part2gas_Temp_* (:582-654).
-// Corner weights of the round-indexed linear stencil, once per particle in
-// sorted order (every lane busy): w[d][s] for d = (dz*2+dy)*2+dx is the
-// contribution of sorted particle s to the centre (its round cell) - (dx,dy,dz),
-// ((fx*fy)*fz)*rhs with fx = xl for dx = 0 and 1-xl for dx = 1 - the operation
-// order of particle.cpp:545-552 / :605-612 / :643-650.  TW is the weight type
-// (double on the FP64 path, float on the mixed path).
+// part2gas_concentration (particle.cpp:522-555) and part2gas_Temp_* (:582-654):
+// ((fx*fy)*fz)*rhs with fx = xl for the centre at the round cell and 1-xl for
+// the one below (the operation order of particle.cpp:545-552, :605-612,
+// :643-650).
+// Both linear-stencil deposits of one sorted particle set in one pass: the
+// heat rate (weights x RHS_T) for this substep and the concentration
+// (weights) that the next substep deposits at the same positions (its x_int
+// is this x_new).  Weights are built per sorted slot from the unsorted
+// payload; the sums keep the order of k_dep_sum8.
 template <typename TW>
-__global__ void k_cic_weights(int64_t np, const double *__restrict__ pay, int with_rhs,
-                              TW *__restrict__ w) {
+__global__ void k_cic_weights2(int64_t np, const int32_t *__restrict__ perm,
+                               const double *__restrict__ pay, TW *__restrict__ wq,
+                               TW *__restrict__ wc) {
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < np;
        s += (int64_t)gridDim.x * blockDim.x) {
-    const TW xl = (TW)pay[s], yl = (TW)pay[np + s], zl = (TW)pay[2 * np + s];
+    const int32_t p = perm[s];
+    const TW xl = (TW)pay[p], yl = (TW)pay[np + p], zl = (TW)pay[2 * np + p];
+    const TW r = (TW)pay[3 * np + p];
     const TW fx[2] = {xl, 1 - xl}, fy[2] = {yl, 1 - yl}, fz[2] = {zl, 1 - zl};
-    const TW r = with_rhs ? (TW)pay[3 * np + s] : (TW)1;
 #pragma unroll
     for (int dy = 0; dy < 2; ++dy)
 #pragma unroll
@@ -394,19 +418,19 @@ __global__ void k_cic_weights(int64_t np, const double *__restrict__ pay, int wi
         const TW fxy = fx[dx] * fy[dy];
 #pragma unroll
         for (int dz = 0; dz < 2; ++dz) {
-          TW v = fxy * fz[dz];
-          if (with_rhs) v = v * r;
-          w[(size_t)((dz * 2 + dy) * 2 + dx) * np + s] = v;
+          const size_t o = (size_t)((dz * 2 + dy) * 2 + dx) * np + s;
+          const TW v = fxy * fz[dz];
+          wc[o] = v;
+          wq[o] = v * r;
         }
       }
   }
 }
 
-// centre c sums, in a fixed order, the corner weights of the particles whose
-// round cell is c + (dx,dy,dz) (cumulative ghost fold included)
 template <typename TW>
-__global__ void k_dep_sum8(Grid g, const int32_t *__restrict__ starts, const TW *__restrict__ w,
-                           int64_t np, double *__restrict__ out, double *__restrict__ partials) {
+__global__ void k_dep_sum8x2(Grid g, const int32_t *__restrict__ starts, const TW *__restrict__ wq,
+                             const TW *__restrict__ wc, int64_t np, double *__restrict__ Q,
+                             double *__restrict__ C, double *__restrict__ partials) {
   __shared__ double sh[32];
   double bsum = 0;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
@@ -414,7 +438,7 @@ __global__ void k_dep_sum8(Grid g, const int32_t *__restrict__ starts, const TW 
     const int i = (int)(c % g.nx);
     const long long t = c / g.nx;
     const int j = (int)(t % g.ny), k = (int)(t / g.ny);
-    TW acc = 0;
+    TW aq = 0, ac = 0;
 #pragma unroll
     for (int dz = 0; dz < 2; ++dz)
 #pragma unroll
@@ -423,17 +447,19 @@ __global__ void k_dep_sum8(Grid g, const int32_t *__restrict__ starts, const TW 
         for (int dx = 0; dx < 2; ++dx) {
           const long long r = at(g, dx ? wrap_p(i, g.nx) : i, dy ? wrap_p(j, g.ny) : j,
                                  dz ? wrap_p(k, g.nz) : k);
-          const TW *wd = w + (size_t)((dz * 2 + dy) * 2 + dx) * np;
+          const size_t o = (size_t)((dz * 2 + dy) * 2 + dx) * np;
           const int32_t s0 = starts[r], e0 = starts[r + 1];
-          for (int32_t s = s0; s < e0; ++s) acc += wd[s];
+          for (int32_t s = s0; s < e0; ++s) {
+            aq += wq[o + s];
+            ac += wc[o + s];
+          }
         }
-    out[c] = (double)acc;
-    bsum += (double)acc;
+    Q[c] = (double)aq;
+    C[c] = (double)ac;
+    bsum += (double)aq;
   }
-  if (partials) {
-    double b = block_sum(bsum, sh);
-    if (threadIdx.x == 0) partials[blockIdx.x] = b;
-  }
+  double b = block_sum(bsum, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = b;
 }
 
 int pblocks(int64_t np) {
@@ -527,45 +553,35 @@ void particle_deposit_momentum(tpm_ctx *c) {
   }
 }
 
-static void cic_deposit(tpm_ctx *c, int buf, bool with_rhs, double *out, double *partials,
-                        const char *tag);
-
-// concentration at x_int (grid.cpp:876) from the round-indexed sort of the
-// previous x_new (= this x_int)
+// concentration at x_int (grid.cpp:876): the previous substep's heat deposit
+// (or the initial one) already summed it at these positions
 void particle_deposit_concentration(tpm_ctx *c) {
   if (c->np == 0) {
     TPM_CUDA_TRY(cudaMemsetAsync(c->C, 0, sizeof(double) * c->g.n, c->stream));
     return;
   }
-  cic_deposit(c, c->rcur, false, c->C, nullptr, "conc");
+  std::swap(c->C, c->C_next);
 }
 
-// linear-stencil deposit from the sorted payload of r-sort buffer `buf`
-static void cic_deposit(tpm_ctx *c, int buf, bool with_rhs, double *out, double *partials,
-                        const char *tag) {
-  const bool mixed = c->p.precision == TPM_PREC_MIXED;
+// sort the round-indexed keys in c->key_r and deposit the heat rate into Q
+// and the concentration of these positions into C_next
+static void heat_deposit(tpm_ctx *c) {
   const int nb = cell_blocks(c->g);
-  if (mixed) {
-    float *w = reinterpret_cast<float *>(c->w8);
-    TPM_LAUNCH(c, with_rhs ? "weights_heat" : "weights_conc", k_cic_weights<float>,
-               pblocks(c->np), kThreads, 0, c->np, c->pay_r_s[buf], (int)with_rhs, w);
-    TPM_LAUNCH(c, with_rhs ? "deposit_heat" : "deposit_conc", k_dep_sum8<float>, nb, kThreads, 0,
-               c->g, c->starts_r[buf], w, c->np, out, partials);
+  sort_by_cell(c, c->key_r, c->perm_r[0], c->starts_r[0]);
+  double *parts = c->partials + kPartQ * kRedBlocks;
+  if (c->p.precision == TPM_PREC_MIXED) {
+    float *wq = reinterpret_cast<float *>(c->w8), *wc = wq + 8 * (size_t)c->np;
+    TPM_LAUNCH(c, "cic_weights", k_cic_weights2<float>, pblocks(c->np), kThreads, 0, c->np,
+               c->perm_r[0], c->pay_r, wq, wc);
+    TPM_LAUNCH(c, "deposit_heat_conc", k_dep_sum8x2<float>, nb, kThreads, 0, c->g,
+               c->starts_r[0], wq, wc, c->np, c->Q, c->C_next, parts);
   } else {
-    TPM_LAUNCH(c, with_rhs ? "weights_heat" : "weights_conc", k_cic_weights<double>,
-               pblocks(c->np), kThreads, 0, c->np, c->pay_r_s[buf], (int)with_rhs, c->w8);
-    TPM_LAUNCH(c, with_rhs ? "deposit_heat" : "deposit_conc", k_dep_sum8<double>, nb, kThreads, 0,
-               c->g, c->starts_r[buf], c->w8, c->np, out, partials);
+    double *wq = c->w8, *wc = wq + 8 * (size_t)c->np;
+    TPM_LAUNCH(c, "cic_weights", k_cic_weights2<double>, pblocks(c->np), kThreads, 0, c->np,
+               c->perm_r[0], c->pay_r, wq, wc);
+    TPM_LAUNCH(c, "deposit_heat_conc", k_dep_sum8x2<double>, nb, kThreads, 0, c->g,
+               c->starts_r[0], wq, wc, c->np, c->Q, c->C_next, parts);
   }
-  (void)tag;
-}
-
-static void heat_deposit_from(tpm_ctx *c, int buf) {
-  int nb = cell_blocks(c->g);
-  sort_by_cell(c, c->key_r, c->perm_r[buf], c->starts_r[buf]);
-  TPM_LAUNCH(c, "payload_gather_r", k_gather_payload<double>, pblocks(c->np), kThreads, 0, c->np, 4,
-             c->perm_r[buf], c->pay_r, c->pay_r_s[buf]);
-  cic_deposit(c, buf, true, c->Q, c->partials + kPartQ * kRedBlocks, "heat");
   c->q_parts = nb;
 }
 
@@ -577,14 +593,11 @@ void particle_heat(tpm_ctx *c) {
                                  c->stream));
     return;
   }
-  int buf = 1 - c->rcur;
-  heat_deposit_from(c, buf);
-  c->rcur = buf;
+  heat_deposit(c);
 }
 
 // grid::Initialize tail (grid.cpp:481-484): T = (P0_int/R)/Rho_int, heat rate
-// at x_int and its deposit; also leaves the round-indexed sort of x_int for
-// the first concentration deposit.
+// at x_int and its deposit, plus the concentration at x_int for stage 0.
 void particle_init_heat(tpm_ctx *c) {
   TPM_LAUNCH(c, "fill_tgas", k_fill_tgas, cell_blocks(c->g), kThreads, 0, c->g.n, c->Rho_int,
              c->hsc->P0_int / c->R, c->Tgas);
@@ -598,26 +611,24 @@ void particle_init_heat(tpm_ctx *c) {
   TPM_LAUNCH(c, "cic_payload", k_cic_payload, pblocks(c->np), kThreads, 0, c->g, c->pq[1][0],
              c->pq[1][1], c->pq[1][2], c->pq[1][6], c->Tgas, iTth, c->np, c->rhs_t, c->key_r,
              c->pay_r, 1);
-  c->rcur = 0;
-  heat_deposit_from(c, 0);
+  heat_deposit(c);
 }
 
-// Continuation from a caller-held state: rebuild the round-indexed sort of
-// x_int (first concentration deposit) from the given heat rates, and the
-// partial sums of the given RHS_Part_Temp (first Update_P0).
+// Continuation from a caller-held state: the given heat rates at x_int give
+// back the caller's RHS_Part_Temp (same sums, same order) and the
+// concentration for the first substep.
 void particle_resume(tpm_ctx *c) {
   int nb = cell_blocks(c->g);
-  TPM_LAUNCH(c, "partial_sums", k_partial_sums, nb, kThreads, 0, c->g.n, c->Q,
-             c->partials + kPartQ * kRedBlocks);
-  c->q_parts = nb;
-  c->rcur = 0;
-  if (c->np == 0) return;
+  if (c->np == 0) {
+    TPM_LAUNCH(c, "partial_sums", k_partial_sums, nb, kThreads, 0, c->g.n, c->Q,
+               c->partials + kPartQ * kRedBlocks);
+    c->q_parts = nb;
+    return;
+  }
   TPM_LAUNCH(c, "cic_payload", k_cic_payload, pblocks(c->np), kThreads, 0, c->g, c->pq[1][0],
              c->pq[1][1], c->pq[1][2], c->pq[1][6], c->Tgas, 0.0, c->np, c->rhs_t, c->key_r,
              c->pay_r, 0);
-  sort_by_cell(c, c->key_r, c->perm_r[0], c->starts_r[0]);
-  TPM_LAUNCH(c, "payload_gather_r", k_gather_payload<double>, pblocks(c->np), kThreads, 0, c->np, 4,
-             c->perm_r[0], c->pay_r, c->pay_r_s[0]);
+  heat_deposit(c);
 }
 
 void particle_zero_fields(tpm_ctx *c) {
