@@ -473,7 +473,6 @@ void fft_plans_create(tpm_ctx *c) {
 // iterative refinement: FP64 residual, FP32 correction, FP64 update).
 template <typename T2>
 static void poisson_iteration_t(tpm_ctx *c) {
-  auto pens_for = [](int n) { return tpm::pens_for(n, (int)sizeof(T2)); };
   const Grid &g = c->g;
   const long long nrows = (long long)g.ny * g.nz;
   T2 *spec = reinterpret_cast<T2 *>(c->spec);
