@@ -310,6 +310,7 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->hsc->P0 = c->hsc->P0_int = c->hsc->P0_np1 = c->hsc->P0_new = c->P0ref;
     push_scalars(c);
     tpm::fft_plans_create(c);
+    tpm::rhs_kernels_setup();
     c->x_blocks = tpm::fft_x_blocks(c);
     c->err_parts = dalloc<double>(c, c->x_blocks);
     // particles

@@ -213,6 +213,114 @@ __global__ void k_rhs_momentum(Grid g, const TIn *__restrict__ U, const TIn *__r
   }
 }
 
+// Tiled form of k_rhs_momentum: one block owns a TX x TY x TZ tile; U and
+// RU_int of the tile plus a one-cell halo are staged in shared memory, the
+// divergence of U and the nine convective fluxes P_{d,e} are evaluated once
+// per cell of the tile (the untiled kernel re-evaluates them 4x and 2x), then
+// each thread assembles its cell.  Every value keeps its operation order, so
+// the results are bit-identical to the untiled kernel.
+constexpr int kTX = 32, kTY = 4, kTZ = 2;
+constexpr int kBX = kTX + 2, kBY = kTY + 2, kBZ = kTZ + 2;  // staged box
+constexpr int kFX = kTX + 1, kFY = kTY + 1, kFZ = kTZ + 1;  // divergence / flux boxes
+constexpr int kBox = kBX * kBY * kBZ, kFBox = kFX * kFY * kFZ;
+
+template <typename TC>
+constexpr size_t rhs_tiled_smem() {
+  return sizeof(TC) * (6 * (size_t)kBox + (size_t)kFBox + 9 * (size_t)kFBox);
+}
+
+template <typename TC, typename TIn>
+__global__ void __launch_bounds__(kTX * kTY * kTZ)
+k_rhs_momentum_tiled(Grid g, const TIn *__restrict__ U, const TIn *__restrict__ RUi,
+                     const TIn *__restrict__ Fp, const double *__restrict__ Rho_int,
+                     const double *__restrict__ RU, const double *__restrict__ np1_in,
+                     double *__restrict__ RU_np1, double *__restrict__ RU_new, RhsArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TC *sU = reinterpret_cast<TC *>(smem_raw);  // [3][kBox]
+  TC *sR = sU + 3 * kBox;                      // [3][kBox]
+  TC *sD = sR + 3 * kBox;                      // [kFBox] divergence, box coords 0..T
+  TC *sP = sD + kFBox;                         // [9][kFBox] fluxes, box coords 1..T+1
+  const int tilesx = (g.nx + kTX - 1) / kTX, tilesy = (g.ny + kTY - 1) / kTY;
+  const int bx = blockIdx.x % tilesx, by = (blockIdx.x / tilesx) % tilesy,
+            bz = blockIdx.x / (tilesx * tilesy);
+  const int i0 = bx * kTX, j0 = by * kTY, k0 = bz * kTZ;
+  const int t = threadIdx.x;
+  const TC inv_d[3] = {(TC)g.inv_dx, (TC)g.inv_dy, (TC)g.inv_dz};
+  const TC inv_d2[3] = {(TC)g.inv_dx2, (TC)g.inv_dy2, (TC)g.inv_dz2};
+  // ---- stage U and RU_int with a one-cell periodic halo
+  for (int b = t; b < kBox; b += blockDim.x) {
+    const int xb = b % kBX, yb = (b / kBX) % kBY, zb = b / (kBX * kBY);
+    const int i = wrap_any(i0 + xb - 1, g.nx), j = wrap_any(j0 + yb - 1, g.ny),
+              k = wrap_any(k0 + zb - 1, g.nz);
+    const long long c = at(g, i, j, k);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      sU[d * kBox + b] = (TC)U[d * g.n + c];
+      sR[d * kBox + b] = (TC)RUi[d * g.n + c];
+    }
+  }
+  __syncthreads();
+  auto B = [](int x, int y, int z) { return (z * kBY + y) * kBX + x; };
+  // ---- divergence of U at box cells 0..T (tile-relative -1..T-1)
+  for (int f = t; f < kFBox; f += blockDim.x) {
+    const int x = f % kFX, y = (f / kFX) % kFY, z = f / (kFX * kFY);
+    const int b = B(x, y, z);
+    sD[f] = (sU[b + 1] - sU[b]) * inv_d[0] + (sU[kBox + b + kBX] - sU[kBox + b]) * inv_d[1] +
+            (sU[2 * kBox + b + kBX * kBY] - sU[2 * kBox + b]) * inv_d[2];
+  }
+  // ---- convective fluxes P_{d,e} = I_e(U_d) * I_d(RU_e) at box cells 1..T+1
+  const int off[3] = {1, kBX, kBX * kBY};
+  for (int f = t; f < 9 * kFBox; f += blockDim.x) {
+    const int de = f / kFBox, r = f % kFBox;
+    const int d = de / 3, e = de % 3;
+    const int x = r % kFX + 1, y = (r / kFX) % kFY + 1, z = r / (kFX * kFY) + 1;
+    const int b = B(x, y, z);
+    const TC iu = (sU[d * kBox + b] + sU[d * kBox + b - off[e]]) * (TC)0.5;
+    const TC ir = (sR[e * kBox + b] + sR[e * kBox + b - off[d]]) * (TC)0.5;
+    sP[f] = iu * ir;
+  }
+  __syncthreads();
+  // ---- assemble each cell of the tile
+  const int rx = t % kTX, ry = (t / kTX) % kTY, rz = t / (kTX * kTY);
+  const int i = i0 + rx, j = j0 + ry, k = k0 + rz;
+  if (i >= g.nx || j >= g.ny || k >= g.nz) return;
+  const long long c = at(g, i, j, k);
+  const int b = B(rx + 1, ry + 1, rz + 1);
+  const int fb = (rz + 1) * kFX * kFY + (ry + 1) * kFX + (rx + 1);  // divergence index of the cell
+  const int fp = rz * kFX * kFY + ry * kFX + rx;                    // flux index of the cell
+  const int foff[3] = {1, kFX, kFX * kFY};
+  const TC div_c = sD[fb];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const TC *Ud = sU + d * kBox;
+    TC gd = (div_c - sD[fb - foff[d]]) * inv_d[d];
+    TC ud = Ud[b];
+    TC lap = (Ud[b + off[0]] - 2 * ud + Ud[b - off[0]]) * inv_d2[0] +
+             (Ud[b + off[1]] - 2 * ud + Ud[b - off[1]]) * inv_d2[1] +
+             (Ud[b + off[2]] - 2 * ud + Ud[b - off[2]]) * inv_d2[2];
+    TC rhs = (TC)a.a_fp * (TC)Fp[d * g.n + c] + (TC)a.b_gd * gd + (TC)a.c_lap * lap;
+    TC tt[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+      const TC *Pde = sP + (d * 3 + e) * kFBox;
+      tt[e] = (Pde[fp + foff[e]] - Pde[fp]) * inv_d[e];
+    }
+    rhs -= tt[0] + tt[1] + tt[2];
+    rhs += (TC)a.A * sR[d * kBox + b];
+    if (a.has_g) {
+      const long long cm = d == 0 ? at(g, wrap_m(i, g.nx), j, k)
+                           : d == 1 ? at(g, i, wrap_m(j, g.ny), k)
+                                    : at(g, i, j, wrap_m(k, g.nz));
+      TC rf = ((TC)Rho_int[c] + (TC)Rho_int[cm]) * (TC)0.5;
+      rhs += (rf - (TC)a.Rho0) * (TC)a.g[d];
+    }
+    const double r64 = (double)rhs;
+    double np1 = np1_in[d * g.n + c] + a.dtpo * r64;
+    RU_np1[d * g.n + c] = np1;
+    RU_new[d * g.n + c] = (a.stage != 3) ? 1 * RU[d * g.n + c] + a.dtpr * r64 : np1;
+  }
+}
+
 // ---------------------------------------------------- Poisson right side
 // grid::Compute_Div_U_new (grid.cpp:832-839), grid::Compute_RHS_Pois
 // (grid.cpp:841-849) and the coefficient set-up of grid::Solve_Poisson /
@@ -595,14 +703,16 @@ void launch_rhs_momentum(tpm_ctx *c, int s, bool np1_in_base) {
   a.dtpo = c->p.dt * kPost[s];
   a.dtpr = c->p.dt * kPre[s];
   a.stage = s;
+  const int tiles = ((c->g.nx + kTX - 1) / kTX) * ((c->g.ny + kTY - 1) / kTY) *
+                    ((c->g.nz + kTZ - 1) / kTZ);
   if (c->p.precision == TPM_PREC_MIXED)
-    TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum<float, float>), cell_blocks(c->g), kThreads, 0,
-               c->g, c->U32, c->RUi32, c->Fp32, c->Rho_int, c->RU,
+    TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum_tiled<float, float>), tiles, kTX * kTY * kTZ,
+               rhs_tiled_smem<float>(), c->g, c->U32, c->RUi32, c->Fp32, c->Rho_int, c->RU,
                np1_in_base ? c->RU : c->RU_np1, c->RU_np1, c->RU_new, a);
   else
-    TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum<double, double>), cell_blocks(c->g), kThreads, 0, c->g,
-               c->U, c->RU_int, c->Fp, c->Rho_int, c->RU, np1_in_base ? c->RU : c->RU_np1,
-               c->RU_np1, c->RU_new, a);
+    TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum_tiled<double, double>), tiles,
+               kTX * kTY * kTZ, rhs_tiled_smem<double>(), c->g, c->U, c->RU_int, c->Fp,
+               c->Rho_int, c->RU, np1_in_base ? c->RU : c->RU_np1, c->RU_np1, c->RU_new, a);
 }
 
 void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
@@ -652,6 +762,15 @@ void launch_to_float(tpm_ctx *c, const double *src, float *dst, long long n) {
 
 void launch_to_double(tpm_ctx *c, const float *src, double *dst, long long n) {
   TPM_LAUNCH(c, "to_double", k_to_double, cell_blocks(c->g), kThreads, 0, src, dst, n);
+}
+
+void rhs_kernels_setup() {
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_rhs_momentum_tiled<double, double>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)rhs_tiled_smem<double>()));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_rhs_momentum_tiled<float, float>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)rhs_tiled_smem<float>()));
 }
 
 void launch_mean_reset(tpm_ctx *c) {

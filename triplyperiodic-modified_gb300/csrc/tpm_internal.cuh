@@ -157,6 +157,7 @@ void launch_p0_update(tpm_ctx *c, int stage);
 void launch_rho_update(tpm_ctx *c, int stage, bool np1_in_base);
 void launch_face_velocity(tpm_ctx *c);
 void launch_rhs_momentum(tpm_ctx *c, int stage, bool np1_in_base);
+void rhs_kernels_setup();
 void launch_poisson_rhs(tpm_ctx *c, int stage, bool store_div);
 void launch_project(tpm_ctx *c, int stage);
 void launch_div_residual(tpm_ctx *c, int stage);
