@@ -240,6 +240,23 @@ def cpu_baseline_port(workload):
                       f"reference"}
 
 
+def max_over_ranks(x, dist, device="cpu"):
+    """Max of a per-rank float over the job (the slowest rank sets the time)."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, ncell, steps, max_ms):
+    """Replicas: every rank advances its own box of `ncell` cells `steps` times;
+    the job's rate is all ranks' cell-steps over the slowest rank's time."""
+    return world * ncell * steps / (max_ms * 1e-3) / 1e6
+
+
 def kernel_bytes(name, ncell, npart, mixed):
     bc, bp = KERNEL_BYTES.get(name, (0, 0))
     if mixed:  # complex64 spectrum on the mixed path
@@ -266,7 +283,7 @@ def path_result(p, s, ms, steps, world, n_it, launches, prof, clocks, mixed, pea
     sgbs = sb / (ms_per_step * 1e-3) / 1e9
     total_prof = sum(v[1] for v in prof.values())
     return {
-        "value": world * p.ncell * steps / (ms * 1e-3) / 1e6,
+        "value": whole_job_rate(world, p.ncell, steps, ms),
         "ms_per_step": ms_per_step, "n_it": n_it, "launches": launches, "clocks": clocks,
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
@@ -303,10 +320,7 @@ def gpu_main(args):
         p = p64.replace(precision=P.PREC_MIXED if name == "mixed" else P.PREC_FP64)
         ctx, ms, n_it, launches, prof, clocks = time_gpu(p, s, args.steps, args.warmup, dist,
                                                          local)
-        if dist:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(ms, dist, "cuda")
         res[name] = path_result(p, s, ms, args.steps, world, n_it, launches, prof, clocks,
                                 name == "mixed", peak)
         ctxs[name] = ctx
@@ -328,11 +342,8 @@ def gpu_main(args):
         ctxs["fp64"].close()
     hctx = ctxs[head]
     e2e_ms, h2d, d2h = time_e2e(hctx, max(1, min(args.steps, 3)))
-    if dist:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * p64.ncell / (e2e_ms * 1e-3) / 1e6
+    e2e_ms = max_over_ranks(e2e_ms, dist, "cuda")
+    e2e_value = whole_job_rate(world, p64.ncell, 1, e2e_ms)
     r = res[head]
     line = {
         "metric": METRIC, "value": round(r["value"], 3), "unit": UNIT, "n_gpus": world,

@@ -153,6 +153,20 @@ int tpm_set_particle_tau(tpm_ctx *ctx, const double *tau);
 int tpm_set_scalars(tpm_ctx *ctx, double P0, double T_cur, int64_t num_timestep);
 int tpm_get_scalars(tpm_ctx *ctx, tpm_scalars *out);
 
+/* Restart files in the reference's format, the set its Initial=1 branch reads
+ * (grid.cpp:221-238, particle.cpp:939-989): Restart_RU.bin, Restart_Rho.bin,
+ * Restart_P.bin (raw FP64, [Nz][Ny][Nx], RU as x,y,z blocks),
+ * Restart_Part_{x,y,z,u,v,w,T}.bin (FP64), Restart_Part_flag.bin (int32) and
+ * Restart_numbers.dat ("P0 T_cur num_timestep").  tpm_write_restart writes the
+ * current base state; tpm_read_restart uploads one, after which tpm_initialize
+ * does what the reference does after reading it. */
+int tpm_write_restart(tpm_ctx *ctx, const char *dir);
+int tpm_read_restart(tpm_ctx *ctx, const char *dir);
+/* The dumps of grid::Store / particle::Store_All (grid.cpp:525-592,
+ * particle.cpp:848-897) at the current step n: RU_<n>.bin, Rho_<n>.bin, P_<n>.bin,
+ * Part_{x,y,z,u,v,w,T,flag}_<n>.bin and numbers_<n>.dat. */
+int tpm_store(tpm_ctx *ctx, const char *dir);
+
 /* grid::Initialize tail (grid.cpp:461-484): stage copies, face density and
  * the initial particle heat coupling.  Call after uploading RU, Rho, P,
  * particles and scalars. */

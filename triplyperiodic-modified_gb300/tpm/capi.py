@@ -44,6 +44,9 @@ SIGNATURES = {
     "tpm_upload_particle_rhs_t": (_i, [_vp, _dp]),
     "tpm_set_particle_tau": (_i, [_vp, _dp]),
     "tpm_resume": (_i, [_vp]),
+    "tpm_write_restart": (_i, [_vp, ctypes.c_char_p]),
+    "tpm_read_restart": (_i, [_vp, ctypes.c_char_p]),
+    "tpm_store": (_i, [_vp, ctypes.c_char_p]),
     "tpm_stream": (_vp, [_vp]),
     "tpm_set_scalars": (_i, [_vp, _d, _d, _i64]),
     "tpm_get_scalars": (_i, [_vp, _vp]),
@@ -169,6 +172,15 @@ class Context:
     def upload_rhs_t(self, a):
         a = np.ascontiguousarray(a, dtype=np.float64)
         self._check(self.L.tpm_upload_particle_rhs_t(self.h, _dptr(a)))
+
+    def write_restart(self, dirpath):
+        self._check(self.L.tpm_write_restart(self.h, dirpath.encode()))
+
+    def read_restart(self, dirpath):
+        self._check(self.L.tpm_read_restart(self.h, dirpath.encode()))
+
+    def store(self, dirpath):
+        self._check(self.L.tpm_store(self.h, dirpath.encode()))
 
     def resume(self):
         self._check(self.L.tpm_resume(self.h))
