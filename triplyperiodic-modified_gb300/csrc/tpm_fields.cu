@@ -705,9 +705,11 @@ void launch_rhs_momentum(tpm_ctx *c, int s, bool np1_in_base) {
   a.stage = s;
   const int tiles = ((c->g.nx + kTX - 1) / kTX) * ((c->g.ny + kTY - 1) / kTY) *
                     ((c->g.nz + kTZ - 1) / kTZ);
+  // FP32: the cached per-cell form is faster (6.1 ms tiled vs 4.2 ms per 256^3
+  // step); FP64: the tiled form saves FP64 issue slots (28.7 vs 31.5 ms).
   if (c->p.precision == TPM_PREC_MIXED)
-    TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum_tiled<float, float>), tiles, kTX * kTY * kTZ,
-               rhs_tiled_smem<float>(), c->g, c->U32, c->RUi32, c->Fp32, c->Rho_int, c->RU,
+    TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum<float, float>), cell_blocks(c->g), kThreads, 0,
+               c->g, c->U32, c->RUi32, c->Fp32, c->Rho_int, c->RU,
                np1_in_base ? c->RU : c->RU_np1, c->RU_np1, c->RU_new, a);
   else
     TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum_tiled<double, double>), tiles,
@@ -768,9 +770,6 @@ void rhs_kernels_setup() {
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_rhs_momentum_tiled<double, double>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)rhs_tiled_smem<double>()));
-  TPM_CUDA_TRY(cudaFuncSetAttribute(k_rhs_momentum_tiled<float, float>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)rhs_tiled_smem<float>()));
 }
 
 void launch_mean_reset(tpm_ctx *c) {
