@@ -238,6 +238,55 @@ enum {
 };
 int tpm_set_option(tpm_ctx *ctx, int option, int value);
 
+/* ---------------------------------------------------------------- diagnostics
+ * Statistics of the current step-boundary state, computed on the device.  The
+ * first block is grid::Statistics (grid.cpp:902-940), which the reference calls
+ * after each step (simulation.cpp:92) and writes to <Stat_dir>/<name>.dat; the
+ * names in the comments are those files.  Quantities of the last RK4 stage
+ * (TKE2, HT_mean, num_iteration) are those of the step just taken; before the
+ * first step they are 0.  The second block is not in the reference. */
+typedef struct tpm_stats {
+  double T_cur;
+  int64_t num_timestep;
+  double Rho_mean, Rho_max, Rho_min;  /* Rho_Mean, Rho_Max, Rho_Min */
+  double C_mean, C_max, C_min;        /* C_Mean, C_Max, C_Min */
+  double TKE2;                 /* RU: U.mean_squares() of the stage-3 velocity
+                                  RU_new/Rho_face before projection (grid.cpp:911) */
+  double TKE_U, TKE_V, TKE_W;  /* TKE_U/V/W: mean(RU_d/Rho_face_d * RU_d) */
+  double TKE;                  /* TKE_U + TKE_V + TKE_W (twice the kinetic energy) */
+  double Gas_CFL_Max;          /* Max_CFL_U: max_d max(U_d) dt/d_d, signed max */
+  double Gas_Max_Diff_CFL;     /* dt/(dx^2 Rho_min/Mu0)*6 */
+  double u_max;                /* max over components of max(U_d) */
+  double Vp_max, Tp_max;       /* max of particle u and T (-1e9 with no particles) */
+  double Tp_mean;              /* Tp: mean particle temperature */
+  double HT_mean;              /* HT: mean(RHS_Part_Temp) used by the stage-3 P0 update */
+  double Tg_mean;              /* Tg: mean(P0/R/Rho) */
+  double P0;                   /* P0 */
+  int32_t num_iteration;       /* Num_Iteration: Poisson iterations of the last solve */
+  int32_t reserved;
+  /* not computed by the reference */
+  double C_var;                /* mean(C^2) - mean(C)^2, particle concentration variance */
+  double u_rms;                /* sqrt(mean(u^2+v^2+w^2)/3), u = RU/I_C2F(Rho) */
+  double dissipation;          /* 2 (Mu0/Rho0) <S_ij S_ij>, strain rate from the face
+                                  velocity with the staggered differences */
+} tpm_stats;
+int tpm_statistics(tpm_ctx *ctx, tpm_stats *out);
+
+/* Energy spectrum of the face velocity u = RU/I_C2F(Rho): E[s] is the sum of
+ * |u_hat(k)|^2/2 (u_hat = DFT/(Nx Ny Nz), all three components) over wave
+ * vectors with nint(|k|/dk) = s, dk = min_d 2 pi/L_d, so sum_s E[s] =
+ * mean(u^2+v^2+w^2)/2.  tpm_spectrum_shells gives the number of shells and
+ * dk; tpm_spectrum needs nshells at least that number. */
+int tpm_spectrum_shells(tpm_ctx *ctx, int *nshells, double *dk);
+int tpm_spectrum(tpm_ctx *ctx, double *E, int nshells);
+
+/* Radial distribution function of the base particle positions: pairs[b] is
+ * the number of unordered pairs with minimum-image distance r in
+ * [b dr, (b+1) dr), dr = r_max/nbins; g[b] (optional) is pairs[b] divided by
+ * its ideal-gas expectation Np(Np-1)/2 * (4/3)pi((b+1)^3-b^3)dr^3/(Lx Ly Lz).
+ * r_max must be at most min_d L_d/3. */
+int tpm_rdf(tpm_ctx *ctx, double r_max, int nbins, unsigned long long *pairs, double *g);
+
 /* Per-kernel timing with CUDA events on the context stream (for the bench). */
 int tpm_profile_enable(tpm_ctx *ctx, int on);
 /* Fills names (NUL separated, up to cap bytes), launches and total ms per

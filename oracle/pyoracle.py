@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 sys.path.insert(0, os.path.join(REPO, "triplyperiodic-modified_gb300"))
 
-from tpm.params import Params, TpmScalars  # noqa: E402
+from tpm.params import Params, TpmScalars, TpmStats  # noqa: E402
 from tpm import inputs  # noqa: E402
 
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
@@ -70,6 +70,10 @@ def lib():
         L.orc_step.argtypes = [vp, ip]
         L.orc_poisson_solve.restype = ip
         L.orc_poisson_solve.argtypes = [vp, dp, dp, dp, ip, ctypes.c_double, dp]
+        L.orc_statistics.argtypes = [vp, vp]
+        L.orc_rdf_pairs.argtypes = [dp, dp, dp, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_double, ctypes.c_double, ip,
+                                    ctypes.POINTER(ctypes.c_uint64)]
         _lib = L
     return _lib
 
@@ -161,6 +165,11 @@ class Oracle:
     def step(self, with_particles=True):
         lib().orc_step(self.h, int(with_particles))
 
+    def statistics(self):
+        s = TpmStats()
+        lib().orc_statistics(self.h, ctypes.byref(s))
+        return s.as_dict()
+
     def poisson_solve(self, C3, P, RHS, max_it, eps):
         C3 = np.ascontiguousarray(C3, dtype=np.float64)
         P = np.ascontiguousarray(P, dtype=np.float64).copy()
@@ -171,16 +180,67 @@ class Oracle:
         return P, it, err.value
 
 
+def rdf_pairs(x, y, z, L, r_max, nbins):
+    """All-pairs (O(Np^2), C) histogram of minimum-image distances."""
+    x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+    out = np.zeros(nbins, dtype=np.uint64)
+    lib().orc_rdf_pairs(_dp(x), _dp(y), _dp(z), x.shape[0], float(L[0]), float(L[1]),
+                        float(L[2]), float(r_max), int(nbins),
+                        out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+    return out
+
+
+def face_velocity(RU, Rho):
+    """u_d = RU_d / I_C2F_d(Rho), I_C2F(f)[i] = (f[i] + f[i-1]) * 0.5 (tensor0.cpp:268-362)."""
+    U = np.empty_like(RU)
+    for d, ax in enumerate((2, 1, 0)):  # x, y, z are the last, middle, first array axes
+        U[d] = RU[d] / ((Rho + np.roll(Rho, 1, axis=ax)) * 0.5)
+    return U
+
+
+def spectrum(p: Params, RU, Rho):
+    """Shell-summed energy spectrum of the face velocity (tpm_spectrum's definition):
+    E[s] = sum over wave vectors with nint(|k|/dk) = s of |u_hat|^2/2, u_hat = DFT/N^3."""
+    U = face_velocity(RU, Rho)
+    ntot = p.Nx * p.Ny * p.Nz
+    e = np.zeros((p.Nz, p.Ny, p.Nx // 2 + 1))
+    for d in range(3):
+        F = np.fft.rfftn(U[d]) / ntot
+        e += F.real * F.real + F.imag * F.imag
+    w = np.full(p.Nx // 2 + 1, 1.0)
+    w[0] = 0.5
+    w[-1] = 0.5
+    e *= w[None, None, :]
+    two_pi = 2 * 3.141592653589793
+    kx0, ky0, kz0 = two_pi / p.Lx, two_pi / p.Ly, two_pi / p.Lz
+    dk = min(kx0, ky0, kz0)
+    kx = np.arange(p.Nx // 2 + 1) * kx0
+    ky = np.where(np.arange(p.Ny) <= p.Ny // 2, np.arange(p.Ny), np.arange(p.Ny) - p.Ny) * ky0
+    kz = np.where(np.arange(p.Nz) <= p.Nz // 2, np.arange(p.Nz), np.arange(p.Nz) - p.Nz) * kz0
+    km = np.sqrt(kx[None, None, :] ** 2 + ky[None, :, None] ** 2 + kz[:, None, None] ** 2)
+    shell = np.floor(km / dk + 0.5).astype(np.int64)
+    return np.bincount(shell.ravel(), weights=e.ravel()), dk
+
+
 # ---------------------------------------------------------------- reference
 def have_reference() -> bool:
     return os.path.exists(REF_BIN)
 
 
+# grid::Statistics output files (grid.cpp:32-57) -> tpm_stats members
+STAT_FILES = {"Tg": "Tg_mean", "Tp": "Tp_mean", "HT": "HT_mean", "RU": "TKE2",
+              "TKE_U": "TKE_U", "TKE_V": "TKE_V", "TKE_W": "TKE_W", "P0": "P0",
+              "C_Max": "C_max", "C_Min": "C_min", "C_Mean": "C_mean", "Rho_Max": "Rho_max",
+              "Rho_Min": "Rho_min", "Rho_Mean": "Rho_mean", "Max_CFL_U": "Gas_CFL_Max"}
+
+
 def run_reference(p: Params, s: inputs.State, nsteps: int, substeps: int = 0,
-                  as_shipped: bool = False, workdir: str | None = None) -> dict:
-    """Run the reference build on state `s`; returns its dumped state."""
+                  as_shipped: bool = False, workdir: str | None = None,
+                  stats: bool = False) -> dict:
+    """Run the reference build on state `s`; returns its dumped state (and,
+    with stats, the per-step grid::Statistics values it wrote)."""
     tmp = workdir or tempfile.mkdtemp(prefix="tpm_ref_")
-    inputs.write_restart(tmp, p, s)
+    inputs.write_restart(tmp, p, s, statistics=stats)
     out = os.path.join(tmp, "out")
     os.makedirs(out, exist_ok=True)
     cmd = [REF_BIN, "deck.txt", str(nsteps), out]
@@ -188,9 +248,18 @@ def run_reference(p: Params, s: inputs.State, nsteps: int, substeps: int = 0,
         cmd.append("--as-shipped")
     if substeps:
         cmd += ["--substeps", str(substeps)]
+    if stats:
+        cmd.append("--stats")
     res = subprocess.run(cmd, cwd=tmp, capture_output=True, text=True, check=True)
     info = json.loads(res.stdout.strip().splitlines()[-1])
-    return read_reference_dump(p, out, info)
+    d = read_reference_dump(p, out, info)
+    if stats:
+        d["stats"] = {}
+        for fname, key in STAT_FILES.items():
+            rows = np.loadtxt(os.path.join(tmp, fname + ".dat"), ndmin=2)
+            d["stats"][key] = rows[:, 1]
+            d["stats"]["T_cur"] = rows[:, 0]
+    return d
 
 
 def read_reference_dump(p: Params, out: str, info: dict | None = None) -> dict:

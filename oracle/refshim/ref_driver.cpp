@@ -8,11 +8,13 @@
 // called, so that two-way coupling and particle heating are active.  Passing
 // `--as-shipped` skips it and reproduces the shipped loop.
 //
-// usage: tpm_ref <deck> <nsteps> <outdir> [--as-shipped] [--substeps S]
+// usage: tpm_ref <deck> <nsteps> <outdir> [--as-shipped] [--substeps S] [--stats]
 //   Run in a directory holding the Restart_* files the deck's Initial=1 reads
 //   (grid.cpp:221-238, particle.cpp:939-989).  With --substeps S (1..4) only
 //   the first S RK4 substeps of the first step run and no end-of-step work is
-//   done, for substep-level comparisons.
+//   done, for substep-level comparisons.  With --stats grid::Statistics runs
+//   after each step, as at simulation.cpp:92 (the deck must set Statistics=1;
+//   it appends to <Stat_dir>/<name>.dat).
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -46,10 +48,11 @@ int main(int argc, char **argv) {
   }
   int nsteps = std::atoi(argv[2]);
   std::string out = argv[3];
-  bool as_shipped = false;
+  bool as_shipped = false, stats = false;
   int substeps = 0;
   for (int a = 4; a < argc; ++a) {
     if (!std::strcmp(argv[a], "--as-shipped")) as_shipped = true;
+    else if (!std::strcmp(argv[a], "--stats")) stats = true;
     else if (!std::strcmp(argv[a], "--substeps") && a + 1 < argc) substeps = std::atoi(argv[++a]);
   }
   MPI_Init(&argc, &argv);
@@ -95,6 +98,7 @@ int main(int argc, char **argv) {
       }
       GRID.RU_np1.make_mean_U0(RhoU_);
       GRID.TimeAdvance();
+      if (stats) GRID.Statistics();
     }
   }
   auto t1 = std::chrono::steady_clock::now();

@@ -50,6 +50,8 @@ struct orc {
   int64_t num_timestep;
   int Iteration, n_it, total_it;
   double A, gx, gy, gz, I0, last_err;
+  double met;  /* mean_energy_transferred of the last Update_P0 (grid.cpp:818) */
+  int stepped; /* a full step has run since orc_initialize */
 };
 
 static const double RK4_pre[4] = {0.5, 0.5, 1., 1. / 6.};   /* grid.cpp:18-21 */
@@ -501,6 +503,7 @@ static void update_rho(orc *o, int s) {
 /* grid::Update_P0, grid.cpp:816-830 */
 static void update_p0(orc *o, int s) {
   double mean_energy_transferred = field_mean(o, o->RHS_Part_Temp);
+  o->met = mean_energy_transferred;
   if (o->p.cooling)
     o->dP0_dt = 0;
   else
@@ -737,6 +740,7 @@ void orc_end_step(orc *o) {
   pcopy(o, 0, 3);
   o->T_cur += o->p.dt;
   o->num_timestep++;
+  o->stepped = 1;
 }
 
 void orc_step(orc *o, int with_particles) {
@@ -747,6 +751,7 @@ void orc_step(orc *o, int with_particles) {
 
 /* grid::Initialize tail, grid.cpp:461-484 */
 void orc_initialize(orc *o) {
+  o->stepped = 0;
   vcopy(o, o->RU_int, o->RU);
   vcopy(o, o->RU_np1, o->RU);
   memcpy(o->Rho_int, o->Rho, sizeof(double) * (size_t)o->n);
@@ -854,4 +859,150 @@ void orc_get_scalars(orc *o, tpm_scalars *s) {
   s->total_poisson_iterations = o->total_it;
   s->last_poisson_error = o->last_err;
   s->max_abs_div = -1;
+}
+
+/* ------------------------------------------------------------ statistics */
+/* tensor0::max / min (tensor0.cpp:453-491): serial scan from the first
+ * interior element */
+static double field_max(orc *o, const double *f) {
+  double m = f[0];
+  for (int i = 0; i < o->nx; ++i)
+    for (int j = 0; j < o->ny; ++j)
+      for (int k = 0; k < o->nz; ++k)
+        if (f[IDX(o, i, j, k)] > m) m = f[IDX(o, i, j, k)];
+  return m;
+}
+static double field_min(orc *o, const double *f) {
+  double m = f[0];
+  for (int i = 0; i < o->nx; ++i)
+    for (int j = 0; j < o->ny; ++j)
+      for (int k = 0; k < o->nz; ++k)
+        if (f[IDX(o, i, j, k)] < m) m = f[IDX(o, i, j, k)];
+  return m;
+}
+/* tensor0::sum_squares (tensor0.cpp:493-504) */
+static double field_sum_squares(orc *o, const double *f) {
+  double s = 0;
+  for (int i = 0; i < o->nx; ++i)
+    for (int j = 0; j < o->ny; ++j)
+      for (int k = 0; k < o->nz; ++k) s += f[IDX(o, i, j, k)] * f[IDX(o, i, j, k)];
+  return s;
+}
+/* particle::max (particle.cpp:668-684), -1e9 for an empty set */
+static double part_max(orc *o, const double *v) {
+  if (o->np == 0) return -1e9;
+  double m = v[0];
+  for (long i = 1; i < o->np; ++i)
+    if (v[i] > m) m = v[i];
+  return m;
+}
+
+/* grid::Statistics (grid.cpp:902-940) on the step-boundary state, without
+ * touching the solver state (the reference overwrites U and dummy; with the
+ * particle stage on, U is recomputed before its next use, grid.cpp:868).
+ * The last three members are extensions: C variance (tensor0::var,
+ * tensor0.cpp:516-519), rms velocity, and 2 nu <S:S> with the strain rate of
+ * the face velocity from the staggered differences. */
+void orc_statistics(orc *o, tpm_stats *s) {
+  const long n = o->n;
+  const double size_tot = (double)(o->nx * o->ny * o->nz);
+  memset(s, 0, sizeof(*s));
+  s->T_cur = o->T_cur;
+  s->num_timestep = o->num_timestep;
+  s->Rho_mean = field_mean(o, o->Rho);
+  s->Rho_max = field_max(o, o->Rho);
+  s->Rho_min = field_min(o, o->Rho);
+  s->C_max = field_max(o, o->C);
+  s->C_min = field_min(o, o->C);
+  s->C_mean = field_mean(o, o->C);
+  /* TKE2 = U.mean_squares() (tensor1.cpp:351-359) of U as the last stage
+   * left it (RU_new/Rho_face before projection, grid.cpp:844) */
+  s->TKE2 = o->stepped ? (field_sum_squares(o, o->U.x) + field_sum_squares(o, o->U.y) +
+                          field_sum_squares(o, o->U.z)) / size_tot
+                       : 0.0;
+  vec3 V = valloc(n);
+  vdivide(o, o->RU_np1, o->Rho_face, V); /* U.Equal_Divide(RU_np1, Rho_face) */
+  double mx = field_max(o, V.x) * o->p.dt / o->dx; /* tensor1::max_cfl */
+  double my = field_max(o, V.y) * o->p.dt / o->dy;
+  double mz = field_max(o, V.z) * o->p.dt / o->dz;
+  mx = (my > mx) ? my : mx;
+  mx = (mz > mx) ? mz : mx;
+  s->Gas_CFL_Max = mx;
+  double ux = field_max(o, V.x), uy = field_max(o, V.y), uz = field_max(o, V.z); /* tensor1::max */
+  ux = (uy > ux) ? uy : ux;
+  ux = (uz > ux) ? uz : ux;
+  s->u_max = ux;
+  s->Vp_max = part_max(o, o->q[0][QU]);
+  s->Tp_max = part_max(o, o->q[0][QT]);
+  /* extensions on the same velocity */
+  s->u_rms = sqrt((field_sum_squares(o, V.x) + field_sum_squares(o, V.y) +
+                   field_sum_squares(o, V.z)) / size_tot / 3.0);
+  {
+    double ss = 0;
+    for (int i = 0; i < o->nx; ++i)
+      for (int j = 0; j < o->ny; ++j)
+        for (int k = 0; k < o->nz; ++k) {
+          const long c = IDX(o, i, j, k);
+          const int ip = wrap(i + 1, o->nx), im = wrap(i - 1, o->nx);
+          const int jp = wrap(j + 1, o->ny), jm = wrap(j - 1, o->ny);
+          const int kp = wrap(k + 1, o->nz), km = wrap(k - 1, o->nz);
+          const double sxx = (V.x[IDX(o, ip, j, k)] - V.x[c]) * o->inv_dx;
+          const double syy = (V.y[IDX(o, i, jp, k)] - V.y[c]) * o->inv_dy;
+          const double szz = (V.z[IDX(o, i, j, kp)] - V.z[c]) * o->inv_dz;
+          const double sxy = 0.5 * ((V.x[c] - V.x[IDX(o, i, jm, k)]) * o->inv_dy +
+                                    (V.y[c] - V.y[IDX(o, im, j, k)]) * o->inv_dx);
+          const double sxz = 0.5 * ((V.x[c] - V.x[IDX(o, i, j, km)]) * o->inv_dz +
+                                    (V.z[c] - V.z[IDX(o, im, j, k)]) * o->inv_dx);
+          const double syz = 0.5 * ((V.y[c] - V.y[IDX(o, i, j, km)]) * o->inv_dz +
+                                    (V.z[c] - V.z[IDX(o, i, jm, k)]) * o->inv_dy);
+          ss += sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz);
+        }
+    s->dissipation = 2.0 * (o->p.Mu0 / o->p.Rho0) * (ss / size_tot);
+  }
+  for (long c = 0; c < n; ++c) { /* U *= RU_np1 */
+    V.x[c] *= o->RU_np1.x[c];
+    V.y[c] *= o->RU_np1.y[c];
+    V.z[c] *= o->RU_np1.z[c];
+  }
+  s->TKE_U = field_mean(o, V.x);
+  s->TKE_V = field_mean(o, V.y);
+  s->TKE_W = field_mean(o, V.z);
+  s->TKE = s->TKE_U + s->TKE_V + s->TKE_W;
+  s->Gas_Max_Diff_CFL = o->p.dt / (o->dx * o->dx * s->Rho_min / o->p.Mu0) * 6.;
+  { /* particle::mean (particle.cpp:700-715) */
+    double sum = 0;
+    for (long i = 0; i < o->np; ++i) sum += o->q[0][QT][i];
+    s->Tp_mean = o->np > 0 ? sum / (double)o->np : 0.0;
+  }
+  s->HT_mean = o->stepped ? o->met : 0.0;
+  { /* dummy.x.Equal_Divide(P0/R, Rho); Tg_mean = dummy.x.mean() */
+    const double a = o->P0 / o->R;
+    for (long c = 0; c < n; ++c) V.x[c] = a / o->Rho[c];
+    s->Tg_mean = field_mean(o, V.x);
+  }
+  s->P0 = o->P0;
+  s->num_iteration = o->stepped ? o->n_it : 0;
+  s->C_var = field_sum_squares(o, o->C) / size_tot - s->C_mean * s->C_mean;
+  vfree(V);
+}
+
+/* Unordered particle pairs by minimum-image distance, all pairs i < j
+ * (the O(Np^2) definition the cell-list count on the GPU must equal). */
+void orc_rdf_pairs(const double *x, const double *y, const double *z, int64_t np, double Lx,
+                   double Ly, double Lz, double r_max, int nbins, uint64_t *pairs) {
+  const double hx = 0.5 * Lx, hy = 0.5 * Ly, hz = 0.5 * Lz, r2max = r_max * r_max;
+  const double dr = r_max / nbins;
+  for (int b = 0; b < nbins; ++b) pairs[b] = 0;
+  for (int64_t i = 0; i < np; ++i)
+    for (int64_t j = i + 1; j < np; ++j) {
+      double dx = x[j] - x[i], dy = y[j] - y[i], dz = z[j] - z[i];
+      if (dx > hx) dx -= Lx; else if (dx < -hx) dx += Lx;
+      if (dy > hy) dy -= Ly; else if (dy < -hy) dy += Ly;
+      if (dz > hz) dz -= Lz; else if (dz < -hz) dz += Lz;
+      const double r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 < r2max) {
+        const int b = (int)(sqrt(r2) / dr);
+        if (b < nbins) pairs[b]++;
+      }
+    }
 }

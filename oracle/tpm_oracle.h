@@ -48,6 +48,12 @@ void orc_substep(orc *o, int rk_stage, int with_particles);
 void orc_end_step(orc *o);
 void orc_step(orc *o, int with_particles);
 
+/* grid::Statistics (grid.cpp:902-940) plus the extensions of tpm_stats. */
+void orc_statistics(orc *o, tpm_stats *s);
+/* O(Np^2) pair histogram by minimum-image distance (tpm_rdf's definition). */
+void orc_rdf_pairs(const double *x, const double *y, const double *z, int64_t np, double Lx,
+                   double Ly, double Lz, double r_max, int nbins, uint64_t *pairs);
+
 /* poisson::Solve (Solver==0) on caller buffers; returns iterations. */
 int orc_poisson_solve(orc *o, const double *C3, double *P, const double *RHS, int max_it,
                       double eps, double *err_out);

@@ -7,6 +7,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 NAMES = ("heated16_2steps", "cooled24_gravity_switch", "shipped24_1step")
+STATS_NAMES = ("stats16_3steps",)
 
 
 def load(name):
@@ -23,4 +24,5 @@ def load(name):
     ref["part"] = {q: z[f"part_{q}"] for q in list(inputs.PQ) + ["flag", "RHS_T"]}
     ref["P0"] = float(z["P0"])
     ref["T_cur"] = float(z["T_cur"])
+    ref["stats"] = {k[5:]: z[k] for k in z.files if k.startswith("stat_")}
     return p, s, ref, int(z["nsteps"]), bool(int(z["as_shipped"]))

@@ -5,7 +5,7 @@ Each fixture holds the seeded input state, the deck parameters and the state
 the reference produced after the given number of RK4 steps.  Run from the
 repository root:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 
 The reference has no golden vectors or tests of its own, so these fixtures
 are the pin for the oracle (tests/test_oracle_pin.py) and for the GPU path
@@ -41,6 +41,11 @@ CASES = {
     "shipped24_1step": dict(N=24, npart=100, nu=0.02, A=0.1, tau_p=0.1, mass_loading=0.2,
                             heating_Q=0.0, iterations=2, epsilon=0.0, seed=13, nsteps=1,
                             as_shipped=True),
+    # grid::Statistics after each of 3 steps, as the reference writes it
+    # (<name>.dat files, 6 significant digits)
+    "stats16_3steps": dict(N=16, npart=2000, nu=0.02, A=0.1, tau_p=0.1, mass_loading=0.5,
+                           heating_Q=0.5, iterations=20, epsilon=1e-13, seed=21, nsteps=3,
+                           stats=True),
 }
 
 
@@ -50,7 +55,8 @@ def make(name, c):
                    iterations=c["iterations"], epsilon=c["epsilon"])
     s = inputs.make_state(p, c["npart"], seed=c["seed"])
     p = p.replace(dt=inputs.cfl_dt(p, s.RU), **c.get("extra", {}))
-    ref = po.run_reference(p, s, c["nsteps"], as_shipped=c.get("as_shipped", False))
+    ref = po.run_reference(p, s, c["nsteps"], as_shipped=c.get("as_shipped", False),
+                           stats=c.get("stats", False))
     out = dict(
         params=json.dumps(dataclasses.asdict(p)), nsteps=c["nsteps"],
         as_shipped=int(c.get("as_shipped", False)),
@@ -59,6 +65,7 @@ def make(name, c):
         RU=ref["RU"], RU_int=ref["RU_int"], Rho=ref["Rho"], P=ref["P"], C=ref["C"],
         Q=ref["RHS_Part_Temp"], P0=ref["P0"], T_cur=ref["T_cur"],
         **{f"part_{q}": ref["part"][q] for q in list(inputs.PQ) + ["flag", "RHS_T"]},
+        **{f"stat_{k}": v for k, v in ref.get("stats", {}).items()},
     )
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(name, "written")
@@ -67,5 +74,6 @@ def make(name, c):
 if __name__ == "__main__":
     if not po.have_reference():
         po.build()
-    for name, c in CASES.items():
-        make(name, c)
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        make(name, CASES[name])

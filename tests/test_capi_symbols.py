@@ -44,16 +44,17 @@ def test_params_struct_layout_matches_header():
     import subprocess
     import tempfile
 
-    from tpm.params import TpmParams, TpmScalars
+    from tpm.params import TpmParams, TpmScalars, TpmStats
 
     src = r'''
 #include <stdio.h>
 #include <stddef.h>
 #include "tpm.h"
 int main(void){
- printf("%zu %zu %zu %zu %zu %zu\n", sizeof(tpm_params), offsetof(tpm_params, epsilon),
+ printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(tpm_params), offsetof(tpm_params, epsilon),
    offsetof(tpm_params, A1), offsetof(tpm_params, I02), sizeof(tpm_scalars),
-   offsetof(tpm_scalars, max_abs_div));
+   offsetof(tpm_scalars, max_abs_div), sizeof(tpm_stats), offsetof(tpm_stats, num_iteration),
+   offsetof(tpm_stats, dissipation));
  return 0;}
 '''
     with tempfile.TemporaryDirectory() as d:
@@ -63,7 +64,8 @@ int main(void){
         subprocess.check_call(["gcc", "-I", os.path.join(REPO, "include"), c, "-o", exe])
         got = list(map(int, subprocess.check_output([exe]).split()))
     want = [ctypes.sizeof(TpmParams), TpmParams.epsilon.offset, TpmParams.A1.offset,
-            TpmParams.I02.offset, ctypes.sizeof(TpmScalars), TpmScalars.max_abs_div.offset]
+            TpmParams.I02.offset, ctypes.sizeof(TpmScalars), TpmScalars.max_abs_div.offset,
+            ctypes.sizeof(TpmStats), TpmStats.num_iteration.offset, TpmStats.dissipation.offset]
     assert got == want
 
 

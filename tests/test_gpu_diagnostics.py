@@ -1,0 +1,165 @@
+"""Diagnostics on the device (tpm_statistics, tpm_spectrum, tpm_rdf) against
+the oracle and the reference's own stat files.
+
+Bars: grid::Statistics scalars and the extensions within 1e-12 relative of
+the oracle (extrema exact); the reference's stat files to their 6 printed
+digits; spectrum shells within 1e-12 of the total energy; RDF pair counts
+identical to the O(Np^2) count.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from golden import STATS_NAMES, load
+from tpm import inputs, params as P
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+TOL_PRINTED = 6e-6
+EXACT = ("Rho_max", "Rho_min", "C_max", "C_min", "u_max", "Gas_CFL_Max", "Vp_max", "Tp_max",
+         "P0", "T_cur", "num_timestep", "num_iteration", "Gas_Max_Diff_CFL")
+
+
+@pytest.fixture(scope="module")
+def capi():
+    from tpm import build, capi
+
+    build.build()
+    return capi
+
+
+def case(N=32, npart=10_000, seed=7, heat=0.5, **kw):
+    p = P.physical(N, npart, nu=0.02, A=0.1, tau_p=0.1, mass_loading=0.5, heating_Q=heat,
+                   iterations=20, epsilon=1e-13, **kw)
+    s = inputs.make_state(p, npart, seed=seed)
+    return p.replace(dt=inputs.cfl_dt(p, s.RU)), s
+
+
+def compare_stats(g, o, tol=TOL):
+    for k, want in o.items():
+        got = g[k]
+        if k in EXACT:
+            assert got == want, (k, got, want)
+        else:
+            assert abs(got - want) <= tol * max(abs(want), 1e-300), (k, got, want)
+
+
+@pytest.mark.parametrize("nsteps", [0, 2])
+def test_statistics_match_oracle(capi, oracle_lib, nsteps):
+    p, s = case()
+    ctx = capi.Context(p, s.npart)
+    ctx.load(s)
+    ctx.initialize()
+    o = oracle_lib.Oracle(p, s.npart)
+    o.load(s)
+    o.initialize()
+    for _ in range(nsteps):
+        ctx.step()
+        o.step()
+    g = ctx.statistics()
+    compare_stats(g, o.statistics())
+    assert ctx.statistics() == g  # bit-reproducible
+
+
+@pytest.mark.parametrize("name", STATS_NAMES)
+def test_statistics_match_reference_stat_files(capi, name):
+    p, s, ref, nsteps, _ = load(name)
+    ctx = capi.Context(p, s.npart)
+    ctx.load(s)
+    ctx.initialize()
+    for st in range(nsteps):
+        ctx.step()
+        got = ctx.statistics()
+        for key, vals in ref["stats"].items():
+            r = float(vals[st])
+            assert abs(got[key] - r) <= TOL_PRINTED * abs(r) + 1e-300, (st, key, got[key], r)
+
+
+def test_statistics_need_a_step_boundary(capi):
+    p, s = case(N=16, npart=100)
+    ctx = capi.Context(p, s.npart)
+    ctx.load(s)
+    ctx.initialize()
+    ctx.substep(0)
+    with pytest.raises(capi.TpmError):
+        ctx.statistics()
+
+
+def test_mixed_statistics_close_to_fp64(capi):
+    p, s = case(N=32, npart=10_000, seed=8)
+    out = []
+    for prec in (P.PREC_FP64, P.PREC_MIXED):
+        ctx = capi.Context(p.replace(precision=prec), s.npart)
+        ctx.load(s)
+        ctx.initialize()
+        ctx.run(3)
+        out.append(ctx.statistics())
+    for k in ("TKE", "TKE2", "dissipation", "C_var", "Tg_mean", "Tp_mean", "u_rms"):
+        assert abs(out[1][k] - out[0][k]) <= 1e-5 * abs(out[0][k]), k
+
+
+@pytest.mark.parametrize("dims", [(32, 32, 32), (24, 30, 16)])
+def test_spectrum_matches_numpy(capi, oracle_lib, dims):
+    nx, ny, nz = dims
+    p, s = case(N=nx, npart=2000, seed=9)
+    if (ny, nz) != (nx, nx):
+        p = p.replace(Ny=ny, Nz=nz, Ly=p.Lx * ny / nx, Lz=p.Lx * nz / nx)
+        s = inputs.make_state(p, 2000, seed=9)
+        p = p.replace(dt=inputs.cfl_dt(p, s.RU))
+    ctx = capi.Context(p, s.npart)
+    ctx.load(s)
+    ctx.initialize()
+    ctx.run(2)
+    E, dk = ctx.spectrum()
+    want, dk_w = oracle_lib.spectrum(p, ctx.download_field("RU"), ctx.download_field("RHO"))
+    assert dk == dk_w and E.shape == want.shape
+    assert np.abs(E - want).max() <= TOL * want.sum()
+    U = oracle_lib.face_velocity(ctx.download_field("RU"), ctx.download_field("RHO"))
+    assert abs(E.sum() - 0.5 * np.mean(U ** 2) * 3) <= TOL * E.sum()
+
+
+def test_spectrum_large_box_parseval(capi):
+    p, s = case(N=128, npart=100_000, seed=10, heat=0.1)
+    ctx = capi.Context(p, s.npart)
+    ctx.load(s)
+    ctx.initialize()
+    ctx.step()
+    E, _ = ctx.spectrum()
+    st = ctx.statistics()
+    assert abs(E.sum() - 1.5 * st["u_rms"] ** 2) <= 1e-12 * E.sum()
+    # the initial spectrum peaks near k = 4 and is negligible in the top shells
+    assert 2 <= int(np.argmax(E)) <= 6
+    assert E[-5:].sum() <= 1e-6 * E.sum()
+
+
+@pytest.mark.parametrize("clustered", [False, True])
+def test_rdf_pairs_match_brute_force(capi, oracle_lib, clustered):
+    p, s = case(N=32, npart=20_000, seed=11)
+    if clustered:  # most particles in a few cells, some on the boundary planes
+        rng = np.random.default_rng(11)
+        for q, L in zip(("x", "y", "z"), (p.Lx, p.Ly, p.Lz)):
+            s.part[q] = np.where(rng.random(s.npart) < 0.7, 0.3 + 0.05 * rng.random(s.npart),
+                                 s.part[q])
+        s.part["x"][:50] = 0.0
+        s.part["y"][50:100] = p.Ly
+    ctx = capi.Context(p, s.npart)
+    ctx.load(s)
+    ctx.initialize()
+    for r_max, nb in ((0.5, 50), (p.Lx / 3, 64)):
+        pairs, g = ctx.rdf(r_max, nb)
+        base = ctx.download_particles("base")
+        want = oracle_lib.rdf_pairs(base["x"], base["y"], base["z"], (p.Lx, p.Ly, p.Lz), r_max, nb)
+        assert np.array_equal(pairs, want)
+        assert np.array_equal(ctx.rdf(r_max, nb)[0], pairs)
+    if not clustered:  # uniform random positions: g ~ 1 away from r = 0
+        assert abs(g[nb // 2:].mean() - 1.0) < 0.02
+
+
+def test_rdf_rejects_r_max_beyond_a_third_of_the_box(capi):
+    p, s = case(N=16, npart=100)
+    ctx = capi.Context(p, s.npart)
+    ctx.load(s)
+    ctx.initialize()
+    with pytest.raises(capi.TpmError):
+        ctx.rdf(p.Lx / 2, 10)

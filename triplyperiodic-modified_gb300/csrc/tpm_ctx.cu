@@ -18,6 +18,9 @@
 #include "tpm_reduce.cuh"
 
 using tpm::Grid;
+using tpm::dalloc;
+using tpm::fail;
+using tpm::guarded;
 
 namespace {
 
@@ -28,40 +31,6 @@ bool factorable(int n) {
   for (int f : {2, 3, 5})
     while (n % f == 0) n /= f;
   return n == 1;
-}
-
-template <typename T>
-T *dalloc(tpm_ctx *c, size_t count) {
-  void *p = nullptr;
-  if (count == 0) count = 1;
-  cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    throw std::make_pair(TPM_ERR_NOMEM, std::string("cudaMalloc of ") +
-                                            std::to_string(count * sizeof(T)) + " bytes failed");
-  }
-  c->allocs.push_back(p);
-  return reinterpret_cast<T *>(p);
-}
-
-int fail(tpm_ctx *c, int code, const std::string &msg) {
-  if (c) c->err = msg;
-  return code;
-}
-
-// Runs f, mapping exceptions to status codes (the library never exits).
-template <typename F>
-int guarded(tpm_ctx *c, F &&f) {
-  if (!c) return TPM_ERR_ARG;
-  try {
-    return f();
-  } catch (const std::pair<int, std::string> &e) {
-    return fail(c, e.first, e.second);
-  } catch (const std::string &s) {
-    return fail(c, TPM_ERR_CUDA, s);
-  } catch (const std::bad_alloc &) {
-    return fail(c, TPM_ERR_NOMEM, "host allocation failed");
-  }
 }
 
 void push_scalars(tpm_ctx *c) {
@@ -194,6 +163,7 @@ void end_step(tpm_ctx *c) {
   c->T_cur += c->p.dt;
   c->num_timestep++;
   c->np1_is_base = true;
+  c->stepped = true;
 }
 
 }  // namespace
@@ -539,6 +509,7 @@ int tpm_initialize(tpm_ctx *c) {
     tpm::particle_init_heat(c);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->initialized = true;
+    c->stepped = false;
     return TPM_OK;
   });
 }
@@ -561,6 +532,7 @@ int tpm_resume(tpm_ctx *c) {
     tpm::particle_resume(c);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->initialized = true;
+    c->stepped = false;
     return TPM_OK;
   });
 }

@@ -157,6 +157,32 @@ __device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
   return ((long long)k * g.ny + j) * g.nx + i;
 }
 
+// Real-to-complex post-processing of npen x-rows held as Nx/2-point complex
+// transforms z (row q at stride npen): X[k] = Fe[k] + W^k Fo[k], k <= Nx/2,
+// stored to the half spectrum.
+template <typename T2>
+__device__ __forceinline__ void r2c_store(const Grid &g, const T2 *z, int npen, int M,
+                                          long long row0, long long nrows,
+                                          const T2 *__restrict__ r2c_tw, T2 *__restrict__ spec) {
+  using T = typename Cx<T2>::T;
+  const int nxh = g.nxh;
+  for (int idx = threadIdx.x; idx < npen * nxh; idx += blockDim.x) {
+    const int q = idx / nxh, kx = idx % nxh;
+    const long long row = row0 + q;
+    if (row >= nrows) continue;
+    T2 Z = z[(kx % M) * npen + q];
+    T2 Zc = z[((M - kx) % M) * npen + q];
+    Zc.y = -Zc.y;
+    T fer = (Z.x + Zc.x) * (T)0.5, fei = (Z.y + Zc.y) * (T)0.5;
+    T dr = Z.x - Zc.x, di = Z.y - Zc.y;
+    T for_ = di * (T)0.5, foi = -dr * (T)0.5;  // (Z - Zc) / (2i)
+    T2 w = r2c_tw[kx];
+    T xr = Cx<T2>::fma_(w.x, for_, Cx<T2>::fma_(-w.y, foi, fer));
+    T xi = Cx<T2>::fma_(w.x, foi, Cx<T2>::fma_(w.y, for_, fei));
+    spec[row * nxh + kx] = Cx<T2>::mk(xr, xi);
+  }
+}
+
 // ------------------------------------------------- 1. residual + R2C along x
 // poisson.cpp:399-404 (residual) and the first third of fft_3d (:431).
 // kScaled (mixed path): Cf holds C*(1/d^2) per component, and the residual is
@@ -213,23 +239,7 @@ __global__ void k_xfwd_resid(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   }
   __syncthreads();
   T2 *z = smem_fft(a, b, npen, pl, -1);
-  // real-to-complex post-processing: X[k] = Fe[k] + W^k Fo[k]
-  const int nxh = g.nxh;
-  for (int idx = threadIdx.x; idx < npen * nxh; idx += blockDim.x) {
-    const int q = idx / nxh, kx = idx % nxh;
-    const long long row = row0 + q;
-    if (row >= nrows) continue;
-    T2 Z = z[(kx % M) * npen + q];
-    T2 Zc = z[((M - kx) % M) * npen + q];
-    Zc.y = -Zc.y;
-    T fer = (Z.x + Zc.x) * (T)0.5, fei = (Z.y + Zc.y) * (T)0.5;
-    T dr = Z.x - Zc.x, di = Z.y - Zc.y;
-    T for_ = di * (T)0.5, foi = -dr * (T)0.5;  // (Z - Zc) / (2i)
-    T2 w = r2c_tw[kx];
-    T xr = Cx<T2>::fma_(w.x, for_, Cx<T2>::fma_(-w.y, foi, fer));
-    T xi = Cx<T2>::fma_(w.x, foi, Cx<T2>::fma_(w.y, for_, fei));
-    spec[row * nxh + kx] = Cx<T2>::mk(xr, xi);
-  }
+  r2c_store(g, z, npen, M, row0, nrows, r2c_tw, spec);
 }
 
 // ------------------------------------------------------- 2./4. y pencils
@@ -533,6 +543,97 @@ int fft_x_blocks(const tpm_ctx *c) {
   const long long nrows = (long long)c->g.ny * c->g.nz;
   int npen = pens_for(c->g.nx / 2);
   return (int)((nrows + npen - 1) / npen);
+}
+
+// ---------------------------------------------------------- energy spectrum
+// Forward 3-D transform of one real face-velocity component with the same
+// pencil passes (no residual, no solve), then |X/N^3|^2/2 per half-spectrum
+// mode, doubled for 0 < kx < Nx/2 (their conjugates are not stored), summed
+// over the three components into emode[(kz*Ny + ky)*(Nx/2+1) + kx].
+namespace {
+
+__global__ void k_spec_xfwd(Grid g, FftPlan pl, const double2 *__restrict__ r2c_tw,
+                            const double *__restrict__ f, double2 *__restrict__ spec, int npen) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2 *a = reinterpret_cast<double2 *>(smem_raw);
+  const int M = pl.n;
+  double2 *b = a + M * npen;
+  const long long nrows = (long long)g.ny * g.nz;
+  const long long row0 = (long long)blockIdx.x * npen;
+  for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
+    const int q = idx / g.nx, i = idx % g.nx;
+    const long long row = row0 + q;
+    double *slot = reinterpret_cast<double *>(&a[(i >> 1) * npen + q]);
+    slot[i & 1] = row < nrows ? f[row * g.nx + i] : 0.0;
+  }
+  __syncthreads();
+  double2 *z = smem_fft(a, b, npen, pl, -1);
+  r2c_store(g, z, npen, M, row0, nrows, r2c_tw, spec);
+}
+
+__global__ void k_spec_z_energy(Grid g, FftPlan pl, const double2 *__restrict__ spec,
+                                double *__restrict__ emode, int npen, int accumulate) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2 *a = reinterpret_cast<double2 *>(smem_raw);
+  double2 *b = a + pl.n * npen;
+  const int tiles = (g.nxh + npen - 1) / npen;
+  const int ky = blockIdx.x / tiles, kx0 = (blockIdx.x % tiles) * npen;
+  const long long plane = (long long)g.ny * g.nxh;
+  const long long base = (long long)ky * g.nxh + kx0;
+  for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
+    const int q = idx % npen, kz = idx / npen;
+    a[kz * npen + q] = (kx0 + q < g.nxh) ? spec[base + kz * plane + q] : make_double2(0, 0);
+  }
+  __syncthreads();
+  const double2 *r = smem_fft(a, b, npen, pl, -1);
+  const double inv_tot = 1.0 / ((double)g.nx * (double)g.ny * (double)g.nz);
+  for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
+    const int q = idx % npen, kz = idx / npen;
+    const int kx = kx0 + q;
+    if (kx >= g.nxh) continue;
+    const double2 v = r[kz * npen + q];
+    const double ur = v.x * inv_tot, ui = v.y * inv_tot;
+    const double w = (kx == 0 || 2 * kx == g.nx) ? 0.5 : 1.0;
+    const double e = w * (ur * ur + ui * ui);
+    const long long m = base + kz * plane + q;
+    emode[m] = accumulate ? emode[m] + e : e;
+  }
+}
+
+}  // namespace
+
+void spectrum_mode_energy(tpm_ctx *c, const double *U3, double2 *spec, double *emode) {
+  const Grid &g = c->g;
+  const long long nrows = (long long)g.ny * g.nz;
+  for (int d = 0; d < 3; ++d) {
+    {
+      int npen = pens_for(c->fx.n);
+      int blocks = (int)((nrows + npen - 1) / npen);
+      size_t smem = 2 * (size_t)npen * c->fx.n * sizeof(double2);
+      TPM_LAUNCH(c, "spec_x", k_spec_xfwd, blocks, kFftThreads, smem, g, c->fx, c->r2c64,
+                 U3 + d * g.n, spec, npen);
+    }
+    {
+      int npen = pens_for(c->fy.n);
+      int blocks = g.nz * ((g.nxh + npen - 1) / npen);
+      size_t smem = 2 * (size_t)npen * c->fy.n * sizeof(double2);
+      TPM_LAUNCH(c, "spec_y", k_fft_y<double2>, blocks, kFftThreads, smem, g, c->fy, spec, npen,
+                 -1);
+    }
+    {
+      int npen = pens_for(c->fz.n);
+      int blocks = g.ny * ((g.nxh + npen - 1) / npen);
+      size_t smem = 2 * (size_t)npen * c->fz.n * sizeof(double2);
+      TPM_LAUNCH(c, "spec_z_energy", k_spec_z_energy, blocks, kFftThreads, smem, g, c->fz, spec,
+                 emode, npen, d > 0);
+    }
+  }
+}
+
+void spectrum_kernels_setup() {
+  const int smem64 = 2 * kFftSmemPoints * (int)sizeof(double2);
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_spec_xfwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_spec_z_energy, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
 }
 }  // namespace tpm
 

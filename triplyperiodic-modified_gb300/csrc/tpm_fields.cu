@@ -337,11 +337,12 @@ __global__ void k_poisson_rhs(Grid g, const double *__restrict__ Rho_new,
                               const double *__restrict__ RUn, const DevScalars *__restrict__ s,
                               double *__restrict__ RHS, double *__restrict__ divg,
                               double *__restrict__ Cface, double *__restrict__ cc,
-                              double *__restrict__ partials, PoisArgs a) {
+                              double *__restrict__ partials, double *__restrict__ tke_parts,
+                              PoisArgs a) {
   __shared__ double sh[kThreads];
   const double coef = s->coef_div, meanQ = s->mean_Q;
   const double OneThird = 1. / 3.;
-  double acc = 0;
+  double acc = 0, usq = 0;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
@@ -368,6 +369,7 @@ __global__ void k_poisson_rhs(Grid g, const double *__restrict__ Rho_new,
       double u_hi = R[nb.p[d]] / rf_hi[d];
       double u_lo = R[c] / rf_lo[d];
       t[d] = (u_hi - u_lo) * (d == 0 ? g.inv_dx : d == 1 ? g.inv_dy : g.inv_dz);
+      usq += u_lo * u_lo;
     }
     double rhs = t[0] + t[1] + t[2];
     rhs -= dv;
@@ -388,6 +390,10 @@ __global__ void k_poisson_rhs(Grid g, const double *__restrict__ Rho_new,
   }
   double bs = block_sum(acc, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = bs;
+  if (tke_parts) {  // last stage: sum of U^2 for grid::Statistics' TKE2 (grid.cpp:911)
+    double bu = block_sum(usq, sh);
+    if (threadIdx.x == 0) tke_parts[blockIdx.x] = bu;
+  }
 }
 
 // ------------------------------------------------ mixed-path variants
@@ -465,11 +471,12 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
                                     const double *__restrict__ Cface,
                                     const DevScalars *__restrict__ s, double *__restrict__ RHS,
                                     double *__restrict__ divg, double *__restrict__ cc,
-                                    double *__restrict__ partials, PoisArgs a) {
+                                    double *__restrict__ partials, double *__restrict__ tke_parts,
+                                    PoisArgs a) {
   __shared__ double sh[kThreads];
   const double coef = s->coef_div, meanQ = s->mean_Q;
   const double inv_d[3] = {g.inv_dx, g.inv_dy, g.inv_dz};
-  double acc = 0;
+  double acc = 0, usq = 0;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
@@ -487,8 +494,10 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
     for (int d = 0; d < 3; ++d) {
       const double clo = Cface[d * g.n + c], chi = Cface[d * g.n + nb.p[d]];
       const double *R = RUn + d * g.n;
-      t[d] = (R[nb.p[d]] * chi - R[c] * clo) * inv_d[d];
+      const double u_lo = R[c] * clo;
+      t[d] = (R[nb.p[d]] * chi - u_lo) * inv_d[d];
       msum += ((float)clo + (float)chi) * 0.5f;
+      usq += u_lo * u_lo;
     }
     double rhs = (t[0] + t[1] + t[2] - dv) * a.inv_dtpre;
     RHS[c] = rhs;
@@ -497,6 +506,10 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
   }
   double bs = block_sum(acc, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = bs;
+  if (tke_parts) {
+    double bu = block_sum(usq, sh);
+    if (threadIdx.x == 0) tke_parts[blockIdx.x] = bu;
+  }
 }
 
 // face velocity of the mixed path: only the FP32 stencil and the particle
@@ -724,19 +737,23 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
   a.cooling = c->p.cooling;
   a.store_div = store_div;
   int nb = cell_blocks(c->g);
+  double *tke_parts = s == 3 ? c->partials + kPartTke2 * kRedBlocks : nullptr;
   if (c->p.precision == TPM_PREC_MIXED) {
     TPM_LAUNCH(c, "face_coeff", k_face_coeff_mixed, nb, kThreads, 0, c->g, c->Rho_new, c->Cface,
                c->Cs);
     TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_mixed, nb, kThreads, 0, c->g, c->inv_rho, c->Q,
                c->RU_new, c->Cface, c->dsc, c->RHS, c->divg, c->cc,
-               c->partials + kPartRhs * kRedBlocks, a);
+               c->partials + kPartRhs * kRedBlocks, tke_parts, a);
   } else
   TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs, nb, kThreads, 0, c->g, c->Rho_new, c->inv_rho,
              c->Q, c->RU_new, c->dsc, c->RHS, c->divg, c->Cface, c->cc,
-             c->partials + kPartRhs * kRedBlocks, a);
+             c->partials + kPartRhs * kRedBlocks, tke_parts, a);
   TPM_LAUNCH(c, "finish_mean", k_finish_mean, 1, kThreads, 0, c->partials + kPartRhs * kRedBlocks,
              nb, c->g.n,
              &c->dsc->mean_rhs);
+  if (tke_parts)
+    TPM_LAUNCH(c, "finish_mean", k_finish_mean, 1, kThreads, 0, tke_parts, nb, c->g.n,
+               &c->dsc->tke2);
 }
 
 void launch_project(tpm_ctx *c, int s) {

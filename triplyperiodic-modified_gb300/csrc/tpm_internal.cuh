@@ -14,7 +14,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "tpm.h"
@@ -50,6 +52,7 @@ struct DevScalars {
   double err;        // max|dp| of the last Poisson iteration (poisson.cpp:407)
   double mean_ru[3]; // RU_np1 component means (simulation.cpp:80)
   double max_div;    // FP64 post-projection residual (mixed path)
+  double tke2;       // mean(U^2) of the last stage before projection (grid.cpp:911)
   int nonfinite;
   int pad;
 };
@@ -96,6 +99,7 @@ struct tpm_ctx {
   int64_t num_timestep = 0;
   bool initialized = false;
   bool np1_is_base = true;  // np1 copies equal base (after initialize / end of step)
+  bool stepped = false;     // a full step has run since initialize / resume
   int last_it = 0, total_it = 0;
   double last_err = 0;
 
@@ -140,6 +144,22 @@ struct tpm_ctx {
   bool store_div = false;
   bool div_every_stage = false;
 
+  // ---- diagnostics (allocated on first use; tpm_diag.cu) ----
+  double *diag_u = nullptr;      // 3n: face velocity RU/I_C2F(Rho) of the base state
+  double *diag_parts = nullptr;  // per-block partials of the statistics
+  double *diag_out = nullptr;    // finished statistics
+  double2 *diag_spec = nullptr;  // FP64 half spectrum for the energy spectrum
+  double *diag_emode = nullptr;  // energy per half-spectrum mode
+  int32_t *diag_modes = nullptr;        // mode indices grouped by shell
+  int32_t *diag_shell_start = nullptr;  // nshell + 1 offsets into diag_modes
+  int diag_nshell = 0;
+  double diag_dk = 0;
+  int32_t *rdf_counts = nullptr, *rdf_start = nullptr, *rdf_fill = nullptr;
+  double *rdf_pos = nullptr;                 // 3np positions grouped by cell
+  unsigned long long *rdf_hist = nullptr;
+  long long rdf_cells_cap = 0;
+  int rdf_bins_cap = 0;
+
   // ---- profiling ----
   bool prof_on = false;
   std::vector<tpm::ProfEntry> prof;
@@ -173,6 +193,10 @@ void fft_plans_create(tpm_ctx *c);
 int fft_x_blocks(const tpm_ctx *c);
 // one Richardson iteration; returns nothing (error lands in dsc->err)
 void poisson_iteration(tpm_ctx *c);
+// energy per half-spectrum mode of the face velocity U3 (3n), summed over
+// components (spec: FP64 half-spectrum scratch)
+void spectrum_mode_energy(tpm_ctx *c, const double *U3, double2 *spec, double *emode);
+void spectrum_kernels_setup();
 
 // ---- particles (tpm_particles.cu) ----
 void launch_particle_push(tpm_ctx *c, int stage, bool np1_in_base);
@@ -182,6 +206,45 @@ void particle_heat(tpm_ctx *c);
 void particle_init_heat(tpm_ctx *c);
 void particle_resume(tpm_ctx *c);
 void particle_zero_fields(tpm_ctx *c);
+
+}  // namespace tpm
+
+namespace tpm {
+
+// Device allocation owned by the context (freed by tpm_destroy).
+template <typename T>
+T *dalloc(tpm_ctx *c, size_t count) {
+  void *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw std::make_pair(TPM_ERR_NOMEM, std::string("cudaMalloc of ") +
+                                            std::to_string(count * sizeof(T)) + " bytes failed");
+  }
+  c->allocs.push_back(p);
+  return reinterpret_cast<T *>(p);
+}
+
+inline int fail(tpm_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+// Runs f, mapping exceptions to status codes (the library never exits).
+template <typename F>
+int guarded(tpm_ctx *c, F &&f) {
+  if (!c) return TPM_ERR_ARG;
+  try {
+    return f();
+  } catch (const std::pair<int, std::string> &e) {
+    return fail(c, e.first, e.second);
+  } catch (const std::string &s) {
+    return fail(c, TPM_ERR_CUDA, s);
+  } catch (const std::bad_alloc &) {
+    return fail(c, TPM_ERR_NOMEM, "host allocation failed");
+  }
+}
 
 }  // namespace tpm
 

@@ -57,6 +57,6 @@ __device__ __forceinline__ T block_max(T v, T *sh) {
 
 // regions of tpm_ctx::partials (kRedBlocks doubles each)
 enum { kPartQ = 0, kPartRhs = 1, kPartRu = 2 /* 3 regions */, kPartErr = 5, kPartDiv = 6,
-       kPartRegions = 8 };
+       kPartTke2 = 7, kPartRegions = 8 };
 
 }  // namespace tpm

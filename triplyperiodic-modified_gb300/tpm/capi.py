@@ -13,7 +13,7 @@ import os
 import numpy as np
 
 from . import inputs
-from .params import Params, TpmParams, TpmScalars
+from .params import Params, TpmParams, TpmScalars, TpmStats
 
 PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG, "lib", "libtpm.so")
@@ -44,6 +44,11 @@ SIGNATURES = {
     "tpm_upload_particle_rhs_t": (_i, [_vp, _dp]),
     "tpm_set_particle_tau": (_i, [_vp, _dp]),
     "tpm_resume": (_i, [_vp]),
+    "tpm_statistics": (_i, [_vp, _vp]),
+    "tpm_spectrum_shells": (_i, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
+    "tpm_spectrum": (_i, [_vp, ctypes.POINTER(ctypes.c_double), _i]),
+    "tpm_rdf": (_i, [_vp, ctypes.c_double, _i, ctypes.POINTER(ctypes.c_uint64),
+                     ctypes.POINTER(ctypes.c_double)]),
     "tpm_write_restart": (_i, [_vp, ctypes.c_char_p]),
     "tpm_read_restart": (_i, [_vp, ctypes.c_char_p]),
     "tpm_store": (_i, [_vp, ctypes.c_char_p]),
@@ -172,6 +177,28 @@ class Context:
     def upload_rhs_t(self, a):
         a = np.ascontiguousarray(a, dtype=np.float64)
         self._check(self.L.tpm_upload_particle_rhs_t(self.h, _dptr(a)))
+
+    # ---- diagnostics ----
+    def statistics(self):
+        s = TpmStats()
+        self._check(self.L.tpm_statistics(self.h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def spectrum(self):
+        n, dk = ctypes.c_int(0), ctypes.c_double(0)
+        self._check(self.L.tpm_spectrum_shells(self.h, ctypes.byref(n), ctypes.byref(dk)))
+        E = np.zeros(n.value)
+        self._check(self.L.tpm_spectrum(self.h, E.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                        n.value))
+        return E, dk.value
+
+    def rdf(self, r_max, nbins):
+        pairs = np.zeros(nbins, dtype=np.uint64)
+        g = np.zeros(nbins)
+        self._check(self.L.tpm_rdf(self.h, float(r_max), int(nbins),
+                                   pairs.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                   g.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return pairs, g
 
     def write_restart(self, dirpath):
         self._check(self.L.tpm_write_restart(self.h, dirpath.encode()))

@@ -108,11 +108,11 @@ def make_state(p: Params, npart: int, seed: int) -> State:
 
 
 # ------------------------------------------------------------------ files
-def write_restart(dirpath: str, p: Params, s: State) -> None:
+def write_restart(dirpath: str, p: Params, s: State, statistics: bool = False) -> None:
     """Write deck + Restart_* files for the reference's Initial=1 branch."""
     os.makedirs(dirpath, exist_ok=True)
     with open(os.path.join(dirpath, "deck.txt"), "w") as f:
-        f.write(p.deck_text())
+        f.write(p.deck_text(statistics))
     np.ascontiguousarray(s.RU, dtype=np.float64).tofile(os.path.join(dirpath, "Restart_RU.bin"))
     np.ascontiguousarray(s.Rho, dtype=np.float64).tofile(os.path.join(dirpath, "Restart_Rho.bin"))
     np.ascontiguousarray(s.P, dtype=np.float64).tofile(os.path.join(dirpath, "Restart_P.bin"))

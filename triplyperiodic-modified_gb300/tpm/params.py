@@ -58,6 +58,22 @@ class TpmScalars(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class TpmStats(ctypes.Structure):
+    """Binary layout of ``struct tpm_stats`` in include/tpm.h."""
+
+    _fields_ = [("T_cur", ctypes.c_double), ("num_timestep", ctypes.c_int64)] + [
+        (n, ctypes.c_double) for n in (
+            "Rho_mean", "Rho_max", "Rho_min", "C_mean", "C_max", "C_min", "TKE2",
+            "TKE_U", "TKE_V", "TKE_W", "TKE", "Gas_CFL_Max", "Gas_Max_Diff_CFL", "u_max",
+            "Vp_max", "Tp_max", "Tp_mean", "HT_mean", "Tg_mean", "P0")
+    ] + [("num_iteration", ctypes.c_int32), ("reserved", ctypes.c_int32)] + [
+        (n, ctypes.c_double) for n in ("C_var", "u_rms", "dissipation")
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
+
+
 @dataclass
 class Params:
     """The deck fields the substep uses (params.h:9-59), with reference names."""
@@ -151,7 +167,7 @@ class Params:
         return Params(**d)
 
     # ---- reference deck (params.cpp:23-63) ----
-    def deck_text(self) -> str:
+    def deck_text(self, statistics: bool = False) -> str:
         g = lambda v: repr(float(v))  # shortest round-trip repr == %.17g semantics
         lines = [
             "# deck written by tpm.params (token order of params.cpp:23-63)",
@@ -163,7 +179,7 @@ class Params:
             "1",  # bs
             "0",  # Np_track
             f"{g(1e30)} {g(self.dt)} {g(self.threshold)}",  # T_final dt threshold
-            "0 0",  # Statistics Stat_print
+            "1 0" if statistics else "0 0",  # Statistics Stat_print
             "1000000000 1000000000",  # Data_freq_fast Data_freq_slow
             "./ ./",  # Data_dir Stat_dir
             "1",  # Initial: restart files
