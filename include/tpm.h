@@ -232,9 +232,15 @@ int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, double Ly, doub
 enum {
   TPM_OPT_STORE_DIVERGENCE = 1, /* keep the divergence constraint field for download
                                    (grid.h:97); off by default to save bandwidth */
-  TPM_OPT_DIV_RESIDUAL_EVERY_STAGE = 2 /* mixed path: evaluate the FP64 post-projection
+  TPM_OPT_DIV_RESIDUAL_EVERY_STAGE = 2, /* mixed path: evaluate the FP64 post-projection
                                           divergence residual after every stage, not
                                           only after the last one of each step */
+  TPM_OPT_CUDA_GRAPH = 3 /* tpm_step/tpm_run replay each step from a CUDA graph
+                            captured on first use (one per distinct host state:
+                            the step-copy pointer swaps alternate, so two); the
+                            Poisson stopping test then runs on the device.
+                            Results are bit-identical to eager stepping.  Not used
+                            while profiling is on. */
 };
 int tpm_set_option(tpm_ctx *ctx, int option, int value);
 
@@ -286,6 +292,31 @@ int tpm_spectrum(tpm_ctx *ctx, double *E, int nshells);
  * its ideal-gas expectation Np(Np-1)/2 * (4/3)pi((b+1)^3-b^3)dr^3/(Lx Ly Lz).
  * r_max must be at most min_d L_d/3. */
 int tpm_rdf(tpm_ctx *ctx, double r_max, int nbins, unsigned long long *pairs, double *g);
+
+/* Picks the pencils per block of each FFT pass (x, y, z) of the pressure solve
+ * by timing Poisson iterations on the context's grid; results do not depend on
+ * the choice (each pencil is transformed independently).  The state is kept:
+ * P and the device scalars are restored afterwards.  pens_out (3 ints,
+ * optional) receives the choice. */
+int tpm_autotune(tpm_ctx *ctx, int *pens_out);
+
+/* ---------------------------------------------------------------- ensembles
+ * A batch owns nboxes independent contexts (grids and particle counts may
+ * differ; all on the current device).  tpm_batch_run advances every box by
+ * nsteps: with use_graph, each step of all boxes is one CUDA graph launch
+ * (captured once per distinct state) whose per-box kernel chains run
+ * concurrently on the boxes' streams; without, the boxes step one after
+ * another, eagerly.  Boxes are loaded, initialised and read through the
+ * tpm_ctx API on tpm_batch_box(b, i).  Not in the reference, which runs one
+ * box per MPI job. */
+typedef struct tpm_batch tpm_batch;
+int tpm_batch_create(const tpm_params *params, const int64_t *np, int nboxes, tpm_batch **out);
+int tpm_batch_destroy(tpm_batch *b);
+const char *tpm_batch_last_error(const tpm_batch *b);
+tpm_ctx *tpm_batch_box(tpm_batch *b, int i);
+int tpm_batch_autotune(tpm_batch *b);  /* tpm_autotune once per distinct grid shape */
+int tpm_batch_run(tpm_batch *b, int nsteps, int use_graph);
+int tpm_batch_sync(tpm_batch *b);
 
 /* Per-kernel timing with CUDA events on the context stream (for the bench). */
 int tpm_profile_enable(tpm_ctx *ctx, int on);

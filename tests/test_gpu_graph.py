@@ -1,0 +1,128 @@
+"""Whole-step CUDA graphs, the FFT tile autotuner and batched ensembles.
+
+Every one of these changes only how the kernels are launched, never what they
+compute, so the bar is bit-identical fields, particles and scalars against
+eager stepping of the same boxes.
+"""
+import numpy as np
+import pytest
+
+from golden import load
+from tpm import inputs, params as P
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("RU", "RU_INT", "RHO", "P", "C", "Q")
+
+
+@pytest.fixture(scope="module")
+def capi():
+    from tpm import build, capi
+
+    build.build()
+    return capi
+
+
+def case(dims=(32, 32, 32), npart=5000, seed=3, heat=0.5, eps=1e-13, prec=P.PREC_FP64, **extra):
+    nx, ny, nz = dims
+    p = P.physical(nx, npart, nu=0.02, A=0.1, tau_p=0.1, mass_loading=0.5, heating_Q=heat,
+                   iterations=20, epsilon=eps, precision=prec)
+    if (ny, nz) != (nx, nx):
+        p = p.replace(Ny=ny, Nz=nz, Ly=p.Lx * ny / nx, Lz=p.Lx * nz / nx)
+    s = inputs.make_state(p, npart, seed=seed)
+    return p.replace(dt=inputs.cfl_dt(p, s.RU), **extra), s
+
+
+def state(ctx):
+    out = {f: ctx.download_field(f) for f in FIELDS}
+    out.update({"p_" + k: v for k, v in ctx.download_particles("base").items()})
+    sc = ctx.scalars()
+    out.update({k: sc[k] for k in ("P0", "T_cur", "num_timestep", "last_poisson_iterations",
+                                   "total_poisson_iterations")})
+    return out
+
+
+def assert_same(a, b):
+    assert a.keys() == b.keys()
+    for k in a:
+        assert np.array_equal(np.asarray(a[k]), np.asarray(b[k])), k
+
+
+def run(capi, p, s, nsteps, graph=False, autotune=False):
+    ctx = capi.Context(p, s.npart)
+    ctx.load(s)
+    if autotune:
+        ctx.autotune()
+    ctx.initialize()
+    if graph:
+        ctx.set_graph(True)
+    ctx.run(nsteps)
+    ctx.sync()
+    return ctx
+
+
+@pytest.mark.parametrize("prec,eps", [(P.PREC_FP64, 1e-13), (P.PREC_FP64, 0.0),
+                                      (P.PREC_MIXED, 1e-13)])
+def test_graph_steps_bit_identical_to_eager(capi, prec, eps):
+    p, s = case(prec=prec, eps=eps)
+    eager = run(capi, p, s, 5)
+    graph = run(capi, p, s, 5, graph=True)
+    assert_same(state(graph), state(eager))
+    # a captured step enqueues every allowed Poisson iteration (those after the
+    # device-side stop return at once); eagerly the host stops enqueuing
+    assert graph.launch_count() >= eager.launch_count()
+    if eps > 0:
+        assert 0 < graph.scalars()["last_poisson_iterations"] < 20
+
+
+def test_graph_follows_the_parameter_switch(capi):
+    # threshold crossed after the first step: A, g and Iteration change (params.cpp:80-86)
+    p, s, _, _, _ = load("cooled24_gravity_switch")
+    eager = run(capi, p, s, 4)
+    graph = run(capi, p, s, 4, graph=True)
+    assert_same(state(graph), state(eager))
+
+
+def test_graph_then_eager_then_graph(capi):
+    p, s = case(dims=(24, 30, 16), npart=3000, seed=4)
+    eager = run(capi, p, s, 6)
+    ctx = capi.Context(p, s.npart)
+    ctx.load(s)
+    ctx.initialize()
+    ctx.set_graph(True)
+    ctx.run(2)
+    ctx.set_graph(False)
+    ctx.run(1)
+    ctx.set_graph(True)
+    ctx.run(3)
+    ctx.sync()
+    assert_same(state(ctx), state(eager))
+
+
+def test_autotune_keeps_results(capi):
+    p, s = case(dims=(64, 64, 64), npart=20_000, seed=5)
+    ref = run(capi, p, s, 2)
+    tuned = run(capi, p, s, 2, autotune=True)
+    assert_same(state(tuned), state(ref))
+    pens = tuned.autotune()
+    assert len(pens) == 3 and all(1 <= q <= 32 for q in pens)
+
+
+def test_batch_matches_boxes_run_alone(capi):
+    shapes = [((16, 16, 16), 1000), ((24, 24, 24), 4000), ((32, 32, 32), 9000),
+              ((32, 24, 16), 2500), ((16, 16, 16), 500)]
+    cases = [case(dims=d, npart=n, seed=10 + i, heat=0.3 * (i % 2))
+             for i, (d, n) in enumerate(shapes)]
+    alone = [state(run(capi, p, s, 4)) for p, s in cases]
+    for graph in (True, False):
+        b = capi.Batch([p for p, _ in cases], [s.npart for _, s in cases])
+        for box, (p, s) in zip(b.boxes, cases):
+            box.load(s)
+        b.autotune()
+        for box in b.boxes:
+            box.initialize()
+        b.run(4, graph=graph)
+        b.sync()
+        for box, want in zip(b.boxes, alone):
+            assert_same(state(box), want)
+        b.close()

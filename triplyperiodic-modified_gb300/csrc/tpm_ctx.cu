@@ -96,8 +96,19 @@ void param_update(tpm_ctx *c) {
   }
 }
 
-// poisson::FFT iteration control (poisson.cpp:395-410)
+// poisson::FFT iteration control (poisson.cpp:395-410).  Eagerly, the host
+// reads max|dp| after each iteration when epsilon > 0, as the reference's loop
+// does.  Inside a captured step (device_loop) all max_it iterations are
+// enqueued and the device applies the same test: once max|dp| <= epsilon the
+// remaining iterations' kernels return at once, so the result and the
+// iteration count are the same.
 void poisson_loop(tpm_ctx *c, int max_it, double eps) {
+  TPM_CUDA_TRY(cudaMemsetAsync(&c->dsc->skip, 0, 2 * sizeof(int), c->stream));  // skip, it
+  if (c->device_loop) {
+    for (int k = 0; k < max_it; ++k) tpm::poisson_iteration(c, eps > 0 ? eps : 0.0);
+    c->last_it = -1;  // on the device (DevScalars::it)
+    return;
+  }
   int it = 0;
   double error = 100;
   const bool need_err = eps > 0;
@@ -169,6 +180,13 @@ void end_step(tpm_ctx *c) {
 }  // namespace
 
 namespace tpm {
+
+void step_param_update(tpm_ctx *c) { param_update(c); }
+
+void step_body(tpm_ctx *c) {
+  for (int s = 0; s < 4; ++s) substep(c, s);
+  end_step(c);
+}
 
 void prof_begin(tpm_ctx *c, const char *, cudaEvent_t *ev0) {
   cudaEventCreate(ev0);
@@ -281,8 +299,7 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     push_scalars(c);
     tpm::fft_plans_create(c);
     tpm::rhs_kernels_setup();
-    c->x_blocks = tpm::fft_x_blocks(c);
-    c->err_parts = dalloc<double>(c, c->x_blocks);
+    c->err_parts = dalloc<double>(c, (size_t)g.ny * g.nz);
     // particles
     for (int s = 0; s < 4; ++s)
       for (int q = 0; q < 7; ++q) {
@@ -320,6 +337,7 @@ int tpm_destroy(tpm_ctx *c) {
       cudaEventDestroy(ev.first);
       cudaEventDestroy(ev.second);
     }
+  tpm::graphs_clear(c->graphs);
   for (void *p : c->allocs) cudaFree(p);
   if (c->fft_mem) cudaFree(c->fft_mem);
   if (c->hsc) cudaFreeHost(c->hsc);
@@ -336,6 +354,10 @@ int tpm_set_option(tpm_ctx *c, int option, int value) {
     }
     if (option == TPM_OPT_DIV_RESIDUAL_EVERY_STAGE) {
       c->div_every_stage = value != 0;
+      return TPM_OK;
+    }
+    if (option == TPM_OPT_CUDA_GRAPH) {
+      c->graph_mode = value != 0;
       return TPM_OK;
     }
     return fail(c, TPM_ERR_ARG, "unknown option");
@@ -477,8 +499,8 @@ int tpm_get_scalars(tpm_ctx *c, tpm_scalars *out) {
     out->P0_np1 = c->np1_is_base ? c->hsc->P0 : c->hsc->P0_np1;
     out->T_cur = c->T_cur;
     out->num_timestep = c->num_timestep;
-    out->last_poisson_iterations = c->last_it;
-    out->total_poisson_iterations = c->total_it;
+    out->last_poisson_iterations = c->hsc->it;
+    out->total_poisson_iterations = c->hsc->it_sum;
     out->last_poisson_error = c->p.epsilon > 0 ? c->last_err : c->hsc->err;
     out->max_abs_div = c->p.precision == TPM_PREC_MIXED ? c->hsc->max_div : -1.0;
     if (!std::isfinite(c->hsc->mean_ru[0]) || !std::isfinite(c->hsc->mean_ru[1]) ||
@@ -557,9 +579,7 @@ int tpm_end_step(tpm_ctx *c) {
 int tpm_step(tpm_ctx *c) {
   return guarded(c, [&]() -> int {
     if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
-    param_update(c);
-    for (int s = 0; s < 4; ++s) substep(c, s);
-    end_step(c);
+    tpm::step_any(c);
     return TPM_OK;
   });
 }
@@ -567,11 +587,7 @@ int tpm_step(tpm_ctx *c) {
 int tpm_run(tpm_ctx *c, int nsteps) {
   return guarded(c, [&]() -> int {
     if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
-    for (int k = 0; k < nsteps; ++k) {
-      param_update(c);
-      for (int s = 0; s < 4; ++s) substep(c, s);
-      end_step(c);
-    }
+    for (int k = 0; k < nsteps; ++k) tpm::step_any(c);
     return TPM_OK;
   });
 }

@@ -427,7 +427,7 @@ int tpm_statistics(tpm_ctx *c, tpm_stats *out) {
     s.P0 = ds.P0;
     s.TKE2 = c->stepped ? ds.tke2 : 0.0;
     s.HT_mean = c->stepped ? ds.mean_Q : 0.0;
-    s.num_iteration = c->stepped ? c->last_it : 0;
+    s.num_iteration = c->stepped ? ds.it : 0;
     s.C_var = v[S_C_SQ] / n - s.C_mean * s.C_mean;  // tensor0::var
     s.u_rms = std::sqrt(v[S_USQ] / n / 3.0);
     s.dissipation = 2.0 * (c->p.Mu0 / c->p.Rho0) * (v[S_SS] / n);

@@ -193,6 +193,7 @@ __global__ void k_xfwd_resid(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
                              const double *__restrict__ P, const double *__restrict__ Cf,
                              const double *__restrict__ cc, const double *__restrict__ RHS,
                              const DevScalars *__restrict__ s, T2 *__restrict__ spec, int npen) {
+  if (s->skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using T = typename Cx<T2>::T;
   T2 *a = reinterpret_cast<T2 *>(smem_raw);
@@ -244,7 +245,9 @@ __global__ void k_xfwd_resid(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
 
 // ------------------------------------------------------- 2./4. y pencils
 template <typename T2>
-__global__ void k_fft_y(Grid g, FftPlan pl, T2 *__restrict__ spec, int npen, int sign) {
+__global__ void k_fft_y(Grid g, FftPlan pl, T2 *__restrict__ spec, int npen, int sign,
+                        const int *__restrict__ skip) {
+  if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T2 *a = reinterpret_cast<T2 *>(smem_raw);
   T2 *b = a + pl.n * npen;
@@ -268,7 +271,8 @@ __global__ void k_fft_y(Grid g, FftPlan pl, T2 *__restrict__ spec, int npen, int
 template <typename T2>
 __global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const double *__restrict__ ax,
                               const double *__restrict__ ay, const double *__restrict__ az,
-                              int npen) {
+                              int npen, const int *__restrict__ skip) {
+  if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using T = typename Cx<T2>::T;
   T2 *a = reinterpret_cast<T2 *>(smem_raw);
@@ -314,7 +318,9 @@ __global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const d
 template <typename T2>
 __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
                               const T2 *__restrict__ spec, double *__restrict__ P,
-                              double *__restrict__ partials, int npen) {
+                              double *__restrict__ partials, int npen,
+                              const int *__restrict__ skip) {
+  if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double sh[32];
   using T = typename Cx<T2>::T;
@@ -362,12 +368,20 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   if (threadIdx.x == 0) partials[blockIdx.x] = bm;
 }
 
-__global__ void k_finish_max(const double *__restrict__ partials, int nparts, DevScalars *s) {
+__global__ void k_finish_max(const double *__restrict__ partials, int nparts, DevScalars *s,
+                             double eps_ctl) {
+  if (s->skip) return;
   __shared__ double sh[32];
   double v = 0;
   for (int b = threadIdx.x; b < nparts; b += blockDim.x) v = partials[b] > v ? partials[b] : v;
   double m = block_max(v, sh);
-  if (threadIdx.x == 0) s->err = m;
+  if (threadIdx.x == 0) {
+    s->err = m;
+    s->it += 1;
+    s->it_sum += 1;
+    // poisson.cpp:397: the next iteration runs only while error > epsilon
+    if (eps_ctl > 0 && !(m > eps_ctl)) s->skip = 1;
+  }
 }
 
 // pencils per block: two ping-pong buffers of 32 KB each
@@ -376,6 +390,12 @@ int pens_for(int n, int elem_bytes = 16) {
   if (p < 1) p = 1;
   if (p > 32) p = 32;
   return p;
+}
+
+// largest pencil count whose double2 buffers fit the 64 KB set per kernel
+int pens_cap(int n) {
+  int p = kFftSmemPoints / n;
+  return p < 1 ? 1 : (p > 32 ? 32 : p);
 }
 
 void factorize(int n, FftPlan &pl) {
@@ -411,6 +431,9 @@ void fft_plans_create(tpm_ctx *c) {
   factorize(g.nx / 2, c->fx);
   factorize(g.ny, c->fy);
   factorize(g.nz, c->fz);
+  c->pen[0] = pens_for(c->fx.n);
+  c->pen[1] = pens_for(c->fy.n);
+  c->pen[2] = pens_for(c->fz.n);
   // twiddles: one block of [n] double2 + [n] float2 per plan, plus the r2c table
   auto table = [](int n, std::vector<double2> &d, std::vector<float2> &f) {
     d.resize(n);
@@ -482,68 +505,62 @@ void fft_plans_create(tpm_ctx *c) {
 // path; float2 on the mixed path, where each iteration is one step of
 // iterative refinement: FP64 residual, FP32 correction, FP64 update).
 template <typename T2>
-static void poisson_iteration_t(tpm_ctx *c) {
+static void poisson_iteration_t(tpm_ctx *c, double eps_ctl) {
   const Grid &g = c->g;
   const long long nrows = (long long)g.ny * g.nz;
   T2 *spec = reinterpret_cast<T2 *>(c->spec);
   const T2 *r2c = sizeof(T2) == sizeof(double2) ? reinterpret_cast<const T2 *>(c->r2c64)
                                                 : reinterpret_cast<const T2 *>(c->r2c32);
+  const int *skip = &c->dsc->skip;
+  const int npx = c->pen[0], npy = c->pen[1], npz = c->pen[2];
+  const int xblocks = (int)((nrows + npx - 1) / npx);
   {
-    int npen = pens_for(c->fx.n);
-    int blocks = (int)((nrows + npen - 1) / npen);
-    size_t smem = 2 * (size_t)npen * c->fx.n * sizeof(T2);
+    size_t smem = 2 * (size_t)npx * c->fx.n * sizeof(T2);
     if (c->p.precision == TPM_PREC_MIXED)
-      TPM_LAUNCH(c, "fft_x_fwd_resid", (k_xfwd_resid<T2, true>), blocks, kFftThreads, smem, g,
-                 c->fx, r2c, c->P, c->Cs, c->cc, c->RHS, c->dsc, spec, npen);
+      TPM_LAUNCH(c, "fft_x_fwd_resid", (k_xfwd_resid<T2, true>), xblocks, kFftThreads, smem, g,
+                 c->fx, r2c, c->P, c->Cs, c->cc, c->RHS, c->dsc, spec, npx);
     else
-      TPM_LAUNCH(c, "fft_x_fwd_resid", (k_xfwd_resid<T2, false>), blocks, kFftThreads, smem, g,
-                 c->fx, r2c, c->P, c->Cface, c->cc, c->RHS, c->dsc, spec, npen);
+      TPM_LAUNCH(c, "fft_x_fwd_resid", (k_xfwd_resid<T2, false>), xblocks, kFftThreads, smem, g,
+                 c->fx, r2c, c->P, c->Cface, c->cc, c->RHS, c->dsc, spec, npx);
   }
   {
-    int npen = pens_for(c->fy.n);
-    int blocks = g.nz * ((g.nxh + npen - 1) / npen);
-    size_t smem = 2 * (size_t)npen * c->fy.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, kFftThreads, smem, g, c->fy, spec, npen, -1);
+    int blocks = g.nz * ((g.nxh + npy - 1) / npy);
+    size_t smem = 2 * (size_t)npy * c->fy.n * sizeof(T2);
+    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, kFftThreads, smem, g, c->fy, spec, npy, -1, skip);
   }
   {
-    int npen = pens_for(c->fz.n);
-    int blocks = g.ny * ((g.nxh + npen - 1) / npen);
-    size_t smem = 2 * (size_t)npen * c->fz.n * sizeof(T2);
+    int blocks = g.ny * ((g.nxh + npz - 1) / npz);
+    size_t smem = 2 * (size_t)npz * c->fz.n * sizeof(T2);
     TPM_LAUNCH(c, "fft_z_solve", k_fft_z_solve<T2>, blocks, kFftThreads, smem, g, c->fz, spec,
-               c->ax, c->ay, c->az, npen);
+               c->ax, c->ay, c->az, npz, skip);
   }
   {
-    int npen = pens_for(c->fy.n);
-    int blocks = g.nz * ((g.nxh + npen - 1) / npen);
-    size_t smem = 2 * (size_t)npen * c->fy.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, kFftThreads, smem, g, c->fy, spec, npen, +1);
+    int blocks = g.nz * ((g.nxh + npy - 1) / npy);
+    size_t smem = 2 * (size_t)npy * c->fy.n * sizeof(T2);
+    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, kFftThreads, smem, g, c->fy, spec, npy, +1, skip);
   }
   {
-    int npen = pens_for(c->fx.n);
-    int blocks = (int)((nrows + npen - 1) / npen);
-    size_t smem = 2 * (size_t)npen * c->fx.n * sizeof(T2);
+    size_t smem = 2 * (size_t)npx * c->fx.n * sizeof(T2);
     double *parts = c->err_parts;
-    TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, blocks, kFftThreads, smem, g, c->fx,
-               r2c, spec, c->P, parts, npen);
-    TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 256, 0, parts, blocks, c->dsc);
+    TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, xblocks, kFftThreads, smem, g, c->fx,
+               r2c, spec, c->P, parts, npx, skip);
+    TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 256, 0, parts, xblocks, c->dsc, eps_ctl);
   }
 }
 
-void poisson_iteration(tpm_ctx *c) {
+void poisson_iteration(tpm_ctx *c, double eps_ctl) {
   if (c->p.precision == TPM_PREC_MIXED)
-    poisson_iteration_t<float2>(c);
+    poisson_iteration_t<float2>(c, eps_ctl);
   else
-    poisson_iteration_t<double2>(c);
+    poisson_iteration_t<double2>(c, eps_ctl);
 }
+
+int pens_default(int n, int elem_bytes) { return pens_for(n, elem_bytes); }
+int pens_max(int n, int) { return pens_cap(n); }
 
 }  // namespace tpm
 
 namespace tpm {
-int fft_x_blocks(const tpm_ctx *c) {
-  const long long nrows = (long long)c->g.ny * c->g.nz;
-  int npen = pens_for(c->g.nx / 2);
-  return (int)((nrows + npen - 1) / npen);
-}
 
 // ---------------------------------------------------------- energy spectrum
 // Forward 3-D transform of one real face-velocity component with the same
@@ -618,7 +635,7 @@ void spectrum_mode_energy(tpm_ctx *c, const double *U3, double2 *spec, double *e
       int blocks = g.nz * ((g.nxh + npen - 1) / npen);
       size_t smem = 2 * (size_t)npen * c->fy.n * sizeof(double2);
       TPM_LAUNCH(c, "spec_y", k_fft_y<double2>, blocks, kFftThreads, smem, g, c->fy, spec, npen,
-                 -1);
+                 -1, nullptr);
     }
     {
       int npen = pens_for(c->fz.n);
@@ -809,24 +826,24 @@ extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, doub
       int npen = pens_for(fy.n);
       int blocks = Nz * ((g.nxh + npen - 1) / npen);
       size_t smem = 2 * (size_t)npen * fy.n * sizeof(double2);
-      k_fft_y<double2><<<blocks, kFftThreads, smem, st>>>(g, fy, spec, npen, -1);
+      k_fft_y<double2><<<blocks, kFftThreads, smem, st>>>(g, fy, spec, npen, -1, nullptr);
     }
     {
       int npen = pens_for(fz.n);
       int blocks = Ny * ((g.nxh + npen - 1) / npen);
       size_t smem = 2 * (size_t)npen * fz.n * sizeof(double2);
-      k_fft_z_solve<double2><<<blocks, kFftThreads, smem, st>>>(g, fz, spec, ax, ay, az, npen);
+      k_fft_z_solve<double2><<<blocks, kFftThreads, smem, st>>>(g, fz, spec, ax, ay, az, npen, nullptr);
     }
     {
       int npen = pens_for(fy.n);
       int blocks = Nz * ((g.nxh + npen - 1) / npen);
       size_t smem = 2 * (size_t)npen * fy.n * sizeof(double2);
-      k_fft_y<double2><<<blocks, kFftThreads, smem, st>>>(g, fy, spec, npen, +1);
+      k_fft_y<double2><<<blocks, kFftThreads, smem, st>>>(g, fy, spec, npen, +1, nullptr);
     }
     {
       size_t smem = 2 * (size_t)npx * fx.n * sizeof(double2);
-      k_xinv_update<double2><<<xblocks, kFftThreads, smem, st>>>(g, fx, r2c, spec, P, errp, npx);
-      k_finish_max<<<1, 256, 0, st>>>(errp, xblocks, dsc);
+      k_xinv_update<double2><<<xblocks, kFftThreads, smem, st>>>(g, fx, r2c, spec, P, errp, npx, nullptr);
+      k_finish_max<<<1, 256, 0, st>>>(errp, xblocks, dsc, 0.0);
     }
     if (cudaGetLastError() != cudaSuccess) return TPM_ERR_CUDA;
     it++;

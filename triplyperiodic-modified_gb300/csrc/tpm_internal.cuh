@@ -54,7 +54,13 @@ struct DevScalars {
   double max_div;    // FP64 post-projection residual (mixed path)
   double tke2;       // mean(U^2) of the last stage before projection (grid.cpp:911)
   int nonfinite;
-  int pad;
+  // Poisson iteration control on the device (graph-captured steps): `skip`
+  // turns the remaining captured iterations of a solve into no-ops once
+  // max|dp| <= epsilon (poisson.cpp:397); `it` counts the iterations run by
+  // the current solve, `it_sum` all iterations since create.
+  int skip;
+  int it;
+  int it_sum;
 };
 
 // 1-D FFT plan in device memory: radices and exp(-2 pi i m / n) twiddles.
@@ -75,6 +81,30 @@ struct ProfEntry {
   int launches = 0;
   double total_ms = 0;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+};
+
+// Host-side state that decides what a step launches: the buffers each role
+// points at (the RK and step copies are pointer swaps), the flags and the
+// parameters baked into kernel arguments.  A CUDA graph captured from one
+// state replays correctly exactly when the context is in that state again.
+struct HostState {
+  double *RU_int, *RU_new, *Rho, *Rho_int, *Rho_new, *Rho_np1, *C, *C_next;
+  float *RUi32, *RUn32;
+  double *pq[4][7];
+  const double *tau;
+  int q_parts;
+  int np1_is_base, rui32_stale, stepped, store_div, div_every_stage;
+  int Iteration;
+  int pen[3];
+  double A, gx, gy, gz, I0;
+};
+
+// One captured step of one or more boxes, with the host states before and
+// after it (one per box) and the kernels it launches per box.
+struct GraphEntry {
+  std::vector<HostState> pre, post;
+  std::vector<int64_t> launches;
+  cudaGraphExec_t exec = nullptr;
 };
 
 }  // namespace tpm
@@ -122,8 +152,9 @@ struct tpm_ctx {
   tpm::FftPlan fx, fy, fz;
   const double2 *r2c64 = nullptr;
   const float2 *r2c32 = nullptr;
-  double *err_parts = nullptr;  // one max|dp| per x-pass block
-  int x_blocks = 0;
+  double *err_parts = nullptr;  // one max|dp| per x-pass block (sized for one row per block)
+  int pen[3] = {1, 1, 1};       // FFT pencils per block of the x, y, z passes (autotuned)
+  bool device_loop = false;     // Poisson stopping test on the device (no host read)
   void *fft_mem = nullptr;
 
   // ---- particles (device) ----
@@ -143,6 +174,10 @@ struct tpm_ctx {
 
   bool store_div = false;
   bool div_every_stage = false;
+
+  // ---- CUDA graph replay of whole steps (tpm_graph.cu) ----
+  bool graph_mode = false;
+  std::vector<tpm::GraphEntry> graphs;
 
   // ---- diagnostics (allocated on first use; tpm_diag.cu) ----
   double *diag_u = nullptr;      // 3n: face velocity RU/I_C2F(Rho) of the base state
@@ -190,13 +225,22 @@ void launch_to_double(tpm_ctx *c, const float *src, double *dst, long long n);
 
 // ---- Poisson / FFT (tpm_fft.cu) ----
 void fft_plans_create(tpm_ctx *c);
-int fft_x_blocks(const tpm_ctx *c);
-// one Richardson iteration; returns nothing (error lands in dsc->err)
-void poisson_iteration(tpm_ctx *c);
+// one Richardson iteration; returns nothing (error lands in dsc->err).  With
+// eps_ctl > 0 the iteration also sets dsc->skip once max|dp| <= eps_ctl, and
+// every kernel of a later iteration returns at once while it is set.
+void poisson_iteration(tpm_ctx *c, double eps_ctl = 0.0);
+int pens_default(int n, int elem_bytes);
+int pens_max(int n, int elem_bytes);
 // energy per half-spectrum mode of the face velocity U3 (3n), summed over
 // components (spec: FP64 half-spectrum scratch)
 void spectrum_mode_energy(tpm_ctx *c, const double *U3, double2 *spec, double *emode);
 void spectrum_kernels_setup();
+
+// ---- step driver (tpm_ctx.cu) and graph replay (tpm_graph.cu) ----
+void step_param_update(tpm_ctx *c);  // PARAM.update (params.cpp:80-86)
+void step_body(tpm_ctx *c);          // four substeps and the end of step
+void step_any(tpm_ctx *c);           // one step, replayed from a graph in graph mode
+void graphs_clear(std::vector<GraphEntry> &cache);
 
 // ---- particles (tpm_particles.cu) ----
 void launch_particle_push(tpm_ctx *c, int stage, bool np1_in_base);

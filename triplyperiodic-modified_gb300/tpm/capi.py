@@ -24,6 +24,7 @@ VECTOR = {"RU", "RU_INT", "RU_NEW", "RU_NP1", "FP"}
 PSET = dict(base=0, int=1, new=2, np1=3)
 OPT_STORE_DIVERGENCE = 1
 OPT_DIV_RESIDUAL_EVERY_STAGE = 2
+OPT_CUDA_GRAPH = 3
 STATUS = {0: "TPM_OK", -1: "TPM_ERR_ARG", -2: "TPM_ERR_CUDA", -3: "TPM_ERR_TIMEOUT",
           -4: "TPM_ERR_NONFINITE", -5: "TPM_ERR_UNSUPPORTED", -6: "TPM_ERR_STATE",
           -7: "TPM_ERR_NOMEM"}
@@ -69,6 +70,14 @@ SIGNATURES = {
     "tpm_profile_report": (_i, [_vp, ctypes.c_char_p, _i, ctypes.POINTER(_i), _dp, _i]),
     "tpm_profile_reset": (_i, [_vp]),
     "tpm_launch_count": (_i64, [_vp]),
+    "tpm_autotune": (_i, [_vp, ctypes.POINTER(_i)]),
+    "tpm_batch_create": (_i, [_vp, ctypes.POINTER(_i64), _i, ctypes.POINTER(_vp)]),
+    "tpm_batch_destroy": (_i, [_vp]),
+    "tpm_batch_last_error": (ctypes.c_char_p, [_vp]),
+    "tpm_batch_box": (_vp, [_vp, _i]),
+    "tpm_batch_autotune": (_i, [_vp]),
+    "tpm_batch_run": (_i, [_vp, _i, _i]),
+    "tpm_batch_sync": (_i, [_vp]),
 }
 
 _lib = None
@@ -116,15 +125,38 @@ class Context:
             self.h = None
             raise TpmError(rc, msg)
 
+    @classmethod
+    def borrowed(cls, handle, p: Params, npart: int, owner):
+        """A view of a context owned elsewhere (a box of a Batch)."""
+        self = cls.__new__(cls)
+        self.L = load_library()
+        self.p = p
+        self.npart = int(npart)
+        self._cp = p.to_c()
+        self.h = _vp(handle)
+        self._owner = owner
+        return self
+
     def _check(self, rc):
         if rc != 0:
             raise TpmError(rc, self.L.tpm_last_error(self.h).decode())
         return rc
 
     def close(self):
+        if getattr(self, "_owner", None) is not None:
+            self.h = None
+            return
         if getattr(self, "h", None):
             self.L.tpm_destroy(self.h)
             self.h = None
+
+    def set_graph(self, on=True):
+        self.set_option(OPT_CUDA_GRAPH, int(on))
+
+    def autotune(self):
+        pens = (_i * 3)()
+        self._check(self.L.tpm_autotune(self.h, pens))
+        return list(pens)
 
     def __del__(self):
         self.close()
@@ -364,3 +396,45 @@ class Grid:
         if name in alias:
             return self.ctx.download_field(alias[name])
         raise AttributeError(name)
+
+
+class Batch:
+    """Independent boxes stepped together (tpm_batch_*)."""
+
+    def __init__(self, params: list, nparts: list):
+        self.L = load_library()
+        self.params = list(params)
+        self.nparts = [int(n) for n in nparts]
+        arr = (TpmParams * len(params))(*[p.to_c() for p in params])
+        nps = (_i64 * len(params))(*self.nparts)
+        h = _vp()
+        rc = self.L.tpm_batch_create(arr, nps, len(params), ctypes.byref(h))
+        if rc != 0:
+            raise TpmError(rc, "batch create failed")
+        self.h = h
+        self.boxes = [Context.borrowed(self.L.tpm_batch_box(h, i), p, n, self)
+                      for i, (p, n) in enumerate(zip(self.params, self.nparts))]
+
+    def _check(self, rc):
+        if rc != 0:
+            raise TpmError(rc, self.L.tpm_batch_last_error(self.h).decode())
+        return rc
+
+    def autotune(self):
+        self._check(self.L.tpm_batch_autotune(self.h))
+
+    def run(self, nsteps, graph=True):
+        self._check(self.L.tpm_batch_run(self.h, int(nsteps), int(graph)))
+
+    def sync(self):
+        self._check(self.L.tpm_batch_sync(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            for b in self.boxes:
+                b.h = None
+            self.L.tpm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
