@@ -72,7 +72,7 @@ typedef struct tpm_params {
   double epsilon;           /* Poisson stop criterion on max|dp| */
   int32_t ParticleGravity;
   int32_t elongated_box;    /* must be 0 (outside the ported path) */
-  int32_t solve_for_scalar; /* must be 0 */
+  int32_t solve_for_scalar; /* passive scalar transport (grid.cpp:743-772) */
   int32_t solve_for_vector; /* must be 0 */
   double A1, A2;            /* linear forcing coefficient */
   double Rho0;
@@ -84,6 +84,10 @@ typedef struct tpm_params {
   double np0;               /* particle number density */
   double Dp, Rhop, Cvp, epsilonp, Nu;
   double I01, I02;          /* radiative intensity */
+  double D_M;               /* passive-scalar diffusivity (params.h:51) */
+  int32_t S1_type;          /* passive-scalar source (params.h:53): 0 = cos(x) source with
+                               its mean removed, else -u (mean gradient along x) */
+  int32_t reserved;
 } tpm_params;
 
 /* Field identifiers for upload/download.  Vector fields are 3*N doubles. */

@@ -32,6 +32,7 @@ class State:
     T_cur: float = 0.0
     num_timestep: int = 0
     tau: np.ndarray | None = None   # optional per-particle Stokes time (extension)
+    PS: np.ndarray | None = None    # optional passive scalar (Nz, Ny, Nx)
 
     @property
     def npart(self) -> int:
@@ -123,6 +124,9 @@ def write_restart(dirpath: str, p: Params, s: State, statistics: bool = False) -
         os.path.join(dirpath, "Restart_Part_flag.bin"))
     with open(os.path.join(dirpath, "Restart_numbers.dat"), "w") as f:
         f.write(f"{s.P0!r} {s.T_cur!r} {s.num_timestep}\n")
+    if s.PS is not None:  # read when Initial_C = 1 (grid.cpp:445-450)
+        np.ascontiguousarray(s.PS, dtype=np.float64).tofile(
+            os.path.join(dirpath, "Restart_Passive_Scalar.bin"))
 
 
 def read_restart(dirpath: str, p: Params) -> State:
@@ -133,6 +137,24 @@ def read_restart(dirpath: str, p: Params) -> State:
     part["flag"] = rd("Restart_Part_flag.bin", np.int32)
     with open(os.path.join(dirpath, "Restart_numbers.dat")) as f:
         tok = f.read().split()
+    ps = os.path.join(dirpath, "Restart_Passive_Scalar.bin")
+    PS = rd("Restart_Passive_Scalar.bin").reshape(shape) if os.path.exists(ps) else None
     return State(RU=RU, Rho=rd("Restart_Rho.bin").reshape(shape),
                  P=rd("Restart_P.bin").reshape(shape), part=part, P0=float(tok[0]),
-                 T_cur=float(tok[1]), num_timestep=int(tok[2]))
+                 T_cur=float(tok[1]), num_timestep=int(tok[2]), PS=PS)
+
+
+def passive_scalar(p: Params, seed: int) -> np.ndarray:
+    """A smooth random scalar field at the cell centres: a few low Fourier modes."""
+    rng = np.random.Generator(np.random.PCG64(1000 + seed))
+    z, y, x = np.meshgrid((np.arange(p.Nz) + 0.5) * (p.Lz / p.Nz),
+                          (np.arange(p.Ny) + 0.5) * (p.Ly / p.Ny),
+                          (np.arange(p.Nx) + 0.5) * (p.Lx / p.Nx), indexing="ij")
+    f = np.zeros((p.Nz, p.Ny, p.Nx))
+    for _ in range(6):
+        k = rng.integers(-3, 4, size=3)
+        ph = rng.uniform(0, 2 * np.pi)
+        f += rng.standard_normal() * np.cos(k[0] * 2 * np.pi / p.Lx * x +
+                                            k[1] * 2 * np.pi / p.Ly * y +
+                                            k[2] * 2 * np.pi / p.Lz * z + ph)
+    return f

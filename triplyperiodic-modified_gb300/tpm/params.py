@@ -39,6 +39,7 @@ class TpmParams(ctypes.Structure):
         ("Dp", ctypes.c_double), ("Rhop", ctypes.c_double), ("Cvp", ctypes.c_double),
         ("epsilonp", ctypes.c_double), ("Nu", ctypes.c_double),
         ("I01", ctypes.c_double), ("I02", ctypes.c_double),
+        ("D_M", ctypes.c_double), ("S1_type", ctypes.c_int32), ("reserved", ctypes.c_int32),
     ]
 
 
@@ -121,6 +122,8 @@ class Params:
     elongated_box: int = 0
     solve_for_scalar: int = 0
     solve_for_vector: int = 0
+    D_M: float = 0.0          # passive-scalar diffusivity (params.h:51)
+    S1_type: int = 1          # passive-scalar source type (params.h:53, token s1t)
 
     # ---- derived (params.cpp:70-77, params.h:133-138) ----
     @property
@@ -158,7 +161,8 @@ class Params:
     def to_c(self) -> TpmParams:
         c = TpmParams()
         for f in TpmParams._fields_:
-            setattr(c, f[0], getattr(self, f[0]))
+            if f[0] != "reserved":
+                setattr(c, f[0], getattr(self, f[0]))
         return c
 
     def replace(self, **kw) -> "Params":
@@ -183,7 +187,7 @@ class Params:
             "1000000000 1000000000",  # Data_freq_fast Data_freq_slow
             "./ ./",  # Data_dir Stat_dir
             "1",  # Initial: restart files
-            "5",  # Initial_C: analytic scalar (never advanced)
+            "1" if self.solve_for_scalar else "5",  # Initial_C: Restart_Passive_Scalar.bin
             "2",  # Initial_V: RV = 0
             "0 0",  # PreCond Solver (0 = FFT)
             f"{self.cooling}",
@@ -204,9 +208,9 @@ class Params:
             f"{g(self.epsilonp)}",
             f"{g(self.Nu)}",
             f"{g(self.I01)} {g(self.I02)}",
-            "0",  # D_M
+            f"{g(self.D_M)}",  # D_M
             "0",  # eta
-            "1",  # s1t
+            f"{self.S1_type}",  # s1t
             "1",  # s2t
         ]
         return "\n".join(lines) + "\n"
@@ -258,3 +262,25 @@ WORKLOADS = {
     "box64_p2e5": dict(N=64, npart=200_000, nu=0.01, A=0.1, tau_p=0.1, mass_loading=0.3,
                        heating_Q=0.0, seed=3),
 }
+
+
+def ensemble_boxes(nboxes: int = 48, precision: int = PREC_MIXED):
+    """The batched-ensemble workload: box b (seed b) has N drawn uniformly from
+    {32, 48, 64, 96} and a particle count log-uniform in [1e4, 5e5], with the
+    physics of the 32^3 workload (A = 0.1, tau_p = 0.1, mass loading 0.2, no
+    heating) and nu set so that kmax*eta = 1.5.  With the seeded spectrum
+    E(k) ~ k^4 exp(-2 (k/4)^2) at u_rms = 1, <|grad u|^2> = 2*(3/2)*20 = 60, so
+    eps = 60 nu, eta = (nu^3/eps)^(1/4), and kmax = N/2 gives nu = sqrt(60)*9/N^2.
+    Returns [(Params, npart, seed)]."""
+    import numpy as np
+
+    out = []
+    for b in range(nboxes):
+        rng = np.random.Generator(np.random.PCG64(b))
+        N = int(rng.choice([32, 48, 64, 96]))
+        npart = int(round(np.exp(rng.uniform(np.log(1e4), np.log(5e5)))))
+        nu = float(np.sqrt(60.0) * 9.0 / N ** 2)
+        p = physical(N, npart, nu=nu, A=0.1, tau_p=0.1, mass_loading=0.2, heating_Q=0.0,
+                     iterations=20, epsilon=1e-13, precision=precision)
+        out.append((p, npart, b))
+    return out
