@@ -107,6 +107,7 @@ enum {
                             before the -mp/Vcell factor (vector)               */
   TPM_FIELD_RHS_POIS,    /* grid.h:76  Poisson right-hand side (mean removed)  */
   TPM_FIELD_DIVERGENCE,  /* grid.h:97  thermodynamic divergence constraint     */
+  TPM_FIELD_PASSIVE_SCALAR, /* grid.h:66 Passive_Scalar (solve_for_scalar only)  */
   TPM_FIELD_COUNT
 };
 
@@ -279,6 +280,8 @@ typedef struct tpm_stats {
   double u_rms;                /* sqrt(mean(u^2+v^2+w^2)/3), u = RU/I_C2F(Rho) */
   double dissipation;          /* 2 (Mu0/Rho0) <S_ij S_ij>, strain rate from the face
                                   velocity with the staggered differences */
+  double Passive_Scalar_mean;  /* Passive_Scalar_mean: mean of the squared scalar
+                                  (grid.cpp:913); 0 without solve_for_scalar */
 } tpm_stats;
 int tpm_statistics(tpm_ctx *ctx, tpm_stats *out);
 

@@ -30,7 +30,7 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "tpm_ref")
 
 F = dict(RU=0, RU_INT=1, RU_NEW=2, RU_NP1=3, RHO=4, RHO_INT=5, RHO_NEW=6, RHO_NP1=7, P=8,
-         C=9, Q=10, FP=11, RHS_POIS=12, DIVERGENCE=13)
+         C=9, Q=10, FP=11, RHS_POIS=12, DIVERGENCE=13, PASSIVE_SCALAR=14)
 VECTOR_FIELDS = {"RU", "RU_INT", "RU_NEW", "RU_NP1", "FP"}
 
 
@@ -147,6 +147,8 @@ class Oracle:
         self.set_field("RU", s.RU)
         self.set_field("RHO", s.Rho)
         self.set_field("P", s.P)
+        if s.PS is not None:
+            self.set_field("PASSIVE_SCALAR", s.PS)
         self.set_particles(s.part, 0)
         lib().orc_set_scalars(self.h, s.P0, s.T_cur, s.num_timestep)
         if s.tau is not None:
@@ -271,6 +273,8 @@ def read_reference_dump(p: Params, out: str, info: dict | None = None) -> dict:
     for name in ("Rho", "Rho_new", "Rho_np1", "P", "C", "RHS_Part_Temp", "RHS_Pois",
                  "divergence"):
         d[name] = rd(name + ".bin").reshape(shape)
+    if os.path.exists(os.path.join(out, "Passive_Scalar.bin")):
+        d["Passive_Scalar"] = rd("Passive_Scalar.bin").reshape(shape)
     part = {q: rd(f"Part_{q}.bin") for q in inputs.PQ}
     part["flag"] = rd("Part_flag.bin", np.int32)
     part["RHS_T"] = rd("Part_RHS_T.bin")

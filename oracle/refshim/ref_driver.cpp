@@ -75,6 +75,7 @@ int main(int argc, char **argv) {
       GRID.Update_Rho();
       GRID.Update_P0();
       if (!as_shipped) GRID.Update_Particle();
+      if (PARAM.solve_for_scalar()) GRID.Update_Passive_Scalar();  // simulation.cpp:65
       GRID.Update_RU_WOP();
       GRID.Compute_Div_U_new();
       GRID.Compute_RHS_Pois();
@@ -89,6 +90,7 @@ int main(int argc, char **argv) {
         GRID.Update_Rho();
         GRID.Update_P0();
         if (!as_shipped) GRID.Update_Particle();
+        if (PARAM.solve_for_scalar()) GRID.Update_Passive_Scalar();  // simulation.cpp:65
         GRID.Update_RU_WOP();
         GRID.Compute_Div_U_new();
         GRID.Compute_RHS_Pois();
@@ -119,6 +121,8 @@ int main(int argc, char **argv) {
   COMM.write(GRID.RHS_RU, (char *)P("RHS_RU.bin").c_str());
   COMM.write(GRID.RHS_Pois, (char *)P("RHS_Pois.bin").c_str());
   COMM.write(GRID.divergence, (char *)P("divergence.bin").c_str());
+  if (PARAM.solve_for_scalar())
+    COMM.write(GRID.Passive_Scalar, (char *)P("Passive_Scalar.bin").c_str());
   int np = GRID.part.Np;
   dump_vec(P("Part_x.bin"), GRID.part.x, np);
   dump_vec(P("Part_y.bin"), GRID.part.y, np);

@@ -51,6 +51,9 @@ struct orc {
   int Iteration, n_it, total_it;
   double A, gx, gy, gz, I0, last_err;
   double met;  /* mean_energy_transferred of the last Update_P0 (grid.cpp:818) */
+  /* passive scalar (grid.h:64-70), allocated with solve_for_scalar */
+  double *PS, *PS_int, *PS_new, *PS_np1, *RHS_PS, *S1;
+  vec3 PS_face, ps_tmp;
   int stepped; /* a full step has run since orc_initialize */
 };
 
@@ -105,6 +108,11 @@ orc *orc_create(const tpm_params *p, int64_t np) {
   o->Iteration = p->Iteration1; o->A = p->A1;
   o->gx = p->gx1; o->gy = p->gy1; o->gz = p->gz1; o->I0 = p->I01;
   o->P0 = p->Rho0 * p->T0 * o->R; /* params.cpp:71 */
+  if (p->solve_for_scalar) {
+    o->PS = alloc(n); o->PS_int = alloc(n); o->PS_new = alloc(n); o->PS_np1 = alloc(n);
+    o->RHS_PS = alloc(n); o->S1 = alloc(n);
+    o->PS_face = valloc(n); o->ps_tmp = valloc(n);
+  }
   return o;
 }
 
@@ -113,6 +121,10 @@ void orc_destroy(orc *o) {
   vec3 *vs[] = {&o->RU, &o->RU_int, &o->RU_new, &o->RU_np1, &o->RHS_RU, &o->U, &o->Rho_face, &o->Fp,
                 &o->dummy, &o->dummy2, &o->pdummy};
   for (size_t i = 0; i < sizeof(vs) / sizeof(vs[0]); ++i) vfree(*vs[i]);
+  if (o->PS) {
+    vfree(o->PS_face); vfree(o->ps_tmp);
+    free(o->PS); free(o->PS_int); free(o->PS_new); free(o->PS_np1); free(o->RHS_PS); free(o->S1);
+  }
   double *ss[] = {o->Rho, o->Rho_int, o->Rho_new, o->Rho_np1, o->RHS_Rho, o->P, o->C, o->T,
                   o->divergence, o->RHS_Pois, o->RHS_Part_Temp, o->center_coeff, o->RHS_new,
                   o->fft, o->RHS_u, o->RHS_v, o->RHS_w, o->RHS_T, o->ug, o->vg, o->wg, o->Tg,
@@ -700,6 +712,7 @@ static void time_advance_rk4(orc *o) {
   vcopy(o, o->RU_int, o->RU_new);
   o->P0_int = o->P0_new;
   pcopy(o, 1, 2);
+  if (o->PS) memcpy(o->PS_int, o->PS_new, sizeof(double) * (size_t)o->n); /* grid.cpp:897 */
 }
 
 /* PARAM.update, params.cpp:80-86 */
@@ -712,10 +725,61 @@ static void param_update(orc *o) {
   }
 }
 
+/* grid::C_Source (grid.cpp:718-741) with scalar_source.h's Scalar_Source
+ * (A*cos(k*x), A = k = 1), called with (X, Y, X, T) */
+static void c_source(orc *o) {
+  for (int k = 0; k < o->nz; ++k)
+    for (int j = 0; j < o->ny; ++j)
+      for (int i = 0; i < o->nx; ++i) {
+        const double X = o->dx / 2. + i * o->dx;
+        const double A = 1., kk = 1.;
+        o->S1[IDX(o, i, j, k)] = A * cos(kk * X);
+      }
+}
+
+/* grid::Update_Passive_Scalar, grid.cpp:743-772 */
+static void update_passive_scalar(orc *o, int s) {
+  const long n = o->n;
+  vdivide(o, o->RU_int, o->Rho_face, o->U); /* U = RU_int / Rho_face */
+  vec3 d = o->ps_tmp;                       /* dummy = U * Passive_Scalar_face */
+  for (long c = 0; c < n; ++c) {
+    d.x[c] = o->U.x[c] * o->PS_face.x[c];
+    d.y[c] = o->U.y[c] * o->PS_face.y[c];
+    d.z[c] = o->U.z[c] * o->PS_face.z[c];
+  }
+  double *conv = o->RHS_new; /* dummy2.x: poisson scratch, dead here */
+  div_f2c(o, d, conv);
+  double *diff = o->center_coeff; /* dummy2.y */
+  del2(o, o->PS_int, diff);
+  c_source(o);
+  for (long c = 0; c < n; ++c) o->RHS_PS[c] = o->p.D_M * diff[c] + -1 * conv[c];
+  if (!o->p.S1_type) {
+    double m = field_mean(o, o->S1);
+    for (long c = 0; c < n; ++c) o->S1[c] -= m;
+    for (long c = 0; c < n; ++c) o->RHS_PS[c] += o->S1[c];
+  } else {
+    for (int i = 0; i < o->nx; ++i) /* dummy.x = Ix_F2C(U.x) (tensor0.cpp:268-271) */
+      for (int j = 0; j < o->ny; ++j)
+        for (int k = 0; k < o->nz; ++k)
+          d.x[IDX(o, i, j, k)] = (o->U.x[IDX(o, i, j, k)] + o->U.x[IDX(o, wrap(i + 1, o->nx), j, k)]) * 0.5;
+    for (long c = 0; c < n; ++c) o->RHS_PS[c] += -1 * d.x[c];
+  }
+  const double a = o->p.dt * RK4_post[s];
+  for (long c = 0; c < n; ++c) o->PS_np1[c] += a * o->RHS_PS[c];
+  if (s != 3) {
+    const double b = o->p.dt * RK4_pre[s];
+    for (long c = 0; c < n; ++c) o->PS_new[c] = 1 * o->PS[c] + b * o->RHS_PS[c];
+  } else {
+    memcpy(o->PS_new, o->PS_np1, sizeof(double) * (size_t)n);
+  }
+  interp_c2f_vec(o, o->PS_new, o->PS_face);
+}
+
 void orc_substep(orc *o, int s, int with_particles) {
   update_rho(o, s);
   update_p0(o, s);
   if (with_particles) update_particle(o, s);
+  if (o->PS) update_passive_scalar(o, s);
   update_ru_wop(o, s);
   compute_div_u_new(o);
   compute_rhs_pois(o, s);
@@ -735,6 +799,7 @@ void orc_end_step(orc *o) {
     for (long c = 0; c < o->n; ++c) f[d][c] += RhoU[d];
   }
   memcpy(o->Rho, o->Rho_np1, sizeof(double) * (size_t)o->n);
+  if (o->PS) memcpy(o->PS, o->PS_np1, sizeof(double) * (size_t)o->n); /* grid.cpp:598 */
   vcopy(o, o->RU, o->RU_np1);
   o->P0 = o->P0_np1;
   pcopy(o, 0, 3);
@@ -752,6 +817,11 @@ void orc_step(orc *o, int with_particles) {
 /* grid::Initialize tail, grid.cpp:461-484 */
 void orc_initialize(orc *o) {
   o->stepped = 0;
+  if (o->PS) { /* grid.cpp:465-476 */
+    memcpy(o->PS_int, o->PS, sizeof(double) * (size_t)o->n);
+    memcpy(o->PS_np1, o->PS, sizeof(double) * (size_t)o->n);
+    interp_c2f_vec(o, o->PS, o->PS_face);
+  }
   vcopy(o, o->RU_int, o->RU);
   vcopy(o, o->RU_np1, o->RU);
   memcpy(o->Rho_int, o->Rho, sizeof(double) * (size_t)o->n);
@@ -787,6 +857,7 @@ static double *field_ptr(orc *o, int f, int *nvec) {
     case TPM_FIELD_Q: return o->RHS_Part_Temp;
     case TPM_FIELD_RHS_POIS: return o->RHS_Pois;
     case TPM_FIELD_DIVERGENCE: return o->divergence;
+    case TPM_FIELD_PASSIVE_SCALAR: return o->PS;
     default: return NULL;
   }
   *nvec = 3;
@@ -983,6 +1054,7 @@ void orc_statistics(orc *o, tpm_stats *s) {
   s->P0 = o->P0;
   s->num_iteration = o->stepped ? o->n_it : 0;
   s->C_var = field_sum_squares(o, o->C) / size_tot - s->C_mean * s->C_mean;
+  s->Passive_Scalar_mean = o->PS ? field_sum_squares(o, o->PS) / size_tot : 0.0; /* grid.cpp:913 */
   vfree(V);
 }
 

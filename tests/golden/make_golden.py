@@ -41,6 +41,15 @@ CASES = {
     "shipped24_1step": dict(N=24, npart=100, nu=0.02, A=0.1, tau_p=0.1, mass_loading=0.2,
                             heating_Q=0.0, iterations=2, epsilon=0.0, seed=13, nsteps=1,
                             as_shipped=True),
+    # passive scalar transport (grid.cpp:743-772) with each source type
+    "scalar16_source_2steps": dict(N=16, npart=1000, nu=0.02, A=0.1, tau_p=0.1,
+                                   mass_loading=0.5, heating_Q=0.5, iterations=20,
+                                   epsilon=1e-13, seed=31, nsteps=2, scalar=True,
+                                   extra=dict(solve_for_scalar=1, D_M=0.03, S1_type=0)),
+    "scalar24_meangrad_2steps": dict(N=24, npart=800, nu=0.01, A=0.1, tau_p=0.2,
+                                     mass_loading=0.3, heating_Q=0.0, iterations=20,
+                                     epsilon=1e-13, seed=32, nsteps=2, scalar=True,
+                                     extra=dict(solve_for_scalar=1, D_M=0.01, S1_type=1)),
     # grid::Statistics after each of 3 steps, as the reference writes it
     # (<name>.dat files, 6 significant digits)
     "stats16_3steps": dict(N=16, npart=2000, nu=0.02, A=0.1, tau_p=0.1, mass_loading=0.5,
@@ -55,6 +64,8 @@ def make(name, c):
                    iterations=c["iterations"], epsilon=c["epsilon"])
     s = inputs.make_state(p, c["npart"], seed=c["seed"])
     p = p.replace(dt=inputs.cfl_dt(p, s.RU), **c.get("extra", {}))
+    if c.get("scalar"):
+        s.PS = inputs.passive_scalar(p, c["seed"])
     ref = po.run_reference(p, s, c["nsteps"], as_shipped=c.get("as_shipped", False),
                            stats=c.get("stats", False))
     out = dict(
@@ -66,6 +77,7 @@ def make(name, c):
         Q=ref["RHS_Part_Temp"], P0=ref["P0"], T_cur=ref["T_cur"],
         **{f"part_{q}": ref["part"][q] for q in list(inputs.PQ) + ["flag", "RHS_T"]},
         **{f"stat_{k}": v for k, v in ref.get("stats", {}).items()},
+        **({"in_PS": s.PS, "PS": ref["Passive_Scalar"]} if c.get("scalar") else {}),
     )
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
     print(name, "written")

@@ -79,11 +79,11 @@ def test_null_context_calls_fail_cleanly(lib):
 def test_create_rejects_out_of_scope_options_before_touching_the_device(lib):
     from tpm.params import Params
 
-    p = Params(Nx=16, Ny=16, Nz=16, solve_for_scalar=1)
+    p = Params(Nx=16, Ny=16, Nz=16, solve_for_vector=1)
     h = ctypes.c_void_p()
     rc = lib.tpm_create(ctypes.byref(p.to_c()), 10, ctypes.byref(h))
     assert rc == -5  # TPM_ERR_UNSUPPORTED
-    assert b"passive scalar" in lib.tpm_last_error(h)
+    assert b"passive vector" in lib.tpm_last_error(h)
     lib.tpm_destroy(h)
     bad = Params(Nx=14, Ny=16, Nz=16)  # 14 = 2*7 does not factor into 2,3,5
     rc = lib.tpm_create(ctypes.byref(bad.to_c()), 10, ctypes.byref(h))

@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 from conftest import rel_err
-from golden import NAMES, load
+from golden import NAMES, SCALAR_NAMES, load
 from tpm import inputs, params as P
 
 TOL = 1e-12  # relative, per field (FP64 parity bar)
@@ -96,3 +96,13 @@ def test_oracle_matches_fresh_reference_run(oracle_lib, seed, N, steps, heat):
                 "part": ref["part"]}, TOL)
     assert rel_err(o.get_field("C"), ref["C"]) <= TOL
     assert rel_err(o.get_field("Q"), ref["RHS_Part_Temp"]) <= 1e-11
+
+
+@pytest.mark.parametrize("name", SCALAR_NAMES)
+def test_oracle_passive_scalar_matches_golden(oracle_lib, name):
+    """Passive scalar transport (grid.cpp:743-772) with each source type."""
+    p, s, ref, nsteps, _ = load(name)
+    o = run_oracle(oracle_lib, p, s, nsteps)
+    compare(o, ref, TOL)
+    assert rel_err(o.get_field("PASSIVE_SCALAR"), ref["PS"]) <= TOL
+    assert rel_err(ref["PS"], s.PS) > 1e-3  # the scalar did move

@@ -13,6 +13,7 @@
 #include <new>
 #include <string>
 #include <utility>
+#include <vector>
 
 #include "tpm_internal.cuh"
 #include "tpm_reduce.cuh"
@@ -65,6 +66,7 @@ double *field_ptr(tpm_ctx *c, int f, long long *len, bool for_download) {
     case TPM_FIELD_FP: *len = 3 * n; return c->Fp;
     case TPM_FIELD_RHS_POIS: return c->RHS;
     case TPM_FIELD_DIVERGENCE: return c->divg;
+    case TPM_FIELD_PASSIVE_SCALAR: return c->PS;  // null without solve_for_scalar
     default: return nullptr;
   }
 }
@@ -76,6 +78,8 @@ void materialize_np1(tpm_ctx *c) {
   const long long n = c->g.n;
   TPM_CUDA_TRY(cudaMemcpyAsync(c->RU_np1, c->RU, sizeof(double) * 3 * n, cudaMemcpyDeviceToDevice, c->stream));
   TPM_CUDA_TRY(cudaMemcpyAsync(c->Rho_np1, c->Rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+  if (c->PS)
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->PS_np1, c->PS, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
   for (int q = 0; q < 7 && c->np > 0; ++q)
     TPM_CUDA_TRY(cudaMemcpyAsync(c->pq[3][q], c->pq[0][q], sizeof(double) * c->np,
                                  cudaMemcpyDeviceToDevice, c->stream));
@@ -132,6 +136,7 @@ void swap_stage(tpm_ctx *c) {
   std::swap(c->RU_int, c->RU_new);
   std::swap(c->RUi32, c->RUn32);
   std::swap(c->Rho_int, c->Rho_new);
+  std::swap(c->PS_int, c->PS_new);  // grid.cpp:897
   for (int q = 0; q < 7; ++q) std::swap(c->pq[1][q], c->pq[2][q]);
   TPM_CUDA_TRY(cudaMemcpyAsync(&c->dsc->P0_int, &c->dsc->P0_new, sizeof(double),
                                cudaMemcpyDeviceToDevice, c->stream));
@@ -154,6 +159,7 @@ void substep(tpm_ctx *c, int s) {
   tpm::particle_deposit_momentum(c);
   tpm::particle_deposit_concentration(c);
   tpm::particle_heat(c);
+  if (c->PS) tpm::launch_passive_scalar(c, s, nb);  // simulation.cpp:65
   tpm::launch_rhs_momentum(c, s, nb);
   tpm::launch_poisson_rhs(c, s, c->store_div || c->p.precision == TPM_PREC_MIXED);
   poisson_loop(c, c->Iteration, c->p.epsilon);
@@ -168,6 +174,7 @@ void end_step(tpm_ctx *c) {
   // simulation.cpp:80 then grid::TimeAdvance (grid.cpp:595-606)
   tpm::launch_mean_reset(c);
   std::swap(c->Rho, c->Rho_np1);
+  std::swap(c->PS, c->PS_np1);  // grid.cpp:598
   for (int q = 0; q < 7; ++q) std::swap(c->pq[0][q], c->pq[3][q]);
   TPM_CUDA_TRY(cudaMemcpyAsync(&c->dsc->P0, &c->dsc->P0_np1, sizeof(double),
                                cudaMemcpyDeviceToDevice, c->stream));
@@ -224,9 +231,9 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
   if (!c) return TPM_ERR_NOMEM;
   c->p = *p;
   *out = c;
-  if (p->elongated_box || p->solve_for_scalar || p->solve_for_vector)
+  if (p->elongated_box || p->solve_for_vector)
     return fail(c, TPM_ERR_UNSUPPORTED,
-                "elongated box, passive scalar and passive vector are outside the ported path");
+                "elongated box and passive vector are outside the ported path");
   if (p->precision != TPM_PREC_FP64 && p->precision != TPM_PREC_MIXED)
     return fail(c, TPM_ERR_ARG, "unknown precision");
   if (!factorable(p->Nx) || !factorable(p->Ny) || !factorable(p->Nz) || (p->Nx % 2) ||
@@ -322,6 +329,34 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->pay_r = dalloc<double>(c, 4 * (size_t)np);
     c->w8 = dalloc<double>(c, 16 * (size_t)np);
     c->C_next = dalloc<double>(c, n);
+    if (p->solve_for_scalar) {
+      c->PS = dalloc<double>(c, n); c->PS_int = dalloc<double>(c, n);
+      c->PS_new = dalloc<double>(c, n); c->PS_np1 = dalloc<double>(c, n);
+      c->PS_face = dalloc<double>(c, 3 * n);
+      for (double *f : {c->PS, c->PS_int, c->PS_new, c->PS_np1})
+        TPM_CUDA_TRY(cudaMemsetAsync(f, 0, sizeof(double) * n, c->stream));
+      TPM_CUDA_TRY(cudaMemsetAsync(c->PS_face, 0, sizeof(double) * 3 * n, c->stream));
+      if (p->S1_type == 0) {
+        // grid::C_Source (grid.cpp:718-741) with scalar_source.h: S1 = 1.*cos(1.*X)
+        // at the cell centres, then S1 -= S1.mean() in tensor0::sum's order
+        // (i, then j, then k innermost); time independent, so formed once here
+        std::vector<double> h((size_t)n);
+        for (int k = 0; k < g.nz; ++k)
+          for (int j = 0; j < g.ny; ++j)
+            for (int i = 0; i < g.nx; ++i) {
+              const double X = g.dx / 2. + i * g.dx;
+              h[((size_t)k * g.ny + j) * g.nx + i] = 1. * cos(1. * X);
+            }
+        double sum = 0;
+        for (int i = 0; i < g.nx; ++i)
+          for (int j = 0; j < g.ny; ++j)
+            for (int k = 0; k < g.nz; ++k) sum += h[((size_t)k * g.ny + j) * g.nx + i];
+        const double mean = sum / (double)n;
+        for (double &v : h) v -= mean;
+        c->S1 = dalloc<double>(c, n);
+        TPM_CUDA_TRY(cudaMemcpy(c->S1, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+      }
+    }
     TPM_CUDA_TRY(cudaMemsetAsync(c->C_next, 0, sizeof(double) * n, c->stream));
     TPM_CUDA_TRY(cudaMemsetAsync(c->starts_r[0], 0, sizeof(int32_t) * (n + 1), c->stream));
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -525,6 +560,10 @@ int tpm_initialize(tpm_ctx *c) {
     push_scalars(c);
     c->np1_is_base = true;
     c->rui32_stale = true;
+    if (c->PS) {  // grid.cpp:465-476
+      TPM_CUDA_TRY(cudaMemcpyAsync(c->PS_int, c->PS, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+      tpm::launch_passive_scalar_face(c, c->PS);
+    }
     // grid.cpp:474 (Rho_face is recomputed from Rho_int where it is needed)
     // grid.cpp:481-484: initial particle heat coupling
     tpm::particle_zero_fields(c);
@@ -551,6 +590,10 @@ int tpm_resume(tpm_ctx *c) {
     push_scalars(c);
     c->np1_is_base = true;
     c->rui32_stale = true;
+    if (c->PS) {
+      TPM_CUDA_TRY(cudaMemcpyAsync(c->PS_int, c->PS, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+      tpm::launch_passive_scalar_face(c, c->PS);
+    }
     tpm::particle_resume(c);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->initialized = true;

@@ -31,7 +31,7 @@ enum Slot {
   S_TG_SUM,
   S_TKE_U, S_TKE_V, S_TKE_W,
   S_UMAX_X, S_UMAX_Y, S_UMAX_Z,
-  S_USQ, S_SS,
+  S_USQ, S_SS, S_PS_SQ,
   S_VP_MAX, S_TP_MAX, S_TP_SUM,
   S_COUNT
 };
@@ -98,8 +98,8 @@ __global__ void k_diag_velocity(Grid g, const double *__restrict__ RU,
 // summed over cells is the volume integral.
 __global__ void __launch_bounds__(kDiagThreads)
 k_diag_cells(Grid g, const double *__restrict__ Rho, const double *__restrict__ C,
-             const double *__restrict__ RU, const double *__restrict__ U, double a_tg,
-             double *__restrict__ parts) {
+             const double *__restrict__ RU, const double *__restrict__ U,
+             const double *__restrict__ PS, double a_tg, double *__restrict__ parts) {
   __shared__ double sh[32];
   double v[S_VP_MAX];
 #pragma unroll
@@ -135,6 +135,7 @@ k_diag_cells(Grid g, const double *__restrict__ Rho, const double *__restrict__ 
     const double sxz = 0.5 * ((u[c] - u[at(g, i, j, km)]) * g.inv_dz + (w[c] - w[at(g, im, j, k)]) * g.inv_dx);
     const double syz = 0.5 * ((vv[c] - vv[at(g, i, j, km)]) * g.inv_dz + (w[c] - w[at(g, i, jm, k)]) * g.inv_dy);
     v[S_SS] += sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz);
+    if (PS) v[S_PS_SQ] += PS[c] * PS[c];
   }
 #pragma unroll
   for (int s = 0; s < S_VP_MAX; ++s) {
@@ -385,7 +386,7 @@ int tpm_statistics(tpm_ctx *c, tpm_stats *out) {
     const double a_tg = ds.P0 / c->R;  // P0/param_->R() (grid.cpp:939)
     const int cb = diag_blocks(g.n), pb = diag_blocks(c->np);
     TPM_LAUNCH(c, "diag_cells", k_diag_cells, cb, kDiagThreads, 0, g, c->Rho, c->C, c->RU,
-               c->diag_u, a_tg, c->diag_parts);
+               c->diag_u, c->PS, a_tg, c->diag_parts);
     if (c->np > 0)
       TPM_LAUNCH(c, "diag_particles", k_diag_particles, pb, kDiagThreads, 0, c->np, c->pq[0][3],
                  c->pq[0][6], c->diag_parts);
@@ -431,6 +432,7 @@ int tpm_statistics(tpm_ctx *c, tpm_stats *out) {
     s.C_var = v[S_C_SQ] / n - s.C_mean * s.C_mean;  // tensor0::var
     s.u_rms = std::sqrt(v[S_USQ] / n / 3.0);
     s.dissipation = 2.0 * (c->p.Mu0 / c->p.Rho0) * (v[S_SS] / n);
+    s.Passive_Scalar_mean = c->PS ? v[S_PS_SQ] / n : 0.0;  // tensor0::mean_squares
     *out = s;
     return TPM_OK;
   });

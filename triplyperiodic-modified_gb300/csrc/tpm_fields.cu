@@ -549,6 +549,61 @@ __global__ void k_finish_mean(const double *__restrict__ partials, int nparts, l
   if (threadIdx.x == 0) *out = sum / (double)ntot;
 }
 
+// -------------------------------------------------------- passive scalar
+// grid::Update_Passive_Scalar (grid.cpp:743-772) at one cell: with U the face
+// velocity RU_int/Rho_face (TU: FP32 copy on the mixed path),
+//   RHS = D_M Del2(PS_int) + (-1) div_F2C(U * PS_face) + source,
+// source = S1 - mean(S1) (S1_type 0, scalar_source.h) or (-1) Ix_F2C(U.x);
+//   PS_np1 += (dt*post) RHS,  PS_new = 1*PS + (dt*pre) RHS  (stage 3: PS_np1).
+struct PsArgs {
+  double D_M, dtpo, dtpr;
+  int stage, s1_type;
+};
+
+template <typename TU>
+__global__ void k_passive_scalar(Grid g, const TU *__restrict__ U, const double *__restrict__ PSf,
+                                 const double *__restrict__ PSi, const double *__restrict__ PS,
+                                 const double *__restrict__ PSnp1_in, double *__restrict__ PSnp1,
+                                 double *__restrict__ PSnew, const double *__restrict__ S1,
+                                 PsArgs a) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    Nbr nb = nbr_of(g, q);
+    const TU *Ux = U, *Uy = U + g.n, *Uz = U + 2 * g.n;
+    const double *Fx = PSf, *Fy = PSf + g.n, *Fz = PSf + 2 * g.n;
+    // dummy = U * PS_face; div_F2C(dummy) (tensor0.cpp:249-256)
+    const double conv = ((double)Ux[nb.p[0]] * Fx[nb.p[0]] - (double)Ux[c] * Fx[c]) * g.inv_dx +
+                        ((double)Uy[nb.p[1]] * Fy[nb.p[1]] - (double)Uy[c] * Fy[c]) * g.inv_dy +
+                        ((double)Uz[nb.p[2]] * Fz[nb.p[2]] - (double)Uz[c] * Fz[c]) * g.inv_dz;
+    const double pc = PSi[c];
+    const double lap = (PSi[nb.p[0]] - 2 * pc + PSi[nb.m[0]]) * g.inv_dx2 +
+                       (PSi[nb.p[1]] - 2 * pc + PSi[nb.m[1]]) * g.inv_dy2 +
+                       (PSi[nb.p[2]] - 2 * pc + PSi[nb.m[2]]) * g.inv_dz2;
+    double rhs = a.D_M * lap + -1 * conv;
+    if (a.s1_type == 0)
+      rhs += S1[c];
+    else
+      rhs += -1 * (((double)Ux[c] + (double)Ux[nb.p[0]]) * 0.5);
+    const double np1 = PSnp1_in[c] + a.dtpo * rhs;
+    PSnp1[c] = np1;
+    PSnew[c] = a.stage != 3 ? 1 * PS[c] + a.dtpr * rhs : np1;
+  }
+}
+
+// Passive_Scalar_face = I_C2F(src) (tensor1.cpp:278-283, tensor0.cpp:283-296)
+__global__ void k_ps_face(Grid g, const double *__restrict__ src, double *__restrict__ F) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    Nbr nb = nbr_of(g, q);
+    const double v = src[c];
+    F[c] = (v + src[nb.m[0]]) * 0.5;
+    F[g.n + c] = (v + src[nb.m[1]]) * 0.5;
+    F[2 * g.n + c] = (v + src[nb.m[2]]) * 0.5;
+  }
+}
+
 // ---------------------------------------------------------- projection
 // grid::Update_RU_WP, grid.cpp:857-863.  At the last stage the per-component
 // sums of RU_np1 for make_mean_U0 (simulation.cpp:80) are reduced too.
@@ -765,6 +820,29 @@ void launch_project(tpm_ctx *c, int s) {
     TPM_LAUNCH(c, "finish_means3", k_finish_means3, 1, kThreads, 0,
                c->partials + kPartRu * kRedBlocks, nb, c->g.n,
                c->dsc);
+}
+
+void launch_passive_scalar(tpm_ctx *c, int s, bool np1_in_base) {
+  PsArgs a;
+  a.D_M = c->p.D_M;
+  a.dtpo = c->p.dt * kPost[s];
+  a.dtpr = c->p.dt * kPre[s];
+  a.stage = s;
+  a.s1_type = c->p.S1_type;
+  const double *np1_in = np1_in_base ? c->PS : c->PS_np1;
+  if (c->p.precision == TPM_PREC_MIXED)
+    TPM_LAUNCH(c, "passive_scalar", k_passive_scalar<float>, cell_blocks(c->g), kThreads, 0,
+               c->g, c->U32, c->PS_face, c->PS_int, c->PS, np1_in, c->PS_np1, c->PS_new, c->S1,
+               a);
+  else
+    TPM_LAUNCH(c, "passive_scalar", k_passive_scalar<double>, cell_blocks(c->g), kThreads, 0,
+               c->g, c->U, c->PS_face, c->PS_int, c->PS, np1_in, c->PS_np1, c->PS_new, c->S1, a);
+  launch_passive_scalar_face(c, c->PS_new);
+}
+
+void launch_passive_scalar_face(tpm_ctx *c, const double *src) {
+  TPM_LAUNCH(c, "passive_scalar_face", k_ps_face, cell_blocks(c->g), kThreads, 0, c->g, src,
+             c->PS_face);
 }
 
 void launch_div_residual(tpm_ctx *c, int s) {

@@ -37,6 +37,7 @@ HostState snapshot(const tpm_ctx *c) {
   h.C = c->C; h.C_next = c->C_next;
   h.RUi32 = c->RUi32; h.RUn32 = c->RUn32;
   std::memcpy(h.pq, c->pq, sizeof(h.pq));
+  h.PS = c->PS; h.PS_int = c->PS_int; h.PS_new = c->PS_new; h.PS_np1 = c->PS_np1;
   h.tau = c->tau;
   h.q_parts = c->q_parts;
   h.np1_is_base = c->np1_is_base; h.rui32_stale = c->rui32_stale; h.stepped = c->stepped;
@@ -53,6 +54,7 @@ void restore(tpm_ctx *c, const HostState &h) {
   c->C = h.C; c->C_next = h.C_next;
   c->RUi32 = h.RUi32; c->RUn32 = h.RUn32;
   std::memcpy(c->pq, h.pq, sizeof(h.pq));
+  c->PS = h.PS; c->PS_int = h.PS_int; c->PS_new = h.PS_new; c->PS_np1 = h.PS_np1;
   c->q_parts = h.q_parts;
   c->np1_is_base = h.np1_is_base; c->rui32_stale = h.rui32_stale; c->stepped = h.stepped;
 }

@@ -91,6 +91,7 @@ struct HostState {
   double *RU_int, *RU_new, *Rho, *Rho_int, *Rho_new, *Rho_np1, *C, *C_next;
   float *RUi32, *RUn32;
   double *pq[4][7];
+  double *PS, *PS_int, *PS_new, *PS_np1;
   const double *tau;
   int q_parts;
   int np1_is_base, rui32_stale, stepped, store_div, div_every_stage;
@@ -170,6 +171,10 @@ struct tpm_ctx {
   double *pay_r = nullptr;  // 4*np: round-indexed fractions and heat rate, unsorted
   double *w8 = nullptr;  // 16*np corner weights (heat, concentration; sorted order)
   double *C_next = nullptr;  // concentration at this x_new = next substep's x_int
+  // passive scalar (solve_for_scalar): RK copies, face values I_C2F(PS_new)
+  // of the last stage, and the mean-free source field of S1_type 0
+  double *PS = nullptr, *PS_int = nullptr, *PS_new = nullptr, *PS_np1 = nullptr;
+  double *PS_face = nullptr /*3n*/, *S1 = nullptr;
   int q_parts = 1;  // number of valid partial sums of Q (heat deposit blocks)
 
   bool store_div = false;
@@ -217,6 +222,8 @@ void launch_poisson_rhs(tpm_ctx *c, int stage, bool store_div);
 void launch_project(tpm_ctx *c, int stage);
 void launch_div_residual(tpm_ctx *c, int stage);
 void launch_mean_reset(tpm_ctx *c);
+void launch_passive_scalar(tpm_ctx *c, int stage, bool np1_in_base);  // grid.cpp:743-772
+void launch_passive_scalar_face(tpm_ctx *c, const double *src);      // PS_face = I_C2F(src)
 void launch_init_fields(tpm_ctx *c);
 int cell_blocks(const Grid &g);
 void launch_center_coeff_from_C(tpm_ctx *c);  // operator-level Poisson entry

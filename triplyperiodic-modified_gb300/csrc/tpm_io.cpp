@@ -7,9 +7,11 @@
 //    blocks), Restart_Rho.bin, Restart_P.bin - raw native FP64, C order
 //    [Nz][Ny][Nx] (communicator.cpp:114-134); Restart_Part_{x,y,z,u,v,w,T}.bin
 //    FP64 [Np] and Restart_Part_flag.bin int32 [Np]; Restart_numbers.dat with
-//    "P0 T_cur num_timestep" (written here with 17 significant digits).
+//    "P0 T_cur num_timestep" (written here with 17 significant digits); with
+//    solve_for_scalar also Restart_Passive_Scalar.bin (Initial_C = 1,
+//    grid.cpp:445-450).
 //  * dumps written by grid::Store (grid.cpp:525-592) and particle::Store_All
-//    (particle.cpp:848-897): RU_<n>.bin, Rho_<n>.bin, P_<n>.bin,
+//    (particle.cpp:848-897): RU_<n>.bin, Rho_<n>.bin, P_<n>.bin, Passive_Scalar_<n>.bin,
 //    Part_{x,...,flag}_<n>.bin and numbers_<n>.dat, n = num_timestep.
 #include <cstdio>
 #include <string>
@@ -59,7 +61,7 @@ int read_raw(tpm_ctx *ctx, const std::string &path, std::vector<T> &v) {
 }
 
 struct Host {
-  std::vector<double> RU, Rho, P;
+  std::vector<double> RU, Rho, P, PS;
   std::vector<double> q[7];
   std::vector<int32_t> flag;
 };
@@ -72,6 +74,10 @@ int download_all(tpm_ctx *ctx, long long n, int64_t np, Host &h) {
   if ((rc = tpm_download_field(ctx, TPM_FIELD_RU, h.RU.data()))) return rc;
   if ((rc = tpm_download_field(ctx, TPM_FIELD_RHO, h.Rho.data()))) return rc;
   if ((rc = tpm_download_field(ctx, TPM_FIELD_P, h.P.data()))) return rc;
+  if (ctx->PS) {
+    h.PS.resize(n);
+    if ((rc = tpm_download_field(ctx, TPM_FIELD_PASSIVE_SCALAR, h.PS.data()))) return rc;
+  }
   for (auto &v : h.q) v.resize(np);
   h.flag.resize(np);
   if (np > 0)
@@ -99,6 +105,7 @@ int tpm_write_restart(tpm_ctx *ctx, const char *dir) {
   if ((rc = write_raw(ctx, join(dir, "Restart_RU.bin"), h.RU))) return rc;
   if ((rc = write_raw(ctx, join(dir, "Restart_Rho.bin"), h.Rho))) return rc;
   if ((rc = write_raw(ctx, join(dir, "Restart_P.bin"), h.P))) return rc;
+  if (ctx->PS && (rc = write_raw(ctx, join(dir, "Restart_Passive_Scalar.bin"), h.PS))) return rc;
   for (int q = 0; q < 7; ++q)
     if ((rc = write_raw(ctx, join(dir, std::string("Restart_Part_") + kQ[q] + ".bin"), h.q[q])))
       return rc;
@@ -122,6 +129,10 @@ int tpm_read_restart(tpm_ctx *ctx, const char *dir) {
   if ((rc = read_raw(ctx, join(dir, "Restart_RU.bin"), h.RU))) return rc;
   if ((rc = read_raw(ctx, join(dir, "Restart_Rho.bin"), h.Rho))) return rc;
   if ((rc = read_raw(ctx, join(dir, "Restart_P.bin"), h.P))) return rc;
+  if (ctx->PS) {  // Initial_C = 1 (grid.cpp:445-450)
+    h.PS.resize(n);
+    if ((rc = read_raw(ctx, join(dir, "Restart_Passive_Scalar.bin"), h.PS))) return rc;
+  }
   for (int q = 0; q < 7; ++q) {
     h.q[q].resize(np);
     if ((rc = read_raw(ctx, join(dir, std::string("Restart_Part_") + kQ[q] + ".bin"), h.q[q])))
@@ -140,6 +151,7 @@ int tpm_read_restart(tpm_ctx *ctx, const char *dir) {
   if ((rc = tpm_upload_field(ctx, TPM_FIELD_RU, h.RU.data()))) return rc;
   if ((rc = tpm_upload_field(ctx, TPM_FIELD_RHO, h.Rho.data()))) return rc;
   if ((rc = tpm_upload_field(ctx, TPM_FIELD_P, h.P.data()))) return rc;
+  if (ctx->PS && (rc = tpm_upload_field(ctx, TPM_FIELD_PASSIVE_SCALAR, h.PS.data()))) return rc;
   if (np > 0 &&
       (rc = tpm_upload_particles(ctx, TPM_PSET_BASE, h.q[0].data(), h.q[1].data(), h.q[2].data(),
                                  h.q[3].data(), h.q[4].data(), h.q[5].data(), h.q[6].data(),
@@ -161,6 +173,7 @@ int tpm_store(tpm_ctx *ctx, const char *dir) {
   if ((rc = write_raw(ctx, join(dir, "RU" + s + ".bin"), h.RU))) return rc;
   if ((rc = write_raw(ctx, join(dir, "Rho" + s + ".bin"), h.Rho))) return rc;
   if ((rc = write_raw(ctx, join(dir, "P" + s + ".bin"), h.P))) return rc;
+  if (ctx->PS && (rc = write_raw(ctx, join(dir, "Passive_Scalar" + s + ".bin"), h.PS))) return rc;
   for (int q = 0; q < 7; ++q)
     if ((rc = write_raw(ctx, join(dir, std::string("Part_") + kQ[q] + s + ".bin"), h.q[q]))) return rc;
   if ((rc = write_raw(ctx, join(dir, "Part_flag" + s + ".bin"), h.flag))) return rc;

@@ -19,7 +19,7 @@ PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG, "lib", "libtpm.so")
 
 FIELD = dict(RU=0, RU_INT=1, RU_NEW=2, RU_NP1=3, RHO=4, RHO_INT=5, RHO_NEW=6, RHO_NP1=7, P=8,
-             C=9, Q=10, FP=11, RHS_POIS=12, DIVERGENCE=13)
+             C=9, Q=10, FP=11, RHS_POIS=12, DIVERGENCE=13, PASSIVE_SCALAR=14)
 VECTOR = {"RU", "RU_INT", "RU_NEW", "RU_NP1", "FP"}
 PSET = dict(base=0, int=1, new=2, np1=3)
 OPT_STORE_DIVERGENCE = 1
@@ -293,6 +293,8 @@ class Context:
         self.upload_field("RU", s.RU)
         self.upload_field("RHO", s.Rho)
         self.upload_field("P", s.P)
+        if s.PS is not None:
+            self.upload_field("PASSIVE_SCALAR", s.PS)
         if self.npart:
             self.upload_particles(s.part, "base")
         self.set_scalars(s.P0, s.T_cur, s.num_timestep)

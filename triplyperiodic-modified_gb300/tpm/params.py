@@ -68,7 +68,7 @@ class TpmStats(ctypes.Structure):
             "TKE_U", "TKE_V", "TKE_W", "TKE", "Gas_CFL_Max", "Gas_Max_Diff_CFL", "u_max",
             "Vp_max", "Tp_max", "Tp_mean", "HT_mean", "Tg_mean", "P0")
     ] + [("num_iteration", ctypes.c_int32), ("reserved", ctypes.c_int32)] + [
-        (n, ctypes.c_double) for n in ("C_var", "u_rms", "dissipation")
+        (n, ctypes.c_double) for n in ("C_var", "u_rms", "dissipation", "Passive_Scalar_mean")
     ]
 
     def as_dict(self):
