@@ -163,8 +163,11 @@ def time_gpu(p, s, steps, warmup, dist, device):
         dist.barrier()
     ms = e0.elapsed_time(e1)
     sc = ctx.scalars()
-    n_it = (sc["total_poisson_iterations"] - it0) / (4.0 * steps)
-    launches = ctx.launch_count() - l0
+    iters = sc["total_poisson_iterations"] - it0
+    n_it = iters / (4.0 * steps)
+    # the launch counter counts a graph's Poisson loop body (6 kernels) once per
+    # solve; the device repeats it once per further iteration
+    launches = ctx.launch_count() - l0 + 6 * max(0, iters - 4 * steps)
     # per-kernel durations (CUDA events around each launch on the same stream;
     # profiled steps run eagerly)
     ctx.profile(True)
@@ -425,14 +428,18 @@ def ensemble_main(args):
         b.run(args.warmup, graph=graph)
         b.sync()
         l0 = sum(box.launch_count() for box in b.boxes)
+        it0 = [box.scalars()["total_poisson_iterations"] for box in b.boxes]
         torch.cuda.synchronize()
         with ClockSampler(local) as clk:
             t0 = time.perf_counter()
             b.run(args.steps, graph=graph)
             b.sync()
             secs = time.perf_counter() - t0
-        out[mode] = {"secs": secs, "launches": sum(box.launch_count() for box in b.boxes) - l0,
-                     "clocks": clk.summary()}
+        launches = sum(box.launch_count() for box in b.boxes) - l0
+        if graph:  # loop bodies repeated on the device (6 kernels per extra iteration)
+            launches += sum(6 * max(0, box.scalars()["total_poisson_iterations"] - i0 - 4 * args.steps)
+                            for box, i0 in zip(b.boxes, it0))
+        out[mode] = {"secs": secs, "launches": launches, "clocks": clk.summary()}
         if mode == "graph":  # end to end: each step's statistics read back to the host
             t0 = time.perf_counter()
             for _ in range(args.steps):

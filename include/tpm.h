@@ -332,7 +332,10 @@ int tpm_profile_enable(tpm_ctx *ctx, int on);
 int tpm_profile_report(tpm_ctx *ctx, char *names, int cap, int *launches, double *total_ms,
                        int max_kernels);
 int tpm_profile_reset(tpm_ctx *ctx);
-/* Number of kernel launches issued by this context since create. */
+/* Number of kernel launches issued by this context since create.  A graph
+ * replay counts the kernels it holds; the body of a captured Poisson loop (a
+ * conditional while node, 6 kernels) is counted once per solve although the
+ * device runs it once per iteration. */
 int64_t tpm_launch_count(const tpm_ctx *ctx);
 
 #ifdef __cplusplus

@@ -68,9 +68,9 @@ def test_graph_steps_bit_identical_to_eager(capi, prec, eps):
     eager = run(capi, p, s, 5)
     graph = run(capi, p, s, 5, graph=True)
     assert_same(state(graph), state(eager))
-    # a captured step enqueues every allowed Poisson iteration (those after the
-    # device-side stop return at once); eagerly the host stops enqueuing
-    assert graph.launch_count() >= eager.launch_count()
+    # the Poisson loop is a conditional while node: its body is enqueued once
+    # per solve and repeats on the device, so fewer launches are issued
+    assert graph.launch_count() <= eager.launch_count()
     if eps > 0:
         assert 0 < graph.scalars()["last_poisson_iterations"] < 20
 

@@ -109,8 +109,44 @@ void param_update(tpm_ctx *c) {
 void poisson_loop(tpm_ctx *c, int max_it, double eps) {
   TPM_CUDA_TRY(cudaMemsetAsync(&c->dsc->skip, 0, 2 * sizeof(int), c->stream));  // skip, it
   if (c->device_loop) {
-    for (int k = 0; k < max_it; ++k) tpm::poisson_iteration(c, eps > 0 ? eps : 0.0);
     c->last_it = -1;  // on the device (DevScalars::it)
+    if (max_it <= 0) return;
+    // the loop as a conditional while node of the graph being captured: its
+    // body (one iteration, captured on the side stream) repeats until the
+    // last kernel of an iteration reports it < max_it && max|dp| > eps false
+    cudaStreamCaptureStatus st;
+    cudaGraph_t graph = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    TPM_CUDA_TRY(cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &graph, &deps, nullptr, &ndeps));
+    if (st != cudaStreamCaptureStatusActive) throw std::string("device loop outside a capture");
+    tpm::LoopCtl loop;
+    loop.max_it = max_it;
+    TPM_CUDA_TRY(cudaGraphConditionalHandleCreate(&loop.handle, graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = loop.handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    TPM_CUDA_TRY(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    TPM_CUDA_TRY(cudaStreamBeginCaptureToGraph(c->side, body, nullptr, nullptr, 0,
+                                               cudaStreamCaptureModeThreadLocal));
+    std::swap(c->stream, c->side);
+    try {
+      tpm::poisson_iteration(c, eps > 0 ? eps : 0.0, &loop);
+    } catch (...) {
+      std::swap(c->stream, c->side);
+      cudaGraph_t g2 = nullptr;
+      cudaStreamEndCapture(c->side, &g2);
+      throw;
+    }
+    std::swap(c->stream, c->side);
+    cudaGraph_t captured = nullptr;
+    TPM_CUDA_TRY(cudaStreamEndCapture(c->side, &captured));
+    TPM_CUDA_TRY(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1,
+                                                     cudaStreamSetCaptureDependencies));
     return;
   }
   int it = 0;
@@ -268,6 +304,7 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->A = p->A1; c->gx = p->gx1; c->gy = p->gy1; c->gz = p->gz1; c->I0 = p->I01;
     c->np = np;
     TPM_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    TPM_CUDA_TRY(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
     // fields
     c->RU = dalloc<double>(c, 3 * n); c->RU_int = dalloc<double>(c, 3 * n);
     c->RU_new = dalloc<double>(c, 3 * n); c->RU_np1 = dalloc<double>(c, 3 * n);
@@ -377,6 +414,7 @@ int tpm_destroy(tpm_ctx *c) {
   if (c->fft_mem) cudaFree(c->fft_mem);
   if (c->hsc) cudaFreeHost(c->hsc);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->side) cudaStreamDestroy(c->side);
   delete c;
   return TPM_OK;
 }

@@ -368,9 +368,15 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   if (threadIdx.x == 0) partials[blockIdx.x] = bm;
 }
 
+// max|dp| of the iteration (poisson.cpp:407) and the loop test of
+// poisson.cpp:397 for iterations run from a graph: with a conditional handle
+// (loop_max > 0) the enclosing while node repeats while it < max_it and
+// max|dp| > epsilon; without one, a satisfied test turns the remaining
+// unrolled iterations into no-ops (skip).  `it` counts up by one per
+// iteration, so the loop ends after at most loop_max bodies.
 __global__ void k_finish_max(const double *__restrict__ partials, int nparts, DevScalars *s,
-                             double eps_ctl) {
-  if (s->skip) return;
+                             double eps_ctl, cudaGraphConditionalHandle loop, int loop_max) {
+  if (loop_max == 0 && s->skip) return;
   __shared__ double sh[32];
   double v = 0;
   for (int b = threadIdx.x; b < nparts; b += blockDim.x) v = partials[b] > v ? partials[b] : v;
@@ -379,8 +385,11 @@ __global__ void k_finish_max(const double *__restrict__ partials, int nparts, De
     s->err = m;
     s->it += 1;
     s->it_sum += 1;
-    // poisson.cpp:397: the next iteration runs only while error > epsilon
-    if (eps_ctl > 0 && !(m > eps_ctl)) s->skip = 1;
+    const bool more = !(eps_ctl > 0 && !(m > eps_ctl));
+    if (loop_max > 0)
+      cudaGraphSetConditional(loop, (s->it < loop_max && more) ? 1u : 0u);
+    else if (!more)
+      s->skip = 1;
   }
 }
 
@@ -505,7 +514,7 @@ void fft_plans_create(tpm_ctx *c) {
 // path; float2 on the mixed path, where each iteration is one step of
 // iterative refinement: FP64 residual, FP32 correction, FP64 update).
 template <typename T2>
-static void poisson_iteration_t(tpm_ctx *c, double eps_ctl) {
+static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop) {
   const Grid &g = c->g;
   const long long nrows = (long long)g.ny * g.nz;
   T2 *spec = reinterpret_cast<T2 *>(c->spec);
@@ -544,15 +553,16 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl) {
     double *parts = c->err_parts;
     TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, xblocks, kFftThreads, smem, g, c->fx,
                r2c, spec, c->P, parts, npx, skip);
-    TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 256, 0, parts, xblocks, c->dsc, eps_ctl);
+    TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 256, 0, parts, xblocks, c->dsc, eps_ctl,
+               loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0);
   }
 }
 
-void poisson_iteration(tpm_ctx *c, double eps_ctl) {
+void poisson_iteration(tpm_ctx *c, double eps_ctl, const LoopCtl *loop) {
   if (c->p.precision == TPM_PREC_MIXED)
-    poisson_iteration_t<float2>(c, eps_ctl);
+    poisson_iteration_t<float2>(c, eps_ctl, loop);
   else
-    poisson_iteration_t<double2>(c, eps_ctl);
+    poisson_iteration_t<double2>(c, eps_ctl, loop);
 }
 
 int pens_default(int n, int elem_bytes) { return pens_for(n, elem_bytes); }
@@ -843,7 +853,7 @@ extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, doub
     {
       size_t smem = 2 * (size_t)npx * fx.n * sizeof(double2);
       k_xinv_update<double2><<<xblocks, kFftThreads, smem, st>>>(g, fx, r2c, spec, P, errp, npx, nullptr);
-      k_finish_max<<<1, 256, 0, st>>>(errp, xblocks, dsc, 0.0);
+      k_finish_max<<<1, 256, 0, st>>>(errp, xblocks, dsc, 0.0, cudaGraphConditionalHandle{}, 0);
     }
     if (cudaGetLastError() != cudaSuccess) return TPM_ERR_CUDA;
     it++;

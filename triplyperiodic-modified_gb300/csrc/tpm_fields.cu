@@ -369,7 +369,7 @@ __global__ void k_poisson_rhs(Grid g, const double *__restrict__ Rho_new,
       double u_hi = R[nb.p[d]] / rf_hi[d];
       double u_lo = R[c] / rf_lo[d];
       t[d] = (u_hi - u_lo) * (d == 0 ? g.inv_dx : d == 1 ? g.inv_dy : g.inv_dz);
-      usq += u_lo * u_lo;
+      if (tke_parts) usq += u_lo * u_lo;
     }
     double rhs = t[0] + t[1] + t[2];
     rhs -= dv;
@@ -497,7 +497,7 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
       const double u_lo = R[c] * clo;
       t[d] = (R[nb.p[d]] * chi - u_lo) * inv_d[d];
       msum += ((float)clo + (float)chi) * 0.5f;
-      usq += u_lo * u_lo;
+      if (tke_parts) usq += u_lo * u_lo;
     }
     double rhs = (t[0] + t[1] + t[2] - dv) * a.inv_dtpre;
     RHS[c] = rhs;

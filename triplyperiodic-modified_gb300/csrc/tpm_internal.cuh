@@ -117,6 +117,7 @@ struct tpm_ctx {
   int64_t np = 0;
   int dev = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // captures the body of a conditional (while) graph node
   std::string err;
   int64_t launches = 0;
 
@@ -232,10 +233,16 @@ void launch_to_double(tpm_ctx *c, const float *src, double *dst, long long n);
 
 // ---- Poisson / FFT (tpm_fft.cu) ----
 void fft_plans_create(tpm_ctx *c);
+// A Richardson loop captured as a conditional while node: the body's last
+// kernel sets `handle` to continue while it < max_it and max|dp| > epsilon.
+struct LoopCtl {
+  cudaGraphConditionalHandle handle;
+  int max_it;
+};
 // one Richardson iteration; returns nothing (error lands in dsc->err).  With
-// eps_ctl > 0 the iteration also sets dsc->skip once max|dp| <= eps_ctl, and
-// every kernel of a later iteration returns at once while it is set.
-void poisson_iteration(tpm_ctx *c, double eps_ctl = 0.0);
+// eps_ctl > 0 and no loop control the iteration sets dsc->skip once
+// max|dp| <= eps_ctl, and every kernel of a later iteration returns at once.
+void poisson_iteration(tpm_ctx *c, double eps_ctl = 0.0, const LoopCtl *loop = nullptr);
 int pens_default(int n, int elem_bytes);
 int pens_max(int n, int elem_bytes);
 // energy per half-spectrum mode of the face velocity U3 (3n), summed over
