@@ -87,7 +87,12 @@ typedef struct tpm_params {
   double D_M;               /* passive-scalar diffusivity (params.h:51) */
   int32_t S1_type;          /* passive-scalar source (params.h:53): 0 = cos(x) source with
                                its mean removed, else -u (mean gradient along x) */
-  int32_t reserved;
+  int32_t Solver;           /* pressure solver (params.h, deck token Solver): 0 = FFT-
+                               preconditioned Richardson, stop on max|dp| <= epsilon
+                               (poisson.cpp:391-411); 2 = conjugate gradients, stop on
+                               ||r||_2/||b||_2 < epsilon as the reference's PCG does
+                               (poisson.cpp:214-245), preconditioned here by the
+                               constant-coefficient FFT solve instead of BoomerAMG */
 } tpm_params;
 
 /* Field identifiers for upload/download.  Vector fields are 3*N doubles. */

@@ -100,71 +100,107 @@ void param_update(tpm_ctx *c) {
   }
 }
 
+// Captures `body` (one iteration) as the body of a conditional while node
+// appended to the graph being captured on c->stream; the body's last kernel
+// sets the handle (tpm::LoopCtl) to continue or stop.
+template <typename F>
+void capture_while(tpm_ctx *c, tpm::LoopCtl &loop, F &&body) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t graph = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t ndeps = 0;
+  TPM_CUDA_TRY(cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &graph, &deps, nullptr, &ndeps));
+  if (st != cudaStreamCaptureStatusActive) throw std::string("device loop outside a capture");
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = loop.handle;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  TPM_CUDA_TRY(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &cp));
+  cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
+  TPM_CUDA_TRY(cudaStreamBeginCaptureToGraph(c->side, bodyg, nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeThreadLocal));
+  std::swap(c->stream, c->side);
+  try {
+    body();
+  } catch (...) {
+    std::swap(c->stream, c->side);
+    cudaGraph_t g2 = nullptr;
+    cudaStreamEndCapture(c->side, &g2);
+    throw;
+  }
+  std::swap(c->stream, c->side);
+  cudaGraph_t captured = nullptr;
+  TPM_CUDA_TRY(cudaStreamEndCapture(c->side, &captured));
+  TPM_CUDA_TRY(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1,
+                                                   cudaStreamSetCaptureDependencies));
+}
+
+tpm::LoopCtl new_loop(tpm_ctx *c, int max_it) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t graph = nullptr;
+  TPM_CUDA_TRY(cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &graph, nullptr, nullptr, nullptr));
+  tpm::LoopCtl loop;
+  loop.max_it = max_it;
+  TPM_CUDA_TRY(cudaGraphConditionalHandleCreate(&loop.handle, graph, 1, cudaGraphCondAssignDefault));
+  return loop;
+}
+
+double read_err(tpm_ctx *c) {
+  TPM_CUDA_TRY(cudaMemcpyAsync(&c->hsc->err, &c->dsc->err, sizeof(double), cudaMemcpyDeviceToHost,
+                               c->stream));
+  TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return c->hsc->err;
+}
+
 // poisson::FFT iteration control (poisson.cpp:395-410).  Eagerly, the host
 // reads max|dp| after each iteration when epsilon > 0, as the reference's loop
-// does.  Inside a captured step (device_loop) all max_it iterations are
-// enqueued and the device applies the same test: once max|dp| <= epsilon the
-// remaining iterations' kernels return at once, so the result and the
-// iteration count are the same.
+// does.  Inside a captured step (device_loop) the loop is a conditional while
+// node whose body is one iteration; the device applies the same test, so the
+// result and the iteration count are the same.  Solver = 2 runs PCG
+// (tpm_pcg.cu) under the same control with its two-norm test.
 void poisson_loop(tpm_ctx *c, int max_it, double eps) {
   TPM_CUDA_TRY(cudaMemsetAsync(&c->dsc->skip, 0, 2 * sizeof(int), c->stream));  // skip, it
+  const double eps_ctl = eps > 0 ? eps : 0.0;
+  if (c->p.Solver == 2) {
+    if (c->device_loop) {
+      c->last_it = -1;
+      tpm::LoopCtl loop = new_loop(c, max_it);
+      tpm::pcg_setup(c, eps_ctl, max_it > 0 ? &loop : nullptr);
+      if (max_it > 0) capture_while(c, loop, [&] { tpm::pcg_step(c, eps_ctl, &loop); });
+      return;
+    }
+    tpm::pcg_setup(c, eps_ctl, nullptr);
+    double error = eps > 0 ? read_err(c) : 100;
+    int it = 0;
+    while (it < max_it && error > eps) {
+      tpm::pcg_step(c, eps_ctl, nullptr);
+      it++;
+      if (eps > 0) error = read_err(c);
+    }
+    c->last_it = it;
+    c->total_it += it;
+    if (eps > 0) c->last_err = error;
+    return;
+  }
   if (c->device_loop) {
     c->last_it = -1;  // on the device (DevScalars::it)
     if (max_it <= 0) return;
-    // the loop as a conditional while node of the graph being captured: its
-    // body (one iteration, captured on the side stream) repeats until the
-    // last kernel of an iteration reports it < max_it && max|dp| > eps false
-    cudaStreamCaptureStatus st;
-    cudaGraph_t graph = nullptr;
-    const cudaGraphNode_t *deps = nullptr;
-    size_t ndeps = 0;
-    TPM_CUDA_TRY(cudaStreamGetCaptureInfo(c->stream, &st, nullptr, &graph, &deps, nullptr, &ndeps));
-    if (st != cudaStreamCaptureStatusActive) throw std::string("device loop outside a capture");
-    tpm::LoopCtl loop;
-    loop.max_it = max_it;
-    TPM_CUDA_TRY(cudaGraphConditionalHandleCreate(&loop.handle, graph, 1, cudaGraphCondAssignDefault));
-    cudaGraphNodeParams cp = {};
-    cp.type = cudaGraphNodeTypeConditional;
-    cp.conditional.handle = loop.handle;
-    cp.conditional.type = cudaGraphCondTypeWhile;
-    cp.conditional.size = 1;
-    cudaGraphNode_t node;
-    TPM_CUDA_TRY(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &cp));
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    TPM_CUDA_TRY(cudaStreamBeginCaptureToGraph(c->side, body, nullptr, nullptr, 0,
-                                               cudaStreamCaptureModeThreadLocal));
-    std::swap(c->stream, c->side);
-    try {
-      tpm::poisson_iteration(c, eps > 0 ? eps : 0.0, &loop);
-    } catch (...) {
-      std::swap(c->stream, c->side);
-      cudaGraph_t g2 = nullptr;
-      cudaStreamEndCapture(c->side, &g2);
-      throw;
-    }
-    std::swap(c->stream, c->side);
-    cudaGraph_t captured = nullptr;
-    TPM_CUDA_TRY(cudaStreamEndCapture(c->side, &captured));
-    TPM_CUDA_TRY(cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1,
-                                                     cudaStreamSetCaptureDependencies));
+    tpm::LoopCtl loop = new_loop(c, max_it);
+    capture_while(c, loop, [&] { tpm::poisson_iteration(c, eps_ctl, &loop); });
     return;
   }
   int it = 0;
   double error = 100;
-  const bool need_err = eps > 0;
   while ((it < max_it) && (error > eps)) {
     tpm::poisson_iteration(c);
     it++;
-    if (need_err) {
-      TPM_CUDA_TRY(cudaMemcpyAsync(&c->hsc->err, &c->dsc->err, sizeof(double),
-                                   cudaMemcpyDeviceToHost, c->stream));
-      TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
-      error = c->hsc->err;
-    }
+    if (eps > 0) error = read_err(c);
   }
   c->last_it = it;
   c->total_it += it;
-  if (need_err) c->last_err = error;
+  if (eps > 0) c->last_err = error;
 }
 
 void swap_stage(tpm_ctx *c) {
@@ -272,6 +308,9 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
                 "elongated box and passive vector are outside the ported path");
   if (p->precision != TPM_PREC_FP64 && p->precision != TPM_PREC_MIXED)
     return fail(c, TPM_ERR_ARG, "unknown precision");
+  if (p->Solver != 0 && p->Solver != 2)
+    return fail(c, TPM_ERR_UNSUPPORTED,
+                "Solver must be 0 (FFT-preconditioned Richardson) or 2 (PCG)");
   if (!factorable(p->Nx) || !factorable(p->Ny) || !factorable(p->Nz) || (p->Nx % 2) ||
       p->Nx < 4 || p->Ny < 2 || p->Nz < 2)
     return fail(c, TPM_ERR_ARG, "grid sizes must be products of 2, 3, 5 with Nx even and >= 4");

@@ -657,6 +657,131 @@ void spectrum_mode_energy(tpm_ctx *c, const double *U3, double2 *spec, double *e
   }
 }
 
+// ------------------------------------------------ FFT preconditioner (PCG)
+// z = M^-1 r with M = c0 (-Lap_h): the constant-coefficient operator of the
+// Richardson loop, here symmetric (one coefficient c0 for the whole box) so
+// that it can precondition conjugate gradients.  x-pass forward of r/c0,
+// y forward, z forward + divide by the modified wave number + z inverse, y
+// inverse, x-pass inverse storing z = x/N^3 with per-block partials of r.z.
+namespace {
+
+template <typename T2>
+__global__ void k_pc_xfwd(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
+                          const double *__restrict__ r, double scale, T2 *__restrict__ spec,
+                          int npen, const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using T = typename Cx<T2>::T;
+  T2 *a = reinterpret_cast<T2 *>(smem_raw);
+  const int M = pl.n;
+  T2 *b = a + M * npen;
+  const long long nrows = (long long)g.ny * g.nz;
+  const long long row0 = (long long)blockIdx.x * npen;
+  for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
+    const int q = idx / g.nx, i = idx % g.nx;
+    const long long row = row0 + q;
+    T *slot = reinterpret_cast<T *>(&a[(i >> 1) * npen + q]);
+    slot[i & 1] = row < nrows ? (T)(r[row * g.nx + i] * scale) : (T)0;
+  }
+  __syncthreads();
+  T2 *z = smem_fft(a, b, npen, pl, -1);
+  r2c_store(g, z, npen, M, row0, nrows, r2c_tw, spec);
+}
+
+template <typename T2>
+__global__ void k_pc_xinv(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
+                          const T2 *__restrict__ spec, const double *__restrict__ r,
+                          double *__restrict__ zout, double *__restrict__ partials, int npen,
+                          const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double sh[32];
+  using T = typename Cx<T2>::T;
+  T2 *a = reinterpret_cast<T2 *>(smem_raw);
+  const int M = pl.n;
+  T2 *b = a + M * npen;
+  const long long nrows = (long long)g.ny * g.nz;
+  const long long row0 = (long long)blockIdx.x * npen;
+  const int nxh = g.nxh;
+  for (int idx = threadIdx.x; idx < npen * M; idx += blockDim.x) {
+    const int q = idx / M, kx = idx % M;
+    const long long row = row0 + q;
+    T2 Z = Cx<T2>::mk(0, 0);
+    if (row < nrows) {
+      T2 X = spec[row * nxh + kx];
+      T2 Y = spec[row * nxh + (M - kx)];
+      Y.y = -Y.y;
+      T fer = X.x + Y.x, fei = X.y + Y.y;
+      T dr = X.x - Y.x, di = X.y - Y.y;
+      T2 w = r2c_tw[kx];
+      T for_ = Cx<T2>::fma_(dr, w.x, di * w.y);
+      T foi = Cx<T2>::fma_(di, w.x, -dr * w.y);
+      Z = Cx<T2>::mk(fer - foi, fei + for_);
+    }
+    a[kx * npen + q] = Z;
+  }
+  __syncthreads();
+  T2 *zz = smem_fft(a, b, npen, pl, +1);
+  const double inv_tot = 1.0 / (double)(g.nx * g.ny * g.nz);
+  double acc = 0;
+  for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
+    const int q = idx / g.nx, i = idx % g.nx;
+    const long long row = row0 + q;
+    if (row >= nrows) continue;
+    const T *v = reinterpret_cast<const T *>(&zz[(i >> 1) * npen + q]);
+    const long long c = row * g.nx + i;
+    const double zc = (double)v[i & 1] * inv_tot;
+    zout[c] = zc;
+    acc += r[c] * zc;
+  }
+  double bs = block_sum(acc, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = bs;
+}
+
+template <typename T2>
+void precondition_t(tpm_ctx *c, const double *r, double scale, double *z, double *parts,
+                    const int *skip) {
+  const Grid &g = c->g;
+  const long long nrows = (long long)g.ny * g.nz;
+  T2 *spec = reinterpret_cast<T2 *>(c->spec);
+  const T2 *r2c = sizeof(T2) == sizeof(double2) ? reinterpret_cast<const T2 *>(c->r2c64)
+                                                : reinterpret_cast<const T2 *>(c->r2c32);
+  const int npx = c->pen[0], npy = c->pen[1], npz = c->pen[2];
+  const int xblocks = (int)((nrows + npx - 1) / npx);
+  const size_t sx = 2 * (size_t)npx * c->fx.n * sizeof(T2);
+  const size_t sy = 2 * (size_t)npy * c->fy.n * sizeof(T2);
+  const size_t sz = 2 * (size_t)npz * c->fz.n * sizeof(T2);
+  TPM_LAUNCH(c, "pcg_fft_x_fwd", k_pc_xfwd<T2>, xblocks, kFftThreads, sx, g, c->fx, r2c, r, scale,
+             spec, npx, skip);
+  TPM_LAUNCH(c, "pcg_fft_y", k_fft_y<T2>, g.nz * ((g.nxh + npy - 1) / npy), kFftThreads, sy, g,
+             c->fy, spec, npy, -1, skip);
+  TPM_LAUNCH(c, "pcg_fft_z_solve", k_fft_z_solve<T2>, g.ny * ((g.nxh + npz - 1) / npz),
+             kFftThreads, sz, g, c->fz, spec, c->ax, c->ay, c->az, npz, skip);
+  TPM_LAUNCH(c, "pcg_fft_y", k_fft_y<T2>, g.nz * ((g.nxh + npy - 1) / npy), kFftThreads, sy, g,
+             c->fy, spec, npy, +1, skip);
+  TPM_LAUNCH(c, "pcg_fft_x_inv", k_pc_xinv<T2>, xblocks, kFftThreads, sx, g, c->fx, r2c, spec, r,
+             z, parts, npx, skip);
+}
+
+}  // namespace
+
+int fft_precondition(tpm_ctx *c, const double *r, double scale, double *z, double *parts,
+                     const int *skip) {
+  if (c->p.precision == TPM_PREC_MIXED)
+    precondition_t<float2>(c, r, scale, z, parts, skip);
+  else
+    precondition_t<double2>(c, r, scale, z, parts, skip);
+  return (int)(((long long)c->g.ny * c->g.nz + c->pen[0] - 1) / c->pen[0]);
+}
+
+void precondition_setup() {
+  const int smem64 = 2 * kFftSmemPoints * (int)sizeof(double2);
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_pc_xfwd<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_pc_xfwd<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_pc_xinv<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_pc_xinv<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+}
+
 void spectrum_kernels_setup() {
   const int smem64 = 2 * kFftSmemPoints * (int)sizeof(double2);
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_spec_xfwd, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));

@@ -707,6 +707,15 @@ __global__ void k_mean_reset(Grid g, const double *__restrict__ RU_np1, double *
 // grid::Initialize (grid.cpp:474): nothing to store on the device beyond the
 // copies done by the host; kept for the operator-level Poisson entry point:
 // center_coeff = -1/I_F2C(C) for a caller-supplied C (poisson.cpp:393-394).
+// Cs_d = C_d / d^2 for caller-supplied face coefficients (operator-level solve)
+__global__ void k_scale_faces(Grid g, const double *__restrict__ Cf, double *__restrict__ Cs) {
+  const double inv_d2[3] = {g.inv_dx2, g.inv_dy2, g.inv_dz2};
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) Cs[d * g.n + c] = Cf[d * g.n + c] * inv_d2[d];
+}
+
 __global__ void k_center_coeff(Grid g, const double *__restrict__ Cf, double *__restrict__ cc) {
   const double OneThird = 1. / 3.;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
@@ -875,6 +884,9 @@ void launch_mean_reset(tpm_ctx *c) {
 void launch_center_coeff_from_C(tpm_ctx *c) {
   TPM_LAUNCH(c, "center_coeff", k_center_coeff, cell_blocks(c->g), kThreads, 0, c->g, c->Cface,
              c->cc);
+  if (c->p.precision == TPM_PREC_MIXED)  // the mixed residual reads C/d^2
+    TPM_LAUNCH(c, "face_coeff_scaled", k_scale_faces, cell_blocks(c->g), kThreads, 0, c->g,
+               c->Cface, c->Cs);
 }
 
 void launch_init_fields(tpm_ctx *) {}

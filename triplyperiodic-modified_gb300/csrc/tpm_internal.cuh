@@ -181,6 +181,10 @@ struct tpm_ctx {
   bool store_div = false;
   bool div_every_stage = false;
 
+  // ---- PCG pressure solve (Solver = 2; allocated on first use) ----
+  double *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr;
+  double *pcg_sc = nullptr, *pcg_parts = nullptr;
+
   // ---- CUDA graph replay of whole steps (tpm_graph.cu) ----
   bool graph_mode = false;
   std::vector<tpm::GraphEntry> graphs;
@@ -243,6 +247,14 @@ struct LoopCtl {
 // eps_ctl > 0 and no loop control the iteration sets dsc->skip once
 // max|dp| <= eps_ctl, and every kernel of a later iteration returns at once.
 void poisson_iteration(tpm_ctx *c, double eps_ctl = 0.0, const LoopCtl *loop = nullptr);
+// z = M^-1 r (M = -Lap_h/scale, FFT passes of the Poisson solve) with per-block
+// partials of r.z; returns the number of partials
+int fft_precondition(tpm_ctx *c, const double *r, double scale, double *z, double *parts,
+                     const int *skip);
+void precondition_setup();
+// PCG pressure solve (Solver = 2; tpm_pcg.cu): set-up, then one iteration
+void pcg_setup(tpm_ctx *c, double eps, const LoopCtl *loop);
+void pcg_step(tpm_ctx *c, double eps, const LoopCtl *loop);
 int pens_default(int n, int elem_bytes);
 int pens_max(int n, int elem_bytes);
 // energy per half-spectrum mode of the face velocity U3 (3n), summed over

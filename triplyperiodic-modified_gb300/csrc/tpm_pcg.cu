@@ -1,0 +1,276 @@
+// Pressure solve by preconditioned conjugate gradients (Solver = 2).
+//
+// The reference offers HYPRE Krylov solvers besides the FFT-preconditioned
+// Richardson loop (poisson.cpp:117-388; Solver 2 is PCG with a two-norm
+// relative stopping test ||r||/||b|| < epsilon and at most Iteration
+// iterations, poisson.cpp:214-245).  Here the same operator
+// div(C grad P) = RHS (7-point, face coefficients C = 1/Rho_face) is solved by
+// PCG with the constant-coefficient FFT solve as the preconditioner
+// (M = -Lap_h, the Richardson loop's spectral solve without its pointwise
+// scale, so that M is symmetric).  For strongly heated flows, where the
+// density ratio and with it the Richardson contraction factor grow, CG needs
+// about the square root of the iterations.  Vectors and reductions are FP64;
+// on the mixed path the preconditioner's FFTs are FP32.
+//
+// Per iteration: p = z + beta p; q = A p (A = -div(C grad .)) with p.q;
+// alpha; P += alpha p, r -= alpha q with r.r; z = M^-1 r with r.z; beta and
+// the stopping test.  Every reduction is a fixed-order tree over per-block
+// partials, so a solve is bit-reproducible.
+#include <cmath>
+
+#include "tpm_internal.cuh"
+#include "tpm_reduce.cuh"
+
+namespace tpm {
+namespace {
+
+constexpr int kThreadsPcg = 256;
+
+// device scalars of the iteration
+enum { PC_RHO = 0, PC_PQ, PC_ALPHA, PC_BETA, PC_RR, PC_BB, PC_ERR, PC_COUNT };
+
+__device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
+  return ((long long)k * g.ny + j) * g.nx + i;
+}
+
+// div(C grad f) at cell c with the operation order of the Richardson
+// residual (poisson.cpp:399-401); kScaled: Cf holds C/d^2 per component.
+template <bool kScaled>
+__device__ __forceinline__ double lap_c(const Grid &g, const double *__restrict__ f,
+                                        const double *__restrict__ Cf, long long c) {
+  const int i = (int)(c % g.nx), j = (int)((c / g.nx) % g.ny), k = (int)(c / ((long long)g.nx * g.ny));
+  const double *Cx = Cf, *Cy = Cf + g.n, *Cz = Cf + 2 * g.n;
+  const long long xp = at(g, wrap_p(i, g.nx), j, k), xm = at(g, wrap_m(i, g.nx), j, k);
+  const long long yp = at(g, i, wrap_p(j, g.ny), k), ym = at(g, i, wrap_m(j, g.ny), k);
+  const long long zp = at(g, i, j, wrap_p(k, g.nz)), zm = at(g, i, j, wrap_m(k, g.nz));
+  const double fc = f[c];
+  if (kScaled)
+    return (Cx[xp] * (f[xp] - fc) - Cx[c] * (fc - f[xm])) +
+           (Cy[yp] * (f[yp] - fc) - Cy[c] * (fc - f[ym])) +
+           (Cz[zp] * (f[zp] - fc) - Cz[c] * (fc - f[zm]));
+  const double gx_hi = (f[xp] - fc) * g.inv_dx * Cx[xp], gx_lo = (fc - f[xm]) * g.inv_dx * Cx[c];
+  const double gy_hi = (f[yp] - fc) * g.inv_dy * Cy[yp], gy_lo = (fc - f[ym]) * g.inv_dy * Cy[c];
+  const double gz_hi = (f[zp] - fc) * g.inv_dz * Cz[zp], gz_lo = (fc - f[zm]) * g.inv_dz * Cz[c];
+  return (gx_hi - gx_lo) * g.inv_dx + (gy_hi - gy_lo) * g.inv_dy + (gz_hi - gz_lo) * g.inv_dz;
+}
+
+// r = b - A P = div(C grad P) - (RHS - mean(RHS)); partials of r.r and b.b
+template <bool kScaled>
+__global__ void k_pcg_residual(Grid g, const double *__restrict__ P, const double *__restrict__ Cf,
+                               const double *__restrict__ RHS, const DevScalars *__restrict__ s,
+                               double *__restrict__ r, double *__restrict__ parts_rr,
+                               double *__restrict__ parts_bb) {
+  __shared__ double sh[32];
+  const double mean = s->mean_rhs;
+  double rr = 0, bb = 0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    const double b = RHS[c] - mean;
+    const double rc = lap_c<kScaled>(g, P, Cf, c) - b;
+    r[c] = rc;
+    rr += rc * rc;
+    bb += b * b;
+  }
+  double v = block_sum(rr, sh);
+  if (threadIdx.x == 0) parts_rr[blockIdx.x] = v;
+  v = block_sum(bb, sh);
+  if (threadIdx.x == 0) parts_bb[blockIdx.x] = v;
+}
+
+__device__ double sum_parts(const double *__restrict__ parts, int n, double *sh) {
+  double v = 0;
+  for (int b = threadIdx.x; b < n; b += blockDim.x) v += parts[b];
+  return block_sum(v, sh);
+}
+
+// after the first preconditioning: rho = r.z, b.b, the relative residual,
+// and whether the loop runs at all (poisson.cpp:214-245's HYPRE PCG stops on
+// ||r||_2 / ||b||_2 < epsilon)
+__global__ void k_pcg_init(const double *__restrict__ parts_rz, int n_rz,
+                           const double *__restrict__ parts_rr, const double *__restrict__ parts_bb,
+                           int n_c, double *__restrict__ sc, DevScalars *__restrict__ s, double eps,
+                           cudaGraphConditionalHandle loop, int loop_max) {
+  __shared__ double sh[32];
+  const double rz = sum_parts(parts_rz, n_rz, sh);
+  __syncthreads();
+  const double rr = sum_parts(parts_rr, n_c, sh);
+  __syncthreads();
+  const double bb = sum_parts(parts_bb, n_c, sh);
+  if (threadIdx.x == 0) {
+    sc[PC_RHO] = rz;
+    sc[PC_BETA] = 0.0;
+    sc[PC_RR] = rr;
+    sc[PC_BB] = bb;
+    const double rel = bb > 0 ? sqrt(rr) / sqrt(bb) : 0.0;
+    sc[PC_ERR] = rel;
+    s->err = rel;
+    const bool more = bb > 0 && !(eps > 0 && !(rel > eps));
+    s->skip = more ? 0 : 1;
+    if (loop_max > 0) cudaGraphSetConditional(loop, more ? 1u : 0u);
+  }
+}
+
+// p = z + beta p
+__global__ void k_pcg_p(long long n, const double *__restrict__ z, double *__restrict__ p,
+                        const double *__restrict__ sc, const int *__restrict__ skip) {
+  if (*skip) return;
+  const double beta = sc[PC_BETA];
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x)
+    p[c] = z[c] + beta * p[c];
+}
+
+// q = A p = -div(C grad p); partials of p.q
+template <bool kScaled>
+__global__ void k_pcg_matvec(Grid g, const double *__restrict__ p, const double *__restrict__ Cf,
+                             double *__restrict__ q, double *__restrict__ parts,
+                             const int *__restrict__ skip) {
+  if (*skip) return;
+  __shared__ double sh[32];
+  double acc = 0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    const double qc = -lap_c<kScaled>(g, p, Cf, c);
+    q[c] = qc;
+    acc += p[c] * qc;
+  }
+  double v = block_sum(acc, sh);
+  if (threadIdx.x == 0) parts[blockIdx.x] = v;
+}
+
+__global__ void k_pcg_alpha(const double *__restrict__ parts, int n, double *__restrict__ sc,
+                            const int *__restrict__ skip) {
+  if (*skip) return;
+  __shared__ double sh[32];
+  const double pq = sum_parts(parts, n, sh);
+  if (threadIdx.x == 0) {
+    sc[PC_PQ] = pq;
+    sc[PC_ALPHA] = pq != 0 ? sc[PC_RHO] / pq : 0.0;
+  }
+}
+
+// P += alpha p, r -= alpha q; partials of r.r and max|alpha p|
+__global__ void k_pcg_update(long long n, double *__restrict__ P, double *__restrict__ r,
+                             const double *__restrict__ p, const double *__restrict__ q,
+                             const double *__restrict__ sc, double *__restrict__ parts_rr,
+                             double *__restrict__ parts_dx, const int *__restrict__ skip) {
+  if (*skip) return;
+  __shared__ double sh[32];
+  const double alpha = sc[PC_ALPHA];
+  double rr = 0, mx = 0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+       c += (long long)gridDim.x * blockDim.x) {
+    const double dx = alpha * p[c];
+    P[c] += dx;
+    const double rc = r[c] - alpha * q[c];
+    r[c] = rc;
+    rr += rc * rc;
+    const double a = fabs(dx);
+    mx = a > mx ? a : mx;
+  }
+  double v = block_sum(rr, sh);
+  if (threadIdx.x == 0) parts_rr[blockIdx.x] = v;
+  v = block_max(mx, sh);
+  if (threadIdx.x == 0) parts_dx[blockIdx.x] = v;
+}
+
+// beta = r.z / rho, the stopping test, the iteration count
+__global__ void k_pcg_finish(const double *__restrict__ parts_rz, int n_rz,
+                             const double *__restrict__ parts_rr,
+                             const double *__restrict__ parts_dx, int n_c, double *__restrict__ sc,
+                             DevScalars *__restrict__ s, double eps,
+                             cudaGraphConditionalHandle loop, int loop_max) {
+  if (loop_max == 0 && s->skip) return;
+  __shared__ double sh[32];
+  const double rz = sum_parts(parts_rz, n_rz, sh);
+  __syncthreads();
+  const double rr = sum_parts(parts_rr, n_c, sh);
+  __syncthreads();
+  double v = 0;
+  for (int b = threadIdx.x; b < n_c; b += blockDim.x) v = parts_dx[b] > v ? parts_dx[b] : v;
+  const double mdx = block_max(v, sh);
+  if (threadIdx.x == 0) {
+    const double rho = sc[PC_RHO];
+    sc[PC_BETA] = rho != 0 ? rz / rho : 0.0;
+    sc[PC_RHO] = rz;
+    sc[PC_RR] = rr;
+    const double rel = sc[PC_BB] > 0 ? sqrt(rr) / sqrt(sc[PC_BB]) : 0.0;
+    sc[PC_ERR] = rel;
+    s->err = rel;
+    (void)mdx;
+    s->it += 1;
+    s->it_sum += 1;
+    const bool more = !(eps > 0 && !(rel > eps));
+    if (loop_max > 0)
+      cudaGraphSetConditional(loop, (s->it < loop_max && more) ? 1u : 0u);
+    else if (!more)
+      s->skip = 1;
+  }
+}
+
+int cblocks(const Grid &g) {
+  long long b = (g.n + kThreadsPcg - 1) / kThreadsPcg;
+  return (int)(b < kRedBlocks ? b : kRedBlocks);
+}
+
+void ensure_pcg(tpm_ctx *c) {
+  if (c->pcg_r) return;
+  const size_t n = (size_t)c->g.n;
+  c->pcg_r = dalloc<double>(c, n);
+  c->pcg_z = dalloc<double>(c, n);
+  c->pcg_p = dalloc<double>(c, n);
+  c->pcg_q = dalloc<double>(c, n);
+  c->pcg_sc = dalloc<double>(c, PC_COUNT);
+  c->pcg_parts = dalloc<double>(c, 4 * (size_t)kRedBlocks + (size_t)c->g.ny * c->g.nz);
+  precondition_setup();
+}
+
+}  // namespace
+
+// One PCG iteration (everything after the set-up); `loop` when captured.
+static void pcg_iteration(tpm_ctx *c, double eps, const LoopCtl *loop) {
+  const Grid &g = c->g;
+  const bool scaled = c->p.precision == TPM_PREC_MIXED;
+  const double *Cf = scaled ? c->Cs : c->Cface;
+  const int nb = cblocks(g);
+  const int *skip = &c->dsc->skip;
+  double *pq = c->pcg_parts, *prr = pq + kRedBlocks, *pdx = prr + kRedBlocks,
+         *prz = pdx + 2 * kRedBlocks;
+  TPM_LAUNCH(c, "pcg_p", k_pcg_p, nb, kThreadsPcg, 0, g.n, c->pcg_z, c->pcg_p, c->pcg_sc, skip);
+  if (scaled)
+    TPM_LAUNCH(c, "pcg_matvec", k_pcg_matvec<true>, nb, kThreadsPcg, 0, g, c->pcg_p, Cf, c->pcg_q,
+               pq, skip);
+  else
+    TPM_LAUNCH(c, "pcg_matvec", k_pcg_matvec<false>, nb, kThreadsPcg, 0, g, c->pcg_p, Cf, c->pcg_q,
+               pq, skip);
+  TPM_LAUNCH(c, "pcg_alpha", k_pcg_alpha, 1, kThreadsPcg, 0, pq, nb, c->pcg_sc, skip);
+  TPM_LAUNCH(c, "pcg_update", k_pcg_update, nb, kThreadsPcg, 0, g.n, c->P, c->pcg_r, c->pcg_p,
+             c->pcg_q, c->pcg_sc, prr, pdx, skip);
+  const int nrz = fft_precondition(c, c->pcg_r, 1.0, c->pcg_z, prz, skip);
+  TPM_LAUNCH(c, "pcg_finish", k_pcg_finish, 1, kThreadsPcg, 0, prz, nrz, prr, pdx, nb, c->pcg_sc,
+             c->dsc, eps, loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0);
+}
+
+// Set-up of a solve: r = b - A P, z = M^-1 r, rho = r.z, the initial test.
+void pcg_setup(tpm_ctx *c, double eps, const LoopCtl *loop) {
+  ensure_pcg(c);
+  const Grid &g = c->g;
+  const bool scaled = c->p.precision == TPM_PREC_MIXED;
+  const double *Cf = scaled ? c->Cs : c->Cface;
+  const int nb = cblocks(g);
+  double *prr = c->pcg_parts + kRedBlocks, *pbb = c->pcg_parts,
+         *prz = c->pcg_parts + 3 * kRedBlocks;
+  if (scaled)
+    TPM_LAUNCH(c, "pcg_residual", k_pcg_residual<true>, nb, kThreadsPcg, 0, g, c->P, Cf, c->RHS,
+               c->dsc, c->pcg_r, prr, pbb);
+  else
+    TPM_LAUNCH(c, "pcg_residual", k_pcg_residual<false>, nb, kThreadsPcg, 0, g, c->P, Cf, c->RHS,
+               c->dsc, c->pcg_r, prr, pbb);
+  const int nrz = fft_precondition(c, c->pcg_r, 1.0, c->pcg_z, prz, nullptr);
+  TPM_LAUNCH(c, "pcg_init", k_pcg_init, 1, kThreadsPcg, 0, prz, nrz, prr, pbb, nb, c->pcg_sc,
+             c->dsc, eps, loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0);
+}
+
+void pcg_step(tpm_ctx *c, double eps, const LoopCtl *loop) { pcg_iteration(c, eps, loop); }
+
+}  // namespace tpm

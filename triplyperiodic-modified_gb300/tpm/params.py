@@ -39,7 +39,7 @@ class TpmParams(ctypes.Structure):
         ("Dp", ctypes.c_double), ("Rhop", ctypes.c_double), ("Cvp", ctypes.c_double),
         ("epsilonp", ctypes.c_double), ("Nu", ctypes.c_double),
         ("I01", ctypes.c_double), ("I02", ctypes.c_double),
-        ("D_M", ctypes.c_double), ("S1_type", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("D_M", ctypes.c_double), ("S1_type", ctypes.c_int32), ("Solver", ctypes.c_int32),
     ]
 
 
@@ -124,6 +124,7 @@ class Params:
     solve_for_vector: int = 0
     D_M: float = 0.0          # passive-scalar diffusivity (params.h:51)
     S1_type: int = 1          # passive-scalar source type (params.h:53, token s1t)
+    Solver: int = 0           # 0: FFT-preconditioned Richardson; 2: PCG (tpm_params.Solver)
 
     # ---- derived (params.cpp:70-77, params.h:133-138) ----
     @property
@@ -161,8 +162,7 @@ class Params:
     def to_c(self) -> TpmParams:
         c = TpmParams()
         for f in TpmParams._fields_:
-            if f[0] != "reserved":
-                setattr(c, f[0], getattr(self, f[0]))
+            setattr(c, f[0], getattr(self, f[0]))
         return c
 
     def replace(self, **kw) -> "Params":
@@ -189,7 +189,7 @@ class Params:
             "1",  # Initial: restart files
             "1" if self.solve_for_scalar else "5",  # Initial_C: Restart_Passive_Scalar.bin
             "2",  # Initial_V: RV = 0
-            "0 0",  # PreCond Solver (0 = FFT)
+            f"0 {self.Solver}",  # PreCond Solver (0 = FFT)
             f"{self.cooling}",
             f"{self.Iteration1} {self.Iteration2} {g(self.epsilon)}",
             f"{self.TWC} {self.ParticleGravity}",
