@@ -405,6 +405,7 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->pay_r = dalloc<double>(c, 4 * (size_t)np);
     c->w8 = dalloc<double>(c, 16 * (size_t)np);
     c->C_next = dalloc<double>(c, n);
+    if (p->Solver == 2) tpm::pcg_alloc(c);
     if (p->solve_for_scalar) {
       c->PS = dalloc<double>(c, n); c->PS_int = dalloc<double>(c, n);
       c->PS_new = dalloc<double>(c, n); c->PS_np1 = dalloc<double>(c, n);

@@ -253,6 +253,7 @@ int fft_precondition(tpm_ctx *c, const double *r, double scale, double *z, doubl
                      const int *skip);
 void precondition_setup();
 // PCG pressure solve (Solver = 2; tpm_pcg.cu): set-up, then one iteration
+void pcg_alloc(tpm_ctx *c);
 void pcg_setup(tpm_ctx *c, double eps, const LoopCtl *loop);
 void pcg_step(tpm_ctx *c, double eps, const LoopCtl *loop);
 int pens_default(int n, int elem_bytes);

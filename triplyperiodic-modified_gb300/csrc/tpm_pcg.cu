@@ -115,6 +115,12 @@ __global__ void k_pcg_p(long long n, const double *__restrict__ z, double *__res
                         const double *__restrict__ sc, const int *__restrict__ skip) {
   if (*skip) return;
   const double beta = sc[PC_BETA];
+  if (beta == 0.0) {  // first iteration: p = z (p holds the previous solve)
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
+         c += (long long)gridDim.x * blockDim.x)
+      p[c] = z[c];
+    return;
+  }
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
        c += (long long)gridDim.x * blockDim.x)
     p[c] = z[c] + beta * p[c];
@@ -213,7 +219,10 @@ int cblocks(const Grid &g) {
   return (int)(b < kRedBlocks ? b : kRedBlocks);
 }
 
-void ensure_pcg(tpm_ctx *c) {
+}  // namespace
+
+// Buffers of the solver; called by tpm_create (never inside a graph capture).
+void pcg_alloc(tpm_ctx *c) {
   if (c->pcg_r) return;
   const size_t n = (size_t)c->g.n;
   c->pcg_r = dalloc<double>(c, n);
@@ -221,11 +230,14 @@ void ensure_pcg(tpm_ctx *c) {
   c->pcg_p = dalloc<double>(c, n);
   c->pcg_q = dalloc<double>(c, n);
   c->pcg_sc = dalloc<double>(c, PC_COUNT);
-  c->pcg_parts = dalloc<double>(c, 4 * (size_t)kRedBlocks + (size_t)c->g.ny * c->g.nz);
+  const size_t np = 4 * (size_t)kRedBlocks + (size_t)c->g.ny * c->g.nz;
+  c->pcg_parts = dalloc<double>(c, np);
+  for (double *v : {c->pcg_r, c->pcg_z, c->pcg_p, c->pcg_q})
+    TPM_CUDA_TRY(cudaMemsetAsync(v, 0, sizeof(double) * n, c->stream));
+  TPM_CUDA_TRY(cudaMemsetAsync(c->pcg_sc, 0, sizeof(double) * PC_COUNT, c->stream));
+  TPM_CUDA_TRY(cudaMemsetAsync(c->pcg_parts, 0, sizeof(double) * np, c->stream));
   precondition_setup();
 }
-
-}  // namespace
 
 // One PCG iteration (everything after the set-up); `loop` when captured.
 static void pcg_iteration(tpm_ctx *c, double eps, const LoopCtl *loop) {
@@ -253,7 +265,7 @@ static void pcg_iteration(tpm_ctx *c, double eps, const LoopCtl *loop) {
 
 // Set-up of a solve: r = b - A P, z = M^-1 r, rho = r.z, the initial test.
 void pcg_setup(tpm_ctx *c, double eps, const LoopCtl *loop) {
-  ensure_pcg(c);
+  if (!c->pcg_r) throw std::string("PCG buffers not allocated (Solver != 2 at create)");
   const Grid &g = c->g;
   const bool scaled = c->p.precision == TPM_PREC_MIXED;
   const double *Cf = scaled ? c->Cs : c->Cface;
