@@ -658,17 +658,19 @@ void spectrum_mode_energy(tpm_ctx *c, const double *U3, double2 *spec, double *e
 }
 
 // ------------------------------------------------ FFT preconditioner (PCG)
-// z = M^-1 r with M = c0 (-Lap_h): the constant-coefficient operator of the
-// Richardson loop, here symmetric (one coefficient c0 for the whole box) so
-// that it can precondition conjugate gradients.  x-pass forward of r/c0,
-// y forward, z forward + divide by the modified wave number + z inverse, y
-// inverse, x-pass inverse storing z = x/N^3 with per-block partials of r.z.
+// z = M^-1 r with M^-1 = S (-Lap_h)^-1 S, S = diag(sc): the Richardson loop's
+// preconditioner (poisson.cpp:393-394 scale by -1/I_F2C(C), then the
+// constant-coefficient spectral solve) in its symmetric form, sc = 1/sqrt(C_c)
+// at the cell centres, so that it can precondition conjugate gradients.
+// x-pass forward of sc*r, y forward, z forward + divide by the modified wave
+// number + z inverse, y inverse, x-pass inverse storing z = sc*x/N^3 with
+// per-block partials of r.z.
 namespace {
 
 template <typename T2>
 __global__ void k_pc_xfwd(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
-                          const double *__restrict__ r, double scale, T2 *__restrict__ spec,
-                          int npen, const int *__restrict__ skip) {
+                          const double *__restrict__ r, const double *__restrict__ sc,
+                          T2 *__restrict__ spec, int npen, const int *__restrict__ skip) {
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using T = typename Cx<T2>::T;
@@ -681,7 +683,8 @@ __global__ void k_pc_xfwd(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
     const int q = idx / g.nx, i = idx % g.nx;
     const long long row = row0 + q;
     T *slot = reinterpret_cast<T *>(&a[(i >> 1) * npen + q]);
-    slot[i & 1] = row < nrows ? (T)(r[row * g.nx + i] * scale) : (T)0;
+    const long long c = row * g.nx + i;
+    slot[i & 1] = row < nrows ? (T)(r[c] * sc[c]) : (T)0;
   }
   __syncthreads();
   T2 *z = smem_fft(a, b, npen, pl, -1);
@@ -691,8 +694,8 @@ __global__ void k_pc_xfwd(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
 template <typename T2>
 __global__ void k_pc_xinv(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
                           const T2 *__restrict__ spec, const double *__restrict__ r,
-                          double *__restrict__ zout, double *__restrict__ partials, int npen,
-                          const int *__restrict__ skip) {
+                          const double *__restrict__ sc, double *__restrict__ zout,
+                          double *__restrict__ partials, int npen, const int *__restrict__ skip) {
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double sh[32];
@@ -730,7 +733,7 @@ __global__ void k_pc_xinv(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
     if (row >= nrows) continue;
     const T *v = reinterpret_cast<const T *>(&zz[(i >> 1) * npen + q]);
     const long long c = row * g.nx + i;
-    const double zc = (double)v[i & 1] * inv_tot;
+    const double zc = ((double)v[i & 1] * inv_tot) * sc[c];
     zout[c] = zc;
     acc += r[c] * zc;
   }
@@ -739,7 +742,7 @@ __global__ void k_pc_xinv(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
 }
 
 template <typename T2>
-void precondition_t(tpm_ctx *c, const double *r, double scale, double *z, double *parts,
+void precondition_t(tpm_ctx *c, const double *r, const double *sc, double *z, double *parts,
                     const int *skip) {
   const Grid &g = c->g;
   const long long nrows = (long long)g.ny * g.nz;
@@ -751,7 +754,7 @@ void precondition_t(tpm_ctx *c, const double *r, double scale, double *z, double
   const size_t sx = 2 * (size_t)npx * c->fx.n * sizeof(T2);
   const size_t sy = 2 * (size_t)npy * c->fy.n * sizeof(T2);
   const size_t sz = 2 * (size_t)npz * c->fz.n * sizeof(T2);
-  TPM_LAUNCH(c, "pcg_fft_x_fwd", k_pc_xfwd<T2>, xblocks, kFftThreads, sx, g, c->fx, r2c, r, scale,
+  TPM_LAUNCH(c, "pcg_fft_x_fwd", k_pc_xfwd<T2>, xblocks, kFftThreads, sx, g, c->fx, r2c, r, sc,
              spec, npx, skip);
   TPM_LAUNCH(c, "pcg_fft_y", k_fft_y<T2>, g.nz * ((g.nxh + npy - 1) / npy), kFftThreads, sy, g,
              c->fy, spec, npy, -1, skip);
@@ -760,17 +763,17 @@ void precondition_t(tpm_ctx *c, const double *r, double scale, double *z, double
   TPM_LAUNCH(c, "pcg_fft_y", k_fft_y<T2>, g.nz * ((g.nxh + npy - 1) / npy), kFftThreads, sy, g,
              c->fy, spec, npy, +1, skip);
   TPM_LAUNCH(c, "pcg_fft_x_inv", k_pc_xinv<T2>, xblocks, kFftThreads, sx, g, c->fx, r2c, spec, r,
-             z, parts, npx, skip);
+             sc, z, parts, npx, skip);
 }
 
 }  // namespace
 
-int fft_precondition(tpm_ctx *c, const double *r, double scale, double *z, double *parts,
+int fft_precondition(tpm_ctx *c, const double *r, const double *sc, double *z, double *parts,
                      const int *skip) {
   if (c->p.precision == TPM_PREC_MIXED)
-    precondition_t<float2>(c, r, scale, z, parts, skip);
+    precondition_t<float2>(c, r, sc, z, parts, skip);
   else
-    precondition_t<double2>(c, r, scale, z, parts, skip);
+    precondition_t<double2>(c, r, sc, z, parts, skip);
   return (int)(((long long)c->g.ny * c->g.nz + c->pen[0] - 1) / c->pen[0]);
 }
 

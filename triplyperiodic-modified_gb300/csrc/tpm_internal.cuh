@@ -183,6 +183,7 @@ struct tpm_ctx {
 
   // ---- PCG pressure solve (Solver = 2; allocated on first use) ----
   double *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr;
+  double *pcg_s = nullptr;  // 1/sqrt(C at the cell centre) = sqrt(-cc)
   double *pcg_sc = nullptr, *pcg_parts = nullptr;
 
   // ---- CUDA graph replay of whole steps (tpm_graph.cu) ----
@@ -247,9 +248,9 @@ struct LoopCtl {
 // eps_ctl > 0 and no loop control the iteration sets dsc->skip once
 // max|dp| <= eps_ctl, and every kernel of a later iteration returns at once.
 void poisson_iteration(tpm_ctx *c, double eps_ctl = 0.0, const LoopCtl *loop = nullptr);
-// z = M^-1 r (M = -Lap_h/scale, FFT passes of the Poisson solve) with per-block
-// partials of r.z; returns the number of partials
-int fft_precondition(tpm_ctx *c, const double *r, double scale, double *z, double *parts,
+// z = S (-Lap_h)^-1 S r, S = diag(sc) (FFT passes of the Poisson solve), with
+// per-block partials of r.z; returns the number of partials
+int fft_precondition(tpm_ctx *c, const double *r, const double *sc, double *z, double *parts,
                      const int *skip);
 void precondition_setup();
 // PCG pressure solve (Solver = 2; tpm_pcg.cu): set-up, then one iteration

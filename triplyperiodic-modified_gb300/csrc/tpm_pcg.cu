@@ -5,9 +5,10 @@
 // relative stopping test ||r||/||b|| < epsilon and at most Iteration
 // iterations, poisson.cpp:214-245).  Here the same operator
 // div(C grad P) = RHS (7-point, face coefficients C = 1/Rho_face) is solved by
-// PCG with the constant-coefficient FFT solve as the preconditioner
-// (M = -Lap_h, the Richardson loop's spectral solve without its pointwise
-// scale, so that M is symmetric).  For strongly heated flows, where the
+// PCG preconditioned by the Richardson loop's own approximate inverse in
+// symmetric form, M^-1 = S (-Lap_h)^-1 S with S = diag(1/sqrt(C_c)) and C_c the
+// centre-averaged coefficient (poisson.cpp:393-394), applied with the same
+// pencil FFTs.  For strongly heated flows, where the
 // density ratio and with it the Richardson contraction factor grow, CG needs
 // about the square root of the iterations.  Vectors and reductions are FP64;
 // on the mixed path the preconditioner's FFTs are FP32.
@@ -54,10 +55,12 @@ __device__ __forceinline__ double lap_c(const Grid &g, const double *__restrict_
   return (gx_hi - gx_lo) * g.inv_dx + (gy_hi - gy_lo) * g.inv_dy + (gz_hi - gz_lo) * g.inv_dz;
 }
 
-// r = b - A P = div(C grad P) - (RHS - mean(RHS)); partials of r.r and b.b
+// r = b - A P = div(C grad P) - (RHS - mean(RHS)); partials of r.r and b.b;
+// the preconditioner scale sc = sqrt(-cc) = 1/sqrt(I_F2C(C)) once per solve
 template <bool kScaled>
 __global__ void k_pcg_residual(Grid g, const double *__restrict__ P, const double *__restrict__ Cf,
                                const double *__restrict__ RHS, const DevScalars *__restrict__ s,
+                               const double *__restrict__ cc, double *__restrict__ scale,
                                double *__restrict__ r, double *__restrict__ parts_rr,
                                double *__restrict__ parts_bb) {
   __shared__ double sh[32];
@@ -68,6 +71,7 @@ __global__ void k_pcg_residual(Grid g, const double *__restrict__ P, const doubl
     const double b = RHS[c] - mean;
     const double rc = lap_c<kScaled>(g, P, Cf, c) - b;
     r[c] = rc;
+    scale[c] = sqrt(-cc[c]);
     rr += rc * rc;
     bb += b * b;
   }
@@ -229,10 +233,11 @@ void pcg_alloc(tpm_ctx *c) {
   c->pcg_z = dalloc<double>(c, n);
   c->pcg_p = dalloc<double>(c, n);
   c->pcg_q = dalloc<double>(c, n);
+  c->pcg_s = dalloc<double>(c, n);
   c->pcg_sc = dalloc<double>(c, PC_COUNT);
   const size_t np = 4 * (size_t)kRedBlocks + (size_t)c->g.ny * c->g.nz;
   c->pcg_parts = dalloc<double>(c, np);
-  for (double *v : {c->pcg_r, c->pcg_z, c->pcg_p, c->pcg_q})
+  for (double *v : {c->pcg_r, c->pcg_z, c->pcg_p, c->pcg_q, c->pcg_s})
     TPM_CUDA_TRY(cudaMemsetAsync(v, 0, sizeof(double) * n, c->stream));
   TPM_CUDA_TRY(cudaMemsetAsync(c->pcg_sc, 0, sizeof(double) * PC_COUNT, c->stream));
   TPM_CUDA_TRY(cudaMemsetAsync(c->pcg_parts, 0, sizeof(double) * np, c->stream));
@@ -258,7 +263,7 @@ static void pcg_iteration(tpm_ctx *c, double eps, const LoopCtl *loop) {
   TPM_LAUNCH(c, "pcg_alpha", k_pcg_alpha, 1, kThreadsPcg, 0, pq, nb, c->pcg_sc, skip);
   TPM_LAUNCH(c, "pcg_update", k_pcg_update, nb, kThreadsPcg, 0, g.n, c->P, c->pcg_r, c->pcg_p,
              c->pcg_q, c->pcg_sc, prr, pdx, skip);
-  const int nrz = fft_precondition(c, c->pcg_r, 1.0, c->pcg_z, prz, skip);
+  const int nrz = fft_precondition(c, c->pcg_r, c->pcg_s, c->pcg_z, prz, skip);
   TPM_LAUNCH(c, "pcg_finish", k_pcg_finish, 1, kThreadsPcg, 0, prz, nrz, prr, pdx, nb, c->pcg_sc,
              c->dsc, eps, loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0);
 }
@@ -274,11 +279,11 @@ void pcg_setup(tpm_ctx *c, double eps, const LoopCtl *loop) {
          *prz = c->pcg_parts + 3 * kRedBlocks;
   if (scaled)
     TPM_LAUNCH(c, "pcg_residual", k_pcg_residual<true>, nb, kThreadsPcg, 0, g, c->P, Cf, c->RHS,
-               c->dsc, c->pcg_r, prr, pbb);
+               c->dsc, c->cc, c->pcg_s, c->pcg_r, prr, pbb);
   else
     TPM_LAUNCH(c, "pcg_residual", k_pcg_residual<false>, nb, kThreadsPcg, 0, g, c->P, Cf, c->RHS,
-               c->dsc, c->pcg_r, prr, pbb);
-  const int nrz = fft_precondition(c, c->pcg_r, 1.0, c->pcg_z, prz, nullptr);
+               c->dsc, c->cc, c->pcg_s, c->pcg_r, prr, pbb);
+  const int nrz = fft_precondition(c, c->pcg_r, c->pcg_s, c->pcg_z, prz, nullptr);
   TPM_LAUNCH(c, "pcg_init", k_pcg_init, 1, kThreadsPcg, 0, prz, nrz, prr, pbb, nb, c->pcg_sc,
              c->dsc, eps, loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0);
 }
