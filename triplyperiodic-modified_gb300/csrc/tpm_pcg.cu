@@ -92,8 +92,7 @@ __device__ double sum_parts(const double *__restrict__ parts, int n, double *sh)
 // ||r||_2 / ||b||_2 < epsilon)
 __global__ void k_pcg_init(const double *__restrict__ parts_rz, int n_rz,
                            const double *__restrict__ parts_rr, const double *__restrict__ parts_bb,
-                           int n_c, double *__restrict__ sc, DevScalars *__restrict__ s, double eps,
-                           cudaGraphConditionalHandle loop, int loop_max) {
+                           int n_c, double *__restrict__ sc, DevScalars *__restrict__ s, double eps) {
   __shared__ double sh[32];
   const double rz = sum_parts(parts_rz, n_rz, sh);
   __syncthreads();
@@ -109,8 +108,7 @@ __global__ void k_pcg_init(const double *__restrict__ parts_rz, int n_rz,
     sc[PC_ERR] = rel;
     s->err = rel;
     const bool more = bb > 0 && !(eps > 0 && !(rel > eps));
-    s->skip = more ? 0 : 1;
-    if (loop_max > 0) cudaGraphSetConditional(loop, more ? 1u : 0u);
+    s->skip = more ? 0 : 1;  // a captured loop then runs one no-op body and stops
   }
 }
 
@@ -190,7 +188,10 @@ __global__ void k_pcg_finish(const double *__restrict__ parts_rz, int n_rz,
                              const double *__restrict__ parts_dx, int n_c, double *__restrict__ sc,
                              DevScalars *__restrict__ s, double eps,
                              cudaGraphConditionalHandle loop, int loop_max) {
-  if (loop_max == 0 && s->skip) return;
+  if (s->skip) {  // converged before this body (set-up or previous iteration)
+    if (loop_max > 0 && threadIdx.x == 0) cudaGraphSetConditional(loop, 0u);
+    return;
+  }
   __shared__ double sh[32];
   const double rz = sum_parts(parts_rz, n_rz, sh);
   __syncthreads();
@@ -285,7 +286,8 @@ void pcg_setup(tpm_ctx *c, double eps, const LoopCtl *loop) {
                c->dsc, c->cc, c->pcg_s, c->pcg_r, prr, pbb);
   const int nrz = fft_precondition(c, c->pcg_r, c->pcg_s, c->pcg_z, prz, nullptr);
   TPM_LAUNCH(c, "pcg_init", k_pcg_init, 1, kThreadsPcg, 0, prz, nrz, prr, pbb, nb, c->pcg_sc,
-             c->dsc, eps, loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0);
+             c->dsc, eps);
+  (void)loop;
 }
 
 void pcg_step(tpm_ctx *c, double eps, const LoopCtl *loop) { pcg_iteration(c, eps, loop); }
