@@ -305,6 +305,21 @@ int tpm_spectrum(tpm_ctx *ctx, double *E, int nshells);
  * r_max must be at most min_d L_d/3. */
 int tpm_rdf(tpm_ctx *ctx, double r_max, int nbins, unsigned long long *pairs, double *g);
 
+/* Discrete adjoint of nsteps RK4 steps from the current state (right after
+ * tpm_initialize or tpm_resume), for the unheated, uncooled, gravity-free
+ * uniform-density regime (FP64 path; other settings return
+ * TPM_ERR_UNSUPPORTED).  Objective at the final step boundary:
+ *   J = w_tke * 0.5 * sum_d mean(RU_d^2 / Rho_face_d) + w_cvar * var(C),
+ * C the cloud-in-cell concentration of the final particle positions
+ * (particle.cpp:522-555 weights).  Outputs (each optional): J; dJ/dRU(0)
+ * (3*N doubles on the host, projected on discretely divergence-free fields);
+ * dJ/dA (forcing coefficient A1 = A2); dJ/dtau_p (uniform shift of the Stokes
+ * time).  Forward states are recomputed from checkpoints taken every
+ * checkpoint_every steps.  Returns with the context at the final state, as
+ * after tpm_run(ctx, nsteps).  Not in the reference. */
+int tpm_adjoint_run(tpm_ctx *ctx, int nsteps, int checkpoint_every, double w_tke, double w_cvar,
+                    double *J, double *dJ_dRU0, double *dJ_dA, double *dJ_dtau);
+
 /* Picks the pencils per block of each FFT pass (x, y, z) of the pressure solve
  * by timing Poisson iterations on the context's grid; results do not depend on
  * the choice (each pencil is transformed independently).  The state is kept:

@@ -261,6 +261,8 @@ void end_step(tpm_ctx *c) {
 namespace tpm {
 
 void step_param_update(tpm_ctx *c) { param_update(c); }
+void step_substep(tpm_ctx *c, int s) { substep(c, s); }
+void step_end(tpm_ctx *c) { end_step(c); }
 
 void step_body(tpm_ctx *c) {
   for (int s = 0; s < 4; ++s) substep(c, s);
@@ -655,6 +657,19 @@ int tpm_initialize(tpm_ctx *c) {
 
 int tpm_resume(tpm_ctx *c) {
   return guarded(c, [&]() -> int {
+    tpm::resume_device(c);
+    return TPM_OK;
+  });
+}
+
+}  // extern "C"
+
+namespace tpm {
+
+// The step-boundary state (base copies, RU_int, P, Q, rhs_t, scalars) is on
+// the device; rebuild everything a step derives from it.
+void resume_device(tpm_ctx *c) {
+  {
     const long long n = c->g.n;
     // at a step boundary Rho_int == Rho, x_int == x (all particle copies
     // agree), P0_int == P0 and every np1 copy equals its base copy
@@ -676,9 +691,12 @@ int tpm_resume(tpm_ctx *c) {
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->initialized = true;
     c->stepped = false;
-    return TPM_OK;
-  });
+  }
 }
+
+}  // namespace tpm
+
+extern "C" {
 
 int tpm_substep(tpm_ctx *c, int rk_stage) {
   return guarded(c, [&]() -> int {

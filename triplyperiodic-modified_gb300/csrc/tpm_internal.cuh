@@ -267,7 +267,10 @@ void spectrum_kernels_setup();
 // ---- step driver (tpm_ctx.cu) and graph replay (tpm_graph.cu) ----
 void step_param_update(tpm_ctx *c);  // PARAM.update (params.cpp:80-86)
 void step_body(tpm_ctx *c);          // four substeps and the end of step
+void step_substep(tpm_ctx *c, int s); // one RK4 stage
+void step_end(tpm_ctx *c);           // make_mean_U0 and TimeAdvance
 void step_any(tpm_ctx *c);           // one step, replayed from a graph in graph mode
+void resume_device(tpm_ctx *c);      // tpm_resume without the status wrapper
 void graphs_clear(std::vector<GraphEntry> &cache);
 
 // ---- particles (tpm_particles.cu) ----

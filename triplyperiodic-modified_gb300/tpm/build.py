@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libtpm.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["tpm_ctx.cu", "tpm_fields.cu", "tpm_fft.cu", "tpm_particles.cu", "tpm_diag.cu", "tpm_graph.cu", "tpm_pcg.cu", "tpm_io.cpp"]
+SOURCES = ["tpm_ctx.cu", "tpm_fields.cu", "tpm_fft.cu", "tpm_particles.cu", "tpm_diag.cu", "tpm_graph.cu", "tpm_pcg.cu", "tpm_adjoint.cu", "tpm_io.cpp"]
 # per-source extra flags
 EXTRA = {}
 

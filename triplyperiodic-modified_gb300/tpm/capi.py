@@ -71,6 +71,7 @@ SIGNATURES = {
     "tpm_profile_reset": (_i, [_vp]),
     "tpm_launch_count": (_i64, [_vp]),
     "tpm_autotune": (_i, [_vp, ctypes.POINTER(_i)]),
+    "tpm_adjoint_run": (_i, [_vp, _i, _i, _d, _d, _dp, _dp, _dp, _dp]),
     "tpm_batch_create": (_i, [_vp, ctypes.POINTER(_i64), _i, ctypes.POINTER(_vp)]),
     "tpm_batch_destroy": (_i, [_vp]),
     "tpm_batch_last_error": (ctypes.c_char_p, [_vp]),
@@ -152,6 +153,16 @@ class Context:
 
     def set_graph(self, on=True):
         self.set_option(OPT_CUDA_GRAPH, int(on))
+
+    def adjoint(self, nsteps, checkpoint_every=20, w_tke=1.0, w_cvar=0.0, grad_ru0=True):
+        """J and (dJ/dRU0, dJ/dA, dJ/dtau) by the discrete adjoint (tpm_adjoint_run)."""
+        J, gA, gt = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        g = np.empty((3, self.p.Nz, self.p.Ny, self.p.Nx)) if grad_ru0 else None
+        self._check(self.L.tpm_adjoint_run(self.h, int(nsteps), int(checkpoint_every),
+                                           float(w_tke), float(w_cvar), ctypes.byref(J),
+                                           _dptr(g) if g is not None else None,
+                                           ctypes.byref(gA), ctypes.byref(gt)))
+        return J.value, g, gA.value, gt.value
 
     def autotune(self):
         pens = (_i * 3)()
