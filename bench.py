@@ -472,6 +472,67 @@ def ensemble_main(args):
         print(json.dumps(line), flush=True)
 
 
+ADJOINT = "adjoint64"
+
+
+def adjoint_main(args):
+    """Gradient of J = TKE + var(C) after a 200-step horizon (64^3 cells, 2e5
+    two-way-coupled particles, checkpoints every 20 steps) by the discrete
+    adjoint, timed against the same forward steps alone."""
+    import numpy as np
+    import torch
+    from tpm import capi, params as P
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    horizon = args.steps if args.steps != 10 else 200
+    p, s = make_workload("box64_p2e5", P.PREC_FP64)
+
+    def fresh():
+        c = capi.Context(p, s.npart)
+        c.load(s)
+        c.initialize()
+        return c
+
+    c = fresh()
+    c.run(args.warmup)
+    c.sync()
+    c = fresh()
+    t0 = time.perf_counter()
+    c.run(horizon)
+    c.sync()
+    fwd = time.perf_counter() - t0
+    c = fresh()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        J, g, gA, gt = c.adjoint(horizon, checkpoint_every=20, w_tke=1.0, w_cvar=1.0)
+        adj = time.perf_counter() - t0
+    value = world * p.ncell * horizon / adj / 1e6
+    line = {
+        "metric": "adjoint Mcell-steps/s (forward + checkpointed recomputation + backward), "
+                  "64^3 + 2e5 particles, 200-step horizon",
+        "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": horizon,
+        "warmup": args.warmup, "ms_per_step": round(adj * 1e3 / horizon, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seed 3, solenoidal E(k)~k^4 exp(-2(k/4)^2), uniform particles)",
+        "config": {"workload": f"{ADJOINT}: {p.Nx}^3, {s.npart} particles, nu={p.Mu0:g}, "
+                               f"tau_p=0.1, mass loading 0.3, checkpoints every 20 steps",
+                   "parallelism": f"replicas x{world}"},
+        "adjoint_over_forward": round(adj / fwd, 3),
+        "forward_ms_per_step": round(fwd * 1e3 / horizon, 3),
+        "J": J, "grad_norms": {"dJ_dRU0_l2": float(np.sqrt(np.sum(g * g))), "dJ_dA": gA,
+                               "dJ_dtau": gt},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(g.nbytes / horizon)},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def ctypes_sizeof_stats():
     import ctypes
 
@@ -485,6 +546,10 @@ def reference_main(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
+        return
+    if args.workload in (ENSEMBLE, ADJOINT):
+        print(json.dumps({"impl": "reference", "unavailable":
+                          "the reference runs one box per MPI job and has no adjoint"}), flush=True)
         return
     sys.path.insert(0, os.path.join(HERE, "oracle"))
     import pyoracle
@@ -544,6 +609,8 @@ def main():
         reference_main(args)
     elif args.workload == ENSEMBLE:
         ensemble_main(args)
+    elif args.workload == ADJOINT:
+        adjoint_main(args)
     else:
         gpu_main(args)
 
