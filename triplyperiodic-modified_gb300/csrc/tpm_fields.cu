@@ -204,11 +204,15 @@ __global__ void k_rhs_momentum(Grid g, const TIn *__restrict__ U, const TIn *__r
                 (TC)0.5;
         rhs += (rf - (TC)a.Rho0) * (TC)a.g[d];
       }
-      // RU_np1 += dt*post*RHS ; RU_new = RU + dt*pre*RHS  (grid.cpp:811-813)
+      // RU_np1 += dt*post*RHS ; RU_new = RU + dt*pre*RHS  (grid.cpp:811-813);
+      // FMAs on the mixed path (FP32 stencil, FP64 accumulation)
       const double r64 = (double)rhs;
-      double np1 = np1_in[d * g.n + c] + a.dtpo * r64;
+      constexpr bool kFma = sizeof(TC) == sizeof(float);
+      double np1 = kFma ? fma(a.dtpo, r64, np1_in[d * g.n + c]) : np1_in[d * g.n + c] + a.dtpo * r64;
       RU_np1[d * g.n + c] = np1;
-      RU_new[d * g.n + c] = (a.stage != 3) ? 1 * RU[d * g.n + c] + a.dtpr * r64 : np1;
+      RU_new[d * g.n + c] = (a.stage != 3) ? (kFma ? fma(a.dtpr, r64, RU[d * g.n + c])
+                                                   : 1 * RU[d * g.n + c] + a.dtpr * r64)
+                                           : np1;
     }
   }
 }
@@ -427,11 +431,11 @@ __global__ void k_rho_update_mixed(Grid g, const double *__restrict__ RUi,
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
-    double D = (RUx[at(g, wrap_p(q.i, g.nx), q.j, q.k)] - RUx[c]) * g.inv_dx +
-               (RUy[at(g, q.i, wrap_p(q.j, g.ny), q.k)] - RUy[c]) * g.inv_dy +
-               (RUz[at(g, q.i, q.j, wrap_p(q.k, g.nz))] - RUz[c]) * g.inv_dz;
-    double np1 = np1_in[c] + a_np1 * D;
-    double nw = (stage != 3) ? Rho[c] + b_new * D : np1;
+    double D = (RUx[at(g, wrap_p(q.i, g.nx), q.j, q.k)] - RUx[c]) * g.inv_dx;
+    D = fma(RUy[at(g, q.i, wrap_p(q.j, g.ny), q.k)] - RUy[c], g.inv_dy, D);
+    D = fma(RUz[at(g, q.i, q.j, wrap_p(q.k, g.nz))] - RUz[c], g.inv_dz, D);
+    double np1 = fma(a_np1, D, np1_in[c]);
+    double nw = (stage != 3) ? fma(b_new, D, Rho[c]) : np1;
     Rho_np1[c] = np1;
     Rho_new[c] = nw;
     double ir = rcp64(nw);
@@ -481,25 +485,27 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
     Nbr nb = nbr_of(g, q);
+    // FMA chains throughout (this kernel is FP64-pipe bound; the mixed path
+    // has no bitwise-parity constraint)
     double ir = inv_rho[c];
-    double lap = (inv_rho[nb.p[0]] - 2 * ir + inv_rho[nb.m[0]]) * g.inv_dx2 +
-                 (inv_rho[nb.p[1]] - 2 * ir + inv_rho[nb.m[1]]) * g.inv_dy2 +
-                 (inv_rho[nb.p[2]] - 2 * ir + inv_rho[nb.m[2]]) * g.inv_dz2;
+    double lap = (fma(-2.0, ir, inv_rho[nb.p[0]]) + inv_rho[nb.m[0]]) * g.inv_dx2;
+    lap = fma(fma(-2.0, ir, inv_rho[nb.p[1]]) + inv_rho[nb.m[1]], g.inv_dy2, lap);
+    lap = fma(fma(-2.0, ir, inv_rho[nb.p[2]]) + inv_rho[nb.m[2]], g.inv_dz2, lap);
     double Qc = a.cooling ? Q[c] - meanQ : Q[c];
-    double dv = a.kCp * lap + coef * Qc;
+    double dv = fma(a.kCp, lap, coef * Qc);
     divg[c] = dv;
-    double t[3];
+    double divu = -dv;
     float msum = 0.f;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const double clo = Cface[d * g.n + c], chi = Cface[d * g.n + nb.p[d]];
       const double *R = RUn + d * g.n;
       const double u_lo = R[c] * clo;
-      t[d] = (R[nb.p[d]] * chi - u_lo) * inv_d[d];
+      divu = fma(fma(R[nb.p[d]], chi, -u_lo), inv_d[d], divu);
       msum += ((float)clo + (float)chi) * 0.5f;
       if (tke_parts) usq += u_lo * u_lo;
     }
-    double rhs = (t[0] + t[1] + t[2] - dv) * a.inv_dtpre;
+    double rhs = divu * a.inv_dtpre;
     RHS[c] = rhs;
     acc += rhs;
     cc[c] = (double)(-3.0f / msum);
@@ -607,6 +613,8 @@ __global__ void k_ps_face(Grid g, const double *__restrict__ src, double *__rest
 // ---------------------------------------------------------- projection
 // grid::Update_RU_WP, grid.cpp:857-863.  At the last stage the per-component
 // sums of RU_np1 for make_mean_U0 (simulation.cpp:80) are reduced too.
+// kFma (mixed path): the updates as FMAs
+template <bool kFma>
 __global__ void k_project(Grid g, const double *__restrict__ P, double *__restrict__ RU_np1,
                           double *__restrict__ RU_new, double a_np1, double b_new, int stage,
                           double *__restrict__ partials, float *__restrict__ RUn32) {
@@ -621,9 +629,11 @@ __global__ void k_project(Grid g, const double *__restrict__ P, double *__restri
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       double G = (pc - P[nb.m[d]]) * inv_d[d];
-      double np1 = RU_np1[d * g.n + c] + a_np1 * G;
+      double np1 = kFma ? fma(a_np1, G, RU_np1[d * g.n + c]) : RU_np1[d * g.n + c] + a_np1 * G;
       RU_np1[d * g.n + c] = np1;
-      const double nw = (stage != 3) ? RU_new[d * g.n + c] + b_new * G : np1;
+      const double nw = (stage != 3) ? (kFma ? fma(b_new, G, RU_new[d * g.n + c])
+                                             : RU_new[d * g.n + c] + b_new * G)
+                                     : np1;
       RU_new[d * g.n + c] = nw;
       if (RUn32) RUn32[d * g.n + c] = (float)nw;
       acc[d] += np1;
@@ -822,9 +832,14 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
 
 void launch_project(tpm_ctx *c, int s) {
   int nb = cell_blocks(c->g);
-  TPM_LAUNCH(c, "project", k_project, nb, kThreads, 0, c->g, c->P, c->RU_np1, c->RU_new,
-             -(c->p.dt * kPost[s]), -(c->p.dt * kPre[s]), s, c->partials + kPartRu * kRedBlocks,
-             c->p.precision == TPM_PREC_MIXED ? c->RUn32 : nullptr);
+  if (c->p.precision == TPM_PREC_MIXED)
+    TPM_LAUNCH(c, "project", k_project<true>, nb, kThreads, 0, c->g, c->P, c->RU_np1, c->RU_new,
+               -(c->p.dt * kPost[s]), -(c->p.dt * kPre[s]), s,
+               c->partials + kPartRu * kRedBlocks, c->RUn32);
+  else
+    TPM_LAUNCH(c, "project", k_project<false>, nb, kThreads, 0, c->g, c->P, c->RU_np1, c->RU_new,
+               -(c->p.dt * kPost[s]), -(c->p.dt * kPre[s]), s,
+               c->partials + kPartRu * kRedBlocks, nullptr);
   if (s == 3)
     TPM_LAUNCH(c, "finish_means3", k_finish_means3, 1, kThreads, 0,
                c->partials + kPartRu * kRedBlocks, nb, c->g.n,

@@ -80,22 +80,29 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
                     (1 - zf) * (float)U[2 * g.n + c0]);
     }
     // ---- update_position (particle.cpp:314-338) ----
+    // (the mixed path, TU = float, accumulates with FMAs; the FP64 path keeps
+    // the reference's separate multiply and add)
+    constexpr bool kFma = sizeof(TU) == sizeof(float);
     double xn[3], xp[3], xb[3];
     const double uint_[3] = {ui, vi, wi};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       xb[d] = ps.b[d][p];
-      xp[d] = ps.np1_in[d][p] + a.dtpo * uint_[d];
-      xn[d] = (a.stage != 3) ? xb[d] + a.dtpr * uint_[d] : xp[d];
+      xp[d] = kFma ? fma(a.dtpo, uint_[d], ps.np1_in[d][p]) : ps.np1_in[d][p] + a.dtpo * uint_[d];
+      xn[d] = (a.stage != 3) ? (kFma ? fma(a.dtpr, uint_[d], xb[d]) : xb[d] + a.dtpr * uint_[d])
+                             : xp[d];
     }
     // ---- update_velocity (particle.cpp:362-399) ----
     const double iTp = a.has_tau ? 1. / tau[p] : a.iTp;
     const double rhs[3] = {(ug - ui) * iTp, (vg - vi) * iTp, (wg - wi) * iTp};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      double np1 = ps.np1_in[3 + d][p] + a.dtpo * (rhs[d] + a.gp[d]);
+      const double f = rhs[d] + a.gp[d];
+      double np1 = kFma ? fma(a.dtpo, f, ps.np1_in[3 + d][p]) : ps.np1_in[3 + d][p] + a.dtpo * f;
       ps.np1[3 + d][p] = np1;
-      ps.nw[3 + d][p] = (a.stage != 3) ? ps.b[3 + d][p] + a.dtpr * (rhs[d] + a.gp[d]) : np1;
+      ps.nw[3 + d][p] = (a.stage != 3) ? (kFma ? fma(a.dtpr, f, ps.b[3 + d][p])
+                                               : ps.b[3 + d][p] + a.dtpr * f)
+                                       : np1;
     }
     // ---- update_Temp with the previous heat rate (particle.cpp:477-492) ----
     const double rt_old = rhs_t[p];
