@@ -358,17 +358,35 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   T2 *z = smem_fft(a, b, npen, pl, +1);
   const double inv_tot = 1.0 / (double)(g.nx * g.ny * g.nz);
   double mx = 0;
-  for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
-    const int q = idx / g.nx, i = idx % g.nx;
-    const long long row = row0 + q;
-    if (row >= nrows) continue;
-    const T *zz = reinterpret_cast<const T *>(&z[(i >> 1) * npen + q]);
-    double x = (double)zz[i & 1];
-    double dp = -(x * inv_tot);  // poisson.cpp:460, (-1)*re/N^3
-    const long long c = row * g.nx + i;
-    P[c] += dp;
-    double ad = fabs(dp);
-    mx = ad > mx ? ad : mx;
+  if (sizeof(T) == sizeof(float)) {
+    // mixed path: max|x| in FP32 (exact: the maximum picks one x, scaled once
+    // below) and P += -x/N^3 as one FMA, two FP64-pipe operations per cell
+    float mxf = 0.f;
+    for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
+      const int q = idx / g.nx, i = idx % g.nx;
+      const long long row = row0 + q;
+      if (row >= nrows) continue;
+      const T *zz = reinterpret_cast<const T *>(&z[(i >> 1) * npen + q]);
+      const float xf = (float)zz[i & 1];
+      const long long c = row * g.nx + i;
+      P[c] = fma(-(double)xf, inv_tot, P[c]);
+      const float ax = fabsf(xf);
+      mxf = ax > mxf ? ax : mxf;
+    }
+    mx = (double)mxf * inv_tot;
+  } else {
+    for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
+      const int q = idx / g.nx, i = idx % g.nx;
+      const long long row = row0 + q;
+      if (row >= nrows) continue;
+      const T *zz = reinterpret_cast<const T *>(&z[(i >> 1) * npen + q]);
+      double x = (double)zz[i & 1];
+      double dp = -(x * inv_tot);  // poisson.cpp:460, (-1)*re/N^3
+      const long long c = row * g.nx + i;
+      P[c] += dp;
+      double ad = fabs(dp);
+      mx = ad > mx ? ad : mx;
+    }
   }
   double bm = block_max(mx, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = bm;
