@@ -121,8 +121,14 @@ __device__ __forceinline__ void stockham_stage(const T2 *__restrict__ a, T2 *__r
     const int k = i % p;
     T2 v[R];
     v[0] = a[i * npen + q];
+    if (p == 1) {  // first stage: every twiddle is w^0 = 1
 #pragma unroll
-    for (int t = 1; t < R; ++t) v[t] = cmul(a[(i + t * m) * npen + q], Cx<T2>::tw(pl, k * t * step), sign);
+      for (int t = 1; t < R; ++t) v[t] = a[(i + t * m) * npen + q];
+    } else {
+#pragma unroll
+      for (int t = 1; t < R; ++t)
+        v[t] = cmul(a[(i + t * m) * npen + q], Cx<T2>::tw(pl, k * t * step), sign);
+    }
     dft_small(v, R, sign);
     const int j = (i / p) * p * R + k;
 #pragma unroll
