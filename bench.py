@@ -301,6 +301,45 @@ def path_result(p, s, ms, steps, world, n_it, launches, prof, clocks, mixed, pea
     }
 
 
+def cufft_solve_ms(shape, lengths, dtype, reps=10):
+    """A constant-coefficient Poisson solve through cuFFT (torch.fft: 3-D R2C,
+    divide by the modified wave number, C2R), CUDA-event timed: the library
+    comparison for the hand-written pencil FFTs (no residual, no update)."""
+    import torch
+
+    dev = torch.device("cuda")
+    nz, ny, nx = shape
+    x = torch.randn(shape, dtype=dtype, device=dev)
+    ks = []
+    for n, L in ((nz, lengths[2]), (ny, lengths[1])):
+        k = torch.fft.fftfreq(n, d=1.0 / n, device=dev).to(dtype) * (2 * 3.141592653589793 / L)
+        h = L / n
+        ks.append((2.0 / h ** 2) * (1 - torch.cos(k * h)))
+    kx = torch.arange(nx // 2 + 1, device=dev).to(dtype) * (2 * 3.141592653589793 / lengths[0])
+    hx = lengths[0] / nx
+    mwn = ks[0][:, None, None] + ks[1][None, :, None] + ((2.0 / hx ** 2) * (1 - torch.cos(kx * hx)))[None, None, :]
+    mwn[0, 0, 0] = 1.0
+    inv = 1.0 / mwn
+    inv[0, 0, 0] = 0.0
+
+    def solve():
+        return torch.fft.irfftn(torch.fft.rfftn(x) * inv, s=shape)
+
+    for _ in range(3):
+        solve()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        solve()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+FFT_KERNELS = ("fft_x_fwd_resid", "fft_y", "fft_z_solve", "fft_x_inv_update", "finish_max")
+
+
 def gpu_main(args):
     import numpy as np
     import torch
@@ -379,6 +418,19 @@ def gpu_main(args):
         line["mixed_vs_fp64_speedup"] = round(r["value"] / f["value"], 3)
     if accuracy:
         line["mixed_accuracy"] = accuracy
+    # the pencil-FFT pressure iteration against cuFFT doing only the spectral solve
+    import torch
+
+    cmp = {}
+    for name, r_ in res.items():
+        per_it = sum(r_["kernels_ms_per_step"].get(k, 0.0) for k in FFT_KERNELS) / (4 * r_["n_it"])
+        dtype = torch.float32 if name == "mixed" else torch.float64
+        cmp[name] = {"own_iteration_ms": round(per_it, 4),
+                     "cufft_solve_ms": round(cufft_solve_ms((p64.Nz, p64.Ny, p64.Nx),
+                                                            (p64.Lx, p64.Ly, p64.Lz), dtype), 4),
+                     "note": "own = FP64 residual + R2C/C2R pencil FFTs + divide + P update "
+                             "(5 kernels); cuFFT = rfftn, divide, irfftn only"}
+    line["fft_vs_cufft"] = cmp
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(args.workload)
     hctx.close()
@@ -533,6 +585,62 @@ def adjoint_main(args):
         print(json.dumps(line), flush=True)
 
 
+LONGRUN = "longrun256"
+
+
+def longrun_main(args):
+    """Config 2's long check: the mixed and FP64 paths run the 256^3 + 8M
+    workload for 1000 steps (--steps) from the same state and are compared on
+    TKE, dissipation, rms velocity, concentration variance, the energy spectrum
+    and the particle RDF (the flow is chaotic, so fields are not compared)."""
+    import numpy as np
+    import torch
+    from tpm import capi, params as P
+
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    nsteps = args.steps if args.steps != 10 else 1000
+    p64, s = make_workload(WORKLOAD, P.PREC_FP64)
+    out, times = {}, {}
+    for name, prec in (("mixed", P.PREC_MIXED), ("fp64", P.PREC_FP64)):
+        c = capi.Context(p64.replace(precision=prec), s.npart)
+        c.load(s)
+        c.initialize()
+        c.set_graph(True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c.run(nsteps)
+        c.sync()
+        times[name] = time.perf_counter() - t0
+        st = c.statistics()
+        E, _ = c.spectrum()
+        pairs, g = c.rdf(0.3, 30)
+        out[name] = {"stats": st, "E": E, "pairs": pairs.astype(float)}
+        c.close()
+    a, b = out["mixed"], out["fp64"]
+    rel = {k: abs(a["stats"][k] - b["stats"][k]) / abs(b["stats"][k])
+           for k in ("TKE", "dissipation", "u_rms", "C_var", "Tg_mean", "Tp_mean", "P0")}
+    sig = b["E"] > 1e-3 * b["E"].max()
+    rel["spectrum_max_shell"] = float(np.max(np.abs(a["E"][sig] - b["E"][sig]) / b["E"][sig]))
+    ca, cb = np.cumsum(a["pairs"]), np.cumsum(b["pairs"])
+    rel["rdf_cumulative_pairs"] = float(np.max(np.abs(ca[5:] - cb[5:]) / cb[5:]))
+    line = {
+        "metric": "mixed vs FP64 statistics after a long run, 256^3 + 8M particles",
+        "value": max(rel.values()), "unit": "max relative difference", "n_gpus": 1,
+        "steps": nsteps, "warmup": 0, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "mixed vs f64", "data": "synthetic (seed 2)",
+        "config": {"workload": f"{WORKLOAD}, {nsteps} steps each path, graph-replayed"},
+        "relative_differences": rel,
+        "statistics": {k: {q: a["stats"][q] if k == "mixed" else b["stats"][q]
+                           for q in ("TKE", "dissipation", "u_rms", "C_var", "T_cur")}
+                       for k in ("mixed", "fp64")},
+        "seconds": times,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def ctypes_sizeof_stats():
     import ctypes
 
@@ -547,7 +655,7 @@ def reference_main(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
-    if args.workload in (ENSEMBLE, ADJOINT):
+    if args.workload in (ENSEMBLE, ADJOINT, LONGRUN):
         print(json.dumps({"impl": "reference", "unavailable":
                           "the reference runs one box per MPI job and has no adjoint"}), flush=True)
         return
@@ -611,6 +719,8 @@ def main():
         ensemble_main(args)
     elif args.workload == ADJOINT:
         adjoint_main(args)
+    elif args.workload == LONGRUN:
+        longrun_main(args)
     else:
         gpu_main(args)
 
