@@ -294,7 +294,6 @@ __global__ void k_adj_particles(Grid g, int64_t np, PAdj s, const double *__rest
                                 double *__restrict__ lamU, double *__restrict__ gtau) {
   __shared__ double sh_[32];
   const double idn[3] = {g.idx, g.idy, g.idz};
-  const int nn[3] = {g.nx, g.ny, g.nz};
   double acc_tau = 0;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
        p += (int64_t)gridDim.x * blockDim.x) {
@@ -314,7 +313,6 @@ __global__ void k_adj_particles(Grid g, int64_t np, PAdj s, const double *__rest
     const double tp = s.tau ? s.tau[p] : s.tau0;
     for (int d = 0; d < 3; ++d) {
       const long long chi = sh(g, lo, d, 1);
-      (void)nn;
       const Ix qhi = shq(g, lo, d, 1);
       const double Uhi = RU[d * g.n + chi] / rface(g, Rho, qhi, d);
       const double Ulo = RU[d * g.n + clo] / rface(g, Rho, lo, d);
@@ -536,13 +534,13 @@ void record_step(Adj &A, int rec, std::vector<double> &A_of_step) {
   step_end(c);
 }
 
-// backward through one recorded step
-void backward_step(Adj &A, int rec, double Astep, double *gA_parts_acc, std::vector<double> &gA) {
+// backward through one recorded step; appends each stage's <lam_RHS, RU_int>
+// (its part of dJ/dA) to gA
+void backward_step(Adj &A, int rec, double Astep, std::vector<double> &gA) {
   tpm_ctx *c = A.c;
   const Grid &g = c->g;
   const double dt = c->p.dt;
   const int nbc = blocks_for(g.n), nb3 = blocks_for(A.n3), nbp = blocks_for(A.np > 0 ? A.np : 1);
-  (void)gA_parts_acc;
   // end of step: lam_np1 = M(lam_RU) + lam_RUint0; particles np1 = base + int0
   TPM_LAUNCH(c, "adj_means", k_comp_sums, nbc, kAT, 0, g, A.lRU, A.red);
   TPM_LAUNCH(c, "adj_finish", k_finish_sums, 1, kAT, 0, A.red, nbc, 3, 1.0 / (double)g.n,
@@ -738,7 +736,7 @@ extern "C" int tpm_adjoint_run(tpm_ctx *c, int nsteps, int checkpoint_every, dou
       for (int st = s0; st < s1; ++st) record_step(A, st - s0, Asteps);
       for (int st = s1 - 1; st >= s0; --st) {
         std::vector<double> parts;
-        backward_step(A, st - s0, Asteps[st - s0], nullptr, parts);
+        backward_step(A, st - s0, Asteps[st - s0], parts);
         for (double v : parts) gA += v;
       }
     }

@@ -371,8 +371,6 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->dsc = dalloc<tpm::DevScalars>(c, 1);
     TPM_CUDA_TRY(cudaMallocHost(&c->hsc, sizeof(tpm::DevScalars)));
     std::memset(c->hsc, 0, sizeof(tpm::DevScalars));
-    const long long zero_fields[] = {0};
-    (void)zero_fields;
     for (double *f : {c->RU, c->RU_int, c->RU_new, c->RU_np1, c->Fp, c->U, c->Cface})
       TPM_CUDA_TRY(cudaMemsetAsync(f, 0, sizeof(double) * 3 * n, c->stream));
     for (double *f : {c->Rho, c->Rho_int, c->Rho_new, c->Rho_np1, c->P, c->C, c->Q, c->RHS,
@@ -750,8 +748,6 @@ int tpm_poisson_solve(tpm_ctx *c, const double *C3, double *P, const double *RHS
     c->hsc->mean_rhs = 0;  // poisson::Solve uses RHS as given
     push_scalars(c);
     tpm::launch_center_coeff_from_C(c);
-    const double eps_saved = c->last_err;
-    (void)eps_saved;
     poisson_loop(c, max_iterations, epsilon);
     TPM_CUDA_TRY(cudaMemcpyAsync(P, c->P, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
     pull_scalars(c);

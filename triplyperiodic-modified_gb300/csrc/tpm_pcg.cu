@@ -157,35 +157,29 @@ __global__ void k_pcg_alpha(const double *__restrict__ parts, int n, double *__r
   }
 }
 
-// P += alpha p, r -= alpha q; partials of r.r and max|alpha p|
+// P += alpha p, r -= alpha q; partials of r.r
 __global__ void k_pcg_update(long long n, double *__restrict__ P, double *__restrict__ r,
                              const double *__restrict__ p, const double *__restrict__ q,
                              const double *__restrict__ sc, double *__restrict__ parts_rr,
-                             double *__restrict__ parts_dx, const int *__restrict__ skip) {
+                             const int *__restrict__ skip) {
   if (*skip) return;
   __shared__ double sh[32];
   const double alpha = sc[PC_ALPHA];
-  double rr = 0, mx = 0;
+  double rr = 0;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
        c += (long long)gridDim.x * blockDim.x) {
-    const double dx = alpha * p[c];
-    P[c] += dx;
+    P[c] += alpha * p[c];
     const double rc = r[c] - alpha * q[c];
     r[c] = rc;
     rr += rc * rc;
-    const double a = fabs(dx);
-    mx = a > mx ? a : mx;
   }
   double v = block_sum(rr, sh);
   if (threadIdx.x == 0) parts_rr[blockIdx.x] = v;
-  v = block_max(mx, sh);
-  if (threadIdx.x == 0) parts_dx[blockIdx.x] = v;
 }
 
 // beta = r.z / rho, the stopping test, the iteration count
 __global__ void k_pcg_finish(const double *__restrict__ parts_rz, int n_rz,
-                             const double *__restrict__ parts_rr,
-                             const double *__restrict__ parts_dx, int n_c, double *__restrict__ sc,
+                             const double *__restrict__ parts_rr, int n_c, double *__restrict__ sc,
                              DevScalars *__restrict__ s, double eps,
                              cudaGraphConditionalHandle loop, int loop_max) {
   if (s->skip) {  // converged before this body (set-up or previous iteration)
@@ -196,10 +190,6 @@ __global__ void k_pcg_finish(const double *__restrict__ parts_rz, int n_rz,
   const double rz = sum_parts(parts_rz, n_rz, sh);
   __syncthreads();
   const double rr = sum_parts(parts_rr, n_c, sh);
-  __syncthreads();
-  double v = 0;
-  for (int b = threadIdx.x; b < n_c; b += blockDim.x) v = parts_dx[b] > v ? parts_dx[b] : v;
-  const double mdx = block_max(v, sh);
   if (threadIdx.x == 0) {
     const double rho = sc[PC_RHO];
     sc[PC_BETA] = rho != 0 ? rz / rho : 0.0;
@@ -208,7 +198,6 @@ __global__ void k_pcg_finish(const double *__restrict__ parts_rz, int n_rz,
     const double rel = sc[PC_BB] > 0 ? sqrt(rr) / sqrt(sc[PC_BB]) : 0.0;
     sc[PC_ERR] = rel;
     s->err = rel;
-    (void)mdx;
     s->it += 1;
     s->it_sum += 1;
     const bool more = !(eps > 0 && !(rel > eps));
@@ -252,8 +241,7 @@ static void pcg_iteration(tpm_ctx *c, double eps, const LoopCtl *loop) {
   const double *Cf = scaled ? c->Cs : c->Cface;
   const int nb = cblocks(g);
   const int *skip = &c->dsc->skip;
-  double *pq = c->pcg_parts, *prr = pq + kRedBlocks, *pdx = prr + kRedBlocks,
-         *prz = pdx + 2 * kRedBlocks;
+  double *pq = c->pcg_parts, *prr = pq + kRedBlocks, *prz = prr + 3 * kRedBlocks;
   TPM_LAUNCH(c, "pcg_p", k_pcg_p, nb, kThreadsPcg, 0, g.n, c->pcg_z, c->pcg_p, c->pcg_sc, skip);
   if (scaled)
     TPM_LAUNCH(c, "pcg_matvec", k_pcg_matvec<true>, nb, kThreadsPcg, 0, g, c->pcg_p, Cf, c->pcg_q,
@@ -263,9 +251,9 @@ static void pcg_iteration(tpm_ctx *c, double eps, const LoopCtl *loop) {
                pq, skip);
   TPM_LAUNCH(c, "pcg_alpha", k_pcg_alpha, 1, kThreadsPcg, 0, pq, nb, c->pcg_sc, skip);
   TPM_LAUNCH(c, "pcg_update", k_pcg_update, nb, kThreadsPcg, 0, g.n, c->P, c->pcg_r, c->pcg_p,
-             c->pcg_q, c->pcg_sc, prr, pdx, skip);
+             c->pcg_q, c->pcg_sc, prr, skip);
   const int nrz = fft_precondition(c, c->pcg_r, c->pcg_s, c->pcg_z, prz, skip);
-  TPM_LAUNCH(c, "pcg_finish", k_pcg_finish, 1, kThreadsPcg, 0, prz, nrz, prr, pdx, nb, c->pcg_sc,
+  TPM_LAUNCH(c, "pcg_finish", k_pcg_finish, 1, kThreadsPcg, 0, prz, nrz, prr, nb, c->pcg_sc,
              c->dsc, eps, loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0);
 }
 
