@@ -142,6 +142,7 @@ def time_gpu(p, s, steps, warmup, dist, device):
 
     ctx = capi.Context(p, s.npart)
     ctx.load(s)
+    pens = ctx.autotune()  # FFT pencils per block for this grid (results do not change)
     ctx.initialize()
     ctx.set_graph(True)  # each step one CUDA graph launch (bit-identical to eager steps)
     for _ in range(warmup):
@@ -174,6 +175,7 @@ def time_gpu(p, s, steps, warmup, dist, device):
     ctx.run(2)
     prof = ctx.profile_report()
     ctx.profile(False)
+    ctx.fft_pens = pens
     return ctx, ms, n_it, launches, prof, clk.summary()
 
 
@@ -367,6 +369,7 @@ def gpu_main(args):
         ms = max_over_ranks(ms, dist, "cuda")
         res[name] = path_result(p, s, ms, args.steps, world, n_it, launches, prof, clocks,
                                 name == "mixed", peak)
+        res[name]["fft_pencils_per_block"] = ctx.fft_pens
         ctxs[name] = ctx
     head = "mixed" if "mixed" in res else "fp64"
     accuracy = None
@@ -408,10 +411,12 @@ def gpu_main(args):
         "clocks": r["clocks"],
         "kernels_ms_per_step": r["kernels_ms_per_step"],
         "mparticle_steps_per_s": round(r["mparticle_steps_per_s"], 3),
+        "fft_pencils_per_block": r["fft_pencils_per_block"],
     }
     if "fp64" in res and head != "fp64":
         f = res["fp64"]
         line["fp64"] = {"value": round(f["value"], 3), "ms_per_step": round(f["ms_per_step"], 3),
+                        "fft_pencils_per_block": f["fft_pencils_per_block"],
                         "n_it": f["n_it"], "roofline": f["roofline"],
                         "step_roofline": f["step_roofline"], "clocks": f["clocks"],
                         "kernels_ms_per_step": f["kernels_ms_per_step"]}
