@@ -431,11 +431,6 @@ int pens_for(int n, int elem_bytes = 16) {
   return p;
 }
 
-// largest pencil count whose double2 buffers fit the 64 KB set per kernel
-int pens_cap(int n) {
-  int p = kFftSmemPoints / n;
-  return p < 1 ? 1 : (p > 32 ? 32 : p);
-}
 
 void factorize(int n, FftPlan &pl) {
   pl.n = n;
@@ -596,7 +591,10 @@ void poisson_iteration(tpm_ctx *c, double eps_ctl, const LoopCtl *loop) {
 }
 
 int pens_default(int n, int elem_bytes) { return pens_for(n, elem_bytes); }
-int pens_max(int n, int) { return pens_cap(n); }
+int pens_max(int n, int elem_bytes) {
+  int p = (kFftSmemPoints * 16 / elem_bytes) / n;  // both buffers within the 64 KB set per kernel
+  return p < 1 ? 1 : (p > 32 ? 32 : p);
+}
 
 }  // namespace tpm
 

@@ -197,7 +197,7 @@ void autotune(tpm_ctx *c) {
   TPM_CUDA_TRY(cudaEventCreate(&e1));
   const int reps = 3;
   for (int d = 0; d < 3; ++d) {
-    const int cap = pens_max(n_of[d], 16);
+    const int cap = pens_max(n_of[d], c->p.precision == TPM_PREC_MIXED ? 8 : 16);
     int best = c->pen[d];
     double best_ms = time_iterations(c, e0, e1, reps);
     for (int cand = 1; cand <= cap; cand *= 2) {
