@@ -328,21 +328,46 @@ k_rhs_momentum_tiled(Grid g, const TIn *__restrict__ U, const TIn *__restrict__ 
 // ---------------------------------------------------- Poisson right side
 // grid::Compute_Div_U_new (grid.cpp:832-839), grid::Compute_RHS_Pois
 // (grid.cpp:841-849) and the coefficient set-up of grid::Solve_Poisson /
-// poisson::FFT (grid.cpp:853, poisson.cpp:393-394) in one pass.  The mean of
-// RHS_Pois is reduced per block; it is subtracted where RHS_Pois is read.
+// poisson::FFT (grid.cpp:853, poisson.cpp:393-394).  The mean of RHS_Pois is
+// reduced per block; it is subtracted where RHS_Pois is read.
 struct PoisArgs {
   double kCp;        // k/Cp
   double inv_dtpre;  // 1./(dt*pre)
   int cooling, store_div;
 };
 
-__global__ void k_poisson_rhs(Grid g, const double *__restrict__ Rho_new,
-                              const double *__restrict__ inv_rho, const double *__restrict__ Q,
-                              const double *__restrict__ RUn, const DevScalars *__restrict__ s,
-                              double *__restrict__ RHS, double *__restrict__ divg,
-                              double *__restrict__ Cface, double *__restrict__ cc,
-                              double *__restrict__ partials, double *__restrict__ tke_parts,
-                              PoisArgs a) {
+// FP64 path, split in two passes so that each face's two divisions are done
+// once instead of once per adjacent cell (an FP64 division is ~10 FP64-pipe
+// operations; the kernel is FP64-pipe bound):
+//   k_poisson_faces: Rho_face = I_C2F(Rho_new), C = 1/Rho_face (Cface) and
+//                    U = RU_new/Rho_face on the three lower faces of each cell;
+//   k_poisson_rhs2:  divergence constraint, RHS_Pois and the centre coefficient
+//                    from those face values.
+// Every value is formed by the reference's operations in its order, and each
+// face value is the same whichever adjacent cell asks for it.
+__global__ void k_poisson_faces(Grid g, const double *__restrict__ Rho_new,
+                                const double *__restrict__ RUn, double *__restrict__ Cface,
+                                double *__restrict__ Uf) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    Cell q = cell_of(g, c);
+    Nbr nb = nbr_of(g, q);
+    const double r = Rho_new[c];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double rf = (r + Rho_new[nb.m[d]]) * 0.5;
+      Cface[d * g.n + c] = 1. / rf;
+      Uf[d * g.n + c] = RUn[d * g.n + c] / rf;
+    }
+  }
+}
+
+__global__ void k_poisson_rhs2(Grid g, const double *__restrict__ inv_rho,
+                               const double *__restrict__ Q, const double *__restrict__ Uf,
+                               const double *__restrict__ Cface, const DevScalars *__restrict__ s,
+                               double *__restrict__ RHS, double *__restrict__ divg,
+                               double *__restrict__ cc, double *__restrict__ partials,
+                               double *__restrict__ tke_parts, PoisArgs a) {
   __shared__ double sh[kThreads];
   const double coef = s->coef_div, meanQ = s->mean_Q;
   const double OneThird = 1. / 3.;
@@ -351,7 +376,6 @@ __global__ void k_poisson_rhs(Grid g, const double *__restrict__ Rho_new,
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
     Nbr nb = nbr_of(g, q);
-    // divergence = (k/Cp) Del2(1/Rho_new) - R/(Cp P0_new Vcell) Q
     double ir = inv_rho[c];
     double lap = (inv_rho[nb.p[0]] - 2 * ir + inv_rho[nb.m[0]]) * g.inv_dx2 +
                  (inv_rho[nb.p[1]] - 2 * ir + inv_rho[nb.m[1]]) * g.inv_dy2 +
@@ -359,42 +383,27 @@ __global__ void k_poisson_rhs(Grid g, const double *__restrict__ Rho_new,
     double Qc = a.cooling ? Q[c] - meanQ : Q[c];
     double dv = a.kCp * lap + coef * Qc;
     if (a.store_div) divg[c] = dv;
-    // Rho_face = I_C2F(Rho_new) on the 6 faces of the cell
-    double r = Rho_new[c];
-    double rf_lo[3] = {(r + Rho_new[nb.m[0]]) * 0.5, (r + Rho_new[nb.m[1]]) * 0.5,
-                       (r + Rho_new[nb.m[2]]) * 0.5};
-    double rf_hi[3] = {(Rho_new[nb.p[0]] + r) * 0.5, (Rho_new[nb.p[1]] + r) * 0.5,
-                       (Rho_new[nb.p[2]] + r) * 0.5};
-    // U = RU_new / Rho_face ; RHS = (div_F2C(U) - divergence) / (dt*pre)
     double t[3];
+    double csum = 0;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const double *R = RUn + d * g.n;
-      double u_hi = R[nb.p[d]] / rf_hi[d];
-      double u_lo = R[c] / rf_lo[d];
+      const double u_lo = Uf[d * g.n + c], u_hi = Uf[d * g.n + nb.p[d]];
       t[d] = (u_hi - u_lo) * (d == 0 ? g.inv_dx : d == 1 ? g.inv_dy : g.inv_dz);
       if (tke_parts) usq += u_lo * u_lo;
+      const double half = (Cface[d * g.n + c] + Cface[d * g.n + nb.p[d]]) * 0.5;
+      csum = d == 0 ? half : csum + half;
     }
     double rhs = t[0] + t[1] + t[2];
     rhs -= dv;
     rhs *= a.inv_dtpre;
     RHS[c] = rhs;
     acc += rhs;
-    // C = 1/Rho_face ; center_coeff = -1/I_F2C(C)
-    double c_lo[3], c_hi[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      c_lo[d] = 1. / rf_lo[d];
-      c_hi[d] = 1. / rf_hi[d];
-      Cface[d * g.n + c] = c_lo[d];
-    }
-    double m = OneThird * ((c_lo[0] + c_hi[0]) * 0.5 + (c_lo[1] + c_hi[1]) * 0.5 +
-                           (c_lo[2] + c_hi[2]) * 0.5);
+    double m = OneThird * csum;
     cc[c] = -1. / m;
   }
   double bs = block_sum(acc, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = bs;
-  if (tke_parts) {  // last stage: sum of U^2 for grid::Statistics' TKE2 (grid.cpp:911)
+  if (tke_parts) {
     double bu = block_sum(usq, sh);
     if (threadIdx.x == 0) tke_parts[blockIdx.x] = bu;
   }
@@ -818,10 +827,15 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
     TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_mixed, nb, kThreads, 0, c->g, c->inv_rho, c->Q,
                c->RU_new, c->Cface, c->dsc, c->RHS, c->divg, c->cc,
                c->partials + kPartRhs * kRedBlocks, tke_parts, a);
-  } else
-  TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs, nb, kThreads, 0, c->g, c->Rho_new, c->inv_rho,
-             c->Q, c->RU_new, c->dsc, c->RHS, c->divg, c->Cface, c->cc,
-             c->partials + kPartRhs * kRedBlocks, tke_parts, a);
+  } else {
+    // c->U (the face velocity of RU_int) is dead after the momentum RHS; it
+    // holds RU_new/Rho_face here
+    TPM_LAUNCH(c, "poisson_faces", k_poisson_faces, nb, kThreads, 0, c->g, c->Rho_new, c->RU_new,
+               c->Cface, c->U);
+    TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs2, nb, kThreads, 0, c->g, c->inv_rho, c->Q, c->U,
+               c->Cface, c->dsc, c->RHS, c->divg, c->cc, c->partials + kPartRhs * kRedBlocks,
+               tke_parts, a);
+  }
   TPM_LAUNCH(c, "finish_mean", k_finish_mean, 1, kThreads, 0, c->partials + kPartRhs * kRedBlocks,
              nb, c->g.n,
              &c->dsc->mean_rhs);
