@@ -40,6 +40,7 @@ FALLBACK_HBM_GBS = 6800.0
 KERNEL_BYTES = {
     "rhs_momentum": (21 * 8, 0),
     "poisson_rhs": (11 * 8, 0),
+    "poisson_faces": (10 * 8, 0),
     "fft_x_fwd_resid": (6 * 8 + 8, 0),
     "fft_y": (16, 0),
     "fft_z_solve": (16, 0),
@@ -266,6 +267,8 @@ def whole_job_rate(world, ncell, steps, max_ms):
 
 def kernel_bytes(name, ncell, npart, mixed):
     bc, bp = KERNEL_BYTES.get(name, (0, 0))
+    if not mixed and name == "poisson_rhs":  # FP64: face values precomputed by poisson_faces
+        bc = 10 * 8
     if mixed:  # complex64 spectrum on the mixed path
         bc = {"fft_y": 8, "fft_z_solve": 8, "fft_x_fwd_resid": 6 * 8 + 4,
               "fft_x_inv_update": 4 + 16}.get(name, bc)
