@@ -320,11 +320,12 @@ int tpm_rdf(tpm_ctx *ctx, double r_max, int nbins, unsigned long long *pairs, do
 int tpm_adjoint_run(tpm_ctx *ctx, int nsteps, int checkpoint_every, double w_tke, double w_cvar,
                     double *J, double *dJ_dRU0, double *dJ_dA, double *dJ_dtau);
 
-/* Picks the pencils per block of each FFT pass (x, y, z) of the pressure solve
- * by timing Poisson iterations on the context's grid; results do not depend on
- * the choice (each pencil is transformed independently).  The state is kept:
- * P and the device scalars are restored afterwards.  pens_out (3 ints,
- * optional) receives the choice. */
+/* Picks the pencils per block and the threads per block of each FFT pass
+ * (x, y, z) of the pressure solve by timing Poisson iterations on the
+ * context's grid; results do not depend on the choice (each pencil is
+ * transformed independently).  The state is kept: P and the device scalars
+ * are restored afterwards.  pens_out (6 ints, optional) receives the pencils
+ * of the x, y, z passes, then their threads per block. */
 int tpm_autotune(tpm_ctx *ctx, int *pens_out);
 
 /* ---------------------------------------------------------------- ensembles

@@ -105,7 +105,8 @@ def test_autotune_keeps_results(capi):
     tuned = run(capi, p, s, 2, autotune=True)
     assert_same(state(tuned), state(ref))
     pens = tuned.autotune()
-    assert len(pens) == 3 and all(1 <= q <= 32 for q in pens)
+    assert len(pens) == 6 and all(1 <= q <= 32 for q in pens[:3])
+    assert all(t in (128, 256, 512) for t in pens[3:])
 
 
 def test_batch_matches_boxes_run_alone(capi):

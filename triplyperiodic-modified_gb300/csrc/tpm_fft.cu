@@ -547,36 +547,37 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
                                                 : reinterpret_cast<const T2 *>(c->r2c32);
   const int *skip = &c->dsc->skip;
   const int npx = c->pen[0], npy = c->pen[1], npz = c->pen[2];
+  const int tx = c->fthreads[0], ty = c->fthreads[1], tz = c->fthreads[2];
   const int xblocks = (int)((nrows + npx - 1) / npx);
   {
     size_t smem = 2 * (size_t)npx * c->fx.n * sizeof(T2);
     if (c->p.precision == TPM_PREC_MIXED)
-      TPM_LAUNCH(c, "fft_x_fwd_resid", (k_xfwd_resid<T2, true>), xblocks, kFftThreads, smem, g,
+      TPM_LAUNCH(c, "fft_x_fwd_resid", (k_xfwd_resid<T2, true>), xblocks, tx, smem, g,
                  c->fx, r2c, c->P, c->Cs, c->cc, c->RHS, c->dsc, spec, npx);
     else
-      TPM_LAUNCH(c, "fft_x_fwd_resid", (k_xfwd_resid<T2, false>), xblocks, kFftThreads, smem, g,
+      TPM_LAUNCH(c, "fft_x_fwd_resid", (k_xfwd_resid<T2, false>), xblocks, tx, smem, g,
                  c->fx, r2c, c->P, c->Cface, c->cc, c->RHS, c->dsc, spec, npx);
   }
   {
     int blocks = g.nz * ((g.nxh + npy - 1) / npy);
     size_t smem = 2 * (size_t)npy * c->fy.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, kFftThreads, smem, g, c->fy, spec, npy, -1, skip);
+    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, ty, smem, g, c->fy, spec, npy, -1, skip);
   }
   {
     int blocks = g.ny * ((g.nxh + npz - 1) / npz);
     size_t smem = 2 * (size_t)npz * c->fz.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_z_solve", k_fft_z_solve<T2>, blocks, kFftThreads, smem, g, c->fz, spec,
+    TPM_LAUNCH(c, "fft_z_solve", k_fft_z_solve<T2>, blocks, tz, smem, g, c->fz, spec,
                c->ax, c->ay, c->az, npz, skip);
   }
   {
     int blocks = g.nz * ((g.nxh + npy - 1) / npy);
     size_t smem = 2 * (size_t)npy * c->fy.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, kFftThreads, smem, g, c->fy, spec, npy, +1, skip);
+    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, ty, smem, g, c->fy, spec, npy, +1, skip);
   }
   {
     size_t smem = 2 * (size_t)npx * c->fx.n * sizeof(T2);
     double *parts = c->err_parts;
-    TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, xblocks, kFftThreads, smem, g, c->fx,
+    TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, xblocks, tx, smem, g, c->fx,
                r2c, spec, c->P, parts, npx, skip);
     TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 256, 0, parts, xblocks, c->dsc, eps_ctl,
                loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0);
@@ -778,19 +779,20 @@ void precondition_t(tpm_ctx *c, const double *r, const double *sc, double *z, do
   const T2 *r2c = sizeof(T2) == sizeof(double2) ? reinterpret_cast<const T2 *>(c->r2c64)
                                                 : reinterpret_cast<const T2 *>(c->r2c32);
   const int npx = c->pen[0], npy = c->pen[1], npz = c->pen[2];
+  const int tx = c->fthreads[0], ty = c->fthreads[1], tz = c->fthreads[2];
   const int xblocks = (int)((nrows + npx - 1) / npx);
   const size_t sx = 2 * (size_t)npx * c->fx.n * sizeof(T2);
   const size_t sy = 2 * (size_t)npy * c->fy.n * sizeof(T2);
   const size_t sz = 2 * (size_t)npz * c->fz.n * sizeof(T2);
-  TPM_LAUNCH(c, "pcg_fft_x_fwd", k_pc_xfwd<T2>, xblocks, kFftThreads, sx, g, c->fx, r2c, r, sc,
+  TPM_LAUNCH(c, "pcg_fft_x_fwd", k_pc_xfwd<T2>, xblocks, tx, sx, g, c->fx, r2c, r, sc,
              spec, npx, skip);
-  TPM_LAUNCH(c, "pcg_fft_y", k_fft_y<T2>, g.nz * ((g.nxh + npy - 1) / npy), kFftThreads, sy, g,
+  TPM_LAUNCH(c, "pcg_fft_y", k_fft_y<T2>, g.nz * ((g.nxh + npy - 1) / npy), ty, sy, g,
              c->fy, spec, npy, -1, skip);
   TPM_LAUNCH(c, "pcg_fft_z_solve", k_fft_z_solve<T2>, g.ny * ((g.nxh + npz - 1) / npz),
-             kFftThreads, sz, g, c->fz, spec, c->ax, c->ay, c->az, npz, skip);
-  TPM_LAUNCH(c, "pcg_fft_y", k_fft_y<T2>, g.nz * ((g.nxh + npy - 1) / npy), kFftThreads, sy, g,
+             tz, sz, g, c->fz, spec, c->ax, c->ay, c->az, npz, skip);
+  TPM_LAUNCH(c, "pcg_fft_y", k_fft_y<T2>, g.nz * ((g.nxh + npy - 1) / npy), ty, sy, g,
              c->fy, spec, npy, +1, skip);
-  TPM_LAUNCH(c, "pcg_fft_x_inv", k_pc_xinv<T2>, xblocks, kFftThreads, sx, g, c->fx, r2c, spec, r,
+  TPM_LAUNCH(c, "pcg_fft_x_inv", k_pc_xinv<T2>, xblocks, tx, sx, g, c->fx, r2c, spec, r,
              sc, z, parts, npx, skip);
 }
 

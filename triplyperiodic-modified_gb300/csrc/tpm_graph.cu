@@ -180,7 +180,8 @@ void graphs_clear(std::vector<GraphEntry> &cache) {
   cache.clear();
 }
 
-// Coordinate search over the pencils per block of the x, y and z passes.
+// Coordinate search over the pencils per block, then the threads per block,
+// of the x, y and z passes.
 void autotune(tpm_ctx *c) {
   const Grid &g = c->g;
   const int n_of[3] = {c->fx.n, c->fy.n, c->fz.n};
@@ -212,6 +213,19 @@ void autotune(tpm_ctx *c) {
       c->pen[d] = keep;
     }
     c->pen[d] = best;
+    int best_t = c->fthreads[d];
+    for (int th : {128, 256, 512}) {
+      if (th == best_t) continue;
+      const int keep = c->fthreads[d];
+      c->fthreads[d] = th;
+      const double ms = time_iterations(c, e0, e1, reps);
+      if (ms < 0.97 * best_ms) {
+        best_ms = ms;
+        best_t = th;
+      }
+      c->fthreads[d] = keep;
+    }
+    c->fthreads[d] = best_t;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -269,7 +283,10 @@ int tpm_autotune(tpm_ctx *c, int *pens_out) {
     tpm::autotune(c);
     tpm::graphs_clear(c->graphs);  // launch shapes changed
     if (pens_out)
-      for (int d = 0; d < 3; ++d) pens_out[d] = c->pen[d];
+      for (int d = 0; d < 3; ++d) {
+        pens_out[d] = c->pen[d];
+        pens_out[3 + d] = c->fthreads[d];
+      }
     return TPM_OK;
   });
 }
@@ -334,12 +351,15 @@ int tpm_batch_autotune(tpm_batch *b) {
       std::vector<int> key = {c->g.nx, c->g.ny, c->g.nz, c->p.precision};
       auto it = done.find(key);
       if (it != done.end()) {
-        for (int d = 0; d < 3; ++d) c->pen[d] = it->second[d];
+        for (int d = 0; d < 3; ++d) {
+          c->pen[d] = it->second[d];
+          c->fthreads[d] = it->second[3 + d];
+        }
         continue;
       }
-      int pens[3];
+      int pens[6];
       if (int rc = box_rc(b, (int)i, tpm_autotune(c, pens))) return rc;
-      done[key] = {pens[0], pens[1], pens[2]};
+      done[key] = {pens[0], pens[1], pens[2], pens[3], pens[4], pens[5]};
     }
     tpm::graphs_clear(b->graphs);
     return TPM_OK;

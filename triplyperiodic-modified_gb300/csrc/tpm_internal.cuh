@@ -156,6 +156,7 @@ struct tpm_ctx {
   const float2 *r2c32 = nullptr;
   double *err_parts = nullptr;  // one max|dp| per x-pass block (sized for one row per block)
   int pen[3] = {1, 1, 1};       // FFT pencils per block of the x, y, z passes (autotuned)
+  int fthreads[3] = {256, 256, 256};  // threads per block of the x, y, z passes (autotuned)
   bool device_loop = false;     // Poisson stopping test on the device (no host read)
   void *fft_mem = nullptr;
 

@@ -165,7 +165,8 @@ class Context:
         return J.value, g, gA.value, gt.value
 
     def autotune(self):
-        pens = (_i * 3)()
+        """FFT tiles: [pencils x, y, z, threads x, y, z]."""
+        pens = (_i * 6)()
         self._check(self.L.tpm_autotune(self.h, pens))
         return list(pens)
 
