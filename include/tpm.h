@@ -163,6 +163,20 @@ int tpm_set_particle_tau(tpm_ctx *ctx, const double *tau);
 int tpm_set_scalars(tpm_ctx *ctx, double P0, double T_cur, int64_t num_timestep);
 int tpm_get_scalars(tpm_ctx *ctx, tpm_scalars *out);
 
+/* The step-boundary state in one call each way (one stream synchronisation
+ * for the copies): tpm_load_state uploads RU, RU_INT, RHO, P, the base
+ * particle set (part[0..6] = x, y, z, u, v, w, T) and its heat rates, sets
+ * the scalars and resumes (what tpm_upload_field / tpm_upload_particles /
+ * tpm_upload_particle_rhs_t / tpm_set_scalars / tpm_resume do one by one);
+ * tpm_save_state downloads the same arrays and the scalars.  The heat deposit
+ * Q is rebuilt from the heat rates, and particle ids do not change, so neither
+ * is part of it.  A run saved and loaded at every step continues bit for bit. */
+int tpm_load_state(tpm_ctx *ctx, const double *RU, const double *RU_int, const double *Rho,
+                   const double *P, const double *const *part, const double *rhs_t, double P0,
+                   double T_cur, int64_t num_timestep);
+int tpm_save_state(tpm_ctx *ctx, double *RU, double *RU_int, double *Rho, double *P,
+                   double *const *part, double *rhs_t, tpm_scalars *scalars);
+
 /* Restart files in the reference's format, the set its Initial=1 branch reads
  * (grid.cpp:221-238, particle.cpp:939-989): Restart_RU.bin, Restart_Rho.bin,
  * Restart_P.bin (raw FP64, [Nz][Ny][Nx], RU as x,y,z blocks),

@@ -623,6 +623,75 @@ int tpm_get_scalars(tpm_ctx *c, tpm_scalars *out) {
   });
 }
 
+int tpm_load_state(tpm_ctx *c, const double *RU, const double *RU_int, const double *Rho,
+                   const double *P, const double *const *part, const double *rhs_t, double P0,
+                   double T_cur, int64_t num_timestep) {
+  return guarded(c, [&]() -> int {
+    if (!RU || !RU_int || !Rho || !P || (c->np > 0 && (!part || !rhs_t)))
+      return fail(c, TPM_ERR_ARG, "null buffer");
+    const long long n = c->g.n;
+    auto up = [&](double *d, const double *h, size_t m) {
+      TPM_CUDA_TRY(cudaMemcpyAsync(d, h, sizeof(double) * m, cudaMemcpyHostToDevice, c->stream));
+    };
+    up(c->RU, RU, 3 * n);
+    up(c->RU_int, RU_int, 3 * n);
+    up(c->Rho, Rho, n);
+    up(c->P, P, n);
+    if (c->np > 0) {
+      for (int q = 0; q < 7; ++q) {
+        if (!part[q]) return fail(c, TPM_ERR_ARG, "null particle array");
+        up(c->pq[0][q], part[q], c->np);
+      }
+      up(c->rhs_t, rhs_t, c->np);
+    }
+    pull_scalars(c);  // synchronises the copies above
+    c->hsc->P0 = P0;
+    push_scalars(c);
+    c->T_cur = T_cur;
+    c->num_timestep = num_timestep;
+    tpm::resume_device(c);
+    return TPM_OK;
+  });
+}
+
+int tpm_save_state(tpm_ctx *c, double *RU, double *RU_int, double *Rho, double *P,
+                   double *const *part, double *rhs_t, tpm_scalars *sc) {
+  return guarded(c, [&]() -> int {
+    if (!RU || !RU_int || !Rho || !P || (c->np > 0 && (!part || !rhs_t)))
+      return fail(c, TPM_ERR_ARG, "null buffer");
+    if (!c->np1_is_base) return fail(c, TPM_ERR_STATE, "the state is saved at a step boundary");
+    const long long n = c->g.n;
+    auto down = [&](double *h, const double *d, size_t m) {
+      TPM_CUDA_TRY(cudaMemcpyAsync(h, d, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
+    };
+    down(RU, c->RU, 3 * n);
+    down(RU_int, c->RU_int, 3 * n);
+    down(Rho, c->Rho, n);
+    down(P, c->P, n);
+    if (c->np > 0) {
+      for (int q = 0; q < 7; ++q) {
+        if (!part[q]) return fail(c, TPM_ERR_ARG, "null particle array");
+        down(part[q], c->pq[0][q], c->np);
+      }
+      down(rhs_t, c->rhs_t, c->np);
+    }
+    pull_scalars(c);  // synchronises the copies above
+    if (sc) {
+      sc->P0 = c->hsc->P0;
+      sc->P0_int = c->hsc->P0_int;
+      sc->P0_new = c->hsc->P0_new;
+      sc->P0_np1 = c->hsc->P0;
+      sc->T_cur = c->T_cur;
+      sc->num_timestep = c->num_timestep;
+      sc->last_poisson_iterations = c->hsc->it;
+      sc->total_poisson_iterations = c->hsc->it_sum;
+      sc->last_poisson_error = c->p.epsilon > 0 ? c->last_err : c->hsc->err;
+      sc->max_abs_div = c->p.precision == TPM_PREC_MIXED ? c->hsc->max_div : -1.0;
+    }
+    return TPM_OK;
+  });
+}
+
 int tpm_initialize(tpm_ctx *c) {
   return guarded(c, [&]() -> int {
     const long long n = c->g.n;

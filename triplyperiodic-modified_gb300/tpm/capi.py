@@ -45,6 +45,8 @@ SIGNATURES = {
     "tpm_upload_particle_rhs_t": (_i, [_vp, _dp]),
     "tpm_set_particle_tau": (_i, [_vp, _dp]),
     "tpm_resume": (_i, [_vp]),
+    "tpm_load_state": (_i, [_vp, _dp, _dp, _dp, _dp, ctypes.POINTER(_dp), _dp, _d, _d, _i64]),
+    "tpm_save_state": (_i, [_vp, _dp, _dp, _dp, _dp, ctypes.POINTER(_dp), _dp, _vp]),
     "tpm_statistics": (_i, [_vp, _vp]),
     "tpm_spectrum_shells": (_i, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
     "tpm_spectrum": (_i, [_vp, ctypes.POINTER(ctypes.c_double), _i]),
@@ -260,27 +262,41 @@ class Context:
         return self.L.tpm_stream(self.h)
 
     # ---- exact step-boundary state (what tpm_resume needs) ----
-    STATE_FIELDS = ("RU", "RU_INT", "RHO", "P", "Q")
+    STATE_FIELDS = ("RU", "RU_INT", "RHO", "P")
 
     def download_state(self, out=None):
-        """Step-boundary state; with `out` (a previous result, e.g. in pinned
-        host memory) the arrays are filled in place."""
+        """Step-boundary state (tpm_save_state); with `out` (a previous result,
+        e.g. in pinned host memory) the arrays are filled in place."""
         o = out or {}
-        st = {f: self.download_field(f, o.get(f)) for f in self.STATE_FIELDS}
-        st["part"] = self.download_particles("base", o.get("part")) if self.npart else None
-        st["RHS_T"] = self.download_rhs_t(o.get("RHS_T")) if self.npart else None
-        st["scalars"] = self.scalars()
+        st = {}
+        for f in self.STATE_FIELDS:
+            a = o.get(f)
+            st[f] = a if a is not None else np.empty(self._shape(f))
+        part = o.get("part") or {q: np.empty(self.npart) for q in inputs.PQ}
+        rhs_t = o.get("RHS_T")
+        rhs_t = rhs_t if rhs_t is not None else np.empty(max(self.npart, 1))
+        ptrs = (_dp * 7)(*[_dptr(part[q]) for q in inputs.PQ]) if self.npart else None
+        sc = TpmScalars()
+        self._check(self.L.tpm_save_state(self.h, *[_dptr(st[f]) for f in self.STATE_FIELDS],
+                                          ptrs, _dptr(rhs_t), ctypes.byref(sc)))
+        st["part"] = part if self.npart else None
+        st["RHS_T"] = rhs_t if self.npart else None
+        st["scalars"] = sc.as_dict()
         return st
 
     def upload_state(self, st):
-        for f in self.STATE_FIELDS:
-            self.upload_field(f, st[f])
+        """Loads a state from download_state and resumes (tpm_load_state)."""
+        arrs = [np.ascontiguousarray(st[f], dtype=np.float64) for f in self.STATE_FIELDS]
         if self.npart:
-            self.upload_particles(st["part"], "base")
-            self.upload_rhs_t(st["RHS_T"])
+            part = [np.ascontiguousarray(st["part"][q], dtype=np.float64) for q in inputs.PQ]
+            ptrs = (_dp * 7)(*[_dptr(a) for a in part])
+            rhs_t = np.ascontiguousarray(st["RHS_T"], dtype=np.float64)
+        else:
+            ptrs, rhs_t = None, np.zeros(1)
         sc = st["scalars"]
-        self.set_scalars(sc["P0"], sc["T_cur"], sc["num_timestep"])
-        self.resume()
+        self._check(self.L.tpm_load_state(self.h, *[_dptr(a) for a in arrs], ptrs, _dptr(rhs_t),
+                                          float(sc["P0"]), float(sc["T_cur"]),
+                                          int(sc["num_timestep"])))
 
     def set_tau(self, tau):
         if tau is None:
