@@ -436,7 +436,7 @@ def gpu_main(args):
         cmp[name] = {"own_iteration_ms": round(per_it, 4),
                      "cufft_solve_ms": round(cufft_solve_ms((p64.Nz, p64.Ny, p64.Nx),
                                                             (p64.Lx, p64.Ly, p64.Lz), dtype), 4),
-                     "note": "own = FP64 residual + R2C/C2R pencil FFTs + divide + P update "
+                     "note": "own = residual + R2C/C2R pencil FFTs + divide + P update "
                              "(5 kernels); cuFFT = rfftn, divide, irfftn only"}
     line["fft_vs_cufft"] = cmp
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

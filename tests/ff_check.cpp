@@ -1,0 +1,92 @@
+// Host check of the float-float helpers in csrc/tpm_ff.cuh (the mixed path's
+// Poisson refinement): compiled with g++ against a stand-in cuda_runtime.h
+// that maps the bit-cast intrinsics to memcpy, with contraction off so that
+// the error-free transformations see the same IEEE float rounding as on the
+// device.  Prints "ok" or the first failure.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <random>
+
+#include "tpm_ff.cuh"
+
+using namespace tpm;
+
+static int fails = 0;
+#define CHECK(c, ...)                         \
+  do {                                        \
+    if (!(c) && fails++ < 10) {               \
+      std::printf("FAIL %s: ", #c);           \
+      std::printf(__VA_ARGS__);               \
+      std::printf("\n");                      \
+    }                                         \
+  } while (0)
+
+static double pair_value(float2 p) { return (double)p.x + (double)p.y; }
+
+int main() {
+  std::mt19937_64 rng(12345);
+  std::uniform_real_distribution<double> mant(1.0, 2.0), unit(-1.0, 1.0);
+  std::uniform_int_distribution<int> ex(-74, 127);
+  // split: |x - (hi + lo)| <= 2^-48 |x|, hi is x truncated to 24 bits
+  for (int n = 0; n < 2000000; ++n) {
+    double x = std::ldexp(mant(rng), ex(rng)) * (rng() & 1 ? -1.0 : 1.0);
+    float2 p = ff_from_double(x);
+    double err = std::fabs(x - pair_value(p));
+    CHECK(err <= std::ldexp(std::fabs(x), -48), "x=%.17g err=%.3g", x, err);
+    uint64_t b;
+    std::memcpy(&b, &x, 8);
+    b &= ~((uint64_t(1) << 29) - 1);
+    double xt;
+    std::memcpy(&xt, &b, 8);
+    CHECK((double)p.x == xt, "x=%.17g hi=%.9g", x, (double)p.x);
+  }
+  // special values
+  float2 z = ff_from_double(0.0), nz = ff_from_double(-0.0);
+  CHECK(z.x == 0.f && z.y == 0.f && !std::signbit(z.x), "zero");
+  CHECK(nz.x == 0.f && std::signbit(nz.x), "negative zero");
+  float2 t = ff_from_double(-1e-30);  // below 2^-74: lo dropped
+  CHECK(std::fabs(-1e-30 - pair_value(t)) <= std::ldexp(1e-30, -23), "tiny %.9g", (double)t.x);
+  float2 u = ff_from_double(1e-40);  // below 2^-126: flushed
+  CHECK(u.x == 0.f && u.y == 0.f, "underflow");
+  CHECK(std::isinf(ff_from_double(1e39).x) && ff_from_double(1e39).x > 0, "overflow");
+  CHECK(std::isinf(ff_from_double(-INFINITY).x) && ff_from_double(-INFINITY).x < 0, "-inf");
+  CHECK(std::isnan(ff_from_double(NAN).x), "nan");
+  // float -> double, exact
+  std::uniform_int_distribution<uint32_t> bits;
+  for (int n = 0; n < 2000000; ++n) {
+    uint32_t w = bits(rng);
+    float f;
+    std::memcpy(&f, &w, 4);
+    double d = ff_f2d(f);
+    const uint32_t ef = (w >> 23) & 0xffu;
+    if (ef == 0u)
+      CHECK(d == 0.0 && std::signbit(d) == std::signbit(f), "subnormal/zero %08x", w);
+    else if (std::isnan(f))
+      CHECK(std::isnan(d), "nan %08x", w);
+    else
+      CHECK(d == (double)f, "f2d %08x", w);
+  }
+  // TwoSum is exact; the product stays within 2^-44, the sloppy add within 2^-46
+  for (int n = 0; n < 2000000; ++n) {
+    float a = (float)(unit(rng) * std::ldexp(1.0, ex(rng) / 8));
+    float c = (float)(unit(rng) * std::ldexp(1.0, ex(rng) / 8));
+    float2 s = ff_two_sum(a, c);
+    CHECK((long double)s.x + s.y == (long double)a + c, "two_sum %.9g %.9g", a, c);
+    float2 pa = ff_from_double(unit(rng) * 3.0), pb = ff_from_double(unit(rng) * 1e3);
+    long double va = (long double)pa.x + pa.y, vb = (long double)pb.x + pb.y;
+    float2 m = ff_mul(pa, pb);
+    long double em = std::fabs((long double)m.x + m.y - va * vb);
+    CHECK(em <= std::ldexp((long double)std::fabs(va * vb), -44), "mul err %.3Lg", em);
+    float2 ad = ff_add(pa, pb);
+    long double ea = std::fabs((long double)ad.x + ad.y - (va + vb));
+    CHECK(ea <= std::ldexp(std::fabs(va) + std::fabs(vb), -46), "add err %.3Lg", ea);
+  }
+  if (fails) {
+    std::printf("%d failures\n", fails);
+    return 1;
+  }
+  std::printf("ok\n");
+  return 0;
+}

@@ -184,11 +184,13 @@ void poisson_loop(tpm_ctx *c, int max_it, double eps) {
     if (eps > 0) c->last_err = error;
     return;
   }
+  const bool refine = c->p.precision == TPM_PREC_MIXED;
   if (c->device_loop) {
     c->last_it = -1;  // on the device (DevScalars::it)
     if (max_it <= 0) return;
     tpm::LoopCtl loop = new_loop(c, max_it);
     capture_while(c, loop, [&] { tpm::poisson_iteration(c, eps_ctl, &loop); });
+    if (refine) tpm::refine_finish(c);
     return;
   }
   int it = 0;
@@ -198,6 +200,7 @@ void poisson_loop(tpm_ctx *c, int max_it, double eps) {
     it++;
     if (eps > 0) error = read_err(c);
   }
+  if (refine && it > 1) tpm::refine_finish(c);
   c->last_it = it;
   c->total_it += it;
   if (eps > 0) c->last_err = error;
@@ -366,6 +369,14 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
         TPM_CUDA_TRY(cudaMemsetAsync(f, 0, sizeof(float) * 3 * n, c->stream));
       c->Cs = dalloc<double>(c, 3 * n);
       TPM_CUDA_TRY(cudaMemsetAsync(c->Cs, 0, sizeof(double) * 3 * n, c->stream));
+      c->Cs2 = dalloc<float2>(c, 3 * n);
+      c->R0 = dalloc<float2>(c, n);
+      c->cc32 = dalloc<float>(c, n);
+      c->dP = dalloc<double>(c, n);
+      TPM_CUDA_TRY(cudaMemsetAsync(c->Cs2, 0, sizeof(float2) * 3 * n, c->stream));
+      TPM_CUDA_TRY(cudaMemsetAsync(c->R0, 0, sizeof(float2) * n, c->stream));
+      TPM_CUDA_TRY(cudaMemsetAsync(c->dP, 0, sizeof(double) * n, c->stream));
+      TPM_CUDA_TRY(cudaMemsetAsync(c->cc32, 0, sizeof(float) * n, c->stream));
     }
     c->partials = dalloc<double>(c, (size_t)tpm::kPartRegions * tpm::kRedBlocks);
     c->dsc = dalloc<tpm::DevScalars>(c, 1);

@@ -1,0 +1,91 @@
+// Float-float ("double-float") arithmetic for the mixed path's Poisson
+// refinement.  A value is the unevaluated sum hi + lo of two floats (x, y of a
+// float2).  GB300 issues FP64 at 1/58 of its FP32 rate, so the refinement's
+// residual is summed here, on the FP32 pipe, at about 2^-46 relative
+// precision instead of FP64's 2^-53.
+//
+// Methods: Knuth's TwoSum (TAOCP vol. 2, 4.2.2, theorem B), Dekker's
+// FastTwoSum and the FMA form of his exact product (T. J. Dekker, "A
+// floating-point technique for extending the available precision", Numer.
+// Math. 18, 1971).  These error-free transformations need every add rounded
+// to nearest and kept in program order: the kernels that use them are built
+// without fast-math and with --fmad=false (no contraction besides the
+// explicit fmaf below).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace tpm {
+
+// s + e == a + b exactly (TwoSum, 6 adds)
+__device__ __forceinline__ float2 ff_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  const float e = (a - (s - bb)) + (b - bb);
+  return make_float2(s, e);
+}
+
+// s + e == a + b exactly when |a| >= |b| or a == 0 (FastTwoSum, 3 adds)
+__device__ __forceinline__ float2 ff_fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return make_float2(s, b - (s - a));
+}
+
+// a + b for a pair a and a pair b that need not be normalised; the error is
+// within 2^-46 (|a| + |b|), which is what a residual summed from terms of
+// both signs needs (the "sloppy" add: one TwoSum on the high parts)
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+  const float2 s = ff_two_sum(a.x, b.x);
+  return ff_fast_two_sum(s.x, s.y + (a.y + b.y));
+}
+
+// a * b, unnormalised: a.x b.x exactly (FMA) plus the cross terms, within
+// 2^-44 |a b| for pairs from ff_from_double (|lo| < 2^-23 |hi|: the dropped
+// a.y b.y and the roundings of the cross terms)
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+  const float p = a.x * b.x;
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  return make_float2(p, e);
+}
+
+// A double as a pair with |x - (hi + lo)| <= 2^-48 |x| for 2^-74 <= |x| <
+// 2^128, by integer operations on its bits only (conversion instructions
+// issue on the FP64 pipe, and a branch around them is if-converted into
+// evaluating them for every value): hi is x truncated to 24 significant
+// bits, lo the remaining 29 bits rounded to 24.  Below 2^-74 lo is dropped
+// (an error under 2^-97), below 2^-126 x flushes to a signed zero; from 2^128
+// on hi is an infinity of x's sign (nan for nan) and lo zero.
+__device__ __forceinline__ float2 ff_from_double(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int hw = (unsigned int)(b >> 32), lw = (unsigned int)b;
+  const int e = (int)((hw >> 20) & 0x7ffu);  // biased binary exponent
+  const unsigned int sgn = hw & 0x80000000u;
+  // float exponent e - 1023 + 127, the 20 high and 3 next significand bits
+  const unsigned int mant = ((hw & 0xfffffu) << 3) | (lw >> 29);
+  unsigned int hb = sgn | ((unsigned int)(e - 896) << 23) | mant;
+  hb = e < 897 ? sgn : hb;
+  hb = e > 1150 ? (sgn | 0x7f800000u | ((e == 2047 && ((hw & 0xfffffu) | lw)) ? 0x400000u : 0u))
+                : hb;
+  // the low 29 significand bits are worth t * 2^(e - 1075), and 2^(e - 1075)
+  // is the float with biased exponent e - 948 (>= 1 in range)
+  const float t = __uint2float_rn(lw & 0x1fffffffu);
+  const bool lo_ok = e >= 949 && e <= 1150;
+  const float scale = __uint_as_float(lo_ok ? ((unsigned int)(e - 948) << 23) : 0u);
+  const float lo = t * scale;
+  return make_float2(__uint_as_float(hb), __uint_as_float(__float_as_uint(lo) | sgn));
+}
+
+// A float as a double, exactly, by integer operations only; subnormal floats
+// (below 2^-126) flush to a signed zero.
+__device__ __forceinline__ double ff_f2d(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int ef = (u >> 23) & 0xffu;
+  const unsigned long long sgn = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned long long ed = ef == 0xffu ? 0x7ffull : (unsigned long long)(ef + 896u);
+  const unsigned long long bits = sgn | (ed << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)(ef == 0u ? sgn : bits));
+}
+
+}  // namespace tpm

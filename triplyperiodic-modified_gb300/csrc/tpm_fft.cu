@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "tpm_internal.cuh"
+#include "tpm_ff.cuh"
 #include "tpm_reduce.cuh"
 
 namespace tpm {
@@ -191,10 +192,7 @@ __device__ __forceinline__ void r2c_store(const Grid &g, const T2 *z, int npen, 
 
 // ------------------------------------------------- 1. residual + R2C along x
 // poisson.cpp:399-404 (residual) and the first third of fft_3d (:431).
-// kScaled (mixed path): Cf holds C*(1/d^2) per component, and the residual is
-// sum_d Cs_hi (P_hi - P) - Cs_lo (P - P_lo) - RHS, times cc: the same FP64
-// residual with a third fewer FP64 operations.
-template <typename T2, bool kScaled = false>
+template <typename T2>
 __global__ void k_xfwd_resid(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
                              const double *__restrict__ P, const double *__restrict__ Cf,
                              const double *__restrict__ cc, const double *__restrict__ RHS,
@@ -222,27 +220,14 @@ __global__ void k_xfwd_resid(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
       const int kp = wrap_p(k, g.nz), km = wrap_m(k, g.nz);
       const long long cxp = at(g, ip, j, k), cyp = at(g, i, jp, k), czp = at(g, i, j, kp);
       const double pc = P[c];
-      double rn;
-      if (kScaled) {
-        // one FMA chain (the mixed path has no bitwise-parity constraint, and
-        // its FP64 residual is what bounds this kernel: 16 FP64-pipe
-        // operations per cell instead of 21)
-        double acc = -(Cx_[c] * (pc - P[at(g, im, j, k)]));
-        acc = fma(Cx_[cxp], P[cxp] - pc, acc);
-        acc = fma(-Cy_[c], pc - P[at(g, i, jm, k)], acc);
-        acc = fma(Cy_[cyp], P[cyp] - pc, acc);
-        acc = fma(-Cz_[c], pc - P[at(g, i, j, km)], acc);
-        rn = fma(Cz_[czp], P[czp] - pc, acc);
-      } else {
-        // dummy = grad_C2F(P) * C at the low and high faces
-        double gx_hi = (P[cxp] - pc) * g.inv_dx * Cx_[cxp];
-        double gx_lo = (pc - P[at(g, im, j, k)]) * g.inv_dx * Cx_[c];
-        double gy_hi = (P[cyp] - pc) * g.inv_dy * Cy_[cyp];
-        double gy_lo = (pc - P[at(g, i, jm, k)]) * g.inv_dy * Cy_[c];
-        double gz_hi = (P[czp] - pc) * g.inv_dz * Cz_[czp];
-        double gz_lo = (pc - P[at(g, i, j, km)]) * g.inv_dz * Cz_[c];
-        rn = (gx_hi - gx_lo) * g.inv_dx + (gy_hi - gy_lo) * g.inv_dy + (gz_hi - gz_lo) * g.inv_dz;
-      }
+      // dummy = grad_C2F(P) * C at the low and high faces
+      double gx_hi = (P[cxp] - pc) * g.inv_dx * Cx_[cxp];
+      double gx_lo = (pc - P[at(g, im, j, k)]) * g.inv_dx * Cx_[c];
+      double gy_hi = (P[cyp] - pc) * g.inv_dy * Cy_[cyp];
+      double gy_lo = (pc - P[at(g, i, jm, k)]) * g.inv_dy * Cy_[c];
+      double gz_hi = (P[czp] - pc) * g.inv_dz * Cz_[czp];
+      double gz_lo = (pc - P[at(g, i, j, km)]) * g.inv_dz * Cz_[c];
+      double rn = (gx_hi - gx_lo) * g.inv_dx + (gy_hi - gy_lo) * g.inv_dy + (gz_hi - gz_lo) * g.inv_dz;
       rn -= (RHS[c] - mean);
       rn *= cc[c];
       r = rn;
@@ -252,6 +237,69 @@ __global__ void k_xfwd_resid(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   }
   __syncthreads();
   T2 *z = smem_fft(a, b, npen, pl, -1);
+  r2c_store(g, z, npen, M, row0, nrows, r2c_tw, spec);
+}
+
+// Mixed path: the x-pass of one step of iterative refinement.  Iterations 0
+// and 1 of a solve form the residual of P itself, div(C grad P) - (RHS -
+// mean); iteration 0 then corrects P directly, iteration 1 stores its
+// residual as R0 and starts a correction sum dP, and iteration k >= 2 forms
+// R0 + div(C grad dP) (correction form; P += dP once when the loop ends,
+// k_refine_finish).  The rounding noise of a residual scales with the field
+// whose differences it takes: in correction form that is dP, about 1e-6 of P
+// after the first correction, so the iteration converges far below the
+// noise of an FP64 residual of P; R0's own rounding, made once, only shifts
+// the fixed point (by about 1e-14 of P).  The face differences X_nb - X are
+// FP64 subtractions (exact to rounding for the close values of neighbouring
+// cells, and the kernel's only FP64 operations: six or seven per cell
+// against the seventeen of an FP64 residual); each is split into a
+// float-float pair (tpm_ff.cuh), multiplied by Cs2 = C/d^2 and summed as
+// pairs on the FP32 pipe.  The residual times cc is rounded to FP32 for the
+// correction's FFT solve.
+__global__ void k_xfwd_resid_refine(Grid g, FftPlan pl, const float2 *__restrict__ r2c_tw,
+                                    const double *__restrict__ P, const double *__restrict__ dP,
+                                    const float2 *__restrict__ Cs2, const float *__restrict__ cc32,
+                                    const double *__restrict__ RHS,
+                                    const DevScalars *__restrict__ s, float2 *__restrict__ R0,
+                                    float2 *__restrict__ spec, int npen) {
+  if (s->skip) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *a = reinterpret_cast<float2 *>(smem_raw);
+  const int M = pl.n;  // nx/2
+  float2 *b = a + M * npen;
+  const long long nrows = (long long)g.ny * g.nz;
+  const long long row0 = (long long)blockIdx.x * npen;
+  const int it = s->it;
+  const bool direct = it <= 1;
+  const double mean = s->mean_rhs;
+  const double *X = direct ? P : dP;
+  const float2 *Cx_ = Cs2, *Cy_ = Cs2 + g.n, *Cz_ = Cs2 + 2 * g.n;
+  for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
+    const int q = idx / g.nx, i = idx % g.nx;
+    const long long row = row0 + q;
+    float r = 0.f;
+    if (row < nrows) {
+      const int j = (int)(row % g.ny), k = (int)(row / g.ny);
+      const long long c = at(g, i, j, k);
+      const long long cxm = at(g, wrap_m(i, g.nx), j, k), cxp = at(g, wrap_p(i, g.nx), j, k);
+      const long long cym = at(g, i, wrap_m(j, g.ny), k), cyp = at(g, i, wrap_p(j, g.ny), k);
+      const long long czm = at(g, i, j, wrap_m(k, g.nz)), czp = at(g, i, j, wrap_p(k, g.nz));
+      float2 acc = direct ? ff_from_double(mean - RHS[c]) : R0[c];
+      const double xc = X[c];
+      acc = ff_add(acc, ff_mul(Cx_[c], ff_from_double(X[cxm] - xc)));
+      acc = ff_add(acc, ff_mul(Cx_[cxp], ff_from_double(X[cxp] - xc)));
+      acc = ff_add(acc, ff_mul(Cy_[c], ff_from_double(X[cym] - xc)));
+      acc = ff_add(acc, ff_mul(Cy_[cyp], ff_from_double(X[cyp] - xc)));
+      acc = ff_add(acc, ff_mul(Cz_[c], ff_from_double(X[czm] - xc)));
+      acc = ff_add(acc, ff_mul(Cz_[czp], ff_from_double(X[czp] - xc)));
+      if (it == 1) R0[c] = acc;
+      r = (acc.x + acc.y) * cc32[c];
+    }
+    float *slot = reinterpret_cast<float *>(&a[(i >> 1) * npen + q]);
+    slot[i & 1] = r;
+  }
+  __syncthreads();
+  float2 *z = smem_fft(a, b, npen, pl, -1);
   r2c_store(g, z, npen, M, row0, nrows, r2c_tw, spec);
 }
 
@@ -331,7 +379,8 @@ template <typename T2>
 __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
                               const T2 *__restrict__ spec, double *__restrict__ P,
                               double *__restrict__ partials, int npen,
-                              const int *__restrict__ skip) {
+                              const int *__restrict__ skip, double *__restrict__ dP,
+                              const int *__restrict__ it) {
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double sh[32];
@@ -365,8 +414,13 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   const double inv_tot = 1.0 / (double)(g.nx * g.ny * g.nz);
   double mx = 0;
   if (sizeof(T) == sizeof(float)) {
-    // mixed path: max|x| in FP32 (exact: the maximum picks one x, scaled once
-    // below) and P += -x/N^3 as one FMA, two FP64-pipe operations per cell
+    // mixed path: the correction dp = -x/N^3, formed in FP32 and converted
+    // exactly, goes to P at iteration 0, starts the solve's FP64 correction
+    // sum dP at iteration 1 and joins it after (one FP64 operation per cell;
+    // P += dP in k_refine_finish).  max|x| in FP32 (exact: the maximum picks
+    // one x, scaled once below).
+    const int itv = *it;
+    const float inv_tot_f = 1.0f / (float)((long long)g.nx * g.ny * g.nz);
     float mxf = 0.f;
     for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
       const int q = idx / g.nx, i = idx % g.nx;
@@ -375,7 +429,11 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
       const T *zz = reinterpret_cast<const T *>(&z[(i >> 1) * npen + q]);
       const float xf = (float)zz[i & 1];
       const long long c = row * g.nx + i;
-      P[c] = fma(-(double)xf, inv_tot, P[c]);
+      const double dp = ff_f2d(-(xf * inv_tot_f));
+      if (itv == 0)
+        P[c] += dp;
+      else
+        dP[c] = itv == 1 ? dp : dP[c] + dp;
       const float ax = fabsf(xf);
       mxf = ax > mxf ? ax : mxf;
     }
@@ -421,6 +479,16 @@ __global__ void k_finish_max(const double *__restrict__ partials, int nparts, De
     else if (!more)
       s->skip = 1;
   }
+}
+
+// End of a mixed refinement loop that reached the correction form (it >= 2
+// iterations ran): P += dP
+__global__ void k_refine_finish(Grid g, const double *__restrict__ dP,
+                                const DevScalars *__restrict__ s, double *__restrict__ P) {
+  if (s->it <= 1) return;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x)
+    P[c] += dP[c];
 }
 
 // pencils per block: two ping-pong buffers of 32 KB each
@@ -526,7 +594,7 @@ void fft_plans_create(tpm_ctx *c) {
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_fft_y<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_fft_z_solve<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_xinv_update<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
-  TPM_CUDA_TRY(cudaFuncSetAttribute(k_xfwd_resid<float2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  TPM_CUDA_TRY(cudaFuncSetAttribute(k_xfwd_resid_refine, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_fft_y<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_fft_z_solve<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_xinv_update<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
@@ -534,10 +602,12 @@ void fft_plans_create(tpm_ctx *c) {
 
 // One Richardson iteration of poisson::FFT (poisson.cpp:397-409).  Inputs:
 // P, c->Cface, c->cc, c->RHS and dsc->mean_rhs.  Output: P updated and
-// dsc->err = max|dp|.  The residual and the update are FP64 on both paths;
-// T2 is the type of the constant-coefficient FFT solve (double2 on the FP64
-// path; float2 on the mixed path, where each iteration is one step of
-// iterative refinement: FP64 residual, FP32 correction, FP64 update).
+// dsc->err = max|dp|.  T2 is the type of the constant-coefficient FFT solve:
+// double2 on the FP64 path (FP64 residual and update); float2 on the mixed
+// path, where each iteration is one step of iterative refinement: float-float
+// residual from FP64 face differences (c->Cs2, c->cc32), FP32 correction,
+// then from the third iteration on the correction form (c->R0, c->dP) with
+// P += dP once the loop ends (refine_finish).
 template <typename T2>
 static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop) {
   const Grid &g = c->g;
@@ -551,12 +621,12 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
   const int xblocks = (int)((nrows + npx - 1) / npx);
   {
     size_t smem = 2 * (size_t)npx * c->fx.n * sizeof(T2);
-    if (c->p.precision == TPM_PREC_MIXED)
-      TPM_LAUNCH(c, "fft_x_fwd_resid", (k_xfwd_resid<T2, true>), xblocks, tx, smem, g,
-                 c->fx, r2c, c->P, c->Cs, c->cc, c->RHS, c->dsc, spec, npx);
+    if constexpr (sizeof(T2) == sizeof(float2))
+      TPM_LAUNCH(c, "fft_x_fwd_resid", k_xfwd_resid_refine, xblocks, tx, smem, g, c->fx, r2c,
+                 c->P, c->dP, c->Cs2, c->cc32, c->RHS, c->dsc, c->R0, spec, npx);
     else
-      TPM_LAUNCH(c, "fft_x_fwd_resid", (k_xfwd_resid<T2, false>), xblocks, tx, smem, g,
-                 c->fx, r2c, c->P, c->Cface, c->cc, c->RHS, c->dsc, spec, npx);
+      TPM_LAUNCH(c, "fft_x_fwd_resid", k_xfwd_resid<T2>, xblocks, tx, smem, g, c->fx, r2c,
+                 c->P, c->Cface, c->cc, c->RHS, c->dsc, spec, npx);
   }
   {
     int blocks = g.nz * ((g.nxh + npy - 1) / npy);
@@ -578,10 +648,15 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
     size_t smem = 2 * (size_t)npx * c->fx.n * sizeof(T2);
     double *parts = c->err_parts;
     TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, xblocks, tx, smem, g, c->fx,
-               r2c, spec, c->P, parts, npx, skip);
+               r2c, spec, c->P, parts, npx, skip, c->dP, &c->dsc->it);
     TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 256, 0, parts, xblocks, c->dsc, eps_ctl,
                loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0);
   }
+}
+
+void refine_finish(tpm_ctx *c) {
+  TPM_LAUNCH(c, "refine_finish", k_refine_finish, cell_blocks(c->g), 256, 0, c->g, c->dP,
+             c->dsc, c->P);
 }
 
 void poisson_iteration(tpm_ctx *c, double eps_ctl, const LoopCtl *loop) {
@@ -1010,7 +1085,8 @@ extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, doub
     }
     {
       size_t smem = 2 * (size_t)npx * fx.n * sizeof(double2);
-      k_xinv_update<double2><<<xblocks, kFftThreads, smem, st>>>(g, fx, r2c, spec, P, errp, npx, nullptr);
+      k_xinv_update<double2><<<xblocks, kFftThreads, smem, st>>>(g, fx, r2c, spec, P, errp, npx,
+                                                                 nullptr, nullptr, nullptr);
       k_finish_max<<<1, 256, 0, st>>>(errp, xblocks, dsc, 0.0, cudaGraphConditionalHandle{}, 0);
     }
     if (cudaGetLastError() != cudaSuccess) return TPM_ERR_CUDA;

@@ -7,6 +7,7 @@
 // with --fmad=false, so apart from reductions and the FFT the results are
 // the reference's to the last bit.
 #include "tpm_internal.cuh"
+#include "tpm_ff.cuh"
 #include "tpm_reduce.cuh"
 
 namespace tpm {
@@ -457,9 +458,11 @@ __global__ void k_rho_update_mixed(Grid g, const double *__restrict__ RUi,
 // lower faces of each cell (each face once), from an FP32 seed and one FP64
 // Newton step (~1e-14 relative; an FP32 C would perturb the divergence
 // constraint at 1e-7, which the nearly divergence-free right-hand side
-// amplifies in P).  Cs = C/d^2 feeds the FP64 residual of the refinement.
+// amplifies in P).  C/d^2 feeds the refinement's residual as a float-float
+// pair (Cs2) and, for the PCG operator only, as a double (Cs, else null).
 __global__ void k_face_coeff_mixed(Grid g, const double *__restrict__ Rho_new,
-                                   double *__restrict__ Cface, double *__restrict__ Cs) {
+                                   double *__restrict__ Cface, float2 *__restrict__ Cs2,
+                                   double *__restrict__ Cs) {
   const double inv_d2[3] = {g.inv_dx2, g.inv_dy2, g.inv_dz2};
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
@@ -470,7 +473,9 @@ __global__ void k_face_coeff_mixed(Grid g, const double *__restrict__ Rho_new,
     for (int d = 0; d < 3; ++d) {
       const double clo = rcp64_1((r + Rho_new[nb.m[d]]) * 0.5);
       Cface[d * g.n + c] = clo;
-      Cs[d * g.n + c] = clo * inv_d2[d];
+      const double cs = clo * inv_d2[d];
+      Cs2[d * g.n + c] = ff_from_double(cs);
+      if (Cs) Cs[d * g.n + c] = cs;
     }
   }
 }
@@ -483,9 +488,9 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
                                     const double *__restrict__ Q, const double *__restrict__ RUn,
                                     const double *__restrict__ Cface,
                                     const DevScalars *__restrict__ s, double *__restrict__ RHS,
-                                    double *__restrict__ divg, double *__restrict__ cc,
-                                    double *__restrict__ partials, double *__restrict__ tke_parts,
-                                    PoisArgs a) {
+                                    double *__restrict__ divg, float *__restrict__ cc32,
+                                    double *__restrict__ cc, double *__restrict__ partials,
+                                    double *__restrict__ tke_parts, PoisArgs a) {
   __shared__ double sh[kThreads];
   const double coef = s->coef_div, meanQ = s->mean_Q;
   const double inv_d[3] = {g.inv_dx, g.inv_dy, g.inv_dz};
@@ -517,7 +522,9 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
     double rhs = divu * a.inv_dtpre;
     RHS[c] = rhs;
     acc += rhs;
-    cc[c] = (double)(-3.0f / msum);
+    const float ccf = -3.0f / msum;
+    cc32[c] = ccf;
+    if (cc) cc[c] = (double)ccf;  // the PCG operator's copy
   }
   double bs = block_sum(acc, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = bs;
@@ -726,13 +733,22 @@ __global__ void k_mean_reset(Grid g, const double *__restrict__ RU_np1, double *
 // grid::Initialize (grid.cpp:474): nothing to store on the device beyond the
 // copies done by the host; kept for the operator-level Poisson entry point:
 // center_coeff = -1/I_F2C(C) for a caller-supplied C (poisson.cpp:393-394).
-// Cs_d = C_d / d^2 for caller-supplied face coefficients (operator-level solve)
-__global__ void k_scale_faces(Grid g, const double *__restrict__ Cf, double *__restrict__ Cs) {
+// Cs_d = C_d / d^2 for caller-supplied face coefficients (operator-level
+// solve), as a double and a float-float pair, and cc in FP32
+__global__ void k_scale_faces(Grid g, const double *__restrict__ Cf, const double *__restrict__ cc,
+                              double *__restrict__ Cs, float2 *__restrict__ Cs2,
+                              float *__restrict__ cc32) {
   const double inv_d2[3] = {g.inv_dx2, g.inv_dy2, g.inv_dz2};
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
-       c += (long long)gridDim.x * blockDim.x)
+       c += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int d = 0; d < 3; ++d) Cs[d * g.n + c] = Cf[d * g.n + c] * inv_d2[d];
+    for (int d = 0; d < 3; ++d) {
+      const double cs = Cf[d * g.n + c] * inv_d2[d];
+      Cs[d * g.n + c] = cs;
+      Cs2[d * g.n + c] = ff_from_double(cs);
+    }
+    cc32[c] = (float)cc[c];
+  }
 }
 
 __global__ void k_center_coeff(Grid g, const double *__restrict__ Cf, double *__restrict__ cc) {
@@ -822,10 +838,11 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
   int nb = cell_blocks(c->g);
   double *tke_parts = s == 3 ? c->partials + kPartTke2 * kRedBlocks : nullptr;
   if (c->p.precision == TPM_PREC_MIXED) {
+    const bool pcg = c->p.Solver == 2;
     TPM_LAUNCH(c, "face_coeff", k_face_coeff_mixed, nb, kThreads, 0, c->g, c->Rho_new, c->Cface,
-               c->Cs);
+               c->Cs2, pcg ? c->Cs : nullptr);
     TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_mixed, nb, kThreads, 0, c->g, c->inv_rho, c->Q,
-               c->RU_new, c->Cface, c->dsc, c->RHS, c->divg, c->cc,
+               c->RU_new, c->Cface, c->dsc, c->RHS, c->divg, c->cc32, pcg ? c->cc : nullptr,
                c->partials + kPartRhs * kRedBlocks, tke_parts, a);
   } else {
     // c->U (the face velocity of RU_int) is dead after the momentum RHS; it
@@ -915,7 +932,7 @@ void launch_center_coeff_from_C(tpm_ctx *c) {
              c->cc);
   if (c->p.precision == TPM_PREC_MIXED)  // the mixed residual reads C/d^2
     TPM_LAUNCH(c, "face_coeff_scaled", k_scale_faces, cell_blocks(c->g), kThreads, 0, c->g,
-               c->Cface, c->Cs);
+               c->Cface, c->cc, c->Cs, c->Cs2, c->cc32);
 }
 
 void launch_init_fields(tpm_ctx *) {}

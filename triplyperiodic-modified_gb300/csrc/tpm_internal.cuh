@@ -144,7 +144,14 @@ struct tpm_ctx {
   // FP32 copies read by the FP32 stencils of the mixed path (written once per
   // value: FP64<->FP32 conversions issue on the FP64 pipe)
   float *U32 = nullptr, *RUi32 = nullptr, *RUn32 = nullptr, *Fp32 = nullptr;  // 3n each
-  double *Cs = nullptr;     // 3n: C/d^2 for the mixed residual
+  double *Cs = nullptr;     // 3n: C/d^2 for the mixed PCG operator
+  // mixed Richardson refinement: C/d^2 per face and the base residual of the
+  // correction form as float-float pairs (hi, lo), cc in FP32, and the
+  // solve's correction sum (P += dP once the loop ends)
+  float2 *Cs2 = nullptr;    // 3n
+  float2 *R0 = nullptr;     // n
+  float *cc32 = nullptr;    // n
+  double *dP = nullptr;     // n
   bool rui32_stale = true;
   double2 *spec = nullptr;
   double *partials = nullptr;  // kRedBlocks * 4
@@ -249,6 +256,8 @@ struct LoopCtl {
 // eps_ctl > 0 and no loop control the iteration sets dsc->skip once
 // max|dp| <= eps_ctl, and every kernel of a later iteration returns at once.
 void poisson_iteration(tpm_ctx *c, double eps_ctl = 0.0, const LoopCtl *loop = nullptr);
+// mixed Richardson loop: P += dP after the loop (a no-op below two iterations)
+void refine_finish(tpm_ctx *c);
 // z = S (-Lap_h)^-1 S r, S = diag(sc) (FFT passes of the Poisson solve), with
 // per-block partials of r.z; returns the number of partials
 int fft_precondition(tpm_ctx *c, const double *r, const double *sc, double *z, double *parts,
