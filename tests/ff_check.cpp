@@ -79,6 +79,13 @@ int main() {
     float2 m = ff_mul(pa, pb);
     long double em = std::fabs((long double)m.x + m.y - va * vb);
     CHECK(em <= std::ldexp((long double)std::fabs(va * vb), -44), "mul err %.3Lg", em);
+    float2 pc = ff_from_double(va * (1.0 + 1e-3 * unit(rng)));  // close to pa
+    float2 sb = ff_sub(pc, pa);
+    long double es = std::fabs((long double)sb.x + sb.y - (((long double)pc.x + pc.y) - va));
+    CHECK(es <= std::ldexp(std::fabs(((long double)pc.x + pc.y) - va), -46), "sub err %.3Lg", es);
+    float2 af = ff_add_f(pa, c);
+    long double ef = std::fabs((long double)af.x + af.y - (va + c));
+    CHECK(ef <= std::ldexp(std::fabs(va) + std::fabs((long double)c), -46), "add_f err %.3Lg", ef);
     float2 ad = ff_add(pa, pb);
     long double ea = std::fabs((long double)ad.x + ad.y - (va + vb));
     CHECK(ea <= std::ldexp(std::fabs(va) + std::fabs(vb), -46), "add err %.3Lg", ea);

@@ -3,7 +3,8 @@
 against a stand-in cuda_runtime.h for its bit-cast intrinsics, with FP
 contraction off, and tests/ff_check.cpp checks the double split (2^-48 bound,
 truncated high part, zero / tiny / overflow / inf / nan), the exact float to
-double conversion, TwoSum's exactness and the product and sum bounds."""
+double conversion, TwoSum's exactness and the bounds of the product, the sums
+and the difference of close pairs."""
 import os
 import shutil
 import subprocess

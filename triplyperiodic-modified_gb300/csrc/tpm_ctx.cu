@@ -372,10 +372,10 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
       c->Cs2 = dalloc<float2>(c, 3 * n);
       c->R0 = dalloc<float2>(c, n);
       c->cc32 = dalloc<float>(c, n);
-      c->dP = dalloc<double>(c, n);
+      c->dP = dalloc<float2>(c, n);
       TPM_CUDA_TRY(cudaMemsetAsync(c->Cs2, 0, sizeof(float2) * 3 * n, c->stream));
       TPM_CUDA_TRY(cudaMemsetAsync(c->R0, 0, sizeof(float2) * n, c->stream));
-      TPM_CUDA_TRY(cudaMemsetAsync(c->dP, 0, sizeof(double) * n, c->stream));
+      TPM_CUDA_TRY(cudaMemsetAsync(c->dP, 0, sizeof(float2) * n, c->stream));
       TPM_CUDA_TRY(cudaMemsetAsync(c->cc32, 0, sizeof(float) * n, c->stream));
     }
     c->partials = dalloc<double>(c, (size_t)tpm::kPartRegions * tpm::kRedBlocks);

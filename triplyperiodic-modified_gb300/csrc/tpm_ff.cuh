@@ -39,6 +39,21 @@ __device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
   return ff_fast_two_sum(s.x, s.y + (a.y + b.y));
 }
 
+// a - b to within 2^-46 |a - b| (both pairs' parts through TwoSum: the
+// difference of two close sums keeps its relative precision)
+__device__ __forceinline__ float2 ff_sub(float2 a, float2 b) {
+  float2 s = ff_two_sum(a.x, -b.x);
+  const float2 t = ff_two_sum(a.y, -b.y);
+  s = ff_fast_two_sum(s.x, s.y + t.x);
+  return ff_fast_two_sum(s.x, s.y + t.y);
+}
+
+// a + b for a pair a and a float b, within 2^-46 (|a| + |b|)
+__device__ __forceinline__ float2 ff_add_f(float2 a, float b) {
+  const float2 s = ff_two_sum(a.x, b);
+  return ff_fast_two_sum(s.x, s.y + a.y);
+}
+
 // a * b, unnormalised: a.x b.x exactly (FMA) plus the cross terms, within
 // 2^-44 |a b| for pairs from ff_from_double (|lo| < 2^-23 |hi|: the dropped
 // a.y b.y and the roundings of the cross terms)

@@ -18,6 +18,7 @@
 // FFTs are mixed-radix (4, 2, 3, 5) Stockham auto-sort with twiddles from a
 // host table (cos/sin of 2 pi m/n).  Butterflies use explicit FMAs; the
 // residual and the update keep the reference's operation order.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -58,6 +59,15 @@ __device__ __forceinline__ T2 cmul(T2 a, T2 w, int sign) {
   using C = Cx<T2>;
   typename C::T wi = sign < 0 ? w.y : -w.y;
   return C::mk(C::fma_(a.x, w.x, -a.y * wi), C::fma_(a.x, wi, a.y * w.x));
+}
+
+// i / d by one multiply-high with m = ceil(2^32 / d), exact for 0 <= i < 2^16
+// and 2 <= d < 2^16 (the error i*(m - 2^32/d)/2^32 < 2^-16 < 1/d cannot carry
+// the quotient past an integer); m = 0 stands for d = 1.  Every index of the
+// pencil passes is below 2^13.
+unsigned fdiv_magic(int d) { return d <= 1 ? 0u : 0xFFFFFFFFu / (unsigned)d + 1u; }
+__device__ __forceinline__ int fdiv(int i, unsigned m) {
+  return m ? (int)__umulhi((unsigned)i, m) : i;
 }
 
 template <typename T2>
@@ -109,17 +119,21 @@ __device__ __forceinline__ void dft_small(T2 *v, int R, int sign) {
 // One Stockham stage of radix R:  for i in [0, n/R): k = i mod p,
 //   v_t = a[i + t n/R] * w^(k t n/(p R)),  V = DFT_R(v),
 //   b[(i/p) p R + k + u p] = V_u.
+// npen = 2^lq pencils; pm is the division magic of p (fdiv_magic).
 template <int R, typename T2>
 __device__ __forceinline__ void stockham_stage(const T2 *__restrict__ a, T2 *__restrict__ b,
-                                               int npen, const FftPlan &pl, int p, int sign) {
+                                               int lq, const FftPlan &pl, int p, unsigned pm,
+                                               int sign) {
   const int n = pl.n;
   const int m = n / R;
   const int step = n / (p * R);
-  const int total = m * npen;
+  const int npen = 1 << lq;
+  const int total = m << lq;
   for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int q = idx % npen;
-    const int i = idx / npen;
-    const int k = i % p;
+    const int q = idx & (npen - 1);
+    const int i = idx >> lq;
+    const int ip = fdiv(i, pm);  // i / p
+    const int k = i - ip * p;
     T2 v[R];
     v[0] = a[i * npen + q];
     if (p == 1) {  // first stage: every twiddle is w^0 = 1
@@ -131,25 +145,28 @@ __device__ __forceinline__ void stockham_stage(const T2 *__restrict__ a, T2 *__r
         v[t] = cmul(a[(i + t * m) * npen + q], Cx<T2>::tw(pl, k * t * step), sign);
     }
     dft_small(v, R, sign);
-    const int j = (i / p) * p * R + k;
+    const int j = ip * p * R + k;
 #pragma unroll
     for (int u = 0; u < R; ++u) b[(j + u * p) * npen + q] = v[u];
   }
 }
 
 // Batched Stockham FFT in shared memory.  Element t of pencil q lives at
-// a[t*npen + q]; consecutive threads take consecutive pencils.  Returns the
-// buffer (a or b) that holds the result.  Ends with __syncthreads().
+// a[t*npen + q]; consecutive threads take consecutive pencils; npen is a power
+// of two.  Returns the buffer (a or b) that holds the result.  Ends with
+// __syncthreads().
 template <typename T2>
 __device__ T2 *smem_fft(T2 *a, T2 *b, int npen, const FftPlan &pl, int sign) {
+  const int lq = __ffs(npen) - 1;
   int p = 1;
   for (int s = 0; s < pl.nst; ++s) {
     const int R = pl.radix[s];
+    const unsigned pm = pl.pmag[s];
     switch (R) {
-      case 4: stockham_stage<4>(a, b, npen, pl, p, sign); break;
-      case 2: stockham_stage<2>(a, b, npen, pl, p, sign); break;
-      case 3: stockham_stage<3>(a, b, npen, pl, p, sign); break;
-      default: stockham_stage<5>(a, b, npen, pl, p, sign); break;
+      case 4: stockham_stage<4>(a, b, lq, pl, p, pm, sign); break;
+      case 2: stockham_stage<2>(a, b, lq, pl, p, pm, sign); break;
+      case 3: stockham_stage<3>(a, b, lq, pl, p, pm, sign); break;
+      default: stockham_stage<5>(a, b, lq, pl, p, pm, sign); break;
     }
     __syncthreads();
     T2 *t = a;
@@ -168,17 +185,17 @@ __device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
 // transforms z (row q at stride npen): X[k] = Fe[k] + W^k Fo[k], k <= Nx/2,
 // stored to the half spectrum.
 template <typename T2>
-__device__ __forceinline__ void r2c_store(const Grid &g, const T2 *z, int npen, int M,
+__device__ __forceinline__ void r2c_store(const Grid &g, const T2 *z, int npen, const FftPlan &pl,
                                           long long row0, long long nrows,
                                           const T2 *__restrict__ r2c_tw, T2 *__restrict__ spec) {
   using T = typename Cx<T2>::T;
-  const int nxh = g.nxh;
+  const int nxh = g.nxh, M = pl.n;
   for (int idx = threadIdx.x; idx < npen * nxh; idx += blockDim.x) {
-    const int q = idx / nxh, kx = idx % nxh;
+    const int q = fdiv(idx, pl.nhmag), kx = idx - q * nxh;
     const long long row = row0 + q;
     if (row >= nrows) continue;
-    T2 Z = z[(kx % M) * npen + q];
-    T2 Zc = z[((M - kx) % M) * npen + q];
+    T2 Z = z[(kx == M ? 0 : kx) * npen + q];
+    T2 Zc = z[(kx == 0 ? 0 : M - kx) * npen + q];
     Zc.y = -Zc.y;
     T fer = (Z.x + Zc.x) * (T)0.5, fei = (Z.y + Zc.y) * (T)0.5;
     T dr = Z.x - Zc.x, di = Z.y - Zc.y;
@@ -209,7 +226,7 @@ __global__ void k_xfwd_resid(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   const double *Cx_ = Cf, *Cy_ = Cf + g.n, *Cz_ = Cf + 2 * g.n;
   // residual, written interleaved as z[m] = r[2m] + i r[2m+1]
   for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
-    const int q = idx / g.nx, i = idx % g.nx;
+    const int q = fdiv(idx, pl.n2mag), i = idx - q * g.nx;
     const long long row = row0 + q;
     double r = 0;
     if (row < nrows) {
@@ -237,27 +254,26 @@ __global__ void k_xfwd_resid(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   }
   __syncthreads();
   T2 *z = smem_fft(a, b, npen, pl, -1);
-  r2c_store(g, z, npen, M, row0, nrows, r2c_tw, spec);
+  r2c_store(g, z, npen, pl, row0, nrows, r2c_tw, spec);
 }
 
 // Mixed path: the x-pass of one step of iterative refinement.  Iterations 0
 // and 1 of a solve form the residual of P itself, div(C grad P) - (RHS -
-// mean); iteration 0 then corrects P directly, iteration 1 stores its
-// residual as R0 and starts a correction sum dP, and iteration k >= 2 forms
-// R0 + div(C grad dP) (correction form; P += dP once when the loop ends,
-// k_refine_finish).  The rounding noise of a residual scales with the field
-// whose differences it takes: in correction form that is dP, about 1e-6 of P
-// after the first correction, so the iteration converges far below the
-// noise of an FP64 residual of P; R0's own rounding, made once, only shifts
-// the fixed point (by about 1e-14 of P).  The face differences X_nb - X are
-// FP64 subtractions (exact to rounding for the close values of neighbouring
-// cells, and the kernel's only FP64 operations: six or seven per cell
-// against the seventeen of an FP64 residual); each is split into a
+// mean), from FP64 face differences P_nb - P (exact to rounding for the close
+// values of neighbouring cells, and the kernel's only FP64 operations: seven
+// per cell against the seventeen of an FP64 residual), each split into a
 // float-float pair (tpm_ff.cuh), multiplied by Cs2 = C/d^2 and summed as
-// pairs on the FP32 pipe.  The residual times cc is rounded to FP32 for the
-// correction's FFT solve.
+// pairs on the FP32 pipe.  Iteration 0 then corrects P directly; iteration 1
+// stores its residual as R0 and starts a correction sum dP (a float-float
+// pair per cell), and iteration k >= 2 forms R0 + div(C grad dP) with no FP64
+// operation (correction form; P += dP once when the loop ends,
+// k_refine_finish).  After the first correction dP is about 1e-6 of P, so
+// the pair carries it and the rounding noise of the correction form, which
+// scales with dP, lies far below that of an FP64 residual of P; R0's own
+// rounding, made once, only shifts the fixed point (by about 1e-14 of P).
+// The residual times cc is rounded to FP32 for the correction's FFT solve.
 __global__ void k_xfwd_resid_refine(Grid g, FftPlan pl, const float2 *__restrict__ r2c_tw,
-                                    const double *__restrict__ P, const double *__restrict__ dP,
+                                    const double *__restrict__ P, const float2 *__restrict__ dP,
                                     const float2 *__restrict__ Cs2, const float *__restrict__ cc32,
                                     const double *__restrict__ RHS,
                                     const DevScalars *__restrict__ s, float2 *__restrict__ R0,
@@ -272,10 +288,9 @@ __global__ void k_xfwd_resid_refine(Grid g, FftPlan pl, const float2 *__restrict
   const int it = s->it;
   const bool direct = it <= 1;
   const double mean = s->mean_rhs;
-  const double *X = direct ? P : dP;
   const float2 *Cx_ = Cs2, *Cy_ = Cs2 + g.n, *Cz_ = Cs2 + 2 * g.n;
   for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
-    const int q = idx / g.nx, i = idx % g.nx;
+    const int q = fdiv(idx, pl.n2mag), i = idx - q * g.nx;
     const long long row = row0 + q;
     float r = 0.f;
     if (row < nrows) {
@@ -284,15 +299,27 @@ __global__ void k_xfwd_resid_refine(Grid g, FftPlan pl, const float2 *__restrict
       const long long cxm = at(g, wrap_m(i, g.nx), j, k), cxp = at(g, wrap_p(i, g.nx), j, k);
       const long long cym = at(g, i, wrap_m(j, g.ny), k), cyp = at(g, i, wrap_p(j, g.ny), k);
       const long long czm = at(g, i, j, wrap_m(k, g.nz)), czp = at(g, i, j, wrap_p(k, g.nz));
-      float2 acc = direct ? ff_from_double(mean - RHS[c]) : R0[c];
-      const double xc = X[c];
-      acc = ff_add(acc, ff_mul(Cx_[c], ff_from_double(X[cxm] - xc)));
-      acc = ff_add(acc, ff_mul(Cx_[cxp], ff_from_double(X[cxp] - xc)));
-      acc = ff_add(acc, ff_mul(Cy_[c], ff_from_double(X[cym] - xc)));
-      acc = ff_add(acc, ff_mul(Cy_[cyp], ff_from_double(X[cyp] - xc)));
-      acc = ff_add(acc, ff_mul(Cz_[c], ff_from_double(X[czm] - xc)));
-      acc = ff_add(acc, ff_mul(Cz_[czp], ff_from_double(X[czp] - xc)));
-      if (it == 1) R0[c] = acc;
+      float2 acc;
+      if (direct) {
+        acc = ff_from_double(mean - RHS[c]);
+        const double pc = P[c];
+        acc = ff_add(acc, ff_mul(Cx_[c], ff_from_double(P[cxm] - pc)));
+        acc = ff_add(acc, ff_mul(Cx_[cxp], ff_from_double(P[cxp] - pc)));
+        acc = ff_add(acc, ff_mul(Cy_[c], ff_from_double(P[cym] - pc)));
+        acc = ff_add(acc, ff_mul(Cy_[cyp], ff_from_double(P[cyp] - pc)));
+        acc = ff_add(acc, ff_mul(Cz_[c], ff_from_double(P[czm] - pc)));
+        acc = ff_add(acc, ff_mul(Cz_[czp], ff_from_double(P[czp] - pc)));
+        if (it == 1) R0[c] = acc;
+      } else {
+        acc = R0[c];
+        const float2 dc = dP[c];
+        acc = ff_add(acc, ff_mul(Cx_[c], ff_sub(dP[cxm], dc)));
+        acc = ff_add(acc, ff_mul(Cx_[cxp], ff_sub(dP[cxp], dc)));
+        acc = ff_add(acc, ff_mul(Cy_[c], ff_sub(dP[cym], dc)));
+        acc = ff_add(acc, ff_mul(Cy_[cyp], ff_sub(dP[cyp], dc)));
+        acc = ff_add(acc, ff_mul(Cz_[c], ff_sub(dP[czm], dc)));
+        acc = ff_add(acc, ff_mul(Cz_[czp], ff_sub(dP[czp], dc)));
+      }
       r = (acc.x + acc.y) * cc32[c];
     }
     float *slot = reinterpret_cast<float *>(&a[(i >> 1) * npen + q]);
@@ -300,7 +327,7 @@ __global__ void k_xfwd_resid_refine(Grid g, FftPlan pl, const float2 *__restrict
   }
   __syncthreads();
   float2 *z = smem_fft(a, b, npen, pl, -1);
-  r2c_store(g, z, npen, M, row0, nrows, r2c_tw, spec);
+  r2c_store(g, z, npen, pl, row0, nrows, r2c_tw, spec);
 }
 
 // ------------------------------------------------------- 2./4. y pencils
@@ -309,21 +336,53 @@ __global__ void k_fft_y(Grid g, FftPlan pl, T2 *__restrict__ spec, int npen, int
                         const int *__restrict__ skip) {
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lq = __ffs(npen) - 1;  // npen is a power of two
   T2 *a = reinterpret_cast<T2 *>(smem_raw);
   T2 *b = a + pl.n * npen;
   const int tiles = (g.nxh + npen - 1) / npen;
   const int kz = blockIdx.x / tiles, kx0 = (blockIdx.x % tiles) * npen;
   const long long base = (long long)kz * g.ny * g.nxh;
   for (int idx = threadIdx.x; idx < npen * g.ny; idx += blockDim.x) {
-    const int q = idx % npen, ky = idx / npen;
+    const int q = idx & (npen - 1), ky = idx >> lq;
     a[ky * npen + q] = (kx0 + q < g.nxh) ? spec[base + (long long)ky * g.nxh + kx0 + q]
                                          : Cx<T2>::mk(0, 0);
   }
   __syncthreads();
   T2 *r = smem_fft(a, b, npen, pl, sign);
   for (int idx = threadIdx.x; idx < npen * g.ny; idx += blockDim.x) {
-    const int q = idx % npen, ky = idx / npen;
+    const int q = idx & (npen - 1), ky = idx >> lq;
     if (kx0 + q < g.nxh) spec[base + (long long)ky * g.nxh + kx0 + q] = r[ky * npen + q];
+  }
+}
+
+// 1/(ax[kx] + ay[ky] + az[kz]): FP64 on the FP64 path, FP32 for the mixed
+// path's correction solve
+template <typename T>
+__device__ __forceinline__ T inv_mwn_at(const double *ax, const double *ay, const double *az,
+                                        int kx, int ky, int kz);
+template <>
+__device__ __forceinline__ double inv_mwn_at<double>(const double *ax, const double *ay,
+                                                     const double *az, int kx, int ky, int kz) {
+  return 1.0 / (ax[kx] + ay[ky] + az[kz]);
+}
+template <>
+__device__ __forceinline__ float inv_mwn_at<float>(const double *ax, const double *ay,
+                                                   const double *az, int kx, int ky, int kz) {
+  return 1.0f / ((float)ax[kx] + (float)ay[ky] + (float)az[kz]);
+}
+
+// the table of those reciprocals over the half spectrum (1 at the zero mode,
+// which the solve leaves alone), built once per context
+template <typename T>
+__global__ void k_inv_mwn(Grid g, const double *__restrict__ ax, const double *__restrict__ ay,
+                          const double *__restrict__ az, T *__restrict__ tab) {
+  const long long total = (long long)g.nxh * g.ny * g.nz;
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < total;
+       m += (long long)gridDim.x * blockDim.x) {
+    const int kx = (int)(m % g.nxh);
+    const long long r = m / g.nxh;
+    const int ky = (int)(r % g.ny), kz = (int)(r / g.ny);
+    tab[m] = (kx + ky + kz) > 0 ? inv_mwn_at<T>(ax, ay, az, kx, ky, kz) : (T)1;
   }
 }
 
@@ -331,9 +390,11 @@ __global__ void k_fft_y(Grid g, FftPlan pl, T2 *__restrict__ spec, int npen, int
 template <typename T2>
 __global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const double *__restrict__ ax,
                               const double *__restrict__ ay, const double *__restrict__ az,
-                              int npen, const int *__restrict__ skip) {
+                              const typename Cx<T2>::T *__restrict__ inv_mwn, int npen,
+                              const int *__restrict__ skip) {
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lq = __ffs(npen) - 1;  // npen is a power of two
   using T = typename Cx<T2>::T;
   T2 *a = reinterpret_cast<T2 *>(smem_raw);
   T2 *b = a + pl.n * npen;
@@ -342,7 +403,7 @@ __global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const d
   const long long plane = (long long)g.ny * g.nxh;
   const long long base = (long long)ky * g.nxh + kx0;
   for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
-    const int q = idx % npen, kz = idx / npen;
+    const int q = idx & (npen - 1), kz = idx >> lq;
     a[kz * npen + q] = (kx0 + q < g.nxh) ? spec[base + kz * plane + q] : Cx<T2>::mk(0, 0);
   }
   __syncthreads();
@@ -350,26 +411,23 @@ __global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const d
   T2 *other = (r == a) ? b : a;
   // divide by the modified wave number except the zero mode (poisson.cpp:442-449)
   for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
-    const int q = idx % npen, kz = idx / npen;
+    const int q = idx & (npen - 1), kz = idx >> lq;
     const int kx = kx0 + q;
     if (kx < g.nxh && (kx + ky + kz) > 0) {
       T2 v = r[kz * npen + q];
-      if (sizeof(T) == sizeof(double)) {
-        const double inv = 1.0 / (ax[kx] + ay[ky] + az[kz]);
-        v.y = (T)((double)v.y * inv);
-        v.x = (T)((double)v.x * inv);
-      } else {  // FP32 correction solve of the mixed path
-        const float inv = 1.0f / ((float)ax[kx] + (float)ay[ky] + (float)az[kz]);
-        v.y = (T)((float)v.y * inv);
-        v.x = (T)((float)v.x * inv);
-      }
+      // the reciprocal from the per-mode table (k_inv_mwn, same expression)
+      // when there is one
+      const T inv = inv_mwn ? inv_mwn[((long long)kz * g.ny + ky) * g.nxh + kx]
+                            : inv_mwn_at<T>(ax, ay, az, kx, ky, kz);
+      v.y = v.y * inv;
+      v.x = v.x * inv;
       r[kz * npen + q] = v;
     }
   }
   __syncthreads();
   T2 *o = smem_fft(r, other, npen, pl, +1);
   for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
-    const int q = idx % npen, kz = idx / npen;
+    const int q = idx & (npen - 1), kz = idx >> lq;
     if (kx0 + q < g.nxh) spec[base + kz * plane + q] = o[kz * npen + q];
   }
 }
@@ -379,7 +437,7 @@ template <typename T2>
 __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
                               const T2 *__restrict__ spec, double *__restrict__ P,
                               double *__restrict__ partials, int npen,
-                              const int *__restrict__ skip, double *__restrict__ dP,
+                              const int *__restrict__ skip, float2 *__restrict__ dP,
                               const int *__restrict__ it) {
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -393,7 +451,7 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   const int nxh = g.nxh;
   // Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) W^-k, k < M
   for (int idx = threadIdx.x; idx < npen * M; idx += blockDim.x) {
-    const int q = idx / M, kx = idx % M;
+    const int q = fdiv(idx, pl.nmag), kx = idx - q * M;
     const long long row = row0 + q;
     T2 Z = Cx<T2>::mk(0, 0);
     if (row < nrows) {
@@ -414,33 +472,33 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   const double inv_tot = 1.0 / (double)(g.nx * g.ny * g.nz);
   double mx = 0;
   if (sizeof(T) == sizeof(float)) {
-    // mixed path: the correction dp = -x/N^3, formed in FP32 and converted
-    // exactly, goes to P at iteration 0, starts the solve's FP64 correction
-    // sum dP at iteration 1 and joins it after (one FP64 operation per cell;
-    // P += dP in k_refine_finish).  max|x| in FP32 (exact: the maximum picks
-    // one x, scaled once below).
+    // mixed path: the correction dp = -x/N^3, formed in FP32, goes to P at
+    // iteration 0 (converted exactly, one FP64 operation per cell), starts
+    // the solve's float-float correction sum dP at iteration 1 and joins it
+    // after (P += dP in k_refine_finish).  max|x| in FP32 (exact: the maximum
+    // picks one x, scaled once below).
     const int itv = *it;
     const float inv_tot_f = 1.0f / (float)((long long)g.nx * g.ny * g.nz);
     float mxf = 0.f;
     for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
-      const int q = idx / g.nx, i = idx % g.nx;
+      const int q = fdiv(idx, pl.n2mag), i = idx - q * g.nx;
       const long long row = row0 + q;
       if (row >= nrows) continue;
       const T *zz = reinterpret_cast<const T *>(&z[(i >> 1) * npen + q]);
       const float xf = (float)zz[i & 1];
       const long long c = row * g.nx + i;
-      const double dp = ff_f2d(-(xf * inv_tot_f));
+      const float dp = -(xf * inv_tot_f);
       if (itv == 0)
-        P[c] += dp;
+        P[c] += ff_f2d(dp);
       else
-        dP[c] = itv == 1 ? dp : dP[c] + dp;
+        dP[c] = itv == 1 ? make_float2(dp, 0.f) : ff_add_f(dP[c], dp);
       const float ax = fabsf(xf);
       mxf = ax > mxf ? ax : mxf;
     }
     mx = (double)mxf * inv_tot;
   } else {
     for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
-      const int q = idx / g.nx, i = idx % g.nx;
+      const int q = fdiv(idx, pl.n2mag), i = idx - q * g.nx;
       const long long row = row0 + q;
       if (row >= nrows) continue;
       const T *zz = reinterpret_cast<const T *>(&z[(i >> 1) * npen + q]);
@@ -483,19 +541,22 @@ __global__ void k_finish_max(const double *__restrict__ partials, int nparts, De
 
 // End of a mixed refinement loop that reached the correction form (it >= 2
 // iterations ran): P += dP
-__global__ void k_refine_finish(Grid g, const double *__restrict__ dP,
+__global__ void k_refine_finish(Grid g, const float2 *__restrict__ dP,
                                 const DevScalars *__restrict__ s, double *__restrict__ P) {
   if (s->it <= 1) return;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
-       c += (long long)gridDim.x * blockDim.x)
-    P[c] += dP[c];
+       c += (long long)gridDim.x * blockDim.x) {
+    const float2 d = dP[c];
+    P[c] = (P[c] + ff_f2d(d.x)) + ff_f2d(d.y);
+  }
 }
 
-// pencils per block: two ping-pong buffers of 32 KB each
+// pencils per block: two ping-pong buffers of 32 KB each, a power of two
 int pens_for(int n, int elem_bytes = 16) {
-  int p = (kFftSmemPoints * 16 / elem_bytes) / n;
-  if (p < 1) p = 1;
-  if (p > 32) p = 32;
+  int cap = (kFftSmemPoints * 16 / elem_bytes) / n;
+  if (cap > 32) cap = 32;
+  int p = 1;
+  while (2 * p <= cap) p *= 2;
   return p;
 }
 
@@ -509,6 +570,14 @@ void factorize(int n, FftPlan &pl) {
   while (m % 3 == 0) { pl.radix[pl.nst++] = 3; m /= 3; }
   while (m % 5 == 0) { pl.radix[pl.nst++] = 5; m /= 5; }
   if (m != 1) throw std::string("grid size must factor into 2, 3 and 5");
+  int p = 1;
+  for (int st = 0; st < pl.nst; ++st) {
+    pl.pmag[st] = fdiv_magic(p);
+    p *= pl.radix[st];
+  }
+  pl.nmag = fdiv_magic(n);
+  pl.n2mag = fdiv_magic(2 * n);
+  pl.nhmag = fdiv_magic(n + 1);
 }
 
 }  // namespace
@@ -588,6 +657,20 @@ void fft_plans_create(tpm_ctx *c) {
   TPM_CUDA_TRY(cudaMemcpy(c->ax, ax.data(), ax.size() * 8, cudaMemcpyHostToDevice));
   TPM_CUDA_TRY(cudaMemcpy(c->ay, ay.data(), ay.size() * 8, cudaMemcpyHostToDevice));
   TPM_CUDA_TRY(cudaMemcpy(c->az, az.data(), az.size() * 8, cudaMemcpyHostToDevice));
+  {  // per-mode reciprocals of the wave-number sum for the z-pass solve
+    const long long nmodes = (long long)g.nxh * g.ny * g.nz;
+    const int blocks = (int)std::min<long long>((nmodes + 255) / 256, 4096);
+    if (c->p.precision == TPM_PREC_MIXED) {
+      float *t = dalloc<float>(c, nmodes);
+      k_inv_mwn<float><<<blocks, 256, 0, c->stream>>>(g, c->ax, c->ay, c->az, t);
+      c->inv_mwn = t;
+    } else {
+      double *t = dalloc<double>(c, nmodes);
+      k_inv_mwn<double><<<blocks, 256, 0, c->stream>>>(g, c->ax, c->ay, c->az, t);
+      c->inv_mwn = t;
+    }
+    TPM_CUDA_TRY(cudaGetLastError());
+  }
   // dynamic shared memory above 48 KB
   int smem64 = 2 * kFftSmemPoints * (int)sizeof(double2);
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_xfwd_resid<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
@@ -605,9 +688,10 @@ void fft_plans_create(tpm_ctx *c) {
 // dsc->err = max|dp|.  T2 is the type of the constant-coefficient FFT solve:
 // double2 on the FP64 path (FP64 residual and update); float2 on the mixed
 // path, where each iteration is one step of iterative refinement: float-float
-// residual from FP64 face differences (c->Cs2, c->cc32), FP32 correction,
-// then from the third iteration on the correction form (c->R0, c->dP) with
-// P += dP once the loop ends (refine_finish).
+// residual (c->Cs2, c->cc32) from FP64 face differences of P, FP32
+// correction, then from the third iteration on the correction form (c->R0
+// and the float-float correction sum c->dP) with P += dP once the loop ends
+// (refine_finish).
 template <typename T2>
 static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop) {
   const Grid &g = c->g;
@@ -637,7 +721,7 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
     int blocks = g.ny * ((g.nxh + npz - 1) / npz);
     size_t smem = 2 * (size_t)npz * c->fz.n * sizeof(T2);
     TPM_LAUNCH(c, "fft_z_solve", k_fft_z_solve<T2>, blocks, tz, smem, g, c->fz, spec,
-               c->ax, c->ay, c->az, npz, skip);
+               c->ax, c->ay, c->az, static_cast<const typename Cx<T2>::T *>(c->inv_mwn), npz, skip);
   }
   {
     int blocks = g.nz * ((g.nxh + npy - 1) / npy);
@@ -668,8 +752,7 @@ void poisson_iteration(tpm_ctx *c, double eps_ctl, const LoopCtl *loop) {
 
 int pens_default(int n, int elem_bytes) { return pens_for(n, elem_bytes); }
 int pens_max(int n, int elem_bytes) {
-  int p = (kFftSmemPoints * 16 / elem_bytes) / n;  // both buffers within the 64 KB set per kernel
-  return p < 1 ? 1 : (p > 32 ? 32 : p);
+  return pens_for(n, elem_bytes);  // both buffers within the 64 KB set per kernel
 }
 
 }  // namespace tpm
@@ -692,19 +775,20 @@ __global__ void k_spec_xfwd(Grid g, FftPlan pl, const double2 *__restrict__ r2c_
   const long long nrows = (long long)g.ny * g.nz;
   const long long row0 = (long long)blockIdx.x * npen;
   for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
-    const int q = idx / g.nx, i = idx % g.nx;
+    const int q = fdiv(idx, pl.n2mag), i = idx - q * g.nx;
     const long long row = row0 + q;
     double *slot = reinterpret_cast<double *>(&a[(i >> 1) * npen + q]);
     slot[i & 1] = row < nrows ? f[row * g.nx + i] : 0.0;
   }
   __syncthreads();
   double2 *z = smem_fft(a, b, npen, pl, -1);
-  r2c_store(g, z, npen, M, row0, nrows, r2c_tw, spec);
+  r2c_store(g, z, npen, pl, row0, nrows, r2c_tw, spec);
 }
 
 __global__ void k_spec_z_energy(Grid g, FftPlan pl, const double2 *__restrict__ spec,
                                 double *__restrict__ emode, int npen, int accumulate) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lq = __ffs(npen) - 1;  // npen is a power of two
   double2 *a = reinterpret_cast<double2 *>(smem_raw);
   double2 *b = a + pl.n * npen;
   const int tiles = (g.nxh + npen - 1) / npen;
@@ -712,14 +796,14 @@ __global__ void k_spec_z_energy(Grid g, FftPlan pl, const double2 *__restrict__ 
   const long long plane = (long long)g.ny * g.nxh;
   const long long base = (long long)ky * g.nxh + kx0;
   for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
-    const int q = idx % npen, kz = idx / npen;
+    const int q = idx & (npen - 1), kz = idx >> lq;
     a[kz * npen + q] = (kx0 + q < g.nxh) ? spec[base + kz * plane + q] : make_double2(0, 0);
   }
   __syncthreads();
   const double2 *r = smem_fft(a, b, npen, pl, -1);
   const double inv_tot = 1.0 / ((double)g.nx * (double)g.ny * (double)g.nz);
   for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
-    const int q = idx % npen, kz = idx / npen;
+    const int q = idx & (npen - 1), kz = idx >> lq;
     const int kx = kx0 + q;
     if (kx >= g.nxh) continue;
     const double2 v = r[kz * npen + q];
@@ -784,7 +868,7 @@ __global__ void k_pc_xfwd(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   const long long nrows = (long long)g.ny * g.nz;
   const long long row0 = (long long)blockIdx.x * npen;
   for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
-    const int q = idx / g.nx, i = idx % g.nx;
+    const int q = fdiv(idx, pl.n2mag), i = idx - q * g.nx;
     const long long row = row0 + q;
     T *slot = reinterpret_cast<T *>(&a[(i >> 1) * npen + q]);
     const long long c = row * g.nx + i;
@@ -792,7 +876,7 @@ __global__ void k_pc_xfwd(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   }
   __syncthreads();
   T2 *z = smem_fft(a, b, npen, pl, -1);
-  r2c_store(g, z, npen, M, row0, nrows, r2c_tw, spec);
+  r2c_store(g, z, npen, pl, row0, nrows, r2c_tw, spec);
 }
 
 template <typename T2>
@@ -811,7 +895,7 @@ __global__ void k_pc_xinv(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   const long long row0 = (long long)blockIdx.x * npen;
   const int nxh = g.nxh;
   for (int idx = threadIdx.x; idx < npen * M; idx += blockDim.x) {
-    const int q = idx / M, kx = idx % M;
+    const int q = fdiv(idx, pl.nmag), kx = idx - q * M;
     const long long row = row0 + q;
     T2 Z = Cx<T2>::mk(0, 0);
     if (row < nrows) {
@@ -832,7 +916,7 @@ __global__ void k_pc_xinv(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   const double inv_tot = 1.0 / (double)(g.nx * g.ny * g.nz);
   double acc = 0;
   for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
-    const int q = idx / g.nx, i = idx % g.nx;
+    const int q = fdiv(idx, pl.n2mag), i = idx - q * g.nx;
     const long long row = row0 + q;
     if (row >= nrows) continue;
     const T *v = reinterpret_cast<const T *>(&zz[(i >> 1) * npen + q]);
@@ -864,7 +948,8 @@ void precondition_t(tpm_ctx *c, const double *r, const double *sc, double *z, do
   TPM_LAUNCH(c, "pcg_fft_y", k_fft_y<T2>, g.nz * ((g.nxh + npy - 1) / npy), ty, sy, g,
              c->fy, spec, npy, -1, skip);
   TPM_LAUNCH(c, "pcg_fft_z_solve", k_fft_z_solve<T2>, g.ny * ((g.nxh + npz - 1) / npz),
-             tz, sz, g, c->fz, spec, c->ax, c->ay, c->az, npz, skip);
+             tz, sz, g, c->fz, spec, c->ax, c->ay, c->az,
+             static_cast<const typename Cx<T2>::T *>(c->inv_mwn), npz, skip);
   TPM_LAUNCH(c, "pcg_fft_y", k_fft_y<T2>, g.nz * ((g.nxh + npy - 1) / npy), ty, sy, g,
              c->fy, spec, npy, +1, skip);
   TPM_LAUNCH(c, "pcg_fft_x_inv", k_pc_xinv<T2>, xblocks, tx, sx, g, c->fx, r2c, spec, r,
@@ -1075,7 +1160,8 @@ extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, doub
       int npen = pens_for(fz.n);
       int blocks = Ny * ((g.nxh + npen - 1) / npen);
       size_t smem = 2 * (size_t)npen * fz.n * sizeof(double2);
-      k_fft_z_solve<double2><<<blocks, kFftThreads, smem, st>>>(g, fz, spec, ax, ay, az, npen, nullptr);
+      k_fft_z_solve<double2><<<blocks, kFftThreads, smem, st>>>(g, fz, spec, ax, ay, az, nullptr, npen,
+                                                                 nullptr);
     }
     {
       int npen = pens_for(fy.n);

@@ -63,11 +63,16 @@ struct DevScalars {
   int it_sum;
 };
 
-// 1-D FFT plan in device memory: radices and exp(-2 pi i m / n) twiddles.
+// 1-D FFT plan in device memory: radices and exp(-2 pi i m / n) twiddles,
+// and multiply-high magic numbers (ceil(2^32/d), 0 for d = 1) for the integer
+// divisions of the pencil passes: by the span p of each stage, by n, 2n and
+// n + 1 (the real-to-complex x pass holds rows of 2n reals and n + 1 modes).
 struct FftPlan {
   int n;
   int nst;
   int radix[16];
+  unsigned pmag[16];
+  unsigned nmag, n2mag, nhmag;
   const double2 *tw64;  // n entries
   const float2 *tw32;   // n entries
 };
@@ -151,13 +156,16 @@ struct tpm_ctx {
   float2 *Cs2 = nullptr;    // 3n
   float2 *R0 = nullptr;     // n
   float *cc32 = nullptr;    // n
-  double *dP = nullptr;     // n
+  float2 *dP = nullptr;     // n
   bool rui32_stale = true;
   double2 *spec = nullptr;
   double *partials = nullptr;  // kRedBlocks * 4
   tpm::DevScalars *dsc = nullptr;
   tpm::DevScalars *hsc = nullptr;  // pinned mirror
   double *ax = nullptr, *ay = nullptr, *az = nullptr;  // modified wave number tables
+  // 1/(ax[kx] + ay[ky] + az[kz]) per half-spectrum mode (1 at the zero mode),
+  // double on the FP64 path and float on the mixed path
+  void *inv_mwn = nullptr;
   tpm::FftPlan fx, fy, fz;
   const double2 *r2c64 = nullptr;
   const float2 *r2c32 = nullptr;
