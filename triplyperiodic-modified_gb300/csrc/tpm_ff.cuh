@@ -92,6 +92,21 @@ __device__ __forceinline__ float2 ff_from_double(double x) {
   return make_float2(__uint_as_float(hb), __uint_as_float(__float_as_uint(lo) | sgn));
 }
 
+// x truncated to a float (within 2^-23 |x|; below 2^-126 a signed zero, from
+// 2^128 on an infinity of x's sign, nan for nan) by integer operations only:
+// the FP32 copy of an FP64 value without an FP64-pipe conversion
+__device__ __forceinline__ float ff_hi(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned int hw = (unsigned int)(b >> 32), lw = (unsigned int)b;
+  const int e = (int)((hw >> 20) & 0x7ffu);
+  const unsigned int sgn = hw & 0x80000000u;
+  unsigned int hb = sgn | ((unsigned int)(e - 896) << 23) | ((hw & 0xfffffu) << 3) | (lw >> 29);
+  hb = e < 897 ? sgn : hb;
+  hb = e > 1150 ? (sgn | 0x7f800000u | ((e == 2047 && ((hw & 0xfffffu) | lw)) ? 0x400000u : 0u))
+                : hb;
+  return __uint_as_float(hb);
+}
+
 // A float as a double, exactly, by integer operations only; subnormal floats
 // (below 2^-126) flush to a signed zero.
 __device__ __forceinline__ double ff_f2d(float f) {
@@ -102,5 +117,9 @@ __device__ __forceinline__ double ff_f2d(float f) {
   const unsigned long long bits = sgn | (ed << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
   return __longlong_as_double((long long)(ef == 0u ? sgn : bits));
 }
+
+// a normalised so that |lo| <= ulp(hi) / 2 (for pairs whose lo is already
+// small against hi, as ff_mul leaves them)
+__device__ __forceinline__ float2 ff_norm(float2 a) { return ff_fast_two_sum(a.x, a.y); }
 
 }  // namespace tpm

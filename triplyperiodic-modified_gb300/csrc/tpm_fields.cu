@@ -414,17 +414,10 @@ __global__ void k_poisson_rhs2(Grid g, const double *__restrict__ inv_rho,
 // 1/x to FP64 accuracy from an FP32 seed and two Newton steps (4 FMAs): on
 // GB300 an FP64 division costs several times that on the scarce FP64 pipe.
 __device__ __forceinline__ double rcp64(double x) {
-  double r = (double)__frcp_rn((float)x);
+  double r = ff_f2d(__frcp_rn(ff_hi(x)));  // seed without FP64-pipe conversions
   double e = __fma_rn(-x, r, 1.0);
   r = __fma_rn(r, e, r);
   e = __fma_rn(-x, r, 1.0);
-  return __fma_rn(r, e, r);
-}
-
-// 1/x to ~1e-14 relative: FP32 seed and one Newton step (2 FMAs)
-__device__ __forceinline__ double rcp64_1(double x) {
-  double r = (double)__frcp_rn((float)x);
-  double e = __fma_rn(-x, r, 1.0);
   return __fma_rn(r, e, r);
 }
 
@@ -464,6 +457,8 @@ __global__ void k_face_coeff_mixed(Grid g, const double *__restrict__ Rho_new,
                                    double *__restrict__ Cface, float2 *__restrict__ Cs2,
                                    double *__restrict__ Cs) {
   const double inv_d2[3] = {g.inv_dx2, g.inv_dy2, g.inv_dz2};
+  const float2 inv_d2f[3] = {ff_from_double(g.inv_dx2), ff_from_double(g.inv_dy2),
+                             ff_from_double(g.inv_dz2)};
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
@@ -471,11 +466,13 @@ __global__ void k_face_coeff_mixed(Grid g, const double *__restrict__ Rho_new,
     const double r = Rho_new[c];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const double clo = rcp64_1((r + Rho_new[nb.m[d]]) * 0.5);
+      // FP32 seed of 1/rho_face with no FP64-pipe conversion, one Newton step
+      const double h = (r + Rho_new[nb.m[d]]) * 0.5;
+      const double r0 = ff_f2d(__frcp_rn(ff_hi(h)));
+      const double clo = __fma_rn(r0, __fma_rn(-h, r0, 1.0), r0);
       Cface[d * g.n + c] = clo;
-      const double cs = clo * inv_d2[d];
-      Cs2[d * g.n + c] = ff_from_double(cs);
-      if (Cs) Cs[d * g.n + c] = cs;
+      Cs2[d * g.n + c] = ff_norm(ff_mul(ff_from_double(clo), inv_d2f[d]));
+      if (Cs) Cs[d * g.n + c] = clo * inv_d2[d];
     }
   }
 }
@@ -516,7 +513,7 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
       const double *R = RUn + d * g.n;
       const double u_lo = R[c] * clo;
       divu = fma(fma(R[nb.p[d]], chi, -u_lo), inv_d[d], divu);
-      msum += ((float)clo + (float)chi) * 0.5f;
+      msum += (ff_hi(clo) + ff_hi(chi)) * 0.5f;  // FP32 copies without FP64-pipe conversions
       if (tke_parts) usq += u_lo * u_lo;
     }
     double rhs = divu * a.inv_dtpre;
@@ -524,7 +521,7 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
     acc += rhs;
     const float ccf = -3.0f / msum;
     cc32[c] = ccf;
-    if (cc) cc[c] = (double)ccf;  // the PCG operator's copy
+    if (cc) cc[c] = ff_f2d(ccf);  // the PCG operator's copy
   }
   double bs = block_sum(acc, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = bs;
@@ -541,18 +538,21 @@ __global__ void k_face_velocity_mixed(Grid g, const float *__restrict__ RUi32,
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
-    const double r = Rho_int[c];
-    U[c] = RUi32[c] / (float)((r + Rho_int[at(g, wrap_m(q.i, g.nx), q.j, q.k)]) * 0.5);
-    U[g.n + c] = RUi32[g.n + c] / (float)((r + Rho_int[at(g, q.i, wrap_m(q.j, g.ny), q.k)]) * 0.5);
+    // the face density in FP32 (it only divides the FP32 momentum copy)
+    const float r = ff_hi(Rho_int[c]);
+    U[c] = RUi32[c] / ((r + ff_hi(Rho_int[at(g, wrap_m(q.i, g.nx), q.j, q.k)])) * 0.5f);
+    U[g.n + c] = RUi32[g.n + c] / ((r + ff_hi(Rho_int[at(g, q.i, wrap_m(q.j, g.ny), q.k)])) * 0.5f);
     U[2 * g.n + c] =
-        RUi32[2 * g.n + c] / (float)((r + Rho_int[at(g, q.i, q.j, wrap_m(q.k, g.nz))]) * 0.5);
+        RUi32[2 * g.n + c] / ((r + ff_hi(Rho_int[at(g, q.i, q.j, wrap_m(q.k, g.nz))])) * 0.5f);
   }
 }
 
+// FP32 copies of FP64 fields for the mixed path's stencils (truncated, by
+// integer operations)
 __global__ void k_to_float(const double *__restrict__ a, float *__restrict__ b, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    b[i] = (float)a[i];
+    b[i] = ff_hi(a[i]);
 }
 
 __global__ void k_to_double(const float *__restrict__ a, double *__restrict__ b, long long n) {
@@ -651,7 +651,7 @@ __global__ void k_project(Grid g, const double *__restrict__ P, double *__restri
                                              : RU_new[d * g.n + c] + b_new * G)
                                      : np1;
       RU_new[d * g.n + c] = nw;
-      if (RUn32) RUn32[d * g.n + c] = (float)nw;
+      if (RUn32) RUn32[d * g.n + c] = ff_hi(nw);
       acc[d] += np1;
     }
   }
