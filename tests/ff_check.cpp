@@ -68,7 +68,7 @@ int main() {
     else
       CHECK(d == (double)f, "f2d %08x", w);
   }
-  // TwoSum is exact; the product stays within 2^-44, the sloppy add within 2^-46
+  // TwoSum is exact; the product stays within 2^-45, the sloppy add within 2^-46
   for (int n = 0; n < 2000000; ++n) {
     float a = (float)(unit(rng) * std::ldexp(1.0, ex(rng) / 8));
     float c = (float)(unit(rng) * std::ldexp(1.0, ex(rng) / 8));
@@ -78,7 +78,7 @@ int main() {
     long double va = (long double)pa.x + pa.y, vb = (long double)pb.x + pb.y;
     float2 m = ff_mul(pa, pb);
     long double em = std::fabs((long double)m.x + m.y - va * vb);
-    CHECK(em <= std::ldexp((long double)std::fabs(va * vb), -44), "mul err %.3Lg", em);
+    CHECK(em <= std::ldexp((long double)std::fabs(va * vb), -45), "mul err %.3Lg", em);
     float2 pc = ff_from_double(va * (1.0 + 1e-3 * unit(rng)));  // close to pa
     float2 sb = ff_sub(pc, pa);
     long double es = std::fabs((long double)sb.x + sb.y - (((long double)pc.x + pc.y) - va));

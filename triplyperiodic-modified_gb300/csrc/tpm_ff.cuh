@@ -54,12 +54,14 @@ __device__ __forceinline__ float2 ff_add_f(float2 a, float b) {
   return ff_fast_two_sum(s.x, s.y + a.y);
 }
 
-// a * b, unnormalised: a.x b.x exactly (FMA) plus the cross terms, within
-// 2^-44 |a b| for pairs from ff_from_double (|lo| < 2^-23 |hi|: the dropped
-// a.y b.y and the roundings of the cross terms)
+// a * b, unnormalised: a.x b.x exactly (FMA) plus the other three partial
+// products, within 2^-45 |a b| for pairs from ff_from_double (|lo| < 2^-23
+// |hi|: the roundings of the cross terms).  a.y b.y is kept: for truncated
+// splits the low parts carry the sign of their values, so dropping it would
+// bias every product by up to 2^-46.
 __device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
   const float p = a.x * b.x;
-  float e = fmaf(a.x, b.x, -p);
+  float e = fmaf(a.y, b.y, fmaf(a.x, b.x, -p));
   e = fmaf(a.x, b.y, e);
   e = fmaf(a.y, b.x, e);
   return make_float2(p, e);
@@ -117,6 +119,9 @@ __device__ __forceinline__ double ff_f2d(float f) {
   const unsigned long long bits = sgn | (ed << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
   return __longlong_as_double((long long)(ef == 0u ? sgn : bits));
 }
+
+// hi + lo as a double (two exact conversions and one FP64 addition)
+__device__ __forceinline__ double ff_to_double(float2 a) { return ff_f2d(a.x) + ff_f2d(a.y); }
 
 // a normalised so that |lo| <= ulp(hi) / 2 (for pairs whose lo is already
 // small against hi, as ff_mul leaves them)

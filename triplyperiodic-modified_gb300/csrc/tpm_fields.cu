@@ -477,10 +477,22 @@ __global__ void k_face_coeff_mixed(Grid g, const double *__restrict__ Rho_new,
   }
 }
 
-// k_poisson_rhs of the mixed path: FP64 right-hand side (it feeds the FP64
-// residual), U = RU*C with the face coefficients above; the preconditioner
-// scale cc is FP32 (it sets the rate of the Richardson iteration, not its
-// fixed point).
+// k_poisson_rhs of the mixed path, in float-float pairs (tpm_ff.cuh) on the
+// FP32 pipe: every FP64 input is split into a pair by integer operations,
+// and the thermal divergence dv = (k/Cp) lap(1/rho) + coef (Q - mean Q) and
+// div(RU C) - dv are formed and summed as pairs (the neighbour differences of
+// 1/rho and of the face fluxes through the exact-difference subtraction; each
+// face's flux is the same pair for both of its cells, so the fluxes still
+// telescope).  The pairs carry about 2^-47 of each flux, which leaves the
+// projection a divergence error near 1e-12, under the 1e-10 the mixed path
+// keeps.  The last factor, 1/(dt pre), is an FP64 product: a right-hand side
+// rebuilt from a pair has a fixed pattern in its low bits, which would bias
+// the rounding when the refinement splits mean - RHS into pairs again and
+// leave its residual a nonzero mean that the iteration cannot remove.  FP64
+// operations per cell: four (three more for the kinetic energy sum of the
+// last stage) against about twenty-four for the same sums in FP64.  The
+// preconditioner scale cc is FP32 (it sets the rate of the Richardson
+// iteration, not its fixed point).
 __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
                                     const double *__restrict__ Q, const double *__restrict__ RUn,
                                     const double *__restrict__ Cface,
@@ -489,34 +501,46 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
                                     double *__restrict__ cc, double *__restrict__ partials,
                                     double *__restrict__ tke_parts, PoisArgs a) {
   __shared__ double sh[kThreads];
-  const double coef = s->coef_div, meanQ = s->mean_Q;
-  const double inv_d[3] = {g.inv_dx, g.inv_dy, g.inv_dz};
+  const float2 coef = ff_from_double(s->coef_div), meanQ = ff_from_double(s->mean_Q);
+  const float2 kCp = ff_from_double(a.kCp);
+  const float2 inv_d2[3] = {ff_from_double(g.inv_dx2), ff_from_double(g.inv_dy2),
+                            ff_from_double(g.inv_dz2)};
+  const float2 inv_d[3] = {ff_from_double(g.inv_dx), ff_from_double(g.inv_dy),
+                           ff_from_double(g.inv_dz)};
   double acc = 0, usq = 0;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
     Nbr nb = nbr_of(g, q);
-    // FMA chains throughout (this kernel is FP64-pipe bound; the mixed path
-    // has no bitwise-parity constraint)
-    double ir = inv_rho[c];
-    double lap = (fma(-2.0, ir, inv_rho[nb.p[0]]) + inv_rho[nb.m[0]]) * g.inv_dx2;
-    lap = fma(fma(-2.0, ir, inv_rho[nb.p[1]]) + inv_rho[nb.m[1]], g.inv_dy2, lap);
-    lap = fma(fma(-2.0, ir, inv_rho[nb.p[2]]) + inv_rho[nb.m[2]], g.inv_dz2, lap);
-    double Qc = a.cooling ? Q[c] - meanQ : Q[c];
-    double dv = fma(a.kCp, lap, coef * Qc);
-    divg[c] = dv;
-    double divu = -dv;
+    const float2 ir = ff_from_double(inv_rho[c]);
+    float2 lap = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float2 sec = ff_add(ff_sub(ff_from_double(inv_rho[nb.p[d]]), ir),
+                                ff_sub(ff_from_double(inv_rho[nb.m[d]]), ir));
+      lap = ff_add(lap, ff_mul(sec, inv_d2[d]));
+    }
+    float2 Qc = ff_from_double(Q[c]);
+    if (a.cooling) Qc = ff_sub(Qc, meanQ);
+    const float2 dv = ff_add(ff_mul(kCp, lap), ff_mul(coef, Qc));
+    divg[c] = ff_to_double(dv);
+    float2 divu = make_float2(-dv.x, -dv.y);
     float msum = 0.f;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const double clo = Cface[d * g.n + c], chi = Cface[d * g.n + nb.p[d]];
+      const float2 clo = ff_from_double(Cface[d * g.n + c]);
+      const float2 chi = ff_from_double(Cface[d * g.n + nb.p[d]]);
       const double *R = RUn + d * g.n;
-      const double u_lo = R[c] * clo;
-      divu = fma(fma(R[nb.p[d]], chi, -u_lo), inv_d[d], divu);
-      msum += (ff_hi(clo) + ff_hi(chi)) * 0.5f;  // FP32 copies without FP64-pipe conversions
-      if (tke_parts) usq += u_lo * u_lo;
+      const float2 u_lo = ff_norm(ff_mul(ff_from_double(R[c]), clo));
+      const float2 u_hi = ff_norm(ff_mul(ff_from_double(R[nb.p[d]]), chi));
+      divu = ff_add(divu, ff_mul(ff_sub(u_hi, u_lo), inv_d[d]));
+      msum += (clo.x + chi.x) * 0.5f;
+      if (tke_parts) {
+        const double ul = ff_f2d(u_lo.x);
+        usq = fma(ul, ul, usq);
+      }
     }
-    double rhs = divu * a.inv_dtpre;
+    const double rhs = ff_to_double(divu) * a.inv_dtpre;
     RHS[c] = rhs;
     acc += rhs;
     const float ccf = -3.0f / msum;
