@@ -16,6 +16,7 @@
 //    reproducible run to run; they differ from the reference's particle-order
 //    sums only by FP64 reassociation.
 #include "tpm_internal.cuh"
+#include "tpm_ff.cuh"
 #include "tpm_reduce.cuh"
 
 namespace tpm {
@@ -71,13 +72,15 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
       vg = yl * (double)U[g.n + at(g, i0, wrap_p(j0, g.ny), k0)] + (1 - yl) * (double)U[g.n + c0];
       wg = zl * (double)U[2 * g.n + at(g, i0, j0, wrap_p(k0, g.nz))] +
            (1 - zl) * (double)U[2 * g.n + c0];
-    } else {  // FP32 interpolation of the FP32 face velocity (mixed path)
-      const float xf = (float)xl, yf = (float)yl, zf = (float)zl;
-      ug = (double)(xf * (float)U[at(g, wrap_p(i0, g.nx), j0, k0)] + (1 - xf) * (float)U[c0]);
-      vg = (double)(yf * (float)U[g.n + at(g, i0, wrap_p(j0, g.ny), k0)] +
-                    (1 - yf) * (float)U[g.n + c0]);
-      wg = (double)(zf * (float)U[2 * g.n + at(g, i0, j0, wrap_p(k0, g.nz))] +
-                    (1 - zf) * (float)U[2 * g.n + c0]);
+    } else {  // FP32 interpolation of the FP32 face velocity (mixed path); the
+      // FP64<->FP32 conversions by integer operations (the conversion
+      // instructions issue on the FP64 pipe)
+      const float xf = ff_hi(xl), yf = ff_hi(yl), zf = ff_hi(zl);
+      ug = ff_f2d(xf * (float)U[at(g, wrap_p(i0, g.nx), j0, k0)] + (1 - xf) * (float)U[c0]);
+      vg = ff_f2d(yf * (float)U[g.n + at(g, i0, wrap_p(j0, g.ny), k0)] +
+                  (1 - yf) * (float)U[g.n + c0]);
+      wg = ff_f2d(zf * (float)U[2 * g.n + at(g, i0, j0, wrap_p(k0, g.nz))] +
+                  (1 - zf) * (float)U[2 * g.n + c0]);
     }
     // ---- update_position (particle.cpp:314-338) ----
     // (the mixed path, TU = float, accumulates with FMAs; the FP64 path keeps
@@ -113,12 +116,23 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     // ---- part2gas_velocity payload at x_int (particle.cpp:494-520) ----
     if (a.twc) {
       key_t[p] = (int32_t)c0;
-      pay_t[0 * np + p] = (TP)((1 - xl) * rhs[0]);
-      pay_t[1 * np + p] = (TP)(xl * rhs[0]);
-      pay_t[2 * np + p] = (TP)((1 - yl) * rhs[1]);
-      pay_t[3 * np + p] = (TP)(yl * rhs[1]);
-      pay_t[4 * np + p] = (TP)((1 - zl) * rhs[2]);
-      pay_t[5 * np + p] = (TP)(zl * rhs[2]);
+      if (kFma) {  // FP32 payload (mixed path): FP32 products of truncated copies
+        const float xf = ff_hi(xl), yf = ff_hi(yl), zf = ff_hi(zl);
+        const float r0 = ff_hi(rhs[0]), r1 = ff_hi(rhs[1]), r2 = ff_hi(rhs[2]);
+        pay_t[0 * np + p] = (TP)((1 - xf) * r0);
+        pay_t[1 * np + p] = (TP)(xf * r0);
+        pay_t[2 * np + p] = (TP)((1 - yf) * r1);
+        pay_t[3 * np + p] = (TP)(yf * r1);
+        pay_t[4 * np + p] = (TP)((1 - zf) * r2);
+        pay_t[5 * np + p] = (TP)(zf * r2);
+      } else {
+        pay_t[0 * np + p] = (TP)((1 - xl) * rhs[0]);
+        pay_t[1 * np + p] = (TP)(xl * rhs[0]);
+        pay_t[2 * np + p] = (TP)((1 - yl) * rhs[1]);
+        pay_t[3 * np + p] = (TP)(yl * rhs[1]);
+        pay_t[4 * np + p] = (TP)((1 - zl) * rhs[2]);
+        pay_t[5 * np + p] = (TP)(zl * rhs[2]);
+      }
     }
     // ---- Send_Recv on one rank = periodic wrap (particle.cpp:58-104, 150-250) ----
     const double L[3] = {g.Lx, g.Ly, g.Lz};
@@ -166,20 +180,20 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
       // one); the differences are FP64, the small weighted sum FP32, so the
       // heat rate - a difference of nearly equal temperatures - keeps its
       // relative accuracy
-      const float xf = (float)x_l, yf = (float)y_l, zf = (float)z_l;
-      const float d0 = (float)(Tgas[at(g, i1, j1, k1)] - Tnew);
-      const float d1 = (float)(Tgas[at(g, im, j1, k1)] - Tnew);
-      const float d2 = (float)(Tgas[at(g, i1, jm, k1)] - Tnew);
-      const float d3 = (float)(Tgas[at(g, i1, j1, km)] - Tnew);
-      const float d4 = (float)(Tgas[at(g, im, jm, k1)] - Tnew);
-      const float d5 = (float)(Tgas[at(g, im, j1, km)] - Tnew);
-      const float d6 = (float)(Tgas[at(g, i1, jm, km)] - Tnew);
-      const float d7 = (float)(Tgas[at(g, im, jm, km)] - Tnew);
+      const float xf = ff_hi(x_l), yf = ff_hi(y_l), zf = ff_hi(z_l);
+      const float d0 = ff_hi(Tgas[at(g, i1, j1, k1)] - Tnew);
+      const float d1 = ff_hi(Tgas[at(g, im, j1, k1)] - Tnew);
+      const float d2 = ff_hi(Tgas[at(g, i1, jm, k1)] - Tnew);
+      const float d3 = ff_hi(Tgas[at(g, i1, j1, km)] - Tnew);
+      const float d4 = ff_hi(Tgas[at(g, im, jm, k1)] - Tnew);
+      const float d5 = ff_hi(Tgas[at(g, im, j1, km)] - Tnew);
+      const float d6 = ff_hi(Tgas[at(g, i1, jm, km)] - Tnew);
+      const float d7 = ff_hi(Tgas[at(g, im, jm, km)] - Tnew);
       const float sum = xf * yf * zf * d0 + (1 - xf) * yf * zf * d1 + xf * (1 - yf) * zf * d2 +
                         xf * yf * (1 - zf) * d3 + (1 - xf) * (1 - yf) * zf * d4 +
                         (1 - xf) * yf * (1 - zf) * d5 + xf * (1 - yf) * (1 - zf) * d6 +
                         (1 - xf) * (1 - yf) * (1 - zf) * d7;
-      rt = (double)sum * a.iTth;
+      rt = ff_f2d(sum) * a.iTth;
     }
     rhs_t[p] = rt;
     key_r[p] = (int32_t)at(g, i1, j1, k1);
@@ -408,6 +422,15 @@ __global__ void k_dep_momentum(Grid g, const int32_t *__restrict__ starts,
 // (weights) that the next substep deposits at the same positions (its x_int
 // is this x_new).  Weights are built per sorted slot from the unsorted
 // payload; the sums keep the order of k_dep_sum8.
+// FP64 <-> TW for the deposit weights: for TW = float by integer operations
+// (truncation; the conversion instructions issue on the FP64 pipe)
+template <typename TW>
+__device__ __forceinline__ TW to_tw(double x) { return (TW)x; }
+template <>
+__device__ __forceinline__ float to_tw<float>(double x) { return ff_hi(x); }
+__device__ __forceinline__ double from_tw(double x) { return x; }
+__device__ __forceinline__ double from_tw(float x) { return ff_f2d(x); }
+
 template <typename TW>
 __global__ void k_cic_weights2(int64_t np, const int32_t *__restrict__ perm,
                                const double *__restrict__ pay, TW *__restrict__ wq,
@@ -415,8 +438,8 @@ __global__ void k_cic_weights2(int64_t np, const int32_t *__restrict__ perm,
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < np;
        s += (int64_t)gridDim.x * blockDim.x) {
     const int32_t p = perm[s];
-    const TW xl = (TW)pay[p], yl = (TW)pay[np + p], zl = (TW)pay[2 * np + p];
-    const TW r = (TW)pay[3 * np + p];
+    const TW xl = to_tw<TW>(pay[p]), yl = to_tw<TW>(pay[np + p]), zl = to_tw<TW>(pay[2 * np + p]);
+    const TW r = to_tw<TW>(pay[3 * np + p]);
     const TW fx[2] = {xl, 1 - xl}, fy[2] = {yl, 1 - yl}, fz[2] = {zl, 1 - zl};
 #pragma unroll
     for (int dy = 0; dy < 2; ++dy)
@@ -461,9 +484,10 @@ __global__ void k_dep_sum8x2(Grid g, const int32_t *__restrict__ starts, const T
             ac += wc[o + s];
           }
         }
-    Q[c] = (double)aq;
-    C[c] = (double)ac;
-    bsum += (double)aq;
+    const double qd = from_tw(aq);
+    Q[c] = qd;
+    C[c] = from_tw(ac);
+    bsum += qd;
   }
   double b = block_sum(bsum, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = b;
