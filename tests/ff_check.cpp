@@ -90,6 +90,31 @@ int main() {
     long double ea = std::fabs((long double)ad.x + ad.y - (va + vb));
     CHECK(ea <= std::ldexp(std::fabs(va) + std::fabs(vb), -46), "add err %.3Lg", ea);
   }
+  // trunc / fraction / half decision from the bits of a double
+  for (int n = 0; n < 2000000; ++n) {
+    const double u = (rng() & 1 ? -1.0 : 1.0) *
+                     std::ldexp(mant(rng), (int)(rng() % 40) - 20);  // 2^-20 .. 2^20
+    int ip;
+    float fr;
+    bool up;
+    ff_int_frac(u, ip, fr, up);
+    const double t = std::trunc(u), f = u - t;  // exact
+    CHECK(ip == (int)t, "trunc %.17g -> %d", u, ip);
+    CHECK(std::fabs((double)fr - f) <= std::ldexp(std::fabs(f), -23) && std::fabs((double)fr) <= std::fabs(f),
+          "frac %.17g -> %.9g", u, (double)fr);
+    CHECK(up == (std::fabs(f) >= 0.5), "half %.17g", u);
+  }
+  for (double u : {0.0, 0.5, 1.0, 2.5, -2.5, 3.0, -0.25, 255.99999999999997}) {
+    int ip;
+    float fr;
+    bool up;
+    ff_int_frac(u, ip, fr, up);
+    const double t = std::trunc(u), f = u - t;
+    CHECK(ip == (int)t && std::fabs((double)fr) <= std::fabs(f) &&
+              std::fabs((double)fr - f) <= std::ldexp(std::fabs(f), -23) &&
+              up == (std::fabs(f) >= 0.5),
+          "edge %.17g -> %d %.9g %d", u, ip, (double)fr, (int)up);
+  }
   if (fails) {
     std::printf("%d failures\n", fails);
     return 1;

@@ -3,8 +3,9 @@
 against a stand-in cuda_runtime.h for its bit-cast intrinsics, with FP
 contraction off, and tests/ff_check.cpp checks the double split (2^-48 bound,
 truncated high part, zero / tiny / overflow / inf / nan), the exact float to
-double conversion, TwoSum's exactness and the bounds of the product, the sums
-and the difference of close pairs."""
+double conversion, TwoSum's exactness, the bounds of the product, the sums
+and the difference of close pairs, and the integer part / fraction / half
+decision read from a double's bits."""
 import os
 import shutil
 import subprocess
@@ -26,6 +27,7 @@ inline double __longlong_as_double(long long v) { double r; std::memcpy(&r, &v, 
 inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
 inline float __uint2float_rn(unsigned u) { return (float)u; }
+inline int __clzll(long long x) { return __builtin_clzll((unsigned long long)x); }
 """
 
 

@@ -120,6 +120,41 @@ __device__ __forceinline__ double ff_f2d(float f) {
   return __longlong_as_double((long long)(ef == 0u ? sgn : bits));
 }
 
+// u = ip + fr with ip = trunc(u) (toward zero) and fr = u - ip truncated to a
+// float, and up = (|fr| >= 1/2) decided on the exact bits; by integer
+// operations only (the FP64 route is a truncating conversion, a conversion
+// back and a subtraction, all on the FP64 pipe).  For |u| < 2^31; beyond,
+// ip saturates and fr is 0.
+__device__ __forceinline__ void ff_int_frac(double u, int &ip, float &fr, bool &up) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(u);
+  const bool neg = (b >> 63) != 0;
+  const int e = (int)((b >> 52) & 0x7ffu) - 1023;  // |u| in [2^e, 2^(e+1))
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  // e >= 0: integer part m >> (52 - e), fraction bits fb worth fb * 2^-(52 - e)
+  const int sh = 52 - (e < 0 ? 0 : (e > 30 ? 30 : e));
+  const unsigned long long fb = m & ((1ull << sh) - 1ull);
+  const int lz = __clzll((long long)(fb | 1ull));
+  const unsigned long long nb = (fb << lz) << 1;  // fraction bits after the leading one
+  const unsigned int fbits =
+      fb ? (((unsigned int)(63 - lz - sh + 127) << 23) | (unsigned int)(nb >> 41)) : 0u;
+  int ia = (int)(m >> sh);
+  float fa = __uint_as_float(fbits);
+  bool half = ((fb >> (sh - 1)) & 1ull) != 0;
+  if (e < 0) {  // |u| < 1: no integer part, the fraction is |u|
+    ia = 0;
+    fa = __uint_as_float(__float_as_uint(ff_hi(u)) & 0x7fffffffu);
+    half = e == -1;
+  }
+  if (e > 30) {
+    ia = 0x7fffffff;
+    fa = 0.f;
+    half = false;
+  }
+  ip = neg ? -ia : ia;
+  fr = neg ? -fa : fa;
+  up = half;
+}
+
 // hi + lo as a double (two exact conversions and one FP64 addition)
 __device__ __forceinline__ double ff_to_double(float2 a) { return ff_f2d(a.x) + ff_f2d(a.y); }
 

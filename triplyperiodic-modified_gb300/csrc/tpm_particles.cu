@@ -57,13 +57,28 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
                        double *__restrict__ pay_r) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
        p += (int64_t)gridDim.x * blockDim.x) {
+    constexpr bool kMixed = sizeof(TU) == sizeof(float);
     const double xi = ps.in[0][p], yi = ps.in[1][p], zi = ps.in[2][p];
     const double ui = ps.in[3][p], vi = ps.in[4][p], wi = ps.in[5][p];
     // ---- gas2part_velocity at x_int (particle.cpp:340-360) ----
-    const int tx = (int)(xi * g.idx), ty = (int)(yi * g.idy), tz = (int)(zi * g.idz);
-    const double xl = (xi * g.idx - ((int)(xi * g.idx)));
-    const double yl = (yi * g.idy - ((int)(yi * g.idy)));
-    const double zl = (zi * g.idz - ((int)(zi * g.idz)));
+    int tx, ty, tz;
+    double xl = 0, yl = 0, zl = 0;     // FP64 path: fractions in FP64
+    float xf_i = 0, yf_i = 0, zf_i = 0;  // mixed path: the same fractions truncated to FP32
+    if constexpr (kMixed) {
+      // trunc(x/d) and its fraction from the bits of the FP64 product (the
+      // same cell as the FP64 route, no FP64-pipe conversions)
+      bool h;
+      ff_int_frac(xi * g.idx, tx, xf_i, h);
+      ff_int_frac(yi * g.idy, ty, yf_i, h);
+      ff_int_frac(zi * g.idz, tz, zf_i, h);
+    } else {
+      tx = (int)(xi * g.idx);
+      ty = (int)(yi * g.idy);
+      tz = (int)(zi * g.idz);
+      xl = (xi * g.idx - ((int)(xi * g.idx)));
+      yl = (yi * g.idy - ((int)(yi * g.idy)));
+      zl = (zi * g.idz - ((int)(zi * g.idz)));
+    }
     const int i0 = wrap_any(tx, g.nx), j0 = wrap_any(ty, g.ny), k0 = wrap_any(tz, g.nz);
     const long long c0 = at(g, i0, j0, k0);
     double ug, vg, wg;
@@ -75,7 +90,7 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     } else {  // FP32 interpolation of the FP32 face velocity (mixed path); the
       // FP64<->FP32 conversions by integer operations (the conversion
       // instructions issue on the FP64 pipe)
-      const float xf = ff_hi(xl), yf = ff_hi(yl), zf = ff_hi(zl);
+      const float xf = xf_i, yf = yf_i, zf = zf_i;
       ug = ff_f2d(xf * (float)U[at(g, wrap_p(i0, g.nx), j0, k0)] + (1 - xf) * (float)U[c0]);
       vg = ff_f2d(yf * (float)U[g.n + at(g, i0, wrap_p(j0, g.ny), k0)] +
                   (1 - yf) * (float)U[g.n + c0]);
@@ -117,7 +132,7 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     if (a.twc) {
       key_t[p] = (int32_t)c0;
       if (kFma) {  // FP32 payload (mixed path): FP32 products of truncated copies
-        const float xf = ff_hi(xl), yf = ff_hi(yl), zf = ff_hi(zl);
+        const float xf = xf_i, yf = yf_i, zf = zf_i;
         const float r0 = ff_hi(rhs[0]), r1 = ff_hi(rhs[1]), r2 = ff_hi(rhs[2]);
         pay_t[0 * np + p] = (TP)((1 - xf) * r0);
         pay_t[1 * np + p] = (TP)(xf * r0);
@@ -139,7 +154,14 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     const double hi[3] = {g.xh, g.yh, g.zh};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      if (xn[d] > hi[d] || xn[d] < 0) {
+      // mixed path: the two tests on the bit patterns (integer compares; for
+      // hi > 0, x > hi iff the signed patterns compare so, and x < 0 iff the
+      // sign is set on a nonzero magnitude)
+      const long long bx_ = __double_as_longlong(xn[d]);
+      const bool out = kMixed ? (bx_ > __double_as_longlong(hi[d]) ||
+                                 (unsigned long long)bx_ > 0x8000000000000000ull)
+                              : (xn[d] > hi[d] || xn[d] < 0);
+      if (out) {
         if (xn[d] > L[d]) {
           xn[d] -= L[d];
           xb[d] -= L[d];
@@ -156,11 +178,36 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
       ps.nw[d][p] = xn[d];
     }
     // ---- gas2part_Temp_new + Compute_RHS_Temp_new at x_new (particle.cpp:430-474) ----
-    const int ri = (int)(round(xn[0] * g.idx)), rj = (int)(round(xn[1] * g.idy)),
-              rk = (int)(round(xn[2] * g.idz));
-    const double x_l = xn[0] * g.idx - ri + 0.5;
-    const double y_l = xn[1] * g.idy - rj + 0.5;
-    const double z_l = xn[2] * g.idz - rk + 0.5;
+    int ri, rj, rk;
+    double x_l, y_l, z_l;
+    float xl_f[3] = {0, 0, 0};  // mixed: the fractions in FP32
+    if constexpr (kMixed) {
+      // round(x/d) (half away from zero) and x/d - round + 1/2 from the bits
+      // of the FP64 product
+      const double u[3] = {xn[0] * g.idx, xn[1] * g.idy, xn[2] * g.idz};
+      int r[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        int ip;
+        float fr;
+        bool up;
+        ff_int_frac(u[d], ip, fr, up);
+        const bool neg = __double_as_longlong(u[d]) < 0;  // sign bit, no FP64 compare
+        r[d] = ip + (up ? (neg ? -1 : 1) : 0);
+        xl_f[d] = fr + 0.5f + (up ? (neg ? 1.f : -1.f) : 0.f);
+      }
+      ri = r[0]; rj = r[1]; rk = r[2];
+      x_l = ff_f2d(xl_f[0]);
+      y_l = ff_f2d(xl_f[1]);
+      z_l = ff_f2d(xl_f[2]);
+    } else {
+      ri = (int)(round(xn[0] * g.idx));
+      rj = (int)(round(xn[1] * g.idy));
+      rk = (int)(round(xn[2] * g.idz));
+      x_l = xn[0] * g.idx - ri + 0.5;
+      y_l = xn[1] * g.idy - rj + 0.5;
+      z_l = xn[2] * g.idz - rk + 0.5;
+    }
     const int i1 = wrap_any(ri, g.nx), im = wrap_any(ri - 1, g.nx);
     const int j1 = wrap_any(rj, g.ny), jm = wrap_any(rj - 1, g.ny);
     const int k1 = wrap_any(rk, g.nz), km = wrap_any(rk - 1, g.nz);
@@ -180,15 +227,22 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
       // one); the differences are FP64, the small weighted sum FP32, so the
       // heat rate - a difference of nearly equal temperatures - keeps its
       // relative accuracy
-      const float xf = ff_hi(x_l), yf = ff_hi(y_l), zf = ff_hi(z_l);
-      const float d0 = ff_hi(Tgas[at(g, i1, j1, k1)] - Tnew);
-      const float d1 = ff_hi(Tgas[at(g, im, j1, k1)] - Tnew);
-      const float d2 = ff_hi(Tgas[at(g, i1, jm, k1)] - Tnew);
-      const float d3 = ff_hi(Tgas[at(g, i1, j1, km)] - Tnew);
-      const float d4 = ff_hi(Tgas[at(g, im, jm, k1)] - Tnew);
-      const float d5 = ff_hi(Tgas[at(g, im, j1, km)] - Tnew);
-      const float d6 = ff_hi(Tgas[at(g, i1, jm, km)] - Tnew);
-      const float d7 = ff_hi(Tgas[at(g, im, jm, km)] - Tnew);
+      // (the differences from split pairs: the high parts of two close
+      // temperatures subtract exactly, the low parts add their remainder)
+      const float xf = xl_f[0], yf = xl_f[1], zf = xl_f[2];
+      const float2 tn = ff_from_double(Tnew);
+      auto dT = [&](long long cell) {
+        const float2 t = ff_from_double(Tgas[cell]);
+        return (t.x - tn.x) + (t.y - tn.y);
+      };
+      const float d0 = dT(at(g, i1, j1, k1));
+      const float d1 = dT(at(g, im, j1, k1));
+      const float d2 = dT(at(g, i1, jm, k1));
+      const float d3 = dT(at(g, i1, j1, km));
+      const float d4 = dT(at(g, im, jm, k1));
+      const float d5 = dT(at(g, im, j1, km));
+      const float d6 = dT(at(g, i1, jm, km));
+      const float d7 = dT(at(g, im, jm, km));
       const float sum = xf * yf * zf * d0 + (1 - xf) * yf * zf * d1 + xf * (1 - yf) * zf * d2 +
                         xf * yf * (1 - zf) * d3 + (1 - xf) * (1 - yf) * zf * d4 +
                         (1 - xf) * yf * (1 - zf) * d5 + xf * (1 - yf) * (1 - zf) * d6 +
