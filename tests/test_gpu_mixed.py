@@ -83,3 +83,29 @@ def test_mixed_matches_fp64_gpu_128(capi):
     pm, pf = m.download_particles("base"), f.download_particles("base")
     for q in inputs.PQ:
         assert rel_err(pm[q], pf[q]) <= TOL_MIXED, q
+
+
+def test_mixed_keeps_the_callers_particle_order(capi):
+    """The mixed path keeps its particles in cell order in memory (a
+    permutation at every step boundary); every transfer is in the caller's
+    order: flags come back unchanged, per-particle Stokes times stay with
+    their particles, and each particle matches the FP64 path's."""
+    p, s = setup(32, 5000, seed=11, heat=0.5, precision=P.PREC_MIXED)
+    rng = np.random.default_rng(5)
+    s.part["flag"] = rng.permutation(s.npart).astype(np.int32)
+    tau = rng.uniform(0.05, 0.2, s.npart)
+    out = []
+    for prec in (P.PREC_MIXED, P.PREC_FP64):
+        ctx = capi.Context(p.replace(precision=prec), s.npart)
+        ctx.load(s)
+        ctx.set_tau(tau)
+        ctx.initialize()
+        ctx.run(4)
+        ctx.sync()
+        out.append((ctx.download_particles("base"), ctx.download_rhs_t()))
+    (pm, rm), (pf, rf) = out
+    assert np.array_equal(pm["flag"], s.part["flag"])
+    for q in inputs.PQ:
+        assert rel_err(pm[q], pf[q]) <= TOL_MIXED, q
+        assert np.abs(pm[q] - pf[q]).max() <= 1e-4 * np.abs(pf[q]).max(), q
+    assert rel_err(rm, rf) <= TOL_MIXED

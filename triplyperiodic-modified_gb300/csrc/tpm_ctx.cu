@@ -257,6 +257,7 @@ void end_step(tpm_ctx *c) {
   c->num_timestep++;
   c->np1_is_base = true;
   c->stepped = true;
+  tpm::particle_reorder(c);  // mixed path: cell order of the stage-3 positions
 }
 
 }  // namespace
@@ -414,6 +415,15 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->pay_t = dalloc<double>(c, 6 * (size_t)np);
     c->pay_t_s = dalloc<double>(c, 6 * (size_t)np);
     c->pay_r = dalloc<double>(c, 4 * (size_t)np);
+    if (p->precision == TPM_PREC_MIXED && np > 0) {  // particles kept in cell order
+      c->reorder = true;
+      c->pid = dalloc<int32_t>(c, np);
+      c->pid2 = dalloc<int32_t>(c, np);
+      c->flag2 = dalloc<int32_t>(c, np);
+      c->rhs_t2 = dalloc<double>(c, np);
+      c->pstage = dalloc<double>(c, np);
+      tpm::particles_reorder_init(c);
+    }
     c->w8 = dalloc<double>(c, 16 * (size_t)np);
     c->C_next = dalloc<double>(c, n);
     if (p->Solver == 2) tpm::pcg_alloc(c);
@@ -533,12 +543,8 @@ int tpm_upload_particles(tpm_ctx *c, int set, const double *x, const double *y, 
     if (set == TPM_PSET_BASE || set == TPM_PSET_NP1) materialize_np1(c);
     const double *src[7] = {x, y, z, u, v, w, T};
     for (int q = 0; q < 7; ++q)
-      if (src[q] && c->np)
-        TPM_CUDA_TRY(cudaMemcpyAsync(c->pq[set][q], src[q], sizeof(double) * c->np,
-                                     cudaMemcpyHostToDevice, c->stream));
-    if (flag && c->np)
-      TPM_CUDA_TRY(cudaMemcpyAsync(c->flag, flag, sizeof(int32_t) * c->np, cudaMemcpyHostToDevice,
-                                   c->stream));
+      if (src[q]) tpm::particles_from_host(c, c->pq[set][q], src[q], 8);
+    if (flag) tpm::particles_from_host(c, c->flag, flag, 4);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return TPM_OK;
   });
@@ -551,12 +557,8 @@ int tpm_download_particles(tpm_ctx *c, int set, double *x, double *y, double *z,
     int s = (set == TPM_PSET_NP1 && c->np1_is_base) ? TPM_PSET_BASE : set;
     double *dst[7] = {x, y, z, u, v, w, T};
     for (int q = 0; q < 7; ++q)
-      if (dst[q] && c->np)
-        TPM_CUDA_TRY(cudaMemcpyAsync(dst[q], c->pq[s][q], sizeof(double) * c->np,
-                                     cudaMemcpyDeviceToHost, c->stream));
-    if (flag && c->np)
-      TPM_CUDA_TRY(cudaMemcpyAsync(flag, c->flag, sizeof(int32_t) * c->np, cudaMemcpyDeviceToHost,
-                                   c->stream));
+      if (dst[q]) tpm::particles_to_host(c, dst[q], c->pq[s][q], 8);
+    if (flag) tpm::particles_to_host(c, flag, c->flag, 4);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return TPM_OK;
   });
@@ -565,9 +567,7 @@ int tpm_download_particles(tpm_ctx *c, int set, double *x, double *y, double *z,
 int tpm_download_particle_rhs_t(tpm_ctx *c, double *rhs_t) {
   return guarded(c, [&]() -> int {
     if (!rhs_t) return fail(c, TPM_ERR_ARG, "null host buffer");
-    if (c->np)
-      TPM_CUDA_TRY(cudaMemcpyAsync(rhs_t, c->rhs_t, sizeof(double) * c->np, cudaMemcpyDeviceToHost,
-                                   c->stream));
+    tpm::particles_to_host(c, rhs_t, c->rhs_t, 8);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return TPM_OK;
   });
@@ -576,9 +576,7 @@ int tpm_download_particle_rhs_t(tpm_ctx *c, double *rhs_t) {
 int tpm_upload_particle_rhs_t(tpm_ctx *c, const double *rhs_t) {
   return guarded(c, [&]() -> int {
     if (!rhs_t) return fail(c, TPM_ERR_ARG, "null host buffer");
-    if (c->np)
-      TPM_CUDA_TRY(cudaMemcpyAsync(c->rhs_t, rhs_t, sizeof(double) * c->np, cudaMemcpyHostToDevice,
-                                   c->stream));
+    tpm::particles_from_host(c, c->rhs_t, rhs_t, 8);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return TPM_OK;
   });
@@ -593,9 +591,8 @@ int tpm_set_particle_tau(tpm_ctx *c, const double *tau) {
     for (int64_t i = 0; i < c->np; ++i)
       if (!(tau[i] > 0)) return fail(c, TPM_ERR_ARG, "particle relaxation times must be > 0");
     if (!c->tau_buf) c->tau_buf = dalloc<double>(c, c->np);
-    if (c->np)
-      TPM_CUDA_TRY(cudaMemcpyAsync(c->tau_buf, tau, sizeof(double) * c->np, cudaMemcpyHostToDevice,
-                                   c->stream));
+    if (c->reorder && !c->tau2) c->tau2 = dalloc<double>(c, c->np);
+    tpm::particles_from_host(c, c->tau_buf, tau, 8);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->tau = c->tau_buf;
     return TPM_OK;
@@ -651,9 +648,9 @@ int tpm_load_state(tpm_ctx *c, const double *RU, const double *RU_int, const dou
     if (c->np > 0) {
       for (int q = 0; q < 7; ++q) {
         if (!part[q]) return fail(c, TPM_ERR_ARG, "null particle array");
-        up(c->pq[0][q], part[q], c->np);
+        tpm::particles_from_host(c, c->pq[0][q], part[q], 8);
       }
-      up(c->rhs_t, rhs_t, c->np);
+      tpm::particles_from_host(c, c->rhs_t, rhs_t, 8);
     }
     pull_scalars(c);  // synchronises the copies above
     c->hsc->P0 = P0;
@@ -682,9 +679,9 @@ int tpm_save_state(tpm_ctx *c, double *RU, double *RU_int, double *Rho, double *
     if (c->np > 0) {
       for (int q = 0; q < 7; ++q) {
         if (!part[q]) return fail(c, TPM_ERR_ARG, "null particle array");
-        down(part[q], c->pq[0][q], c->np);
+        tpm::particles_to_host(c, part[q], c->pq[0][q], 8);
       }
-      down(rhs_t, c->rhs_t, c->np);
+      tpm::particles_to_host(c, rhs_t, c->rhs_t, 8);
     }
     pull_scalars(c);  // synchronises the copies above
     if (sc) {
@@ -726,6 +723,7 @@ int tpm_initialize(tpm_ctx *c) {
     // grid.cpp:481-484: initial particle heat coupling
     tpm::particle_zero_fields(c);
     tpm::particle_init_heat(c);
+    tpm::particle_reorder(c);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->initialized = true;
     c->stepped = false;
@@ -766,6 +764,7 @@ void resume_device(tpm_ctx *c) {
       tpm::launch_passive_scalar_face(c, c->PS);
     }
     tpm::particle_resume(c);
+    tpm::particle_reorder(c);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->initialized = true;
     c->stepped = false;

@@ -186,6 +186,13 @@ struct tpm_ctx {
   int32_t *scan_blocks = nullptr;
   double *pay_t = nullptr, *pay_t_s = nullptr;          // 6*np
   double *pay_r = nullptr;  // 4*np: round-indexed fractions and heat rate, unsorted
+  // mixed path: particles kept in cell order (particle_reorder).  pid[s] is the
+  // caller's index of the particle in storage slot s; host transfers of
+  // per-particle data go through it.  pid2 / flag2 / rhs_t2 / tau2 take the
+  // permuted copies, pstage (np x 8 bytes) stages the caller-ordered arrays.
+  bool reorder = false;
+  int32_t *pid = nullptr, *pid2 = nullptr, *flag2 = nullptr;
+  double *rhs_t2 = nullptr, *tau2 = nullptr, *pstage = nullptr;
   double *w8 = nullptr;  // 16*np corner weights (heat, concentration; sorted order)
   double *C_next = nullptr;  // concentration at this x_new = next substep's x_int
   // passive scalar (solve_for_scalar): RK copies, face values I_C2F(PS_new)
@@ -299,6 +306,14 @@ void particle_heat(tpm_ctx *c);
 void particle_init_heat(tpm_ctx *c);
 void particle_resume(tpm_ctx *c);
 void particle_zero_fields(tpm_ctx *c);
+// mixed path: permute the particles into the cell order of the last heat
+// deposit's sort (at a step boundary; pq[2], pq[3] are free there)
+void particle_reorder(tpm_ctx *c);
+void particles_reorder_init(tpm_ctx *c);  // pid = identity (the caller order)
+// per-particle arrays between the caller's order and storage order (elem =
+// 8 or 4 bytes); plain copies unless c->reorder
+void particles_from_host(tpm_ctx *c, void *dev, const void *host, int elem);
+void particles_to_host(tpm_ctx *c, void *host, const void *dev, int elem);
 
 }  // namespace tpm
 

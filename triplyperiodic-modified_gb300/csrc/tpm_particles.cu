@@ -15,6 +15,8 @@
 //    a fixed order.  No floating-point atomics, so the sources are bit-
 //    reproducible run to run; they differ from the reference's particle-order
 //    sums only by FP64 reassociation.
+#include <utility>
+
 #include "tpm_internal.cuh"
 #include "tpm_ff.cuh"
 #include "tpm_reduce.cuh"
@@ -319,10 +321,24 @@ __global__ void k_fill_tgas(long long n, const double *__restrict__ Rho, double 
 }
 
 // ------------------------------------------------------------ counting sort
+// The counting sort's atomics are aggregated per warp over equal keys: with
+// the particles in cell order (mixed path) neighbouring lanes share a cell,
+// and one atomic per cell and warp replaces up to 32 on the same address.
+// The warp walks the particles together (uniform trip count) so that the
+// match covers exactly the lanes holding a particle.
 __global__ void k_hist(const int32_t *__restrict__ key, int64_t np, int32_t *__restrict__ counts) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
-       p += (int64_t)gridDim.x * blockDim.x)
-    atomicAdd(&counts[key[p]], 1);
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < np;
+       base += stride) {
+    const int64_t p = base + lane;
+    const unsigned live = __ballot_sync(0xffffffffu, p < np);
+    if (p < np) {
+      const int32_t k = key[p];
+      const unsigned peers = __match_any_sync(live, k);
+      if (lane == __ffs(peers) - 1) atomicAdd(&counts[k], __popc(peers));
+    }
+  }
 }
 
 constexpr int kScanThreads = 512;
@@ -404,11 +420,22 @@ __global__ void k_scan_apply(int32_t *__restrict__ counts, long long n,
 __global__ void k_scatter(const int32_t *__restrict__ key, int64_t np,
                           const int32_t *__restrict__ starts, int32_t *__restrict__ cursor,
                           int32_t *__restrict__ perm) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    int32_t k = key[p];
-    int32_t slot = starts[k] + atomicAdd(&cursor[k], 1);
-    perm[slot] = (int32_t)p;
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < np;
+       base += stride) {
+    const int64_t p = base + lane;
+    const unsigned live = __ballot_sync(0xffffffffu, p < np);
+    if (p < np) {
+      const int32_t k = key[p];
+      const unsigned peers = __match_any_sync(live, k);
+      const int leader = __ffs(peers) - 1;
+      int32_t first = 0;
+      if (lane == leader) first = atomicAdd(&cursor[k], __popc(peers));
+      first = __shfl_sync(live, first, leader);
+      const int32_t slot = starts[k] + first + __popc(peers & ((1u << lane) - 1u));
+      perm[slot] = (int32_t)p;
+    }
   }
 }
 
@@ -569,6 +596,56 @@ void sort_by_cell(tpm_ctx *c, const int32_t *key, int32_t *perm, int32_t *starts
   TPM_LAUNCH(c, "sort_segsort", k_segsort, cell_blocks(c->g), kThreads, 0, n, starts, perm);
 }
 
+__global__ void k_iota(int32_t *__restrict__ a, int64_t np) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+       p += (int64_t)gridDim.x * blockDim.x)
+    a[p] = (int32_t)p;
+}
+
+struct ReorderArgs {
+  const double *src[7];
+  double *d0[7], *d1[7];
+  const double *rhs_t, *tau;
+  double *rhs_t2, *tau2;
+  const int32_t *flag, *pid;
+  int32_t *flag2, *pid2;
+};
+
+// slot s of the new order takes particle perm[s] of the old one (both copies
+// of the base set, the heat rate, the flag, the caller index, the Stokes time)
+__global__ void k_reorder(int64_t np, const int32_t *__restrict__ perm, ReorderArgs a) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < np;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t p = perm[s];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+      const double v = a.src[q][p];
+      a.d0[q][s] = v;
+      a.d1[q][s] = v;
+    }
+    a.rhs_t2[s] = a.rhs_t[p];
+    a.flag2[s] = a.flag[p];
+    a.pid2[s] = a.pid[p];
+    if (a.tau) a.tau2[s] = a.tau[p];
+  }
+}
+
+// storage slot s <- caller element pid[s], and back
+template <typename T>
+__global__ void k_from_caller(int64_t np, const int32_t *__restrict__ pid, const T *__restrict__ in,
+                              T *__restrict__ out) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < np;
+       s += (int64_t)gridDim.x * blockDim.x)
+    out[s] = in[pid[s]];
+}
+template <typename T>
+__global__ void k_to_caller(int64_t np, const int32_t *__restrict__ pid, const T *__restrict__ in,
+                            T *__restrict__ out) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < np;
+       s += (int64_t)gridDim.x * blockDim.x)
+    out[pid[s]] = in[s];
+}
+
 PState pstate(tpm_ctx *c, bool np1_in_base) {
   PState s;
   for (int q = 0; q < 7; ++q) {
@@ -714,6 +791,76 @@ void particle_resume(tpm_ctx *c) {
              c->pq[1][1], c->pq[1][2], c->pq[1][6], c->Tgas, 0.0, c->np, c->rhs_t, c->key_r,
              c->pay_r, 0);
   heat_deposit(c);
+}
+
+void particle_reorder(tpm_ctx *c) {
+  if (!c->reorder || c->np == 0 || !c->np1_is_base) return;
+  ReorderArgs a;
+  for (int q = 0; q < 7; ++q) {
+    a.src[q] = c->pq[0][q];
+    a.d0[q] = c->pq[3][q];
+    a.d1[q] = c->pq[2][q];
+  }
+  a.rhs_t = c->rhs_t; a.rhs_t2 = c->rhs_t2;
+  a.tau = c->tau; a.tau2 = c->tau2;
+  a.flag = c->flag; a.flag2 = c->flag2;
+  a.pid = c->pid; a.pid2 = c->pid2;
+  TPM_LAUNCH(c, "particle_reorder", k_reorder, pblocks(c->np), kThreads, 0, c->np, c->perm_r[0],
+             a);
+  // the small arrays go back in place; the base set and its int copy take the
+  // two filled buffers, so that over a step the buffer pointers still only
+  // alternate between two states (two captured graphs)
+  TPM_CUDA_TRY(cudaMemcpyAsync(c->rhs_t, c->rhs_t2, sizeof(double) * c->np,
+                               cudaMemcpyDeviceToDevice, c->stream));
+  TPM_CUDA_TRY(cudaMemcpyAsync(c->flag, c->flag2, sizeof(int32_t) * c->np,
+                               cudaMemcpyDeviceToDevice, c->stream));
+  TPM_CUDA_TRY(cudaMemcpyAsync(c->pid, c->pid2, sizeof(int32_t) * c->np,
+                               cudaMemcpyDeviceToDevice, c->stream));
+  if (c->tau)
+    TPM_CUDA_TRY(cudaMemcpyAsync(const_cast<double *>(c->tau), c->tau2, sizeof(double) * c->np,
+                                 cudaMemcpyDeviceToDevice, c->stream));
+  for (int q = 0; q < 7; ++q) {
+    std::swap(c->pq[0][q], c->pq[3][q]);
+    std::swap(c->pq[1][q], c->pq[2][q]);
+  }
+}
+
+void particles_reorder_init(tpm_ctx *c) {
+  if (c->reorder && c->np)
+    TPM_LAUNCH(c, "pid_init", k_iota, pblocks(c->np), kThreads, 0, c->pid, c->np);
+}
+
+void particles_from_host(tpm_ctx *c, void *dev, const void *host, int elem) {
+  if (c->np == 0) return;
+  const size_t bytes = (size_t)elem * c->np;
+  if (!c->reorder) {
+    TPM_CUDA_TRY(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, c->stream));
+    return;
+  }
+  TPM_CUDA_TRY(cudaMemcpyAsync(c->pstage, host, bytes, cudaMemcpyHostToDevice, c->stream));
+  if (elem == 8)
+    TPM_LAUNCH(c, "from_caller", k_from_caller<double>, pblocks(c->np), kThreads, 0, c->np, c->pid,
+               c->pstage, static_cast<double *>(dev));
+  else
+    TPM_LAUNCH(c, "from_caller", k_from_caller<int32_t>, pblocks(c->np), kThreads, 0, c->np, c->pid,
+               reinterpret_cast<const int32_t *>(c->pstage), static_cast<int32_t *>(dev));
+}
+
+void particles_to_host(tpm_ctx *c, void *host, const void *dev, int elem) {
+  if (c->np == 0) return;
+  const size_t bytes = (size_t)elem * c->np;
+  if (!c->reorder) {
+    TPM_CUDA_TRY(cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->stream));
+    return;
+  }
+  if (elem == 8)
+    TPM_LAUNCH(c, "to_caller", k_to_caller<double>, pblocks(c->np), kThreads, 0, c->np, c->pid,
+               static_cast<const double *>(dev), c->pstage);
+  else
+    TPM_LAUNCH(c, "to_caller", k_to_caller<int32_t>, pblocks(c->np), kThreads, 0, c->np, c->pid,
+               static_cast<const int32_t *>(dev), reinterpret_cast<int32_t *>(c->pstage));
+  // the next transfer reuses pstage: it is enqueued after this copy on the stream
+  TPM_CUDA_TRY(cudaMemcpyAsync(host, c->pstage, bytes, cudaMemcpyDeviceToHost, c->stream));
 }
 
 void particle_zero_fields(tpm_ctx *c) {
