@@ -37,6 +37,14 @@ FALLBACK_HBM_GBS = 6800.0
 # particle) for FP64 storage; the derivation is tabulated in the design doc.
 # `value` is the headline (mixed-precision) path; the FP64 path is reported
 # beside it under "fp64".
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of a
+# kernel on a workload, the mean over the launches of one ncu capture of this
+# bench's own command (the profiles/ summary of that kernel gives the command)
+NCU_TRAFFIC = {
+    # profiles/k_xfwd_resid_refine_mixed_box256_box128.md
+    ("box256_p8e6_heated", True, "fft_x_fwd_resid"): 8.35e8,
+}
+
 KERNEL_BYTES = {
     "rhs_momentum": (21 * 8, 0),
     "poisson_rhs": (11 * 8, 0),
@@ -290,7 +298,8 @@ def step_bytes(ncell, npart, n_it, mixed):
     return ncell * per_cell + npart * 4 * (37 * 8 + 16)
 
 
-def path_result(p, s, ms, steps, world, n_it, launches, prof, clocks, mixed, peak):
+def path_result(p, s, ms, steps, world, n_it, launches, prof, clocks, mixed, peak,
+                workload=None):
     ms_per_step = ms / steps
     dom_name, (nl, tot_ms) = max(prof.items(), key=lambda kv: kv[1][1])
     per_launch = kernel_bytes(dom_name, p.ncell, s.npart, mixed)
@@ -303,7 +312,9 @@ def path_result(p, s, ms, steps, world, n_it, launches, prof, clocks, mixed, pea
         "ms_per_step": ms_per_step, "n_it": n_it, "launches": launches, "clocks": clocks,
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                     "traffic": None, "kernel_share": round(tot_ms / total_prof, 4)},
+                     "traffic": NCU_TRAFFIC.get((workload, mixed, dom_name)),
+                     "algorithmic_bytes": int(per_launch),
+                     "kernel_share": round(tot_ms / total_prof, 4)},
         "step_roofline": {"achieved_gbs": round(sgbs, 1), "frac": round(sgbs / peak, 4),
                           "algorithmic_bytes_per_step": int(sb)},
         "kernels_ms_per_step": {k: round(v[1] / 2, 3) for k, v in
@@ -377,7 +388,7 @@ def gpu_main(args):
                                                          local)
         ms = max_over_ranks(ms, dist, "cuda")
         res[name] = path_result(p, s, ms, args.steps, world, n_it, launches, prof, clocks,
-                                name == "mixed", peak)
+                                name == "mixed", peak, workload=args.workload)
         res[name]["fft_pencils_per_block"] = ctx.fft_pens
         ctxs[name] = ctx
     head = "mixed" if "mixed" in res else "fp64"
