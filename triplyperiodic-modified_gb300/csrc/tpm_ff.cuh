@@ -158,6 +158,15 @@ __device__ __forceinline__ void ff_int_frac(double u, int &ip, float &fr, bool &
 // hi + lo as a double (two exact conversions and one FP64 addition)
 __device__ __forceinline__ double ff_to_double(float2 a) { return ff_f2d(a.x) + ff_f2d(a.y); }
 
+// double -> T and back for code templated on its compute type: for float by
+// integer operations (truncation down, exact up), for double the identity
+template <typename T>
+__device__ __forceinline__ T ff_cast(double x) { return (T)x; }
+template <>
+__device__ __forceinline__ float ff_cast<float>(double x) { return ff_hi(x); }
+__device__ __forceinline__ double ff_widen(double x) { return x; }
+__device__ __forceinline__ double ff_widen(float x) { return ff_f2d(x); }
+
 // a normalised so that |lo| <= ulp(hi) / 2 (for pairs whose lo is already
 // small against hi, as ff_mul leaves them)
 __device__ __forceinline__ float2 ff_norm(float2 a) { return ff_fast_two_sum(a.x, a.y); }

@@ -161,6 +161,10 @@ __global__ void k_rhs_momentum(Grid g, const TIn *__restrict__ U, const TIn *__r
                                double *__restrict__ RU_np1, double *__restrict__ RU_new, RhsArgs a) {
   const TC inv_d[3] = {(TC)g.inv_dx, (TC)g.inv_dy, (TC)g.inv_dz};
   const TC inv_d2[3] = {(TC)g.inv_dx2, (TC)g.inv_dy2, (TC)g.inv_dz2};
+  // the coefficients once per thread; per-cell FP64 values below go through
+  // ff_cast / ff_widen (integer operations when TC is float)
+  const TC a_fp = (TC)a.a_fp, b_gd = (TC)a.b_gd, c_lap = (TC)a.c_lap, A_ = (TC)a.A;
+  const TC Rho0 = (TC)a.Rho0, gv[3] = {(TC)a.g[0], (TC)a.g[1], (TC)a.g[2]};
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
@@ -180,7 +184,7 @@ __global__ void k_rhs_momentum(Grid g, const TIn *__restrict__ U, const TIn *__r
                ((TC)Ud[nb.p[1]] - 2 * ud + (TC)Ud[nb.m[1]]) * inv_d2[1] +
                ((TC)Ud[nb.p[2]] - 2 * ud + (TC)Ud[nb.m[2]]) * inv_d2[2];
       // RHS = -mp/Vcell*F_p + mu/3 grad(div U) + mu Del2 U  (grid.cpp:783)
-      TC rhs = (TC)a.a_fp * (TC)Fp[d * g.n + c] + (TC)a.b_gd * gd + (TC)a.c_lap * lap;
+      TC rhs = a_fp * (TC)Fp[d * g.n + c] + b_gd * gd + c_lap * lap;
       // convection: Div_F2C(I_C2F(U_d) * I_d,C2F(RU_int))  (grid.cpp:785-801)
       TC conv = 0;
       {
@@ -198,16 +202,17 @@ __global__ void k_rhs_momentum(Grid g, const TIn *__restrict__ U, const TIn *__r
       }
       rhs -= conv;
       // artificial (linear) forcing A*RU_int (grid.cpp:803)
-      rhs += (TC)a.A * (TC)RUi[d * g.n + c];
+      rhs += A_ * (TC)RUi[d * g.n + c];
       // body force (Rho_face - Rho0)*g (grid.cpp:805-809)
       if (a.has_g) {
-        TC rf = ((TC)Rho_int[c] + (TC)Rho_int[d == 0 ? nb.m[0] : d == 1 ? nb.m[1] : nb.m[2]]) *
+        TC rf = (ff_cast<TC>(Rho_int[c]) +
+                 ff_cast<TC>(Rho_int[d == 0 ? nb.m[0] : d == 1 ? nb.m[1] : nb.m[2]])) *
                 (TC)0.5;
-        rhs += (rf - (TC)a.Rho0) * (TC)a.g[d];
+        rhs += (rf - Rho0) * gv[d];
       }
       // RU_np1 += dt*post*RHS ; RU_new = RU + dt*pre*RHS  (grid.cpp:811-813);
       // FMAs on the mixed path (FP32 stencil, FP64 accumulation)
-      const double r64 = (double)rhs;
+      const double r64 = ff_widen(rhs);
       constexpr bool kFma = sizeof(TC) == sizeof(float);
       double np1 = kFma ? fma(a.dtpo, r64, np1_in[d * g.n + c]) : np1_in[d * g.n + c] + a.dtpo * r64;
       RU_np1[d * g.n + c] = np1;
@@ -668,11 +673,15 @@ __global__ void k_project(Grid g, const double *__restrict__ P, double *__restri
     double pc = P[c];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      double G = (pc - P[nb.m[d]]) * inv_d[d];
-      double np1 = kFma ? fma(a_np1, G, RU_np1[d * g.n + c]) : RU_np1[d * g.n + c] + a_np1 * G;
+      // mixed path: the pressure difference times the folded constants
+      // a/d, b/d (one FP64 product fewer per face; no bitwise parity there)
+      const double dp = pc - P[nb.m[d]];
+      const double G = kFma ? dp : dp * inv_d[d];
+      const double ca = kFma ? a_np1 * inv_d[d] : a_np1, cb = kFma ? b_new * inv_d[d] : b_new;
+      double np1 = kFma ? fma(ca, G, RU_np1[d * g.n + c]) : RU_np1[d * g.n + c] + ca * G;
       RU_np1[d * g.n + c] = np1;
-      const double nw = (stage != 3) ? (kFma ? fma(b_new, G, RU_new[d * g.n + c])
-                                             : RU_new[d * g.n + c] + b_new * G)
+      const double nw = (stage != 3) ? (kFma ? fma(cb, G, RU_new[d * g.n + c])
+                                             : RU_new[d * g.n + c] + cb * G)
                                      : np1;
       RU_new[d * g.n + c] = nw;
       if (RUn32) RUn32[d * g.n + c] = ff_hi(nw);

@@ -384,35 +384,69 @@ __global__ void k_scan_chunks(int32_t *__restrict__ chunk_sums, int nchunks) {
 }
 
 // phase 3: starts[c] = offset + exclusive scan within the chunk; counts
-// are cleared so the scatter can reuse them as cursors
+// are cleared so the scatter can reuse them as cursors.  Each thread takes 8
+// consecutive counts (two 16-byte loads where the chunk is whole), the block
+// scans its threads' sums with warp shuffles and one pass over the 16 warp
+// totals.
 __global__ void k_scan_apply(int32_t *__restrict__ counts, long long n,
                              const int32_t *__restrict__ chunk_off, int32_t *__restrict__ starts,
                              int32_t total) {
-  __shared__ int32_t sh[kScanThreads];
-  long long base = (long long)blockIdx.x * kScanChunk + threadIdx.x * kScanPer;
+  static_assert(kScanPer == 8 && kScanThreads % 32 == 0, "two int4 per thread");
+  __shared__ int32_t wsum[kScanThreads / 32];
+  const long long base = (long long)blockIdx.x * kScanChunk + threadIdx.x * kScanPer;
+  const bool whole = base + kScanPer <= n;
   int32_t v[kScanPer];
+  if (whole) {
+    const int4 a = *reinterpret_cast<const int4 *>(counts + base);
+    const int4 b = *reinterpret_cast<const int4 *>(counts + base + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  } else {
+#pragma unroll
+    for (int e = 0; e < kScanPer; ++e) v[e] = (base + e < n) ? counts[base + e] : 0;
+  }
   int32_t s = 0;
 #pragma unroll
-  for (int e = 0; e < kScanPer; ++e) {
-    v[e] = (base + e < n) ? counts[base + e] : 0;
-    s += v[e];
+  for (int e = 0; e < kScanPer; ++e) s += v[e];
+  // inclusive scan of the thread sums within the warp, then over the warps
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int32_t incl = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t w = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += w;
   }
-  sh[threadIdx.x] = s;
+  if (lane == 31) wsum[warp] = incl;
   __syncthreads();
-  for (int o = 1; o < kScanThreads; o <<= 1) {
-    int32_t w = threadIdx.x >= (unsigned)o ? sh[threadIdx.x - o] : 0;
-    __syncthreads();
-    sh[threadIdx.x] += w;
-    __syncthreads();
+  if (warp == 0) {
+    int32_t t = lane < kScanThreads / 32 ? wsum[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t w = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += w;
+    }
+    if (lane < kScanThreads / 32) wsum[lane] = t;  // inclusive warp prefixes
   }
-  int32_t run = chunk_off[blockIdx.x] + sh[threadIdx.x] - s;
+  __syncthreads();
+  int32_t run = chunk_off[blockIdx.x] + (warp ? wsum[warp - 1] : 0) + incl - s;
+  int32_t out[kScanPer];
 #pragma unroll
   for (int e = 0; e < kScanPer; ++e) {
-    if (base + e < n) {
-      starts[base + e] = run;
-      counts[base + e] = 0;
-    }
+    out[e] = run;
     run += v[e];
+  }
+  if (whole) {
+    *reinterpret_cast<int4 *>(starts + base) = make_int4(out[0], out[1], out[2], out[3]);
+    *reinterpret_cast<int4 *>(starts + base + 4) = make_int4(out[4], out[5], out[6], out[7]);
+    *reinterpret_cast<int4 *>(counts + base) = make_int4(0, 0, 0, 0);
+    *reinterpret_cast<int4 *>(counts + base + 4) = make_int4(0, 0, 0, 0);
+  } else {
+#pragma unroll
+    for (int e = 0; e < kScanPer; ++e)
+      if (base + e < n) {
+        starts[base + e] = out[e];
+        counts[base + e] = 0;
+      }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) starts[n] = total;
 }
@@ -503,15 +537,6 @@ __global__ void k_dep_momentum(Grid g, const int32_t *__restrict__ starts,
 // (weights) that the next substep deposits at the same positions (its x_int
 // is this x_new).  Weights are built per sorted slot from the unsorted
 // payload; the sums keep the order of k_dep_sum8.
-// FP64 <-> TW for the deposit weights: for TW = float by integer operations
-// (truncation; the conversion instructions issue on the FP64 pipe)
-template <typename TW>
-__device__ __forceinline__ TW to_tw(double x) { return (TW)x; }
-template <>
-__device__ __forceinline__ float to_tw<float>(double x) { return ff_hi(x); }
-__device__ __forceinline__ double from_tw(double x) { return x; }
-__device__ __forceinline__ double from_tw(float x) { return ff_f2d(x); }
-
 template <typename TW>
 __global__ void k_cic_weights2(int64_t np, const int32_t *__restrict__ perm,
                                const double *__restrict__ pay, TW *__restrict__ wq,
@@ -519,8 +544,9 @@ __global__ void k_cic_weights2(int64_t np, const int32_t *__restrict__ perm,
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < np;
        s += (int64_t)gridDim.x * blockDim.x) {
     const int32_t p = perm[s];
-    const TW xl = to_tw<TW>(pay[p]), yl = to_tw<TW>(pay[np + p]), zl = to_tw<TW>(pay[2 * np + p]);
-    const TW r = to_tw<TW>(pay[3 * np + p]);
+    // (FP64 -> FP32 by integer operations on the mixed path: ff_cast)
+    const TW xl = ff_cast<TW>(pay[p]), yl = ff_cast<TW>(pay[np + p]), zl = ff_cast<TW>(pay[2 * np + p]);
+    const TW r = ff_cast<TW>(pay[3 * np + p]);
     const TW fx[2] = {xl, 1 - xl}, fy[2] = {yl, 1 - yl}, fz[2] = {zl, 1 - zl};
 #pragma unroll
     for (int dy = 0; dy < 2; ++dy)
@@ -565,9 +591,9 @@ __global__ void k_dep_sum8x2(Grid g, const int32_t *__restrict__ starts, const T
             ac += wc[o + s];
           }
         }
-    const double qd = from_tw(aq);
+    const double qd = ff_widen(aq);
     Q[c] = qd;
-    C[c] = from_tw(ac);
+    C[c] = ff_widen(ac);
     bsum += qd;
   }
   double b = block_sum(bsum, sh);
