@@ -424,7 +424,10 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
       c->pstage = dalloc<double>(c, np);
       tpm::particles_reorder_init(c);
     }
-    c->w8 = dalloc<double>(c, 16 * (size_t)np);
+    if (p->precision == TPM_PREC_MIXED)
+      c->corner_sums = dalloc<float>(c, 16 * (size_t)n);
+    else
+      c->w8 = dalloc<double>(c, 16 * (size_t)np);
     c->C_next = dalloc<double>(c, n);
     if (p->Solver == 2) tpm::pcg_alloc(c);
     if (p->solve_for_scalar) {

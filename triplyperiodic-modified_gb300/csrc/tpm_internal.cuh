@@ -194,6 +194,7 @@ struct tpm_ctx {
   int32_t *pid = nullptr, *pid2 = nullptr, *flag2 = nullptr;
   double *rhs_t2 = nullptr, *tau2 = nullptr, *pstage = nullptr;
   double *w8 = nullptr;  // 16*np corner weights (heat, concentration; sorted order)
+  float *corner_sums = nullptr;  // mixed: 16*n per-source-cell corner sums (heat, conc.)
   double *C_next = nullptr;  // concentration at this x_new = next substep's x_int
   // passive scalar (solve_for_scalar): RK copies, face values I_C2F(PS_new)
   // of the last stage, and the mean-free source field of S1_type 0

@@ -600,6 +600,81 @@ __global__ void k_dep_sum8x2(Grid g, const int32_t *__restrict__ starts, const T
   if (threadIdx.x == 0) partials[blockIdx.x] = b;
 }
 
+// Mixed path, the same deposit in two passes without the per-particle corner
+// weights.  Pass 1, per source cell r (the round-indexed cell of its
+// particles): every particle's eight corner weights
+// ((fx[dx] fy[dy]) fz[dz], the operation order of k_cic_weights2) and their
+// products with its heat rate are summed over the cell's particles in slot
+// order into 8 + 8 corner sums of r.  Pass 2, per target cell c: the corner
+// sums of the 8 cells r = c + (dx, dy, dz) in corner order.  Deterministic;
+// the sums associate per corner first.
+__global__ void k_dep_corners(Grid g, const int32_t *__restrict__ starts,
+                              const int32_t *__restrict__ perm, const double *__restrict__ pay,
+                              int64_t np, float *__restrict__ sums) {
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.n;
+       r += (long long)gridDim.x * blockDim.x) {
+    float sq[8], sc[8];
+#pragma unroll
+    for (int o = 0; o < 8; ++o) sq[o] = sc[o] = 0.f;
+    const int32_t s0 = starts[r], e0 = starts[r + 1];
+    for (int32_t s = s0; s < e0; ++s) {
+      const int32_t p = perm[s];
+      const float xl = ff_hi(pay[p]), yl = ff_hi(pay[np + p]), zl = ff_hi(pay[2 * np + p]);
+      const float rt = ff_hi(pay[3 * np + p]);
+      const float fx[2] = {xl, 1 - xl}, fy[2] = {yl, 1 - yl}, fz[2] = {zl, 1 - zl};
+#pragma unroll
+      for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+        for (int dx = 0; dx < 2; ++dx) {
+          const float fxy = fx[dx] * fy[dy];
+#pragma unroll
+          for (int dz = 0; dz < 2; ++dz) {
+            const int o = (dz * 2 + dy) * 2 + dx;
+            const float v = fxy * fz[dz];
+            sc[o] += v;
+            sq[o] += v * rt;
+          }
+        }
+    }
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      sums[(size_t)o * g.n + r] = sq[o];
+      sums[(size_t)(8 + o) * g.n + r] = sc[o];
+    }
+  }
+}
+
+__global__ void k_dep_gather8(Grid g, const float *__restrict__ sums, double *__restrict__ Q,
+                              double *__restrict__ C, double *__restrict__ partials) {
+  __shared__ double sh[32];
+  double bsum = 0;
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % g.nx);
+    const long long t = c / g.nx;
+    const int j = (int)(t % g.ny), k = (int)(t / g.ny);
+    float aq = 0.f, ac = 0.f;
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+      for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+        for (int dx = 0; dx < 2; ++dx) {
+          const long long r = at(g, dx ? wrap_p(i, g.nx) : i, dy ? wrap_p(j, g.ny) : j,
+                                 dz ? wrap_p(k, g.nz) : k);
+          const int o = (dz * 2 + dy) * 2 + dx;
+          aq += sums[(size_t)o * g.n + r];
+          ac += sums[(size_t)(8 + o) * g.n + r];
+        }
+    const double qd = ff_f2d(aq);
+    Q[c] = qd;
+    C[c] = ff_f2d(ac);
+    bsum += qd;
+  }
+  double b = block_sum(bsum, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = b;
+}
+
 int pblocks(int64_t np) {
   int64_t b = (np + kThreads - 1) / kThreads;
   if (b > 152 * 32) b = 152 * 32;
@@ -758,11 +833,10 @@ static void heat_deposit(tpm_ctx *c) {
   sort_by_cell(c, c->key_r, c->perm_r[0], c->starts_r[0]);
   double *parts = c->partials + kPartQ * kRedBlocks;
   if (c->p.precision == TPM_PREC_MIXED) {
-    float *wq = reinterpret_cast<float *>(c->w8), *wc = wq + 8 * (size_t)c->np;
-    TPM_LAUNCH(c, "cic_weights", k_cic_weights2<float>, pblocks(c->np), kThreads, 0, c->np,
-               c->perm_r[0], c->pay_r, wq, wc);
-    TPM_LAUNCH(c, "deposit_heat_conc", k_dep_sum8x2<float>, nb, kThreads, 0, c->g,
-               c->starts_r[0], wq, wc, c->np, c->Q, c->C_next, parts);
+    TPM_LAUNCH(c, "deposit_corner_sums", k_dep_corners, nb, kThreads, 0, c->g, c->starts_r[0],
+               c->perm_r[0], c->pay_r, c->np, c->corner_sums);
+    TPM_LAUNCH(c, "deposit_heat_conc", k_dep_gather8, nb, kThreads, 0, c->g, c->corner_sums,
+               c->Q, c->C_next, parts);
   } else {
     double *wq = c->w8, *wc = wq + 8 * (size_t)c->np;
     TPM_LAUNCH(c, "cic_weights", k_cic_weights2<double>, pblocks(c->np), kThreads, 0, c->np,
