@@ -675,6 +675,43 @@ __global__ void k_dep_gather8(Grid g, const float *__restrict__ sums, double *__
   if (threadIdx.x == 0) partials[blockIdx.x] = b;
 }
 
+// Mixed path, the two-way momentum deposit in two passes without the sorted
+// payload copy.  Pass 1, per source cell r (the cell of its particles at
+// x_int): the six payload components (lower and upper weight times the
+// momentum source, per axis) summed over the cell's particles in slot order.
+// Pass 2, per face: face d of cell c takes the upper sum of cell c - e_d plus
+// the lower sum of cell c (the order of k_dep_momentum).
+__global__ void k_dep_mom_cells(Grid g, const int32_t *__restrict__ starts,
+                                const int32_t *__restrict__ perm, const float *__restrict__ pay,
+                                int64_t np, float *__restrict__ sums) {
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.n;
+       r += (long long)gridDim.x * blockDim.x) {
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const int32_t s0 = starts[r], e0 = starts[r + 1];
+    for (int32_t s = s0; s < e0; ++s) {
+      const int32_t p = perm[s];
+#pragma unroll
+      for (int f = 0; f < 6; ++f) acc[f] += pay[f * np + p];
+    }
+#pragma unroll
+    for (int f = 0; f < 6; ++f) sums[(size_t)f * g.n + r] = acc[f];
+  }
+}
+
+__global__ void k_dep_mom_faces(Grid g, const float *__restrict__ sums, float *__restrict__ Fp) {
+  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c % g.nx);
+    const long long t = c / g.nx;
+    const int j = (int)(t % g.ny), k = (int)(t / g.ny);
+    const long long m[3] = {at(g, wrap_m(i, g.nx), j, k), at(g, i, wrap_m(j, g.ny), k),
+                            at(g, i, j, wrap_m(k, g.nz))};
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      Fp[d * g.n + c] = sums[(size_t)(2 * d + 1) * g.n + m[d]] + sums[(size_t)(2 * d) * g.n + c];
+  }
+}
+
 int pblocks(int64_t np) {
   int64_t b = (np + kThreads - 1) / kThreads;
   if (b > 152 * 32) b = 152 * 32;
@@ -803,11 +840,13 @@ void particle_deposit_momentum(tpm_ctx *c) {
   }
   sort_by_cell(c, c->key_t, c->perm_t, c->starts_t);
   if (mixed) {
-    float *pt = reinterpret_cast<float *>(c->pay_t), *pts = reinterpret_cast<float *>(c->pay_t_s);
-    TPM_LAUNCH(c, "payload_gather_t", k_gather_payload<float>, pblocks(c->np), kThreads, 0, c->np,
-               6, c->perm_t, pt, pts);
-    TPM_LAUNCH(c, "deposit_momentum", (k_dep_momentum<float, float>), cell_blocks(c->g), kThreads,
-               0, c->g, c->starts_t, pts, c->np, c->Fp32);
+    // the 16 n corner-sum floats of the heat deposit hold these 6 n (the two
+    // deposits run one after the other)
+    TPM_LAUNCH(c, "deposit_momentum_cells", k_dep_mom_cells, cell_blocks(c->g), kThreads, 0,
+               c->g, c->starts_t, c->perm_t, reinterpret_cast<const float *>(c->pay_t), c->np,
+               c->corner_sums);
+    TPM_LAUNCH(c, "deposit_momentum", k_dep_mom_faces, cell_blocks(c->g), kThreads, 0, c->g,
+               c->corner_sums, c->Fp32);
   } else {
     TPM_LAUNCH(c, "payload_gather_t", k_gather_payload<double>, pblocks(c->np), kThreads, 0, c->np,
                6, c->perm_t, c->pay_t, c->pay_t_s);
