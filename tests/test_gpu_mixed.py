@@ -109,3 +109,47 @@ def test_mixed_keeps_the_callers_particle_order(capi):
         assert rel_err(pm[q], pf[q]) <= TOL_MIXED, q
         assert np.abs(pm[q] - pf[q]).max() <= 1e-4 * np.abs(pf[q]).max(), q
     assert rel_err(rm, rf) <= TOL_MIXED
+
+
+def test_mixed_restart_and_state_transfer_in_callers_order(capi, tmp_path):
+    """Restart files and the step-boundary state carry the caller's particle
+    order on the mixed path, whose particles sit in cell order in memory:
+    after 3 steps both hold exactly what download_particles returns; a fresh
+    context reading the files gives them back unchanged and steps on like a
+    context loaded from the same arrays; and a context loaded with
+    tpm_load_state continues like the first run.  Mixed runs whose inputs
+    differ in rounding (here the in-cell order of the deposit sums, since a
+    fresh context's particles start in the caller's order) part at the level
+    of their FP32 increments, ~1e-8 after two steps; a wrong particle order
+    would show as an O(1) difference."""
+    p, s = setup(32, 6000, seed=13, heat=0.5, precision=P.PREC_MIXED)
+    a = run(capi, p, s, 3)
+    d = str(tmp_path)
+    a.write_restart(d)
+    r = inputs.read_restart(d, p)
+    st = a.download_state()
+    base = a.download_particles("base")
+    for q in inputs.PQ + ("flag",):
+        assert np.array_equal(r.part[q], base[q]), q
+    for q in inputs.PQ:
+        assert np.array_equal(st["part"][q], base[q]), q
+    b = capi.Context(p, s.npart)
+    b.read_restart(d)
+    back = b.download_particles("base")
+    for q in inputs.PQ:
+        assert np.array_equal(back[q], base[q]), q
+    b.initialize()
+    b2 = capi.Context(p, s.npart)
+    b2.load(r)
+    b2.initialize()
+    c = capi.Context(p, s.npart)
+    c.upload_state(st)
+    for ctx in (a, b, b2, c):
+        ctx.run(2)
+        ctx.sync()
+    for x, y in ((b, b2), (c, a)):
+        for g in ("RU", "RHO", "P", "C", "Q"):
+            assert rel_err(x.download_field(g), y.download_field(g)) <= 1e-7, g
+        px, py = x.download_particles("base"), y.download_particles("base")
+        for q in inputs.PQ:
+            assert rel_err(px[q], py[q]) <= 1e-7, q
