@@ -438,10 +438,11 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
                               const T2 *__restrict__ spec, double *__restrict__ P,
                               double *__restrict__ partials, int npen,
                               const int *__restrict__ skip, float2 *__restrict__ dP,
-                              const int *__restrict__ it) {
+                              const int *__restrict__ it, double inv_tot) {
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double sh[32];
+  __shared__ float shf[32];
   using T = typename Cx<T2>::T;
   T2 *a = reinterpret_cast<T2 *>(smem_raw);
   const int M = pl.n;
@@ -469,7 +470,8 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   }
   __syncthreads();
   T2 *z = smem_fft(a, b, npen, pl, +1);
-  const double inv_tot = 1.0 / (double)(g.nx * g.ny * g.nz);
+  // inv_tot = 1/(Nx Ny Nz) from the host (an FP64 division per thread would
+  // cost about as much as the update itself on this FP64 pipe)
   double mx = 0;
   if (sizeof(T) == sizeof(float)) {
     // mixed path: the correction dp = -x/N^3, formed in FP32, goes to P at
@@ -495,7 +497,11 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
       const float ax = fabsf(xf);
       mxf = ax > mxf ? ax : mxf;
     }
-    mx = (double)mxf * inv_tot;
+    // the block maximum in FP32 too (FP64 compares issue on the FP64 pipe);
+    // one conversion and one product per block
+    const float bm = block_max(mxf, shf);
+    if (threadIdx.x == 0) partials[blockIdx.x] = ff_f2d(bm) * inv_tot;
+    return;
   } else {
     for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
       const int q = fdiv(idx, pl.n2mag), i = idx - q * g.nx;
@@ -732,7 +738,8 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
     size_t smem = 2 * (size_t)npx * c->fx.n * sizeof(T2);
     double *parts = c->err_parts;
     TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, xblocks, tx, smem, g, c->fx,
-               r2c, spec, c->P, parts, npx, skip, c->dP, &c->dsc->it);
+               r2c, spec, c->P, parts, npx, skip, c->dP, &c->dsc->it,
+               1.0 / (double)((long long)g.nx * g.ny * g.nz));
     TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 256, 0, parts, xblocks, c->dsc, eps_ctl,
                loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0);
   }
@@ -1172,7 +1179,8 @@ extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, doub
     {
       size_t smem = 2 * (size_t)npx * fx.n * sizeof(double2);
       k_xinv_update<double2><<<xblocks, kFftThreads, smem, st>>>(g, fx, r2c, spec, P, errp, npx,
-                                                                 nullptr, nullptr, nullptr);
+                                                                 nullptr, nullptr, nullptr,
+                                                                 1.0 / (double)((long long)Nx * Ny * Nz));
       k_finish_max<<<1, 256, 0, st>>>(errp, xblocks, dsc, 0.0, cudaGraphConditionalHandle{}, 0);
     }
     if (cudaGetLastError() != cudaSuccess) return TPM_ERR_CUDA;
