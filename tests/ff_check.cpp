@@ -83,6 +83,9 @@ int main() {
     float2 sb = ff_sub(pc, pa);
     long double es = std::fabs((long double)sb.x + sb.y - (((long double)pc.x + pc.y) - va));
     CHECK(es <= std::ldexp(std::fabs(((long double)pc.x + pc.y) - va), -46), "sub err %.3Lg", es);
+    float2 ss = ff_sub_sloppy(pa, pb);
+    long double e2 = std::fabs((long double)ss.x + ss.y - (va - vb));
+    CHECK(e2 <= std::ldexp(std::fabs(va) + std::fabs(vb), -46), "sloppy sub err %.3Lg", e2);
     float2 af = ff_add_f(pa, c);
     long double ef = std::fabs((long double)af.x + af.y - (va + c));
     CHECK(ef <= std::ldexp(std::fabs(va) + std::fabs((long double)c), -46), "add_f err %.3Lg", ef);

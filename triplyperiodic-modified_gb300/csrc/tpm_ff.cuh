@@ -48,6 +48,13 @@ __device__ __forceinline__ float2 ff_sub(float2 a, float2 b) {
   return ff_fast_two_sum(s.x, s.y + t.y);
 }
 
+// a - b within 2^-46 (|a| + |b|) (one TwoSum on the high parts: for pairs
+// whose difference need not keep its own relative precision)
+__device__ __forceinline__ float2 ff_sub_sloppy(float2 a, float2 b) {
+  const float2 s = ff_two_sum(a.x, -b.x);
+  return make_float2(s.x, s.y + (a.y - b.y));
+}
+
 // a + b for a pair a and a float b, within 2^-46 (|a| + |b|)
 __device__ __forceinline__ float2 ff_add_f(float2 a, float b) {
   const float2 s = ff_two_sum(a.x, b);
