@@ -219,6 +219,20 @@ def test_boundary_and_clustered_particles(capi, oracle_lib):
         assert np.all(a[q] >= 0) and np.all(a[q] <= L)
 
 
+def test_crowded_cell_matches_oracle(capi, oracle_lib):
+    """200 coincident particles in one cell: the counting sort orders that
+    cell's particles by a heap sort instead of the insertion sort of the usual
+    few, and the deposits still sum in particle order like the oracle's."""
+    p, s = make_case(16, 300, seed=6, mass_loading=1e-3)
+    part = s.part
+    for q, v in (("x", 5.4), ("y", 2.2), ("z", 9.7)):
+        part[q][:200] = v * p.dx
+    ctx = gpu_run(capi, p, s, 2)
+    o = oracle_run(oracle_lib, p, s, 2)
+    assert_state_close(ctx, o, TOL1)
+    assert ctx.scalars()["num_timestep"] == 2  # no crowded-cell error below 65536
+
+
 def test_single_particle(capi, oracle_lib):
     p, s = make_case(12, 1, seed=6, mass_loading=1e-4)
     ctx = gpu_run(capi, p, s, 3)

@@ -381,6 +381,7 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     }
     c->partials = dalloc<double>(c, (size_t)tpm::kPartRegions * tpm::kRedBlocks);
     c->dsc = dalloc<tpm::DevScalars>(c, 1);
+    TPM_CUDA_TRY(cudaMemsetAsync(c->dsc, 0, sizeof(tpm::DevScalars), c->stream));
     TPM_CUDA_TRY(cudaMallocHost(&c->hsc, sizeof(tpm::DevScalars)));
     std::memset(c->hsc, 0, sizeof(tpm::DevScalars));
     for (double *f : {c->RU, c->RU_int, c->RU_new, c->RU_np1, c->Fp, c->U, c->Cface})
@@ -630,6 +631,10 @@ int tpm_get_scalars(tpm_ctx *c, tpm_scalars *out) {
     if (!std::isfinite(c->hsc->mean_ru[0]) || !std::isfinite(c->hsc->mean_ru[1]) ||
         !std::isfinite(c->hsc->mean_ru[2]) || !std::isfinite(c->hsc->P0))
       return fail(c, TPM_ERR_NONFINITE, "non-finite momentum or pressure in the state");
+    if (c->hsc->crowded)
+      return fail(c, TPM_ERR_NONFINITE,
+                  "more than 65536 particles crowded into one cell (a diverging run); their "
+                  "deposits were summed in arrival order");
     return TPM_OK;
   });
 }

@@ -61,6 +61,9 @@ struct DevScalars {
   int skip;
   int it;
   int it_sum;
+  // set (and kept) when a cell held more particles than the counting sort
+  // orders (kSortMaxRun): only a diverging run crowds its particles so
+  int crowded;
 };
 
 // 1-D FFT plan in device memory: radices and exp(-2 pi i m / n) twiddles,

@@ -474,20 +474,53 @@ __global__ void k_scatter(const int32_t *__restrict__ key, int64_t np,
 }
 
 // order each cell's particles by index: the deposit sums become independent
-// of the scatter's atomic order
+// of the scatter's atomic order.  Insertion sort for the usual few particles
+// per cell, an in-place heap sort (O(m log m), bounded) up to kSortMaxRun;
+// a cell beyond that (a diverging run crowding its particles) is left in
+// arrival order and flagged, so that no cell costs a thread more than
+// ~kSortMaxRun log2(kSortMaxRun) steps.
+constexpr int32_t kSortMaxRun = 65536;
+
+__device__ __forceinline__ void sift_down(int32_t *a, int32_t root, int32_t end) {
+  while (true) {
+    int32_t child = 2 * root + 1;
+    if (child >= end) return;
+    if (child + 1 < end && a[child] < a[child + 1]) ++child;
+    if (!(a[root] < a[child])) return;
+    const int32_t t = a[root];
+    a[root] = a[child];
+    a[child] = t;
+    root = child;
+  }
+}
+
 __global__ void k_segsort(long long n, const int32_t *__restrict__ starts,
-                          int32_t *__restrict__ perm) {
+                          int32_t *__restrict__ perm, int *__restrict__ crowded) {
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
        c += (long long)gridDim.x * blockDim.x) {
     int32_t s = starts[c], e = starts[c + 1];
-    for (int32_t a = s + 1; a < e; ++a) {
-      int32_t v = perm[a];
-      int32_t b = a - 1;
-      while (b >= s && perm[b] > v) {
-        perm[b + 1] = perm[b];
-        --b;
+    const int32_t m = e - s;
+    if (m <= 32) {
+      for (int32_t a = s + 1; a < e; ++a) {
+        int32_t v = perm[a];
+        int32_t b = a - 1;
+        while (b >= s && perm[b] > v) {
+          perm[b + 1] = perm[b];
+          --b;
+        }
+        perm[b + 1] = v;
       }
-      perm[b + 1] = v;
+    } else if (m <= kSortMaxRun) {
+      int32_t *a = perm + s;
+      for (int32_t i = m / 2 - 1; i >= 0; --i) sift_down(a, i, m);
+      for (int32_t end = m - 1; end > 0; --end) {
+        const int32_t t = a[0];
+        a[0] = a[end];
+        a[end] = t;
+        sift_down(a, 0, end);
+      }
+    } else {
+      *crowded = 1;
     }
   }
 }
@@ -731,7 +764,8 @@ void sort_by_cell(tpm_ctx *c, const int32_t *key, int32_t *perm, int32_t *starts
              c->scan_blocks, starts, (int32_t)c->np);
   TPM_LAUNCH(c, "sort_scatter", k_scatter, pblocks(c->np), kThreads, 0, key, c->np, starts,
              c->counts, perm);
-  TPM_LAUNCH(c, "sort_segsort", k_segsort, cell_blocks(c->g), kThreads, 0, n, starts, perm);
+  TPM_LAUNCH(c, "sort_segsort", k_segsort, cell_blocks(c->g), kThreads, 0, n, starts, perm,
+             &c->dsc->crowded);
 }
 
 __global__ void k_iota(int32_t *__restrict__ a, int64_t np) {
