@@ -42,7 +42,11 @@ FALLBACK_HBM_GBS = 6800.0
 # bench's own command (the profiles/ summary of that kernel gives the command)
 NCU_TRAFFIC = {
     # profiles/k_xfwd_resid_refine_mixed_box256_box128.md
-    ("box256_p8e6_heated", True, "fft_x_fwd_resid"): 8.35e8,
+    ("box256_p8e6_heated", True, "fft_x_fwd_resid"): 8.29e8,
+    # profiles/k_push_mixed_box256_box128.md
+    ("box256_p8e6_heated", True, "particle_push"): 2.99e9,
+    # the same capture (k_rhs_momentum<float, float>: 2.36 and 2.77 GB)
+    ("box256_p8e6_heated", True, "rhs_momentum"): 2.56e9,
 }
 
 KERNEL_BYTES = {
