@@ -10,6 +10,8 @@
 #include <random>
 
 #include "tpm_ff.cuh"
+#define TPM_HOST_CHECK
+#include "tpm_index.cuh"
 
 using namespace tpm;
 
@@ -93,6 +95,20 @@ int main() {
     long double ea = std::fabs((long double)ad.x + ad.y - (va + vb));
     CHECK(ea <= std::ldexp(std::fabs(va) + std::fabs(vb), -46), "add err %.3Lg", ea);
   }
+  // reciprocal of a split double and of a sum of two splits: within 2^-45
+  for (int n = 0; n < 2000000; ++n) {
+    const double x = std::ldexp(mant(rng), (int)(rng() % 200) - 100) * (rng() & 1 ? -1.0 : 1.0);
+    const float2 r = ff_rcp(ff_from_double(x));
+    const long double vx = pair_value(ff_from_double(x));
+    const long double er = std::fabs(((long double)r.x + r.y) * vx - 1.0L);
+    CHECK(er <= std::ldexp(1.0L, -45), "rcp x=%.17g err=%.3Lg", x, er);
+    const double a = mant(rng), b = mant(rng) * std::ldexp(1.0, (int)(rng() % 5) - 2);
+    const float2 s = ff_add(ff_from_double(a), ff_from_double(b));
+    const float2 h = ff_rcp(s);
+    const long double vs = (long double)s.x + s.y;
+    const long double eh = std::fabs(((long double)h.x + h.y) * vs - 1.0L);
+    CHECK(eh <= std::ldexp(1.0L, -45), "rcp of sum %.17g %.17g err=%.3Lg", a, b, eh);
+  }
   // trunc / fraction / half decision from the bits of a double
   for (int n = 0; n < 2000000; ++n) {
     const double u = (rng() & 1 ? -1.0 : 1.0) *
@@ -117,6 +133,23 @@ int main() {
               std::fabs((double)fr - f) <= std::ldexp(std::fabs(f), -23) &&
               up == (std::fabs(f) >= 0.5),
           "edge %.17g -> %d %.9g %d", u, ip, (double)fr, (int)up);
+  }
+  // index division: every divisor up to 4096 against edge and random
+  // numerators below 2^31
+  for (unsigned d = 1; d <= 4096; ++d) {
+    const unsigned long long m = udiv_magic(d);
+    const unsigned edges[] = {0u, 1u, d - 1u, d, d + 1u, 2u * d - 1u, 0x7ffffffeu,
+                              0x7fffffffu, (0x7fffffffu / d) * d, (0x7fffffffu / d) * d - 1u};
+    for (unsigned a : edges) CHECK(udiv(a, m) == a / d, "udiv %u / %u", a, d);
+    for (int n = 0; n < 2000; ++n) {
+      const unsigned a = (unsigned)(rng() & 0x7fffffffu);
+      CHECK(udiv(a, m) == a / d, "udiv %u / %u", a, d);
+    }
+  }
+  for (unsigned d : {3u, 7u, 256u, 1000u, 2048u, 65535u, 65536u}) {
+    const unsigned long long m = udiv_magic(d);
+    for (unsigned a : {0xffffffffu, 0xfffffffeu, 0x80000000u})
+      CHECK(udiv(a, m) == a / d, "udiv %u / %u", a, d);
   }
   if (fails) {
     std::printf("%d failures\n", fails);

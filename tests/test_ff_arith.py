@@ -4,8 +4,10 @@ against a stand-in cuda_runtime.h for its bit-cast intrinsics, with FP
 contraction off, and tests/ff_check.cpp checks the double split (2^-48 bound,
 truncated high part, zero / tiny / overflow / inf / nan), the exact float to
 double conversion, TwoSum's exactness, the bounds of the product, the sums
-and the difference of close pairs, and the integer part / fraction / half
-decision read from a double's bits."""
+and the difference of close pairs, the reciprocal (2^-45 bound), the
+integer part / fraction / half decision read from a double's bits, and the
+index division by a multiply-high (csrc/tpm_index.cuh) against the integer
+quotient."""
 import os
 import shutil
 import subprocess
@@ -28,6 +30,8 @@ inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); retu
 inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
 inline float __uint2float_rn(unsigned u) { return (float)u; }
 inline int __clzll(long long x) { return __builtin_clzll((unsigned long long)x); }
+inline float __frcp_rn(float x) { return 1.0f / x; }
+inline unsigned __umulhi(unsigned a, unsigned b) { return (unsigned)(((unsigned long long)a * b) >> 32); }
 """
 
 

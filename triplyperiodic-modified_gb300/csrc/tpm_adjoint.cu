@@ -40,8 +40,9 @@ constexpr int kAT = 256;
 constexpr double kPreA[4] = {0.5, 0.5, 1., 1. / 6.};          // grid.cpp:18-21
 constexpr double kPostA[4] = {1. / 6., 1. / 3., 1. / 3., 1. / 6.};
 
+// flat index in 32-bit arithmetic (every box has fewer than 2^31 cells)
 __device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
-  return ((long long)k * g.ny + j) * g.nx + i;
+  return (long long)((k * g.ny + j) * g.nx + i);
 }
 
 struct Ix {
@@ -50,9 +51,7 @@ struct Ix {
 
 __device__ __forceinline__ Ix ix_of(const Grid &g, long long c) {
   Ix r;
-  r.i = (int)(c % g.nx);
-  r.j = (int)((c / g.nx) % g.ny);
-  r.k = (int)(c / ((long long)g.nx * g.ny));
+  cell_ijk(g, c, r.i, r.j, r.k);
   return r;
 }
 

@@ -331,8 +331,10 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     return fail(c, TPM_ERR_ARG, "iteration counts must be >= 0");
   return guarded(c, [&]() -> int {
     TPM_CUDA_TRY(cudaGetDevice(&c->dev));
+    TPM_CUDA_TRY(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->dev));
     Grid &g = c->g;
     g.nx = p->Nx; g.ny = p->Ny; g.nz = p->Nz; g.nxh = p->Nx / 2 + 1; g.n = n;
+    g.mx = tpm::udiv_magic((unsigned)p->Nx); g.my = tpm::udiv_magic((unsigned)p->Ny);
     g.Lx = p->Lx; g.Ly = p->Ly; g.Lz = p->Lz;
     g.dx = p->Lx / p->Nx; g.dy = p->Ly / p->Ny; g.dz = p->Lz / p->Nz;  // gridsize.cpp:25-27
     g.inv_dx = 1. / g.dx; g.inv_dy = 1. / g.dy; g.inv_dz = 1. / g.dz;  // tensor0.cpp:17-22
@@ -394,7 +396,8 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->hsc->P0 = c->hsc->P0_int = c->hsc->P0_np1 = c->hsc->P0_new = c->P0ref;
     push_scalars(c);
     tpm::fft_plans_create(c);
-    tpm::rhs_kernels_setup();
+    tpm::rhs_kernels_setup(c);
+    tpm::particle_kernels_setup(c);
     c->err_parts = dalloc<double>(c, (size_t)g.ny * g.nz);
     // particles
     for (int s = 0; s < 4; ++s)

@@ -70,8 +70,9 @@ __device__ double block_reduce(int op, double v, double *sh) {
   return r;
 }
 
+// flat index in 32-bit arithmetic (every box has fewer than 2^31 cells)
 __device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
-  return ((long long)k * g.ny + j) * g.nx + i;
+  return (long long)((k * g.ny + j) * g.nx + i);
 }
 
 // U = RU / I_C2F(Rho), the velocity grid::Statistics forms from RU_np1 and
@@ -81,7 +82,8 @@ __global__ void k_diag_velocity(Grid g, const double *__restrict__ RU,
                                 const double *__restrict__ Rho, double *__restrict__ U) {
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % g.nx), j = (int)((c / g.nx) % g.ny), k = (int)(c / ((long long)g.nx * g.ny));
+    int i, j, k;
+    cell_ijk(g, c, i, j, k);
     const double r = Rho[c];
     U[c] = RU[c] / ((r + Rho[at(g, wrap_m(i, g.nx), j, k)]) * 0.5);
     U[g.n + c] = RU[g.n + c] / ((r + Rho[at(g, i, wrap_m(j, g.ny), k)]) * 0.5);
@@ -107,7 +109,8 @@ k_diag_cells(Grid g, const double *__restrict__ Rho, const double *__restrict__ 
   const double *u = U, *vv = U + g.n, *w = U + 2 * g.n;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % g.nx), j = (int)((c / g.nx) % g.ny), k = (int)(c / ((long long)g.nx * g.ny));
+    int i, j, k;
+    cell_ijk(g, c, i, j, k);
     const double r = Rho[c];
     v[S_RHO_SUM] += r;
     v[S_RHO_MAX] = r > v[S_RHO_MAX] ? r : v[S_RHO_MAX];

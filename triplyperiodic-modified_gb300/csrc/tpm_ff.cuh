@@ -178,4 +178,15 @@ __device__ __forceinline__ double ff_widen(float x) { return ff_f2d(x); }
 // small against hi, as ff_mul leaves them)
 __device__ __forceinline__ float2 ff_norm(float2 a) { return ff_fast_two_sum(a.x, a.y); }
 
+// 1/h for a pair h with |lo| <= 2^-23 |hi| and hi a normal float, within
+// 2^-45 |1/h|, on the FP32 pipe.  y = 1/hi rounded; 1 - hi y is exact as one
+// FMA for a correctly rounded reciprocal, and e = 1 - h y follows with the
+// low part; then 1/h = y / (1 - e) = y (1 + e + e^2) up to e^3 (|e| < 2^-22).
+__device__ __forceinline__ float2 ff_rcp(float2 h) {
+  const float y = __frcp_rn(h.x);
+  const float r = fmaf(-h.x, y, 1.0f);
+  const float e = fmaf(-h.y, y, r);
+  return ff_fast_two_sum(y, y * fmaf(e, e, e));
+}
+
 }  // namespace tpm

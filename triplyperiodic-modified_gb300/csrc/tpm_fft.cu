@@ -177,8 +177,9 @@ __device__ T2 *smem_fft(T2 *a, T2 *b, int npen, const FftPlan &pl, int sign) {
   return a;
 }
 
+// flat index in 32-bit arithmetic (every box has fewer than 2^31 cells)
 __device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
-  return ((long long)k * g.ny + j) * g.nx + i;
+  return (long long)((k * g.ny + j) * g.nx + i);
 }
 
 // Real-to-complex post-processing of npen x-rows held as Nx/2-point complex
@@ -230,7 +231,8 @@ __global__ void k_xfwd_resid(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
     const long long row = row0 + q;
     double r = 0;
     if (row < nrows) {
-      const int j = (int)(row % g.ny), k = (int)(row / g.ny);
+      int j, k;
+      row_jk(g, row, j, k);
       const long long c = at(g, i, j, k);
       const int ip = wrap_p(i, g.nx), im = wrap_m(i, g.nx);
       const int jp = wrap_p(j, g.ny), jm = wrap_m(j, g.ny);
@@ -294,7 +296,8 @@ __global__ void k_xfwd_resid_refine(Grid g, FftPlan pl, const float2 *__restrict
     const long long row = row0 + q;
     float r = 0.f;
     if (row < nrows) {
-      const int j = (int)(row % g.ny), k = (int)(row / g.ny);
+      int j, k;
+      row_jk(g, row, j, k);
       const long long c = at(g, i, j, k);
       const long long cxm = at(g, wrap_m(i, g.nx), j, k), cxp = at(g, wrap_p(i, g.nx), j, k);
       const long long cym = at(g, i, wrap_m(j, g.ny), k), cyp = at(g, i, wrap_p(j, g.ny), k);
@@ -1025,9 +1028,8 @@ __global__ void k_center_coeff_noalloc(Grid g, const double *__restrict__ Cf, do
   const double OneThird = 1. / 3.;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % g.nx);
-    const long long t = c / g.nx;
-    const int j = (int)(t % g.ny), k = (int)(t / g.ny);
+    int i, j, k;
+    cell_ijk(g, c, i, j, k);
     const long long cxp = at(g, wrap_p(i, g.nx), j, k), cyp = at(g, i, wrap_p(j, g.ny), k),
                     czp = at(g, i, j, wrap_p(k, g.nz));
     double m = OneThird * ((Cf[c] + Cf[cxp]) * 0.5 + (Cf[g.n + c] + Cf[g.n + cyp]) * 0.5 +
@@ -1057,6 +1059,7 @@ extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, doub
   Grid g;
   g.nx = Nx; g.ny = Ny; g.nz = Nz; g.nxh = Nx / 2 + 1;
   g.n = (long long)Nx * Ny * Nz;
+  g.mx = tpm::udiv_magic((unsigned)Nx); g.my = tpm::udiv_magic((unsigned)Ny);
   g.Lx = Lx; g.Ly = Ly; g.Lz = Lz;
   g.dx = Lx / Nx; g.dy = Ly / Ny; g.dz = Lz / Nz;
   g.inv_dx = 1. / g.dx; g.inv_dy = 1. / g.dy; g.inv_dz = 1. / g.dz;

@@ -6,6 +6,10 @@
 // reference's floating-point operation order and the library is compiled
 // with --fmad=false, so apart from reductions and the FFT the results are
 // the reference's to the last bit.
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "tpm_internal.cuh"
 #include "tpm_ff.cuh"
 #include "tpm_reduce.cuh"
@@ -23,15 +27,13 @@ struct Cell {
 __device__ __forceinline__ Cell cell_of(const Grid &g, long long c) {
   Cell r;
   r.c = c;
-  r.i = (int)(c % g.nx);
-  long long t = c / g.nx;
-  r.j = (int)(t % g.ny);
-  r.k = (int)(t / g.ny);
+  cell_ijk(g, c, r.i, r.j, r.k);
   return r;
 }
 
+// flat index in 32-bit arithmetic (every box has fewer than 2^31 cells)
 __device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
-  return ((long long)k * g.ny + j) * g.nx + i;
+  return (long long)((k * g.ny + j) * g.nx + i);
 }
 
 // ---------------------------------------------------------------- P0 update
@@ -105,7 +107,18 @@ struct RhsArgs {
   double A, Rho0, g[3];
   double dtpo, dtpr;
   int stage, has_g;
+  // the same coefficients and 1/d, 1/d^2 rounded to FP32 on the host, for
+  // the FP32 stencil (no per-thread FP64 conversions)
+  float f_a_fp, f_b_gd, f_c_lap, f_A, f_Rho0, f_g[3], f_inv_d[3], f_inv_d2[3];
 };
+
+// a coefficient in the compute type: the FP64 value or its FP32 copy
+template <typename TC>
+__device__ __forceinline__ TC coef(double d, float f);
+template <>
+__device__ __forceinline__ double coef<double>(double d, float) { return d; }
+template <>
+__device__ __forceinline__ float coef<float>(double, float f) { return f; }
 
 // offsets of the neighbour in direction e (0,1,2) at +1 / -1, wrapped
 struct Nbr {
@@ -126,12 +139,13 @@ __device__ __forceinline__ Nbr nbr_of(const Grid &g, const Cell &q) {
 // evaluated in the compute type TC (double on the FP64 path, float on the
 // mixed path; the loads convert)
 template <typename TC, typename TIn>
-__device__ __forceinline__ TC divU_at(const Grid &g, const TIn *U, int i, int j, int k) {
+__device__ __forceinline__ TC divU_at(const Grid &g, const TIn *U, int i, int j, int k,
+                                      const TC *inv_d) {
   long long c = at(g, i, j, k);
   const TIn *Ux = U, *Uy = U + g.n, *Uz = U + 2 * g.n;
-  return ((TC)Ux[at(g, wrap_p(i, g.nx), j, k)] - (TC)Ux[c]) * (TC)g.inv_dx +
-         ((TC)Uy[at(g, i, wrap_p(j, g.ny), k)] - (TC)Uy[c]) * (TC)g.inv_dy +
-         ((TC)Uz[at(g, i, j, wrap_p(k, g.nz))] - (TC)Uz[c]) * (TC)g.inv_dz;
+  return ((TC)Ux[at(g, wrap_p(i, g.nx), j, k)] - (TC)Ux[c]) * inv_d[0] +
+         ((TC)Uy[at(g, i, wrap_p(j, g.ny), k)] - (TC)Uy[c]) * inv_d[1] +
+         ((TC)Uz[at(g, i, j, wrap_p(k, g.nz))] - (TC)Uz[c]) * inv_d[2];
 }
 
 __device__ __forceinline__ long long shift(const Grid &g, int i, int j, int k, int dir, int s) {
@@ -159,20 +173,25 @@ __global__ void k_rhs_momentum(Grid g, const TIn *__restrict__ U, const TIn *__r
                                const TIn *__restrict__ Fp, const double *__restrict__ Rho_int,
                                const double *__restrict__ RU, const double *__restrict__ np1_in,
                                double *__restrict__ RU_np1, double *__restrict__ RU_new, RhsArgs a) {
-  const TC inv_d[3] = {(TC)g.inv_dx, (TC)g.inv_dy, (TC)g.inv_dz};
-  const TC inv_d2[3] = {(TC)g.inv_dx2, (TC)g.inv_dy2, (TC)g.inv_dz2};
-  // the coefficients once per thread; per-cell FP64 values below go through
-  // ff_cast / ff_widen (integer operations when TC is float)
-  const TC a_fp = (TC)a.a_fp, b_gd = (TC)a.b_gd, c_lap = (TC)a.c_lap, A_ = (TC)a.A;
-  const TC Rho0 = (TC)a.Rho0, gv[3] = {(TC)a.g[0], (TC)a.g[1], (TC)a.g[2]};
+  const TC inv_d[3] = {coef<TC>(g.inv_dx, a.f_inv_d[0]), coef<TC>(g.inv_dy, a.f_inv_d[1]),
+                       coef<TC>(g.inv_dz, a.f_inv_d[2])};
+  const TC inv_d2[3] = {coef<TC>(g.inv_dx2, a.f_inv_d2[0]), coef<TC>(g.inv_dy2, a.f_inv_d2[1]),
+                        coef<TC>(g.inv_dz2, a.f_inv_d2[2])};
+  // per-cell FP64 values below go through ff_cast / ff_widen (integer
+  // operations when TC is float)
+  const TC a_fp = coef<TC>(a.a_fp, a.f_a_fp), b_gd = coef<TC>(a.b_gd, a.f_b_gd);
+  const TC c_lap = coef<TC>(a.c_lap, a.f_c_lap), A_ = coef<TC>(a.A, a.f_A);
+  const TC Rho0 = coef<TC>(a.Rho0, a.f_Rho0);
+  const TC gv[3] = {coef<TC>(a.g[0], a.f_g[0]), coef<TC>(a.g[1], a.f_g[1]),
+                    coef<TC>(a.g[2], a.f_g[2])};
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
     Nbr nb = nbr_of(g, q);
-    const TC div_c = divU_at<TC, TIn>(g, U, q.i, q.j, q.k);
-    const TC div_m[3] = {divU_at<TC, TIn>(g, U, wrap_m(q.i, g.nx), q.j, q.k),
-                         divU_at<TC, TIn>(g, U, q.i, wrap_m(q.j, g.ny), q.k),
-                         divU_at<TC, TIn>(g, U, q.i, q.j, wrap_m(q.k, g.nz))};
+    const TC div_c = divU_at<TC, TIn>(g, U, q.i, q.j, q.k, inv_d);
+    const TC div_m[3] = {divU_at<TC, TIn>(g, U, wrap_m(q.i, g.nx), q.j, q.k, inv_d),
+                         divU_at<TC, TIn>(g, U, q.i, wrap_m(q.j, g.ny), q.k, inv_d),
+                         divU_at<TC, TIn>(g, U, q.i, q.j, wrap_m(q.k, g.nz), inv_d)};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const TIn *Ud = U + d * g.n;
@@ -416,48 +435,54 @@ __global__ void k_poisson_rhs2(Grid g, const double *__restrict__ inv_rho,
 }
 
 // ------------------------------------------------ mixed-path variants
-// 1/x to FP64 accuracy from an FP32 seed and two Newton steps (4 FMAs): on
-// GB300 an FP64 division costs several times that on the scarce FP64 pipe.
-__device__ __forceinline__ double rcp64(double x) {
-  double r = ff_f2d(__frcp_rn(ff_hi(x)));  // seed without FP64-pipe conversions
-  double e = __fma_rn(-x, r, 1.0);
-  r = __fma_rn(r, e, r);
-  e = __fma_rn(-x, r, 1.0);
-  return __fma_rn(r, e, r);
-}
-
-// k_rho_update of the mixed path: same FP64 density update, reciprocals
-// instead of divisions
+// k_rho_update of the mixed path: the same FP64 update of the density state
+// (Rho_np1, Rho_new by FMAs), with the divergence of RU_int and the
+// reciprocal 1/Rho_new formed as float-float pairs on the FP32 pipe (each
+// within 2^-45 of its value).  1/Rho_new is stored as its pair (inv_rho2, in
+// the FP64 path's inv_rho buffer): its one reader, the mixed Poisson
+// right-hand side, works in pairs.  FP64 operations per cell: four, against
+// twelve in FP64 arithmetic.
 __global__ void k_rho_update_mixed(Grid g, const double *__restrict__ RUi,
                                    const double *__restrict__ Rho, const double *__restrict__ np1_in,
                                    double *__restrict__ Rho_np1, double *__restrict__ Rho_new,
-                                   double *__restrict__ inv_rho, double *__restrict__ Tgas,
+                                   float2 *__restrict__ inv_rho2, double *__restrict__ Tgas,
                                    const DevScalars *__restrict__ s, double a_np1, double b_new,
                                    int stage) {
   const double *RUx = RUi, *RUy = RUi + g.n, *RUz = RUi + 2 * g.n;
   const double T_scale = s->T_scale;
+  const float2 inv_d[3] = {ff_from_double(g.inv_dx), ff_from_double(g.inv_dy),
+                           ff_from_double(g.inv_dz)};
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
-    double D = (RUx[at(g, wrap_p(q.i, g.nx), q.j, q.k)] - RUx[c]) * g.inv_dx;
-    D = fma(RUy[at(g, q.i, wrap_p(q.j, g.ny), q.k)] - RUy[c], g.inv_dy, D);
-    D = fma(RUz[at(g, q.i, q.j, wrap_p(q.k, g.nz))] - RUz[c], g.inv_dz, D);
-    double np1 = fma(a_np1, D, np1_in[c]);
-    double nw = (stage != 3) ? fma(b_new, D, Rho[c]) : np1;
+    float2 D = ff_mul(ff_sub(ff_from_double(RUx[at(g, wrap_p(q.i, g.nx), q.j, q.k)]),
+                             ff_from_double(RUx[c])),
+                      inv_d[0]);
+    D = ff_add(D, ff_mul(ff_sub(ff_from_double(RUy[at(g, q.i, wrap_p(q.j, g.ny), q.k)]),
+                                ff_from_double(RUy[c])),
+                         inv_d[1]));
+    D = ff_add(D, ff_mul(ff_sub(ff_from_double(RUz[at(g, q.i, q.j, wrap_p(q.k, g.nz))]),
+                                ff_from_double(RUz[c])),
+                         inv_d[2]));
+    const double Dd = ff_to_double(D);
+    double np1 = fma(a_np1, Dd, np1_in[c]);
+    double nw = (stage != 3) ? fma(b_new, Dd, Rho[c]) : np1;
     Rho_np1[c] = np1;
     Rho_new[c] = nw;
-    double ir = rcp64(nw);
-    inv_rho[c] = ir;
-    Tgas[c] = T_scale * ir;
+    const float2 ir = ff_rcp(ff_from_double(nw));
+    inv_rho2[c] = ir;
+    Tgas[c] = T_scale * ff_to_double(ir);
   }
 }
 
 // Face coefficients of the mixed path, C = 1/Rho_face(Rho_new) on the three
-// lower faces of each cell (each face once), from an FP32 seed and one FP64
-// Newton step (~1e-14 relative; an FP32 C would perturb the divergence
-// constraint at 1e-7, which the nearly divergence-free right-hand side
-// amplifies in P).  C/d^2 feeds the refinement's residual as a float-float
-// pair (Cs2) and, for the PCG operator only, as a double (Cs, else null).
+// lower faces of each cell (each face once), as float-float pairs on the FP32
+// pipe: 2 / (Rho + Rho_m) from the pair sum of the two densities (within
+// 2^-45; an FP32 C would perturb the divergence constraint at 1e-7, which the
+// nearly divergence-free right-hand side amplifies in P).  C is stored as a
+// double (one FP64 addition per face) and, times 1/d^2, as the pair (Cs2)
+// that feeds the refinement's residual; for the PCG operator only also as a
+// double C/d^2 (Cs, else null).
 __global__ void k_face_coeff_mixed(Grid g, const double *__restrict__ Rho_new,
                                    double *__restrict__ Cface, float2 *__restrict__ Cs2,
                                    double *__restrict__ Cs) {
@@ -468,15 +493,14 @@ __global__ void k_face_coeff_mixed(Grid g, const double *__restrict__ Rho_new,
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
     Nbr nb = nbr_of(g, q);
-    const double r = Rho_new[c];
+    const float2 r = ff_from_double(Rho_new[c]);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      // FP32 seed of 1/rho_face with no FP64-pipe conversion, one Newton step
-      const double h = (r + Rho_new[nb.m[d]]) * 0.5;
-      const double r0 = ff_f2d(__frcp_rn(ff_hi(h)));
-      const double clo = __fma_rn(r0, __fma_rn(-h, r0, 1.0), r0);
+      const float2 h = ff_rcp(ff_add(r, ff_from_double(Rho_new[nb.m[d]])));
+      const float2 C = make_float2(2.f * h.x, 2.f * h.y);
+      const double clo = ff_to_double(C);
       Cface[d * g.n + c] = clo;
-      Cs2[d * g.n + c] = ff_norm(ff_mul(ff_from_double(clo), inv_d2f[d]));
+      Cs2[d * g.n + c] = ff_norm(ff_mul(C, inv_d2f[d]));
       if (Cs) Cs[d * g.n + c] = clo * inv_d2[d];
     }
   }
@@ -498,7 +522,7 @@ __global__ void k_face_coeff_mixed(Grid g, const double *__restrict__ Rho_new,
 // last stage) against about twenty-four for the same sums in FP64.  The
 // preconditioner scale cc is FP32 (it sets the rate of the Richardson
 // iteration, not its fixed point).
-__global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
+__global__ void k_poisson_rhs_mixed(Grid g, const float2 *__restrict__ inv_rho2,
                                     const double *__restrict__ Q, const double *__restrict__ RUn,
                                     const double *__restrict__ Cface,
                                     const DevScalars *__restrict__ s, double *__restrict__ RHS,
@@ -517,12 +541,11 @@ __global__ void k_poisson_rhs_mixed(Grid g, const double *__restrict__ inv_rho,
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
     Nbr nb = nbr_of(g, q);
-    const float2 ir = ff_from_double(inv_rho[c]);
+    const float2 ir = inv_rho2[c];
     float2 lap = make_float2(0.f, 0.f);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const float2 sec = ff_add(ff_sub(ff_from_double(inv_rho[nb.p[d]]), ir),
-                                ff_sub(ff_from_double(inv_rho[nb.m[d]]), ir));
+      const float2 sec = ff_add(ff_sub(inv_rho2[nb.p[d]], ir), ff_sub(inv_rho2[nb.m[d]], ir));
       lap = ff_add(lap, ff_mul(sec, inv_d2[d]));
     }
     float2 Qc = ff_from_double(Q[c]);
@@ -656,10 +679,10 @@ __global__ void k_ps_face(Grid g, const double *__restrict__ src, double *__rest
 }
 
 // ---------------------------------------------------------- projection
-// grid::Update_RU_WP, grid.cpp:857-863.  At the last stage the per-component
-// sums of RU_np1 for make_mean_U0 (simulation.cpp:80) are reduced too.
-// kFma (mixed path): the updates as FMAs
-template <bool kFma>
+// grid::Update_RU_WP, grid.cpp:857-863.  At the last stage (kSum) the
+// per-component sums of RU_np1 for make_mean_U0 (simulation.cpp:80) are
+// reduced too.  kFma (mixed path): the updates as FMAs
+template <bool kFma, bool kSum>
 __global__ void k_project(Grid g, const double *__restrict__ P, double *__restrict__ RU_np1,
                           double *__restrict__ RU_new, double a_np1, double b_new, int stage,
                           double *__restrict__ partials, float *__restrict__ RUn32) {
@@ -685,10 +708,10 @@ __global__ void k_project(Grid g, const double *__restrict__ P, double *__restri
                                      : np1;
       RU_new[d * g.n + c] = nw;
       if (RUn32) RUn32[d * g.n + c] = ff_hi(nw);
-      acc[d] += np1;
+      if (kSum) acc[d] += np1;
     }
   }
-  if (stage == 3) {
+  if (kSum) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       double bs = block_sum(acc[d], sh);
@@ -803,6 +826,39 @@ int cell_blocks(const Grid &g) {
   return (int)(b < kRedBlocks ? b : kRedBlocks);
 }
 
+int wave_blocks(tpm_ctx *c, const void *kernel, int threads, long long items, bool reduces) {
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, int> occ;
+  int per_sm = 0;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = occ.find({kernel, threads});
+    if (it != occ.end()) {
+      per_sm = it->second;
+    } else {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) !=
+              cudaSuccess ||
+          per_sm < 1)
+        per_sm = 1;
+      occ[{kernel, threads}] = per_sm;
+    }
+  }
+  const long long sms = c->sms > 0 ? c->sms : 1;
+  long long b = sms * per_sm;
+  if (reduces && b > kRedBlocks) b = sms <= kRedBlocks ? (kRedBlocks / sms) * sms : kRedBlocks;
+  const long long need = (items + threads - 1) / threads;
+  if (need < b) b = need > 0 ? need : 1;
+  return (int)b;
+}
+
+namespace {
+// wave_blocks for a cell kernel of this file (kThreads per block)
+template <typename K>
+int cell_waves(tpm_ctx *c, K *kernel, bool reduces) {
+  return wave_blocks(c, reinterpret_cast<const void *>(kernel), kThreads, c->g.n, reduces);
+}
+}  // namespace
+
 static const double kPre[4] = {0.5, 0.5, 1., 1. / 6.};          // grid.cpp:18-21
 static const double kPost[4] = {1. / 6., 1. / 3., 1. / 3., 1. / 6.};  // grid.cpp:22-25
 
@@ -814,23 +870,28 @@ void launch_p0_update(tpm_ctx *c, int s) {
 
 void launch_rho_update(tpm_ctx *c, int s, bool np1_in_base) {
   if (c->p.precision == TPM_PREC_MIXED) {
-    TPM_LAUNCH(c, "rho_update", k_rho_update_mixed, cell_blocks(c->g), kThreads, 0, c->g,
+    TPM_LAUNCH(c, "rho_update", k_rho_update_mixed, cell_waves(c, k_rho_update_mixed, false),
+               kThreads, 0, c->g,
                c->RU_int, c->Rho, np1_in_base ? c->Rho : c->Rho_np1, c->Rho_np1, c->Rho_new,
-               c->inv_rho, c->Tgas, c->dsc, -(c->p.dt * kPost[s]), -c->p.dt * kPre[s], s);
+               reinterpret_cast<float2 *>(c->inv_rho), c->Tgas, c->dsc, -(c->p.dt * kPost[s]),
+               -c->p.dt * kPre[s], s);
     return;
   }
-  TPM_LAUNCH(c, "rho_update", k_rho_update, cell_blocks(c->g), kThreads, 0, c->g, c->RU_int,
+  TPM_LAUNCH(c, "rho_update", k_rho_update, cell_waves(c, k_rho_update, false), kThreads, 0,
+             c->g, c->RU_int,
              c->Rho, np1_in_base ? c->Rho : c->Rho_np1, c->Rho_np1, c->Rho_new, c->inv_rho,
              c->Tgas, c->dsc, -(c->p.dt * kPost[s]), -c->p.dt * kPre[s], s);
 }
 
 void launch_face_velocity(tpm_ctx *c) {
   if (c->p.precision == TPM_PREC_MIXED) {
-    TPM_LAUNCH(c, "face_velocity", k_face_velocity_mixed, cell_blocks(c->g), kThreads, 0, c->g,
+    TPM_LAUNCH(c, "face_velocity", k_face_velocity_mixed,
+               cell_waves(c, k_face_velocity_mixed, false), kThreads, 0, c->g,
                c->RUi32, c->Rho_int, c->U32);
     return;
   }
-  TPM_LAUNCH(c, "face_velocity", k_face_velocity, cell_blocks(c->g), kThreads, 0, c->g,
+  TPM_LAUNCH(c, "face_velocity", k_face_velocity, cell_waves(c, k_face_velocity, false),
+             kThreads, 0, c->g,
              c->RU_int, c->Rho_int, c->U);
 }
 
@@ -848,12 +909,22 @@ void launch_rhs_momentum(tpm_ctx *c, int s, bool np1_in_base) {
   a.dtpo = c->p.dt * kPost[s];
   a.dtpr = c->p.dt * kPre[s];
   a.stage = s;
+  a.f_a_fp = (float)a.a_fp; a.f_b_gd = (float)a.b_gd; a.f_c_lap = (float)a.c_lap;
+  a.f_A = (float)a.A; a.f_Rho0 = (float)a.Rho0;
+  const double inv_d[3] = {c->g.inv_dx, c->g.inv_dy, c->g.inv_dz};
+  const double inv_d2[3] = {c->g.inv_dx2, c->g.inv_dy2, c->g.inv_dz2};
+  for (int d = 0; d < 3; ++d) {
+    a.f_g[d] = (float)a.g[d];
+    a.f_inv_d[d] = (float)inv_d[d];
+    a.f_inv_d2[d] = (float)inv_d2[d];
+  }
   const int tiles = ((c->g.nx + kTX - 1) / kTX) * ((c->g.ny + kTY - 1) / kTY) *
                     ((c->g.nz + kTZ - 1) / kTZ);
   // FP32: the cached per-cell form is faster (6.1 ms tiled vs 4.2 ms per 256^3
   // step); FP64: the tiled form saves FP64 issue slots (28.7 vs 31.5 ms).
   if (c->p.precision == TPM_PREC_MIXED)
-    TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum<float, float>), cell_blocks(c->g), kThreads, 0,
+    TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum<float, float>),
+               cell_waves(c, k_rhs_momentum<float, float>, false), kThreads, 0,
                c->g, c->U32, c->RUi32, c->Fp32, c->Rho_int, c->RU,
                np1_in_base ? c->RU : c->RU_np1, c->RU_np1, c->RU_new, a);
   else
@@ -868,20 +939,23 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
   a.inv_dtpre = (1. / (c->p.dt * kPre[s]));
   a.cooling = c->p.cooling;
   a.store_div = store_div;
-  int nb = cell_blocks(c->g);
+  const bool mixed = c->p.precision == TPM_PREC_MIXED;
+  const int nb = mixed ? cell_waves(c, k_poisson_rhs_mixed, true)
+                       : cell_waves(c, k_poisson_rhs2, true);
   double *tke_parts = s == 3 ? c->partials + kPartTke2 * kRedBlocks : nullptr;
-  if (c->p.precision == TPM_PREC_MIXED) {
+  if (mixed) {
     const bool pcg = c->p.Solver == 2;
-    TPM_LAUNCH(c, "face_coeff", k_face_coeff_mixed, nb, kThreads, 0, c->g, c->Rho_new, c->Cface,
-               c->Cs2, pcg ? c->Cs : nullptr);
-    TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_mixed, nb, kThreads, 0, c->g, c->inv_rho, c->Q,
+    TPM_LAUNCH(c, "face_coeff", k_face_coeff_mixed, cell_waves(c, k_face_coeff_mixed, false),
+               kThreads, 0, c->g, c->Rho_new, c->Cface, c->Cs2, pcg ? c->Cs : nullptr);
+    TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_mixed, nb, kThreads, 0, c->g,
+               reinterpret_cast<const float2 *>(c->inv_rho), c->Q,
                c->RU_new, c->Cface, c->dsc, c->RHS, c->divg, c->cc32, pcg ? c->cc : nullptr,
                c->partials + kPartRhs * kRedBlocks, tke_parts, a);
   } else {
     // c->U (the face velocity of RU_int) is dead after the momentum RHS; it
     // holds RU_new/Rho_face here
-    TPM_LAUNCH(c, "poisson_faces", k_poisson_faces, nb, kThreads, 0, c->g, c->Rho_new, c->RU_new,
-               c->Cface, c->U);
+    TPM_LAUNCH(c, "poisson_faces", k_poisson_faces, cell_waves(c, k_poisson_faces, false),
+               kThreads, 0, c->g, c->Rho_new, c->RU_new, c->Cface, c->U);
     TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs2, nb, kThreads, 0, c->g, c->inv_rho, c->Q, c->U,
                c->Cface, c->dsc, c->RHS, c->divg, c->cc, c->partials + kPartRhs * kRedBlocks,
                tke_parts, a);
@@ -895,15 +969,13 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
 }
 
 void launch_project(tpm_ctx *c, int s) {
-  int nb = cell_blocks(c->g);
-  if (c->p.precision == TPM_PREC_MIXED)
-    TPM_LAUNCH(c, "project", k_project<true>, nb, kThreads, 0, c->g, c->P, c->RU_np1, c->RU_new,
-               -(c->p.dt * kPost[s]), -(c->p.dt * kPre[s]), s,
-               c->partials + kPartRu * kRedBlocks, c->RUn32);
-  else
-    TPM_LAUNCH(c, "project", k_project<false>, nb, kThreads, 0, c->g, c->P, c->RU_np1, c->RU_new,
-               -(c->p.dt * kPost[s]), -(c->p.dt * kPre[s]), s,
-               c->partials + kPartRu * kRedBlocks, nullptr);
+  const bool mixed = c->p.precision == TPM_PREC_MIXED;
+  auto kern = mixed ? (s == 3 ? k_project<true, true> : k_project<true, false>)
+                    : (s == 3 ? k_project<false, true> : k_project<false, false>);
+  const int nb = cell_waves(c, kern, true);
+  TPM_LAUNCH(c, "project", kern, nb, kThreads, 0, c->g, c->P, c->RU_np1, c->RU_new,
+             -(c->p.dt * kPost[s]), -(c->p.dt * kPre[s]), s,
+             c->partials + kPartRu * kRedBlocks, mixed ? c->RUn32 : nullptr);
   if (s == 3)
     TPM_LAUNCH(c, "finish_means3", k_finish_means3, 1, kThreads, 0,
                c->partials + kPartRu * kRedBlocks, nb, c->g.n,
@@ -919,22 +991,25 @@ void launch_passive_scalar(tpm_ctx *c, int s, bool np1_in_base) {
   a.s1_type = c->p.S1_type;
   const double *np1_in = np1_in_base ? c->PS : c->PS_np1;
   if (c->p.precision == TPM_PREC_MIXED)
-    TPM_LAUNCH(c, "passive_scalar", k_passive_scalar<float>, cell_blocks(c->g), kThreads, 0,
+    TPM_LAUNCH(c, "passive_scalar", k_passive_scalar<float>,
+               cell_waves(c, k_passive_scalar<float>, false), kThreads, 0,
                c->g, c->U32, c->PS_face, c->PS_int, c->PS, np1_in, c->PS_np1, c->PS_new, c->S1,
                a);
   else
-    TPM_LAUNCH(c, "passive_scalar", k_passive_scalar<double>, cell_blocks(c->g), kThreads, 0,
+    TPM_LAUNCH(c, "passive_scalar", k_passive_scalar<double>,
+               cell_waves(c, k_passive_scalar<double>, false), kThreads, 0,
                c->g, c->U, c->PS_face, c->PS_int, c->PS, np1_in, c->PS_np1, c->PS_new, c->S1, a);
   launch_passive_scalar_face(c, c->PS_new);
 }
 
 void launch_passive_scalar_face(tpm_ctx *c, const double *src) {
-  TPM_LAUNCH(c, "passive_scalar_face", k_ps_face, cell_blocks(c->g), kThreads, 0, c->g, src,
+  TPM_LAUNCH(c, "passive_scalar_face", k_ps_face, cell_waves(c, k_ps_face, false), kThreads, 0,
+             c->g, src,
              c->PS_face);
 }
 
 void launch_div_residual(tpm_ctx *c, int s) {
-  int nb = cell_blocks(c->g);
+  const int nb = cell_waves(c, k_div_residual, true);
   TPM_LAUNCH(c, "div_residual", k_div_residual, nb, kThreads, 0, c->g, c->RU_new, c->Cface,
              c->divg, c->dsc, c->p.dt * kPre[s], c->partials + kPartDiv * kRedBlocks);
   TPM_LAUNCH(c, "finish_max_div", k_finish_max_div, 1, kThreads, 0,
@@ -949,14 +1024,35 @@ void launch_to_double(tpm_ctx *c, const float *src, double *dst, long long n) {
   TPM_LAUNCH(c, "to_double", k_to_double, cell_blocks(c->g), kThreads, 0, src, dst, n);
 }
 
-void rhs_kernels_setup() {
+void rhs_kernels_setup(tpm_ctx *c) {
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_rhs_momentum_tiled<double, double>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)rhs_tiled_smem<double>()));
+  // the occupancy of every wave-sized kernel, queried here once (not while a
+  // step is being captured into a graph)
+  cell_waves(c, k_rho_update_mixed, false);
+  cell_waves(c, k_rho_update, false);
+  cell_waves(c, k_face_velocity_mixed, false);
+  cell_waves(c, k_face_velocity, false);
+  cell_waves(c, k_rhs_momentum<float, float>, false);
+  cell_waves(c, k_poisson_rhs_mixed, true);
+  cell_waves(c, k_poisson_rhs2, true);
+  cell_waves(c, k_face_coeff_mixed, false);
+  cell_waves(c, k_poisson_faces, false);
+  cell_waves(c, k_project<true, true>, true);
+  cell_waves(c, k_project<true, false>, true);
+  cell_waves(c, k_project<false, true>, true);
+  cell_waves(c, k_project<false, false>, true);
+  cell_waves(c, k_passive_scalar<float>, false);
+  cell_waves(c, k_passive_scalar<double>, false);
+  cell_waves(c, k_ps_face, false);
+  cell_waves(c, k_div_residual, true);
+  cell_waves(c, k_mean_reset, false);
 }
 
 void launch_mean_reset(tpm_ctx *c) {
-  TPM_LAUNCH(c, "mean_reset", k_mean_reset, cell_blocks(c->g), kThreads, 0, c->g, c->RU_np1,
+  TPM_LAUNCH(c, "mean_reset", k_mean_reset, cell_waves(c, k_mean_reset, false), kThreads, 0,
+             c->g, c->RU_np1,
              c->RU, c->dsc, c->p.U0 * c->p.Rho0, c->p.V0 * c->p.Rho0, c->p.W0 * c->p.Rho0);
 }
 

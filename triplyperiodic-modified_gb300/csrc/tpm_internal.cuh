@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "tpm.h"
+#include "tpm_index.cuh"
 
 namespace tpm {
 
@@ -28,6 +29,7 @@ constexpr double kPi = 3.141592653589793;  // params.h:5
 struct Grid {
   int nx, ny, nz, nxh;  // nxh = nx/2 + 1 (half spectrum)
   long long n;          // cells
+  unsigned long long mx, my;  // udiv_magic(nx), udiv_magic(ny)
   double dx, dy, dz;
   double inv_dx, inv_dy, inv_dz, inv_dx2, inv_dy2, inv_dz2;  // tensor0.cpp:17-22
   double idx, idy, idz;                                      // particle.cpp:19-21
@@ -40,6 +42,24 @@ __host__ __device__ __forceinline__ int wrap_any(int i, int n) {
   i %= n;
   return i < 0 ? i + n : i;
 }
+
+#if defined(__CUDACC__)
+// (i, j, k) of the flat cell index c = (k*Ny + j)*Nx + i, by the division
+// magics of the grid (c < 2^31)
+__device__ __forceinline__ void cell_ijk(const Grid &g, long long c, int &i, int &j, int &k) {
+  const unsigned cu = (unsigned)c, t = udiv(cu, g.mx), kk = udiv(t, g.my);
+  i = (int)(cu - t * (unsigned)g.nx);
+  j = (int)(t - kk * (unsigned)g.ny);
+  k = (int)kk;
+}
+
+// (j, k) of a pencil row r = k*Ny + j
+__device__ __forceinline__ void row_jk(const Grid &g, long long r, int &j, int &k) {
+  const unsigned ru = (unsigned)r, kk = udiv(ru, g.my);
+  j = (int)(ru - kk * (unsigned)g.ny);
+  k = (int)kk;
+}
+#endif
 
 // Scalars that live on the device so a whole substep runs without host
 // round trips (grid.h:100-105).
@@ -124,6 +144,7 @@ struct tpm_ctx {
   tpm::Grid g;
   int64_t np = 0;
   int dev = 0;
+  int sms = 0;  // SM count of the device
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // captures the body of a conditional (while) graph node
   std::string err;
@@ -147,6 +168,8 @@ struct tpm_ctx {
   double *RU = nullptr, *RU_int = nullptr, *RU_new = nullptr, *RU_np1 = nullptr;  // 3n each
   double *Rho = nullptr, *Rho_int = nullptr, *Rho_new = nullptr, *Rho_np1 = nullptr;
   double *P = nullptr, *C = nullptr, *Q = nullptr, *Fp = nullptr /*3n*/, *U = nullptr /*3n*/;
+  // inv_rho = 1/Rho_new: doubles on the FP64 path, float-float pairs (one
+  // float2 per cell in the same bytes) on the mixed path
   double *RHS = nullptr, *divg = nullptr, *inv_rho = nullptr, *Tgas = nullptr;
   double *Cface = nullptr /*3n*/, *cc = nullptr;
   // FP32 copies read by the FP32 stencils of the mixed path (written once per
@@ -250,7 +273,8 @@ void launch_p0_update(tpm_ctx *c, int stage);
 void launch_rho_update(tpm_ctx *c, int stage, bool np1_in_base);
 void launch_face_velocity(tpm_ctx *c);
 void launch_rhs_momentum(tpm_ctx *c, int stage, bool np1_in_base);
-void rhs_kernels_setup();
+void rhs_kernels_setup(tpm_ctx *c);
+void particle_kernels_setup(tpm_ctx *c);  // tpm_particles.cu
 void launch_poisson_rhs(tpm_ctx *c, int stage, bool store_div);
 void launch_project(tpm_ctx *c, int stage);
 void launch_div_residual(tpm_ctx *c, int stage);
@@ -259,6 +283,12 @@ void launch_passive_scalar(tpm_ctx *c, int stage, bool np1_in_base);  // grid.cp
 void launch_passive_scalar_face(tpm_ctx *c, const double *src);      // PS_face = I_C2F(src)
 void launch_init_fields(tpm_ctx *c);
 int cell_blocks(const Grid &g);
+// Blocks for a grid-stride kernel over `items` items, `threads` per block:
+// whole waves of the blocks the kernel keeps resident (SMs x resident blocks
+// per SM from the occupancy calculator, cached per kernel), fewer only when
+// the items need fewer.  A reducing kernel (one partial per block) stays
+// within kRedBlocks, in whole waves where the SM count allows.
+int wave_blocks(tpm_ctx *c, const void *kernel, int threads, long long items, bool reduces);
 void launch_center_coeff_from_C(tpm_ctx *c);  // operator-level Poisson entry
 void launch_to_float(tpm_ctx *c, const double *src, float *dst, long long n);
 void launch_to_double(tpm_ctx *c, const float *src, double *dst, long long n);

@@ -26,8 +26,9 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// flat index in 32-bit arithmetic (every box has fewer than 2^31 cells)
 __device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
-  return ((long long)k * g.ny + j) * g.nx + i;
+  return (long long)((k * g.ny + j) * g.nx + i);
 }
 
 struct PushArgs {
@@ -544,9 +545,8 @@ __global__ void k_dep_momentum(Grid g, const int32_t *__restrict__ starts,
                                const TP *__restrict__ pay, int64_t np, TO *__restrict__ Fp) {
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % g.nx);
-    const long long t = c / g.nx;
-    const int j = (int)(t % g.ny), k = (int)(t / g.ny);
+    int i, j, k;
+    cell_ijk(g, c, i, j, k);
     const long long m[3] = {at(g, wrap_m(i, g.nx), j, k), at(g, i, wrap_m(j, g.ny), k),
                             at(g, i, j, wrap_m(k, g.nz))};
     const int32_t s0 = starts[c], e0 = starts[c + 1];
@@ -605,9 +605,8 @@ __global__ void k_dep_sum8x2(Grid g, const int32_t *__restrict__ starts, const T
   double bsum = 0;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % g.nx);
-    const long long t = c / g.nx;
-    const int j = (int)(t % g.ny), k = (int)(t / g.ny);
+    int i, j, k;
+    cell_ijk(g, c, i, j, k);
     TW aq = 0, ac = 0;
 #pragma unroll
     for (int dz = 0; dz < 2; ++dz)
@@ -683,9 +682,8 @@ __global__ void k_dep_gather8(Grid g, const float *__restrict__ sums, double *__
   double bsum = 0;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % g.nx);
-    const long long t = c / g.nx;
-    const int j = (int)(t % g.ny), k = (int)(t / g.ny);
+    int i, j, k;
+    cell_ijk(g, c, i, j, k);
     float aq = 0.f, ac = 0.f;
 #pragma unroll
     for (int dz = 0; dz < 2; ++dz)
@@ -734,15 +732,20 @@ __global__ void k_dep_mom_cells(Grid g, const int32_t *__restrict__ starts,
 __global__ void k_dep_mom_faces(Grid g, const float *__restrict__ sums, float *__restrict__ Fp) {
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(c % g.nx);
-    const long long t = c / g.nx;
-    const int j = (int)(t % g.ny), k = (int)(t / g.ny);
+    int i, j, k;
+    cell_ijk(g, c, i, j, k);
     const long long m[3] = {at(g, wrap_m(i, g.nx), j, k), at(g, i, wrap_m(j, g.ny), k),
                             at(g, i, j, wrap_m(k, g.nz))};
 #pragma unroll
     for (int d = 0; d < 3; ++d)
       Fp[d * g.n + c] = sums[(size_t)(2 * d + 1) * g.n + m[d]] + sums[(size_t)(2 * d) * g.n + c];
   }
+}
+
+// wave_blocks for a cell kernel of this file (kThreads per block)
+template <typename K>
+int cell_waves(tpm_ctx *c, K *kernel, bool reduces) {
+  return wave_blocks(c, reinterpret_cast<const void *>(kernel), kThreads, c->g.n, reduces);
 }
 
 int pblocks(int64_t np) {
@@ -764,7 +767,8 @@ void sort_by_cell(tpm_ctx *c, const int32_t *key, int32_t *perm, int32_t *starts
              c->scan_blocks, starts, (int32_t)c->np);
   TPM_LAUNCH(c, "sort_scatter", k_scatter, pblocks(c->np), kThreads, 0, key, c->np, starts,
              c->counts, perm);
-  TPM_LAUNCH(c, "sort_segsort", k_segsort, cell_blocks(c->g), kThreads, 0, n, starts, perm,
+  TPM_LAUNCH(c, "sort_segsort", k_segsort, cell_waves(c, k_segsort, false), kThreads, 0, n,
+             starts, perm,
              &c->dsc->crowded);
 }
 
@@ -876,15 +880,18 @@ void particle_deposit_momentum(tpm_ctx *c) {
   if (mixed) {
     // the 16 n corner-sum floats of the heat deposit hold these 6 n (the two
     // deposits run one after the other)
-    TPM_LAUNCH(c, "deposit_momentum_cells", k_dep_mom_cells, cell_blocks(c->g), kThreads, 0,
+    TPM_LAUNCH(c, "deposit_momentum_cells", k_dep_mom_cells,
+               cell_waves(c, k_dep_mom_cells, false), kThreads, 0,
                c->g, c->starts_t, c->perm_t, reinterpret_cast<const float *>(c->pay_t), c->np,
                c->corner_sums);
-    TPM_LAUNCH(c, "deposit_momentum", k_dep_mom_faces, cell_blocks(c->g), kThreads, 0, c->g,
+    TPM_LAUNCH(c, "deposit_momentum", k_dep_mom_faces, cell_waves(c, k_dep_mom_faces, false),
+               kThreads, 0, c->g,
                c->corner_sums, c->Fp32);
   } else {
     TPM_LAUNCH(c, "payload_gather_t", k_gather_payload<double>, pblocks(c->np), kThreads, 0, c->np,
                6, c->perm_t, c->pay_t, c->pay_t_s);
-    TPM_LAUNCH(c, "deposit_momentum", (k_dep_momentum<double, double>), cell_blocks(c->g),
+    TPM_LAUNCH(c, "deposit_momentum", (k_dep_momentum<double, double>),
+               cell_waves(c, k_dep_momentum<double, double>, false),
                kThreads, 0, c->g, c->starts_t, c->pay_t_s, c->np, c->Fp);
   }
 }
@@ -902,12 +909,15 @@ void particle_deposit_concentration(tpm_ctx *c) {
 // sort the round-indexed keys in c->key_r and deposit the heat rate into Q
 // and the concentration of these positions into C_next
 static void heat_deposit(tpm_ctx *c) {
-  const int nb = cell_blocks(c->g);
+  const bool mixed = c->p.precision == TPM_PREC_MIXED;
+  const int nb = mixed ? cell_waves(c, k_dep_gather8, true)
+                       : cell_waves(c, k_dep_sum8x2<double>, true);
   sort_by_cell(c, c->key_r, c->perm_r[0], c->starts_r[0]);
   double *parts = c->partials + kPartQ * kRedBlocks;
-  if (c->p.precision == TPM_PREC_MIXED) {
-    TPM_LAUNCH(c, "deposit_corner_sums", k_dep_corners, nb, kThreads, 0, c->g, c->starts_r[0],
-               c->perm_r[0], c->pay_r, c->np, c->corner_sums);
+  if (mixed) {
+    TPM_LAUNCH(c, "deposit_corner_sums", k_dep_corners, cell_waves(c, k_dep_corners, false),
+               kThreads, 0, c->g, c->starts_r[0], c->perm_r[0], c->pay_r, c->np,
+               c->corner_sums);
     TPM_LAUNCH(c, "deposit_heat_conc", k_dep_gather8, nb, kThreads, 0, c->g, c->corner_sums,
                c->Q, c->C_next, parts);
   } else {
@@ -947,6 +957,18 @@ void particle_init_heat(tpm_ctx *c) {
              c->pq[1][1], c->pq[1][2], c->pq[1][6], c->Tgas, iTth, c->np, c->rhs_t, c->key_r,
              c->pay_r, 1);
   heat_deposit(c);
+}
+
+void particle_kernels_setup(tpm_ctx *c) {
+  // the occupancy of every wave-sized kernel, queried once at creation (not
+  // while a step is being captured into a graph)
+  cell_waves(c, k_segsort, false);
+  cell_waves(c, k_dep_mom_cells, false);
+  cell_waves(c, k_dep_mom_faces, false);
+  cell_waves(c, k_dep_momentum<double, double>, false);
+  cell_waves(c, k_dep_gather8, true);
+  cell_waves(c, k_dep_sum8x2<double>, true);
+  cell_waves(c, k_dep_corners, false);
 }
 
 // Continuation from a caller-held state: the given heat rates at x_int give

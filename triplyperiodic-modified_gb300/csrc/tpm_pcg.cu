@@ -30,8 +30,9 @@ constexpr int kThreadsPcg = 256;
 // device scalars of the iteration
 enum { PC_RHO = 0, PC_PQ, PC_ALPHA, PC_BETA, PC_RR, PC_BB, PC_ERR, PC_COUNT };
 
+// flat index in 32-bit arithmetic (every box has fewer than 2^31 cells)
 __device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
-  return ((long long)k * g.ny + j) * g.nx + i;
+  return (long long)((k * g.ny + j) * g.nx + i);
 }
 
 // div(C grad f) at cell c with the operation order of the Richardson
@@ -39,7 +40,8 @@ __device__ __forceinline__ long long at(const Grid &g, int i, int j, int k) {
 template <bool kScaled>
 __device__ __forceinline__ double lap_c(const Grid &g, const double *__restrict__ f,
                                         const double *__restrict__ Cf, long long c) {
-  const int i = (int)(c % g.nx), j = (int)((c / g.nx) % g.ny), k = (int)(c / ((long long)g.nx * g.ny));
+  int i, j, k;
+  cell_ijk(g, c, i, j, k);
   const double *Cx = Cf, *Cy = Cf + g.n, *Cz = Cf + 2 * g.n;
   const long long xp = at(g, wrap_p(i, g.nx), j, k), xm = at(g, wrap_m(i, g.nx), j, k);
   const long long yp = at(g, i, wrap_p(j, g.ny), k), ym = at(g, i, wrap_m(j, g.ny), k);
