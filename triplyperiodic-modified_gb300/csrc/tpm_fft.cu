@@ -70,24 +70,41 @@ __device__ __forceinline__ int fdiv(int i, unsigned m) {
   return m ? (int)__umulhi((unsigned)i, m) : i;
 }
 
+// DFT4 in place: V_u = sum_t v_t W^(t u), W = exp(sign 2 pi i / 4)
+template <typename T2>
+__device__ __forceinline__ void dft4(T2 *v, int sign) {
+  using C = Cx<T2>;
+  T2 a = C::mk(v[0].x + v[2].x, v[0].y + v[2].y);
+  T2 b = C::mk(v[0].x - v[2].x, v[0].y - v[2].y);
+  T2 c = C::mk(v[1].x + v[3].x, v[1].y + v[3].y);
+  T2 d = C::mk(v[1].x - v[3].x, v[1].y - v[3].y);
+  T2 j = sign < 0 ? C::mk(d.y, -d.x) : C::mk(-d.y, d.x);  // d * (sign i)
+  v[0] = C::mk(a.x + c.x, a.y + c.y);
+  v[2] = C::mk(a.x - c.x, a.y - c.y);
+  v[1] = C::mk(b.x + j.x, b.y + j.y);
+  v[3] = C::mk(b.x - j.x, b.y - j.y);
+}
+
+template <typename T2>
+__device__ __forceinline__ void dft8(T2 *v, int sign);
+template <typename T2>
+__device__ __forceinline__ void dft16(T2 *v, int sign);
+
+// V_u = sum_t v_t W^(t u), W = exp(sign 2 pi i / R), in place
 template <typename T2>
 __device__ __forceinline__ void dft_small(T2 *v, int R, int sign) {
   using C = Cx<T2>;
   using T = typename C::T;
-  if (R == 2) {
+  if (R == 16) {
+    dft16(v, sign);
+  } else if (R == 8) {
+    dft8(v, sign);
+  } else if (R == 2) {
     T2 a = v[0], b = v[1];
     v[0] = C::mk(a.x + b.x, a.y + b.y);
     v[1] = C::mk(a.x - b.x, a.y - b.y);
   } else if (R == 4) {
-    T2 a = C::mk(v[0].x + v[2].x, v[0].y + v[2].y);
-    T2 b = C::mk(v[0].x - v[2].x, v[0].y - v[2].y);
-    T2 c = C::mk(v[1].x + v[3].x, v[1].y + v[3].y);
-    T2 d = C::mk(v[1].x - v[3].x, v[1].y - v[3].y);
-    T2 j = sign < 0 ? C::mk(d.y, -d.x) : C::mk(-d.y, d.x);  // d * (sign i)
-    v[0] = C::mk(a.x + c.x, a.y + c.y);
-    v[2] = C::mk(a.x - c.x, a.y - c.y);
-    v[1] = C::mk(b.x + j.x, b.y + j.y);
-    v[3] = C::mk(b.x - j.x, b.y - j.y);
+    dft4(v, sign);
   } else if (R == 3) {
     const T s3 = (T)0.86602540378443864676;
     T s = sign < 0 ? -s3 : s3;
@@ -113,6 +130,68 @@ __device__ __forceinline__ void dft_small(T2 *v, int R, int sign) {
     v[4] = C::mk(p1.x + q1.y, p1.y - q1.x);
     v[2] = C::mk(p2.x - q2.y, p2.y + q2.x);
     v[3] = C::mk(p2.x + q2.y, p2.y - q2.x);
+  }
+}
+
+// a * (wr + i wi) for a constant twiddle
+template <typename T2>
+__device__ __forceinline__ T2 cmulc(T2 a, typename Cx<T2>::T wr, typename Cx<T2>::T wi) {
+  using C = Cx<T2>;
+  return C::mk(C::fma_(a.x, wr, -a.y * wi), C::fma_(a.x, wi, a.y * wr));
+}
+
+// Radix 8 as 4 x 2 (Cooley-Tukey, N = N1 N2 with n = 2 n1 + n2 and
+// k = k1 + 4 k2): DFT4 over the even and the odd elements, the odd ones times
+// W8^k1, then one DFT2 per k1.
+template <typename T2>
+__device__ __forceinline__ void dft8(T2 *v, int sign) {
+  using C = Cx<T2>;
+  using T = typename C::T;
+  const T r = (T)0.70710678118654752440, s = sign < 0 ? (T)-1 : (T)1;
+  T2 e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+  dft4(e, sign);
+  dft4(o, sign);
+  o[1] = cmulc(o[1], r, s * r);
+  o[2] = C::mk(-s * o[2].y, s * o[2].x);
+  o[3] = cmulc(o[3], -r, s * r);
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    v[k] = C::mk(e[k].x + o[k].x, e[k].y + o[k].y);
+    v[k + 4] = C::mk(e[k].x - o[k].x, e[k].y - o[k].y);
+  }
+}
+
+// Radix 16 as 4 x 4 (n = 4 n1 + n2, k = k1 + 4 k2): four DFT4 over n1,
+// the twiddles W16^(n2 k1), four DFT4 over n2; all in registers.
+template <typename T2>
+__device__ __forceinline__ void dft16(T2 *v, int sign) {
+  using C = Cx<T2>;
+  using T = typename C::T;
+  const T c1 = (T)0.92387953251128675613, s1 = (T)0.38268343236508977173;
+  const T r = (T)0.70710678118654752440, s = sign < 0 ? (T)-1 : (T)1;
+  T2 y[4][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    T2 t[4] = {v[n2], v[n2 + 4], v[n2 + 8], v[n2 + 12]};
+    dft4(t, sign);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) y[n2][k1] = t[k1];
+  }
+  y[1][1] = cmulc(y[1][1], c1, s * s1);        // W^1
+  y[1][2] = cmulc(y[1][2], r, s * r);          // W^2
+  y[1][3] = cmulc(y[1][3], s1, s * c1);        // W^3
+  y[2][1] = cmulc(y[2][1], r, s * r);          // W^2
+  y[2][2] = C::mk(-s * y[2][2].y, s * y[2][2].x);  // W^4 = sign i
+  y[2][3] = cmulc(y[2][3], -r, s * r);         // W^6
+  y[3][1] = cmulc(y[3][1], s1, s * c1);        // W^3
+  y[3][2] = cmulc(y[3][2], -r, s * r);         // W^6
+  y[3][3] = cmulc(y[3][3], -c1, -s * s1);      // W^9
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    T2 t[4] = {y[0][k1], y[1][k1], y[2][k1], y[3][k1]};
+    dft4(t, sign);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = t[k2];
   }
 }
 
@@ -162,12 +241,23 @@ __device__ T2 *smem_fft(T2 *a, T2 *b, int npen, const FftPlan &pl, int sign) {
   for (int s = 0; s < pl.nst; ++s) {
     const int R = pl.radix[s];
     const unsigned pm = pl.pmag[s];
+    if constexpr (sizeof(T2) == sizeof(float2)) {  // radices 16 and 8: FP32 plans only
+      if (R == 16) {
+        stockham_stage<16>(a, b, lq, pl, p, pm, sign);
+        goto staged;
+      }
+      if (R == 8) {
+        stockham_stage<8>(a, b, lq, pl, p, pm, sign);
+        goto staged;
+      }
+    }
     switch (R) {
       case 4: stockham_stage<4>(a, b, lq, pl, p, pm, sign); break;
       case 2: stockham_stage<2>(a, b, lq, pl, p, pm, sign); break;
       case 3: stockham_stage<3>(a, b, lq, pl, p, pm, sign); break;
       default: stockham_stage<5>(a, b, lq, pl, p, pm, sign); break;
     }
+  staged:
     __syncthreads();
     T2 *t = a;
     a = b;
@@ -572,10 +662,15 @@ int pens_for(int n, int elem_bytes = 16) {
 }
 
 
-void factorize(int n, FftPlan &pl) {
+// Radices of an n-point plan: 4, 2, 3, 5 (the FP64 passes); with big, 16 and
+// 8 first (the FP32 passes: half the shared-memory stages of radix 4, each
+// butterfly in registers)
+void factorize(int n, FftPlan &pl, bool big = false) {
   pl.n = n;
   pl.nst = 0;
   int m = n;
+  while (big && m % 16 == 0) { pl.radix[pl.nst++] = 16; m /= 16; }
+  while (big && m % 8 == 0) { pl.radix[pl.nst++] = 8; m /= 8; }
   while (m % 4 == 0) { pl.radix[pl.nst++] = 4; m /= 4; }
   while (m % 2 == 0) { pl.radix[pl.nst++] = 2; m /= 2; }
   while (m % 3 == 0) { pl.radix[pl.nst++] = 3; m /= 3; }
@@ -659,6 +754,13 @@ void fft_plans_create(tpm_ctx *c) {
   put(dx_, fx_, &c->fx);
   put(dy_, fy_, &c->fy);
   put(dz_, fz_, &c->fz);
+  // the FP32 plans: the same tables, radices 16 and 8 first
+  c->fx32 = c->fx;
+  c->fy32 = c->fy;
+  c->fz32 = c->fz;
+  factorize(c->fx.n, c->fx32, true);
+  factorize(c->fy.n, c->fy32, true);
+  factorize(c->fz.n, c->fz32, true);
   size_t r0 = put(dr, fr, nullptr);
   c->r2c64 = d64 + r0;
   c->r2c32 = d32 + r0;
@@ -706,6 +808,9 @@ void fft_plans_create(tpm_ctx *c) {
 template <typename T2>
 static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop) {
   const Grid &g = c->g;
+  constexpr bool f32 = sizeof(T2) == sizeof(float2);
+  const FftPlan &plx = f32 ? c->fx32 : c->fx, &ply = f32 ? c->fy32 : c->fy,
+                &plz = f32 ? c->fz32 : c->fz;
   const long long nrows = (long long)g.ny * g.nz;
   T2 *spec = reinterpret_cast<T2 *>(c->spec);
   const T2 *r2c = sizeof(T2) == sizeof(double2) ? reinterpret_cast<const T2 *>(c->r2c64)
@@ -715,34 +820,34 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
   const int tx = c->fthreads[0], ty = c->fthreads[1], tz = c->fthreads[2];
   const int xblocks = (int)((nrows + npx - 1) / npx);
   {
-    size_t smem = 2 * (size_t)npx * c->fx.n * sizeof(T2);
+    size_t smem = 2 * (size_t)npx * plx.n * sizeof(T2);
     if constexpr (sizeof(T2) == sizeof(float2))
-      TPM_LAUNCH(c, "fft_x_fwd_resid", k_xfwd_resid_refine, xblocks, tx, smem, g, c->fx, r2c,
+      TPM_LAUNCH(c, "fft_x_fwd_resid", k_xfwd_resid_refine, xblocks, tx, smem, g, plx, r2c,
                  c->P, c->dP, c->Cs2, c->cc32, c->RHS, c->dsc, c->R0, spec, npx);
     else
-      TPM_LAUNCH(c, "fft_x_fwd_resid", k_xfwd_resid<T2>, xblocks, tx, smem, g, c->fx, r2c,
+      TPM_LAUNCH(c, "fft_x_fwd_resid", k_xfwd_resid<T2>, xblocks, tx, smem, g, plx, r2c,
                  c->P, c->Cface, c->cc, c->RHS, c->dsc, spec, npx);
   }
   {
     int blocks = g.nz * ((g.nxh + npy - 1) / npy);
-    size_t smem = 2 * (size_t)npy * c->fy.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, ty, smem, g, c->fy, spec, npy, -1, skip);
+    size_t smem = 2 * (size_t)npy * ply.n * sizeof(T2);
+    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, ty, smem, g, ply, spec, npy, -1, skip);
   }
   {
     int blocks = g.ny * ((g.nxh + npz - 1) / npz);
-    size_t smem = 2 * (size_t)npz * c->fz.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_z_solve", k_fft_z_solve<T2>, blocks, tz, smem, g, c->fz, spec,
+    size_t smem = 2 * (size_t)npz * plz.n * sizeof(T2);
+    TPM_LAUNCH(c, "fft_z_solve", k_fft_z_solve<T2>, blocks, tz, smem, g, plz, spec,
                c->ax, c->ay, c->az, static_cast<const typename Cx<T2>::T *>(c->inv_mwn), npz, skip);
   }
   {
     int blocks = g.nz * ((g.nxh + npy - 1) / npy);
-    size_t smem = 2 * (size_t)npy * c->fy.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, ty, smem, g, c->fy, spec, npy, +1, skip);
+    size_t smem = 2 * (size_t)npy * ply.n * sizeof(T2);
+    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, ty, smem, g, ply, spec, npy, +1, skip);
   }
   {
-    size_t smem = 2 * (size_t)npx * c->fx.n * sizeof(T2);
+    size_t smem = 2 * (size_t)npx * plx.n * sizeof(T2);
     double *parts = c->err_parts;
-    TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, xblocks, tx, smem, g, c->fx,
+    TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, xblocks, tx, smem, g, plx,
                r2c, spec, c->P, parts, npx, skip, c->dP, &c->dsc->it,
                1.0 / (double)((long long)g.nx * g.ny * g.nz));
     TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 256, 0, parts, xblocks, c->dsc, eps_ctl,
@@ -945,6 +1050,9 @@ template <typename T2>
 void precondition_t(tpm_ctx *c, const double *r, const double *sc, double *z, double *parts,
                     const int *skip) {
   const Grid &g = c->g;
+  constexpr bool f32 = sizeof(T2) == sizeof(float2);
+  const FftPlan &plx = f32 ? c->fx32 : c->fx, &ply = f32 ? c->fy32 : c->fy,
+                &plz = f32 ? c->fz32 : c->fz;
   const long long nrows = (long long)g.ny * g.nz;
   T2 *spec = reinterpret_cast<T2 *>(c->spec);
   const T2 *r2c = sizeof(T2) == sizeof(double2) ? reinterpret_cast<const T2 *>(c->r2c64)
@@ -952,19 +1060,19 @@ void precondition_t(tpm_ctx *c, const double *r, const double *sc, double *z, do
   const int npx = c->pen[0], npy = c->pen[1], npz = c->pen[2];
   const int tx = c->fthreads[0], ty = c->fthreads[1], tz = c->fthreads[2];
   const int xblocks = (int)((nrows + npx - 1) / npx);
-  const size_t sx = 2 * (size_t)npx * c->fx.n * sizeof(T2);
-  const size_t sy = 2 * (size_t)npy * c->fy.n * sizeof(T2);
-  const size_t sz = 2 * (size_t)npz * c->fz.n * sizeof(T2);
-  TPM_LAUNCH(c, "pcg_fft_x_fwd", k_pc_xfwd<T2>, xblocks, tx, sx, g, c->fx, r2c, r, sc,
+  const size_t sx = 2 * (size_t)npx * plx.n * sizeof(T2);
+  const size_t sy = 2 * (size_t)npy * ply.n * sizeof(T2);
+  const size_t sz = 2 * (size_t)npz * plz.n * sizeof(T2);
+  TPM_LAUNCH(c, "pcg_fft_x_fwd", k_pc_xfwd<T2>, xblocks, tx, sx, g, plx, r2c, r, sc,
              spec, npx, skip);
   TPM_LAUNCH(c, "pcg_fft_y", k_fft_y<T2>, g.nz * ((g.nxh + npy - 1) / npy), ty, sy, g,
-             c->fy, spec, npy, -1, skip);
+             ply, spec, npy, -1, skip);
   TPM_LAUNCH(c, "pcg_fft_z_solve", k_fft_z_solve<T2>, g.ny * ((g.nxh + npz - 1) / npz),
-             tz, sz, g, c->fz, spec, c->ax, c->ay, c->az,
+             tz, sz, g, plz, spec, c->ax, c->ay, c->az,
              static_cast<const typename Cx<T2>::T *>(c->inv_mwn), npz, skip);
   TPM_LAUNCH(c, "pcg_fft_y", k_fft_y<T2>, g.nz * ((g.nxh + npy - 1) / npy), ty, sy, g,
-             c->fy, spec, npy, +1, skip);
-  TPM_LAUNCH(c, "pcg_fft_x_inv", k_pc_xinv<T2>, xblocks, tx, sx, g, c->fx, r2c, spec, r,
+             ply, spec, npy, +1, skip);
+  TPM_LAUNCH(c, "pcg_fft_x_inv", k_pc_xinv<T2>, xblocks, tx, sx, g, plx, r2c, spec, r,
              sc, z, parts, npx, skip);
 }
 

@@ -192,7 +192,8 @@ struct tpm_ctx {
   // 1/(ax[kx] + ay[ky] + az[kz]) per half-spectrum mode (1 at the zero mode),
   // double on the FP64 path and float on the mixed path
   void *inv_mwn = nullptr;
-  tpm::FftPlan fx, fy, fz;
+  tpm::FftPlan fx, fy, fz;        // FP64 passes (radices 4, 2, 3, 5)
+  tpm::FftPlan fx32, fy32, fz32;  // FP32 passes (radices 16 and 8 first)
   const double2 *r2c64 = nullptr;
   const float2 *r2c32 = nullptr;
   double *err_parts = nullptr;  // one max|dp| per x-pass block (sized for one row per block)
