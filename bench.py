@@ -149,13 +149,17 @@ def make_workload(name=WORKLOAD, precision=0, N=None, npart=None):
     return p, s
 
 
-def time_gpu(p, s, steps, warmup, dist, device):
+def time_gpu(p, s, steps, warmup, dist, device, tiles=None):
     import torch
     from tpm import capi
 
     ctx = capi.Context(p, s.npart)
     ctx.load(s)
-    pens = ctx.autotune()  # FFT pencils per block for this grid (results do not change)
+    if tiles:  # fixed FFT tiles (reproducible launch shapes, e.g. under a profiler)
+        ctx.set_fft_tiles(tiles)
+        pens = list(tiles)
+    else:
+        pens = ctx.autotune()  # FFT pencils per block for this grid (results do not change)
     ctx.initialize()
     ctx.set_graph(True)  # each step one CUDA graph launch (bit-identical to eager steps)
     for _ in range(warmup):
@@ -389,7 +393,7 @@ def gpu_main(args):
     for name in paths:
         p = p64.replace(precision=P.PREC_MIXED if name == "mixed" else P.PREC_FP64)
         ctx, ms, n_it, launches, prof, clocks = time_gpu(p, s, args.steps, args.warmup, dist,
-                                                         local)
+                                                         local, args.fft_tiles)
         ms = max_over_ranks(ms, dist, "cuda")
         res[name] = path_result(p, s, ms, args.steps, world, n_it, launches, prof, clocks,
                                 name == "mixed", peak, workload=args.workload)
@@ -739,6 +743,9 @@ def main():
     ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fft-tiles", type=lambda v: [int(t) for t in v.split(",")], default=None,
+                    help="pencils x,y,z and threads x,y,z of the FFT passes instead of "
+                         "autotuning them (one precision at a time)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

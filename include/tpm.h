@@ -342,6 +342,13 @@ int tpm_adjoint_run(tpm_ctx *ctx, int nsteps, int checkpoint_every, double w_tke
  * of the x, y, z passes, then their threads per block. */
 int tpm_autotune(tpm_ctx *ctx, int *pens_out);
 
+/* Sets the FFT tiles that tpm_autotune would pick, e.g. ones it picked before
+ * for the same grid: tiles[0..2] the pencils per block of the x, y, z passes
+ * (powers of two, at most what the passes' shared memory holds), tiles[3..5]
+ * their threads per block (multiples of 32, 32..1024).  Results do not depend
+ * on the tiles.  TPM_ERR_ARG for values out of range.  Not in the reference. */
+int tpm_set_fft_tiles(tpm_ctx *ctx, const int *tiles);
+
 /* ---------------------------------------------------------------- ensembles
  * A batch owns nboxes independent contexts (grids and particle counts may
  * differ; all on the current device).  tpm_batch_run advances every box by

@@ -109,6 +109,26 @@ def test_autotune_keeps_results(capi):
     assert all(t in (128, 256, 512) for t in pens[3:])
 
 
+@pytest.mark.parametrize("prec", [P.PREC_FP64, P.PREC_MIXED])
+def test_fixed_fft_tiles_keep_results(capi, prec):
+    # pencils 1, 2, 4 and odd thread counts against the default tiles
+    p, s = case(prec=prec, dims=(32, 48, 40), npart=4000, seed=6)
+    ref = run(capi, p, s, 3)
+    for tiles in ([1, 2, 4, 64, 96, 160], [4, 1, 2, 256, 32, 512]):
+        ctx = capi.Context(p, s.npart)
+        ctx.load(s)
+        ctx.set_fft_tiles(tiles)
+        ctx.initialize()
+        ctx.run(3)
+        ctx.sync()
+        assert_same(state(ctx), state(ref))
+    ctx = capi.Context(p, s.npart)
+    for bad in ([3, 1, 1, 128, 128, 128], [1, 1, 1, 100, 128, 128], [1, 1, 1, 128, 2048, 128],
+                [0, 1, 1, 128, 128, 128], [1, 1, 4096, 128, 128, 128]):
+        with pytest.raises(capi.TpmError):
+            ctx.set_fft_tiles(bad)
+
+
 def test_batch_matches_boxes_run_alone(capi):
     shapes = [((16, 16, 16), 1000), ((24, 24, 24), 4000), ((32, 32, 32), 9000),
               ((32, 24, 16), 2500), ((16, 16, 16), 500)]

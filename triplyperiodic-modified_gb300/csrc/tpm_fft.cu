@@ -425,6 +425,26 @@ __global__ void k_xfwd_resid_refine(Grid g, FftPlan pl, const float2 *__restrict
   r2c_store(g, z, npen, pl, row0, nrows, r2c_tw, spec);
 }
 
+// Pencil tile load a[idx] = src(q, t) for idx = t*npen + q < total (npen =
+// 2^lq): kBatch independent global loads in flight per thread before their
+// shared-memory stores (a plain loop waits one L2 round trip per element).
+template <int kBatch, typename T2, typename F>
+__device__ __forceinline__ void tile_load(T2 *a, int total, int lq, F &&src) {
+  for (int base = threadIdx.x; base < total; base += kBatch * blockDim.x) {
+    T2 v[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int idx = base + u * blockDim.x;
+      v[u] = idx < total ? src(idx & ((1 << lq) - 1), idx >> lq) : Cx<T2>::mk(0, 0);
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int idx = base + u * blockDim.x;
+      if (idx < total) a[idx] = v[u];
+    }
+  }
+}
+
 // ------------------------------------------------------- 2./4. y pencils
 template <typename T2>
 __global__ void k_fft_y(Grid g, FftPlan pl, T2 *__restrict__ spec, int npen, int sign,
@@ -437,11 +457,9 @@ __global__ void k_fft_y(Grid g, FftPlan pl, T2 *__restrict__ spec, int npen, int
   const int tiles = (g.nxh + npen - 1) / npen;
   const int kz = blockIdx.x / tiles, kx0 = (blockIdx.x % tiles) * npen;
   const long long base = (long long)kz * g.ny * g.nxh;
-  for (int idx = threadIdx.x; idx < npen * g.ny; idx += blockDim.x) {
-    const int q = idx & (npen - 1), ky = idx >> lq;
-    a[ky * npen + q] = (kx0 + q < g.nxh) ? spec[base + (long long)ky * g.nxh + kx0 + q]
-                                         : Cx<T2>::mk(0, 0);
-  }
+  tile_load<4>(a, npen * g.ny, lq, [&](int q, int ky) {
+    return (kx0 + q < g.nxh) ? spec[base + (long long)ky * g.nxh + kx0 + q] : Cx<T2>::mk(0, 0);
+  });
   __syncthreads();
   T2 *r = smem_fft(a, b, npen, pl, sign);
   for (int idx = threadIdx.x; idx < npen * g.ny; idx += blockDim.x) {
@@ -497,14 +515,14 @@ __global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const d
   const int ky = blockIdx.x / tiles, kx0 = (blockIdx.x % tiles) * npen;
   const long long plane = (long long)g.ny * g.nxh;
   const long long base = (long long)ky * g.nxh + kx0;
-  for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
-    const int q = idx & (npen - 1), kz = idx >> lq;
-    a[kz * npen + q] = (kx0 + q < g.nxh) ? spec[base + kz * plane + q] : Cx<T2>::mk(0, 0);
-  }
+  tile_load<4>(a, npen * g.nz, lq, [&](int q, int kz) {
+    return (kx0 + q < g.nxh) ? spec[base + kz * plane + q] : Cx<T2>::mk(0, 0);
+  });
   __syncthreads();
   T2 *r = smem_fft(a, b, npen, pl, -1);
   T2 *other = (r == a) ? b : a;
   // divide by the modified wave number except the zero mode (poisson.cpp:442-449)
+#pragma unroll 4
   for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
     const int q = idx & (npen - 1), kz = idx >> lq;
     const int kx = kx0 + q;
@@ -545,23 +563,34 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   const long long nrows = (long long)g.ny * g.nz;
   const long long row0 = (long long)blockIdx.x * npen;
   const int nxh = g.nxh;
-  // Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) W^-k, k < M
-  for (int idx = threadIdx.x; idx < npen * M; idx += blockDim.x) {
-    const int q = fdiv(idx, pl.nmag), kx = idx - q * M;
-    const long long row = row0 + q;
-    T2 Z = Cx<T2>::mk(0, 0);
-    if (row < nrows) {
-      T2 X = spec[row * nxh + kx];
-      T2 Y = spec[row * nxh + (M - kx)];
-      Y.y = -Y.y;
-      T fer = X.x + Y.x, fei = X.y + Y.y;
-      T dr = X.x - Y.x, di = X.y - Y.y;
-      T2 w = r2c_tw[kx];  // exp(-2 pi i k / nx); use its conjugate
+  // Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) W^-k, k < M;
+  // kB elements' loads in flight per thread before their stores
+  constexpr int kB = 4;
+  for (int base = threadIdx.x; base < npen * M; base += kB * blockDim.x) {
+    T2 X[kB], Y[kB], W[kB];
+#pragma unroll
+    for (int u = 0; u < kB; ++u) {
+      const int idx = base + u * blockDim.x;
+      const int q = fdiv(idx, pl.nmag), kx = idx - q * M;
+      const long long row = row0 + q;
+      const bool ok = idx < npen * M && row < nrows;
+      X[u] = ok ? spec[row * nxh + kx] : Cx<T2>::mk(0, 0);
+      Y[u] = ok ? spec[row * nxh + (M - kx)] : Cx<T2>::mk(0, 0);
+      W[u] = ok ? r2c_tw[kx] : Cx<T2>::mk(0, 0);  // exp(-2 pi i k / nx); use its conjugate
+    }
+#pragma unroll
+    for (int u = 0; u < kB; ++u) {
+      const int idx = base + u * blockDim.x;
+      if (idx >= npen * M) break;
+      const int q = fdiv(idx, pl.nmag), kx = idx - q * M;
+      const T2 Xv = X[u], w = W[u];
+      const T yr = Y[u].x, yi = -Y[u].y;
+      T fer = Xv.x + yr, fei = Xv.y + yi;
+      T dr = Xv.x - yr, di = Xv.y - yi;
       T for_ = Cx<T2>::fma_(dr, w.x, di * w.y);
       T foi = Cx<T2>::fma_(di, w.x, -dr * w.y);
-      Z = Cx<T2>::mk(fer - foi, fei + for_);  // Fe + i Fo
+      a[kx * npen + q] = Cx<T2>::mk(fer - foi, fei + for_);  // Fe + i Fo (0 past the rows)
     }
-    a[kx * npen + q] = Z;
   }
   __syncthreads();
   T2 *z = smem_fft(a, b, npen, pl, +1);
@@ -577,20 +606,37 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
     const int itv = *it;
     const float inv_tot_f = 1.0f / (float)((long long)g.nx * g.ny * g.nz);
     float mxf = 0.f;
-    for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
-      const int q = fdiv(idx, pl.n2mag), i = idx - q * g.nx;
-      const long long row = row0 + q;
-      if (row >= nrows) continue;
-      const T *zz = reinterpret_cast<const T *>(&z[(i >> 1) * npen + q]);
-      const float xf = (float)zz[i & 1];
-      const long long c = row * g.nx + i;
-      const float dp = -(xf * inv_tot_f);
-      if (itv == 0)
-        P[c] += ff_f2d(dp);
-      else
-        dP[c] = itv == 1 ? make_float2(dp, 0.f) : ff_add_f(dP[c], dp);
-      const float ax = fabsf(xf);
-      mxf = ax > mxf ? ax : mxf;
+    // kB elements per thread at a time: their P or dP loads in flight together
+    for (int base = threadIdx.x; base < npen * g.nx; base += kB * blockDim.x) {
+      float2 old[kB];
+      double pold[kB];
+#pragma unroll
+      for (int u = 0; u < kB; ++u) {
+        const int idx = base + u * blockDim.x;
+        const int q = fdiv(idx, pl.n2mag), i = idx - q * g.nx;
+        const long long row = row0 + q;
+        const bool ok = idx < npen * g.nx && row < nrows;
+        const long long c = row * g.nx + i;
+        old[u] = ok && itv >= 2 ? dP[c] : make_float2(0.f, 0.f);
+        pold[u] = ok && itv == 0 ? P[c] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kB; ++u) {
+        const int idx = base + u * blockDim.x;
+        const int q = fdiv(idx, pl.n2mag), i = idx - q * g.nx;
+        const long long row = row0 + q;
+        if (idx >= npen * g.nx || row >= nrows) continue;
+        const T *zz = reinterpret_cast<const T *>(&z[(i >> 1) * npen + q]);
+        const float xf = (float)zz[i & 1];
+        const long long c = row * g.nx + i;
+        const float dp = -(xf * inv_tot_f);
+        if (itv == 0)
+          P[c] = pold[u] + ff_f2d(dp);
+        else
+          dP[c] = itv == 1 ? make_float2(dp, 0.f) : ff_add_f(old[u], dp);
+        const float ax = fabsf(xf);
+        mxf = ax > mxf ? ax : mxf;
+      }
     }
     // the block maximum in FP32 too (FP64 compares issue on the FP64 pipe);
     // one conversion and one product per block

@@ -291,6 +291,28 @@ int tpm_autotune(tpm_ctx *c, int *pens_out) {
   });
 }
 
+int tpm_set_fft_tiles(tpm_ctx *c, const int *tiles) {
+  return tpm::guarded(c, [&]() -> int {
+    if (!tiles) return tpm::fail(c, TPM_ERR_ARG, "null tiles");
+    const int n_of[3] = {c->fx.n, c->fy.n, c->fz.n};
+    const int elem = c->p.precision == TPM_PREC_MIXED ? 8 : 16;
+    for (int d = 0; d < 3; ++d) {
+      const int p = tiles[d], t = tiles[3 + d];
+      if (p < 1 || (p & (p - 1)) || p > tpm::pens_max(n_of[d], elem))
+        return tpm::fail(c, TPM_ERR_ARG, "pencils per block must be a power of two within the "
+                                         "pass's shared memory");
+      if (t < 32 || t > 1024 || t % 32)
+        return tpm::fail(c, TPM_ERR_ARG, "threads per block must be a multiple of 32, 32..1024");
+    }
+    for (int d = 0; d < 3; ++d) {
+      c->pen[d] = tiles[d];
+      c->fthreads[d] = tiles[3 + d];
+    }
+    tpm::graphs_clear(c->graphs);  // launch shapes changed
+    return TPM_OK;
+  });
+}
+
 int tpm_batch_create(const tpm_params *params, const int64_t *np, int nboxes, tpm_batch **out) {
   if (!params || !np || !out || nboxes < 1) return TPM_ERR_ARG;
   *out = nullptr;

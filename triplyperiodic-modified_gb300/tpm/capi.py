@@ -73,6 +73,7 @@ SIGNATURES = {
     "tpm_profile_reset": (_i, [_vp]),
     "tpm_launch_count": (_i64, [_vp]),
     "tpm_autotune": (_i, [_vp, ctypes.POINTER(_i)]),
+    "tpm_set_fft_tiles": (_i, [_vp, ctypes.POINTER(_i)]),
     "tpm_adjoint_run": (_i, [_vp, _i, _i, _d, _d, _dp, _dp, _dp, _dp]),
     "tpm_batch_create": (_i, [_vp, ctypes.POINTER(_i64), _i, ctypes.POINTER(_vp)]),
     "tpm_batch_destroy": (_i, [_vp]),
@@ -171,6 +172,12 @@ class Context:
         pens = (_i * 6)()
         self._check(self.L.tpm_autotune(self.h, pens))
         return list(pens)
+
+    def set_fft_tiles(self, tiles):
+        """Fix the FFT tiles ([pencils x, y, z, threads x, y, z], as autotune
+        returns them) instead of searching."""
+        arr = (_i * 6)(*[int(t) for t in tiles])
+        self._check(self.L.tpm_set_fft_tiles(self.h, arr))
 
     def __del__(self):
         self.close()
