@@ -224,18 +224,58 @@ void refresh_rui32(tpm_ctx *c) {
   c->rui32_stale = false;
 }
 
+// kernels launched while alive go to stream s (TPM_LAUNCH uses c->stream)
+struct OnStream {
+  tpm_ctx *c;
+  cudaStream_t saved;
+  OnStream(tpm_ctx *ctx, cudaStream_t s) : c(ctx), saved(ctx->stream) { c->stream = s; }
+  ~OnStream() { c->stream = saved; }
+};
+
+// the auxiliary stream waits for what `stream` has enqueued so far
+void aux_fork(tpm_ctx *c, cudaEvent_t e) {
+  TPM_CUDA_TRY(cudaEventRecord(e, c->stream));
+  TPM_CUDA_TRY(cudaStreamWaitEvent(c->aux, e, 0));
+}
+
+// `stream` waits for what the auxiliary stream has enqueued so far
+void aux_join(tpm_ctx *c, cudaEvent_t e) {
+  TPM_CUDA_TRY(cudaEventRecord(e, c->aux));
+  TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, e, 0));
+}
+
+// One RK4 stage.  Three kernels run on the auxiliary stream beside the ones
+// they do not depend on (in a captured graph: parallel branches):
+//   face velocity U(RU_int, Rho_int)        beside the density update;
+//   face coefficients C(Rho_new) (mixed)    beside the particle push and deposits;
+//   momentum RHS (needs F_p)                beside the heat deposit.
+// Each writes buffers that the kernels beside it neither read nor write; the
+// stream joins back before their results are used (push, Poisson RHS).
+// While per-kernel profiling is on, everything stays on one stream so that
+// each kernel's events time that kernel alone.
 void substep(tpm_ctx *c, int s) {
   refresh_rui32(c);
   const bool nb = c->np1_is_base;
+  const bool par = !c->prof_on;
+  auto beside = [&](int fork, auto &&launch) {
+    if (!par) return launch();
+    aux_fork(c, c->fork_ev[fork]);
+    OnStream on(c, c->aux);
+    launch();
+  };
   tpm::launch_p0_update(c, s);
+  beside(0, [&] { tpm::launch_face_velocity(c); });
+  if (par) TPM_CUDA_TRY(cudaEventRecord(c->join_ev[0], c->aux));
   tpm::launch_rho_update(c, s, nb);
-  tpm::launch_face_velocity(c);
+  beside(1, [&] { tpm::launch_face_coeff(c); });
+  if (par) TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[0], 0));  // U for the push
   tpm::launch_particle_push(c, s, nb);
   tpm::particle_deposit_momentum(c);
+  beside(2, [&] { tpm::launch_rhs_momentum(c, s, nb); });
   tpm::particle_deposit_concentration(c);
   tpm::particle_heat(c);
   if (c->PS) tpm::launch_passive_scalar(c, s, nb);  // simulation.cpp:65
-  tpm::launch_rhs_momentum(c, s, nb);
+  if (par) aux_join(c, c->join_ev[1]);
   tpm::launch_poisson_rhs(c, s, c->store_div || c->p.precision == TPM_PREC_MIXED);
   poisson_loop(c, c->Iteration, c->p.epsilon);
   tpm::launch_project(c, s);
@@ -352,6 +392,9 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->np = np;
     TPM_CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     TPM_CUDA_TRY(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    TPM_CUDA_TRY(cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
+    for (cudaEvent_t &e : c->fork_ev) TPM_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (cudaEvent_t &e : c->join_ev) TPM_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     // fields
     c->RU = dalloc<double>(c, 3 * n); c->RU_int = dalloc<double>(c, 3 * n);
     c->RU_new = dalloc<double>(c, 3 * n); c->RU_np1 = dalloc<double>(c, 3 * n);
@@ -483,6 +526,11 @@ int tpm_destroy(tpm_ctx *c) {
   if (c->hsc) cudaFreeHost(c->hsc);
   if (c->stream) cudaStreamDestroy(c->stream);
   if (c->side) cudaStreamDestroy(c->side);
+  if (c->aux) cudaStreamDestroy(c->aux);
+  for (cudaEvent_t e : c->fork_ev)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->join_ev)
+    if (e) cudaEventDestroy(e);
   delete c;
   return TPM_OK;
 }

@@ -940,6 +940,13 @@ void launch_rhs_momentum(tpm_ctx *c, int s, bool np1_in_base) {
                c->Rho_int, c->RU, np1_in_base ? c->RU : c->RU_np1, c->RU_np1, c->RU_new, a);
 }
 
+void launch_face_coeff(tpm_ctx *c) {
+  if (c->p.precision != TPM_PREC_MIXED) return;
+  TPM_LAUNCH(c, "face_coeff", k_face_coeff_mixed, cell_waves(c, k_face_coeff_mixed, false),
+             kThreads, 0, c->g, c->Rho_new, c->Cface, c->Cs2,
+             c->p.Solver == 2 ? c->Cs : nullptr);
+}
+
 void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
   PoisArgs a;
   a.kCp = c->p.k / c->p.Cp;
@@ -951,9 +958,8 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
                        : cell_waves(c, k_poisson_rhs2, true);
   double *tke_parts = s == 3 ? c->partials + kPartTke2 * kRedBlocks : nullptr;
   if (mixed) {
+    // (C and Cs2 come from launch_face_coeff, run beside the particle stage)
     const bool pcg = c->p.Solver == 2;
-    TPM_LAUNCH(c, "face_coeff", k_face_coeff_mixed, cell_waves(c, k_face_coeff_mixed, false),
-               kThreads, 0, c->g, c->Rho_new, c->Cface, c->Cs2, pcg ? c->Cs : nullptr);
     TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_mixed, nb, kThreads, 0, c->g,
                reinterpret_cast<const float2 *>(c->inv_rho), c->Q,
                c->RU_new, c->Cface, c->dsc, c->RHS, c->divg, c->cc32, pcg ? c->cc : nullptr,

@@ -147,6 +147,11 @@ struct tpm_ctx {
   int sms = 0;  // SM count of the device
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // captures the body of a conditional (while) graph node
+  // a second stream for the kernels of a stage that do not depend on the
+  // ones beside them (face velocity, face coefficients, momentum RHS), with
+  // the events that fork it from and join it to `stream`
+  cudaStream_t aux = nullptr;
+  cudaEvent_t fork_ev[3] = {nullptr, nullptr, nullptr}, join_ev[2] = {nullptr, nullptr};
   std::string err;
   int64_t launches = 0;
 
@@ -276,6 +281,7 @@ void launch_face_velocity(tpm_ctx *c);
 void launch_rhs_momentum(tpm_ctx *c, int stage, bool np1_in_base);
 void rhs_kernels_setup(tpm_ctx *c);
 void particle_kernels_setup(tpm_ctx *c);  // tpm_particles.cu
+void launch_face_coeff(tpm_ctx *c);  // mixed path: C and C/d^2 pairs from Rho_new
 void launch_poisson_rhs(tpm_ctx *c, int stage, bool store_div);
 void launch_project(tpm_ctx *c, int stage);
 void launch_div_residual(tpm_ctx *c, int stage);
