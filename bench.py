@@ -41,12 +41,13 @@ FALLBACK_HBM_GBS = 6800.0
 # kernel on a workload, the mean over the launches of one ncu capture of this
 # bench's own command (the profiles/ summary of that kernel gives the command)
 NCU_TRAFFIC = {
-    # profiles/k_xfwd_resid_refine_mixed_box256_box128.md
-    ("box256_p8e6_heated", True, "fft_x_fwd_resid"): 8.29e8,
+    # profiles/k_xfwd_resid_refine_mixed_box256_box128.md (mean of six launches)
+    ("box256_p8e6_heated", True, "fft_x_fwd_resid"): 8.74e8,
     # profiles/k_push_mixed_box256_box128.md
-    ("box256_p8e6_heated", True, "particle_push"): 2.99e9,
-    # the same capture (k_rhs_momentum<float, float>: 2.36 and 2.77 GB)
-    ("box256_p8e6_heated", True, "rhs_momentum"): 2.56e9,
+    ("box256_p8e6_heated", True, "particle_push"): 3.00e9,
+    # profiles/k_rhs_momentum_k_poisson_rhs_mixed_box256.md
+    ("box256_p8e6_heated", True, "rhs_momentum"): 1.98e9,
+    ("box256_p8e6_heated", True, "poisson_rhs"): 1.84e9,
 }
 
 KERNEL_BYTES = {
