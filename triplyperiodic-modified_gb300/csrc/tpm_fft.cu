@@ -545,13 +545,26 @@ __global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const d
   }
 }
 
+// A block's max|dp| (>= 0): into the iteration's accumulator by an atomic
+// maximum on the bits (non-negative doubles order as their bit patterns, and
+// a maximum does not depend on the order the blocks arrive in), or into the
+// block's partial slot when there is no accumulator
+__device__ __forceinline__ void put_block_max(double v, double *partials,
+                                              unsigned long long *err_acc) {
+  if (err_acc)
+    atomicMax(err_acc, (unsigned long long)__double_as_longlong(v));
+  else
+    partials[blockIdx.x] = v;
+}
+
 // ------------------------------------------- 5. C2R along x + P update
 template <typename T2>
 __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
                               const T2 *__restrict__ spec, double *__restrict__ P,
                               double *__restrict__ partials, int npen,
                               const int *__restrict__ skip, float2 *__restrict__ dP,
-                              const int *__restrict__ it, double inv_tot) {
+                              const int *__restrict__ it, double inv_tot,
+                              unsigned long long *__restrict__ err_acc) {
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double sh[32];
@@ -641,7 +654,7 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
     // the block maximum in FP32 too (FP64 compares issue on the FP64 pipe);
     // one conversion and one product per block
     const float bm = block_max(mxf, shf);
-    if (threadIdx.x == 0) partials[blockIdx.x] = ff_f2d(bm) * inv_tot;
+    if (threadIdx.x == 0) put_block_max(ff_f2d(bm) * inv_tot, partials, err_acc);
     return;
   } else {
     for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
@@ -658,7 +671,7 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
     }
   }
   double bm = block_max(mx, sh);
-  if (threadIdx.x == 0) partials[blockIdx.x] = bm;
+  if (threadIdx.x == 0) put_block_max(bm, partials, err_acc);
 }
 
 // max|dp| of the iteration (poisson.cpp:407) and the loop test of
@@ -668,13 +681,20 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
 // unrolled iterations into no-ops (skip).  `it` counts up by one per
 // iteration, so the loop ends after at most loop_max bodies.
 __global__ void k_finish_max(const double *__restrict__ partials, int nparts, DevScalars *s,
-                             double eps_ctl, cudaGraphConditionalHandle loop, int loop_max) {
+                             double eps_ctl, cudaGraphConditionalHandle loop, int loop_max,
+                             unsigned long long *__restrict__ err_acc) {
   if (loop_max == 0 && s->skip) return;
   __shared__ double sh[32];
-  double v = 0;
-  for (int b = threadIdx.x; b < nparts; b += blockDim.x) v = partials[b] > v ? partials[b] : v;
-  double m = block_max(v, sh);
+  double m;
+  if (err_acc) {  // the blocks' atomic maximum; cleared for the next iteration
+    m = __longlong_as_double((long long)*err_acc);
+  } else {
+    double v = 0;
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x) v = partials[b] > v ? partials[b] : v;
+    m = block_max(v, sh);
+  }
   if (threadIdx.x == 0) {
+    if (err_acc) *err_acc = 0ull;
     s->err = m;
     s->it += 1;
     s->it_sum += 1;
@@ -895,9 +915,10 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
     double *parts = c->err_parts;
     TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, xblocks, tx, smem, g, plx,
                r2c, spec, c->P, parts, npx, skip, c->dP, &c->dsc->it,
-               1.0 / (double)((long long)g.nx * g.ny * g.nz));
-    TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 256, 0, parts, xblocks, c->dsc, eps_ctl,
-               loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0);
+               1.0 / (double)((long long)g.nx * g.ny * g.nz), &c->dsc->err_acc);
+    TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 32, 0, parts, xblocks, c->dsc, eps_ctl,
+               loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0,
+               &c->dsc->err_acc);
   }
 }
 
@@ -1339,8 +1360,10 @@ extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, doub
       size_t smem = 2 * (size_t)npx * fx.n * sizeof(double2);
       k_xinv_update<double2><<<xblocks, kFftThreads, smem, st>>>(g, fx, r2c, spec, P, errp, npx,
                                                                  nullptr, nullptr, nullptr,
-                                                                 1.0 / (double)((long long)Nx * Ny * Nz));
-      k_finish_max<<<1, 256, 0, st>>>(errp, xblocks, dsc, 0.0, cudaGraphConditionalHandle{}, 0);
+                                                                 1.0 / (double)((long long)Nx * Ny * Nz),
+                                                                 nullptr);
+      k_finish_max<<<1, 256, 0, st>>>(errp, xblocks, dsc, 0.0, cudaGraphConditionalHandle{}, 0,
+                                      nullptr);
     }
     if (cudaGetLastError() != cudaSuccess) return TPM_ERR_CUDA;
     it++;

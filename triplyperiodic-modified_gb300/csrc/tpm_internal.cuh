@@ -84,6 +84,9 @@ struct DevScalars {
   // set (and kept) when a cell held more particles than the counting sort
   // orders (kSortMaxRun): only a diverging run crowds its particles so
   int crowded;
+  // bits of max|dp| of the running Poisson iteration (the blocks' atomic
+  // maximum; zero between iterations)
+  unsigned long long err_acc;
 };
 
 // 1-D FFT plan in device memory: radices and exp(-2 pi i m / n) twiddles,
