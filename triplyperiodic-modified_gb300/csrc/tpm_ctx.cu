@@ -200,7 +200,7 @@ void poisson_loop(tpm_ctx *c, int max_it, double eps) {
     it++;
     if (eps > 0) error = read_err(c);
   }
-  if (refine && it > 1) tpm::refine_finish(c);
+  if (refine) tpm::refine_finish(c);  // (P += dP only where the correction sum started)
   c->last_it = it;
   c->total_it += it;
   if (eps > 0) c->last_err = error;
@@ -564,6 +564,8 @@ int tpm_upload_field(tpm_ctx *c, int field, const double *host) {
     if (!d) return fail(c, TPM_ERR_ARG, "unknown field id");
     if (field == TPM_FIELD_RU_INT || field == TPM_FIELD_RU) c->rui32_stale = true;
     TPM_CUDA_TRY(cudaMemcpyAsync(d, host, sizeof(double) * len, cudaMemcpyHostToDevice, c->stream));
+    if (field == TPM_FIELD_P)  // the next refinement solve starts cold
+      TPM_CUDA_TRY(cudaMemsetAsync(&c->dsc->warm, 0, sizeof(int), c->stream));
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     return TPM_OK;
   });
@@ -771,6 +773,7 @@ int tpm_initialize(tpm_ctx *c) {
     pull_scalars(c);
     c->hsc->P0_int = c->hsc->P0;
     c->hsc->P0_np1 = c->hsc->P0;
+    c->hsc->warm = 0;  // P comes from outside the step
     push_scalars(c);
     c->np1_is_base = true;
     c->rui32_stale = true;
@@ -815,6 +818,7 @@ void resume_device(tpm_ctx *c) {
     pull_scalars(c);
     c->hsc->P0_int = c->hsc->P0;
     c->hsc->P0_np1 = c->hsc->P0;
+    c->hsc->warm = 0;  // P comes from outside the step
     push_scalars(c);
     c->np1_is_base = true;
     c->rui32_stale = true;
@@ -884,6 +888,7 @@ int tpm_poisson_solve(tpm_ctx *c, const double *C3, double *P, const double *RHS
     TPM_CUDA_TRY(cudaMemcpyAsync(c->RHS, RHS, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
     pull_scalars(c);
     c->hsc->mean_rhs = 0;  // poisson::Solve uses RHS as given
+    c->hsc->warm = 0;      // and starts from the caller's P
     push_scalars(c);
     tpm::launch_center_coeff_from_C(c);
     poisson_loop(c, max_iterations, epsilon);

@@ -378,7 +378,8 @@ __global__ void k_xfwd_resid_refine(Grid g, FftPlan pl, const float2 *__restrict
   const long long nrows = (long long)g.ny * g.nz;
   const long long row0 = (long long)blockIdx.x * npen;
   const int it = s->it;
-  const bool direct = it <= 1;
+  const int nd = s->warm ? 1 : 2;  // direct iterations of this solve
+  const bool direct = it < nd;
   const double mean = s->mean_rhs;
   const float2 *Cx_ = Cs2, *Cy_ = Cs2 + g.n, *Cz_ = Cs2 + 2 * g.n;
   for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
@@ -402,7 +403,7 @@ __global__ void k_xfwd_resid_refine(Grid g, FftPlan pl, const float2 *__restrict
         acc = ff_add(acc, ff_mul(Cy_[cyp], ff_from_double(P[cyp] - pc)));
         acc = ff_add(acc, ff_mul(Cz_[c], ff_from_double(P[czm] - pc)));
         acc = ff_add(acc, ff_mul(Cz_[czp], ff_from_double(P[czp] - pc)));
-        if (it == 1) R0[c] = acc;
+        if (it == nd - 1) R0[c] = acc;
       } else {
         // (after the rebase dP is ~1e-6 of P: the one-TwoSum difference's
         // error, 2^-46 |dP|, lies near 1e-22 of P)
@@ -563,8 +564,8 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
                               const T2 *__restrict__ spec, double *__restrict__ P,
                               double *__restrict__ partials, int npen,
                               const int *__restrict__ skip, float2 *__restrict__ dP,
-                              const int *__restrict__ it, double inv_tot,
-                              unsigned long long *__restrict__ err_acc) {
+                              const int *__restrict__ it, const int *__restrict__ warm,
+                              double inv_tot, unsigned long long *__restrict__ err_acc) {
   if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double sh[32];
@@ -612,11 +613,13 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   double mx = 0;
   if (sizeof(T) == sizeof(float)) {
     // mixed path: the correction dp = -x/N^3, formed in FP32, goes to P at
-    // iteration 0 (converted exactly, one FP64 operation per cell), starts
-    // the solve's float-float correction sum dP at iteration 1 and joins it
-    // after (P += dP in k_refine_finish).  max|x| in FP32 (exact: the maximum
-    // picks one x, scaled once below).
+    // iteration 0 of a cold solve (converted exactly, one FP64 operation per
+    // cell), starts the solve's float-float correction sum dP at the last
+    // direct iteration (0 warm, 1 cold) and joins it after (P += dP in
+    // k_refine_finish).  max|x| in FP32 (exact: the maximum picks one x,
+    // scaled once below).
     const int itv = *it;
+    const int nd = *warm ? 1 : 2;  // direct iterations of this solve
     const float inv_tot_f = 1.0f / (float)((long long)g.nx * g.ny * g.nz);
     float mxf = 0.f;
     // kB elements per thread at a time: their P or dP loads in flight together
@@ -630,8 +633,8 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
         const long long row = row0 + q;
         const bool ok = idx < npen * g.nx && row < nrows;
         const long long c = row * g.nx + i;
-        old[u] = ok && itv >= 2 ? dP[c] : make_float2(0.f, 0.f);
-        pold[u] = ok && itv == 0 ? P[c] : 0.0;
+        old[u] = ok && itv >= nd ? dP[c] : make_float2(0.f, 0.f);
+        pold[u] = ok && itv < nd - 1 ? P[c] : 0.0;
       }
 #pragma unroll
       for (int u = 0; u < kB; ++u) {
@@ -643,10 +646,10 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
         const float xf = (float)zz[i & 1];
         const long long c = row * g.nx + i;
         const float dp = -(xf * inv_tot_f);
-        if (itv == 0)
+        if (itv < nd - 1)
           P[c] = pold[u] + ff_f2d(dp);
         else
-          dP[c] = itv == 1 ? make_float2(dp, 0.f) : ff_add_f(old[u], dp);
+          dP[c] = itv == nd - 1 ? make_float2(dp, 0.f) : ff_add_f(old[u], dp);
         const float ax = fabsf(xf);
         mxf = ax > mxf ? ax : mxf;
       }
@@ -706,11 +709,11 @@ __global__ void k_finish_max(const double *__restrict__ partials, int nparts, De
   }
 }
 
-// End of a mixed refinement loop that reached the correction form (it >= 2
-// iterations ran): P += dP
+// End of a mixed refinement loop that started the correction sum (at least
+// as many iterations as the solve's direct ones ran): P += dP
 __global__ void k_refine_finish(Grid g, const float2 *__restrict__ dP,
                                 const DevScalars *__restrict__ s, double *__restrict__ P) {
-  if (s->it <= 1) return;
+  if (s->it < (s->warm ? 1 : 2)) return;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     const float2 d = dP[c];
@@ -914,7 +917,7 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
     size_t smem = 2 * (size_t)npx * plx.n * sizeof(T2);
     double *parts = c->err_parts;
     TPM_LAUNCH(c, "fft_x_inv_update", k_xinv_update<T2>, xblocks, tx, smem, g, plx,
-               r2c, spec, c->P, parts, npx, skip, c->dP, &c->dsc->it,
+               r2c, spec, c->P, parts, npx, skip, c->dP, &c->dsc->it, &c->dsc->warm,
                1.0 / (double)((long long)g.nx * g.ny * g.nz), &c->dsc->err_acc);
     TPM_LAUNCH(c, "finish_max", k_finish_max, 1, 32, 0, parts, xblocks, c->dsc, eps_ctl,
                loop ? loop->handle : cudaGraphConditionalHandle{}, loop ? loop->max_it : 0,
@@ -922,9 +925,13 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
   }
 }
 
+// the following solves of the step start from this one's P: warm
+__global__ void k_mark_warm(DevScalars *s) { s->warm = 1; }
+
 void refine_finish(tpm_ctx *c) {
   TPM_LAUNCH(c, "refine_finish", k_refine_finish, cell_blocks(c->g), 256, 0, c->g, c->dP,
              c->dsc, c->P);
+  TPM_LAUNCH(c, "refine_finish", k_mark_warm, 1, 1, 0, c->dsc);
 }
 
 void poisson_iteration(tpm_ctx *c, double eps_ctl, const LoopCtl *loop) {
@@ -1359,7 +1366,7 @@ extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, doub
     {
       size_t smem = 2 * (size_t)npx * fx.n * sizeof(double2);
       k_xinv_update<double2><<<xblocks, kFftThreads, smem, st>>>(g, fx, r2c, spec, P, errp, npx,
-                                                                 nullptr, nullptr, nullptr,
+                                                                 nullptr, nullptr, nullptr, nullptr,
                                                                  1.0 / (double)((long long)Nx * Ny * Nz),
                                                                  nullptr);
       k_finish_max<<<1, 256, 0, st>>>(errp, xblocks, dsc, 0.0, cudaGraphConditionalHandle{}, 0,

@@ -87,6 +87,10 @@ struct DevScalars {
   // bits of max|dp| of the running Poisson iteration (the blocks' atomic
   // maximum; zero between iterations)
   unsigned long long err_acc;
+  // mixed path: 1 once a refinement solve has run since P was last set from
+  // outside the step (initialise, resume, upload, operator-level solve);
+  // a warm solve forms one direct residual of P, a cold one two
+  int warm;
 };
 
 // 1-D FFT plan in device memory: radices and exp(-2 pi i m / n) twiddles,
