@@ -242,6 +242,120 @@ __global__ void k_rhs_momentum(Grid g, const TIn *__restrict__ U, const TIn *__r
   }
 }
 
+// z-marching form of k_rhs_momentum<float, float> (mixed path): a block owns
+// a kZX x kZY column of cells and walks kZZ planes up in z.  The FP32 copies
+// of U and RU_int live in a ring of three shared-memory planes (z - 1, z,
+// z + 1) with a one-cell halo in x and y: each value is loaded from global
+// memory once per column instead of once per stencil use, and the next
+// plane's loads are issued before the current plane is computed.  Every cell
+// is evaluated exactly as in k_rhs_momentum (same expressions, same order),
+// so the results are bit-identical to it.
+constexpr int kZX = 32, kZY = 8, kZZ = 16;
+constexpr int kZPX = kZX + 2, kZPY = kZY + 2, kZPlane = kZPX * kZPY;
+
+__global__ void __launch_bounds__(kZX * kZY)
+k_rhs_momentum_zm(Grid g, const float *__restrict__ U, const float *__restrict__ RUi,
+                  const float *__restrict__ Fp, const double *__restrict__ Rho_int,
+                  const double *__restrict__ RU, const double *__restrict__ np1_in,
+                  double *__restrict__ RU_np1, double *__restrict__ RU_new, RhsArgs a) {
+  // [slot][field][plane]: fields 0-2 U, 3-5 RU_int
+  __shared__ float sp[3][6][kZPlane];
+  const int tx = threadIdx.x % kZX, ty = threadIdx.x / kZX;
+  const int tilesx = (g.nx + kZX - 1) / kZX, tilesy = (g.ny + kZY - 1) / kZY;
+  const int bx = blockIdx.x % tilesx, by = (blockIdx.x / tilesx) % tilesy;
+  const int bz = blockIdx.x / (tilesx * tilesy);
+  const int i0 = bx * kZX, j0 = by * kZY, k0 = bz * kZZ;
+  const int k1 = min(k0 + kZZ, g.nz);
+  const int i = i0 + tx, j = j0 + ty;
+  const bool live = i < g.nx && j < g.ny;
+  const float inv_d[3] = {a.f_inv_d[0], a.f_inv_d[1], a.f_inv_d[2]};
+  const float inv_d2[3] = {a.f_inv_d2[0], a.f_inv_d2[1], a.f_inv_d2[2]};
+  const float a_fp = a.f_a_fp, b_gd = a.f_b_gd, c_lap = a.f_c_lap, A_ = a.f_A, Rho0 = a.f_Rho0;
+  const float gv[3] = {a.f_g[0], a.f_g[1], a.f_g[2]};
+  // plane kk (any integer, wrapped) of the six fields into ring slot `slot`
+  auto load_plane = [&](int kk, int slot) {
+    kk %= g.nz;
+    if (kk < 0) kk += g.nz;
+    for (int e = threadIdx.x; e < kZPlane; e += kZX * kZY) {
+      const int hy = e / kZPX, hx = e - hy * kZPX;
+      int ii = i0 - 1 + hx, jj = j0 - 1 + hy;
+      while (ii < 0) ii += g.nx;
+      while (ii >= g.nx) ii -= g.nx;
+      while (jj < 0) jj += g.ny;
+      while (jj >= g.ny) jj -= g.ny;
+      const long long c = at(g, ii, jj, kk);
+      float v[6];
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        v[f] = U[f * g.n + c];
+        v[3 + f] = RUi[f * g.n + c];
+      }
+#pragma unroll
+      for (int f = 0; f < 6; ++f) sp[slot][f][e] = v[f];
+    }
+  };
+  load_plane(k0 - 1, 0);
+  load_plane(k0, 1);
+  int sm = 0, s0 = 1;  // ring slots of planes k - 1 and k
+  for (int k = k0; k < k1; ++k) {
+    const int sp1 = 3 - sm - s0;  // slot of plane k + 1
+    load_plane(k + 1, sp1);
+    __syncthreads();
+    if (live) {
+      const int slot_of[3] = {sm, s0, sp1};
+      // value of field f at the offset (dx, dy, dz) from the cell
+      auto V = [&](int f, int dx, int dy, int dz) -> float {
+        return sp[slot_of[dz + 1]][f][(ty + 1 + dy) * kZPX + tx + 1 + dx];
+      };
+      auto divU = [&](int ox, int oy, int oz) -> float {
+        return (V(0, ox + 1, oy, oz) - V(0, ox, oy, oz)) * inv_d[0] +
+               (V(1, ox, oy + 1, oz) - V(1, ox, oy, oz)) * inv_d[1] +
+               (V(2, ox, oy, oz + 1) - V(2, ox, oy, oz)) * inv_d[2];
+      };
+      const float div_c = divU(0, 0, 0);
+      const float div_m[3] = {divU(-1, 0, 0), divU(0, -1, 0), divU(0, 0, -1)};
+      const long long c = at(g, i, j, k);
+      const long long cm[3] = {at(g, wrap_m(i, g.nx), j, k), at(g, i, wrap_m(j, g.ny), k),
+                               at(g, i, j, wrap_m(k, g.nz))};
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float gd = (div_c - div_m[d]) * inv_d[d];
+        const float ud = V(d, 0, 0, 0);
+        const float lap = (V(d, 1, 0, 0) - 2 * ud + V(d, -1, 0, 0)) * inv_d2[0] +
+                          (V(d, 0, 1, 0) - 2 * ud + V(d, 0, -1, 0)) * inv_d2[1] +
+                          (V(d, 0, 0, 1) - 2 * ud + V(d, 0, 0, -1)) * inv_d2[2];
+        float rhs = a_fp * Fp[d * g.n + c] + b_gd * gd + c_lap * lap;
+        // flux P_{d,e} at (ox, oy, oz): I_e(U_d) * I_d(RU_e)
+        auto flux = [&](int e, int ox, int oy, int oz) -> float {
+          const int ex = e == 0, ey = e == 1, ez = e == 2;
+          const int dx = d == 0, dy = d == 1, dz = d == 2;
+          const float iu = (V(d, ox, oy, oz) + V(d, ox - ex, oy - ey, oz - ez)) * 0.5f;
+          const float ir = (V(3 + e, ox, oy, oz) + V(3 + e, ox - dx, oy - dy, oz - dz)) * 0.5f;
+          return iu * ir;
+        };
+        float t[3];
+#pragma unroll
+        for (int e = 0; e < 3; ++e)
+          t[e] = (flux(e, e == 0, e == 1, e == 2) - flux(e, 0, 0, 0)) * inv_d[e];
+        const float conv = t[0] + t[1] + t[2];
+        rhs -= conv;
+        rhs += A_ * V(3 + d, 0, 0, 0);
+        if (a.has_g) {
+          const float rf = (ff_cast<float>(Rho_int[c]) + ff_cast<float>(Rho_int[cm[d]])) * 0.5f;
+          rhs += (rf - Rho0) * gv[d];
+        }
+        const double r64 = ff_widen(rhs);
+        const double np1 = fma(a.dtpo, r64, np1_in[d * g.n + c]);
+        RU_np1[d * g.n + c] = np1;
+        RU_new[d * g.n + c] = (a.stage != 3) ? fma(a.dtpr, r64, RU[d * g.n + c]) : np1;
+      }
+    }
+    __syncthreads();  // plane k - 1's slot takes plane k + 2 next
+    sm = s0;
+    s0 = sp1;
+  }
+}
+
 // Tiled form of k_rhs_momentum: one block owns a TX x TY x TZ tile; U and
 // RU_int of the tile plus a one-cell halo are staged in shared memory, the
 // divergence of U and the nine convective fluxes P_{d,e} are evaluated once
@@ -930,9 +1044,10 @@ void launch_rhs_momentum(tpm_ctx *c, int s, bool np1_in_base) {
   // FP32: the cached per-cell form is faster (6.1 ms tiled vs 4.2 ms per 256^3
   // step); FP64: the tiled form saves FP64 issue slots (28.7 vs 31.5 ms).
   if (c->p.precision == TPM_PREC_MIXED)
-    TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum<float, float>),
-               cell_waves(c, k_rhs_momentum<float, float>, false, kRhsThreads), kRhsThreads, 0,
-               c->g, c->U32, c->RUi32, c->Fp32, c->Rho_int, c->RU,
+    TPM_LAUNCH(c, "rhs_momentum", k_rhs_momentum_zm,
+               ((c->g.nx + kZX - 1) / kZX) * ((c->g.ny + kZY - 1) / kZY) *
+                   ((c->g.nz + kZZ - 1) / kZZ),
+               kZX * kZY, 0, c->g, c->U32, c->RUi32, c->Fp32, c->Rho_int, c->RU,
                np1_in_base ? c->RU : c->RU_np1, c->RU_np1, c->RU_new, a);
   else
     TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum_tiled<double, double>), tiles,
