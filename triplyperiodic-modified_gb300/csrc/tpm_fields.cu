@@ -636,58 +636,112 @@ __global__ void k_face_coeff_mixed(Grid g, const double *__restrict__ Rho_new,
 // last stage) against about twenty-four for the same sums in FP64.  The
 // preconditioner scale cc is FP32 (it sets the rate of the Richardson
 // iteration, not its fixed point).
-__global__ void k_poisson_rhs_mixed(Grid g, const float2 *__restrict__ inv_rho2,
-                                    const double *__restrict__ Q, const double *__restrict__ RUn,
-                                    const double *__restrict__ Cface,
-                                    const DevScalars *__restrict__ s, double *__restrict__ RHS,
-                                    double *__restrict__ divg, float *__restrict__ cc32,
-                                    double *__restrict__ cc, double *__restrict__ partials,
-                                    double *__restrict__ tke_parts, PoisArgs a) {
-  __shared__ double sh[kThreads];
+// The kernel is z-marching: a block owns a kZX x kZY column of cells and
+// walks kZZ planes up in z.  Each face's flux pair RU C (and the
+// high part of C, for the preconditioner scale) is formed once into shared
+// memory and read by the two cells it separates (a per-cell form would form
+// every face twice, and split RU and C into pairs twice); the x and y faces
+// of the current plane and the z faces of it and the plane above (a ring of
+// two) are held.  The mean's partial sums take one slot per block in
+// `partials`.
+__global__ void __launch_bounds__(kZX * kZY)
+k_poisson_rhs_zm(Grid g, const float2 *__restrict__ inv_rho2, const double *__restrict__ Q,
+                 const double *__restrict__ RUn, const double *__restrict__ Cface,
+                 const DevScalars *__restrict__ s, double *__restrict__ RHS,
+                 double *__restrict__ divg, float *__restrict__ cc32, double *__restrict__ cc,
+                 double *__restrict__ partials, double *__restrict__ tke_parts, PoisArgs a) {
+  constexpr int kNX = (kZX + 1) * kZY, kNY = kZX * (kZY + 1), kNZ = kZX * kZY;
+  __shared__ float2 fx[kNX], fy[kNY], fz[2][kNZ];  // face fluxes: x, y of plane k; z ring
+  __shared__ float cx[kNX], cy[kNY], cz[2][kNZ];  // high parts of the face C
+  __shared__ double sh[32];
+  const int tx = threadIdx.x % kZX, ty = threadIdx.x / kZX;
+  const int tilesx = (g.nx + kZX - 1) / kZX, tilesy = (g.ny + kZY - 1) / kZY;
+  const int bx = blockIdx.x % tilesx, by = (blockIdx.x / tilesx) % tilesy;
+  const int bz = blockIdx.x / (tilesx * tilesy);
+  const int i0 = bx * kZX, j0 = by * kZY, k0 = bz * kZZ;
+  const int k1 = min(k0 + kZZ, g.nz);
+  const int i = i0 + tx, j = j0 + ty;
+  const bool live = i < g.nx && j < g.ny;
   const float2 coef = ff_from_double(s->coef_div), meanQ = ff_from_double(s->mean_Q);
   const float2 kCp = ff_from_double(a.kCp);
   const float2 inv_d2[3] = {ff_from_double(g.inv_dx2), ff_from_double(g.inv_dy2),
                             ff_from_double(g.inv_dz2)};
   const float2 inv_d[3] = {ff_from_double(g.inv_dx), ff_from_double(g.inv_dy),
                            ff_from_double(g.inv_dz)};
+  auto wrapx = [&](int v) { return v >= g.nx ? v - g.nx : v; };
+  auto wrapy = [&](int v) { return v >= g.ny ? v - g.ny : v; };
+  // the flux pair and C's high part of face d of cell (ii, jj, kk) (wrapped)
+  auto face = [&](int d, int ii, int jj, int kk, float2 &u, float &ch) {
+    const long long c = at(g, ii, jj, kk);
+    const float2 cp = ff_from_double(Cface[d * g.n + c]);
+    u = ff_norm(ff_mul(ff_from_double(RUn[d * g.n + c]), cp));
+    ch = cp.x;
+  };
+  // z faces of plane kk into ring slot `slot`
+  auto zfaces = [&](int kk, int slot) {
+    if (kk >= g.nz) kk -= g.nz;
+    for (int e = threadIdx.x; e < kNZ; e += kZX * kZY) {
+      const int ey = e / kZX, ex = e - ey * kZX;
+      if (i0 + ex < g.nx && j0 + ey < g.ny) face(2, i0 + ex, j0 + ey, kk, fz[slot][e], cz[slot][e]);
+    }
+  };
   double acc = 0, usq = 0;
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
-       c += (long long)gridDim.x * blockDim.x) {
-    Cell q = cell_of(g, c);
-    Nbr nb = nbr_of(g, q);
-    const float2 ir = inv_rho2[c];
-    float2 lap = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const float2 sec = ff_add(ff_sub(inv_rho2[nb.p[d]], ir), ff_sub(inv_rho2[nb.m[d]], ir));
-      lap = ff_add(lap, ff_mul(sec, inv_d2[d]));
+  zfaces(k0, 0);
+  int zs = 0;
+  for (int k = k0; k < k1; ++k) {
+    // x faces (i0 .. i0 + kZX) and y faces (j0 .. j0 + kZY) of plane k, z faces of k + 1
+    for (int e = threadIdx.x; e < kNX; e += kZX * kZY) {
+      const int ey = e / (kZX + 1), ex = e - ey * (kZX + 1);
+      if (i0 + ex <= g.nx && j0 + ey < g.ny) face(0, wrapx(i0 + ex), j0 + ey, k, fx[e], cx[e]);
     }
-    float2 Qc = ff_from_double(Q[c]);
-    if (a.cooling) Qc = ff_sub(Qc, meanQ);
-    const float2 dv = ff_add(ff_mul(kCp, lap), ff_mul(coef, Qc));
-    divg[c] = ff_to_double(dv);
-    float2 divu = make_float2(-dv.x, -dv.y);
-    float msum = 0.f;
+    for (int e = threadIdx.x; e < kNY; e += kZX * kZY) {
+      const int ey = e / kZX, ex = e - ey * kZX;
+      if (i0 + ex < g.nx && j0 + ey <= g.ny) face(1, i0 + ex, wrapy(j0 + ey), k, fy[e], cy[e]);
+    }
+    zfaces(k + 1, zs ^ 1);
+    __syncthreads();
+    if (live) {
+      const long long c = at(g, i, j, k);
+      const long long pn[3] = {at(g, wrap_p(i, g.nx), j, k), at(g, i, wrap_p(j, g.ny), k),
+                               at(g, i, j, wrap_p(k, g.nz))};
+      const long long mn[3] = {at(g, wrap_m(i, g.nx), j, k), at(g, i, wrap_m(j, g.ny), k),
+                               at(g, i, j, wrap_m(k, g.nz))};
+      const float2 ir = inv_rho2[c];
+      float2 lap = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const float2 clo = ff_from_double(Cface[d * g.n + c]);
-      const float2 chi = ff_from_double(Cface[d * g.n + nb.p[d]]);
-      const double *R = RUn + d * g.n;
-      const float2 u_lo = ff_norm(ff_mul(ff_from_double(R[c]), clo));
-      const float2 u_hi = ff_norm(ff_mul(ff_from_double(R[nb.p[d]]), chi));
-      divu = ff_add(divu, ff_mul(ff_sub(u_hi, u_lo), inv_d[d]));
-      msum += (clo.x + chi.x) * 0.5f;
-      if (tke_parts) {
-        const double ul = ff_f2d(u_lo.x);
-        usq = fma(ul, ul, usq);
+      for (int d = 0; d < 3; ++d) {
+        const float2 sec = ff_add(ff_sub(inv_rho2[pn[d]], ir), ff_sub(inv_rho2[mn[d]], ir));
+        lap = ff_add(lap, ff_mul(sec, inv_d2[d]));
       }
+      float2 Qc = ff_from_double(Q[c]);
+      if (a.cooling) Qc = ff_sub(Qc, meanQ);
+      const float2 dv = ff_add(ff_mul(kCp, lap), ff_mul(coef, Qc));
+      divg[c] = ff_to_double(dv);
+      float2 divu = make_float2(-dv.x, -dv.y);
+      float msum = 0.f;
+      const int ex = ty * (kZX + 1) + tx, ey = ty * kZX + tx, ez = ty * kZX + tx;
+      const float2 ulo[3] = {fx[ex], fy[ey], fz[zs][ez]};
+      const float2 uhi[3] = {fx[ex + 1], fy[ey + kZX], fz[zs ^ 1][ez]};
+      const float clo[3] = {cx[ex], cy[ey], cz[zs][ez]};
+      const float chi[3] = {cx[ex + 1], cy[ey + kZX], cz[zs ^ 1][ez]};
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        divu = ff_add(divu, ff_mul(ff_sub(uhi[d], ulo[d]), inv_d[d]));
+        msum += (clo[d] + chi[d]) * 0.5f;
+        if (tke_parts) {
+          const double ul = ff_f2d(ulo[d].x);
+          usq = fma(ul, ul, usq);
+        }
+      }
+      const double rhs = ff_to_double(divu) * a.inv_dtpre;
+      RHS[c] = rhs;
+      acc += rhs;
+      const float ccf = -3.0f / msum;
+      cc32[c] = ccf;
+      if (cc) cc[c] = ff_f2d(ccf);  // the PCG operator's copy
     }
-    const double rhs = ff_to_double(divu) * a.inv_dtpre;
-    RHS[c] = rhs;
-    acc += rhs;
-    const float ccf = -3.0f / msum;
-    cc32[c] = ccf;
-    if (cc) cc[c] = ff_f2d(ccf);  // the PCG operator's copy
+    __syncthreads();  // the faces of plane k are rewritten next
+    zs ^= 1;
   }
   double bs = block_sum(acc, sh);
   if (threadIdx.x == 0) partials[blockIdx.x] = bs;
@@ -965,6 +1019,11 @@ int wave_blocks(tpm_ctx *c, const void *kernel, int threads, long long items, bo
   return (int)b;
 }
 
+// blocks of the z-marching kernels (column tiles x z chunks)
+int zm_blocks(const Grid &g) {
+  return ((g.nx + kZX - 1) / kZX) * ((g.ny + kZY - 1) / kZY) * ((g.nz + kZZ - 1) / kZZ);
+}
+
 namespace {
 // wave_blocks for a cell kernel of this file (kThreads per block unless
 // given)
@@ -973,11 +1032,6 @@ int cell_waves(tpm_ctx *c, K *kernel, bool reduces, int threads = kThreads) {
   return wave_blocks(c, reinterpret_cast<const void *>(kernel), threads, c->g.n, reduces);
 }
 
-// The FP32 momentum stencil holds 96 registers a thread: blocks of 128
-// threads keep 20 warps resident per SM where blocks of 256 keep 16 (the
-// kernel waits on its neighbour loads, so the extra warps pay: 0.82 -> 0.69 ms
-// per 256^3 launch).
-constexpr int kRhsThreads = 128;
 }  // namespace
 
 static const double kPre[4] = {0.5, 0.5, 1., 1. / 6.};          // grid.cpp:18-21
@@ -1069,16 +1123,18 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
   a.cooling = c->p.cooling;
   a.store_div = store_div;
   const bool mixed = c->p.precision == TPM_PREC_MIXED;
-  const int nb = mixed ? cell_waves(c, k_poisson_rhs_mixed, true)
-                       : cell_waves(c, k_poisson_rhs2, true);
-  double *tke_parts = s == 3 ? c->partials + kPartTke2 * kRedBlocks : nullptr;
+  const int nzm = zm_blocks(c->g);
+  const int nb = mixed ? nzm : cell_waves(c, k_poisson_rhs2, true);
+  double *rhs_parts = mixed ? c->zm_parts : c->partials + kPartRhs * kRedBlocks;
+  double *tke_parts =
+      s == 3 ? (mixed ? c->zm_parts + nzm : c->partials + kPartTke2 * kRedBlocks) : nullptr;
   if (mixed) {
     // (C and Cs2 come from launch_face_coeff, run beside the particle stage)
     const bool pcg = c->p.Solver == 2;
-    TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_mixed, nb, kThreads, 0, c->g,
+    TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_zm, nzm, kZX * kZY, 0, c->g,
                reinterpret_cast<const float2 *>(c->inv_rho), c->Q,
                c->RU_new, c->Cface, c->dsc, c->RHS, c->divg, c->cc32, pcg ? c->cc : nullptr,
-               c->partials + kPartRhs * kRedBlocks, tke_parts, a);
+               rhs_parts, tke_parts, a);
   } else {
     // c->U (the face velocity of RU_int) is dead after the momentum RHS; it
     // holds RU_new/Rho_face here
@@ -1088,8 +1144,7 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
                c->Cface, c->dsc, c->RHS, c->divg, c->cc, c->partials + kPartRhs * kRedBlocks,
                tke_parts, a);
   }
-  TPM_LAUNCH(c, "finish_mean", k_finish_mean, 1, kThreads, 0, c->partials + kPartRhs * kRedBlocks,
-             nb, c->g.n,
+  TPM_LAUNCH(c, "finish_mean", k_finish_mean, 1, kThreads, 0, rhs_parts, nb, c->g.n,
              &c->dsc->mean_rhs);
   if (tke_parts)
     TPM_LAUNCH(c, "finish_mean", k_finish_mean, 1, kThreads, 0, tke_parts, nb, c->g.n,
@@ -1162,8 +1217,6 @@ void rhs_kernels_setup(tpm_ctx *c) {
   cell_waves(c, k_rho_update, false);
   cell_waves(c, k_face_velocity_mixed, false);
   cell_waves(c, k_face_velocity, false);
-  cell_waves(c, k_rhs_momentum<float, float>, false, kRhsThreads);
-  cell_waves(c, k_poisson_rhs_mixed, true);
   cell_waves(c, k_poisson_rhs2, true);
   cell_waves(c, k_face_coeff_mixed, false);
   cell_waves(c, k_poisson_faces, false);

@@ -198,6 +198,7 @@ struct tpm_ctx {
   bool rui32_stale = true;
   double2 *spec = nullptr;
   double *partials = nullptr;  // kRedBlocks * 4
+  double *zm_parts = nullptr;  // 2 * zm_blocks: the mixed Poisson RHS's mean and TKE partials
   tpm::DevScalars *dsc = nullptr;
   tpm::DevScalars *hsc = nullptr;  // pinned mirror
   double *ax = nullptr, *ay = nullptr, *az = nullptr;  // modified wave number tables
@@ -303,6 +304,7 @@ int cell_blocks(const Grid &g);
 // the items need fewer.  A reducing kernel (one partial per block) stays
 // within kRedBlocks, in whole waves where the SM count allows.
 int wave_blocks(tpm_ctx *c, const void *kernel, int threads, long long items, bool reduces);
+int zm_blocks(const Grid &g);  // blocks of the z-marching stencil kernels
 void launch_center_coeff_from_C(tpm_ctx *c);  // operator-level Poisson entry
 void launch_to_float(tpm_ctx *c, const double *src, float *dst, long long n);
 void launch_to_double(tpm_ctx *c, const float *src, double *dst, long long n);
