@@ -31,6 +31,7 @@ namespace {
 
 constexpr int kFftThreads = 256;
 constexpr int kFftSmemPoints = 2048;  // complex points per ping-pong buffer
+constexpr int kMaxPens = 32;           // pencils per block at most (pens_for, autotune)
 
 template <typename T2>
 struct Cx;
@@ -382,17 +383,31 @@ __global__ void k_xfwd_resid_refine(Grid g, FftPlan pl, const float2 *__restrict
   const bool direct = it < nd;
   const double mean = s->mean_rhs;
   const float2 *Cx_ = Cs2, *Cy_ = Cs2 + g.n, *Cz_ = Cs2 + 2 * g.n;
+  // per pencil: its first cell and the offsets of its y and z neighbours
+  // (wrapped), once per block instead of once per element
+  __shared__ int rbase[kMaxPens], rym[kMaxPens], ryp[kMaxPens], rzm[kMaxPens], rzp[kMaxPens];
+  for (int q = threadIdx.x; q < npen; q += blockDim.x) {
+    const long long row = row0 + q;
+    if (row < nrows) {
+      int j, k;
+      row_jk(g, row, j, k);
+      const int nxy = g.nx * g.ny;
+      rbase[q] = (int)at(g, 0, j, k);
+      rym[q] = j == 0 ? (g.ny - 1) * g.nx : -g.nx;
+      ryp[q] = j == g.ny - 1 ? -(g.ny - 1) * g.nx : g.nx;
+      rzm[q] = k == 0 ? (g.nz - 1) * nxy : -nxy;
+      rzp[q] = k == g.nz - 1 ? -(g.nz - 1) * nxy : nxy;
+    }
+  }
+  __syncthreads();
   for (int idx = threadIdx.x; idx < npen * g.nx; idx += blockDim.x) {
     const int q = fdiv(idx, pl.n2mag), i = idx - q * g.nx;
     const long long row = row0 + q;
     float r = 0.f;
     if (row < nrows) {
-      int j, k;
-      row_jk(g, row, j, k);
-      const long long c = at(g, i, j, k);
-      const long long cxm = at(g, wrap_m(i, g.nx), j, k), cxp = at(g, wrap_p(i, g.nx), j, k);
-      const long long cym = at(g, i, wrap_m(j, g.ny), k), cyp = at(g, i, wrap_p(j, g.ny), k);
-      const long long czm = at(g, i, j, wrap_m(k, g.nz)), czp = at(g, i, j, wrap_p(k, g.nz));
+      const int c = rbase[q] + i;
+      const int cxm = i == 0 ? c + g.nx - 1 : c - 1, cxp = i == g.nx - 1 ? c - g.nx + 1 : c + 1;
+      const int cym = c + rym[q], cyp = c + ryp[q], czm = c + rzm[q], czp = c + rzp[q];
       float2 acc;
       if (direct) {
         acc = ff_from_double(mean - RHS[c]);
