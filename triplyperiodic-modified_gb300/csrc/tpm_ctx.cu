@@ -425,7 +425,7 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
       TPM_CUDA_TRY(cudaMemsetAsync(c->cc32, 0, sizeof(float) * n, c->stream));
     }
     c->partials = dalloc<double>(c, (size_t)tpm::kPartRegions * tpm::kRedBlocks);
-    c->zm_parts = dalloc<double>(c, 2 * (size_t)tpm::zm_blocks(g));
+    c->zm_parts = dalloc<double>(c, 2 * (size_t)tpm::zm_blocks(c));
     c->dsc = dalloc<tpm::DevScalars>(c, 1);
     TPM_CUDA_TRY(cudaMemsetAsync(c->dsc, 0, sizeof(tpm::DevScalars), c->stream));
     TPM_CUDA_TRY(cudaMallocHost(&c->hsc, sizeof(tpm::DevScalars)));

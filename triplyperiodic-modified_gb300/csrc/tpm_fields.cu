@@ -243,29 +243,30 @@ __global__ void k_rhs_momentum(Grid g, const TIn *__restrict__ U, const TIn *__r
 }
 
 // z-marching form of k_rhs_momentum<float, float> (mixed path): a block owns
-// a kZX x kZY column of cells and walks kZZ planes up in z.  The FP32 copies
+// a kZX x kZY column of cells and walks zlen planes up in z.  The FP32 copies
 // of U and RU_int live in a ring of three shared-memory planes (z - 1, z,
 // z + 1) with a one-cell halo in x and y: each value is loaded from global
 // memory once per column instead of once per stencil use, and the next
 // plane's loads are issued before the current plane is computed.  Every cell
 // is evaluated exactly as in k_rhs_momentum (same expressions, same order),
 // so the results are bit-identical to it.
-constexpr int kZX = 32, kZY = 8, kZZ = 16;
+constexpr int kZX = 32, kZY = 8;  // column tile; the z chunk is zm_zlen planes
 constexpr int kZPX = kZX + 2, kZPY = kZY + 2, kZPlane = kZPX * kZPY;
 
 __global__ void __launch_bounds__(kZX * kZY)
 k_rhs_momentum_zm(Grid g, const float *__restrict__ U, const float *__restrict__ RUi,
                   const float *__restrict__ Fp, const double *__restrict__ Rho_int,
                   const double *__restrict__ RU, const double *__restrict__ np1_in,
-                  double *__restrict__ RU_np1, double *__restrict__ RU_new, RhsArgs a) {
+                  double *__restrict__ RU_np1, double *__restrict__ RU_new, RhsArgs a,
+                  int zlen) {
   // [slot][field][plane]: fields 0-2 U, 3-5 RU_int
   __shared__ float sp[3][6][kZPlane];
   const int tx = threadIdx.x % kZX, ty = threadIdx.x / kZX;
   const int tilesx = (g.nx + kZX - 1) / kZX, tilesy = (g.ny + kZY - 1) / kZY;
   const int bx = blockIdx.x % tilesx, by = (blockIdx.x / tilesx) % tilesy;
   const int bz = blockIdx.x / (tilesx * tilesy);
-  const int i0 = bx * kZX, j0 = by * kZY, k0 = bz * kZZ;
-  const int k1 = min(k0 + kZZ, g.nz);
+  const int i0 = bx * kZX, j0 = by * kZY, k0 = bz * zlen;
+  const int k1 = min(k0 + zlen, g.nz);
   const int i = i0 + tx, j = j0 + ty;
   const bool live = i < g.nx && j < g.ny;
   const float inv_d[3] = {a.f_inv_d[0], a.f_inv_d[1], a.f_inv_d[2]};
@@ -637,7 +638,7 @@ __global__ void k_face_coeff_mixed(Grid g, const double *__restrict__ Rho_new,
 // preconditioner scale cc is FP32 (it sets the rate of the Richardson
 // iteration, not its fixed point).
 // The kernel is z-marching: a block owns a kZX x kZY column of cells and
-// walks kZZ planes up in z.  Each face's flux pair RU C (and the
+// walks zlen planes up in z.  Each face's flux pair RU C (and the
 // high part of C, for the preconditioner scale) is formed once into shared
 // memory and read by the two cells it separates (a per-cell form would form
 // every face twice, and split RU and C into pairs twice); the x and y faces
@@ -649,7 +650,8 @@ k_poisson_rhs_zm(Grid g, const float2 *__restrict__ inv_rho2, const double *__re
                  const double *__restrict__ RUn, const double *__restrict__ Cface,
                  const DevScalars *__restrict__ s, double *__restrict__ RHS,
                  double *__restrict__ divg, float *__restrict__ cc32, double *__restrict__ cc,
-                 double *__restrict__ partials, double *__restrict__ tke_parts, PoisArgs a) {
+                 double *__restrict__ partials, double *__restrict__ tke_parts, PoisArgs a,
+                 int zlen) {
   constexpr int kNX = (kZX + 1) * kZY, kNY = kZX * (kZY + 1), kNZ = kZX * kZY;
   __shared__ float2 fx[kNX], fy[kNY], fz[2][kNZ];  // face fluxes: x, y of plane k; z ring
   __shared__ float cx[kNX], cy[kNY], cz[2][kNZ];  // high parts of the face C
@@ -658,8 +660,8 @@ k_poisson_rhs_zm(Grid g, const float2 *__restrict__ inv_rho2, const double *__re
   const int tilesx = (g.nx + kZX - 1) / kZX, tilesy = (g.ny + kZY - 1) / kZY;
   const int bx = blockIdx.x % tilesx, by = (blockIdx.x / tilesx) % tilesy;
   const int bz = blockIdx.x / (tilesx * tilesy);
-  const int i0 = bx * kZX, j0 = by * kZY, k0 = bz * kZZ;
-  const int k1 = min(k0 + kZZ, g.nz);
+  const int i0 = bx * kZX, j0 = by * kZY, k0 = bz * zlen;
+  const int k1 = min(k0 + zlen, g.nz);
   const int i = i0 + tx, j = j0 + ty;
   const bool live = i < g.nx && j < g.ny;
   const float2 coef = ff_from_double(s->coef_div), meanQ = ff_from_double(s->mean_Q);
@@ -1020,8 +1022,21 @@ int wave_blocks(tpm_ctx *c, const void *kernel, int threads, long long items, bo
 }
 
 // blocks of the z-marching kernels (column tiles x z chunks)
-int zm_blocks(const Grid &g) {
-  return ((g.nx + kZX - 1) / kZX) * ((g.ny + kZY - 1) / kZY) * ((g.nz + kZZ - 1) / kZZ);
+// planes per z chunk: 16 where the grid gives four blocks per SM with them,
+// fewer (at least 4) on small grids so that every SM still gets work
+int zm_zlen(const tpm_ctx *c) {
+  const Grid &g = c->g;
+  const long long cols = (long long)((g.nx + kZX - 1) / kZX) * ((g.ny + kZY - 1) / kZY);
+  const long long want = 4LL * (c->sms > 0 ? c->sms : 1);  // blocks
+  long long z = cols * g.nz / want;
+  z = z > 16 ? 16 : (z < 4 ? 4 : z);
+  return (int)z;
+}
+
+int zm_blocks(const tpm_ctx *c) {
+  const Grid &g = c->g;
+  const int z = zm_zlen(c);
+  return ((g.nx + kZX - 1) / kZX) * ((g.ny + kZY - 1) / kZY) * ((g.nz + z - 1) / z);
 }
 
 namespace {
@@ -1098,11 +1113,9 @@ void launch_rhs_momentum(tpm_ctx *c, int s, bool np1_in_base) {
   // FP32: the cached per-cell form is faster (6.1 ms tiled vs 4.2 ms per 256^3
   // step); FP64: the tiled form saves FP64 issue slots (28.7 vs 31.5 ms).
   if (c->p.precision == TPM_PREC_MIXED)
-    TPM_LAUNCH(c, "rhs_momentum", k_rhs_momentum_zm,
-               ((c->g.nx + kZX - 1) / kZX) * ((c->g.ny + kZY - 1) / kZY) *
-                   ((c->g.nz + kZZ - 1) / kZZ),
-               kZX * kZY, 0, c->g, c->U32, c->RUi32, c->Fp32, c->Rho_int, c->RU,
-               np1_in_base ? c->RU : c->RU_np1, c->RU_np1, c->RU_new, a);
+    TPM_LAUNCH(c, "rhs_momentum", k_rhs_momentum_zm, zm_blocks(c), kZX * kZY, 0, c->g, c->U32,
+               c->RUi32, c->Fp32, c->Rho_int, c->RU, np1_in_base ? c->RU : c->RU_np1,
+               c->RU_np1, c->RU_new, a, zm_zlen(c));
   else
     TPM_LAUNCH(c, "rhs_momentum", (k_rhs_momentum_tiled<double, double>), tiles,
                kTX * kTY * kTZ, rhs_tiled_smem<double>(), c->g, c->U, c->RU_int, c->Fp,
@@ -1123,7 +1136,7 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
   a.cooling = c->p.cooling;
   a.store_div = store_div;
   const bool mixed = c->p.precision == TPM_PREC_MIXED;
-  const int nzm = zm_blocks(c->g);
+  const int nzm = zm_blocks(c);
   const int nb = mixed ? nzm : cell_waves(c, k_poisson_rhs2, true);
   double *rhs_parts = mixed ? c->zm_parts : c->partials + kPartRhs * kRedBlocks;
   double *tke_parts =
@@ -1134,7 +1147,7 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
     TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_zm, nzm, kZX * kZY, 0, c->g,
                reinterpret_cast<const float2 *>(c->inv_rho), c->Q,
                c->RU_new, c->Cface, c->dsc, c->RHS, c->divg, c->cc32, pcg ? c->cc : nullptr,
-               rhs_parts, tke_parts, a);
+               rhs_parts, tke_parts, a, zm_zlen(c));
   } else {
     // c->U (the face velocity of RU_int) is dead after the momentum RHS; it
     // holds RU_new/Rho_face here

@@ -304,7 +304,8 @@ int cell_blocks(const Grid &g);
 // the items need fewer.  A reducing kernel (one partial per block) stays
 // within kRedBlocks, in whole waves where the SM count allows.
 int wave_blocks(tpm_ctx *c, const void *kernel, int threads, long long items, bool reduces);
-int zm_blocks(const Grid &g);  // blocks of the z-marching stencil kernels
+int zm_blocks(const tpm_ctx *c);  // blocks of the z-marching stencil kernels
+int zm_zlen(const tpm_ctx *c);    // their planes per z chunk
 void launch_center_coeff_from_C(tpm_ctx *c);  // operator-level Poisson entry
 void launch_to_float(tpm_ctx *c, const double *src, float *dst, long long n);
 void launch_to_double(tpm_ctx *c, const float *src, double *dst, long long n);
