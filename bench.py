@@ -45,9 +45,9 @@ NCU_TRAFFIC = {
     ("box256_p8e6_heated", True, "fft_x_fwd_resid"): 8.74e8,
     # profiles/k_push_mixed_box256_box128.md
     ("box256_p8e6_heated", True, "particle_push"): 3.00e9,
-    # profiles/k_rhs_momentum_k_poisson_rhs_mixed_box256.md
-    ("box256_p8e6_heated", True, "rhs_momentum"): 1.98e9,
-    ("box256_p8e6_heated", True, "poisson_rhs"): 1.84e9,
+    # profiles/k_rhs_momentum_zm_k_poisson_rhs_zm_mixed_box256_box128.md
+    ("box256_p8e6_heated", True, "rhs_momentum"): 2.01e9,
+    ("box256_p8e6_heated", True, "poisson_rhs"): 1.42e9,
 }
 
 KERNEL_BYTES = {
