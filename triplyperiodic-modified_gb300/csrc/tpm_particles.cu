@@ -57,7 +57,7 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
                        const double *__restrict__ Tgas, double *__restrict__ rhs_t,
                        const double *__restrict__ tau, int32_t *__restrict__ key_t,
                        TP *__restrict__ pay_t, int32_t *__restrict__ key_r,
-                       double *__restrict__ pay_r) {
+                       TP *__restrict__ pay_r) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
        p += (int64_t)gridDim.x * blockDim.x) {
     constexpr bool kMixed = sizeof(TU) == sizeof(float);
@@ -254,20 +254,30 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     }
     rhs_t[p] = rt;
     key_r[p] = (int32_t)at(g, i1, j1, k1);
-    pay_r[0 * np + p] = x_l;
-    pay_r[1 * np + p] = y_l;
-    pay_r[2 * np + p] = z_l;
-    pay_r[3 * np + p] = rt;
+    if constexpr (kMixed) {  // the FP32 values the mixed deposit uses (x_l is one exactly)
+      pay_r[0 * np + p] = ff_hi(x_l);
+      pay_r[1 * np + p] = ff_hi(y_l);
+      pay_r[2 * np + p] = ff_hi(z_l);
+      pay_r[3 * np + p] = ff_hi(rt);
+    } else {
+      pay_r[0 * np + p] = x_l;
+      pay_r[1 * np + p] = y_l;
+      pay_r[2 * np + p] = z_l;
+      pay_r[3 * np + p] = rt;
+    }
   }
 }
 
 // round-indexed key and payload of the given particle set (used at
-// initialisation, at x_int: grid.cpp:481-484)
+// initialisation, at x_int: grid.cpp:481-484); TP float for the mixed
+// deposit (the FP64 values truncated, as that deposit reads them)
+template <typename TP>
 __global__ void k_cic_payload(Grid g, const double *__restrict__ x, const double *__restrict__ y,
                               const double *__restrict__ z, const double *__restrict__ Tp,
                               const double *__restrict__ Tgas, double iTth, int64_t np,
                               double *__restrict__ rhs_t, int32_t *__restrict__ key_r,
-                              double *__restrict__ pay_r, int compute_rhs) {
+                              TP *__restrict__ pay_r, int compute_rhs) {
+  auto put = [&](int f, int64_t p, double v) { pay_r[f * np + p] = ff_cast<TP>(v); };
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
        p += (int64_t)gridDim.x * blockDim.x) {
     const double xx = x[p], yy = y[p], zz = z[p];
@@ -280,11 +290,11 @@ __global__ void k_cic_payload(Grid g, const double *__restrict__ x, const double
     const int j1 = wrap_any(rj, g.ny), jm = wrap_any(rj - 1, g.ny);
     const int k1 = wrap_any(rk, g.nz), km = wrap_any(rk - 1, g.nz);
     key_r[p] = (int32_t)at(g, i1, j1, k1);
-    pay_r[0 * np + p] = x_l;
-    pay_r[1 * np + p] = y_l;
-    pay_r[2 * np + p] = z_l;
+    put(0, p, x_l);
+    put(1, p, y_l);
+    put(2, p, z_l);
     if (!compute_rhs) {  // heat rate given (continuation of a run)
-      pay_r[3 * np + p] = rhs_t[p];
+      put(3, p, rhs_t[p]);
       continue;
     }
     // gas2part_Temp_int + Compute_RHS_Temp_int (particle.cpp:402-466)
@@ -298,7 +308,7 @@ __global__ void k_cic_payload(Grid g, const double *__restrict__ x, const double
                       (1 - x_l) * (1 - y_l) * (1 - z_l) * Tgas[at(g, im, jm, km)];
     const double rt = (Tg - Tp[p]) * iTth;
     rhs_t[p] = rt;
-    pay_r[3 * np + p] = rt;
+    put(3, p, rt);
   }
 }
 
@@ -641,7 +651,7 @@ __global__ void k_dep_sum8x2(Grid g, const int32_t *__restrict__ starts, const T
 // sums of the 8 cells r = c + (dx, dy, dz) in corner order.  Deterministic;
 // the sums associate per corner first.
 __global__ void k_dep_corners(Grid g, const int32_t *__restrict__ starts,
-                              const int32_t *__restrict__ perm, const double *__restrict__ pay,
+                              const int32_t *__restrict__ perm, const float *__restrict__ pay,
                               int64_t np, float *__restrict__ sums) {
   for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < g.n;
        r += (long long)gridDim.x * blockDim.x) {
@@ -651,8 +661,8 @@ __global__ void k_dep_corners(Grid g, const int32_t *__restrict__ starts,
     const int32_t s0 = starts[r], e0 = starts[r + 1];
     for (int32_t s = s0; s < e0; ++s) {
       const int32_t p = perm[s];
-      const float xl = ff_hi(pay[p]), yl = ff_hi(pay[np + p]), zl = ff_hi(pay[2 * np + p]);
-      const float rt = ff_hi(pay[3 * np + p]);
+      const float xl = pay[p], yl = pay[np + p], zl = pay[2 * np + p];
+      const float rt = pay[3 * np + p];
       const float fx[2] = {xl, 1 - xl}, fy[2] = {yl, 1 - yl}, fz[2] = {zl, 1 - zl};
 #pragma unroll
       for (int dy = 0; dy < 2; ++dy)
@@ -859,7 +869,8 @@ void launch_particle_push(tpm_ctx *c, int s, bool np1_in_base) {
   if (c->p.precision == TPM_PREC_MIXED)
     TPM_LAUNCH(c, "particle_push", (k_push<float, float>), pblocks(c->np), kThreads, 0, c->g,
                pstate(c, np1_in_base), a, c->np, c->U32, c->Tgas, c->rhs_t, c->tau, c->key_t,
-               reinterpret_cast<float *>(c->pay_t), c->key_r, c->pay_r);
+               reinterpret_cast<float *>(c->pay_t), c->key_r,
+               reinterpret_cast<float *>(c->pay_r));
   else
     TPM_LAUNCH(c, "particle_push", (k_push<double, double>), pblocks(c->np), kThreads, 0, c->g,
                pstate(c, np1_in_base), a, c->np, c->U, c->Tgas, c->rhs_t, c->tau, c->key_t,
@@ -916,8 +927,8 @@ static void heat_deposit(tpm_ctx *c) {
   double *parts = c->partials + kPartQ * kRedBlocks;
   if (mixed) {
     TPM_LAUNCH(c, "deposit_corner_sums", k_dep_corners, cell_waves(c, k_dep_corners, false),
-               kThreads, 0, c->g, c->starts_r[0], c->perm_r[0], c->pay_r, c->np,
-               c->corner_sums);
+               kThreads, 0, c->g, c->starts_r[0], c->perm_r[0],
+               reinterpret_cast<const float *>(c->pay_r), c->np, c->corner_sums);
     TPM_LAUNCH(c, "deposit_heat_conc", k_dep_gather8, nb, kThreads, 0, c->g, c->corner_sums,
                c->Q, c->C_next, parts);
   } else {
@@ -941,6 +952,18 @@ void particle_heat(tpm_ctx *c) {
   heat_deposit(c);
 }
 
+// key and heat payload of the x_int set (FP32 payload for the mixed deposit)
+static void launch_cic_payload(tpm_ctx *c, double iTth, int compute_rhs) {
+  if (c->p.precision == TPM_PREC_MIXED)
+    TPM_LAUNCH(c, "cic_payload", k_cic_payload<float>, pblocks(c->np), kThreads, 0, c->g,
+               c->pq[1][0], c->pq[1][1], c->pq[1][2], c->pq[1][6], c->Tgas, iTth, c->np,
+               c->rhs_t, c->key_r, reinterpret_cast<float *>(c->pay_r), compute_rhs);
+  else
+    TPM_LAUNCH(c, "cic_payload", k_cic_payload<double>, pblocks(c->np), kThreads, 0, c->g,
+               c->pq[1][0], c->pq[1][1], c->pq[1][2], c->pq[1][6], c->Tgas, iTth, c->np,
+               c->rhs_t, c->key_r, c->pay_r, compute_rhs);
+}
+
 // grid::Initialize tail (grid.cpp:481-484): T = (P0_int/R)/Rho_int, heat rate
 // at x_int and its deposit, plus the concentration at x_int for stage 0.
 void particle_init_heat(tpm_ctx *c) {
@@ -953,9 +976,7 @@ void particle_init_heat(tpm_ctx *c) {
     return;
   }
   double iTth = c->p.Nu * kPi * c->p.Dp * c->p.k;
-  TPM_LAUNCH(c, "cic_payload", k_cic_payload, pblocks(c->np), kThreads, 0, c->g, c->pq[1][0],
-             c->pq[1][1], c->pq[1][2], c->pq[1][6], c->Tgas, iTth, c->np, c->rhs_t, c->key_r,
-             c->pay_r, 1);
+  launch_cic_payload(c, iTth, 1);
   heat_deposit(c);
 }
 
@@ -982,9 +1003,7 @@ void particle_resume(tpm_ctx *c) {
     c->q_parts = nb;
     return;
   }
-  TPM_LAUNCH(c, "cic_payload", k_cic_payload, pblocks(c->np), kThreads, 0, c->g, c->pq[1][0],
-             c->pq[1][1], c->pq[1][2], c->pq[1][6], c->Tgas, 0.0, c->np, c->rhs_t, c->key_r,
-             c->pay_r, 0);
+  launch_cic_payload(c, 0.0, 0);
   heat_deposit(c);
 }
 
