@@ -85,6 +85,25 @@ def test_mixed_matches_fp64_gpu_128(capi):
         assert rel_err(pm[q], pf[q]) <= TOL_MIXED, q
 
 
+def test_mixed_matches_fp64_on_ragged_tiles(capi):
+    """A box whose sides are not multiples of the z-marching kernels' 32 x 8
+    column tiles and whose Nz is not a multiple of their z chunk: mixed vs
+    FP64 GPU after 3 heated steps."""
+    p, s = setup(24, 6000, seed=9, heat=0.5, precision=P.PREC_MIXED)
+    p = p.replace(Ny=20, Nz=18, Ly=p.Lx * 20 / 24, Lz=p.Lx * 18 / 24)
+    s = inputs.make_state(p, s.npart, seed=9)
+    p = p.replace(dt=inputs.cfl_dt(p, s.RU))
+    m = run(capi, p, s, 3)
+    f = run(capi, p.replace(precision=P.PREC_FP64), s, 3)
+    for g in ("RU", "RHO", "P", "C", "Q"):
+        e = rel_err(m.download_field(g), f.download_field(g))
+        assert e <= TOL_MIXED, (g, e)
+    assert m.scalars()["max_abs_div"] <= TOL_DIV
+    pm, pf = m.download_particles("base"), f.download_particles("base")
+    for q in inputs.PQ:
+        assert rel_err(pm[q], pf[q]) <= TOL_MIXED, q
+
+
 def test_mixed_keeps_the_callers_particle_order(capi):
     """The mixed path keeps its particles in cell order in memory (a
     permutation at every step boundary); every transfer is in the caller's
