@@ -112,14 +112,6 @@ struct RhsArgs {
   float f_a_fp, f_b_gd, f_c_lap, f_A, f_Rho0, f_g[3], f_inv_d[3], f_inv_d2[3];
 };
 
-// a coefficient in the compute type: the FP64 value or its FP32 copy
-template <typename TC>
-__device__ __forceinline__ TC coef(double d, float f);
-template <>
-__device__ __forceinline__ double coef<double>(double d, float) { return d; }
-template <>
-__device__ __forceinline__ float coef<float>(double, float f) { return f; }
-
 // offsets of the neighbour in direction e (0,1,2) at +1 / -1, wrapped
 struct Nbr {
   long long p[3], m[3];
@@ -135,121 +127,19 @@ __device__ __forceinline__ Nbr nbr_of(const Grid &g, const Cell &q) {
   return r;
 }
 
-// tensor0::Equal_Div_F2C of U at centre (i,j,k) (tensor0.cpp:249-256),
-// evaluated in the compute type TC (double on the FP64 path, float on the
-// mixed path; the loads convert)
-template <typename TC, typename TIn>
-__device__ __forceinline__ TC divU_at(const Grid &g, const TIn *U, int i, int j, int k,
-                                      const TC *inv_d) {
-  long long c = at(g, i, j, k);
-  const TIn *Ux = U, *Uy = U + g.n, *Uz = U + 2 * g.n;
-  return ((TC)Ux[at(g, wrap_p(i, g.nx), j, k)] - (TC)Ux[c]) * inv_d[0] +
-         ((TC)Uy[at(g, i, wrap_p(j, g.ny), k)] - (TC)Uy[c]) * inv_d[1] +
-         ((TC)Uz[at(g, i, j, wrap_p(k, g.nz))] - (TC)Uz[c]) * inv_d[2];
-}
-
-__device__ __forceinline__ long long shift(const Grid &g, int i, int j, int k, int dir, int s) {
-  if (dir == 0) return at(g, s > 0 ? wrap_p(i, g.nx) : wrap_m(i, g.nx), j, k);
-  if (dir == 1) return at(g, i, s > 0 ? wrap_p(j, g.ny) : wrap_m(j, g.ny), k);
-  return at(g, i, j, s > 0 ? wrap_p(k, g.nz) : wrap_m(k, g.nz));
-}
-
-// flux P_{d,e}(cell) = I_e,C2F(U_d) * I_d,C2F(RU_e)   (grid.cpp:785-800)
-template <typename TC, typename TIn>
-__device__ __forceinline__ TC flux_at(const Grid &g, const TIn *Ud, const TIn *RUe, int i,
-                                      int j, int k, int d, int e) {
-  long long c = at(g, i, j, k);
-  TC iu = ((TC)Ud[c] + (TC)Ud[shift(g, i, j, k, e, -1)]) * (TC)0.5;
-  TC ir = ((TC)RUe[c] + (TC)RUe[shift(g, i, j, k, d, -1)]) * (TC)0.5;
-  return iu * ir;
-}
-
-// grid::Update_RU_WOP (grid.cpp:776-814).  The right-hand side is evaluated
-// in TC; the RK combinations RU_np1 += dt*post*RHS, RU_new = RU + dt*pre*RHS
-// are always FP64.  With TC = TIn = double every operation is the reference's;
-// the mixed path reads FP32 copies of U, RU_int and F_p (TIn = float).
-template <typename TC, typename TIn>
-__global__ void k_rhs_momentum(Grid g, const TIn *__restrict__ U, const TIn *__restrict__ RUi,
-                               const TIn *__restrict__ Fp, const double *__restrict__ Rho_int,
-                               const double *__restrict__ RU, const double *__restrict__ np1_in,
-                               double *__restrict__ RU_np1, double *__restrict__ RU_new, RhsArgs a) {
-  const TC inv_d[3] = {coef<TC>(g.inv_dx, a.f_inv_d[0]), coef<TC>(g.inv_dy, a.f_inv_d[1]),
-                       coef<TC>(g.inv_dz, a.f_inv_d[2])};
-  const TC inv_d2[3] = {coef<TC>(g.inv_dx2, a.f_inv_d2[0]), coef<TC>(g.inv_dy2, a.f_inv_d2[1]),
-                        coef<TC>(g.inv_dz2, a.f_inv_d2[2])};
-  // per-cell FP64 values below go through ff_cast / ff_widen (integer
-  // operations when TC is float)
-  const TC a_fp = coef<TC>(a.a_fp, a.f_a_fp), b_gd = coef<TC>(a.b_gd, a.f_b_gd);
-  const TC c_lap = coef<TC>(a.c_lap, a.f_c_lap), A_ = coef<TC>(a.A, a.f_A);
-  const TC Rho0 = coef<TC>(a.Rho0, a.f_Rho0);
-  const TC gv[3] = {coef<TC>(a.g[0], a.f_g[0]), coef<TC>(a.g[1], a.f_g[1]),
-                    coef<TC>(a.g[2], a.f_g[2])};
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
-       c += (long long)gridDim.x * blockDim.x) {
-    Cell q = cell_of(g, c);
-    Nbr nb = nbr_of(g, q);
-    const TC div_c = divU_at<TC, TIn>(g, U, q.i, q.j, q.k, inv_d);
-    const TC div_m[3] = {divU_at<TC, TIn>(g, U, wrap_m(q.i, g.nx), q.j, q.k, inv_d),
-                         divU_at<TC, TIn>(g, U, q.i, wrap_m(q.j, g.ny), q.k, inv_d),
-                         divU_at<TC, TIn>(g, U, q.i, q.j, wrap_m(q.k, g.nz), inv_d)};
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const TIn *Ud = U + d * g.n;
-      // dummy2 = grad_C2F(div U) (tensor1.cpp:259-270)
-      TC gd = (div_c - div_m[d]) * inv_d[d];
-      // dummy = Del2(U_d) (tensor0.cpp:258-265)
-      TC ud = (TC)Ud[c];
-      TC lap = ((TC)Ud[nb.p[0]] - 2 * ud + (TC)Ud[nb.m[0]]) * inv_d2[0] +
-               ((TC)Ud[nb.p[1]] - 2 * ud + (TC)Ud[nb.m[1]]) * inv_d2[1] +
-               ((TC)Ud[nb.p[2]] - 2 * ud + (TC)Ud[nb.m[2]]) * inv_d2[2];
-      // RHS = -mp/Vcell*F_p + mu/3 grad(div U) + mu Del2 U  (grid.cpp:783)
-      TC rhs = a_fp * (TC)Fp[d * g.n + c] + b_gd * gd + c_lap * lap;
-      // convection: Div_F2C(I_C2F(U_d) * I_d,C2F(RU_int))  (grid.cpp:785-801)
-      TC conv = 0;
-      {
-        TC t[3];
-#pragma unroll
-        for (int e = 0; e < 3; ++e) {
-          const TIn *RUe = RUi + e * g.n;
-          int ip = e == 0 ? wrap_p(q.i, g.nx) : q.i;
-          int jp = e == 1 ? wrap_p(q.j, g.ny) : q.j;
-          int kp = e == 2 ? wrap_p(q.k, g.nz) : q.k;
-          t[e] = (flux_at<TC, TIn>(g, Ud, RUe, ip, jp, kp, d, e) -
-                  flux_at<TC, TIn>(g, Ud, RUe, q.i, q.j, q.k, d, e)) * inv_d[e];
-        }
-        conv = t[0] + t[1] + t[2];
-      }
-      rhs -= conv;
-      // artificial (linear) forcing A*RU_int (grid.cpp:803)
-      rhs += A_ * (TC)RUi[d * g.n + c];
-      // body force (Rho_face - Rho0)*g (grid.cpp:805-809)
-      if (a.has_g) {
-        TC rf = (ff_cast<TC>(Rho_int[c]) +
-                 ff_cast<TC>(Rho_int[d == 0 ? nb.m[0] : d == 1 ? nb.m[1] : nb.m[2]])) *
-                (TC)0.5;
-        rhs += (rf - Rho0) * gv[d];
-      }
-      // RU_np1 += dt*post*RHS ; RU_new = RU + dt*pre*RHS  (grid.cpp:811-813);
-      // FMAs on the mixed path (FP32 stencil, FP64 accumulation)
-      const double r64 = ff_widen(rhs);
-      constexpr bool kFma = sizeof(TC) == sizeof(float);
-      double np1 = kFma ? fma(a.dtpo, r64, np1_in[d * g.n + c]) : np1_in[d * g.n + c] + a.dtpo * r64;
-      RU_np1[d * g.n + c] = np1;
-      RU_new[d * g.n + c] = (a.stage != 3) ? (kFma ? fma(a.dtpr, r64, RU[d * g.n + c])
-                                                   : 1 * RU[d * g.n + c] + a.dtpr * r64)
-                                           : np1;
-    }
-  }
-}
-
-// z-marching form of k_rhs_momentum<float, float> (mixed path): a block owns
-// a kZX x kZY column of cells and walks zlen planes up in z.  The FP32 copies
-// of U and RU_int live in a ring of three shared-memory planes (z - 1, z,
-// z + 1) with a one-cell halo in x and y: each value is loaded from global
-// memory once per column instead of once per stencil use, and the next
-// plane's loads are issued before the current plane is computed.  Every cell
-// is evaluated exactly as in k_rhs_momentum (same expressions, same order),
-// so the results are bit-identical to it.
+// grid::Update_RU_WOP (grid.cpp:776-814) on the mixed path: the right-hand
+// side in FP32 from FP32 copies of U, RU_int and F_p, the RK combinations
+// RU_np1 += dt*post*RHS, RU_new = RU + dt*pre*RHS in FP64 (FMAs).  Per cell
+// and component d: grad_C2F(div U) (tensor1.cpp:259-270, tensor0.cpp:249-256)
+// times Mu0/3, Del2(U_d) (tensor0.cpp:258-265) times Mu0, -mp/Vcell F_p, the
+// convection Div_F2C of the fluxes P_{d,e} = I_e,C2F(U_d) I_d,C2F(RU_e)
+// (grid.cpp:785-801), the forcing A RU_int (grid.cpp:803) and the body force
+// (Rho_face - Rho0) g (grid.cpp:805-809), each in the reference's operation
+// order.  A block owns a kZX x kZY column of cells and walks zlen planes up
+// in z; the FP32 copies of U and RU_int live in a ring of three
+// shared-memory planes (z - 1, z, z + 1) with a one-cell halo in x and y, so
+// each value is loaded from global memory once per column instead of once
+// per stencil use.
 constexpr int kZX = 32, kZY = 8;  // column tile; the z chunk is zm_zlen planes
 constexpr int kZPX = kZX + 2, kZPY = kZY + 2, kZPlane = kZPX * kZPY;
 
@@ -357,12 +247,13 @@ k_rhs_momentum_zm(Grid g, const float *__restrict__ U, const float *__restrict__
   }
 }
 
-// Tiled form of k_rhs_momentum: one block owns a TX x TY x TZ tile; U and
-// RU_int of the tile plus a one-cell halo are staged in shared memory, the
-// divergence of U and the nine convective fluxes P_{d,e} are evaluated once
-// per cell of the tile (the untiled kernel re-evaluates them 4x and 2x), then
-// each thread assembles its cell.  Every value keeps its operation order, so
-// the results are bit-identical to the untiled kernel.
+// grid::Update_RU_WOP (grid.cpp:776-814) on the FP64 path, every operation
+// the reference's (the terms of k_rhs_momentum_zm, in FP64 with separate
+// multiplies and adds).  One block owns a TX x TY x TZ tile; U and RU_int of
+// the tile plus a one-cell halo are staged in shared memory, the divergence
+// of U and the nine convective fluxes P_{d,e} are evaluated once per cell of
+// the tile (a per-cell form re-evaluates them 4x and 2x), then each thread
+// assembles its cell.
 constexpr int kTX = 32, kTY = 4, kTZ = 2;
 constexpr int kBX = kTX + 2, kBY = kTY + 2, kBZ = kTZ + 2;  // staged box
 constexpr int kFX = kTX + 1, kFY = kTY + 1, kFZ = kTZ + 1;  // divergence / flux boxes
