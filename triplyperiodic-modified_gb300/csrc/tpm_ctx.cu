@@ -459,6 +459,8 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->starts_t = dalloc<int32_t>(c, n + 1);
     c->starts_r[0] = dalloc<int32_t>(c, n + 1);
     c->counts = dalloc<int32_t>(c, n);
+    c->unsorted = dalloc<unsigned char>(c, (n + 15) / 16 * 16);
+    TPM_CUDA_TRY(cudaMemsetAsync(c->unsorted, 0, (n + 15) / 16 * 16, c->stream));
     c->scan_blocks = dalloc<int32_t>(c, (size_t)(n / 4096 + 2));
     c->pay_t = dalloc<double>(c, 6 * (size_t)np);
     c->pay_t_s = dalloc<double>(c, 6 * (size_t)np);

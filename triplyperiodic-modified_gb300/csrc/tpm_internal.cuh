@@ -223,6 +223,8 @@ struct tpm_ctx {
   int32_t *perm_t = nullptr, *perm_r[1] = {nullptr};
   int32_t *starts_t = nullptr, *starts_r[1] = {nullptr};
   int32_t *counts = nullptr;
+  // n rounded up to 16: cells the scatter left out of order (all zero between sorts)
+  unsigned char *unsorted = nullptr;
   int32_t *scan_blocks = nullptr;
   double *pay_t = nullptr, *pay_t_s = nullptr;          // 6*np
   double *pay_r = nullptr;  // 4*np: round-indexed fractions and heat rate, unsorted

@@ -462,9 +462,13 @@ __global__ void k_scan_apply(int32_t *__restrict__ counts, long long n,
   if (blockIdx.x == 0 && threadIdx.x == 0) starts[n] = total;
 }
 
+// Lanes of a warp with equal keys take consecutive slots in lane order, that
+// is in particle order; only a cell whose particles arrive from more than one
+// warp (a group smaller than the cell's count) can end up out of order, and
+// only such cells are flagged for k_segsort.
 __global__ void k_scatter(const int32_t *__restrict__ key, int64_t np,
                           const int32_t *__restrict__ starts, int32_t *__restrict__ cursor,
-                          int32_t *__restrict__ perm) {
+                          int32_t *__restrict__ perm, unsigned char *__restrict__ unsorted) {
   const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane; base < np;
@@ -476,7 +480,10 @@ __global__ void k_scatter(const int32_t *__restrict__ key, int64_t np,
       const unsigned peers = __match_any_sync(live, k);
       const int leader = __ffs(peers) - 1;
       int32_t first = 0;
-      if (lane == leader) first = atomicAdd(&cursor[k], __popc(peers));
+      if (lane == leader) {
+        first = atomicAdd(&cursor[k], __popc(peers));
+        if (__popc(peers) != starts[k + 1] - starts[k]) unsorted[k] = 1;
+      }
       first = __shfl_sync(live, first, leader);
       const int32_t slot = starts[k] + first + __popc(peers & ((1u << lane) - 1u));
       perm[slot] = (int32_t)p;
@@ -484,8 +491,9 @@ __global__ void k_scatter(const int32_t *__restrict__ key, int64_t np,
   }
 }
 
-// order each cell's particles by index: the deposit sums become independent
-// of the scatter's atomic order.  Insertion sort for the usual few particles
+// order each flagged cell's particles by index (and clear its flag): the
+// deposit sums become independent of the scatter's atomic order.  Insertion
+// sort for the usual few particles
 // per cell, an in-place heap sort (O(m log m), bounded) up to kSortMaxRun;
 // a cell beyond that (a diverging run crowding its particles) is left in
 // arrival order and flagged, so that no cell costs a thread more than
@@ -505,34 +513,51 @@ __device__ __forceinline__ void sift_down(int32_t *a, int32_t root, int32_t end)
   }
 }
 
-__global__ void k_segsort(long long n, const int32_t *__restrict__ starts,
-                          int32_t *__restrict__ perm, int *__restrict__ crowded) {
-  for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n;
-       c += (long long)gridDim.x * blockDim.x) {
-    int32_t s = starts[c], e = starts[c + 1];
-    const int32_t m = e - s;
-    if (m <= 32) {
-      for (int32_t a = s + 1; a < e; ++a) {
-        int32_t v = perm[a];
-        int32_t b = a - 1;
-        while (b >= s && perm[b] > v) {
-          perm[b + 1] = perm[b];
-          --b;
-        }
-        perm[b + 1] = v;
+__device__ void sort_cell(int32_t s, int32_t e, int32_t *__restrict__ perm,
+                          int *__restrict__ crowded) {
+  const int32_t m = e - s;
+  if (m <= 32) {
+    for (int32_t a = s + 1; a < e; ++a) {
+      int32_t v = perm[a];
+      int32_t b = a - 1;
+      while (b >= s && perm[b] > v) {
+        perm[b + 1] = perm[b];
+        --b;
       }
-    } else if (m <= kSortMaxRun) {
-      int32_t *a = perm + s;
-      for (int32_t i = m / 2 - 1; i >= 0; --i) sift_down(a, i, m);
-      for (int32_t end = m - 1; end > 0; --end) {
-        const int32_t t = a[0];
-        a[0] = a[end];
-        a[end] = t;
-        sift_down(a, 0, end);
-      }
-    } else {
-      *crowded = 1;
+      perm[b + 1] = v;
     }
+  } else if (m <= kSortMaxRun) {
+    int32_t *a = perm + s;
+    for (int32_t i = m / 2 - 1; i >= 0; --i) sift_down(a, i, m);
+    for (int32_t end = m - 1; end > 0; --end) {
+      const int32_t t = a[0];
+      a[0] = a[end];
+      a[end] = t;
+      sift_down(a, 0, end);
+    }
+  } else {
+    *crowded = 1;
+  }
+}
+
+// One thread per 16 flags (the flag array is padded to a multiple of 16
+// bytes, the padding zero): most words are all zero, so the pass is one
+// 16-byte load per thread and iteration.
+__global__ void k_segsort(long long nwords, const int32_t *__restrict__ starts,
+                          int32_t *__restrict__ perm, uint4 *__restrict__ unsorted,
+                          int *__restrict__ crowded) {
+  for (long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x; w < nwords;
+       w += (long long)gridDim.x * blockDim.x) {
+    const uint4 f = unsorted[w];
+    if ((f.x | f.y | f.z | f.w) == 0u) continue;
+    unsorted[w] = make_uint4(0u, 0u, 0u, 0u);
+    const unsigned word[4] = {f.x, f.y, f.z, f.w};
+    for (int q = 0; q < 4; ++q)
+      for (int b = 0; b < 4; ++b)
+        if ((word[q] >> (8 * b)) & 0xffu) {
+          const long long c = w * 16 + q * 4 + b;
+          sort_cell(starts[c], starts[c + 1], perm, crowded);
+        }
   }
 }
 
@@ -776,9 +801,11 @@ void sort_by_cell(tpm_ctx *c, const int32_t *key, int32_t *perm, int32_t *starts
   TPM_LAUNCH(c, "sort_scan_apply", k_scan_apply, nchunks, kScanThreads, 0, c->counts, n,
              c->scan_blocks, starts, (int32_t)c->np);
   TPM_LAUNCH(c, "sort_scatter", k_scatter, pblocks(c->np), kThreads, 0, key, c->np, starts,
-             c->counts, perm);
-  TPM_LAUNCH(c, "sort_segsort", k_segsort, cell_waves(c, k_segsort, false), kThreads, 0, n,
-             starts, perm,
+             c->counts, perm, c->unsorted);
+  const long long nwords = (n + 15) / 16;
+  TPM_LAUNCH(c, "sort_segsort", k_segsort,
+             wave_blocks(c, reinterpret_cast<const void *>(k_segsort), kThreads, nwords, false),
+             kThreads, 0, nwords, starts, perm, reinterpret_cast<uint4 *>(c->unsorted),
              &c->dsc->crowded);
 }
 
