@@ -531,15 +531,46 @@ __global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const d
   const int ky = blockIdx.x / tiles, kx0 = (blockIdx.x % tiles) * npen;
   const long long plane = (long long)g.ny * g.nxh;
   const long long base = (long long)ky * g.nxh + kx0;
-  tile_load<4>(a, npen * g.nz, lq, [&](int q, int kz) {
+  const int tot = npen * g.nz;
+  // the first kInvPre reciprocals of each thread's modes, loaded before the
+  // pencils so that their latency hides behind the loads and the forward FFT
+  constexpr int kInvPre = 8;
+  T invr[kInvPre];
+  if (inv_mwn) {
+#pragma unroll
+    for (int u = 0; u < kInvPre; ++u) {
+      const int idx = threadIdx.x + u * (int)blockDim.x;
+      const int q = idx & (npen - 1), kz = idx >> lq;
+      invr[u] = (idx < tot && kx0 + q < g.nxh)
+                    ? inv_mwn[((long long)kz * g.ny + ky) * g.nxh + kx0 + q]
+                    : T(0);
+    }
+  }
+  tile_load<4>(a, tot, lq, [&](int q, int kz) {
     return (kx0 + q < g.nxh) ? spec[base + kz * plane + q] : Cx<T2>::mk(0, 0);
   });
   __syncthreads();
   T2 *r = smem_fft(a, b, npen, pl, -1);
   T2 *other = (r == a) ? b : a;
   // divide by the modified wave number except the zero mode (poisson.cpp:442-449)
+  int from = threadIdx.x;
+  if (inv_mwn) {
+#pragma unroll
+    for (int u = 0; u < kInvPre; ++u) {
+      const int idx = threadIdx.x + u * (int)blockDim.x;
+      const int q = idx & (npen - 1), kz = idx >> lq;
+      const int kx = kx0 + q;
+      if (idx < tot && kx < g.nxh && (kx + ky + kz) > 0) {
+        T2 v = r[kz * npen + q];
+        v.y = v.y * invr[u];
+        v.x = v.x * invr[u];
+        r[kz * npen + q] = v;
+      }
+    }
+    from += kInvPre * (int)blockDim.x;
+  }
 #pragma unroll 4
-  for (int idx = threadIdx.x; idx < npen * g.nz; idx += blockDim.x) {
+  for (int idx = from; idx < tot; idx += blockDim.x) {
     const int q = idx & (npen - 1), kz = idx >> lq;
     const int kx = kx0 + q;
     if (kx < g.nxh && (kx + ky + kz) > 0) {
