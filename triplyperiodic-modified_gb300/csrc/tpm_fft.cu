@@ -473,7 +473,7 @@ __global__ void k_fft_y(Grid g, FftPlan pl, T2 *__restrict__ spec, int npen, int
   const int tiles = (g.nxh + npen - 1) / npen;
   const int kz = blockIdx.x / tiles, kx0 = (blockIdx.x % tiles) * npen;
   const long long base = (long long)kz * g.ny * g.nxh;
-  tile_load<4>(a, npen * g.ny, lq, [&](int q, int ky) {
+  tile_load<8>(a, npen * g.ny, lq, [&](int q, int ky) {
     return (kx0 + q < g.nxh) ? spec[base + (long long)ky * g.nxh + kx0 + q] : Cx<T2>::mk(0, 0);
   });
   __syncthreads();
@@ -546,7 +546,7 @@ __global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const d
                     : T(0);
     }
   }
-  tile_load<4>(a, tot, lq, [&](int q, int kz) {
+  tile_load<8>(a, tot, lq, [&](int q, int kz) {
     return (kx0 + q < g.nxh) ? spec[base + kz * plane + q] : Cx<T2>::mk(0, 0);
   });
   __syncthreads();
