@@ -332,6 +332,70 @@ def path_result(p, s, ms, steps, world, n_it, launches, prof, clocks, mixed, pea
     }
 
 
+def compare_paths(a, b, idx):
+    """Per-field relative differences of context a (mixed) against b (FP64) at
+    the same step: max|a - b| / max|b| per field and particle quantity, plus
+    the particles whose interpolation cell differs between the two - by
+    truncation, the gas-velocity cell (particle.cpp:340-360), or by rounding,
+    the temperature and concentration cell (particle.cpp:430-456,522-555) -
+    and the particles whose velocity differs by more than 1e-6 of the largest
+    speed (the mark of a particle that took another cell's velocity)."""
+    import numpy as np
+
+    out = {}
+    for g in ("RU", "RHO", "P", "C", "Q"):
+        x, y = a.download_field(g), b.download_field(g)
+        ymax = float(np.abs(y).max())
+        if ymax < 1e-9:  # a field at roundoff level (Q of an unheated run): absolute
+            out[g] = {"abs_diff": float(np.abs(x - y).max()), "fp64_max": ymax}
+        else:
+            out[g] = float(np.abs(x - y).max() / ymax)
+    pa, pb = a.download_particles("base"), b.download_particles("base")
+    out["particles"] = max(float(np.abs(pa[q] - pb[q]).max() / max(np.abs(pb[q]).max(), 1e-300))
+                           for q in ("x", "y", "z", "u", "v", "w", "T"))
+    trunc_diff = np.zeros(len(pa["x"]), bool)
+    round_diff = np.zeros(len(pa["x"]), bool)
+    for q, i in zip(("x", "y", "z"), idx):
+        ua, ub = pa[q] * i, pb[q] * i
+        trunc_diff |= np.trunc(ua) != np.trunc(ub)
+        round_diff |= np.floor(ua + 0.5) != np.floor(ub + 0.5)
+    vmax = max(float(np.abs(pb[q]).max()) for q in ("u", "v", "w"))
+    vdiff = np.zeros(len(pa["x"]), bool)
+    for q in ("u", "v", "w"):
+        vdiff |= np.abs(pa[q] - pb[q]) > 1e-6 * vmax
+    out["particles_other_cell_trunc"] = int(trunc_diff.sum())
+    out["particles_other_cell_round"] = int(round_diff.sum())
+    out["particles_velocity_off_1e-6"] = int(vdiff.sum())
+    return out
+
+
+def mixed_accuracy_fresh(p64, s, checkpoints=(1, 10)):
+    """Mixed against FP64 from the same seeded state on fresh contexts,
+    compared after exactly `checkpoints` RK4 steps (eager stepping; graph
+    replay is bit-identical)."""
+    from tpm import capi, params as P
+
+    ctx = {}
+    for name, prec in (("mixed", P.PREC_MIXED), ("fp64", P.PREC_FP64)):
+        c = capi.Context(p64.replace(precision=prec), s.npart)
+        c.load(s)
+        c.initialize()
+        ctx[name] = c
+    idx = (p64.Nx / p64.Lx, p64.Ny / p64.Ly, p64.Nz / p64.Lz)
+    out, done = {}, 0
+    for n in checkpoints:
+        for c in ctx.values():
+            c.run(n - done)
+            c.sync()
+        done = n
+        r = compare_paths(ctx["mixed"], ctx["fp64"], idx)
+        r["max_abs_div_after_projection"] = ctx["mixed"].scalars()["max_abs_div"]
+        out[f"after_{n}_step" + ("s" if n > 1 else "")] = r
+    for c in ctx.values():
+        c.close()
+    return out
+
+
 def cufft_solve_ms(shape, lengths, dtype, reps=10):
     """A constant-coefficient Poisson solve through cuFFT (torch.fft: 3-D R2C,
     divide by the modified wave number, C2R), CUDA-event timed: the library
@@ -403,23 +467,15 @@ def gpu_main(args):
     head = "mixed" if "mixed" in res else "fp64"
     accuracy = None
     if "mixed" in ctxs and "fp64" in ctxs:
-        # both paths ran the same steps from the same state
+        # both timed paths ran the same steps from the same state
         a, b = ctxs["mixed"], ctxs["fp64"]
-        accuracy = {}
-        for g in ("RU", "RHO", "P", "C", "Q"):
-            x, y = a.download_field(g), b.download_field(g)
-            ymax = float(np.abs(y).max())
-            if ymax < 1e-9:  # a field at roundoff level (Q of an unheated run): absolute
-                accuracy[g] = {"abs_diff": float(np.abs(x - y).max()), "fp64_max": ymax}
-            else:
-                accuracy[g] = float(np.abs(x - y).max() / ymax)
-        pa, pb = a.download_particles("base"), b.download_particles("base")
-        accuracy["particles"] = max(float(np.abs(pa[q] - pb[q]).max() / max(np.abs(pb[q]).max(),
-                                                                           1e-300))
-                                    for q in ("x", "y", "z", "u", "v", "w", "T"))
-        accuracy = {"rel_err_vs_fp64_per_field": accuracy,
-                    "max_abs_div_after_projection": a.scalars()["max_abs_div"]}
+        idx = (p64.Nx / p64.Lx, p64.Ny / p64.Ly, p64.Nz / p64.Lz)
+        after = compare_paths(a, b, idx)
+        after["steps"] = a.scalars()["num_timestep"]
+        after["max_abs_div_after_projection"] = a.scalars()["max_abs_div"]
         ctxs["fp64"].close()
+        accuracy = mixed_accuracy_fresh(p64, s, (1, 10))
+        accuracy["after_timed_run"] = after
     hctx = ctxs[head]
     e2e_ms, h2d, d2h = time_e2e(hctx, max(1, min(args.steps, 3)))
     e2e_ms = max_over_ranks(e2e_ms, dist, "cuda")

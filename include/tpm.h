@@ -135,8 +135,8 @@ typedef struct tpm_ctx tpm_ctx;
 int tpm_abi_version(void);
 
 /* Create a context for one box with np particles on the current CUDA device.
- * Rejects options outside the ported path (HYPRE solvers, passive scalar,
- * passive vector, elongated box) with TPM_ERR_UNSUPPORTED. */
+ * Rejects options outside the ported path (HYPRE solvers other than the PCG
+ * stand-in, passive vector, elongated box) with TPM_ERR_UNSUPPORTED. */
 int tpm_create(const tpm_params *params, int64_t np, tpm_ctx **out);
 int tpm_destroy(tpm_ctx *ctx);
 const char *tpm_last_error(const tpm_ctx *ctx);
@@ -211,6 +211,40 @@ int tpm_resume(tpm_ctx *ctx);
 int tpm_substep(tpm_ctx *ctx, int rk_stage);
 /* End of a time step (simulation.cpp:80,91): RU_np1.make_mean_U0, TimeAdvance. */
 int tpm_end_step(tpm_ctx *ctx);
+
+/*
+ * The reference's grid methods one by one, for a time loop kept in the shape
+ * of simulation.cpp:58-91 (include/tpm_grid.hpp wraps them in a C++ class
+ * with the reference's names).  Each queues the kernels of one method for RK4
+ * stage rk_stage (grid::RK4_count) on the context's stream.  They must come
+ * in the reference loop's order - Update_Rho and Update_P0 (either order),
+ * Update_Particle, Update_Passive_Scalar (solve_for_scalar only),
+ * Update_RU_WOP, Compute_Div_U_new, Compute_RHS_Pois, Solve_Poisson,
+ * Update_RU_WP, TimeAdvance_RK4, and after the fourth stage
+ * RU_np1.make_mean_U0 and TimeAdvance - with rk_stage the stage the context
+ * is at; a call out of that order returns TPM_ERR_STATE and queues nothing.
+ * The sequence gives the same bits as tpm_substep / tpm_end_step (which run
+ * independent kernels of a stage side by side on a second stream).  Where
+ * the GPU path fuses two methods into one pass, the first records its turn
+ * and the second queues the pass: the divergence constraint of
+ * Compute_Div_U_new is formed by Compute_RHS_Pois's pass, and the gas
+ * temperature Update_Particle reads is formed by the density pass, which
+ * therefore queues Update_P0's kernel first when Update_P0 has not run yet
+ * (P0 does not depend on the density, grid.cpp:816-830).
+ */
+int tpm_param_update(tpm_ctx *ctx);                 /* PARAM.update(T_cur), params.cpp:80-86 */
+int tpm_update_rho(tpm_ctx *ctx, int rk_stage);      /* grid::Update_Rho, grid.cpp:608-614 */
+int tpm_update_p0(tpm_ctx *ctx, int rk_stage);       /* grid::Update_P0, grid.cpp:816-830 */
+int tpm_update_particle(tpm_ctx *ctx, int rk_stage); /* grid::Update_Particle, grid.cpp:865-888 */
+int tpm_update_passive_scalar(tpm_ctx *ctx, int rk_stage); /* grid.cpp:743-772 */
+int tpm_update_ru_wop(tpm_ctx *ctx, int rk_stage);   /* grid::Update_RU_WOP, grid.cpp:776-814 */
+int tpm_compute_div_u_new(tpm_ctx *ctx, int rk_stage); /* grid.cpp:832-839 */
+int tpm_compute_rhs_pois(tpm_ctx *ctx, int rk_stage);  /* grid.cpp:841-849 */
+int tpm_solve_poisson(tpm_ctx *ctx, int rk_stage);   /* grid::Solve_Poisson, grid.cpp:851-855 */
+int tpm_update_ru_wp(tpm_ctx *ctx, int rk_stage);    /* grid::Update_RU_WP, grid.cpp:857-863 */
+int tpm_time_advance_rk4(tpm_ctx *ctx, int rk_stage); /* grid::TimeAdvance_RK4, grid.cpp:890-900 */
+int tpm_make_mean_u0(tpm_ctx *ctx);  /* RU_np1.make_mean_U0 (simulation.cpp:80, tensor1.cpp:320-325) */
+int tpm_time_advance(tpm_ctx *ctx);  /* grid::TimeAdvance, grid.cpp:595-606 */
 /* PARAM.update(T_cur) + 4 substeps + end of step (simulation.cpp:58-91). */
 int tpm_step(tpm_ctx *ctx);
 int tpm_run(tpm_ctx *ctx, int nsteps);
@@ -229,10 +263,11 @@ int tpm_poisson_solve(tpm_ctx *ctx, const double *C3, double *P, const double *R
 /*
  * Poisson solve that allocates nothing.  This entry point has no counterpart
  * in the reference.  It is for callers that cannot call cudaMalloc: plug-ins
- * handed device buffers by a host application, code issuing work while a
- * stream is being captured, or runtimes whose memory pool forbids side
- * allocations.  It solves the same problem as tpm_poisson_solve (the
- * reference's poisson::Solve with Solver==0) on DEVICE pointers: C3 (3 face
+ * handed device buffers by a host application that owns all device memory,
+ * or runtimes whose memory pool forbids side allocations.  It solves the same
+ * problem as tpm_poisson_solve (the reference's poisson::Solve with
+ * Solver==0, stopping as poisson.cpp:397 does: while iterations <
+ * max_iterations and max|dp| > epsilon) on DEVICE pointers: C3 (3 face
  * blocks), P (initial guess in, solution out) and RHS, for an Nx*Ny*Nz box of
  * size Lx*Ly*Lz, on `stream` (a cudaStream_t; NULL = legacy default stream).
  * It needs no context and never calls cudaMalloc, cudaFree or any allocating
@@ -240,11 +275,14 @@ int tpm_poisson_solve(tpm_ctx *ctx, const double *C3, double *P, const double *R
  * TPM_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until
  * process exit, which bounds the grid to roughly 100^3 cells; larger grids
  * return TPM_ERR_ARG.  The first call on a device looks up the array's
- * device address and sets kernel attributes, so make that first call before
- * any stream capture.  All calls share the array: calls that overlap on the
- * GPU (other streams, other host threads) race and must be serialised by the
- * caller.  It synchronises `stream` once per call (and once per iteration
- * when epsilon > 0, to test the stopping rule).
+ * device address and sets kernel attributes.  Each call synchronises
+ * `stream` (once, and once per iteration when epsilon > 0, to test the
+ * stopping rule), so `stream` must not be capturing a CUDA graph: the call
+ * then returns TPM_ERR_STATE and does nothing.  All calls on one GPU share
+ * its array: calls that overlap on that GPU (other streams, other host
+ * threads) race and must be serialised by the caller; calls on different
+ * GPUs may run concurrently.  With max_iterations = 0 it reports error 100,
+ * the reference's initial error.
  */
 #define TPM_NOALLOC_SCRATCH_BYTES (16u << 20)
 int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, double Ly, double Lz,

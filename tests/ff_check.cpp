@@ -134,6 +134,30 @@ int main() {
               up == (std::fabs(f) >= 0.5),
           "edge %.17g -> %d %.9g %d", u, ip, (double)fr, (int)up);
   }
+  // trunc and the fraction as a pair: within 2^(e-48) of the exact fraction
+  for (int n = 0; n < 2000000; ++n) {
+    const double u = (rng() & 1 ? -1.0 : 1.0) *
+                     std::ldexp(mant(rng), (int)(rng() % 40) - 20);  // 2^-20 .. 2^20
+    int ip;
+    float2 fr;
+    ff_int_frac2(u, ip, fr);
+    const double t = std::trunc(u), f = u - t;
+    const int e = std::ilogb(u);
+    CHECK(ip == (int)t, "trunc2 %.17g -> %d", u, ip);
+    const long double ef = std::fabs((long double)fr.x + fr.y - f);
+    CHECK(ef <= std::ldexp(1.0L, (e < 0 ? 0 : e) - 48) &&
+              (e >= 0 || ef <= std::ldexp(std::fabs(u), -48)),
+          "frac2 %.17g err %.3Lg", u, ef);
+    CHECK(std::fabs(fr.y) <= std::ldexp(std::fabs(fr.x), -23), "frac2 normalised %.17g", u);
+  }
+  for (double u : {0.0, 0.5, 1.0, 2.5, -2.5, 3.0, -0.25, 255.99999999999997, 127.0 + 1e-13}) {
+    int ip;
+    float2 fr;
+    ff_int_frac2(u, ip, fr);
+    const double t = std::trunc(u), f = u - t;
+    CHECK(ip == (int)t && std::fabs((long double)fr.x + fr.y - f) <= std::ldexp(1.0L, -40),
+          "edge2 %.17g -> %d %.9g %.9g", u, ip, (double)fr.x, (double)fr.y);
+  }
   // index division: every divisor up to 4096 against edge and random
   // numerators below 2^31
   for (unsigned d = 1; d <= 4096; ++d) {

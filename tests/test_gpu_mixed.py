@@ -72,17 +72,31 @@ def test_mixed_matches_fp64_oracle(capi, oracle_lib, heat):
 
 
 def test_mixed_matches_fp64_gpu_128(capi):
-    """Heated 128^3 box with 10^6 particles, 2 steps, mixed vs FP64 GPU."""
+    """Heated 128^3 box with 10^6 particles: mixed vs FP64 GPU after 1 and 10
+    steps, per field and per particle quantity, and no particle in another
+    gas-velocity cell (truncated index) than on the FP64 path."""
     p, s = setup(128, 1_000_000, seed=1, heat=0.1, precision=P.PREC_MIXED, nu=0.005)
-    m = run(capi, p, s, 2)
-    f = run(capi, p.replace(precision=P.PREC_FP64), s, 2)
-    for g in ("RU", "RHO", "P", "C", "Q"):
-        e = rel_err(m.download_field(g), f.download_field(g))
-        assert e <= TOL_MIXED, (g, e)
-    assert m.scalars()["max_abs_div"] <= TOL_DIV
-    pm, pf = m.download_particles("base"), f.download_particles("base")
-    for q in inputs.PQ:
-        assert rel_err(pm[q], pf[q]) <= TOL_MIXED, q
+    ctxs = []
+    for prec in (P.PREC_MIXED, P.PREC_FP64):
+        c = capi.Context(p.replace(precision=prec), s.npart)
+        c.load(s)
+        c.initialize()
+        ctxs.append(c)
+    m, f = ctxs
+    for more in (1, 9):
+        for c in ctxs:
+            c.run(more)
+            c.sync()
+        for g in ("RU", "RHO", "P", "C", "Q"):
+            e = rel_err(m.download_field(g), f.download_field(g))
+            assert e <= TOL_MIXED, (g, e)
+        assert m.scalars()["max_abs_div"] <= TOL_DIV
+        pm, pf = m.download_particles("base"), f.download_particles("base")
+        for q in inputs.PQ:
+            assert rel_err(pm[q], pf[q]) <= TOL_MIXED, q
+        for q, L, n in (("x", p.Lx, p.Nx), ("y", p.Ly, p.Ny), ("z", p.Lz, p.Nz)):
+            idx = n / L
+            assert np.array_equal(np.trunc(pm[q] * idx), np.trunc(pf[q] * idx)), q
 
 
 def test_mixed_matches_fp64_on_ragged_tiles(capi):

@@ -161,7 +161,7 @@ double read_err(tpm_ctx *c) {
 // result and the iteration count are the same.  Solver = 2 runs PCG
 // (tpm_pcg.cu) under the same control with its two-norm test.
 void poisson_loop(tpm_ctx *c, int max_it, double eps) {
-  TPM_CUDA_TRY(cudaMemsetAsync(&c->dsc->skip, 0, 2 * sizeof(int), c->stream));  // skip, it
+  tpm::poisson_loop_begin(c);  // skip = it = 0, err = 100
   const double eps_ctl = eps > 0 ? eps : 0.0;
   if (c->p.Solver == 2) {
     if (c->device_loop) {
@@ -184,19 +184,24 @@ void poisson_loop(tpm_ctx *c, int max_it, double eps) {
     if (eps > 0) c->last_err = error;
     return;
   }
+  // Richardson (poisson.cpp:395-410): the device applies the reference's test
+  // error > epsilon after every iteration, for any epsilon (with epsilon <= 0
+  // it stops only on max|dp| == 0, turning the rest of the iterations into
+  // no-ops); eagerly the host also reads max|dp| when epsilon > 0, to stop
+  // launching
   const bool refine = c->p.precision == TPM_PREC_MIXED;
   if (c->device_loop) {
     c->last_it = -1;  // on the device (DevScalars::it)
     if (max_it <= 0) return;
     tpm::LoopCtl loop = new_loop(c, max_it);
-    capture_while(c, loop, [&] { tpm::poisson_iteration(c, eps_ctl, &loop); });
+    capture_while(c, loop, [&] { tpm::poisson_iteration(c, eps, &loop); });
     if (refine) tpm::refine_finish(c);
     return;
   }
   int it = 0;
   double error = 100;
   while ((it < max_it) && (error > eps)) {
-    tpm::poisson_iteration(c);
+    tpm::poisson_iteration(c, eps);
     it++;
     if (eps > 0) error = read_err(c);
   }
@@ -204,6 +209,25 @@ void poisson_loop(tpm_ctx *c, int max_it, double eps) {
   c->last_it = it;
   c->total_it += it;
   if (eps > 0) c->last_err = error;
+}
+
+// phases of one stage for the reference-granularity entry points
+enum : unsigned {
+  PH_P0 = 1u << 0, PH_RHO = 1u << 1, PH_PART = 1u << 2, PH_PS = 1u << 3, PH_RUWOP = 1u << 4,
+  PH_DIV = 1u << 5, PH_RHSP = 1u << 6, PH_SOLVE = 1u << 7, PH_RUWP = 1u << 8, PH_MEAN = 1u << 9
+};
+
+// May phase `bit` of stage k run now?  `need`: the phases of the stage that
+// the reference's loop (simulation.cpp:60-77) runs before it.
+int phase_check(tpm_ctx *c, int k, unsigned bit, unsigned need, const char *name) {
+  if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
+  if (k < 0 || k > 3) return fail(c, TPM_ERR_ARG, std::string(name) + ": rk_stage must be 0..3");
+  if (k != c->stage_next)
+    return fail(c, TPM_ERR_STATE, std::string(name) + ": the context is at RK4 stage " +
+                                      std::to_string(c->stage_next) + ", not " + std::to_string(k));
+  if ((c->ph_done & bit) || (c->ph_done & need) != need)
+    return fail(c, TPM_ERR_STATE, std::string(name) + ": out of the reference loop's order");
+  return TPM_OK;
 }
 
 void swap_stage(tpm_ctx *c) {
@@ -215,6 +239,9 @@ void swap_stage(tpm_ctx *c) {
   for (int q = 0; q < 7; ++q) std::swap(c->pq[1][q], c->pq[2][q]);
   TPM_CUDA_TRY(cudaMemcpyAsync(&c->dsc->P0_int, &c->dsc->P0_new, sizeof(double),
                                cudaMemcpyDeviceToDevice, c->stream));
+  c->stage_next += 1;
+  c->ph_done = 0;
+  c->p0_called = false;
 }
 
 // FP32 copy of RU_int for the mixed path's stencils
@@ -268,7 +295,10 @@ void substep(tpm_ctx *c, int s) {
   if (par) TPM_CUDA_TRY(cudaEventRecord(c->join_ev[0], c->aux));
   tpm::launch_rho_update(c, s, nb);
   beside(1, [&] { tpm::launch_face_coeff(c); });
-  if (par) TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[0], 0));  // U for the push
+  // the FP64 push and the passive scalar read the face velocity U (the mixed
+  // push interpolates RU_int / I_C2F(Rho_int) itself)
+  if (par && (c->p.precision != TPM_PREC_MIXED || c->PS))
+    TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[0], 0));
   tpm::launch_particle_push(c, s, nb);
   tpm::particle_deposit_momentum(c);
   beside(2, [&] { tpm::launch_rhs_momentum(c, s, nb); });
@@ -285,9 +315,8 @@ void substep(tpm_ctx *c, int s) {
   c->np1_is_base = false;
 }
 
-void end_step(tpm_ctx *c) {
-  // simulation.cpp:80 then grid::TimeAdvance (grid.cpp:595-606)
-  tpm::launch_mean_reset(c);
+// grid::TimeAdvance (grid.cpp:595-606): the step copies base = np1
+void time_advance(tpm_ctx *c) {
   std::swap(c->Rho, c->Rho_np1);
   std::swap(c->PS, c->PS_np1);  // grid.cpp:598
   for (int q = 0; q < 7; ++q) std::swap(c->pq[0][q], c->pq[3][q]);
@@ -297,7 +326,16 @@ void end_step(tpm_ctx *c) {
   c->num_timestep++;
   c->np1_is_base = true;
   c->stepped = true;
+  c->stage_next = 0;
+  c->ph_done = 0;
+  c->p0_called = false;
   tpm::particle_reorder(c);  // mixed path: cell order of the stage-3 positions
+}
+
+void end_step(tpm_ctx *c) {
+  // simulation.cpp:80 (RU_np1.make_mean_U0) then grid::TimeAdvance
+  tpm::launch_mean_reset(c);
+  time_advance(c);
 }
 
 }  // namespace
@@ -780,6 +818,9 @@ int tpm_initialize(tpm_ctx *c) {
     push_scalars(c);
     c->np1_is_base = true;
     c->rui32_stale = true;
+    c->stage_next = 0;
+    c->ph_done = 0;
+    c->p0_called = false;
     if (c->PS) {  // grid.cpp:465-476
       TPM_CUDA_TRY(cudaMemcpyAsync(c->PS_int, c->PS, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
       tpm::launch_passive_scalar_face(c, c->PS);
@@ -825,6 +866,9 @@ void resume_device(tpm_ctx *c) {
     push_scalars(c);
     c->np1_is_base = true;
     c->rui32_stale = true;
+    c->stage_next = 0;
+    c->ph_done = 0;
+    c->p0_called = false;
     if (c->PS) {
       TPM_CUDA_TRY(cudaMemcpyAsync(c->PS_int, c->PS, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
       tpm::launch_passive_scalar_face(c, c->PS);
@@ -845,6 +889,7 @@ int tpm_substep(tpm_ctx *c, int rk_stage) {
   return guarded(c, [&]() -> int {
     if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
     if (rk_stage < 0 || rk_stage > 3) return fail(c, TPM_ERR_ARG, "rk_stage must be 0..3");
+    if (c->ph_done) return fail(c, TPM_ERR_STATE, "a stage is in progress through the phase calls");
     substep(c, rk_stage);
     return TPM_OK;
   });
@@ -853,7 +898,162 @@ int tpm_substep(tpm_ctx *c, int rk_stage) {
 int tpm_end_step(tpm_ctx *c) {
   return guarded(c, [&]() -> int {
     if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
+    if (c->ph_done & ~PH_MEAN)
+      return fail(c, TPM_ERR_STATE, "a stage is in progress through the phase calls");
     end_step(c);
+    return TPM_OK;
+  });
+}
+
+// ---- the reference's grid methods one by one (simulation.cpp:58-91) ----
+// Each call queues the kernels of one method of grid (grid.h:112-136) for
+// RK4 stage rk_stage, on the context's stream, in the reference loop's
+// order; a call out of that order returns TPM_ERR_STATE and queues nothing.
+// The sequence gives the same bits as tpm_substep / tpm_end_step, which
+// queue the same kernels (with independent ones on a second stream).
+
+int tpm_param_update(tpm_ctx *c) {
+  return guarded(c, [&]() -> int {
+    if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
+    if (c->stage_next != 0 || c->ph_done)
+      return fail(c, TPM_ERR_STATE, "PARAM.update belongs at the start of a step");
+    param_update(c);
+    return TPM_OK;
+  });
+}
+
+int tpm_update_rho(tpm_ctx *c, int k) {
+  return guarded(c, [&]() -> int {
+    if (int rc = phase_check(c, k, PH_RHO, 0, "Update_Rho")) return rc;
+    refresh_rui32(c);
+    // the density pass also forms the gas temperature (P0_new/R)/Rho_new that
+    // Update_Particle reads, so P0_new comes first: Update_P0 does not read
+    // what Update_Rho writes (grid.cpp:816-830), so the order of the two is free
+    if (!(c->ph_done & PH_P0)) {
+      tpm::launch_p0_update(c, k);
+      c->ph_done |= PH_P0;
+    }
+    tpm::launch_rho_update(c, k, c->np1_is_base);
+    c->ph_done |= PH_RHO;
+    return TPM_OK;
+  });
+}
+
+int tpm_update_p0(tpm_ctx *c, int k) {
+  return guarded(c, [&]() -> int {
+    if (c->initialized && k == c->stage_next && (c->ph_done & PH_P0) && !c->p0_called) {
+      c->p0_called = true;  // already queued by tpm_update_rho of this stage
+      return TPM_OK;
+    }
+    if (int rc = phase_check(c, k, PH_P0, 0, "Update_P0")) return rc;
+    tpm::launch_p0_update(c, k);
+    c->ph_done |= PH_P0;
+    c->p0_called = true;
+    return TPM_OK;
+  });
+}
+
+int tpm_update_particle(tpm_ctx *c, int k) {
+  return guarded(c, [&]() -> int {
+    if (int rc = phase_check(c, k, PH_PART, PH_P0 | PH_RHO, "Update_Particle")) return rc;
+    const bool nb = c->np1_is_base;
+    tpm::launch_face_velocity(c);  // U = RU_int / Rho_face (grid.cpp:868)
+    tpm::launch_particle_push(c, k, nb);
+    tpm::particle_deposit_momentum(c);
+    tpm::particle_deposit_concentration(c);
+    tpm::particle_heat(c);
+    c->ph_done |= PH_PART;
+    return TPM_OK;
+  });
+}
+
+int tpm_update_passive_scalar(tpm_ctx *c, int k) {
+  return guarded(c, [&]() -> int {
+    if (!c->PS) return fail(c, TPM_ERR_STATE, "solve_for_scalar is off");
+    if (int rc = phase_check(c, k, PH_PS, PH_PART, "Update_Passive_Scalar")) return rc;
+    tpm::launch_passive_scalar(c, k, c->np1_is_base);
+    c->ph_done |= PH_PS;
+    return TPM_OK;
+  });
+}
+
+int tpm_update_ru_wop(tpm_ctx *c, int k) {
+  return guarded(c, [&]() -> int {
+    const unsigned need = PH_PART | (c->PS ? PH_PS : 0u);
+    if (int rc = phase_check(c, k, PH_RUWOP, need, "Update_RU_WOP")) return rc;
+    tpm::launch_rhs_momentum(c, k, c->np1_is_base);
+    c->ph_done |= PH_RUWOP;
+    return TPM_OK;
+  });
+}
+
+int tpm_compute_div_u_new(tpm_ctx *c, int k) {
+  return guarded(c, [&]() -> int {
+    if (int rc = phase_check(c, k, PH_DIV, PH_RUWOP, "Compute_Div_U_new")) return rc;
+    // the divergence constraint (k/Cp) Del2(1/Rho_new) - R/(Cp P0_new Vcell) Q
+    // (grid.cpp:832-839) is formed by the Poisson right-hand-side pass, which
+    // reads Rho_new and Q once for both; it runs at tpm_compute_rhs_pois
+    c->ph_done |= PH_DIV;
+    return TPM_OK;
+  });
+}
+
+int tpm_compute_rhs_pois(tpm_ctx *c, int k) {
+  return guarded(c, [&]() -> int {
+    if (int rc = phase_check(c, k, PH_RHSP, PH_DIV, "Compute_RHS_Pois")) return rc;
+    tpm::launch_face_coeff(c);  // mixed path: C = 1/Rho_face pairs (grid.cpp:852)
+    tpm::launch_poisson_rhs(c, k, c->store_div || c->p.precision == TPM_PREC_MIXED);
+    c->ph_done |= PH_RHSP;
+    return TPM_OK;
+  });
+}
+
+int tpm_solve_poisson(tpm_ctx *c, int k) {
+  return guarded(c, [&]() -> int {
+    if (int rc = phase_check(c, k, PH_SOLVE, PH_RHSP, "Solve_Poisson")) return rc;
+    poisson_loop(c, c->Iteration, c->p.epsilon);
+    c->ph_done |= PH_SOLVE;
+    return TPM_OK;
+  });
+}
+
+int tpm_update_ru_wp(tpm_ctx *c, int k) {
+  return guarded(c, [&]() -> int {
+    if (int rc = phase_check(c, k, PH_RUWP, PH_SOLVE, "Update_RU_WP")) return rc;
+    tpm::launch_project(c, k);
+    if (c->p.precision == TPM_PREC_MIXED && (k == 3 || c->div_every_stage))
+      tpm::launch_div_residual(c, k);
+    c->ph_done |= PH_RUWP;
+    return TPM_OK;
+  });
+}
+
+int tpm_time_advance_rk4(tpm_ctx *c, int k) {
+  return guarded(c, [&]() -> int {
+    if (int rc = phase_check(c, k, 0, PH_RUWP, "TimeAdvance_RK4")) return rc;
+    swap_stage(c);  // next stage, no phase done
+    c->np1_is_base = false;
+    return TPM_OK;
+  });
+}
+
+int tpm_make_mean_u0(tpm_ctx *c) {
+  return guarded(c, [&]() -> int {
+    if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
+    if (c->stage_next != 4 || (c->ph_done & PH_MEAN))
+      return fail(c, TPM_ERR_STATE, "RU_np1.make_mean_U0 belongs after the fourth stage");
+    tpm::launch_mean_reset(c);
+    c->ph_done |= PH_MEAN;
+    return TPM_OK;
+  });
+}
+
+int tpm_time_advance(tpm_ctx *c) {
+  return guarded(c, [&]() -> int {
+    if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
+    if (c->stage_next != 4)
+      return fail(c, TPM_ERR_STATE, "TimeAdvance belongs after the fourth stage");
+    time_advance(c);
     return TPM_OK;
   });
 }
@@ -861,6 +1061,8 @@ int tpm_end_step(tpm_ctx *c) {
 int tpm_step(tpm_ctx *c) {
   return guarded(c, [&]() -> int {
     if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
+    if (c->stage_next || c->ph_done)
+      return fail(c, TPM_ERR_STATE, "a step is in progress through the substep or phase calls");
     tpm::step_any(c);
     return TPM_OK;
   });
@@ -869,6 +1071,8 @@ int tpm_step(tpm_ctx *c) {
 int tpm_run(tpm_ctx *c, int nsteps) {
   return guarded(c, [&]() -> int {
     if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
+    if (c->stage_next || c->ph_done)
+      return fail(c, TPM_ERR_STATE, "a step is in progress through the substep or phase calls");
     for (int k = 0; k < nsteps; ++k) tpm::step_any(c);
     return TPM_OK;
   });
@@ -897,8 +1101,8 @@ int tpm_poisson_solve(tpm_ctx *c, const double *C3, double *P, const double *RHS
     poisson_loop(c, max_iterations, epsilon);
     TPM_CUDA_TRY(cudaMemcpyAsync(P, c->P, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
     pull_scalars(c);
-    if (iterations_out) *iterations_out = c->last_it;
-    if (error_out) *error_out = c->hsc->err;
+    if (iterations_out) *iterations_out = c->hsc->it;  // the iterations the device ran
+    if (error_out) *error_out = c->hsc->err;             // 100 when none ran
     return TPM_OK;
   });
 }

@@ -162,6 +162,39 @@ __device__ __forceinline__ void ff_int_frac(double u, int &ip, float &fr, bool &
   up = half;
 }
 
+// u = ip + fr with ip = trunc(u) and the fraction fr = u - ip as a
+// normalised pair, by integer operations only.  The fraction's bits split at
+// bit 29 into two integers that convert to floats: the high part exactly, the
+// low part rounded to 24 bits, so |fr - (u - ip)| <= 2^(e - 48) for
+// 2^e <= |u| < 2^(e + 1) (2^-41 for |u| < 256), and exactly ff_from_double(u)
+// for |u| < 1.  For |u| < 2^31; beyond, ip saturates and fr is 0.
+__device__ __forceinline__ void ff_int_frac2(double u, int &ip, float2 &fr) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(u);
+  const bool neg = (b >> 63) != 0;
+  const int e = (int)((b >> 52) & 0x7ffu) - 1023;
+  const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const int sh = 52 - (e < 0 ? 0 : (e > 30 ? 30 : e));  // fraction = fb 2^-sh
+  const unsigned long long fb = m & ((1ull << sh) - 1ull);
+  // fb = fh 2^29 + fl: fh < 2^23 converts exactly, and fh 2^(29 - sh) > fl 2^-sh
+  // whenever fh > 0, so FastTwoSum normalises the pair
+  const float hi = __uint2float_rn((unsigned int)(fb >> 29)) *
+                   __uint_as_float((unsigned int)(127 + 29 - sh) << 23);
+  const float lo = __uint2float_rn((unsigned int)(fb & 0x1fffffffull)) *
+                   __uint_as_float((unsigned int)(127 - sh) << 23);
+  float2 f = ff_fast_two_sum(hi, lo);
+  int ia = (int)(m >> sh);
+  if (e < 0) {  // |u| < 1: no integer part, the fraction is |u|
+    ia = 0;
+    f = ff_from_double(__longlong_as_double((long long)(b & 0x7fffffffffffffffull)));
+  }
+  if (e > 30) {
+    ia = 0x7fffffff;
+    f = make_float2(0.f, 0.f);
+  }
+  ip = neg ? -ia : ia;
+  fr = neg ? make_float2(-f.x, -f.y) : f;
+}
+
 // hi + lo as a double (two exact conversions and one FP64 addition)
 __device__ __forceinline__ double ff_to_double(float2 a) { return ff_f2d(a.x) + ff_f2d(a.y); }
 

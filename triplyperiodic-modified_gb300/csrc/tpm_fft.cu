@@ -20,6 +20,7 @@
 // residual and the update keep the reference's operation order.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "tpm_internal.cuh"
@@ -747,7 +748,10 @@ __global__ void k_finish_max(const double *__restrict__ partials, int nparts, De
     s->err = m;
     s->it += 1;
     s->it_sum += 1;
-    const bool more = !(eps_ctl > 0 && !(m > eps_ctl));
+    // poisson.cpp:397: while (i < Iteration && error > epsilon) - for every
+    // epsilon, so with epsilon = 0 a solve stops once max|dp| is exactly 0
+    // (a NaN error stops it too); callers that never stop pass a negative one
+    const bool more = m > eps_ctl;
     if (loop_max > 0)
       cudaGraphSetConditional(loop, (s->it < loop_max && more) ? 1u : 0u);
     else if (!more)
@@ -973,6 +977,16 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
 
 // the following solves of the step start from this one's P: warm
 __global__ void k_mark_warm(DevScalars *s) { s->warm = 1; }
+
+__global__ void k_loop_begin(DevScalars *s) {
+  s->skip = 0;
+  s->it = 0;
+  s->err = 100;
+}
+
+void poisson_loop_begin(tpm_ctx *c) {
+  TPM_LAUNCH(c, "poisson_begin", k_loop_begin, 1, 1, 0, c->dsc);
+}
 
 void refine_finish(tpm_ctx *c) {
   TPM_LAUNCH(c, "refine_finish", k_refine_finish, cell_blocks(c->g), 256, 0, c->g, c->dP,
@@ -1226,14 +1240,15 @@ void spectrum_kernels_setup() {
 // Allocation-free Poisson solve (tpm_poisson_solve_noalloc, include/tpm.h).
 //
 // Some callers cannot allocate device memory at all: a plug-in that only
-// receives buffers from its host application, code running while a stream is
-// being captured into a CUDA graph (cudaMalloc is illegal there), or a
-// runtime with its own pool that forbids side allocations.  This entry point
-// runs the same kernels as tpm_poisson_solve, but every byte of scratch it
-// needs (spectrum, centre coefficients, partial maxima, twiddle and
-// wave-number tables, device scalars) lives in the fixed array below, which
-// each GPU that loads the library holds until the process exits.  The caller
-// passes device pointers for the inputs and the output only.
+// receives buffers from its host application, or a runtime whose memory pool
+// owns the device and forbids side allocations.  This entry point runs the
+// same kernels as tpm_poisson_solve, but every byte of scratch it needs
+// (spectrum, centre coefficients, partial maxima, twiddle and wave-number
+// tables, device scalars) lives in the fixed array below, which each GPU that
+// loads the library holds until the process exits.  The caller passes device
+// pointers for the inputs and the output only.  The call synchronises its
+// stream (the small tables are copied from host staging), so it cannot run
+// while that stream is being captured into a CUDA graph; it refuses to.
 // ===========================================================================
 namespace tpm {
 namespace {
@@ -1243,10 +1258,13 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kStaticScratchBytes];
 
-// device address of g_noalloc_scratch, looked up once per device
+// Host state shared by every calling thread, guarded by g_noalloc_mutex: the
+// device address of g_noalloc_scratch per device (looked up once, with that
+// device current) and the staging arrays of the small tables (fixed size: no
+// host allocation either).  The lock is held from the first write of the
+// staging arrays until the stream has finished copying them.
+std::mutex g_noalloc_mutex;
 void *g_noalloc_ptr[kMaxDevices] = {};
-
-// host staging for the small tables (fixed size: no host allocation either)
 double2 g_tab_host[4 * 2048 + 8];
 double g_mwn_host[2048 + 2048 + 2048 + 8];
 
@@ -1264,6 +1282,25 @@ __global__ void k_center_coeff_noalloc(Grid g, const double *__restrict__ Cf, do
                            (Cf[2 * g.n + c] + Cf[2 * g.n + czp]) * 0.5);
     cc[c] = -1. / m;
   }
+}
+
+// device address of this device's scratch array, resolved on first use
+int noalloc_scratch(int dev, unsigned char **out) {
+  if (!g_noalloc_ptr[dev]) {
+    // the host-side name g_noalloc_scratch is only a stand-in: the kernels
+    // need the address cudaGetSymbolAddress gives for the current device
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return TPM_ERR_CUDA;
+    int smem64 = 2 * kFftSmemPoints * (int)sizeof(double2);
+    if (cudaFuncSetAttribute(k_xfwd_resid<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_y<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64) != cudaSuccess ||
+        cudaFuncSetAttribute(k_fft_z_solve<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64) != cudaSuccess ||
+        cudaFuncSetAttribute(k_xinv_update<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64) != cudaSuccess)
+      return TPM_ERR_CUDA;
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
+  return TPM_OK;
 }
 
 }  // namespace
@@ -1309,32 +1346,12 @@ extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, doub
   if (need > kStaticScratchBytes) return TPM_ERR_ARG;  // grid too large for the fixed scratch
 
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) return TPM_ERR_CUDA;
+  if (cap != cudaStreamCaptureStatusNone) return TPM_ERR_STATE;  // it synchronises the stream
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return TPM_ERR_CUDA;
-  if (!g_noalloc_ptr[dev]) {
-    // once per device, with that device current: resolve the array's device
-    // address (the host-side name is only a stand-in) and allow the FFT
-    // kernels their dynamic shared memory
-    void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return TPM_ERR_CUDA;
-    int smem64 = 2 * kFftSmemPoints * (int)sizeof(double2);
-    if (cudaFuncSetAttribute(k_xfwd_resid<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64) != cudaSuccess ||
-        cudaFuncSetAttribute(k_fft_y<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64) != cudaSuccess ||
-        cudaFuncSetAttribute(k_fft_z_solve<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64) != cudaSuccess ||
-        cudaFuncSetAttribute(k_xinv_update<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64) != cudaSuccess)
-      return TPM_ERR_CUDA;
-    g_noalloc_ptr[dev] = p;
-  }
-  unsigned char *base = static_cast<unsigned char *>(g_noalloc_ptr[dev]);
-  DevScalars *dsc = reinterpret_cast<DevScalars *>(base + o_sc);
-  double2 *spec = reinterpret_cast<double2 *>(base + o_spec);
-  double *cc = reinterpret_cast<double *>(base + o_cc);
-  double *errp = reinterpret_cast<double *>(base + o_err);
-  double2 *tab = reinterpret_cast<double2 *>(base + o_tab);
-  double *mwn = reinterpret_cast<double *>(base + o_mwn);
 
-  // plans and tables (twiddles exp(-2 pi i m/n); wave numbers as in
-  // poisson.cpp:433-447)
   FftPlan fx, fy, fz;
   try {
     factorize(Nx / 2, fx);
@@ -1343,49 +1360,72 @@ extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, doub
   } catch (const std::string &) {
     return TPM_ERR_ARG;
   }
-  int off = 0;
-  auto put_tw = [&](int n) {
-    for (int m = 0; m < n; ++m) {
-      double a = 2.0 * 3.14159265358979323846 * (double)m / (double)n;
-      g_tab_host[off + m] = make_double2(cos(a), -sin(a));
-    }
-    int at0 = off;
-    off += n;
-    return at0;
-  };
-  fx.tw64 = tab + put_tw(Nx / 2);
-  fy.tw64 = tab + put_tw(Ny);
-  fz.tw64 = tab + put_tw(Nz);
-  const double2 *r2c = tab + put_tw(Nx);
-  fx.tw32 = fy.tw32 = fz.tw32 = nullptr;
-  auto put_mwn = [](int n, double L, double d, double *t, int count) {
-    double TWO_PI(2 * 3.141592653589793);
-    double two_pi_over_L = TWO_PI / L;
-    double d2 = 2. / (d * d);
-    for (int i = 0; i < count; ++i) {
-      double kk = ((i < n / 2) ? i : i - n) * two_pi_over_L;
-      t[i] = (d2) * (1 - cos(kk * d));
-    }
-  };
-  put_mwn(Nx, Lx, g.dx, g_mwn_host, g.nxh);
-  put_mwn(Ny, Ly, g.dy, g_mwn_host + g.nxh, Ny);
-  put_mwn(Nz, Lz, g.dz, g_mwn_host + g.nxh + Ny, Nz);
+  unsigned char *base = nullptr;
+  DevScalars *dsc;
+  double *cc, *errp, *mwn;
+  double2 *spec, *tab;
+  const double2 *r2c;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    const int rc = noalloc_scratch(dev, &base);
+    if (rc != TPM_OK) return rc;
+    dsc = reinterpret_cast<DevScalars *>(base + o_sc);
+    spec = reinterpret_cast<double2 *>(base + o_spec);
+    cc = reinterpret_cast<double *>(base + o_cc);
+    errp = reinterpret_cast<double *>(base + o_err);
+    tab = reinterpret_cast<double2 *>(base + o_tab);
+    mwn = reinterpret_cast<double *>(base + o_mwn);
+    // plans and tables (twiddles exp(-2 pi i m/n); wave numbers as in
+    // poisson.cpp:433-447)
+    int off = 0;
+    auto put_tw = [&](int n) {
+      for (int m = 0; m < n; ++m) {
+        double a = 2.0 * 3.14159265358979323846 * (double)m / (double)n;
+        g_tab_host[off + m] = make_double2(cos(a), -sin(a));
+      }
+      int at0 = off;
+      off += n;
+      return at0;
+    };
+    fx.tw64 = tab + put_tw(Nx / 2);
+    fy.tw64 = tab + put_tw(Ny);
+    fz.tw64 = tab + put_tw(Nz);
+    r2c = tab + put_tw(Nx);
+    fx.tw32 = fy.tw32 = fz.tw32 = nullptr;
+    auto put_mwn = [](int n, double L, double d, double *t, int count) {
+      double TWO_PI(2 * 3.141592653589793);
+      double two_pi_over_L = TWO_PI / L;
+      double d2 = 2. / (d * d);
+      for (int i = 0; i < count; ++i) {
+        double kk = ((i < n / 2) ? i : i - n) * two_pi_over_L;
+        t[i] = (d2) * (1 - cos(kk * d));
+      }
+    };
+    put_mwn(Nx, Lx, g.dx, g_mwn_host, g.nxh);
+    put_mwn(Ny, Ly, g.dy, g_mwn_host + g.nxh, Ny);
+    put_mwn(Nz, Lz, g.dz, g_mwn_host + g.nxh + Ny, Nz);
+    if (cudaMemcpyAsync(tab, g_tab_host, sizeof(double2) * ntab, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(mwn, g_mwn_host, sizeof(double) * (g.nxh + Ny + Nz), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemsetAsync(dsc, 0, sizeof(DevScalars), st) != cudaSuccess)  // mean_rhs = 0: RHS used as given
+      return TPM_ERR_CUDA;
+    // the copies read the staging arrays: finish them before another call
+    // may rewrite them
+    if (cudaStreamSynchronize(st) != cudaSuccess) return TPM_ERR_CUDA;
+  }
   const double *ax = mwn, *ay = mwn + g.nxh, *az = mwn + g.nxh + Ny;
-  if (cudaMemcpyAsync(tab, g_tab_host, sizeof(double2) * ntab, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-      cudaMemcpyAsync(mwn, g_mwn_host, sizeof(double) * (g.nxh + Ny + Nz), cudaMemcpyHostToDevice, st) != cudaSuccess ||
-      cudaMemsetAsync(dsc, 0, sizeof(DevScalars), st) != cudaSuccess)  // mean_rhs = 0: RHS used as given
-    return TPM_ERR_CUDA;
-  // table copies come from static host staging: finish them before a later
-  // call may rewrite it
-  if (cudaStreamSynchronize(st) != cudaSuccess) return TPM_ERR_CUDA;
 
   int cb = (int)((g.n + 255) / 256);
   if (cb > kRedBlocks) cb = kRedBlocks;
   k_center_coeff_noalloc<<<cb, 256, 0, st>>>(g, C3, cc);
-  int it = 0;
-  double error = 100, host_err = 0;
-  const bool need_err = epsilon > 0;
-  while ((it < max_iterations) && (error > epsilon)) {
+  k_loop_begin<<<1, 1, 0, st>>>(dsc);  // skip = it = 0, err = 100
+  const int *skip = &dsc->skip;
+  // poisson.cpp:395-410: while (i < Iteration && error > epsilon).  The device
+  // applies the test after every iteration and turns the remaining ones into
+  // no-ops once it fails (with epsilon <= 0: when max|dp| is exactly 0); with
+  // epsilon > 0 the host also reads max|dp| to stop launching.
+  int launched = 0;
+  double error = 100;
+  while ((launched < max_iterations) && (error > epsilon)) {
     {
       size_t smem = 2 * (size_t)npx * fx.n * sizeof(double2);
       k_xfwd_resid<double2><<<xblocks, kFftThreads, smem, st>>>(g, fx, r2c, P, C3, cc, RHS, dsc, spec, npx);
@@ -1394,45 +1434,45 @@ extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, doub
       int npen = pens_for(fy.n);
       int blocks = Nz * ((g.nxh + npen - 1) / npen);
       size_t smem = 2 * (size_t)npen * fy.n * sizeof(double2);
-      k_fft_y<double2><<<blocks, kFftThreads, smem, st>>>(g, fy, spec, npen, -1, nullptr);
+      k_fft_y<double2><<<blocks, kFftThreads, smem, st>>>(g, fy, spec, npen, -1, skip);
     }
     {
       int npen = pens_for(fz.n);
       int blocks = Ny * ((g.nxh + npen - 1) / npen);
       size_t smem = 2 * (size_t)npen * fz.n * sizeof(double2);
       k_fft_z_solve<double2><<<blocks, kFftThreads, smem, st>>>(g, fz, spec, ax, ay, az, nullptr, npen,
-                                                                 nullptr);
+                                                                 skip);
     }
     {
       int npen = pens_for(fy.n);
       int blocks = Nz * ((g.nxh + npen - 1) / npen);
       size_t smem = 2 * (size_t)npen * fy.n * sizeof(double2);
-      k_fft_y<double2><<<blocks, kFftThreads, smem, st>>>(g, fy, spec, npen, +1, nullptr);
+      k_fft_y<double2><<<blocks, kFftThreads, smem, st>>>(g, fy, spec, npen, +1, skip);
     }
     {
       size_t smem = 2 * (size_t)npx * fx.n * sizeof(double2);
       k_xinv_update<double2><<<xblocks, kFftThreads, smem, st>>>(g, fx, r2c, spec, P, errp, npx,
-                                                                 nullptr, nullptr, nullptr, nullptr,
+                                                                 skip, nullptr, nullptr, nullptr,
                                                                  1.0 / (double)((long long)Nx * Ny * Nz),
                                                                  nullptr);
-      k_finish_max<<<1, 256, 0, st>>>(errp, xblocks, dsc, 0.0, cudaGraphConditionalHandle{}, 0,
+      k_finish_max<<<1, 256, 0, st>>>(errp, xblocks, dsc, epsilon, cudaGraphConditionalHandle{}, 0,
                                       nullptr);
     }
     if (cudaGetLastError() != cudaSuccess) return TPM_ERR_CUDA;
-    it++;
-    if (need_err) {
-      if (cudaMemcpyAsync(&host_err, &dsc->err, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+    launched++;
+    if (epsilon > 0) {
+      if (cudaMemcpyAsync(&error, &dsc->err, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
           cudaStreamSynchronize(st) != cudaSuccess)
         return TPM_ERR_CUDA;
-      error = host_err;
     }
   }
-  if (!need_err || error_out) {
-    if (cudaMemcpyAsync(&host_err, &dsc->err, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return TPM_ERR_CUDA;
-  }
+  int it = 0;
+  double err = 0;
+  if (cudaMemcpyAsync(&it, &dsc->it, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaMemcpyAsync(&err, &dsc->err, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return TPM_ERR_CUDA;
   if (iterations_out) *iterations_out = it;
-  if (error_out) *error_out = host_err;
+  if (error_out) *error_out = err;
   return TPM_OK;
 }

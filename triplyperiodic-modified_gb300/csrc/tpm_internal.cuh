@@ -173,6 +173,12 @@ struct tpm_ctx {
   bool initialized = false;
   bool np1_is_base = true;  // np1 copies equal base (after initialize / end of step)
   bool stepped = false;     // a full step has run since initialize / resume
+  // the reference-granularity phase entry points (tpm_update_rho ...): the
+  // RK4 stage the next phase belongs to (0..3; 4 once the fourth stage has
+  // advanced, until the end of the step) and the phases done in it
+  int stage_next = 0;
+  unsigned ph_done = 0;
+  bool p0_called = false;  // tpm_update_p0 was called in this stage
   int last_it = 0, total_it = 0;
   double last_err = 0;
 
@@ -323,7 +329,12 @@ struct LoopCtl {
 // one Richardson iteration; returns nothing (error lands in dsc->err).  With
 // eps_ctl > 0 and no loop control the iteration sets dsc->skip once
 // max|dp| <= eps_ctl, and every kernel of a later iteration returns at once.
-void poisson_iteration(tpm_ctx *c, double eps_ctl = 0.0, const LoopCtl *loop = nullptr);
+// One Richardson iteration; the device stops the solve (skip, or the captured
+// loop's condition) once max|dp| <= eps_ctl (negative: never).
+void poisson_iteration(tpm_ctx *c, double eps_ctl = -1.0, const LoopCtl *loop = nullptr);
+// skip = it = 0 and err = 100 (poisson.cpp:395: the error a solve reports
+// when it runs no iteration) at the start of a solve
+void poisson_loop_begin(tpm_ctx *c);
 // mixed Richardson loop: P += dP after the loop (a no-op below two iterations)
 void refine_finish(tpm_ctx *c);
 // z = S (-Lap_h)^-1 S r, S = diag(sc) (FFT passes of the Poisson solve), with

@@ -54,6 +54,7 @@ struct PState {
 // TP: type of the momentum-deposit payload.
 template <typename TU, typename TP>
 __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__restrict__ U,
+                       const double *__restrict__ RUi, const double *__restrict__ Rhoi,
                        const double *__restrict__ Tgas, double *__restrict__ rhs_t,
                        const double *__restrict__ tau, int32_t *__restrict__ key_t,
                        TP *__restrict__ pay_t, int32_t *__restrict__ key_r,
@@ -66,14 +67,13 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     // ---- gas2part_velocity at x_int (particle.cpp:340-360) ----
     int tx, ty, tz;
     double xl = 0, yl = 0, zl = 0;     // FP64 path: fractions in FP64
-    float xf_i = 0, yf_i = 0, zf_i = 0;  // mixed path: the same fractions truncated to FP32
+    float2 fx, fy, fz;                 // mixed path: the same fractions as pairs
     if constexpr (kMixed) {
       // trunc(x/d) and its fraction from the bits of the FP64 product (the
       // same cell as the FP64 route, no FP64-pipe conversions)
-      bool h;
-      ff_int_frac(xi * g.idx, tx, xf_i, h);
-      ff_int_frac(yi * g.idy, ty, yf_i, h);
-      ff_int_frac(zi * g.idz, tz, zf_i, h);
+      ff_int_frac2(xi * g.idx, tx, fx);
+      ff_int_frac2(yi * g.idy, ty, fy);
+      ff_int_frac2(zi * g.idz, tz, fz);
     } else {
       tx = (int)(xi * g.idx);
       ty = (int)(yi * g.idy);
@@ -85,20 +85,37 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     const int i0 = wrap_any(tx, g.nx), j0 = wrap_any(ty, g.ny), k0 = wrap_any(tz, g.nz);
     const long long c0 = at(g, i0, j0, k0);
     double ug, vg, wg;
-    if (sizeof(TU) == sizeof(double)) {
+    if constexpr (!kMixed) {
       ug = xl * (double)U[at(g, wrap_p(i0, g.nx), j0, k0)] + (1 - xl) * (double)U[c0];
       vg = yl * (double)U[g.n + at(g, i0, wrap_p(j0, g.ny), k0)] + (1 - yl) * (double)U[g.n + c0];
       wg = zl * (double)U[2 * g.n + at(g, i0, j0, wrap_p(k0, g.nz))] +
            (1 - zl) * (double)U[2 * g.n + c0];
-    } else {  // FP32 interpolation of the FP32 face velocity (mixed path); the
-      // FP64<->FP32 conversions by integer operations (the conversion
-      // instructions issue on the FP64 pipe)
-      const float xf = xf_i, yf = yf_i, zf = zf_i;
-      ug = ff_f2d(xf * (float)U[at(g, wrap_p(i0, g.nx), j0, k0)] + (1 - xf) * (float)U[c0]);
-      vg = ff_f2d(yf * (float)U[g.n + at(g, i0, wrap_p(j0, g.ny), k0)] +
-                  (1 - yf) * (float)U[g.n + c0]);
-      wg = ff_f2d(zf * (float)U[2 * g.n + at(g, i0, j0, wrap_p(k0, g.nz))] +
-                  (1 - zf) * (float)U[2 * g.n + c0]);
+    } else {
+      // mixed path: the face velocity RU_int / I_C2F(Rho_int) at the particle's
+      // two faces of each component, and the interpolation between them, in
+      // float-float pairs from the FP64 state (within ~2^-44 of the FP64
+      // route).  An FP32 face velocity would put ~1e-7 into every particle's
+      // gas velocity, and the reference's interpolation is nearest-cell across
+      // the transverse faces (particle.cpp:340-360): a particle whose position
+      // then drifts across a face takes another cell's velocity.
+      const long long cxp = at(g, wrap_p(i0, g.nx), j0, k0), cxm = at(g, wrap_m(i0, g.nx), j0, k0);
+      const long long cyp = at(g, i0, wrap_p(j0, g.ny), k0), cym = at(g, i0, wrap_m(j0, g.ny), k0);
+      const long long czp = at(g, i0, j0, wrap_p(k0, g.nz)), czm = at(g, i0, j0, wrap_m(k0, g.nz));
+      const float2 r0 = ff_from_double(Rhoi[c0]);
+      // RU / ((Rho_a + Rho_b) / 2) = 2 RU / (Rho_a + Rho_b)
+      auto uface = [&](double ru, const float2 &ra, double rb) {
+        const float2 q = ff_mul(ff_from_double(ru), ff_rcp(ff_add(ra, ff_from_double(rb))));
+        return ff_norm(make_float2(2.f * q.x, 2.f * q.y));
+      };
+      auto lerp = [&](const float2 &f, const float2 &u0, const float2 &u1) {
+        return ff_to_double(ff_add(u0, ff_mul(f, ff_sub(u1, u0))));
+      };
+      const float2 rxp = ff_from_double(Rhoi[cxp]), ryp = ff_from_double(Rhoi[cyp]),
+                   rzp = ff_from_double(Rhoi[czp]);
+      ug = lerp(fx, uface(RUi[c0], r0, Rhoi[cxm]), uface(RUi[cxp], rxp, Rhoi[c0]));
+      vg = lerp(fy, uface(RUi[g.n + c0], r0, Rhoi[cym]), uface(RUi[g.n + cyp], ryp, Rhoi[c0]));
+      wg = lerp(fz, uface(RUi[2 * g.n + c0], r0, Rhoi[czm]),
+                uface(RUi[2 * g.n + czp], rzp, Rhoi[c0]));
     }
     // ---- update_position (particle.cpp:314-338) ----
     // (the mixed path, TU = float, accumulates with FMAs; the FP64 path keeps
@@ -135,7 +152,7 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     if (a.twc) {
       key_t[p] = (int32_t)c0;
       if (kFma) {  // FP32 payload (mixed path): FP32 products of truncated copies
-        const float xf = xf_i, yf = yf_i, zf = zf_i;
+        const float xf = fx.x, yf = fy.x, zf = fz.x;
         const float r0 = ff_hi(rhs[0]), r1 = ff_hi(rhs[1]), r2 = ff_hi(rhs[2]);
         pay_t[0 * np + p] = (TP)((1 - xf) * r0);
         pay_t[1 * np + p] = (TP)(xf * r0);
@@ -895,12 +912,13 @@ void launch_particle_push(tpm_ctx *c, int s, bool np1_in_base) {
   a.has_tau = c->tau != nullptr;
   if (c->p.precision == TPM_PREC_MIXED)
     TPM_LAUNCH(c, "particle_push", (k_push<float, float>), pblocks(c->np), kThreads, 0, c->g,
-               pstate(c, np1_in_base), a, c->np, c->U32, c->Tgas, c->rhs_t, c->tau, c->key_t,
+               pstate(c, np1_in_base), a, c->np, static_cast<const float *>(nullptr), c->RU_int,
+               c->Rho_int, c->Tgas, c->rhs_t, c->tau, c->key_t,
                reinterpret_cast<float *>(c->pay_t), c->key_r,
                reinterpret_cast<float *>(c->pay_r));
   else
     TPM_LAUNCH(c, "particle_push", (k_push<double, double>), pblocks(c->np), kThreads, 0, c->g,
-               pstate(c, np1_in_base), a, c->np, c->U, c->Tgas, c->rhs_t, c->tau, c->key_t,
+               pstate(c, np1_in_base), a, c->np, c->U, nullptr, nullptr, c->Tgas, c->rhs_t, c->tau, c->key_t,
                c->pay_t, c->key_r, c->pay_r);
 }
 

@@ -61,6 +61,19 @@ SIGNATURES = {
     "tpm_initialize": (_i, [_vp]),
     "tpm_substep": (_i, [_vp, _i]),
     "tpm_end_step": (_i, [_vp]),
+    "tpm_param_update": (_i, [_vp]),
+    "tpm_update_rho": (_i, [_vp, _i]),
+    "tpm_update_p0": (_i, [_vp, _i]),
+    "tpm_update_particle": (_i, [_vp, _i]),
+    "tpm_update_passive_scalar": (_i, [_vp, _i]),
+    "tpm_update_ru_wop": (_i, [_vp, _i]),
+    "tpm_compute_div_u_new": (_i, [_vp, _i]),
+    "tpm_compute_rhs_pois": (_i, [_vp, _i]),
+    "tpm_solve_poisson": (_i, [_vp, _i]),
+    "tpm_update_ru_wp": (_i, [_vp, _i]),
+    "tpm_time_advance_rk4": (_i, [_vp, _i]),
+    "tpm_make_mean_u0": (_i, [_vp]),
+    "tpm_time_advance": (_i, [_vp]),
     "tpm_step": (_i, [_vp]),
     "tpm_run": (_i, [_vp, _i]),
     "tpm_sync": (_i, [_vp]),
@@ -394,23 +407,72 @@ class Context:
 class Grid:
     """The reference grid's time-stepping surface (grid.h:112-136) on the GPU.
 
+    The methods of the reference's loop (simulation.cpp:58-91) one by one -
+    ``param_update``, ``Update_Rho``, ``Update_P0``, ``Update_Particle``,
+    ``Update_Passive_Scalar``, ``Update_RU_WOP``, ``Compute_Div_U_new``,
+    ``Compute_RHS_Pois``, ``Solve_Poisson``, ``Update_RU_WP``,
+    ``TimeAdvance_RK4`` for stage ``RK4_count``, then ``RU_np1_make_mean_U0``
+    and ``TimeAdvance`` - or whole pieces of it:
     ``Initialize``        -> grid::Initialize tail (grid.cpp:461-484)
     ``substep(k)``        -> Update_Rho ... TimeAdvance_RK4 for RK4_count = k
-    ``TimeAdvance``       -> RU_np1.make_mean_U0 + grid::TimeAdvance
-    ``step``              -> PARAM.update + 4 substeps + TimeAdvance
+    ``end_step``          -> RU_np1.make_mean_U0 + grid::TimeAdvance
+    ``step``              -> PARAM.update + 4 substeps + end of step
     """
 
     def __init__(self, p: Params, state: inputs.State):
         self.ctx = Context(p, state.npart)
         self.ctx.load(state)
+        self.RK4_count = 0
 
     def Initialize(self):
         self.ctx.initialize()
 
+    def _m(self, fn, *args):
+        self.ctx._check(fn(self.ctx.h, *args))
+
+    def param_update(self):
+        self._m(self.ctx.L.tpm_param_update)
+
+    def Update_Rho(self):
+        self._m(self.ctx.L.tpm_update_rho, self.RK4_count)
+
+    def Update_P0(self):
+        self._m(self.ctx.L.tpm_update_p0, self.RK4_count)
+
+    def Update_Particle(self):
+        self._m(self.ctx.L.tpm_update_particle, self.RK4_count)
+
+    def Update_Passive_Scalar(self):
+        self._m(self.ctx.L.tpm_update_passive_scalar, self.RK4_count)
+
+    def Update_RU_WOP(self):
+        self._m(self.ctx.L.tpm_update_ru_wop, self.RK4_count)
+
+    def Compute_Div_U_new(self):
+        self._m(self.ctx.L.tpm_compute_div_u_new, self.RK4_count)
+
+    def Compute_RHS_Pois(self):
+        self._m(self.ctx.L.tpm_compute_rhs_pois, self.RK4_count)
+
+    def Solve_Poisson(self):
+        self._m(self.ctx.L.tpm_solve_poisson, self.RK4_count)
+
+    def Update_RU_WP(self):
+        self._m(self.ctx.L.tpm_update_ru_wp, self.RK4_count)
+
+    def TimeAdvance_RK4(self):
+        self._m(self.ctx.L.tpm_time_advance_rk4, self.RK4_count)
+
+    def RU_np1_make_mean_U0(self):
+        self._m(self.ctx.L.tpm_make_mean_u0)
+
+    def TimeAdvance(self):
+        self._m(self.ctx.L.tpm_time_advance)
+
     def substep(self, rk4_count):
         self.ctx.substep(rk4_count)
 
-    def TimeAdvance(self):
+    def end_step(self):
         self.ctx.end_step()
 
     def step(self):
