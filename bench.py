@@ -19,6 +19,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -33,37 +34,63 @@ UNIT = "Mcell-steps/s"
 WORKLOAD = "box256_p8e6_heated"
 FALLBACK_HBM_GBS = 6800.0
 
-# Algorithmic bytes per launch of each kernel: (bytes per cell, bytes per
-# particle) for FP64 storage; the derivation is tabulated in the design doc.
-# `value` is the headline (mixed-precision) path; the FP64 path is reported
-# beside it under "fp64".
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of a
-# kernel on a workload, the mean over the launches of one ncu capture of this
-# bench's own command (the profiles/ summary of that kernel gives the command)
+# kernel on a workload, the mean over the launches of one single-pass ncu
+# capture of every kernel of this bench's two profiled steps (the command is
+# in the summary of the capture)
 NCU_TRAFFIC = {
-    # profiles/k_xfwd_resid_refine_mixed_box256_box128.md (mean of six launches)
-    ("box256_p8e6_heated", True, "fft_x_fwd_resid"): 8.74e8,
-    # profiles/k_push_mixed_box256_box128.md
-    ("box256_p8e6_heated", True, "particle_push"): 3.00e9,
-    # profiles/k_rhs_momentum_zm_k_poisson_rhs_zm_mixed_box256_box128.md
-    ("box256_p8e6_heated", True, "rhs_momentum"): 2.01e9,
-    ("box256_p8e6_heated", True, "poisson_rhs"): 1.42e9,
+    ("box256_p8e6_heated", True, "fft_x_fwd_resid"): 8.63e8,
+    ("box256_p8e6_heated", True, "particle_push"): 3.546e9,
+    ("box256_p8e6_heated", True, "rhs_momentum"): 2.006e9,
+    ("box256_p8e6_heated", True, "poisson_rhs"): 1.423e9,
+    ("box256_p8e6_heated", False, "rhs_momentum"): 2.595e9,
+    ("box256_p8e6_heated", False, "fft_x_fwd_resid"): 9.36e8,
 }
 
+# FP64 path: FP64 operations per cell per launch of a kernel, from one ncu
+# capture of two eager FP64 steps of the 128^3 box with 1e6 particles
+# (0.48 particles per cell, the headline workload's density):
+# (flops = 2 DFMA + DADD + DMUL thread instructions, FP64-pipe thread
+# instructions of any kind), both divided by the cells of a launch.  The FP64
+# kernels keep the reference's unfused multiply-adds (parity), so a flop
+# costs about one pipe instruction; the FMA peak counts two per instruction.
+FP64_OPS = {
+    "rhs_momentum": (203.0, 222.1),
+    "fft_x_fwd_resid": (47.6, 44.8),
+    "fft_y": (15.2, 13.1),
+    "fft_z_solve": (28.6, 27.6),
+    "fft_x_inv_update": (19.5, 20.8),
+}
+FP64_FLOP_PER_CELL_STEP = 4090.7  # all kernels of a step, same capture
+
+# Algorithmic bytes per launch of each kernel, (bytes per cell, bytes per
+# particle), for FP64 storage: each value a kernel must read or write once.
+# `value` is the headline (mixed-precision) path; the FP64 path is reported
+# beside it under "fp64".
 KERNEL_BYTES = {
+    # U, RU_int, F_p, RU, RU_np1 in; RU_np1, RU_new out (3 each)
     "rhs_momentum": (21 * 8, 0),
+    # RU_new 3, Rho_new, Q, face coefficients 3 in; RHS, divergence, cc out
     "poisson_rhs": (11 * 8, 0),
     "poisson_faces": (10 * 8, 0),
+    # P, C 3, cc, RHS in; the half spectrum (one complex per two cells) out
     "fft_x_fwd_resid": (6 * 8 + 8, 0),
+    # the half spectrum in and out
     "fft_y": (16, 0),
     "fft_z_solve": (16, 0),
+    # the half spectrum in; P in and out
     "fft_x_inv_update": (24, 0),
     "deposit_heat": (4 + 8, 32),
     "deposit_conc": (4 + 8, 24),
     "deposit_momentum": (4 + 24, 48),
+    # base, int and np1 sets in, np1 and new out (7 values each), heat rate in
+    # and out, the cell keys and deposit payloads out
     "particle_push": (0, 488),
+    # RU_int 3, Rho_int in; U 3 out
     "face_velocity": (7 * 8, 0),
+    # RU_int 3, Rho, Rho_np1 in; Rho_new, Rho_np1, 1/Rho_new, T out
     "rho_update": (9 * 8, 0),
+    # P, RU_new 3, RU_np1 3 in; RU_new 3, RU_np1 3 out
     "project": (13 * 8, 0),
 }
 
@@ -237,38 +264,78 @@ def time_e2e(ctx, steps):
     return (time.perf_counter() - t0) * 1e3 / steps, h2d, h2d
 
 
-def cpu_sample(workload, steps_total):
-    """A bounded CPU sample of the workload: a smaller box at the same particle
-    density and physics (128^3 unless that would take more than ~3 minutes)."""
+def cpu_sample(workload):
+    """The bounded CPU sample of a workload: a 128^3 box (the workload's own
+    box if smaller) at the workload's particle density and physics."""
     from tpm import params as P
 
     w = P.WORKLOADS[workload]
-    Ns = 128 if steps_total <= 16 else 96 if steps_total <= 40 else 64
-    Ns = min(Ns, w["N"])
+    Ns = min(128, w["N"])
     nps = int(round(w["npart"] * (Ns / w["N"]) ** 3))
     p, s = make_workload(workload, 0, N=Ns, npart=nps)
     return Ns, nps, p, s
 
 
-def cpu_baseline_port(workload):
-    """The C restatement of the reference on one host core, one RK4 step of a
-    bounded sample of the workload (1 thread)."""
+def host_info():
+    """Core count and CPU model of this host."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"cores": os.cpu_count(), "model": model or platform.machine()}
+
+
+def cpu_rate(workload, warmup, steps):
+    """The reference's CPU implementation of the step on one host core, on the
+    bounded sample of the workload: the reference's own build where it was
+    compiled on this host (its step loop timed by its own clock), else the C
+    restatement of it (warm-up steps, then the timed steps).  Returns the
+    rate, the Poisson iterations per solve of the timed steps (the C
+    restatement's count; the reference's FFT solver does not record it,
+    poisson.cpp:391-411) and a description of the sample."""
     sys.path.insert(0, os.path.join(HERE, "oracle"))
     import pyoracle
 
     pyoracle.build()
-    Ns, nps, p, s = cpu_sample(workload, 1)
-    o = pyoracle.Oracle(p, s.npart)
-    o.load(s)
-    o.initialize()
-    t0 = time.perf_counter()
-    o.step()
-    dt = time.perf_counter() - t0
-    o.close()
-    return {"value": round(p.ncell / dt / 1e6, 4), "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"1 RK4 step of a {Ns}^3 box with {nps} particles (the workload's particle "
-                      f"density and physics), {dt:.1f} s on one core, C restatement of the "
-                      f"reference"}
+    Ns, nps, p, s = cpu_sample(workload)
+    n_it = None
+    if pyoracle.have_reference():
+        kind = "reference"
+        secs = pyoracle.run_reference(p, s, steps)["seconds"]
+        what = "the reference's own sources built on this host"
+    else:
+        kind = "port"
+        o = pyoracle.Oracle(p, s.npart)
+        o.load(s)
+        o.initialize()
+        for _ in range(warmup):
+            o.step()
+        it0 = o.scalars()["total_poisson_iterations"]
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            o.step()
+        secs = time.perf_counter() - t0
+        n_it = (o.scalars()["total_poisson_iterations"] - it0) / (4.0 * steps)
+        o.close()
+        what = f"the C restatement of the reference, after {warmup} warm-up step(s)"
+    host = host_info()
+    return {"value": round(p.ncell * steps / secs / 1e6, 4), "unit": UNIT, "cores": 1,
+            "kind": kind, "n_it": n_it, "seconds_per_step": round(secs / steps, 3),
+            "host": host,
+            "sample": f"{steps} RK4 step(s) of a {Ns}^3 box with {nps} particles (the workload's "
+                      f"particle density and physics), {secs / steps:.1f} s per step on one core "
+                      f"of a {host['cores']}-core {host['model']} host, {what}"}
+
+
+def cpu_baseline_port(workload):
+    """The reported CPU baseline of the GPU arm: the same sample and step
+    count as the reference arm (2 timed steps after 1 warm-up step)."""
+    return cpu_rate(workload, 1, 2)
 
 
 def max_over_ranks(x, dist, device="cpu"):
@@ -299,8 +366,9 @@ def kernel_bytes(name, ncell, npart, mixed):
 
 
 def step_bytes(ncell, npart, n_it, mixed):
-    """Per RK4 step, SURVEY's fixed count with the FFT traffic at the spectrum's
-    width: N^3 [4 ((50 + 4 (n_it-1)) w + 11 n_it w_fft) + 9 w] + Np 4 (37 w_p + 16);
+    """Algorithmic bytes per RK4 step (the fixed count per cell-step: 61
+    stored values per cell and stage plus 15 per further Poisson iteration,
+    and the mean reset), with the FFT traffic at the spectrum's width: N^3 [4 ((50 + 4 (n_it-1)) w + 11 n_it w_fft) + 9 w] + Np 4 (37 w_p + 16);
     w = w_p = 8 (FP64 state on both paths), w_fft = 8 (FP64) or 4 (mixed)."""
     w, wf = 8, (4 if mixed else 8)
     per_cell = 4 * ((50 + 4 * (n_it - 1)) * w + 11 * n_it * wf) + 9 * w
@@ -328,6 +396,7 @@ def path_result(p, s, ms, steps, world, n_it, launches, prof, clocks, mixed, pea
                           "algorithmic_bytes_per_step": int(sb)},
         "kernels_ms_per_step": {k: round(v[1] / 2, 3) for k, v in
                                 sorted(prof.items(), key=lambda kv: -kv[1][1])},
+        "kernel_launches_per_step": {k: v[0] / 2 for k, v in prof.items()},
         "mparticle_steps_per_s": world * s.npart * steps / (ms * 1e-3) / 1e6,
     }
 
@@ -393,6 +462,59 @@ def mixed_accuracy_fresh(p64, s, checkpoints=(1, 10)):
         out[f"after_{n}_step" + ("s" if n > 1 else "")] = r
     for c in ctx.values():
         c.close()
+    return out
+
+
+def fp64_peaks():
+    """The FP64 roof: the library's FMA-chain probe (tpm_measure_fp64_peak)
+    and, for comparison, cuBLAS DGEMM 4096^3 through torch (best of 5)."""
+    import ctypes
+
+    import torch
+    from tpm import capi
+
+    t = ctypes.c_double(0)
+    probe = None
+    if capi.load_library().tpm_measure_fp64_peak(ctypes.byref(t)) == 0 and t.value > 0:
+        probe = t.value
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        a @ b
+    best = 0.0
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return {"fma_probe_tflops": round(probe, 4) if probe else None,
+            "dgemm_tflops": round(best, 4),
+            "how": "FMA probe: 8 independent DFMA chains per thread, 8 blocks of 256 per SM, "
+                   "best of 3 CUDA-event-timed launches; DGEMM: torch.matmul float64 4096^3"}
+
+
+def fp64_roofline(r, ncell, peaks):
+    """The FP64 path against the FP64 pipe (its bound), for its dominant kernel
+    and for the whole step."""
+    peak = peaks["fma_probe_tflops"] or peaks["dgemm_tflops"]
+    name = r["roofline"]["kernel"]
+    out = {"bound": "fp64", "peak_tflops": peak,
+           "peak_source": "measured FMA probe" if peaks["fma_probe_tflops"] else "measured DGEMM"}
+    if name in FP64_OPS:
+        flops, inst = FP64_OPS[name]
+        ms = r["kernels_ms_per_step"][name] / r["kernel_launches_per_step"][name]
+        ach = flops * ncell / (ms * 1e-3) / 1e12
+        inst_rate = inst * ncell / (ms * 1e-3) / 1e12
+        out.update({"kernel": name, "flop_per_cell": flops, "fp64_inst_per_cell": inst,
+                    "achieved_tflops": round(ach, 4), "frac": round(ach / peak, 4),
+                    "achieved_tinst_s": round(inst_rate, 4),
+                    "inst_frac": round(inst_rate / (peak / 2), 4)})
+    step = FP64_FLOP_PER_CELL_STEP * ncell / (r["ms_per_step"] * 1e-3) / 1e12
+    out["step"] = {"flop_per_cell_step": FP64_FLOP_PER_CELL_STEP,
+                   "achieved_tflops": round(step, 4), "frac": round(step / peak, 4)}
     return out
 
 
@@ -507,9 +629,12 @@ def gpu_main(args):
         line["fp64"] = {"value": round(f["value"], 3), "ms_per_step": round(f["ms_per_step"], 3),
                         "fft_pencils_per_block": f["fft_pencils_per_block"],
                         "n_it": f["n_it"], "roofline": f["roofline"],
+                        "fp64_roofline": fp64_roofline(f, p64.ncell, fp64_peaks()),
                         "step_roofline": f["step_roofline"], "clocks": f["clocks"],
                         "kernels_ms_per_step": f["kernels_ms_per_step"]}
         line["mixed_vs_fp64_speedup"] = round(r["value"] / f["value"], 3)
+    if head == "fp64":
+        line["fp64_roofline"] = fp64_roofline(r, p64.ncell, fp64_peaks())
     if accuracy:
         line["mixed_accuracy"] = accuracy
     # the pencil-FFT pressure iteration against cuFFT doing only the spectral solve
@@ -753,43 +878,24 @@ def reference_main(args):
         print(json.dumps({"impl": "reference", "unavailable":
                           "the reference runs one box per MPI job and has no adjoint"}), flush=True)
         return
-    sys.path.insert(0, os.path.join(HERE, "oracle"))
-    import pyoracle
-
-    pyoracle.build()
-    # bounded sample: a smaller box at the workload's particle density and
-    # physics, one RK4 step per timed step
-    Ns, nps, p, s = cpu_sample(args.workload, args.steps + args.warmup)
-    kind = "port"
-    times = []
-    if pyoracle.have_reference():
-        ref = pyoracle.run_reference(p, s, args.steps)
-        kind = "reference"
-        secs = ref["seconds"]
-    else:
-        o = pyoracle.Oracle(p, s.npart)
-        o.load(s)
-        o.initialize()
-        for _ in range(args.warmup):
-            o.step()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            o.step()
-        secs = time.perf_counter() - t0
-        o.close()
-    value = p.ncell * args.steps / secs / 1e6
-    sample = (f"{Ns}^3 box with {nps} particles (the workload's particle density and physics), "
-              f"{args.steps} RK4 steps on one host core")
+    # bounded sample: the 128^3 box at the workload's particle density and
+    # physics; at most 1 warm-up and 2 timed steps whatever --steps/--warmup ask
+    # (one step of the sample takes several seconds on one core)
+    steps_run, warm_run = max(1, min(args.steps, 2)), min(args.warmup, 1)
+    cb = cpu_rate(args.workload, warm_run, steps_run)
+    value = cb["value"]
     line = {
-        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(secs * 1e3 / args.steps, 3), "higher_is_better": True,
+        "ms_per_step": round(cb["seconds_per_step"] * 1e3, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload} (sampled: {Ns}^3, {nps} particles)",
-                   "precision": "fp64", "parallelism": "1 host core"},
-        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": 1, "kind": kind,
-                         "sample": sample},
-        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+        "config": {"workload": f"{args.workload} (sampled: {cb['sample']})",
+                   "precision": "fp64", "parallelism": "1 host core",
+                   "timed_steps": steps_run, "warmup_steps": warm_run},
+        "n_it": cb["n_it"],
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "n_it",
+                                             "host")},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

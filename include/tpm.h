@@ -405,6 +405,13 @@ int tpm_batch_autotune(tpm_batch *b);  /* tpm_autotune once per distinct grid sh
 int tpm_batch_run(tpm_batch *b, int nsteps, int use_graph);
 int tpm_batch_sync(tpm_batch *b);
 
+/* The FP64 FMA throughput of the current device in TFLOP/s (2 flops per FMA),
+ * measured by a kernel of independent FMA chains: the roof of the FP64 path,
+ * whose kernels are bound by the FP64 pipe (GB300 issues FP64 at a small
+ * fraction of its FP32 rate) rather than by HBM.  For the bench; not in the
+ * reference. */
+int tpm_measure_fp64_peak(double *tflops);
+
 /* Per-kernel timing with CUDA events on the context stream (for the bench). */
 int tpm_profile_enable(tpm_ctx *ctx, int on);
 /* Fills names (NUL separated, up to cap bytes), launches and total ms per

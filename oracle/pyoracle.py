@@ -38,7 +38,9 @@ def build(quiet: bool = True) -> None:
     """Compile liboracle.so (and the reference binary when its sources exist)."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.check_call(["make", "-C", HERE, "-s"], stdout=out)
-    if os.path.isdir("/root/reference"):
+    has_ref = subprocess.call(["make", "-C", HERE, "-s", "has-ref"], stdout=subprocess.DEVNULL,
+                              stderr=subprocess.DEVNULL) == 0
+    if has_ref:
         subprocess.check_call(["make", "-C", HERE, "-s", "-j8", "ref"], stdout=out,
                               stderr=subprocess.DEVNULL if quiet else None)
 

@@ -10,6 +10,7 @@
 // Every floating-point reduction is a fixed tree over a fixed number of
 // blocks (no floating-point atomics), so each result is bit-reproducible; the
 // pair counts of the RDF are integers.
+#include <algorithm>
 #include <cmath>
 #include <string>
 #include <vector>
@@ -543,3 +544,59 @@ int tpm_rdf(tpm_ctx *c, double r_max, int nbins, unsigned long long *pairs, doub
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// FP64 FMA throughput of the current device (the roof of the FP64 path,
+// whose kernels are bound by the FP64 pipe rather than by HBM): every thread
+// runs eight independent chains of dependent FMAs, so the pipe never waits
+// on a result; 2 flops per FMA.
+namespace tpm {
+__global__ void k_fp64_fma_peak(double *__restrict__ sink, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) x[j] = (threadIdx.x + 32 * j) * 1e-7;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = fma(x[j], a, b);
+  }
+  double s = 0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += x[j];
+  if (s == -1.0) sink[blockIdx.x] = s;  // never true for these inputs: keeps the chains live
+}
+}  // namespace tpm
+
+extern "C" int tpm_measure_fp64_peak(double *tflops) {
+  if (!tflops) return TPM_ERR_ARG;
+  *tflops = 0;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return TPM_ERR_CUDA;
+  const int threads = 256, blocks = sms * 8, iters = 8192;
+  cudaStream_t st = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = TPM_OK;
+  if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    rc = TPM_ERR_CUDA;
+  } else {
+    double best = 0;
+    for (int r = 0; r < 4 && rc == TPM_OK; ++r) {  // the first launch warms up
+      tpm::k_fp64_fma_peak<<<blocks, threads, 0, st>>>(nullptr, iters, 0.9999999, 1e-9);
+      if (cudaEventRecord(e0, st) != cudaSuccess) rc = TPM_ERR_CUDA;
+      tpm::k_fp64_fma_peak<<<blocks, threads, 0, st>>>(nullptr, iters, 0.9999999, 1e-9);
+      float ms = 0;
+      if (rc != TPM_OK || cudaEventRecord(e1, st) != cudaSuccess ||
+          cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+        rc = TPM_ERR_CUDA;
+      else if (r > 0 && ms > 0)
+        best = std::max(best, 2.0 * 8.0 * iters * (double)threads * blocks / (ms * 1e-3) / 1e12);
+    }
+    *tflops = best;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
+  return rc;
+}

@@ -1149,6 +1149,4 @@ void launch_center_coeff_from_C(tpm_ctx *c) {
                c->Cface, c->cc, c->Cs, c->Cs2, c->cc32);
 }
 
-void launch_init_fields(tpm_ctx *) {}
-
 }  // namespace tpm

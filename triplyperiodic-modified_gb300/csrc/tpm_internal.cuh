@@ -304,7 +304,6 @@ void launch_div_residual(tpm_ctx *c, int stage);
 void launch_mean_reset(tpm_ctx *c);
 void launch_passive_scalar(tpm_ctx *c, int stage, bool np1_in_base);  // grid.cpp:743-772
 void launch_passive_scalar_face(tpm_ctx *c, const double *src);      // PS_face = I_C2F(src)
-void launch_init_fields(tpm_ctx *c);
 int cell_blocks(const Grid &g);
 // Blocks for a grid-stride kernel over `items` items, `threads` per block:
 // whole waves of the blocks the kernel keeps resident (SMs x resident blocks

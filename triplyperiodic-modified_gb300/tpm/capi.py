@@ -81,6 +81,7 @@ SIGNATURES = {
     "tpm_set_option": (_i, [_vp, _i, _i]),
     "tpm_poisson_solve_noalloc": (_i, [_i, _i, _i, _d, _d, _d, _vp, _vp, _vp, _i, _d, _vp,
                                        ctypes.POINTER(_i), _dp]),
+    "tpm_measure_fp64_peak": (_i, [_dp]),
     "tpm_profile_enable": (_i, [_vp, _i]),
     "tpm_profile_report": (_i, [_vp, ctypes.c_char_p, _i, ctypes.POINTER(_i), _dp, _i]),
     "tpm_profile_reset": (_i, [_vp]),
