@@ -230,6 +230,14 @@ int phase_check(tpm_ctx *c, int k, unsigned bit, unsigned need, const char *name
   return TPM_OK;
 }
 
+// the divergence constraint is kept for download (TPM_OPT_STORE_DIVERGENCE)
+// and, on the mixed path, for the post-projection residual of the stages that
+// evaluate it
+bool store_divergence(const tpm_ctx *c, int s) {
+  return c->store_div ||
+         (c->p.precision == TPM_PREC_MIXED && (s == 3 || c->div_every_stage));
+}
+
 void swap_stage(tpm_ctx *c) {
   // grid::TimeAdvance_RK4 (grid.cpp:890-900): int = new
   std::swap(c->RU_int, c->RU_new);
@@ -306,7 +314,7 @@ void substep(tpm_ctx *c, int s) {
   tpm::particle_heat(c);
   if (c->PS) tpm::launch_passive_scalar(c, s, nb);  // simulation.cpp:65
   if (par) aux_join(c, c->join_ev[1]);
-  tpm::launch_poisson_rhs(c, s, c->store_div || c->p.precision == TPM_PREC_MIXED);
+  tpm::launch_poisson_rhs(c, s, store_divergence(c, s));
   poisson_loop(c, c->Iteration, c->p.epsilon);
   tpm::launch_project(c, s);
   if (c->p.precision == TPM_PREC_MIXED && (s == 3 || c->div_every_stage))
@@ -725,6 +733,9 @@ int tpm_get_scalars(tpm_ctx *c, tpm_scalars *out) {
     if (!std::isfinite(c->hsc->mean_ru[0]) || !std::isfinite(c->hsc->mean_ru[1]) ||
         !std::isfinite(c->hsc->mean_ru[2]) || !std::isfinite(c->hsc->P0))
       return fail(c, TPM_ERR_NONFINITE, "non-finite momentum or pressure in the state");
+    if (c->hsc->timeout)
+      return fail(c, TPM_ERR_TIMEOUT,
+                  "a kernel's bounded wait for its tile copies gave up; its results are void");
     if (c->hsc->crowded)
       return fail(c, TPM_ERR_NONFINITE,
                   "more than 65536 particles crowded into one cell (a diverging run); their "
@@ -1002,7 +1013,7 @@ int tpm_compute_rhs_pois(tpm_ctx *c, int k) {
   return guarded(c, [&]() -> int {
     if (int rc = phase_check(c, k, PH_RHSP, PH_DIV, "Compute_RHS_Pois")) return rc;
     tpm::launch_face_coeff(c);  // mixed path: C = 1/Rho_face pairs (grid.cpp:852)
-    tpm::launch_poisson_rhs(c, k, c->store_div || c->p.precision == TPM_PREC_MIXED);
+    tpm::launch_poisson_rhs(c, k, store_divergence(c, k));
     c->ph_done |= PH_RHSP;
     return TPM_OK;
   });

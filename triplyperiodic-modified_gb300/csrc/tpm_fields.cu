@@ -6,6 +6,8 @@
 // reference's floating-point operation order and the library is compiled
 // with --fmad=false, so apart from reductions and the FFT the results are
 // the reference's to the last bit.
+#include <cudaTypedefs.h>
+
 #include <map>
 #include <mutex>
 #include <utility>
@@ -13,6 +15,7 @@
 #include "tpm_internal.cuh"
 #include "tpm_ff.cuh"
 #include "tpm_reduce.cuh"
+#include "tpm_tma.cuh"
 
 namespace tpm {
 namespace {
@@ -476,7 +479,7 @@ __global__ void k_rho_update_mixed(Grid g, const double *__restrict__ RUi,
     Rho_np1[c] = np1;
     Rho_new[c] = nw;
     const float2 ir = ff_rcp(ff_from_double(nw));
-    inv_rho2[c] = ir;
+    if (inv_rho2) inv_rho2[c] = ir;  // (the TMA Poisson pass forms it from Rho_new itself)
     Tgas[c] = T_scale * ff_to_double(ir);
   }
 }
@@ -644,6 +647,296 @@ k_poisson_rhs_zm(Grid g, const float2 *__restrict__ inv_rho2, const double *__re
   }
 }
 
+// ---------------------------------------------------------------------------
+// Mixed path, Solver 0, grids of whole 32 x 8 column tiles: the face
+// coefficients (what k_face_coeff_mixed forms from Rho_new) and the Poisson
+// right-hand side (k_poisson_rhs_zm) in one z-marching pass whose tiles the
+// TMA brings in.  Per plane a block needs Rho_new with a one-cell halo (1/Rho
+// for the Laplacian of the thermal divergence, 2/(Rho + Rho_m) for the face
+// coefficients), RU_new on its faces and Q: one thread issues the boxes of
+// the next plane (cp.async.bulk.tensor, tpm_tma.cuh) into a ring of shared-
+// memory slots while the block computes on the current one, so the pass
+// waits on no global load.  It reads 40 B per cell (Rho_new, RU_new 3, Q) and
+// writes 44 B (RHS, divergence, cc, C/d^2 pairs 3) where the two passes it
+// replaces moved 140 B (1/Rho pairs written by the density update and read
+// back, C as a double written and read back).  The arithmetic is the same
+// float-float arithmetic as those kernels: C = 2 rcp(Rho + Rho_m) and 1/Rho as
+// pairs, each face's flux RU C formed once and read by its two cells.
+namespace {
+
+struct PrSmem {
+  // raw FP64 tiles landed by TMA (byte offsets; every box 128-byte aligned)
+  static constexpr int kRhoSlot = (32 + 256 + 32 + 16 + 16) * 8;  // ylo row | 8 rows | yhi row | xlo 8x2 | xhi 8x2
+  static constexpr int kRhoMain = 256, kRhoYhi = 2304, kRhoXlo = 2560, kRhoXhi = 2688;
+  static constexpr int kRuxSlot = (256 + 16) * 8;  // 8 rows | xhi 8x2
+  static constexpr int kRuySlot = (256 + 32) * 8;  // 8 rows | yhi row
+  static constexpr int kTile = 256 * 8;            // 8 rows of 32
+  static constexpr int oRho = 0;                   // 4 planes
+  static constexpr int oRux = oRho + 4 * kRhoSlot;  // 2 planes
+  static constexpr int oRuy = oRux + 2 * kRuxSlot;  // 2 planes
+  static constexpr int oRuz = oRuy + 2 * kRuySlot;  // 3 planes
+  static constexpr int oQ = oRuz + 3 * kTile;       // 2 planes
+  // 1/Rho pairs of 3 planes, [10][34] (rows j0-1 .. j0+8, columns i0-1 .. i0+32)
+  static constexpr int oIr = oQ + 2 * kTile;
+  static constexpr int kIrPlane = 10 * 34 * 8;
+  // face flux pairs and C pairs: x faces [8][33], y faces [9][32], z faces 2 x [8][32]
+  static constexpr int oFx = oIr + 3 * kIrPlane;
+  static constexpr int oCx = oFx + 264 * 8;
+  static constexpr int oFy = oCx + 264 * 8;
+  static constexpr int oCy = oFy + 288 * 8;
+  static constexpr int oFz = oCy + 288 * 8;
+  static constexpr int oCz = oFz + 512 * 8;
+  static constexpr int oBar = oCz + 512 * 8;  // 2 mbarriers
+  static constexpr int oRed = oBar + 16;      // 32 doubles for the block sums
+  static constexpr int kBytes = oRed + 32 * 8;
+  static constexpr unsigned kStageBytes = kRhoSlot + kRuxSlot + kRuySlot + 2 * kTile;
+  static constexpr unsigned kPrologueBytes = 2 * kRhoSlot + kTile;
+};
+static_assert(PrSmem::oRux % 128 == 0 && PrSmem::oRuy % 128 == 0 && PrSmem::oRuz % 128 == 0 &&
+                  PrSmem::oQ % 128 == 0 && PrSmem::kRhoSlot % 128 == 0 &&
+                  PrSmem::kRuxSlot % 128 == 0 && PrSmem::kRuySlot % 128 == 0,
+              "TMA destinations must stay 128-byte aligned");
+
+// the tensor maps of one launch: Rho_new and RU_new (as [3 nz][ny][nx]) with
+// boxes 32 x 8 (a tile), 32 x 1 (a halo row), 2 x 8 (a halo column pair), Q
+// with tile boxes
+struct PrMaps {
+  CUtensorMap rho_t, rho_r, rho_c, ru_t, ru_r, ru_c, q_t;
+};
+
+__global__ void __launch_bounds__(kZX * kZY)
+k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restrict__ s,
+                  double *__restrict__ RHS, double *__restrict__ divg, float *__restrict__ cc32,
+                  float2 *__restrict__ Cs2, double *__restrict__ partials,
+                  double *__restrict__ tke_parts, PoisArgs a, int zlen) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int tid = threadIdx.x, tx = tid % kZX, ty = tid / kZX;
+  const int tilesx = g.nx / kZX, tilesy = g.ny / kZY;
+  const int bx = blockIdx.x % tilesx, by = (blockIdx.x / tilesx) % tilesy;
+  const int bz = blockIdx.x / (tilesx * tilesy);
+  const int i0 = bx * kZX, j0 = by * kZY, k0 = bz * zlen;
+  const int k1 = min(k0 + zlen, g.nz);
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sm + PrSmem::oBar);
+  double *red = reinterpret_cast<double *>(sm + PrSmem::oRed);
+  if (smem_u32(sm) & 127u) {  // the layout's alignment rests on this: never issue a misaligned box
+    if (tid == 0) s->timeout = 1;
+    return;
+  }
+  auto rho_slot = [&](int kk) { return sm + PrSmem::oRho + ((kk + 4) & 3) * PrSmem::kRhoSlot; };
+  auto rux_slot = [&](int kk) { return sm + PrSmem::oRux + (kk & 1) * PrSmem::kRuxSlot; };
+  auto ruy_slot = [&](int kk) { return sm + PrSmem::oRuy + (kk & 1) * PrSmem::kRuySlot; };
+  auto ruz_slot = [&](int kk) { return sm + PrSmem::oRuz + (kk % 3) * PrSmem::kTile; };
+  auto q_slot = [&](int kk) { return sm + PrSmem::oQ + (kk & 1) * PrSmem::kTile; };
+  auto ir_plane = [&](int kk) {
+    return reinterpret_cast<float2 *>(sm + PrSmem::oIr + ((kk + 3) % 3) * PrSmem::kIrPlane);
+  };
+  float2 *fx = reinterpret_cast<float2 *>(sm + PrSmem::oFx);
+  float2 *cxp = reinterpret_cast<float2 *>(sm + PrSmem::oCx);
+  float2 *fy = reinterpret_cast<float2 *>(sm + PrSmem::oFy);
+  float2 *cyp = reinterpret_cast<float2 *>(sm + PrSmem::oCy);
+  auto fz = [&](int kk) { return reinterpret_cast<float2 *>(sm + PrSmem::oFz) + (kk & 1) * 256; };
+  auto czp = [&](int kk) { return reinterpret_cast<float2 *>(sm + PrSmem::oCz) + (kk & 1) * 256; };
+  const int jlo = j0 == 0 ? g.ny - 1 : j0 - 1, jhi = j0 + kZY == g.ny ? 0 : j0 + kZY;
+  const int ilo = i0 == 0 ? g.nx - 2 : i0 - 2, ihi = i0 + kZX == g.nx ? 0 : i0 + kZX;
+  auto wz = [&](int kk) { return kk < 0 ? kk + g.nz : (kk >= g.nz ? kk - g.nz : kk); };
+  // the boxes of Rho_new plane kk (with its halo) into its slot
+  auto load_rho = [&](int kk, uint64_t *b) {
+    unsigned char *d = rho_slot(kk);
+    const int z = wz(kk);
+    tma_load_3d(d + PrSmem::kRhoMain, &m.rho_t, b, i0, j0, z);
+    tma_load_3d(d, &m.rho_r, b, i0, jlo, z);
+    tma_load_3d(d + PrSmem::kRhoYhi, &m.rho_r, b, i0, jhi, z);
+    tma_load_3d(d + PrSmem::kRhoXlo, &m.rho_c, b, ilo, j0, z);
+    tma_load_3d(d + PrSmem::kRhoXhi, &m.rho_c, b, ihi, j0, z);
+  };
+  // stage kk: Rho plane kk + 1, RU_new x and y faces and Q of plane kk, the z
+  // faces of plane kk + 1
+  auto load_stage = [&](int kk, uint64_t *b) {
+    mbar_arrive_expect_tx(b, PrSmem::kStageBytes);
+    load_rho(kk + 1, b);
+    tma_load_3d(rux_slot(kk), &m.ru_t, b, i0, j0, kk);
+    tma_load_3d(rux_slot(kk) + 2048, &m.ru_c, b, ihi, j0, kk);
+    tma_load_3d(ruy_slot(kk), &m.ru_t, b, i0, j0, g.nz + kk);
+    tma_load_3d(ruy_slot(kk) + 2048, &m.ru_r, b, i0, jhi, g.nz + kk);
+    tma_load_3d(ruz_slot(kk + 1), &m.ru_t, b, i0, j0, 2 * g.nz + wz(kk + 1));
+    tma_load_3d(q_slot(kk), &m.q_t, b, i0, j0, kk);
+  };
+  // waits for stage r (the prologue is stage 0, plane kk is stage kk - k0 + 1)
+  bool ok = true;
+  auto wait_stage = [&](int r) {
+    if (!mbar_wait(&bar[r & 1], (unsigned)(r >> 1) & 1u)) {
+      ok = false;
+      s->timeout = 1;
+    }
+  };
+  // 1/Rho pairs of plane kk from its raw slot: [10][34] with the halo
+  auto convert = [&](int kk) {
+    const double *d = reinterpret_cast<const double *>(rho_slot(kk));
+    float2 *ir = ir_plane(kk);
+    for (int e = tid; e < 336; e += kZX * kZY) {
+      double v;
+      int at_;
+      if (e < 256) {  // main rows
+        v = d[32 + e];
+        at_ = (e / 32 + 1) * 34 + e % 32 + 1;
+      } else if (e < 288) {  // row j0 - 1
+        v = d[e - 256];
+        at_ = e - 256 + 1;
+      } else if (e < 320) {  // row j0 + 8
+        v = d[288 + e - 288];
+        at_ = 9 * 34 + e - 288 + 1;
+      } else if (e < 328) {  // column i0 - 1 (second of the pair)
+        v = d[320 + 2 * (e - 320) + 1];
+        at_ = (e - 320 + 1) * 34;
+      } else {  // column i0 + 32 (first of the pair)
+        v = d[336 + 2 * (e - 328)];
+        at_ = (e - 328 + 1) * 34 + 33;
+      }
+      ir[at_] = ff_rcp(ff_from_double(v));
+    }
+  };
+  // C = 1/Rho_face = 2 / (Rho_a + Rho_b) and the flux RU C, as pairs
+  auto face = [&](double ra, double rb, double ru, float2 &flux, float2 &C) {
+    const float2 h = ff_rcp(ff_add(ff_from_double(ra), ff_from_double(rb)));
+    C = make_float2(2.f * h.x, 2.f * h.y);
+    flux = ff_norm(ff_mul(ff_from_double(ru), C));
+  };
+  // z faces between planes kk - 1 and kk (the lower faces of plane kk)
+  auto zfaces = [&](int kk) {
+    const double *ra = reinterpret_cast<const double *>(rho_slot(kk) + PrSmem::kRhoMain);
+    const double *rb = reinterpret_cast<const double *>(rho_slot(kk - 1) + PrSmem::kRhoMain);
+    const double *ru = reinterpret_cast<const double *>(ruz_slot(kk));
+    float2 *f = fz(kk), *C = czp(kk);
+    for (int e = tid; e < 256; e += kZX * kZY) face(ra[e], rb[e], ru[e], f[e], C[e]);
+  };
+
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init_fence();
+    tma_prefetch_map(&m.rho_t);
+    tma_prefetch_map(&m.ru_t);
+  }
+  __syncthreads();
+  if (tid == 0) {  // prologue: Rho planes k0 - 1, k0 and the z faces of plane k0; then stage k0
+    mbar_arrive_expect_tx(&bar[0], PrSmem::kPrologueBytes);
+    load_rho(k0 - 1, &bar[0]);
+    load_rho(k0, &bar[0]);
+    tma_load_3d(ruz_slot(k0), &m.ru_t, &bar[0], i0, j0, 2 * g.nz + k0);
+    load_stage(k0, &bar[1]);
+  }
+  const float2 coef = ff_from_double(s->coef_div), meanQ = ff_from_double(s->mean_Q);
+  const float2 kCp = ff_from_double(a.kCp);
+  const float2 inv_d2[3] = {ff_from_double(g.inv_dx2), ff_from_double(g.inv_dy2),
+                            ff_from_double(g.inv_dz2)};
+  const float2 inv_d[3] = {ff_from_double(g.inv_dx), ff_from_double(g.inv_dy),
+                           ff_from_double(g.inv_dz)};
+  double acc = 0, usq = 0;
+  int issued = 1;  // stages issued so far: the prologue (0) and stage 1
+  wait_stage(0);
+  ok = __syncthreads_and(ok) != 0;  // every thread takes the same branch
+  if (ok) {
+    convert(k0 - 1);
+    convert(k0);
+    zfaces(k0);
+  }
+  __syncthreads();
+  for (int k = k0; k < k1 && ok; ++k) {
+    const int r = k - k0 + 1;
+    if (k + 1 < k1) {
+      if (tid == 0) {
+        fence_proxy_async();  // the reads of the slots being refilled came before
+        load_stage(k + 1, &bar[(r + 1) & 1]);
+      }
+      issued = r + 1;
+    }
+    wait_stage(r);
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    convert(k + 1);
+    {  // x and y faces of plane k, z faces of plane k + 1
+      const double *rk = reinterpret_cast<const double *>(rho_slot(k));
+      const double *ux = reinterpret_cast<const double *>(rux_slot(k));
+      const double *uy = reinterpret_cast<const double *>(ruy_slot(k));
+      for (int e = tid; e < 264; e += kZX * kZY) {
+        const int ey = e / 33, ex = e - ey * 33;
+        const double ra = ex < 32 ? rk[32 + ey * 32 + ex] : rk[336 + 2 * ey];
+        const double rb = ex > 0 ? rk[32 + ey * 32 + ex - 1] : rk[320 + 2 * ey + 1];
+        const double ru = ex < 32 ? ux[ey * 32 + ex] : ux[256 + 2 * ey];
+        face(ra, rb, ru, fx[e], cxp[e]);
+      }
+      for (int e = tid; e < 288; e += kZX * kZY) {
+        const int ey = e / 32, ex = e - ey * 32;
+        const double ra = rk[32 + ey * 32 + ex];  // row 8 is the j0 + 8 halo row
+        const double rb = ey > 0 ? rk[32 + (ey - 1) * 32 + ex] : rk[ex];
+        const double ru = uy[ey * 32 + ex];       // row 8 is the j0 + 8 halo row
+        face(ra, rb, ru, fy[e], cyp[e]);
+      }
+      zfaces(k + 1);
+    }
+    __syncthreads();
+    {
+      const int i = i0 + tx, j = j0 + ty;
+      const long long c = at(g, i, j, k);
+      const float2 *irk = ir_plane(k), *irm = ir_plane(k - 1), *irp = ir_plane(k + 1);
+      const int o = (ty + 1) * 34 + tx + 1;
+      const float2 ir = irk[o];
+      const float2 pn[3] = {irk[o + 1], irk[o + 34], irp[o]};
+      const float2 mn[3] = {irk[o - 1], irk[o - 34], irm[o]};
+      float2 lap = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float2 sec = ff_add(ff_sub(pn[d], ir), ff_sub(mn[d], ir));
+        lap = ff_add(lap, ff_mul(sec, inv_d2[d]));
+      }
+      float2 Qc = ff_from_double(reinterpret_cast<const double *>(q_slot(k))[tid]);
+      if (a.cooling) Qc = ff_sub(Qc, meanQ);
+      const float2 dv = ff_add(ff_mul(kCp, lap), ff_mul(coef, Qc));
+      if (a.store_div) divg[c] = ff_to_double(dv);
+      float2 divu = make_float2(-dv.x, -dv.y);
+      float msum = 0.f;
+      const int ex = ty * (kZX + 1) + tx, ey = ty * kZX + tx;
+      const float2 ulo[3] = {fx[ex], fy[ey], fz(k)[ey]};
+      const float2 uhi[3] = {fx[ex + 1], fy[ey + kZX], fz(k + 1)[ey]};
+      const float2 clo[3] = {cxp[ex], cyp[ey], czp(k)[ey]};
+      const float chi[3] = {cxp[ex + 1].x, cyp[ey + kZX].x, czp(k + 1)[ey].x};
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        divu = ff_add(divu, ff_mul(ff_sub(uhi[d], ulo[d]), inv_d[d]));
+        msum += (clo[d].x + chi[d]) * 0.5f;
+        if (tke_parts) {
+          const double ul = ff_f2d(ulo[d].x);
+          usq = fma(ul, ul, usq);
+        }
+        Cs2[d * g.n + c] = ff_norm(ff_mul(clo[d], inv_d2[d]));
+      }
+      const double rhs = ff_to_double(divu) * a.inv_dtpre;
+      RHS[c] = rhs;
+      acc += rhs;
+      cc32[c] = -3.0f / msum;
+    }
+    __syncthreads();  // the slots and faces of plane k are refilled next
+  }
+  if (!ok && tid == 0) {
+    // a wait gave up: let the copies of the last two stages issued land
+    // (again bounded) before the block's shared memory is released
+    for (int r = issued > 0 ? issued - 1 : 0; r <= issued; ++r)
+      mbar_wait(&bar[r & 1], (unsigned)(r >> 1) & 1u);
+  }
+  __syncthreads();
+  double bs = block_sum(acc, red);
+  if (tid == 0) partials[blockIdx.x] = bs;
+  if (tke_parts) {
+    __syncthreads();
+    double bu = block_sum(usq, red);
+    if (tid == 0) tke_parts[blockIdx.x] = bu;
+  }
+}
+
+}  // namespace
+
 // face velocity of the mixed path: only the FP32 stencil and the particle
 // gather read it, so it is formed in FP32
 __global__ void k_face_velocity_mixed(Grid g, const float *__restrict__ RUi32,
@@ -797,7 +1090,16 @@ __global__ void k_finish_means3(const double *__restrict__ partials, int nparts,
 // res = div_F2C(RU_new * C) - divergence - dt*pre*mean(RHS_Pois), with
 // C = 1/Rho_face(Rho_new) from k_poisson_rhs.  A converged projection gives
 // res = 0 (grid.cpp:841-863): div u_new = divergence + dt*pre*mean.
-__global__ void k_div_residual(Grid g, const double *__restrict__ RUn, const double *__restrict__ Cf,
+// C = 1/Rho_face on a face from the densities of its two cells, as the
+// mixed path's face coefficients are formed (pairs, 2 rcp(Rho_a + Rho_b)),
+// rounded to a double
+__device__ __forceinline__ double face_c(double ra, double rb) {
+  const float2 h = ff_rcp(ff_add(ff_from_double(ra), ff_from_double(rb)));
+  return ff_to_double(make_float2(2.f * h.x, 2.f * h.y));
+}
+
+__global__ void k_div_residual(Grid g, const double *__restrict__ RUn,
+                               const double *__restrict__ Rho_new,
                                const double *__restrict__ divg, const DevScalars *__restrict__ s,
                                double dtpre, double *__restrict__ partials) {
   __shared__ double sh[kThreads];
@@ -808,11 +1110,13 @@ __global__ void k_div_residual(Grid g, const double *__restrict__ RUn, const dou
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
     Nbr nb = nbr_of(g, q);
+    const double rc = Rho_new[c];
     double dv = 0;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const double *R = RUn + d * g.n, *C = Cf + d * g.n;
-      dv += (R[nb.p[d]] * C[nb.p[d]] - R[c] * C[c]) * inv_d[d];
+      const double *R = RUn + d * g.n;
+      const double cp = face_c(Rho_new[nb.p[d]], rc), cm = face_c(rc, Rho_new[nb.m[d]]);
+      dv += (R[nb.p[d]] * cp - R[c] * cm) * inv_d[d];
     }
     double r = fabs(dv - divg[c] - off);
     mx = r > mx ? r : mx;
@@ -949,13 +1253,52 @@ void launch_p0_update(tpm_ctx *c, int s) {
              c->p.dt * kPre[s], s, (int)c->np1_is_base);
 }
 
+bool make_tensor_map_f64(CUtensorMap *map, const double *base, int nx, int ny, long long nz,
+                         int bx, int by) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  });
+  if (!encode) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[2] = {(cuuint64_t)nx * 8, (cuuint64_t)nx * ny * 8};
+  const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double *>(base), dims, strides,
+                box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// the tensor maps of a device array, built on first use (host work only)
+const TmaField &tma_field(tpm_ctx *c, const double *base, long long layers) {
+  for (const TmaField &f : c->tma_fields)
+    if (f.base == base && f.layers == layers) return f;
+  TmaField f;
+  f.base = base;
+  f.layers = layers;
+  const Grid &g = c->g;
+  if (!make_tensor_map_f64(&f.tile, base, g.nx, g.ny, layers, kZX, kZY) ||
+      !make_tensor_map_f64(&f.row, base, g.nx, g.ny, layers, kZX, 1) ||
+      !make_tensor_map_f64(&f.col, base, g.nx, g.ny, layers, 2, kZY))
+    throw std::string("the driver refused a TMA tensor map");
+  c->tma_fields.push_back(f);
+  return c->tma_fields.back();
+}
+
 void launch_rho_update(tpm_ctx *c, int s, bool np1_in_base) {
   if (c->p.precision == TPM_PREC_MIXED) {
     TPM_LAUNCH(c, "rho_update", k_rho_update_mixed, cell_waves(c, k_rho_update_mixed, false),
                kThreads, 0, c->g,
                c->RU_int, c->Rho, np1_in_base ? c->Rho : c->Rho_np1, c->Rho_np1, c->Rho_new,
-               reinterpret_cast<float2 *>(c->inv_rho), c->Tgas, c->dsc, -(c->p.dt * kPost[s]),
-               -c->p.dt * kPre[s], s);
+               c->tma_rhs ? nullptr : reinterpret_cast<float2 *>(c->inv_rho), c->Tgas, c->dsc,
+               -(c->p.dt * kPost[s]), -c->p.dt * kPre[s], s);
     return;
   }
   TPM_LAUNCH(c, "rho_update", k_rho_update, cell_waves(c, k_rho_update, false), kThreads, 0,
@@ -1014,7 +1357,7 @@ void launch_rhs_momentum(tpm_ctx *c, int s, bool np1_in_base) {
 }
 
 void launch_face_coeff(tpm_ctx *c) {
-  if (c->p.precision != TPM_PREC_MIXED) return;
+  if (c->p.precision != TPM_PREC_MIXED || c->tma_rhs) return;  // (formed by the TMA pass)
   TPM_LAUNCH(c, "face_coeff", k_face_coeff_mixed, cell_waves(c, k_face_coeff_mixed, false),
              kThreads, 0, c->g, c->Rho_new, c->Cface, c->Cs2,
              c->p.Solver == 2 ? c->Cs : nullptr);
@@ -1032,7 +1375,20 @@ void launch_poisson_rhs(tpm_ctx *c, int s, bool store_div) {
   double *rhs_parts = mixed ? c->zm_parts : c->partials + kPartRhs * kRedBlocks;
   double *tke_parts =
       s == 3 ? (mixed ? c->zm_parts + nzm : c->partials + kPartTke2 * kRedBlocks) : nullptr;
-  if (mixed) {
+  if (mixed && c->tma_rhs) {
+    PrMaps m;
+    const TmaField &R = tma_field(c, c->Rho_new, c->g.nz);
+    m.rho_t = R.tile;
+    m.rho_r = R.row;
+    m.rho_c = R.col;
+    const TmaField &U = tma_field(c, c->RU_new, 3LL * c->g.nz);
+    m.ru_t = U.tile;
+    m.ru_r = U.row;
+    m.ru_c = U.col;
+    m.q_t = tma_field(c, c->Q, c->g.nz).tile;
+    TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_tma, nzm, kZX * kZY, PrSmem::kBytes, c->g, m,
+               c->dsc, c->RHS, c->divg, c->cc32, c->Cs2, rhs_parts, tke_parts, a, zm_zlen(c));
+  } else if (mixed) {
     // (C and Cs2 come from launch_face_coeff, run beside the particle stage)
     const bool pcg = c->p.Solver == 2;
     TPM_LAUNCH(c, "poisson_rhs", k_poisson_rhs_zm, nzm, kZX * kZY, 0, c->g,
@@ -1097,7 +1453,7 @@ void launch_passive_scalar_face(tpm_ctx *c, const double *src) {
 
 void launch_div_residual(tpm_ctx *c, int s) {
   const int nb = cell_waves(c, k_div_residual, true);
-  TPM_LAUNCH(c, "div_residual", k_div_residual, nb, kThreads, 0, c->g, c->RU_new, c->Cface,
+  TPM_LAUNCH(c, "div_residual", k_div_residual, nb, kThreads, 0, c->g, c->RU_new, c->Rho_new,
              c->divg, c->dsc, c->p.dt * kPre[s], c->partials + kPartDiv * kRedBlocks);
   TPM_LAUNCH(c, "finish_max_div", k_finish_max_div, 1, kThreads, 0,
              c->partials + kPartDiv * kRedBlocks, nb, c->dsc);
@@ -1115,6 +1471,22 @@ void rhs_kernels_setup(tpm_ctx *c) {
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_rhs_momentum_tiled<double, double>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)rhs_tiled_smem<double>()));
+  // the TMA Poisson pass of the mixed path where the grid is whole 32 x 8
+  // column tiles and the pressure solver is Richardson's; its tensor maps for
+  // both buffers Rho_new and RU_new take turns in, and Q
+  c->tma_rhs = false;
+  if (c->p.precision == TPM_PREC_MIXED && c->p.Solver == 0 && c->g.nx % kZX == 0 &&
+      c->g.ny % kZY == 0) {
+    TPM_CUDA_TRY(cudaFuncSetAttribute(k_poisson_rhs_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      PrSmem::kBytes));
+    try {
+      for (const double *b : {c->Rho_new, c->Rho_int, c->Q}) tma_field(c, b, c->g.nz);
+      for (const double *b : {c->RU_new, c->RU_int}) tma_field(c, b, 3LL * c->g.nz);
+      c->tma_rhs = true;
+    } catch (const std::string &) {
+      c->tma_fields.clear();  // the driver has no TMA maps for us: the two-pass form
+    }
+  }
   // the occupancy of every wave-sized kernel, queried here once (not while a
   // step is being captured into a graph)
   cell_waves(c, k_rho_update_mixed, false);

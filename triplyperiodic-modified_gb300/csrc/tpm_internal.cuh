@@ -11,6 +11,7 @@
 //    (base, int, new, np1 as in particle.h:61-113).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -74,6 +75,8 @@ struct DevScalars {
   double max_div;    // FP64 post-projection residual (mixed path)
   double tke2;       // mean(U^2) of the last stage before projection (grid.cpp:911)
   int nonfinite;
+  // set (and kept) when a kernel's bounded wait on its tile copies gave up
+  int timeout;
   // Poisson iteration control on the device (graph-captured steps): `skip`
   // turns the remaining captured iterations of a solve into no-ops once
   // max|dp| <= epsilon (poisson.cpp:397); `it` counts the iterations run by
@@ -133,6 +136,14 @@ struct HostState {
   int Iteration;
   int pen[3];
   double A, gx, gy, gz, I0;
+};
+
+// TMA tensor maps of one FP64 device array seen as [layers][ny][nx], with
+// boxes of a 32 x 8 tile, a 32 x 1 row and a 2 x 8 column pair (tpm_tma.cuh)
+struct TmaField {
+  const double *base = nullptr;
+  long long layers = 0;
+  CUtensorMap tile, row, col;
 };
 
 // One captured step of one or more boxes, with the host states before and
@@ -252,6 +263,11 @@ struct tpm_ctx {
 
   bool store_div = false;
   bool div_every_stage = false;
+  // mixed path: the face coefficients and the Poisson right-hand side in one
+  // TMA-fed z-marching pass (grids of whole 32 x 8 tiles, Solver 0), with the
+  // tensor maps of the arrays it reads
+  bool tma_rhs = false;
+  std::vector<tpm::TmaField> tma_fields;
 
   // ---- PCG pressure solve (Solver = 2; allocated on first use) ----
   double *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr;
