@@ -671,22 +671,23 @@ struct PrSmem {
   static constexpr int kRuxSlot = (256 + 16) * 8;  // 8 rows | xhi 8x2
   static constexpr int kRuySlot = (256 + 32) * 8;  // 8 rows | yhi row
   static constexpr int kTile = 256 * 8;            // 8 rows of 32
-  static constexpr int oRho = 0;                   // 4 planes
-  static constexpr int oRux = oRho + 4 * kRhoSlot;  // 2 planes
+  static constexpr int oRho = 0;                   // 3 planes
+  static constexpr int oRux = oRho + 3 * kRhoSlot;  // 2 planes
   static constexpr int oRuy = oRux + 2 * kRuxSlot;  // 2 planes
-  static constexpr int oRuz = oRuy + 2 * kRuySlot;  // 3 planes
-  static constexpr int oQ = oRuz + 3 * kTile;       // 2 planes
-  // 1/Rho pairs of 3 planes, [10][34] (rows j0-1 .. j0+8, columns i0-1 .. i0+32)
-  static constexpr int oIr = oQ + 2 * kTile;
-  static constexpr int kIrPlane = 10 * 34 * 8;
-  // face flux pairs and C pairs: x faces [8][33], y faces [9][32], z faces 2 x [8][32]
-  static constexpr int oFx = oIr + 3 * kIrPlane;
-  static constexpr int oCx = oFx + 264 * 8;
-  static constexpr int oFy = oCx + 264 * 8;
-  static constexpr int oCy = oFy + 288 * 8;
-  static constexpr int oFz = oCy + 288 * 8;
-  static constexpr int oCz = oFz + 512 * 8;
-  static constexpr int oBar = oCz + 512 * 8;  // 2 mbarriers
+  static constexpr int oRuz = oRuy + 2 * kRuySlot;  // 2 planes
+  static constexpr int oQ = oRuz + 2 * kTile;       // 2 planes
+  // Rho_new and 1/Rho_new as pairs, [10][34] per plane (rows j0-1 .. j0+8,
+  // columns i0-1 .. i0+32): Rho of 2 planes, 1/Rho of 3
+  static constexpr int kPairPlane = 10 * 34 * 8;
+  static constexpr int oRp = oQ + 2 * kTile;
+  static constexpr int oIr = oRp + 2 * kPairPlane;
+  // flux pairs of the x faces [8][33] and y faces [9][32] of the plane, and
+  // the high parts of their C
+  static constexpr int oFx = oIr + 3 * kPairPlane;
+  static constexpr int oFy = oFx + 264 * 8;
+  static constexpr int oCx = oFy + 288 * 8;
+  static constexpr int oCy = oCx + 264 * 4;
+  static constexpr int oBar = oCy + 288 * 4;  // 2 mbarriers
   static constexpr int oRed = oBar + 16;      // 32 doubles for the block sums
   static constexpr int kBytes = oRed + 32 * 8;
   static constexpr unsigned kStageBytes = kRhoSlot + kRuxSlot + kRuySlot + 2 * kTile;
@@ -694,7 +695,8 @@ struct PrSmem {
 };
 static_assert(PrSmem::oRux % 128 == 0 && PrSmem::oRuy % 128 == 0 && PrSmem::oRuz % 128 == 0 &&
                   PrSmem::oQ % 128 == 0 && PrSmem::kRhoSlot % 128 == 0 &&
-                  PrSmem::kRuxSlot % 128 == 0 && PrSmem::kRuySlot % 128 == 0,
+                  PrSmem::kRuxSlot % 128 == 0 && PrSmem::kRuySlot % 128 == 0 &&
+                  PrSmem::oBar % 8 == 0,
               "TMA destinations must stay 128-byte aligned");
 
 // the tensor maps of one launch: Rho_new and RU_new (as [3 nz][ny][nx]) with
@@ -704,6 +706,19 @@ struct PrMaps {
   CUtensorMap rho_t, rho_r, rho_c, ru_t, ru_r, ru_c, q_t;
 };
 
+// C = 1/Rho_face = 2 / (Rho_a + Rho_b) and the flux RU C, as pairs
+__device__ __forceinline__ void pr_face(float2 ra, float2 rb, double ru, float2 &flux, float2 &C) {
+  const float2 h = ff_rcp(ff_add(ra, rb));
+  C = make_float2(2.f * h.x, 2.f * h.y);
+  flux = ff_norm(ff_mul(ff_from_double(ru), C));
+}
+
+// Thread (tx, ty) owns the cell column (i0 + tx, j0 + ty): it converts that
+// cell of each plane to pairs, forms the cell's lower x, y and z faces (the z
+// faces of the column stay in its registers from one plane to the next), and
+// the right-hand side of the cell; threads 0-79 also convert the tile's halo,
+// threads 0-7 form the x faces at i0 + 32 and threads 32-63 the y faces at
+// j0 + 8.
 __global__ void __launch_bounds__(kZX * kZY)
 k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restrict__ s,
                   double *__restrict__ RHS, double *__restrict__ divg, float *__restrict__ cc32,
@@ -722,26 +737,29 @@ k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restri
     if (tid == 0) s->timeout = 1;
     return;
   }
-  auto rho_slot = [&](int kk) { return sm + PrSmem::oRho + ((kk + 4) & 3) * PrSmem::kRhoSlot; };
+  auto rho_raw = [&](int kk) {
+    return sm + PrSmem::oRho + ((kk + 3) % 3) * PrSmem::kRhoSlot;
+  };
   auto rux_slot = [&](int kk) { return sm + PrSmem::oRux + (kk & 1) * PrSmem::kRuxSlot; };
   auto ruy_slot = [&](int kk) { return sm + PrSmem::oRuy + (kk & 1) * PrSmem::kRuySlot; };
-  auto ruz_slot = [&](int kk) { return sm + PrSmem::oRuz + (kk % 3) * PrSmem::kTile; };
+  auto ruz_slot = [&](int kk) { return sm + PrSmem::oRuz + (kk & 1) * PrSmem::kTile; };
   auto q_slot = [&](int kk) { return sm + PrSmem::oQ + (kk & 1) * PrSmem::kTile; };
+  auto rp_plane = [&](int kk) {
+    return reinterpret_cast<float2 *>(sm + PrSmem::oRp + ((kk + 2) & 1) * PrSmem::kPairPlane);
+  };
   auto ir_plane = [&](int kk) {
-    return reinterpret_cast<float2 *>(sm + PrSmem::oIr + ((kk + 3) % 3) * PrSmem::kIrPlane);
+    return reinterpret_cast<float2 *>(sm + PrSmem::oIr + ((kk + 3) % 3) * PrSmem::kPairPlane);
   };
   float2 *fx = reinterpret_cast<float2 *>(sm + PrSmem::oFx);
-  float2 *cxp = reinterpret_cast<float2 *>(sm + PrSmem::oCx);
   float2 *fy = reinterpret_cast<float2 *>(sm + PrSmem::oFy);
-  float2 *cyp = reinterpret_cast<float2 *>(sm + PrSmem::oCy);
-  auto fz = [&](int kk) { return reinterpret_cast<float2 *>(sm + PrSmem::oFz) + (kk & 1) * 256; };
-  auto czp = [&](int kk) { return reinterpret_cast<float2 *>(sm + PrSmem::oCz) + (kk & 1) * 256; };
+  float *cxh = reinterpret_cast<float *>(sm + PrSmem::oCx);
+  float *cyh = reinterpret_cast<float *>(sm + PrSmem::oCy);
   const int jlo = j0 == 0 ? g.ny - 1 : j0 - 1, jhi = j0 + kZY == g.ny ? 0 : j0 + kZY;
   const int ilo = i0 == 0 ? g.nx - 2 : i0 - 2, ihi = i0 + kZX == g.nx ? 0 : i0 + kZX;
   auto wz = [&](int kk) { return kk < 0 ? kk + g.nz : (kk >= g.nz ? kk - g.nz : kk); };
-  // the boxes of Rho_new plane kk (with its halo) into its slot
+  // the boxes of Rho_new plane kk (with its halo) into its raw slot
   auto load_rho = [&](int kk, uint64_t *b) {
-    unsigned char *d = rho_slot(kk);
+    unsigned char *d = rho_raw(kk);
     const int z = wz(kk);
     tma_load_3d(d + PrSmem::kRhoMain, &m.rho_t, b, i0, j0, z);
     tma_load_3d(d, &m.rho_r, b, i0, jlo, z);
@@ -769,45 +787,34 @@ k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restri
       s->timeout = 1;
     }
   };
-  // 1/Rho pairs of plane kk from its raw slot: [10][34] with the halo
+  // this thread's part of the halo of a plane: raw index and pair index
+  int h_raw = -1, h_at = 0;
+  if (tid < 32) {
+    h_raw = tid;  // row j0 - 1
+    h_at = tid + 1;
+  } else if (tid < 64) {
+    h_raw = 288 + tid - 32;  // row j0 + 8
+    h_at = 9 * 34 + tid - 32 + 1;
+  } else if (tid < 72) {
+    h_raw = 320 + 2 * (tid - 64) + 1;  // column i0 - 1: the second of the pair
+    h_at = (tid - 64 + 1) * 34;
+  } else if (tid < 80) {
+    h_raw = 336 + 2 * (tid - 72);  // column i0 + 32: the first of the pair
+    h_at = (tid - 72 + 1) * 34 + 33;
+  }
+  const int own = (ty + 1) * 34 + tx + 1;  // the owned cell in a pair plane
+  // Rho and 1/Rho pairs of plane kk (the owned cell and the halo part)
   auto convert = [&](int kk) {
-    const double *d = reinterpret_cast<const double *>(rho_slot(kk));
-    float2 *ir = ir_plane(kk);
-    for (int e = tid; e < 336; e += kZX * kZY) {
-      double v;
-      int at_;
-      if (e < 256) {  // main rows
-        v = d[32 + e];
-        at_ = (e / 32 + 1) * 34 + e % 32 + 1;
-      } else if (e < 288) {  // row j0 - 1
-        v = d[e - 256];
-        at_ = e - 256 + 1;
-      } else if (e < 320) {  // row j0 + 8
-        v = d[288 + e - 288];
-        at_ = 9 * 34 + e - 288 + 1;
-      } else if (e < 328) {  // column i0 - 1 (second of the pair)
-        v = d[320 + 2 * (e - 320) + 1];
-        at_ = (e - 320 + 1) * 34;
-      } else {  // column i0 + 32 (first of the pair)
-        v = d[336 + 2 * (e - 328)];
-        at_ = (e - 328 + 1) * 34 + 33;
-      }
-      ir[at_] = ff_rcp(ff_from_double(v));
+    const double *d = reinterpret_cast<const double *>(rho_raw(kk));
+    float2 *rp = rp_plane(kk), *ir = ir_plane(kk);
+    const float2 v = ff_from_double(d[32 + tid]);
+    rp[own] = v;
+    ir[own] = ff_rcp(v);
+    if (h_raw >= 0) {
+      const float2 w = ff_from_double(d[h_raw]);
+      rp[h_at] = w;
+      ir[h_at] = ff_rcp(w);
     }
-  };
-  // C = 1/Rho_face = 2 / (Rho_a + Rho_b) and the flux RU C, as pairs
-  auto face = [&](double ra, double rb, double ru, float2 &flux, float2 &C) {
-    const float2 h = ff_rcp(ff_add(ff_from_double(ra), ff_from_double(rb)));
-    C = make_float2(2.f * h.x, 2.f * h.y);
-    flux = ff_norm(ff_mul(ff_from_double(ru), C));
-  };
-  // z faces between planes kk - 1 and kk (the lower faces of plane kk)
-  auto zfaces = [&](int kk) {
-    const double *ra = reinterpret_cast<const double *>(rho_slot(kk) + PrSmem::kRhoMain);
-    const double *rb = reinterpret_cast<const double *>(rho_slot(kk - 1) + PrSmem::kRhoMain);
-    const double *ru = reinterpret_cast<const double *>(ruz_slot(kk));
-    float2 *f = fz(kk), *C = czp(kk);
-    for (int e = tid; e < 256; e += kZX * kZY) face(ra[e], rb[e], ru[e], f[e], C[e]);
   };
 
   if (tid == 0) {
@@ -833,12 +840,14 @@ k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restri
                            ff_from_double(g.inv_dz)};
   double acc = 0, usq = 0;
   int issued = 1;  // stages issued so far: the prologue (0) and stage 1
+  float2 fz_lo = make_float2(0.f, 0.f), cz_lo = fz_lo;  // the column's lower z face
   wait_stage(0);
   ok = __syncthreads_and(ok) != 0;  // every thread takes the same branch
   if (ok) {
     convert(k0 - 1);
     convert(k0);
-    zfaces(k0);
+    pr_face(rp_plane(k0)[own], rp_plane(k0 - 1)[own],
+            reinterpret_cast<const double *>(ruz_slot(k0))[tid], fz_lo, cz_lo);
   }
   __syncthreads();
   for (int k = k0; k < k1 && ok; ++k) {
@@ -856,35 +865,42 @@ k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restri
       break;
     }
     convert(k + 1);
-    {  // x and y faces of plane k, z faces of plane k + 1
-      const double *rk = reinterpret_cast<const double *>(rho_slot(k));
-      const double *ux = reinterpret_cast<const double *>(rux_slot(k));
-      const double *uy = reinterpret_cast<const double *>(ruy_slot(k));
-      for (int e = tid; e < 264; e += kZX * kZY) {
-        const int ey = e / 33, ex = e - ey * 33;
-        const double ra = ex < 32 ? rk[32 + ey * 32 + ex] : rk[336 + 2 * ey];
-        const double rb = ex > 0 ? rk[32 + ey * 32 + ex - 1] : rk[320 + 2 * ey + 1];
-        const double ru = ex < 32 ? ux[ey * 32 + ex] : ux[256 + 2 * ey];
-        face(ra, rb, ru, fx[e], cxp[e]);
+    // faces: lower x, y of the owned cell in plane k, lower z of plane k + 1
+    const float2 *rk = rp_plane(k);
+    float2 cx_lo, cy_lo, fz_hi, cz_hi;
+    {
+      float2 f;
+      pr_face(rk[own], rk[own - 1], reinterpret_cast<const double *>(rux_slot(k))[tid], f, cx_lo);
+      fx[ty * 33 + tx] = f;
+      cxh[ty * 33 + tx] = cx_lo.x;
+      pr_face(rk[own], rk[own - 34], reinterpret_cast<const double *>(ruy_slot(k))[tid], f, cy_lo);
+      fy[tid] = f;
+      cyh[tid] = cy_lo.x;
+      pr_face(rp_plane(k + 1)[own], rk[own],
+              reinterpret_cast<const double *>(ruz_slot(k + 1))[tid], fz_hi, cz_hi);
+      float2 C;
+      if (tid < 8) {  // x face at i0 + 32 of row tid
+        const int o = (tid + 1) * 34 + 33;
+        pr_face(rk[o], rk[o - 1], reinterpret_cast<const double *>(rux_slot(k))[256 + 2 * tid],
+                f, C);
+        fx[tid * 33 + 32] = f;
+        cxh[tid * 33 + 32] = C.x;
+      } else if (tid >= 32 && tid < 64) {  // y face at j0 + 8 of column tid - 32
+        const int o = 9 * 34 + tid - 32 + 1;
+        pr_face(rk[o], rk[o - 34], reinterpret_cast<const double *>(ruy_slot(k))[256 + tid - 32],
+                f, C);
+        fy[256 + tid - 32] = f;
+        cyh[256 + tid - 32] = C.x;
       }
-      for (int e = tid; e < 288; e += kZX * kZY) {
-        const int ey = e / 32, ex = e - ey * 32;
-        const double ra = rk[32 + ey * 32 + ex];  // row 8 is the j0 + 8 halo row
-        const double rb = ey > 0 ? rk[32 + (ey - 1) * 32 + ex] : rk[ex];
-        const double ru = uy[ey * 32 + ex];       // row 8 is the j0 + 8 halo row
-        face(ra, rb, ru, fy[e], cyp[e]);
-      }
-      zfaces(k + 1);
     }
     __syncthreads();
     {
       const int i = i0 + tx, j = j0 + ty;
       const long long c = at(g, i, j, k);
-      const float2 *irk = ir_plane(k), *irm = ir_plane(k - 1), *irp = ir_plane(k + 1);
-      const int o = (ty + 1) * 34 + tx + 1;
-      const float2 ir = irk[o];
-      const float2 pn[3] = {irk[o + 1], irk[o + 34], irp[o]};
-      const float2 mn[3] = {irk[o - 1], irk[o - 34], irm[o]};
+      const float2 *irk = ir_plane(k);
+      const float2 ir = irk[own];
+      const float2 pn[3] = {irk[own + 1], irk[own + 34], ir_plane(k + 1)[own]};
+      const float2 mn[3] = {irk[own - 1], irk[own - 34], ir_plane(k - 1)[own]};
       float2 lap = make_float2(0.f, 0.f);
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
@@ -896,12 +912,12 @@ k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restri
       const float2 dv = ff_add(ff_mul(kCp, lap), ff_mul(coef, Qc));
       if (a.store_div) divg[c] = ff_to_double(dv);
       float2 divu = make_float2(-dv.x, -dv.y);
+      const int ex = ty * (kZX + 1) + tx;
+      const float2 ulo[3] = {fx[ex], fy[tid], fz_lo};
+      const float2 uhi[3] = {fx[ex + 1], fy[tid + kZX], fz_hi};
+      const float2 clo[3] = {cx_lo, cy_lo, cz_lo};
+      const float chi[3] = {cxh[ex + 1], cyh[tid + kZX], cz_hi.x};
       float msum = 0.f;
-      const int ex = ty * (kZX + 1) + tx, ey = ty * kZX + tx;
-      const float2 ulo[3] = {fx[ex], fy[ey], fz(k)[ey]};
-      const float2 uhi[3] = {fx[ex + 1], fy[ey + kZX], fz(k + 1)[ey]};
-      const float2 clo[3] = {cxp[ex], cyp[ey], czp(k)[ey]};
-      const float chi[3] = {cxp[ex + 1].x, cyp[ey + kZX].x, czp(k + 1)[ey].x};
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         divu = ff_add(divu, ff_mul(ff_sub(uhi[d], ulo[d]), inv_d[d]));
@@ -917,7 +933,9 @@ k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restri
       acc += rhs;
       cc32[c] = -3.0f / msum;
     }
-    __syncthreads();  // the slots and faces of plane k are refilled next
+    fz_lo = fz_hi;
+    cz_lo = cz_hi;
+    __syncthreads();  // the slots, pair planes and faces of plane k are refilled next
   }
   if (!ok && tid == 0) {
     // a wait gave up: let the copies of the last two stages issued land
@@ -929,7 +947,6 @@ k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restri
   double bs = block_sum(acc, red);
   if (tid == 0) partials[blockIdx.x] = bs;
   if (tke_parts) {
-    __syncthreads();
     double bu = block_sum(usq, red);
     if (tid == 0) tke_parts[blockIdx.x] = bu;
   }
@@ -1086,39 +1103,39 @@ __global__ void k_finish_means3(const double *__restrict__ partials, int nparts,
   }
 }
 
-// FP64 post-projection divergence residual of the mixed path:
+// Post-projection divergence residual of the mixed path:
 // res = div_F2C(RU_new * C) - divergence - dt*pre*mean(RHS_Pois), with
-// C = 1/Rho_face(Rho_new) from k_poisson_rhs.  A converged projection gives
-// res = 0 (grid.cpp:841-863): div u_new = divergence + dt*pre*mean.
-// C = 1/Rho_face on a face from the densities of its two cells, as the
-// mixed path's face coefficients are formed (pairs, 2 rcp(Rho_a + Rho_b)),
-// rounded to a double
-__device__ __forceinline__ double face_c(double ra, double rb) {
-  const float2 h = ff_rcp(ff_add(ff_from_double(ra), ff_from_double(rb)));
-  return ff_to_double(make_float2(2.f * h.x, 2.f * h.y));
-}
-
+// C = 1/Rho_face(Rho_new).  A converged projection gives res = 0
+// (grid.cpp:841-863): div u_new = divergence + dt*pre*mean.  Formed to FP64
+// accuracy in float-float pairs on the FP32 pipe: the face
+// coefficients of this stage are the pairs C/d^2 the Poisson right-hand side
+// pass wrote (Cs2, formed from this stage's Rho_new), so
+// div(RU C) = sum_d d (RU_p Cs2_p - RU_c Cs2_c); each flux pair carries about
+// 2^-46 of its value, far below the 1e-10 the residual is held to.  Two FP64
+// operations per cell (the constraint and its mean offset) instead of the
+// FP64 fluxes.
 __global__ void k_div_residual(Grid g, const double *__restrict__ RUn,
-                               const double *__restrict__ Rho_new,
+                               const float2 *__restrict__ Cs2,
                                const double *__restrict__ divg, const DevScalars *__restrict__ s,
                                double dtpre, double *__restrict__ partials) {
   __shared__ double sh[kThreads];
   const double off = dtpre * s->mean_rhs;
-  const double inv_d[3] = {g.inv_dx, g.inv_dy, g.inv_dz};
+  const float2 dd[3] = {ff_from_double(g.dx), ff_from_double(g.dy), ff_from_double(g.dz)};
   double mx = 0;
   for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < g.n;
        c += (long long)gridDim.x * blockDim.x) {
     Cell q = cell_of(g, c);
     Nbr nb = nbr_of(g, q);
-    const double rc = Rho_new[c];
-    double dv = 0;
+    float2 dv = ff_from_double(-(divg[c] + off));
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       const double *R = RUn + d * g.n;
-      const double cp = face_c(Rho_new[nb.p[d]], rc), cm = face_c(rc, Rho_new[nb.m[d]]);
-      dv += (R[nb.p[d]] * cp - R[c] * cm) * inv_d[d];
+      const float2 *C = Cs2 + d * g.n;
+      const float2 fp = ff_mul(ff_from_double(R[nb.p[d]]), C[nb.p[d]]);
+      const float2 fc = ff_mul(ff_from_double(R[c]), C[c]);
+      dv = ff_add(dv, ff_mul(ff_sub(ff_norm(fp), ff_norm(fc)), dd[d]));
     }
-    double r = fabs(dv - divg[c] - off);
+    const double r = fabs(ff_to_double(dv));
     mx = r > mx ? r : mx;
   }
   double b = block_max(mx, sh);
@@ -1453,7 +1470,7 @@ void launch_passive_scalar_face(tpm_ctx *c, const double *src) {
 
 void launch_div_residual(tpm_ctx *c, int s) {
   const int nb = cell_waves(c, k_div_residual, true);
-  TPM_LAUNCH(c, "div_residual", k_div_residual, nb, kThreads, 0, c->g, c->RU_new, c->Rho_new,
+  TPM_LAUNCH(c, "div_residual", k_div_residual, nb, kThreads, 0, c->g, c->RU_new, c->Cs2,
              c->divg, c->dsc, c->p.dt * kPre[s], c->partials + kPartDiv * kRedBlocks);
   TPM_LAUNCH(c, "finish_max_div", k_finish_max_div, 1, kThreads, 0,
              c->partials + kPartDiv * kRedBlocks, nb, c->dsc);
