@@ -419,7 +419,7 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     TPM_CUDA_TRY(cudaGetDevice(&c->dev));
     TPM_CUDA_TRY(cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->dev));
     Grid &g = c->g;
-    g.nx = p->Nx; g.ny = p->Ny; g.nz = p->Nz; g.nxh = p->Nx / 2 + 1; g.n = n;
+    g.nx = p->Nx; g.ny = p->Ny; g.nz = p->Nz; g.nxh = p->Nx / 2 + 1; g.sxh = g.nxh; g.n = n;
     g.mx = tpm::udiv_magic((unsigned)p->Nx); g.my = tpm::udiv_magic((unsigned)p->Ny);
     g.Lx = p->Lx; g.Ly = p->Ly; g.Lz = p->Lz;
     g.dx = p->Lx / p->Nx; g.dy = p->Ly / p->Ny; g.dz = p->Lz / p->Nz;  // gridsize.cpp:25-27

@@ -26,6 +26,7 @@
 #include "tpm_internal.cuh"
 #include "tpm_ff.cuh"
 #include "tpm_reduce.cuh"
+#include "tpm_tma.cuh"
 
 namespace tpm {
 namespace {
@@ -204,7 +205,7 @@ __device__ __forceinline__ void dft16(T2 *v, int sign) {
 template <int R, typename T2>
 __device__ __forceinline__ void stockham_stage(const T2 *__restrict__ a, T2 *__restrict__ b,
                                                int lq, const FftPlan &pl, int p, unsigned pm,
-                                               int sign) {
+                                               int sign, const T2 *__restrict__ tws) {
   const int n = pl.n;
   const int m = n / R;
   const int step = n / (p * R);
@@ -223,7 +224,8 @@ __device__ __forceinline__ void stockham_stage(const T2 *__restrict__ a, T2 *__r
     } else {
 #pragma unroll
       for (int t = 1; t < R; ++t)
-        v[t] = cmul(a[(i + t * m) * npen + q], Cx<T2>::tw(pl, k * t * step), sign);
+        v[t] = cmul(a[(i + t * m) * npen + q],
+                    tws ? tws[k * t * step] : Cx<T2>::tw(pl, k * t * step), sign);
     }
     dft_small(v, R, sign);
     const int j = ip * p * R + k;
@@ -237,7 +239,8 @@ __device__ __forceinline__ void stockham_stage(const T2 *__restrict__ a, T2 *__r
 // of two.  Returns the buffer (a or b) that holds the result.  Ends with
 // __syncthreads().
 template <typename T2>
-__device__ T2 *smem_fft(T2 *a, T2 *b, int npen, const FftPlan &pl, int sign) {
+__device__ T2 *smem_fft(T2 *a, T2 *b, int npen, const FftPlan &pl, int sign,
+                        const T2 *tws = nullptr) {
   const int lq = __ffs(npen) - 1;
   int p = 1;
   for (int s = 0; s < pl.nst; ++s) {
@@ -245,19 +248,19 @@ __device__ T2 *smem_fft(T2 *a, T2 *b, int npen, const FftPlan &pl, int sign) {
     const unsigned pm = pl.pmag[s];
     if constexpr (sizeof(T2) == sizeof(float2)) {  // radices 16 and 8: FP32 plans only
       if (R == 16) {
-        stockham_stage<16>(a, b, lq, pl, p, pm, sign);
+        stockham_stage<16>(a, b, lq, pl, p, pm, sign, tws);
         goto staged;
       }
       if (R == 8) {
-        stockham_stage<8>(a, b, lq, pl, p, pm, sign);
+        stockham_stage<8>(a, b, lq, pl, p, pm, sign, tws);
         goto staged;
       }
     }
     switch (R) {
-      case 4: stockham_stage<4>(a, b, lq, pl, p, pm, sign); break;
-      case 2: stockham_stage<2>(a, b, lq, pl, p, pm, sign); break;
-      case 3: stockham_stage<3>(a, b, lq, pl, p, pm, sign); break;
-      default: stockham_stage<5>(a, b, lq, pl, p, pm, sign); break;
+      case 4: stockham_stage<4>(a, b, lq, pl, p, pm, sign, tws); break;
+      case 2: stockham_stage<2>(a, b, lq, pl, p, pm, sign, tws); break;
+      case 3: stockham_stage<3>(a, b, lq, pl, p, pm, sign, tws); break;
+      default: stockham_stage<5>(a, b, lq, pl, p, pm, sign, tws); break;
     }
   staged:
     __syncthreads();
@@ -296,7 +299,7 @@ __device__ __forceinline__ void r2c_store(const Grid &g, const T2 *z, int npen, 
     T2 w = r2c_tw[kx];
     T xr = Cx<T2>::fma_(w.x, for_, Cx<T2>::fma_(-w.y, foi, fer));
     T xi = Cx<T2>::fma_(w.x, foi, Cx<T2>::fma_(w.y, for_, fei));
-    spec[row * nxh + kx] = Cx<T2>::mk(xr, xi);
+    spec[row * g.sxh + kx] = Cx<T2>::mk(xr, xi);
   }
 }
 
@@ -473,15 +476,15 @@ __global__ void k_fft_y(Grid g, FftPlan pl, T2 *__restrict__ spec, int npen, int
   T2 *b = a + pl.n * npen;
   const int tiles = (g.nxh + npen - 1) / npen;
   const int kz = blockIdx.x / tiles, kx0 = (blockIdx.x % tiles) * npen;
-  const long long base = (long long)kz * g.ny * g.nxh;
+  const long long base = (long long)kz * g.ny * g.sxh;
   tile_load<8>(a, npen * g.ny, lq, [&](int q, int ky) {
-    return (kx0 + q < g.nxh) ? spec[base + (long long)ky * g.nxh + kx0 + q] : Cx<T2>::mk(0, 0);
+    return (kx0 + q < g.nxh) ? spec[base + (long long)ky * g.sxh + kx0 + q] : Cx<T2>::mk(0, 0);
   });
   __syncthreads();
   T2 *r = smem_fft(a, b, npen, pl, sign);
   for (int idx = threadIdx.x; idx < npen * g.ny; idx += blockDim.x) {
     const int q = idx & (npen - 1), ky = idx >> lq;
-    if (kx0 + q < g.nxh) spec[base + (long long)ky * g.nxh + kx0 + q] = r[ky * npen + q];
+    if (kx0 + q < g.nxh) spec[base + (long long)ky * g.sxh + kx0 + q] = r[ky * npen + q];
   }
 }
 
@@ -530,8 +533,8 @@ __global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const d
   T2 *b = a + pl.n * npen;
   const int tiles = (g.nxh + npen - 1) / npen;
   const int ky = blockIdx.x / tiles, kx0 = (blockIdx.x % tiles) * npen;
-  const long long plane = (long long)g.ny * g.nxh;
-  const long long base = (long long)ky * g.nxh + kx0;
+  const long long plane = (long long)g.ny * g.sxh;
+  const long long base = (long long)ky * g.sxh + kx0;
   const int tot = npen * g.nz;
   // the first kInvPre reciprocals of each thread's modes, loaded before the
   // pencils so that their latency hides behind the loads and the forward FFT
@@ -593,6 +596,154 @@ __global__ void k_fft_z_solve(Grid g, FftPlan pl, T2 *__restrict__ spec, const d
   }
 }
 
+// ------------------------------------- 2.-4. y and z passes fed by the TMA
+// Mixed path, pencils of at most 256 points: the y pass and the z pass (with
+// the wave-number divide between its forward and inverse transforms) on tiles
+// of 8 pencils moved by the tensor memory accelerator.  The blocks are
+// persistent: each walks its share of the tiles, and while it transforms one
+// tile the next one's box is already being loaded (cp.async.bulk.tensor into
+// the other of two tile buffers, completion counted on that buffer's
+// mbarrier); the result box goes back by a bulk tensor store that runs while
+// the next tile is waited for.  A tile lands as [points][8 pencils], exactly
+// the layout the Stockham stages read.  The bulk store skips the elements past
+// the half spectrum's Nx/2 + 1 columns, so the last, partial tile needs no
+// special case, and the spectrum's rows are padded to an even number of
+// float2 so that a row is a 16-byte multiple, as a tensor map requires.
+// Every wait is bounded (a timeout is recorded for the host).
+constexpr int kTmaPens = 8;
+
+// bytes of one tile buffer of n points, rounded to the 128-byte alignment a
+// TMA box destination needs
+__host__ __device__ __forceinline__ int tma_tile_bytes(int n) {
+  return (n * kTmaPens * (int)sizeof(float2) + 127) & ~127;
+}
+
+// dynamic shared memory of k_fft_yz_tma: two tile buffers, the scratch
+// buffer, the n twiddles (an eighth of a tile, 128-byte rounded) and two
+// mbarriers
+__host__ __device__ __forceinline__ size_t tma_yz_smem(int n) {
+  return 3 * (size_t)tma_tile_bytes(n) + tma_tile_bytes(n) / kTmaPens + 16;
+}
+
+template <bool kZ>
+__global__ void __launch_bounds__(256)
+k_fft_yz_tma(Grid g, FftPlan pl, const __grid_constant__ CUtensorMap map, int sign,
+             const float *__restrict__ inv_mwn, const int *__restrict__ skip,
+             DevScalars *__restrict__ s, int ntiles) {
+  if (skip && *skip) return;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int tb = tma_tile_bytes(pl.n);
+  auto buf = [&](int slot) { return reinterpret_cast<float2 *>(sm + slot * tb); };
+  float2 *scratch = reinterpret_cast<float2 *>(sm + 2 * tb);
+  float2 *tw = reinterpret_cast<float2 *>(sm + 3 * tb);  // the plan's twiddles, n entries
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sm + 3 * tb + tma_tile_bytes(pl.n) / kTmaPens);
+  constexpr int lq = 3;  // log2(kTmaPens)
+  const int tiles = (g.nxh + kTmaPens - 1) / kTmaPens;
+  const unsigned bytes = (unsigned)(pl.n * kTmaPens * sizeof(float2));
+  const int tot = kTmaPens * pl.n;
+  if (smem_u32(sm) & 127u) {  // never issue a box to a misaligned address
+    if (threadIdx.x == 0) s->timeout = 1;
+    return;
+  }
+  // box coordinates of tile t: y pass (kx0, 0, kz), z pass (kx0, ky, 0)
+  auto coords = [&](int t, int &x, int &y, int &z) {
+    const int outer = t / tiles;
+    x = (t - outer * tiles) * kTmaPens;
+    y = kZ ? outer : 0;
+    z = kZ ? 0 : outer;
+  };
+  auto load = [&](int t, int slot) {
+    int x, y, z;
+    coords(t, x, y, z);
+    mbar_arrive_expect_tx(&bar[slot], bytes);
+    tma_load_3d(buf(slot), &map, &bar[slot], x, y, z);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init_fence();
+    if ((int)blockIdx.x < ntiles) load(blockIdx.x, 0);
+  }
+  // the twiddles in shared memory for all of the block's tiles (a block with
+  // one tile reads them from the plan: the copy would cost more than it saves)
+  const bool one_tile = (int)gridDim.x >= ntiles;
+  if (!one_tile)
+    for (int m = threadIdx.x; m < pl.n; m += blockDim.x) tw[m] = pl.tw32[m];
+  const float2 *tws = one_tile ? nullptr : tw;
+  __syncthreads();
+  // a transform ends in its input buffer after an even number of Stockham
+  // stages (the z pass runs two transforms of the same plan): then the store
+  // of a tile reads only that tile's buffer, which the load two tiles later
+  // refills, and only the thread that issues both waits for the store; else
+  // (a y pass with an odd number of stages) the store reads the scratch buffer
+  // the next transform writes, and the block waits for it
+  const bool store_from_scratch = !kZ && (pl.nst & 1);
+  bool ok = true;
+  int it = 0;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
+    const int slot = it & 1;
+    if (threadIdx.x == 0) bulk_wait_read_all();  // the last store has read its buffer
+    if (store_from_scratch) __syncthreads();
+    if (threadIdx.x == 0 && t + (int)gridDim.x < ntiles) load(t + gridDim.x, slot ^ 1);
+    int x, y, z;
+    coords(t, x, y, z);
+    // z pass: the reciprocals of this thread's modes (the table of
+    // k_inv_mwn), loaded while the tile is in flight
+    constexpr int kInv = 8;  // tot <= 8 * 256 = kInv * blockDim.x
+    float invr[kInv];
+    if constexpr (kZ) {
+#pragma unroll
+      for (int u = 0; u < kInv; ++u) {
+        const int idx = threadIdx.x + u * (int)blockDim.x;
+        const int q = idx & (kTmaPens - 1), kz = idx >> lq;
+        invr[u] = (idx < tot && x + q < g.nxh)
+                      ? inv_mwn[((long long)kz * g.ny + y) * g.nxh + x + q]
+                      : 0.f;
+      }
+    }
+    ok = mbar_wait(&bar[slot], (unsigned)(it >> 1) & 1u);
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    float2 *r = smem_fft(buf(slot), scratch, kTmaPens, pl, kZ ? -1 : sign, tws);
+    if constexpr (kZ) {
+      float2 *other = (r == scratch) ? buf(slot) : scratch;
+      // divide by the modified wave number except the zero mode (poisson.cpp:442-449)
+#pragma unroll
+      for (int u = 0; u < kInv; ++u) {
+        const int idx = threadIdx.x + u * (int)blockDim.x;
+        const int q = idx & (kTmaPens - 1), kz = idx >> lq;
+        const int kx = x + q;
+        if (idx < tot && kx < g.nxh && (kx + y + kz) > 0) {
+          float2 v = r[kz * kTmaPens + q];
+          v.y = v.y * invr[u];
+          v.x = v.x * invr[u];
+          r[kz * kTmaPens + q] = v;
+        }
+      }
+      __syncthreads();
+      r = smem_fft(r, other, kTmaPens, pl, +1, tws);
+    }
+    fence_proxy_async();  // the transform's shared-memory writes, before the bulk store reads them
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tma_store_3d(&map, r, x, y, z);
+      bulk_commit();
+    }
+  }
+  if (threadIdx.x == 0) {
+    if (!ok) {
+      s->timeout = 1;
+      // let the loads still in flight land (bounded) before the block's
+      // shared memory is released
+      mbar_wait(&bar[it & 1], (unsigned)(it >> 1) & 1u);
+      mbar_wait(&bar[(it + 1) & 1], (unsigned)((it + 1) >> 1) & 1u);
+    }
+    bulk_wait_read_all();
+  }
+}
+
 // A block's max|dp| (>= 0): into the iteration's accumulator by an atomic
 // maximum on the bits (non-negative doubles order as their bit patterns, and
 // a maximum does not depend on the order the blocks arrive in), or into the
@@ -623,7 +774,7 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   T2 *b = a + M * npen;
   const long long nrows = (long long)g.ny * g.nz;
   const long long row0 = (long long)blockIdx.x * npen;
-  const int nxh = g.nxh;
+  const int sxh = g.sxh;
   // Z[k] = (X[k] + conj X[M-k]) + i (X[k] - conj X[M-k]) W^-k, k < M;
   // kB elements' loads in flight per thread before their stores
   constexpr int kB = 4;
@@ -635,8 +786,8 @@ __global__ void k_xinv_update(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
       const int q = fdiv(idx, pl.nmag), kx = idx - q * M;
       const long long row = row0 + q;
       const bool ok = idx < npen * M && row < nrows;
-      X[u] = ok ? spec[row * nxh + kx] : Cx<T2>::mk(0, 0);
-      Y[u] = ok ? spec[row * nxh + (M - kx)] : Cx<T2>::mk(0, 0);
+      X[u] = ok ? spec[row * sxh + kx] : Cx<T2>::mk(0, 0);
+      Y[u] = ok ? spec[row * sxh + (M - kx)] : Cx<T2>::mk(0, 0);
       W[u] = ok ? r2c_tw[kx] : Cx<T2>::mk(0, 0);  // exp(-2 pi i k / nx); use its conjugate
     }
 #pragma unroll
@@ -913,6 +1064,35 @@ void fft_plans_create(tpm_ctx *c) {
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_fft_y<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_fft_z_solve<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
   TPM_CUDA_TRY(cudaFuncSetAttribute(k_xinv_update<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem64));
+  // the Richardson loop's spectrum: FP64 rows of Nx/2 + 1 double2; on the
+  // mixed path rows of an even number of float2 (the buffer holds double2
+  // rows, so the padded float2 rows fit), and where the pencils of the y and z
+  // passes fit one TMA box (at most 256 points) the tile maps of those passes
+  c->spec_pitch = g.nxh;
+  c->tma_fft = false;
+  if (c->p.precision == TPM_PREC_MIXED) {
+    c->spec_pitch = g.nxh + (g.nxh & 1);
+    if (g.ny <= 256 && g.nz <= 256 &&
+        make_tensor_map_8b(&c->fft_map_y, c->spec, g.nxh, g.ny, g.nz, c->spec_pitch, kTmaPens,
+                           g.ny, 1) &&
+        make_tensor_map_8b(&c->fft_map_z, c->spec, g.nxh, g.ny, g.nz, c->spec_pitch, kTmaPens, 1,
+                           g.nz)) {
+      // persistent blocks: as many as stay resident (SMs x blocks per SM)
+      const int ns[2] = {c->fy32.n, c->fz32.n};
+      const void *kern[2] = {reinterpret_cast<const void *>(k_fft_yz_tma<false>),
+                             reinterpret_cast<const void *>(k_fft_yz_tma<true>)};
+      bool fits = true;
+      for (int d = 0; d < 2; ++d) {
+        const int smem = (int)tma_yz_smem(ns[d]);
+        TPM_CUDA_TRY(cudaFuncSetAttribute(kern[d], cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        int per_sm = 0;
+        TPM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern[d], 256, smem));
+        c->tma_fft_blocks[d] = per_sm * (c->sms > 0 ? c->sms : 1);
+        fits = fits && per_sm > 0;
+      }
+      c->tma_fft = fits;
+    }
+  }
 }
 
 // One Richardson iteration of poisson::FFT (poisson.cpp:397-409).  Inputs:
@@ -926,7 +1106,8 @@ void fft_plans_create(tpm_ctx *c) {
 // (refine_finish).
 template <typename T2>
 static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop) {
-  const Grid &g = c->g;
+  Grid g = c->g;
+  g.sxh = c->spec_pitch;  // the loop's spectrum rows (padded on the mixed path)
   constexpr bool f32 = sizeof(T2) == sizeof(float2);
   const FftPlan &plx = f32 ? c->fx32 : c->fx, &ply = f32 ? c->fy32 : c->fy,
                 &plz = f32 ? c->fz32 : c->fz;
@@ -947,22 +1128,35 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
       TPM_LAUNCH(c, "fft_x_fwd_resid", k_xfwd_resid<T2>, xblocks, tx, smem, g, plx, r2c,
                  c->P, c->Cface, c->cc, c->RHS, c->dsc, spec, npx);
   }
-  {
+  const int tma_tiles = (g.nxh + kTmaPens - 1) / kTmaPens;
+  auto y_pass = [&](int sign) {
+    if (f32 && c->tma_fft) {
+      const int ntiles = g.nz * tma_tiles;
+      TPM_LAUNCH(c, "fft_y", k_fft_yz_tma<false>, std::min(ntiles, c->tma_fft_blocks[0]), 256,
+                 tma_yz_smem(ply.n), g, ply, c->fft_map_y, sign,
+                 static_cast<const float *>(nullptr), skip, c->dsc, ntiles);
+      return;
+    }
     int blocks = g.nz * ((g.nxh + npy - 1) / npy);
     size_t smem = 2 * (size_t)npy * ply.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, ty, smem, g, ply, spec, npy, -1, skip);
-  }
-  {
+    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, ty, smem, g, ply, spec, npy, sign, skip);
+  };
+  y_pass(-1);
+  if (f32 && c->tma_fft) {
+    const int ntiles = g.ny * tma_tiles;
+    // (one tile per block: the z pass's two transforms give its blocks enough
+    // work between loads, and its tiles load while other blocks compute;
+    // persistent blocks measured the same, 1.05 ms per 256^3 step)
+    TPM_LAUNCH(c, "fft_z_solve", k_fft_yz_tma<true>, ntiles, 256,
+               tma_yz_smem(plz.n), g, plz, c->fft_map_z, -1,
+               static_cast<const float *>(c->inv_mwn), skip, c->dsc, ntiles);
+  } else {
     int blocks = g.ny * ((g.nxh + npz - 1) / npz);
     size_t smem = 2 * (size_t)npz * plz.n * sizeof(T2);
     TPM_LAUNCH(c, "fft_z_solve", k_fft_z_solve<T2>, blocks, tz, smem, g, plz, spec,
                c->ax, c->ay, c->az, static_cast<const typename Cx<T2>::T *>(c->inv_mwn), npz, skip);
   }
-  {
-    int blocks = g.nz * ((g.nxh + npy - 1) / npy);
-    size_t smem = 2 * (size_t)npy * ply.n * sizeof(T2);
-    TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, ty, smem, g, ply, spec, npy, +1, skip);
-  }
+  y_pass(+1);
   {
     size_t smem = 2 * (size_t)npx * plx.n * sizeof(T2);
     double *parts = c->err_parts;
@@ -1144,14 +1338,13 @@ __global__ void k_pc_xinv(Grid g, FftPlan pl, const T2 *__restrict__ r2c_tw,
   T2 *b = a + M * npen;
   const long long nrows = (long long)g.ny * g.nz;
   const long long row0 = (long long)blockIdx.x * npen;
-  const int nxh = g.nxh;
   for (int idx = threadIdx.x; idx < npen * M; idx += blockDim.x) {
     const int q = fdiv(idx, pl.nmag), kx = idx - q * M;
     const long long row = row0 + q;
     T2 Z = Cx<T2>::mk(0, 0);
     if (row < nrows) {
-      T2 X = spec[row * nxh + kx];
-      T2 Y = spec[row * nxh + (M - kx)];
+      T2 X = spec[row * g.sxh + kx];
+      T2 Y = spec[row * g.sxh + (M - kx)];
       Y.y = -Y.y;
       T fer = X.x + Y.x, fei = X.y + Y.y;
       T dr = X.x - Y.x, di = X.y - Y.y;
@@ -1322,7 +1515,7 @@ extern "C" int tpm_poisson_solve_noalloc(int Nx, int Ny, int Nz, double Lx, doub
       Nx / 2 > 2048 || Ny > 2048 || Nz > 2048 || !(Lx > 0) || !(Ly > 0) || !(Lz > 0))
     return TPM_ERR_ARG;
   Grid g;
-  g.nx = Nx; g.ny = Ny; g.nz = Nz; g.nxh = Nx / 2 + 1;
+  g.nx = Nx; g.ny = Ny; g.nz = Nz; g.nxh = Nx / 2 + 1; g.sxh = g.nxh;
   g.n = (long long)Nx * Ny * Nz;
   g.mx = tpm::udiv_magic((unsigned)Nx); g.my = tpm::udiv_magic((unsigned)Ny);
   g.Lx = Lx; g.Ly = Ly; g.Lz = Lz;

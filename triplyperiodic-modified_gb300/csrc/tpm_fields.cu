@@ -144,6 +144,50 @@ __device__ __forceinline__ Nbr nbr_of(const Grid &g, const Cell &q) {
 // each value is loaded from global memory once per column instead of once
 // per stencil use.
 constexpr int kZX = 32, kZY = 8;  // column tile; the z chunk is zm_zlen planes
+
+// The FP32 momentum right-hand side of one cell, all three components, from
+// its stencil values V(f, dx, dy, dz) (f 0-2 the face velocity U, 3-5 RU_int,
+// at the offset (dx, dy, dz) from the cell) and its F_p: per component d
+// (grid.cpp:785-803) -mp/Vcell F_p + Mu0/3 grad_C2F(div U) + Mu0 Del2(U_d)
+// - Div_F2C(P_{d,e}) + A RU_int, the fluxes P_{d,e} = I_e(U_d) I_d(RU_e), in
+// the reference's operation order (the body force is the caller's).
+template <typename VF>
+__device__ __forceinline__ void momentum_rhs(const VF &V, const float fp[3], const float inv_d[3],
+                                             const float inv_d2[3], float a_fp, float b_gd,
+                                             float c_lap, float A_, float rhs[3]) {
+  auto divU = [&](int ox, int oy, int oz) -> float {
+    return (V(0, ox + 1, oy, oz) - V(0, ox, oy, oz)) * inv_d[0] +
+           (V(1, ox, oy + 1, oz) - V(1, ox, oy, oz)) * inv_d[1] +
+           (V(2, ox, oy, oz + 1) - V(2, ox, oy, oz)) * inv_d[2];
+  };
+  const float div_c = divU(0, 0, 0);
+  const float div_m[3] = {divU(-1, 0, 0), divU(0, -1, 0), divU(0, 0, -1)};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float gd = (div_c - div_m[d]) * inv_d[d];
+    const float ud = V(d, 0, 0, 0);
+    const float lap = (V(d, 1, 0, 0) - 2 * ud + V(d, -1, 0, 0)) * inv_d2[0] +
+                      (V(d, 0, 1, 0) - 2 * ud + V(d, 0, -1, 0)) * inv_d2[1] +
+                      (V(d, 0, 0, 1) - 2 * ud + V(d, 0, 0, -1)) * inv_d2[2];
+    float r = a_fp * fp[d] + b_gd * gd + c_lap * lap;
+    // flux P_{d,e} at (ox, oy, oz): I_e(U_d) * I_d(RU_e)
+    auto flux = [&](int e, int ox, int oy, int oz) -> float {
+      const int ex = e == 0, ey = e == 1, ez = e == 2;
+      const int dx = d == 0, dy = d == 1, dz = d == 2;
+      const float iu = (V(d, ox, oy, oz) + V(d, ox - ex, oy - ey, oz - ez)) * 0.5f;
+      const float ir = (V(3 + e, ox, oy, oz) + V(3 + e, ox - dx, oy - dy, oz - dz)) * 0.5f;
+      return iu * ir;
+    };
+    float t[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e)
+      t[e] = (flux(e, e == 0, e == 1, e == 2) - flux(e, 0, 0, 0)) * inv_d[e];
+    const float conv = t[0] + t[1] + t[2];
+    r -= conv;
+    r += A_ * V(3 + d, 0, 0, 0);
+    rhs[d] = r;
+  }
+}
 constexpr int kZPX = kZX + 2, kZPY = kZY + 2, kZPlane = kZPX * kZPY;
 
 __global__ void __launch_bounds__(kZX * kZY)
@@ -201,44 +245,21 @@ k_rhs_momentum_zm(Grid g, const float *__restrict__ U, const float *__restrict__
       auto V = [&](int f, int dx, int dy, int dz) -> float {
         return sp[slot_of[dz + 1]][f][(ty + 1 + dy) * kZPX + tx + 1 + dx];
       };
-      auto divU = [&](int ox, int oy, int oz) -> float {
-        return (V(0, ox + 1, oy, oz) - V(0, ox, oy, oz)) * inv_d[0] +
-               (V(1, ox, oy + 1, oz) - V(1, ox, oy, oz)) * inv_d[1] +
-               (V(2, ox, oy, oz + 1) - V(2, ox, oy, oz)) * inv_d[2];
-      };
-      const float div_c = divU(0, 0, 0);
-      const float div_m[3] = {divU(-1, 0, 0), divU(0, -1, 0), divU(0, 0, -1)};
       const long long c = at(g, i, j, k);
       const long long cm[3] = {at(g, wrap_m(i, g.nx), j, k), at(g, i, wrap_m(j, g.ny), k),
                                at(g, i, j, wrap_m(k, g.nz))};
+      float fp[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) fp[d] = Fp[d * g.n + c];
+      float rhs[3];
+      momentum_rhs(V, fp, inv_d, inv_d2, a_fp, b_gd, c_lap, A_, rhs);
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        const float gd = (div_c - div_m[d]) * inv_d[d];
-        const float ud = V(d, 0, 0, 0);
-        const float lap = (V(d, 1, 0, 0) - 2 * ud + V(d, -1, 0, 0)) * inv_d2[0] +
-                          (V(d, 0, 1, 0) - 2 * ud + V(d, 0, -1, 0)) * inv_d2[1] +
-                          (V(d, 0, 0, 1) - 2 * ud + V(d, 0, 0, -1)) * inv_d2[2];
-        float rhs = a_fp * Fp[d * g.n + c] + b_gd * gd + c_lap * lap;
-        // flux P_{d,e} at (ox, oy, oz): I_e(U_d) * I_d(RU_e)
-        auto flux = [&](int e, int ox, int oy, int oz) -> float {
-          const int ex = e == 0, ey = e == 1, ez = e == 2;
-          const int dx = d == 0, dy = d == 1, dz = d == 2;
-          const float iu = (V(d, ox, oy, oz) + V(d, ox - ex, oy - ey, oz - ez)) * 0.5f;
-          const float ir = (V(3 + e, ox, oy, oz) + V(3 + e, ox - dx, oy - dy, oz - dz)) * 0.5f;
-          return iu * ir;
-        };
-        float t[3];
-#pragma unroll
-        for (int e = 0; e < 3; ++e)
-          t[e] = (flux(e, e == 0, e == 1, e == 2) - flux(e, 0, 0, 0)) * inv_d[e];
-        const float conv = t[0] + t[1] + t[2];
-        rhs -= conv;
-        rhs += A_ * V(3 + d, 0, 0, 0);
         if (a.has_g) {
           const float rf = (ff_cast<float>(Rho_int[c]) + ff_cast<float>(Rho_int[cm[d]])) * 0.5f;
-          rhs += (rf - Rho0) * gv[d];
+          rhs[d] += (rf - Rho0) * gv[d];
         }
-        const double r64 = ff_widen(rhs);
+        const double r64 = ff_widen(rhs[d]);
         const double np1 = fma(a.dtpo, r64, np1_in[d * g.n + c]);
         RU_np1[d * g.n + c] = np1;
         RU_new[d * g.n + c] = (a.stage != 3) ? fma(a.dtpr, r64, RU[d * g.n + c]) : np1;
@@ -1270,8 +1291,8 @@ void launch_p0_update(tpm_ctx *c, int s) {
              c->p.dt * kPre[s], s, (int)c->np1_is_base);
 }
 
-bool make_tensor_map_f64(CUtensorMap *map, const double *base, int nx, int ny, long long nz,
-                         int bx, int by) {
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   static std::once_flag once;
   std::call_once(once, [] {
@@ -1282,15 +1303,32 @@ bool make_tensor_map_f64(CUtensorMap *map, const double *base, int nx, int ny, l
         q == cudaDriverEntryPointSuccess)
       encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   });
+  return encode;
+}
+
+bool encode_3d_8b(CUtensorMap *map, const void *base, long long nx, long long ny, long long nz,
+                  long long pitch, int bx, int by, int bz) {
+  PFN_cuTensorMapEncodeTiled_v12000 encode = tensor_map_encoder();
   if (!encode) return false;
   const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
-  const cuuint64_t strides[2] = {(cuuint64_t)nx * 8, (cuuint64_t)nx * ny * 8};
-  const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+  const cuuint64_t strides[2] = {(cuuint64_t)pitch * 8, (cuuint64_t)pitch * ny * 8};
+  const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, (cuuint32_t)bz};
   const cuuint32_t estr[3] = {1, 1, 1};
-  return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double *>(base), dims, strides,
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<void *>(base), dims, strides,
                 box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+}  // namespace
+
+bool make_tensor_map_f64(CUtensorMap *map, const double *base, int nx, int ny, long long nz,
+                         int bx, int by) {
+  return encode_3d_8b(map, base, nx, ny, nz, nx, bx, by, 1);
+}
+
+bool make_tensor_map_8b(CUtensorMap *map, const void *base, int nx, int ny, int nz, int pitch,
+                        int bx, int by, int bz) {
+  return encode_3d_8b(map, base, nx, ny, nz, pitch, bx, by, bz);
 }
 
 // the tensor maps of a device array, built on first use (host work only)

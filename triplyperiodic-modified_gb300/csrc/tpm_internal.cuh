@@ -29,6 +29,7 @@ constexpr double kPi = 3.141592653589793;  // params.h:5
 
 struct Grid {
   int nx, ny, nz, nxh;  // nxh = nx/2 + 1 (half spectrum)
+  int sxh;              // row pitch of the half spectrum in elements (>= nxh)
   long long n;          // cells
   unsigned long long mx, my;  // udiv_magic(nx), udiv_magic(ny)
   double dx, dy, dz;
@@ -268,6 +269,13 @@ struct tpm_ctx {
   // tensor maps of the arrays it reads
   bool tma_rhs = false;
   std::vector<tpm::TmaField> tma_fields;
+  // mixed path: the spectrum of the Richardson loop has rows padded to an
+  // even number of float2 (a 16-byte multiple) so that the y and z pencil
+  // passes move their tiles by TMA (tensor maps of the y and z tiles)
+  int spec_pitch = 0;
+  bool tma_fft = false;
+  int tma_fft_blocks[2] = {0, 0};  // persistent blocks of the y and z passes
+  CUtensorMap fft_map_y, fft_map_z;
 
   // ---- PCG pressure solve (Solver = 2; allocated on first use) ----
   double *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr;

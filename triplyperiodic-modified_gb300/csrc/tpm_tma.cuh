@@ -85,6 +85,26 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, u
       : "memory");
 }
 
+// box of `map` at (x, y, z) from shared memory at src, in the bulk group of
+// this thread (elements out of the array's range are not written)
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, const void *src, int x, int y,
+                                             int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(
+          reinterpret_cast<uint64_t>(map)),
+      "r"(smem_u32(src)), "r"(x), "r"(y), "r"(z)
+      : "memory");
+}
+
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+
+// the bulk stores of this thread have read their shared-memory sources
+__device__ __forceinline__ void bulk_wait_read_all() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
 __device__ __forceinline__ void tma_prefetch_map(const CUtensorMap *map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
@@ -94,5 +114,9 @@ __device__ __forceinline__ void tma_prefetch_map(const CUtensorMap *map) {
 // the driver refuses it.
 bool make_tensor_map_f64(CUtensorMap *map, const double *base, int nx, int ny, long long nz,
                          int bx, int by);
+// Host: a tensor map of 8-byte elements [nz][ny][nx] whose rows are `pitch`
+// elements apart (pitch >= nx, pitch * 8 a multiple of 16), boxes bx x by x bz.
+bool make_tensor_map_8b(CUtensorMap *map, const void *base, int nx, int ny, int nz, int pitch,
+                        int bx, int by, int bz);
 
 }  // namespace tpm
