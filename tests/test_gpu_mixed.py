@@ -118,6 +118,36 @@ def test_mixed_matches_fp64_on_ragged_tiles(capi):
         assert rel_err(pm[q], pf[q]) <= TOL_MIXED, q
 
 
+@pytest.mark.parametrize("shape", [(32, 32, 256), (32, 256, 32)])
+def test_mixed_matches_fp64_with_256_point_pencils(capi, shape):
+    """Boxes with 256-point z (or y) pencils, the size whose z pass runs its
+    second forward stage, the divide and the first inverse stage in registers:
+    mixed vs FP64 GPU after 1 and 3 heated steps."""
+    nx, ny, nz = shape
+    p, s = setup(nx, 20_000, seed=13, heat=0.5, precision=P.PREC_MIXED)
+    p = p.replace(Ny=ny, Nz=nz, Ly=p.Lx * ny / nx, Lz=p.Lx * nz / nx)
+    s = inputs.make_state(p, s.npart, seed=13)
+    p = p.replace(dt=inputs.cfl_dt(p, s.RU))
+    ctxs = []
+    for prec in (P.PREC_MIXED, P.PREC_FP64):
+        c = capi.Context(p.replace(precision=prec), s.npart)
+        c.load(s)
+        c.initialize()
+        ctxs.append(c)
+    m, f = ctxs
+    for more in (1, 2):
+        for c in ctxs:
+            c.run(more)
+            c.sync()
+        for g in ("RU", "RHO", "P", "C", "Q"):
+            e = rel_err(m.download_field(g), f.download_field(g))
+            assert e <= TOL_MIXED, (g, e)
+        assert m.scalars()["max_abs_div"] <= TOL_DIV
+        pm, pf = m.download_particles("base"), f.download_particles("base")
+        for q in inputs.PQ:
+            assert rel_err(pm[q], pf[q]) <= TOL_MIXED, q
+
+
 def test_mixed_keeps_the_callers_particle_order(capi):
     """The mixed path keeps its particles in cell order in memory (a
     permutation at every step boundary); every transfer is in the caller's

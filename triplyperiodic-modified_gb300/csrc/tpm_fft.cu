@@ -625,8 +625,15 @@ __host__ __device__ __forceinline__ size_t tma_yz_smem(int n) {
   return 3 * (size_t)tma_tile_bytes(n) + tma_tile_bytes(n) / kTmaPens + 16;
 }
 
-template <bool kZ>
-__global__ void __launch_bounds__(256)
+// z pass of a 256-point plan (two radix-16 stages), kFused: the forward
+// transform's second stage leaves thread (i, q) < 128 holding modes
+// kz = i + 16 u (u < 16) of pencil q, exactly the elements the inverse
+// transform's first stage gives that thread.  So the second forward stage,
+// the divide and the first inverse stage run in its registers, with no
+// shared-memory round trip and no barrier between them; the arithmetic is
+// the unfused path's, operation for operation.
+template <bool kZ, bool kFused = false>
+__global__ void __launch_bounds__(256, kFused ? 4 : 1)
 k_fft_yz_tma(Grid g, FftPlan pl, const __grid_constant__ CUtensorMap map, int sign,
              const float *__restrict__ inv_mwn, const int *__restrict__ skip,
              DevScalars *__restrict__ s, int ntiles) {
@@ -677,7 +684,8 @@ k_fft_yz_tma(Grid g, FftPlan pl, const __grid_constant__ CUtensorMap map, int si
   // refills, and only the thread that issues both waits for the store; else
   // (a y pass with an odd number of stages) the store reads the scratch buffer
   // the next transform writes, and the block waits for it
-  const bool store_from_scratch = !kZ && (pl.nst & 1);
+  const bool store_from_scratch = kFused || (!kZ && (pl.nst & 1));
+  static_assert(kZ || !kFused, "only the z pass fuses its transforms");
   bool ok = true;
   int it = 0;
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
@@ -689,9 +697,16 @@ k_fft_yz_tma(Grid g, FftPlan pl, const __grid_constant__ CUtensorMap map, int si
     coords(t, x, y, z);
     // z pass: the reciprocals of this thread's modes (the table of
     // k_inv_mwn), loaded while the tile is in flight
-    constexpr int kInv = 8;  // tot <= 8 * 256 = kInv * blockDim.x
+    constexpr int kInv = kFused ? 16 : 8;  // tot <= 8 * 256 = 8 * blockDim.x
     float invr[kInv];
-    if constexpr (kZ) {
+    if constexpr (kFused) {  // thread (i, q) < 128: modes kz = i + 16 u of pencil q
+      const int kx = x + (threadIdx.x & 7), i = threadIdx.x >> 3;
+#pragma unroll
+      for (int u = 0; u < kInv; ++u)
+        invr[u] = (threadIdx.x < 128 && kx < g.nxh)
+                      ? inv_mwn[((long long)(i + 16 * u) * g.ny + y) * g.nxh + kx]
+                      : 0.f;
+    } else if constexpr (kZ) {
 #pragma unroll
       for (int u = 0; u < kInv; ++u) {
         const int idx = threadIdx.x + u * (int)blockDim.x;
@@ -706,8 +721,38 @@ k_fft_yz_tma(Grid g, FftPlan pl, const __grid_constant__ CUtensorMap map, int si
       ok = false;
       break;
     }
-    float2 *r = smem_fft(buf(slot), scratch, kTmaPens, pl, kZ ? -1 : sign, tws);
-    if constexpr (kZ) {
+    float2 *r;
+    if constexpr (kFused) {
+      stockham_stage<16>(buf(slot), scratch, lq, pl, 1, pl.pmag[0], -1, tws);
+      __syncthreads();
+      if (threadIdx.x < 128) {
+        const int i = threadIdx.x >> 3, q = threadIdx.x & 7, kx = x + q;
+        float2 v[16];
+        v[0] = scratch[i * kTmaPens + q];
+#pragma unroll
+        for (int t = 1; t < 16; ++t)
+          v[t] = cmul(scratch[(i + 16 * t) * kTmaPens + q], tws ? tws[i * t] : pl.tw32[i * t], -1);
+        dft16(v, -1);
+        // divide by the modified wave number except the zero mode (poisson.cpp:442-449)
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          if (kx < g.nxh && (kx + y + i + 16 * u) > 0) {
+            v[u].y = v[u].y * invr[u];
+            v[u].x = v[u].x * invr[u];
+          }
+        }
+        dft16(v, +1);
+#pragma unroll
+        for (int u = 0; u < 16; ++u) buf(slot)[(16 * i + u) * kTmaPens + q] = v[u];
+      }
+      __syncthreads();
+      stockham_stage<16>(buf(slot), scratch, lq, pl, 16, pl.pmag[1], +1, tws);
+      __syncthreads();
+      r = scratch;
+    } else {
+      r = smem_fft(buf(slot), scratch, kTmaPens, pl, kZ ? -1 : sign, tws);
+    }
+    if constexpr (kZ && !kFused) {
       float2 *other = (r == scratch) ? buf(slot) : scratch;
       // divide by the modified wave number except the zero mode (poisson.cpp:442-449)
 #pragma unroll
@@ -1078,16 +1123,17 @@ void fft_plans_create(tpm_ctx *c) {
         make_tensor_map_8b(&c->fft_map_z, c->spec, g.nxh, g.ny, g.nz, c->spec_pitch, kTmaPens, 1,
                            g.nz)) {
       // persistent blocks: as many as stay resident (SMs x blocks per SM)
-      const int ns[2] = {c->fy32.n, c->fz32.n};
-      const void *kern[2] = {reinterpret_cast<const void *>(k_fft_yz_tma<false>),
-                             reinterpret_cast<const void *>(k_fft_yz_tma<true>)};
+      const int ns[3] = {c->fy32.n, c->fz32.n, c->fz32.n};
+      const void *kern[3] = {reinterpret_cast<const void *>(k_fft_yz_tma<false>),
+                             reinterpret_cast<const void *>(k_fft_yz_tma<true>),
+                             reinterpret_cast<const void *>(k_fft_yz_tma<true, true>)};
       bool fits = true;
-      for (int d = 0; d < 2; ++d) {
+      for (int d = 0; d < 3; ++d) {
         const int smem = (int)tma_yz_smem(ns[d]);
         TPM_CUDA_TRY(cudaFuncSetAttribute(kern[d], cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         int per_sm = 0;
         TPM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern[d], 256, smem));
-        c->tma_fft_blocks[d] = per_sm * (c->sms > 0 ? c->sms : 1);
+        if (d < 2) c->tma_fft_blocks[d] = per_sm * (c->sms > 0 ? c->sms : 1);
         fits = fits && per_sm > 0;
       }
       c->tma_fft = fits;
@@ -1147,9 +1193,14 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
     // (one tile per block: the z pass's two transforms give its blocks enough
     // work between loads, and its tiles load while other blocks compute;
     // persistent blocks measured the same, 1.05 ms per 256^3 step)
-    TPM_LAUNCH(c, "fft_z_solve", k_fft_yz_tma<true>, ntiles, 256,
-               tma_yz_smem(plz.n), g, plz, c->fft_map_z, -1,
-               static_cast<const float *>(c->inv_mwn), skip, c->dsc, ntiles);
+    if (plz.nst == 2 && plz.radix[0] == 16 && plz.radix[1] == 16)
+      TPM_LAUNCH(c, "fft_z_solve", (k_fft_yz_tma<true, true>), ntiles, 256,
+                 tma_yz_smem(plz.n), g, plz, c->fft_map_z, -1,
+                 static_cast<const float *>(c->inv_mwn), skip, c->dsc, ntiles);
+    else
+      TPM_LAUNCH(c, "fft_z_solve", k_fft_yz_tma<true>, ntiles, 256,
+                 tma_yz_smem(plz.n), g, plz, c->fft_map_z, -1,
+                 static_cast<const float *>(c->inv_mwn), skip, c->dsc, ntiles);
   } else {
     int blocks = g.ny * ((g.nxh + npz - 1) / npz);
     size_t smem = 2 * (size_t)npz * plz.n * sizeof(T2);
