@@ -163,7 +163,9 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- GPU arm
-def make_workload(name=WORKLOAD, precision=0, N=None, npart=None):
+def make_workload(name=WORKLOAD, precision=0, N=None, npart=None, grid=None):
+    """The workload's parameters and seeded state; `grid` (nx, ny, nz) replaces
+    its cubic box by one of equal cells (a small case of the same kernels)."""
     from tpm import inputs, params as P
 
     w = dict(P.WORKLOADS[name])
@@ -172,6 +174,10 @@ def make_workload(name=WORKLOAD, precision=0, N=None, npart=None):
     p = P.physical(N, npart, nu=w["nu"], A=w["A"], tau_p=w["tau_p"],
                    mass_loading=w["mass_loading"], heating_Q=w["heating_Q"], iterations=20,
                    epsilon=1e-13, precision=precision)
+    if grid:
+        nx, ny, nz = grid
+        d = p.Lx / p.Nx
+        p = p.replace(Nx=nx, Ny=ny, Nz=nz, Lx=d * nx, Ly=d * ny, Lz=d * nz)
     s = inputs.make_state(p, npart, seed=w["seed"])
     p = p.replace(dt=inputs.cfl_dt(p, s.RU))
     return p, s
@@ -573,7 +579,7 @@ def gpu_main(args):
         dist = td
     from tpm import params as P
 
-    p64, s = make_workload(args.workload, 0)
+    p64, s = make_workload(args.workload, 0, npart=args.particles, grid=args.grid)
     peak, peak_kind = peaks()
     paths = ["fp64", "mixed"] if args.precision == "both" else [args.precision]
     res, ctxs = {}, {}
@@ -603,13 +609,14 @@ def gpu_main(args):
     e2e_ms = max_over_ranks(e2e_ms, dist, "cuda")
     e2e_value = whole_job_rate(world, p64.ncell, 1, e2e_ms)
     r = res[head]
+    box = (f"{p64.Nx}^3" if p64.Nx == p64.Ny == p64.Nz else f"{p64.Nx}x{p64.Ny}x{p64.Nz}")
     line = {
         "metric": METRIC, "value": round(r["value"], 3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(r["ms_per_step"], 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if head == "fp64" else "mixed (f32 compute, f64 state and residuals)",
         "data": "synthetic (seeded solenoidal E(k)~k^4 exp(-2(k/4)^2) velocity, uniform particles)",
-        "config": {"workload": f"{args.workload}: {p64.Nx}^3 cells, {s.npart} particles, heated, "
+        "config": {"workload": f"{args.workload}: {box} cells, {s.npart} particles, heated, "
                                f"two-way coupled, Poisson eps=1e-13 (mean {r['n_it']:.2f} "
                                f"iterations)",
                    "precision": head, "parallelism": f"replicas x{world}",
@@ -913,6 +920,11 @@ def main():
     ap.add_argument("--fft-tiles", type=lambda v: [int(t) for t in v.split(",")], default=None,
                     help="pencils x,y,z and threads x,y,z of the FFT passes instead of "
                          "autotuning them (one precision at a time)")
+    ap.add_argument("--grid", type=lambda v: tuple(int(t) for t in v.split(",")), default=None,
+                    help="nx,ny,nz: the workload's physics on this box of the same cell size "
+                         "(small cases for profilers)")
+    ap.add_argument("--particles", type=int, default=None,
+                    help="particle count instead of the workload's")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         args.warmup = 3

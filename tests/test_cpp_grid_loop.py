@@ -91,15 +91,17 @@ def phase_step(ctx):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_method_calls_equal_the_fused_step(precision):
+@pytest.mark.parametrize("precision,n", [("fp64", 24), ("mixed", 24), ("mixed", 32)])
+def test_method_calls_equal_the_fused_step(precision, n):
     """Two steps by the per-method entry points are bit-identical to two
-    fused steps, on both paths (heated, two-way coupled, passive scalar on)."""
+    fused steps, on both paths (heated, two-way coupled, passive scalar on);
+    at 32^3 the mixed path's density pass also forms the face velocity and its
+    Poisson right-hand-side pass the face coefficients (TMA-fed tiles)."""
     from tpm import build, capi, inputs, params as P
 
     build.build()
     prec = P.PREC_MIXED if precision == "mixed" else P.PREC_FP64
-    p = P.physical(24, 3000, nu=0.02, A=0.1, tau_p=0.1, mass_loading=0.5, heating_Q=0.5,
+    p = P.physical(n, 3000, nu=0.02, A=0.1, tau_p=0.1, mass_loading=0.5, heating_Q=0.5,
                    iterations=20, epsilon=1e-13, precision=prec)
     s = inputs.make_state(p, 3000, seed=14)
     s.PS = inputs.passive_scalar(p, seed=14)

@@ -281,8 +281,11 @@ void aux_join(tpm_ctx *c, cudaEvent_t e) {
 
 // One RK4 stage.  Three kernels run on the auxiliary stream beside the ones
 // they do not depend on (in a captured graph: parallel branches):
-//   face velocity U(RU_int, Rho_int)        beside the density update;
-//   face coefficients C(Rho_new) (mixed)    beside the particle push and deposits;
+//   face velocity U(RU_int, Rho_int)        beside the density update (unless
+//                                           the density pass forms it);
+//   face coefficients C(Rho_new) (mixed)    beside the particle push and deposits
+//                                           (unless the Poisson right-hand-side
+//                                           pass forms them);
 //   momentum RHS (needs F_p)                beside the heat deposit.
 // Each writes buffers that the kernels beside it neither read nor write; the
 // stream joins back before their results are used (push, Poisson RHS).
@@ -299,13 +302,16 @@ void substep(tpm_ctx *c, int s) {
     launch();
   };
   tpm::launch_p0_update(c, s);
-  beside(0, [&] { tpm::launch_face_velocity(c); });
-  if (par) TPM_CUDA_TRY(cudaEventRecord(c->join_ev[0], c->aux));
+  const bool own_u = !tpm::face_velocity_in_rho_pass(c);
+  if (own_u) {
+    beside(0, [&] { tpm::launch_face_velocity(c); });
+    if (par) TPM_CUDA_TRY(cudaEventRecord(c->join_ev[0], c->aux));
+  }
   tpm::launch_rho_update(c, s, nb);
   beside(1, [&] { tpm::launch_face_coeff(c); });
   // the FP64 push and the passive scalar read the face velocity U (the mixed
   // push interpolates RU_int / I_C2F(Rho_int) itself)
-  if (par && (c->p.precision != TPM_PREC_MIXED || c->PS))
+  if (par && own_u && (c->p.precision != TPM_PREC_MIXED || c->PS))
     TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[0], 0));
   tpm::launch_particle_push(c, s, nb);
   tpm::particle_deposit_momentum(c);

@@ -633,7 +633,7 @@ __host__ __device__ __forceinline__ size_t tma_yz_smem(int n) {
 // shared-memory round trip and no barrier between them; the arithmetic is
 // the unfused path's, operation for operation.
 template <bool kZ, bool kFused = false>
-__global__ void __launch_bounds__(256, kFused ? 4 : 1)
+__global__ void __launch_bounds__(256, 4)
 k_fft_yz_tma(Grid g, FftPlan pl, const __grid_constant__ CUtensorMap map, int sign,
              const float *__restrict__ inv_mwn, const int *__restrict__ skip,
              DevScalars *__restrict__ s, int ntiles) {

@@ -975,6 +975,167 @@ k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restri
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Mixed path, grids of whole 32 x 8 column tiles: grid::Update_Rho
+// (grid.cpp:608-614) and the face velocity U = RU_int / Rho_face(Rho_int)
+// that Update_Particle forms first (grid.cpp:868) in one z-marching pass fed
+// by the TMA.  Both read RU_int: the two kernels this replaces
+// (k_rho_update_mixed, k_face_velocity_mixed) read it twice (in FP64 and as
+// its FP32 copy, which equals its truncation ff_hi) and gather the
+// neighbours of every cell with scattered loads.  Per plane k a block needs
+// RU_int's x component with the column pair at i0 + 32, its y component with
+// the row at j0 + 8, its z component of plane k + 1 (plane k's stays in the
+// thread's registers), and Rho_int with the row at j0 - 1 and the column pair
+// at i0 - 2 (plane k - 1's stays in registers); Rho and the RK input of
+// Rho_np1 are plain coalesced loads issued before the wait.  One thread
+// issues the next plane's boxes into the other of two slots while the block
+// computes.  The arithmetic is the two kernels', operation for operation, so
+// the results are bit-identical.
+namespace {
+
+struct RfSmem {
+  // one slot (bytes; every box 128-byte aligned): RU_int x tile [8][32] |
+  // x column pair [8][2] at i0 + 32 | y tile | y row [32] at j0 + 8 | z tile of
+  // plane k + 1 | Rho_int row [32] at j0 - 1 | Rho_int tile | column pair
+  // [8][2] at i0 - 2
+  static constexpr int kRuxXhi = 2048;
+  static constexpr int kRuy = kRuxXhi + 128;
+  static constexpr int kRuyYhi = kRuy + 2048;
+  static constexpr int kRuz = kRuyYhi + 256;
+  static constexpr int kRhoYlo = kRuz + 2048;
+  static constexpr int kRho = kRhoYlo + 256;
+  static constexpr int kRhoXlo = kRho + 2048;
+  static constexpr int kSlot = kRhoXlo + 128;  // the bytes of one stage's boxes
+  static constexpr int oBar = 2 * kSlot;
+  static constexpr int kBytes = oBar + 16;
+};
+static_assert(RfSmem::kRuy % 128 == 0 && RfSmem::kRuyYhi % 128 == 0 && RfSmem::kRuz % 128 == 0 &&
+                  RfSmem::kRhoYlo % 128 == 0 && RfSmem::kRho % 128 == 0 &&
+                  RfSmem::kRhoXlo % 128 == 0 && RfSmem::kSlot % 128 == 0,
+              "TMA destinations must stay 128-byte aligned");
+
+// RU_int (as [3 nz][ny][nx]) and Rho_int: tile, row and column-pair boxes
+struct RfMaps {
+  CUtensorMap ru_t, ru_r, ru_c, rho_t, rho_r, rho_c;
+};
+
+__global__ void __launch_bounds__(kZX * kZY)
+k_rho_face_tma(Grid g, const __grid_constant__ RfMaps m, DevScalars *__restrict__ s,
+               const double *__restrict__ RUi, const double *__restrict__ Rho_int,
+               const double *__restrict__ Rho, const double *__restrict__ np1_in,
+               double *__restrict__ Rho_np1, double *__restrict__ Rho_new,
+               double *__restrict__ Tgas, float *__restrict__ U, double a_np1, double b_new,
+               int stage, int zlen) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  const int tid = threadIdx.x, tx = tid % kZX, ty = tid / kZX;
+  const int tilesx = g.nx / kZX, tilesy = g.ny / kZY;
+  const int bx = blockIdx.x % tilesx, by = (blockIdx.x / tilesx) % tilesy;
+  const int bz = blockIdx.x / (tilesx * tilesy);
+  const int i0 = bx * kZX, j0 = by * kZY, k0 = bz * zlen;
+  const int nplanes = min(k0 + zlen, g.nz) - k0;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(sm + RfSmem::oBar);
+  if (smem_u32(sm) & 127u) {  // never issue a box to a misaligned address
+    if (tid == 0) s->timeout = 1;
+    return;
+  }
+  const int jlo = j0 == 0 ? g.ny - 1 : j0 - 1, jhi = j0 + kZY == g.ny ? 0 : j0 + kZY;
+  const int ilo = i0 == 0 ? g.nx - 2 : i0 - 2, ihi = i0 + kZX == g.nx ? 0 : i0 + kZX;
+  auto slot = [&](int r) { return sm + (r & 1) * RfSmem::kSlot; };
+  // the boxes of plane k0 + r into slot r & 1, counted on bar[r & 1]
+  auto load_stage = [&](int r) {
+    uint64_t *b = &bar[r & 1];
+    unsigned char *d = slot(r);
+    const int k = k0 + r, kp = k + 1 == g.nz ? 0 : k + 1;
+    mbar_arrive_expect_tx(b, RfSmem::kSlot);
+    tma_load_3d(d, &m.ru_t, b, i0, j0, k);
+    tma_load_3d(d + RfSmem::kRuxXhi, &m.ru_c, b, ihi, j0, k);
+    tma_load_3d(d + RfSmem::kRuy, &m.ru_t, b, i0, j0, g.nz + k);
+    tma_load_3d(d + RfSmem::kRuyYhi, &m.ru_r, b, i0, jhi, g.nz + k);
+    tma_load_3d(d + RfSmem::kRuz, &m.ru_t, b, i0, j0, 2 * g.nz + kp);
+    tma_load_3d(d + RfSmem::kRhoYlo, &m.rho_r, b, i0, jlo, k);
+    tma_load_3d(d + RfSmem::kRho, &m.rho_t, b, i0, j0, k);
+    tma_load_3d(d + RfSmem::kRhoXlo, &m.rho_c, b, ilo, j0, k);
+  };
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init_fence();
+    tma_prefetch_map(&m.ru_t);
+    tma_prefetch_map(&m.rho_t);
+  }
+  __syncthreads();
+  if (tid == 0 && nplanes > 0) load_stage(0);
+  const int i = i0 + tx, j = j0 + ty;
+  // the column's RU_int z component at plane k0 and Rho_int at plane k0 - 1
+  double ruz_c = nplanes > 0 ? RUi[2 * g.n + at(g, i, j, k0)] : 0.0;
+  double rho_zm = nplanes > 0 ? Rho_int[at(g, i, j, k0 == 0 ? g.nz - 1 : k0 - 1)] : 0.0;
+  const double T_scale = s->T_scale;
+  const float2 inv_d[3] = {ff_from_double(g.inv_dx), ff_from_double(g.inv_dy),
+                           ff_from_double(g.inv_dz)};
+  bool ok = true;
+  int issued = 0;  // the last stage issued
+  for (int r = 0; r < nplanes; ++r) {
+    const int k = k0 + r;
+    if (r + 1 < nplanes) {
+      if (tid == 0) {
+        fence_proxy_async();  // the reads of the slot being refilled came before
+        load_stage(r + 1);
+      }
+      issued = r + 1;
+    }
+    const long long c = at(g, i, j, k);
+    const double rho_b = Rho[c], np1_b = np1_in[c];
+    ok = mbar_wait(&bar[r & 1], (unsigned)(r >> 1) & 1u);
+    if (!ok) s->timeout = 1;
+    if (!__syncthreads_and(ok)) {
+      ok = false;
+      break;
+    }
+    const unsigned char *d = slot(r);
+    const double *rux = reinterpret_cast<const double *>(d);
+    const double *ruy = reinterpret_cast<const double *>(d + RfSmem::kRuy);
+    const double *rho = reinterpret_cast<const double *>(d + RfSmem::kRho);
+    const double rux_c = rux[tid];
+    const double rux_p =
+        tx < kZX - 1 ? rux[tid + 1] : reinterpret_cast<const double *>(d + RfSmem::kRuxXhi)[2 * ty];
+    const double ruy_c = ruy[tid];
+    const double ruy_p =
+        ty < kZY - 1 ? ruy[tid + kZX] : reinterpret_cast<const double *>(d + RfSmem::kRuyYhi)[tx];
+    const double ruz_p = reinterpret_cast<const double *>(d + RfSmem::kRuz)[tid];
+    // Update_Rho: the divergence of RU_int as a pair, the FP64 state update
+    float2 D = ff_mul(ff_sub(ff_from_double(rux_p), ff_from_double(rux_c)), inv_d[0]);
+    D = ff_add(D, ff_mul(ff_sub(ff_from_double(ruy_p), ff_from_double(ruy_c)), inv_d[1]));
+    D = ff_add(D, ff_mul(ff_sub(ff_from_double(ruz_p), ff_from_double(ruz_c)), inv_d[2]));
+    const double Dd = ff_to_double(D);
+    const double np1 = fma(a_np1, Dd, np1_b);
+    const double nw = (stage != 3) ? fma(b_new, Dd, rho_b) : np1;
+    Rho_np1[c] = np1;
+    Rho_new[c] = nw;
+    Tgas[c] = T_scale * ff_to_double(ff_rcp(ff_from_double(nw)));
+    // the face velocity in FP32 from the truncated RU_int and Rho_int
+    const double rho_c = rho[tid];
+    const double rho_xm =
+        tx > 0 ? rho[tid - 1] : reinterpret_cast<const double *>(d + RfSmem::kRhoXlo)[2 * ty + 1];
+    const double rho_ym =
+        ty > 0 ? rho[tid - kZX] : reinterpret_cast<const double *>(d + RfSmem::kRhoYlo)[tx];
+    const float rf = ff_hi(rho_c);
+    U[c] = ff_hi(rux_c) / ((rf + ff_hi(rho_xm)) * 0.5f);
+    U[g.n + c] = ff_hi(ruy_c) / ((rf + ff_hi(rho_ym)) * 0.5f);
+    U[2 * g.n + c] = ff_hi(ruz_c) / ((rf + ff_hi(rho_zm)) * 0.5f);
+    ruz_c = ruz_p;
+    rho_zm = rho_c;
+    __syncthreads();  // slot r & 1 is refilled by stage r + 2
+  }
+  if (!ok && tid == 0) {
+    // a wait gave up: let the copies issued land (again bounded) before the
+    // block's shared memory is released
+    for (int r = issued > 0 ? issued - 1 : 0; r <= issued; ++r)
+      mbar_wait(&bar[r & 1], (unsigned)(r >> 1) & 1u);
+  }
+}
+
+}  // namespace
+
 // face velocity of the mixed path: only the FP32 stencil and the particle
 // gather read it, so it is formed in FP32
 __global__ void k_face_velocity_mixed(Grid g, const float *__restrict__ RUi32,
@@ -1348,6 +1509,22 @@ const TmaField &tma_field(tpm_ctx *c, const double *base, long long layers) {
 }
 
 void launch_rho_update(tpm_ctx *c, int s, bool np1_in_base) {
+  if (c->p.precision == TPM_PREC_MIXED && c->tma_rhs) {  // with the face velocity
+    RfMaps m;
+    const TmaField &R = tma_field(c, c->RU_int, 3LL * c->g.nz);
+    m.ru_t = R.tile;
+    m.ru_r = R.row;
+    m.ru_c = R.col;
+    const TmaField &D = tma_field(c, c->Rho_int, c->g.nz);
+    m.rho_t = D.tile;
+    m.rho_r = D.row;
+    m.rho_c = D.col;
+    TPM_LAUNCH(c, "rho_update", k_rho_face_tma, zm_blocks(c), kZX * kZY, RfSmem::kBytes, c->g, m,
+               c->dsc, c->RU_int, c->Rho_int, c->Rho, np1_in_base ? c->Rho : c->Rho_np1,
+               c->Rho_np1, c->Rho_new, c->Tgas, c->U32, -(c->p.dt * kPost[s]),
+               -c->p.dt * kPre[s], s, zm_zlen(c));
+    return;
+  }
   if (c->p.precision == TPM_PREC_MIXED) {
     TPM_LAUNCH(c, "rho_update", k_rho_update_mixed, cell_waves(c, k_rho_update_mixed, false),
                kThreads, 0, c->g,
@@ -1362,7 +1539,12 @@ void launch_rho_update(tpm_ctx *c, int s, bool np1_in_base) {
              c->Tgas, c->dsc, -(c->p.dt * kPost[s]), -c->p.dt * kPre[s], s);
 }
 
+bool face_velocity_in_rho_pass(const tpm_ctx *c) {
+  return c->p.precision == TPM_PREC_MIXED && c->tma_rhs;
+}
+
 void launch_face_velocity(tpm_ctx *c) {
+  if (face_velocity_in_rho_pass(c)) return;  // k_rho_face_tma formed it
   if (c->p.precision == TPM_PREC_MIXED) {
     TPM_LAUNCH(c, "face_velocity", k_face_velocity_mixed,
                cell_waves(c, k_face_velocity_mixed, false), kThreads, 0, c->g,

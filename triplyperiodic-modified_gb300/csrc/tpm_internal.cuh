@@ -318,6 +318,9 @@ void prof_end(tpm_ctx *c, const char *name, cudaEvent_t ev0);
 void launch_p0_update(tpm_ctx *c, int stage);
 void launch_rho_update(tpm_ctx *c, int stage, bool np1_in_base);
 void launch_face_velocity(tpm_ctx *c);
+// the mixed path on grids of whole TMA tiles forms the face velocity in the
+// density pass (launch_face_velocity is then a no-op)
+bool face_velocity_in_rho_pass(const tpm_ctx *c);
 void launch_rhs_momentum(tpm_ctx *c, int stage, bool np1_in_base);
 void rhs_kernels_setup(tpm_ctx *c);
 void particle_kernels_setup(tpm_ctx *c);  // tpm_particles.cu
