@@ -39,10 +39,11 @@ FALLBACK_HBM_GBS = 6800.0
 # capture of every kernel of this bench's two profiled steps (the command is
 # in the summary of the capture)
 NCU_TRAFFIC = {
-    ("box256_p8e6_heated", True, "fft_x_fwd_resid"): 8.63e8,
-    ("box256_p8e6_heated", True, "particle_push"): 3.546e9,
-    ("box256_p8e6_heated", True, "rhs_momentum"): 2.006e9,
-    ("box256_p8e6_heated", True, "poisson_rhs"): 1.423e9,
+    ("box256_p8e6_heated", True, "fft_x_fwd_resid"): 8.654e8,
+    ("box256_p8e6_heated", True, "particle_push"): 3.557e9,
+    ("box256_p8e6_heated", True, "rhs_momentum"): 2.009e9,
+    ("box256_p8e6_heated", True, "poisson_rhs"): 1.279e9,
+    ("box256_p8e6_heated", True, "rho_update"): 1.347e9,
     ("box256_p8e6_heated", False, "rhs_momentum"): 2.595e9,
     ("box256_p8e6_heated", False, "fft_x_fwd_resid"): 9.36e8,
 }
@@ -365,9 +366,15 @@ def kernel_bytes(name, ncell, npart, mixed):
     bc, bp = KERNEL_BYTES.get(name, (0, 0))
     if not mixed and name == "poisson_rhs":  # FP64: face values precomputed by poisson_faces
         bc = 10 * 8
-    if mixed:  # complex64 spectrum on the mixed path
+    if mixed:  # complex64 spectrum on the mixed path; its fused TMA passes
+        # (on grids of whole 32 x 8 tiles): the density update with the face
+        # velocity (RU_int 3, Rho_int, Rho, Rho_np1 in; Rho_np1, Rho_new, T and
+        # U 3 in FP32 out) and the Poisson right-hand side with the face
+        # coefficients (Rho_new, RU_new 3, Q in; RHS, divergence, cc in FP32,
+        # C/d^2 3 as FP32 pairs out)
         bc = {"fft_y": 8, "fft_z_solve": 8, "fft_x_fwd_resid": 6 * 8 + 4,
-              "fft_x_inv_update": 4 + 16}.get(name, bc)
+              "fft_x_inv_update": 4 + 16, "rho_update": 6 * 8 + 3 * 8 + 12,
+              "poisson_rhs": 5 * 8 + 2 * 8 + 4 + 3 * 8}.get(name, bc)
     return bc * ncell + bp * npart
 
 

@@ -1066,9 +1066,10 @@ k_rho_face_tma(Grid g, const __grid_constant__ RfMaps m, DevScalars *__restrict_
   __syncthreads();
   if (tid == 0 && nplanes > 0) load_stage(0);
   const int i = i0 + tx, j = j0 + ty;
-  // the column's RU_int z component at plane k0 and Rho_int at plane k0 - 1
-  double ruz_c = nplanes > 0 ? RUi[2 * g.n + at(g, i, j, k0)] : 0.0;
-  double rho_zm = nplanes > 0 ? Rho_int[at(g, i, j, k0 == 0 ? g.nz - 1 : k0 - 1)] : 0.0;
+  // the column's RU_int z component at plane k0 (as its pair) and Rho_int at
+  // plane k0 - 1 (truncated): carried from one plane to the next
+  float2 pz_c = ff_from_double(nplanes > 0 ? RUi[2 * g.n + at(g, i, j, k0)] : 0.0);
+  float rho_zm = ff_hi(nplanes > 0 ? Rho_int[at(g, i, j, k0 == 0 ? g.nz - 1 : k0 - 1)] : 0.0);
   const double T_scale = s->T_scale;
   const float2 inv_d[3] = {ff_from_double(g.inv_dx), ff_from_double(g.inv_dy),
                            ff_from_double(g.inv_dz)};
@@ -1101,29 +1102,30 @@ k_rho_face_tma(Grid g, const __grid_constant__ RfMaps m, DevScalars *__restrict_
     const double ruy_c = ruy[tid];
     const double ruy_p =
         ty < kZY - 1 ? ruy[tid + kZX] : reinterpret_cast<const double *>(d + RfSmem::kRuyYhi)[tx];
-    const double ruz_p = reinterpret_cast<const double *>(d + RfSmem::kRuz)[tid];
+    const float2 pz_p = ff_from_double(reinterpret_cast<const double *>(d + RfSmem::kRuz)[tid]);
     // Update_Rho: the divergence of RU_int as a pair, the FP64 state update
-    float2 D = ff_mul(ff_sub(ff_from_double(rux_p), ff_from_double(rux_c)), inv_d[0]);
-    D = ff_add(D, ff_mul(ff_sub(ff_from_double(ruy_p), ff_from_double(ruy_c)), inv_d[1]));
-    D = ff_add(D, ff_mul(ff_sub(ff_from_double(ruz_p), ff_from_double(ruz_c)), inv_d[2]));
+    const float2 px_c = ff_from_double(rux_c), py_c = ff_from_double(ruy_c);
+    float2 D = ff_mul(ff_sub(ff_from_double(rux_p), px_c), inv_d[0]);
+    D = ff_add(D, ff_mul(ff_sub(ff_from_double(ruy_p), py_c), inv_d[1]));
+    D = ff_add(D, ff_mul(ff_sub(pz_p, pz_c), inv_d[2]));
     const double Dd = ff_to_double(D);
     const double np1 = fma(a_np1, Dd, np1_b);
     const double nw = (stage != 3) ? fma(b_new, Dd, rho_b) : np1;
     Rho_np1[c] = np1;
     Rho_new[c] = nw;
     Tgas[c] = T_scale * ff_to_double(ff_rcp(ff_from_double(nw)));
-    // the face velocity in FP32 from the truncated RU_int and Rho_int
-    const double rho_c = rho[tid];
+    // the face velocity in FP32 from the truncated RU_int (the high parts of
+    // its pairs) and Rho_int
     const double rho_xm =
         tx > 0 ? rho[tid - 1] : reinterpret_cast<const double *>(d + RfSmem::kRhoXlo)[2 * ty + 1];
     const double rho_ym =
         ty > 0 ? rho[tid - kZX] : reinterpret_cast<const double *>(d + RfSmem::kRhoYlo)[tx];
-    const float rf = ff_hi(rho_c);
-    U[c] = ff_hi(rux_c) / ((rf + ff_hi(rho_xm)) * 0.5f);
-    U[g.n + c] = ff_hi(ruy_c) / ((rf + ff_hi(rho_ym)) * 0.5f);
-    U[2 * g.n + c] = ff_hi(ruz_c) / ((rf + ff_hi(rho_zm)) * 0.5f);
-    ruz_c = ruz_p;
-    rho_zm = rho_c;
+    const float rf = ff_hi(rho[tid]);
+    U[c] = px_c.x / ((rf + ff_hi(rho_xm)) * 0.5f);
+    U[g.n + c] = py_c.x / ((rf + ff_hi(rho_ym)) * 0.5f);
+    U[2 * g.n + c] = pz_c.x / ((rf + rho_zm) * 0.5f);
+    pz_c = pz_p;
+    rho_zm = rf;
     __syncthreads();  // slot r & 1 is refilled by stage r + 2
   }
   if (!ok && tid == 0) {
