@@ -229,8 +229,26 @@ __device__ __forceinline__ void stockham_stage(const T2 *__restrict__ a, T2 *__r
     }
     dft_small(v, R, sign);
     const int j = ip * p * R + k;
+    if (sizeof(T2) == sizeof(float2) && p == 1 && (R & (R - 1)) == 0 && npen >= 4 && npen <= 8) {
+      // first stage: the lanes of a warp hold 32 / npen consecutive i, whose
+      // outputs u sit R * npen elements apart, all on the same banks when
+      // written in the same order; lanes with odd i (and, at 4 pencils, with
+      // i = 2, 3 mod 4) write their outputs in a swapped order, so that one
+      // store instruction covers both halves of the banks
+      const int sw = i & (npen == 8 ? 1 : 3);
 #pragma unroll
-    for (int u = 0; u < R; ++u) b[(j + u * p) * npen + q] = v[u];
+      for (int u = 0; u < R; ++u) {
+        T2 w = (sw & 1) ? v[u ^ 1] : v[u];
+        if (npen == 4) {
+          const T2 w2 = (sw & 1) ? v[u ^ 3] : v[u ^ 2];
+          w = (sw & 2) ? w2 : w;
+        }
+        b[(j + (u ^ sw) * p) * npen + q] = w;
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < R; ++u) b[(j + u * p) * npen + q] = v[u];
+    }
   }
 }
 
@@ -742,8 +760,11 @@ k_fft_yz_tma(Grid g, FftPlan pl, const __grid_constant__ CUtensorMap map, int si
           }
         }
         dft16(v, +1);
+        // (odd i in swapped order: a store instruction covers both bank
+        // halves, as in the first Stockham stage)
 #pragma unroll
-        for (int u = 0; u < 16; ++u) buf(slot)[(16 * i + u) * kTmaPens + q] = v[u];
+        for (int u = 0; u < 16; ++u)
+          buf(slot)[(16 * i + (u ^ (i & 1))) * kTmaPens + q] = (i & 1) ? v[u ^ 1] : v[u];
       }
       __syncthreads();
       stockham_stage<16>(buf(slot), scratch, lq, pl, 16, pl.pmag[1], +1, tws);
