@@ -237,10 +237,11 @@ def time_gpu(p, s, steps, warmup, dist, device, tiles=None):
     return ctx, ms, n_it, launches, prof, clk.summary()
 
 
-def time_e2e(ctx, steps):
+def time_e2e(ctx, steps, warmup=1):
     """Same metric through the C ABI with host buffers: every step uploads the
     step-boundary state from pinned host memory, resumes, steps, and reads the
-    state back."""
+    state back.  `warmup` untimed rounds first (the first step after a resume
+    may capture its CUDA graph)."""
     import numpy as np
     import torch
 
@@ -261,6 +262,10 @@ def time_e2e(ctx, steps):
     h2d = sum(host[k].nbytes for k in ctx.STATE_FIELDS)
     if ctx.npart:
         h2d += sum(v.nbytes for v in host["part"].values()) + host["RHS_T"].nbytes
+    for _ in range(warmup):
+        ctx.upload_state(host)
+        ctx.step()
+        host = ctx.download_state(out=host)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
@@ -612,7 +617,7 @@ def gpu_main(args):
         accuracy = mixed_accuracy_fresh(p64, s, (1, 10))
         accuracy["after_timed_run"] = after
     hctx = ctxs[head]
-    e2e_ms, h2d, d2h = time_e2e(hctx, max(1, min(args.steps, 3)))
+    e2e_ms, h2d, d2h = time_e2e(hctx, max(1, min(args.steps, 5)))
     e2e_ms = max_over_ranks(e2e_ms, dist, "cuda")
     e2e_value = whole_job_rate(world, p64.ncell, 1, e2e_ms)
     r = res[head]

@@ -129,10 +129,14 @@ def test_fixed_fft_tiles_keep_results(capi, prec):
             ctx.set_fft_tiles(bad)
 
 
-def test_batch_matches_boxes_run_alone(capi):
+@pytest.mark.parametrize("prec", [P.PREC_FP64, P.PREC_MIXED])
+def test_batch_matches_boxes_run_alone(capi, prec):
+    """Boxes stepped together (one graph per step, a stream per box) are
+    bit-identical to each box run alone; on the mixed path the 32-wide boxes
+    take the TMA-fed passes."""
     shapes = [((16, 16, 16), 1000), ((24, 24, 24), 4000), ((32, 32, 32), 9000),
               ((32, 24, 16), 2500), ((16, 16, 16), 500)]
-    cases = [case(dims=d, npart=n, seed=10 + i, heat=0.3 * (i % 2))
+    cases = [case(dims=d, npart=n, seed=10 + i, heat=0.3 * (i % 2), prec=prec)
              for i, (d, n) in enumerate(shapes)]
     alone = [state(run(capi, p, s, 4)) for p, s in cases]
     for graph in (True, False):
