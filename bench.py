@@ -267,13 +267,26 @@ def time_e2e(ctx, steps, warmup=1):
         ctx.step()
         host = ctx.download_state(out=host)
     torch.cuda.synchronize()
+    parts = [0.0, 0.0, 0.0]  # upload and resume, step, download (host clock)
     t0 = time.perf_counter()
     for _ in range(steps):
+        ta = time.perf_counter()
         ctx.upload_state(host)
+        tb = time.perf_counter()
         ctx.step()
+        ctx.sync()
+        tc = time.perf_counter()
         host = ctx.download_state(out=host)
+        td = time.perf_counter()
+        parts[0] += tb - ta
+        parts[1] += tc - tb
+        parts[2] += td - tc
     torch.cuda.synchronize()
-    return (time.perf_counter() - t0) * 1e3 / steps, h2d, h2d
+    ms = (time.perf_counter() - t0) * 1e3 / steps
+    split = {"upload_and_resume_ms": round(parts[0] * 1e3 / steps, 3),
+             "step_ms": round(parts[1] * 1e3 / steps, 3),
+             "download_ms": round(parts[2] * 1e3 / steps, 3)}
+    return ms, h2d, h2d, split
 
 
 def cpu_sample(workload):
@@ -617,7 +630,7 @@ def gpu_main(args):
         accuracy = mixed_accuracy_fresh(p64, s, (1, 10))
         accuracy["after_timed_run"] = after
     hctx = ctxs[head]
-    e2e_ms, h2d, d2h = time_e2e(hctx, max(1, min(args.steps, 5)))
+    e2e_ms, h2d, d2h, e2e_split = time_e2e(hctx, max(1, min(args.steps, 5)))
     e2e_ms = max_over_ranks(e2e_ms, dist, "cuda")
     e2e_value = whole_job_rate(world, p64.ncell, 1, e2e_ms)
     r = res[head]
@@ -635,8 +648,8 @@ def gpu_main(args):
                    "l2": "inputs larger than L2 (working set ~8 GB per path)"},
         "roofline": dict(r["roofline"], peak_source=f"{peak_kind} HBM copy bandwidth"),
         "step_roofline": r["step_roofline"],
-        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+        "e2e": dict({"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                     "d2h_bytes_per_step": int(d2h)}, **e2e_split),
         "gpu_launches": int(r["launches"]),
         "clocks": r["clocks"],
         "kernels_ms_per_step": r["kernels_ms_per_step"],

@@ -1150,8 +1150,12 @@ void fft_plans_create(tpm_ctx *c) {
                              reinterpret_cast<const void *>(k_fft_yz_tma<true, true>)};
       bool fits = true;
       for (int d = 0; d < 3; ++d) {
+        // (the attribute belongs to the kernel, not to this context: it is set
+        // to the largest pencil the pass takes, so that contexts of different
+        // grids in one process never lower it below another's launches)
         const int smem = (int)tma_yz_smem(ns[d]);
-        TPM_CUDA_TRY(cudaFuncSetAttribute(kern[d], cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        TPM_CUDA_TRY(cudaFuncSetAttribute(kern[d], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)tma_yz_smem(256)));
         int per_sm = 0;
         TPM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern[d], 256, smem));
         if (d < 2) c->tma_fft_blocks[d] = per_sm * (c->sms > 0 ? c->sms : 1);
