@@ -302,7 +302,13 @@ enum {
                             the step-copy pointer swaps alternate, so two); the
                             Poisson stopping test then runs on the device.
                             Results are bit-identical to eager stepping.  Not used
-                            while profiling is on. */
+                            while profiling is on. */,
+  TPM_OPT_FFT_TMA = 4 /* mixed path: the y and z pencil passes take tiles of 8
+                         pencils moved by the TMA (1; the default where every
+                         pencil has at most 256 points) or plain tiles (0).
+                         tpm_autotune may turn either pass's TMA tiles off on a
+                         grid where plain tiles are faster.  Results do not
+                         depend on it.  (Not in the reference.) */
 };
 int tpm_set_option(tpm_ctx *ctx, int option, int value);
 

@@ -109,6 +109,26 @@ def test_autotune_keeps_results(capi):
     assert all(t in (128, 256, 512) for t in pens[3:])
 
 
+@pytest.mark.parametrize("dims", [(32, 48, 40), (32, 32, 256)])
+def test_fft_tma_tiles_keep_results(capi, dims):
+    """The mixed path's y and z passes with TMA tiles (the default; at 256
+    points the z pass with its middle stages in registers) and with plain
+    tiles give the same bits, eagerly and from graphs, and after autotuning."""
+    p, s = case(prec=P.PREC_MIXED, dims=dims, npart=4000, seed=8)
+    ref = state(run(capi, p, s, 3))
+    for graph in (False, True):
+        ctx = capi.Context(p, s.npart)
+        ctx.load(s)
+        ctx.set_option(capi.OPT_FFT_TMA, 0)
+        ctx.initialize()
+        if graph:
+            ctx.set_graph(True)
+        ctx.run(3)
+        ctx.sync()
+        assert_same(state(ctx), ref)
+    assert_same(state(run(capi, p, s, 3, graph=True, autotune=True)), ref)
+
+
 @pytest.mark.parametrize("prec", [P.PREC_FP64, P.PREC_MIXED])
 def test_fixed_fft_tiles_keep_results(capi, prec):
     # pencils 1, 2, 4 and odd thread counts against the default tiles

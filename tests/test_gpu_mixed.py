@@ -183,8 +183,8 @@ def test_mixed_restart_and_state_transfer_in_callers_order(capi, tmp_path):
     tpm_load_state continues like the first run.  Mixed runs whose inputs
     differ in rounding (here the in-cell order of the deposit sums, since a
     fresh context's particles start in the caller's order) part at the level
-    of their FP32 increments, ~1e-8 after two steps; a wrong particle order
-    would show as an O(1) difference."""
+    of their FP32 increments, 1e-8 to 1e-7 after two steps (held to 1e-6); a
+    wrong particle order would show as an O(1) difference."""
     p, s = setup(32, 6000, seed=13, heat=0.5, precision=P.PREC_MIXED)
     a = run(capi, p, s, 3)
     d = str(tmp_path)
@@ -212,7 +212,7 @@ def test_mixed_restart_and_state_transfer_in_callers_order(capi, tmp_path):
         ctx.sync()
     for x, y in ((b, b2), (c, a)):
         for g in ("RU", "RHO", "P", "C", "Q"):
-            assert rel_err(x.download_field(g), y.download_field(g)) <= 1e-7, g
+            assert rel_err(x.download_field(g), y.download_field(g)) <= 1e-6, g
         px, py = x.download_particles("base"), y.download_particles("base")
         for q in inputs.PQ:
-            assert rel_err(px[q], py[q]) <= 1e-7, q
+            assert rel_err(px[q], py[q]) <= 1e-6, q

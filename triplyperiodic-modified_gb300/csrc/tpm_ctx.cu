@@ -600,6 +600,11 @@ int tpm_set_option(tpm_ctx *c, int option, int value) {
       c->div_every_stage = value != 0;
       return TPM_OK;
     }
+    if (option == TPM_OPT_FFT_TMA) {
+      c->tma_y = c->tma_z = value != 0 && c->tma_fft;
+      tpm::graphs_clear(c->graphs);  // launch shapes changed
+      return TPM_OK;
+    }
     if (option == TPM_OPT_CUDA_GRAPH) {
       c->graph_mode = value != 0;
       return TPM_OK;

@@ -1162,6 +1162,7 @@ void fft_plans_create(tpm_ctx *c) {
         fits = fits && per_sm > 0;
       }
       c->tma_fft = fits;
+      c->tma_y = c->tma_z = fits;
     }
   }
 }
@@ -1201,7 +1202,7 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
   }
   const int tma_tiles = (g.nxh + kTmaPens - 1) / kTmaPens;
   auto y_pass = [&](int sign) {
-    if (f32 && c->tma_fft) {
+    if (f32 && c->tma_y) {
       const int ntiles = g.nz * tma_tiles;
       TPM_LAUNCH(c, "fft_y", k_fft_yz_tma<false>, std::min(ntiles, c->tma_fft_blocks[0]), 256,
                  tma_yz_smem(ply.n), g, ply, c->fft_map_y, sign,
@@ -1213,7 +1214,7 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
     TPM_LAUNCH(c, "fft_y", k_fft_y<T2>, blocks, ty, smem, g, ply, spec, npy, sign, skip);
   };
   y_pass(-1);
-  if (f32 && c->tma_fft) {
+  if (f32 && c->tma_z) {
     const int ntiles = g.ny * tma_tiles;
     // (one tile per block: the z pass's two transforms give its blocks enough
     // work between loads, and its tiles load while other blocks compute;

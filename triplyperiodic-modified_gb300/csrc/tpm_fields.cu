@@ -680,9 +680,12 @@ k_poisson_rhs_zm(Grid g, const float2 *__restrict__ inv_rho2, const double *__re
 // waits on no global load.  It reads 40 B per cell (Rho_new, RU_new 3, Q) and
 // writes 44 B (RHS, divergence, cc, C/d^2 pairs 3) where the two passes it
 // replaces moved 140 B (1/Rho pairs written by the density update and read
-// back, C as a double written and read back).  The arithmetic is the same
-// float-float arithmetic as those kernels: C = 2 rcp(Rho + Rho_m) and 1/Rho as
-// pairs, each face's flux RU C formed once and read by its two cells.
+// back, C as a double written and read back).  The arithmetic is the
+// float-float arithmetic of those kernels: C = 2 rcp(Rho + Rho_m) and 1/Rho as
+// pairs, each face's flux RU C formed once and read by its two cells; the
+// differences of neighbouring pairs (fluxes, 1/Rho) take one TwoSum on the
+// high parts (ff_sub_sloppy, within 2^-46 of the operands: about 1e-12 of the
+// divergence, a hundredth of the 1e-10 the projection is held to).
 namespace {
 
 struct PrSmem {
@@ -925,7 +928,7 @@ k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restri
       float2 lap = make_float2(0.f, 0.f);
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        const float2 sec = ff_add(ff_sub(pn[d], ir), ff_sub(mn[d], ir));
+        const float2 sec = ff_add(ff_sub_sloppy(pn[d], ir), ff_sub_sloppy(mn[d], ir));
         lap = ff_add(lap, ff_mul(sec, inv_d2[d]));
       }
       float2 Qc = ff_from_double(reinterpret_cast<const double *>(q_slot(k))[tid]);
@@ -941,7 +944,7 @@ k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restri
       float msum = 0.f;
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        divu = ff_add(divu, ff_mul(ff_sub(uhi[d], ulo[d]), inv_d[d]));
+        divu = ff_add(divu, ff_mul(ff_sub_sloppy(uhi[d], ulo[d]), inv_d[d]));
         msum += (clo[d].x + chi[d]) * 0.5f;
         if (tke_parts) {
           const double ul = ff_f2d(ulo[d].x);
@@ -989,8 +992,10 @@ k_poisson_rhs_tma(Grid g, const __grid_constant__ PrMaps m, DevScalars *__restri
 // at i0 - 2 (plane k - 1's stays in registers); Rho and the RK input of
 // Rho_np1 are plain coalesced loads issued before the wait.  One thread
 // issues the next plane's boxes into the other of two slots while the block
-// computes.  The arithmetic is the two kernels', operation for operation, so
-// the results are bit-identical.
+// computes.  The arithmetic is the two kernels' except for the differences
+// of neighbouring RU_int pairs, which take one TwoSum on the high parts
+// (ff_sub_sloppy: within 2^-46 of the operands, about 1e-15 of Rho per
+// stage, far below the FP32 parts of the mixed step) instead of two.
 namespace {
 
 struct RfSmem {
@@ -1105,9 +1110,9 @@ k_rho_face_tma(Grid g, const __grid_constant__ RfMaps m, DevScalars *__restrict_
     const float2 pz_p = ff_from_double(reinterpret_cast<const double *>(d + RfSmem::kRuz)[tid]);
     // Update_Rho: the divergence of RU_int as a pair, the FP64 state update
     const float2 px_c = ff_from_double(rux_c), py_c = ff_from_double(ruy_c);
-    float2 D = ff_mul(ff_sub(ff_from_double(rux_p), px_c), inv_d[0]);
-    D = ff_add(D, ff_mul(ff_sub(ff_from_double(ruy_p), py_c), inv_d[1]));
-    D = ff_add(D, ff_mul(ff_sub(pz_p, pz_c), inv_d[2]));
+    float2 D = ff_mul(ff_sub_sloppy(ff_from_double(rux_p), px_c), inv_d[0]);
+    D = ff_add(D, ff_mul(ff_sub_sloppy(ff_from_double(ruy_p), py_c), inv_d[1]));
+    D = ff_add(D, ff_mul(ff_sub_sloppy(pz_p, pz_c), inv_d[2]));
     const double Dd = ff_to_double(D);
     const double np1 = fma(a_np1, Dd, np1_b);
     const double nw = (stage != 3) ? fma(b_new, Dd, rho_b) : np1;

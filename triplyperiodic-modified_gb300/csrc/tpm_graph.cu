@@ -198,6 +198,17 @@ void autotune(tpm_ctx *c) {
   TPM_CUDA_TRY(cudaEventCreate(&e1));
   const int reps = 3;
   for (int d = 0; d < 3; ++d) {
+    // the y and z passes of the mixed path: TMA tiles of 8 pencils (fixed
+    // shape) against the best plain tiles found below; the TMA ones stay unless
+    // the plain ones are clearly faster (small grids, whose Nx/2 + 1 columns
+    // fill the 8-pencil tiles poorly)
+    bool *tma = (d == 1) ? &c->tma_y : (d == 2) ? &c->tma_z : nullptr;
+    double tma_ms = -1;
+    if (tma && c->tma_fft) {
+      *tma = true;
+      tma_ms = time_iterations(c, e0, e1, reps);
+      *tma = false;
+    }
     const int cap = pens_max(n_of[d], c->p.precision == TPM_PREC_MIXED ? 8 : 16);
     int best = c->pen[d];
     double best_ms = time_iterations(c, e0, e1, reps);
@@ -226,6 +237,7 @@ void autotune(tpm_ctx *c) {
       c->fthreads[d] = keep;
     }
     c->fthreads[d] = best_t;
+    if (tma_ms >= 0) *tma = !(best_ms < 0.97 * tma_ms);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

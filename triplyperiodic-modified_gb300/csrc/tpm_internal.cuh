@@ -273,7 +273,8 @@ struct tpm_ctx {
   // even number of float2 (a 16-byte multiple) so that the y and z pencil
   // passes move their tiles by TMA (tensor maps of the y and z tiles)
   int spec_pitch = 0;
-  bool tma_fft = false;
+  bool tma_fft = false;  // the y and z passes can take TMA tiles (mixed path, pencils <= 256)
+  bool tma_y = false, tma_z = false;  // ... and do (on by default; the autotuner may turn one off)
   int tma_fft_blocks[2] = {0, 0};  // persistent blocks of the y and z passes
   CUtensorMap fft_map_y, fft_map_z;
 
