@@ -638,9 +638,9 @@ __host__ __device__ __forceinline__ int tma_tile_bytes(int n) {
 
 // dynamic shared memory of k_fft_yz_tma: two tile buffers, the scratch
 // buffer, the n twiddles (an eighth of a tile, 128-byte rounded) and two
-// mbarriers
-__host__ __device__ __forceinline__ size_t tma_yz_smem(int n) {
-  return 3 * (size_t)tma_tile_bytes(n) + tma_tile_bytes(n) / kTmaPens + 16;
+// mbarriers; with one tile per block (ring = 1) a single tile buffer
+__host__ __device__ __forceinline__ size_t tma_yz_smem(int n, int ring = 2) {
+  return (ring + 1) * (size_t)tma_tile_bytes(n) + tma_tile_bytes(n) / kTmaPens + 16;
 }
 
 // z pass of a 256-point plan (two radix-16 stages), kFused: the forward
@@ -654,19 +654,23 @@ template <bool kZ, bool kFused = false>
 __global__ void __launch_bounds__(256, 4)
 k_fft_yz_tma(Grid g, FftPlan pl, const __grid_constant__ CUtensorMap map, int sign,
              const float *__restrict__ inv_mwn, const int *__restrict__ skip,
-             DevScalars *__restrict__ s, int ntiles) {
+             DevScalars *__restrict__ s, int ntiles, int ring) {
   if (skip && *skip) return;
   extern __shared__ __align__(1024) unsigned char sm[];
   const int tb = tma_tile_bytes(pl.n);
+  // ring = 2: persistent blocks, the next tile loading into the other buffer;
+  // ring = 1: one tile per block (the grid covers the tiles), one buffer
   auto buf = [&](int slot) { return reinterpret_cast<float2 *>(sm + slot * tb); };
-  float2 *scratch = reinterpret_cast<float2 *>(sm + 2 * tb);
-  float2 *tw = reinterpret_cast<float2 *>(sm + 3 * tb);  // the plan's twiddles, n entries
-  uint64_t *bar = reinterpret_cast<uint64_t *>(sm + 3 * tb + tma_tile_bytes(pl.n) / kTmaPens);
+  float2 *scratch = reinterpret_cast<float2 *>(sm + ring * tb);
+  float2 *tw = reinterpret_cast<float2 *>(sm + (ring + 1) * tb);  // the plan's twiddles
+  uint64_t *bar =
+      reinterpret_cast<uint64_t *>(sm + (ring + 1) * tb + tma_tile_bytes(pl.n) / kTmaPens);
   constexpr int lq = 3;  // log2(kTmaPens)
   const int tiles = (g.nxh + kTmaPens - 1) / kTmaPens;
   const unsigned bytes = (unsigned)(pl.n * kTmaPens * sizeof(float2));
   const int tot = kTmaPens * pl.n;
-  if (smem_u32(sm) & 127u) {  // never issue a box to a misaligned address
+  if ((smem_u32(sm) & 127u) || (ring == 1 && (int)gridDim.x < ntiles)) {
+    // never issue a box to a misaligned address, nor to a buffer in use
     if (threadIdx.x == 0) s->timeout = 1;
     return;
   }
@@ -804,7 +808,7 @@ k_fft_yz_tma(Grid g, FftPlan pl, const __grid_constant__ CUtensorMap map, int si
       // let the loads still in flight land (bounded) before the block's
       // shared memory is released
       mbar_wait(&bar[it & 1], (unsigned)(it >> 1) & 1u);
-      mbar_wait(&bar[(it + 1) & 1], (unsigned)((it + 1) >> 1) & 1u);
+      if (ring == 2) mbar_wait(&bar[(it + 1) & 1], (unsigned)((it + 1) >> 1) & 1u);
     }
     bulk_wait_read_all();
   }
@@ -1204,9 +1208,11 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
   auto y_pass = [&](int sign) {
     if (f32 && c->tma_y) {
       const int ntiles = g.nz * tma_tiles;
-      TPM_LAUNCH(c, "fft_y", k_fft_yz_tma<false>, std::min(ntiles, c->tma_fft_blocks[0]), 256,
-                 tma_yz_smem(ply.n), g, ply, c->fft_map_y, sign,
-                 static_cast<const float *>(nullptr), skip, c->dsc, ntiles);
+      // one tile per block, 128 threads (a stage's items): more blocks resident
+      // than persistent 256-thread blocks with two tile buffers
+      TPM_LAUNCH(c, "fft_y", k_fft_yz_tma<false>, ntiles, 128, tma_yz_smem(ply.n, 1), g, ply,
+                 c->fft_map_y, sign, static_cast<const float *>(nullptr), skip, c->dsc, ntiles,
+                 1);
       return;
     }
     int blocks = g.nz * ((g.nxh + npy - 1) / npy);
@@ -1218,15 +1224,16 @@ static void poisson_iteration_t(tpm_ctx *c, double eps_ctl, const LoopCtl *loop)
     const int ntiles = g.ny * tma_tiles;
     // (one tile per block: the z pass's two transforms give its blocks enough
     // work between loads, and its tiles load while other blocks compute;
-    // persistent blocks measured the same, 1.05 ms per 256^3 step)
+    // persistent blocks measured the same, 1.05 ms per 256^3 step; 128
+    // threads, one per item of a stage, where the divide allows)
     if (plz.nst == 2 && plz.radix[0] == 16 && plz.radix[1] == 16)
-      TPM_LAUNCH(c, "fft_z_solve", (k_fft_yz_tma<true, true>), ntiles, 256,
-                 tma_yz_smem(plz.n), g, plz, c->fft_map_z, -1,
-                 static_cast<const float *>(c->inv_mwn), skip, c->dsc, ntiles);
-    else
+      TPM_LAUNCH(c, "fft_z_solve", (k_fft_yz_tma<true, true>), ntiles, 128,
+                 tma_yz_smem(plz.n, 1), g, plz, c->fft_map_z, -1,
+                 static_cast<const float *>(c->inv_mwn), skip, c->dsc, ntiles, 1);
+    else  // (its divide preloads 8 modes per thread: 256 threads)
       TPM_LAUNCH(c, "fft_z_solve", k_fft_yz_tma<true>, ntiles, 256,
-                 tma_yz_smem(plz.n), g, plz, c->fft_map_z, -1,
-                 static_cast<const float *>(c->inv_mwn), skip, c->dsc, ntiles);
+                 tma_yz_smem(plz.n, 1), g, plz, c->fft_map_z, -1,
+                 static_cast<const float *>(c->inv_mwn), skip, c->dsc, ntiles, 1);
   } else {
     int blocks = g.ny * ((g.nxh + npz - 1) / npz);
     size_t smem = 2 * (size_t)npz * plz.n * sizeof(T2);
