@@ -190,7 +190,7 @@ __device__ __forceinline__ void momentum_rhs(const VF &V, const float fp[3], con
 }
 constexpr int kZPX = kZX + 2, kZPY = kZY + 2, kZPlane = kZPX * kZPY;
 
-__global__ void __launch_bounds__(kZX * kZY)
+__global__ void __launch_bounds__(kZX * kZY, 4)
 k_rhs_momentum_zm(Grid g, const float *__restrict__ U, const float *__restrict__ RUi,
                   const float *__restrict__ Fp, const double *__restrict__ Rho_int,
                   const double *__restrict__ RU, const double *__restrict__ np1_in,
@@ -210,35 +210,53 @@ k_rhs_momentum_zm(Grid g, const float *__restrict__ U, const float *__restrict__
   const float inv_d2[3] = {a.f_inv_d2[0], a.f_inv_d2[1], a.f_inv_d2[2]};
   const float a_fp = a.f_a_fp, b_gd = a.f_b_gd, c_lap = a.f_c_lap, A_ = a.f_A, Rho0 = a.f_Rho0;
   const float gv[3] = {a.f_g[0], a.f_g[1], a.f_g[2]};
-  // plane kk (any integer, wrapped) of the six fields into ring slot `slot`
-  auto load_plane = [&](int kk, int slot) {
+  // plane kk (any integer, wrapped) of the six fields: a thread's share of the
+  // 34 x 10 halo plane (at most two elements) is fetched into registers, then
+  // stored into a ring slot; the fetch of plane k + 2 is issued before plane k
+  // is computed, so its loads are in flight during the stencil
+  constexpr int kPer = (kZPlane + kZX * kZY - 1) / (kZX * kZY);
+  float pre[kPer][6];
+  auto fetch_plane = [&](int kk) {
     kk %= g.nz;
     if (kk < 0) kk += g.nz;
-    for (int e = threadIdx.x; e < kZPlane; e += kZX * kZY) {
-      const int hy = e / kZPX, hx = e - hy * kZPX;
-      int ii = i0 - 1 + hx, jj = j0 - 1 + hy;
-      while (ii < 0) ii += g.nx;
-      while (ii >= g.nx) ii -= g.nx;
-      while (jj < 0) jj += g.ny;
-      while (jj >= g.ny) jj -= g.ny;
-      const long long c = at(g, ii, jj, kk);
-      float v[6];
 #pragma unroll
-      for (int f = 0; f < 3; ++f) {
-        v[f] = U[f * g.n + c];
-        v[3 + f] = RUi[f * g.n + c];
+    for (int u = 0; u < kPer; ++u) {
+      const int e = threadIdx.x + u * kZX * kZY;
+      if (e < kZPlane) {
+        const int hy = e / kZPX, hx = e - hy * kZPX;
+        int ii = i0 - 1 + hx, jj = j0 - 1 + hy;  // one cell of halo: one wrap at most
+        ii = ii < 0 ? ii + g.nx : (ii >= g.nx ? ii - g.nx : ii);
+        jj = jj < 0 ? jj + g.ny : (jj >= g.ny ? jj - g.ny : jj);
+        const long long c = at(g, ii, jj, kk);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+          pre[u][f] = U[f * g.n + c];
+          pre[u][3 + f] = RUi[f * g.n + c];
+        }
       }
-#pragma unroll
-      for (int f = 0; f < 6; ++f) sp[slot][f][e] = v[f];
     }
   };
-  load_plane(k0 - 1, 0);
-  load_plane(k0, 1);
+  auto store_plane = [&](int slot) {
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const int e = threadIdx.x + u * kZX * kZY;
+      if (e < kZPlane) {
+#pragma unroll
+        for (int f = 0; f < 6; ++f) sp[slot][f][e] = pre[u][f];
+      }
+    }
+  };
+  fetch_plane(k0 - 1);
+  store_plane(0);
+  fetch_plane(k0);
+  store_plane(1);
+  fetch_plane(k0 + 1);
   int sm = 0, s0 = 1;  // ring slots of planes k - 1 and k
   for (int k = k0; k < k1; ++k) {
     const int sp1 = 3 - sm - s0;  // slot of plane k + 1
-    load_plane(k + 1, sp1);
+    store_plane(sp1);
     __syncthreads();
+    if (k + 1 < k1) fetch_plane(k + 2);
     if (live) {
       const int slot_of[3] = {sm, s0, sp1};
       // value of field f at the offset (dx, dy, dz) from the cell
@@ -248,9 +266,15 @@ k_rhs_momentum_zm(Grid g, const float *__restrict__ U, const float *__restrict__
       const long long c = at(g, i, j, k);
       const long long cm[3] = {at(g, wrap_m(i, g.nx), j, k), at(g, i, wrap_m(j, g.ny), k),
                                at(g, i, j, wrap_m(k, g.nz))};
+      // the cell's own inputs, loaded ahead of the stencil arithmetic
       float fp[3];
+      double in_np1[3], in_ru[3];
 #pragma unroll
-      for (int d = 0; d < 3; ++d) fp[d] = Fp[d * g.n + c];
+      for (int d = 0; d < 3; ++d) {
+        fp[d] = Fp[d * g.n + c];
+        in_np1[d] = np1_in[d * g.n + c];
+        in_ru[d] = a.stage != 3 ? RU[d * g.n + c] : 0.0;
+      }
       float rhs[3];
       momentum_rhs(V, fp, inv_d, inv_d2, a_fp, b_gd, c_lap, A_, rhs);
 #pragma unroll
@@ -260,9 +284,9 @@ k_rhs_momentum_zm(Grid g, const float *__restrict__ U, const float *__restrict__
           rhs[d] += (rf - Rho0) * gv[d];
         }
         const double r64 = ff_widen(rhs[d]);
-        const double np1 = fma(a.dtpo, r64, np1_in[d * g.n + c]);
+        const double np1 = fma(a.dtpo, r64, in_np1[d]);
         RU_np1[d * g.n + c] = np1;
-        RU_new[d * g.n + c] = (a.stage != 3) ? fma(a.dtpr, r64, RU[d * g.n + c]) : np1;
+        RU_new[d * g.n + c] = (a.stage != 3) ? fma(a.dtpr, r64, in_ru[d]) : np1;
       }
     }
     __syncthreads();  // plane k - 1's slot takes plane k + 2 next
