@@ -279,14 +279,15 @@ void aux_join(tpm_ctx *c, cudaEvent_t e) {
   TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, e, 0));
 }
 
-// One RK4 stage.  Three kernels run on the auxiliary stream beside the ones
-// they do not depend on (in a captured graph: parallel branches):
+// One RK4 stage.  Work runs on the auxiliary stream beside the kernels it
+// does not depend on (in a captured graph: parallel branches):
 //   face velocity U(RU_int, Rho_int)        beside the density update (unless
 //                                           the density pass forms it);
 //   face coefficients C(Rho_new) (mixed)    beside the particle push and deposits
 //                                           (unless the Poisson right-hand-side
 //                                           pass forms them);
-//   momentum RHS (needs F_p)                beside the heat deposit.
+//   momentum deposit (its own sort scratch) beside the heat deposit (with the
+//   and the momentum RHS (needs F_p)        concentration's swap).
 // Each writes buffers that the kernels beside it neither read nor write; the
 // stream joins back before their results are used (push, Poisson RHS).
 // While per-kernel profiling is on, everything stays on one stream so that
@@ -314,8 +315,10 @@ void substep(tpm_ctx *c, int s) {
   if (par && own_u && (c->p.precision != TPM_PREC_MIXED || c->PS))
     TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[0], 0));
   tpm::launch_particle_push(c, s, nb);
-  tpm::particle_deposit_momentum(c);
-  beside(2, [&] { tpm::launch_rhs_momentum(c, s, nb); });
+  beside(2, [&] {  // (F_p: the momentum deposit, then the RHS that reads it)
+    tpm::particle_deposit_momentum(c);
+    tpm::launch_rhs_momentum(c, s, nb);
+  });
   tpm::particle_deposit_concentration(c);
   tpm::particle_heat(c);
   if (c->PS) tpm::launch_passive_scalar(c, s, nb);  // simulation.cpp:65
@@ -511,9 +514,13 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
     c->starts_t = dalloc<int32_t>(c, n + 1);
     c->starts_r[0] = dalloc<int32_t>(c, n + 1);
     c->counts = dalloc<int32_t>(c, n);
+    c->counts_t = dalloc<int32_t>(c, n);
     c->unsorted = dalloc<unsigned char>(c, (n + 15) / 16 * 16);
+    c->unsorted_t = dalloc<unsigned char>(c, (n + 15) / 16 * 16);
     TPM_CUDA_TRY(cudaMemsetAsync(c->unsorted, 0, (n + 15) / 16 * 16, c->stream));
+    TPM_CUDA_TRY(cudaMemsetAsync(c->unsorted_t, 0, (n + 15) / 16 * 16, c->stream));
     c->scan_blocks = dalloc<int32_t>(c, (size_t)(n / 4096 + 2));
+    c->scan_blocks_t = dalloc<int32_t>(c, (size_t)(n / 4096 + 2));
     c->pay_t = dalloc<double>(c, 6 * (size_t)np);
     c->pay_t_s = dalloc<double>(c, 6 * (size_t)np);
     c->pay_r = dalloc<double>(c, 4 * (size_t)np);
@@ -526,9 +533,10 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
       c->pstage = dalloc<double>(c, np);
       tpm::particles_reorder_init(c);
     }
-    if (p->precision == TPM_PREC_MIXED)
+    if (p->precision == TPM_PREC_MIXED) {
       c->corner_sums = dalloc<float>(c, 16 * (size_t)n);
-    else
+      c->mom_sums = dalloc<float>(c, 6 * (size_t)n);
+    } else
       c->w8 = dalloc<double>(c, 16 * (size_t)np);
     c->C_next = dalloc<double>(c, n);
     if (p->Solver == 2) tpm::pcg_alloc(c);

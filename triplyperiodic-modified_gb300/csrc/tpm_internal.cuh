@@ -240,10 +240,13 @@ struct tpm_ctx {
   int32_t *key_t = nullptr, *key_r = nullptr;
   int32_t *perm_t = nullptr, *perm_r[1] = {nullptr};
   int32_t *starts_t = nullptr, *starts_r[1] = {nullptr};
-  int32_t *counts = nullptr;
-  // n rounded up to 16: cells the scatter left out of order (all zero between sorts)
-  unsigned char *unsorted = nullptr;
-  int32_t *scan_blocks = nullptr;
+  // the counting sorts' scratch, one set per sort (the momentum deposit's
+  // sort, _t, runs beside the heat deposit's): per-cell counts, the cells the
+  // scatter left out of order (n rounded up to 16; all zero between sorts),
+  // the scan's chunk totals
+  int32_t *counts = nullptr, *counts_t = nullptr;
+  unsigned char *unsorted = nullptr, *unsorted_t = nullptr;
+  int32_t *scan_blocks = nullptr, *scan_blocks_t = nullptr;
   double *pay_t = nullptr, *pay_t_s = nullptr;          // 6*np
   double *pay_r = nullptr;  // 4*np: round-indexed fractions and heat rate, unsorted
   // mixed path: particles kept in cell order (particle_reorder).  pid[s] is the
@@ -255,6 +258,7 @@ struct tpm_ctx {
   double *rhs_t2 = nullptr, *tau2 = nullptr, *pstage = nullptr;
   double *w8 = nullptr;  // 16*np corner weights (heat, concentration; sorted order)
   float *corner_sums = nullptr;  // mixed: 16*n per-source-cell corner sums (heat, conc.)
+  float *mom_sums = nullptr;     // mixed: 6*n per-source-cell momentum sums
   double *C_next = nullptr;  // concentration at this x_new = next substep's x_int
   // passive scalar (solve_for_scalar): RK copies, face values I_C2F(PS_new)
   // of the last stage, and the mean-free source field of S1_type 0

@@ -39,6 +39,7 @@ struct PushArgs {
   double iS;               // 1/(mp*Cvp), particle.cpp:483
   double iTth;             // Nu*pi*Dp*k, particle.cpp:470
   int stage, twc, has_tau;
+  int has_gp;              // any gp[d] nonzero
 };
 
 struct PState {
@@ -84,7 +85,8 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     }
     const int i0 = wrap_any(tx, g.nx), j0 = wrap_any(ty, g.ny), k0 = wrap_any(tz, g.nz);
     const long long c0 = at(g, i0, j0, k0);
-    double ug, vg, wg;
+    double ug = 0, vg = 0, wg = 0;  // FP64 path
+    float2 gq[3];                   // mixed path: the gas velocity as pairs
     if constexpr (!kMixed) {
       ug = xl * (double)U[at(g, wrap_p(i0, g.nx), j0, k0)] + (1 - xl) * (double)U[c0];
       vg = yl * (double)U[g.n + at(g, i0, wrap_p(j0, g.ny), k0)] + (1 - yl) * (double)U[g.n + c0];
@@ -108,14 +110,14 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
         return ff_norm(make_float2(2.f * q.x, 2.f * q.y));
       };
       auto lerp = [&](const float2 &f, const float2 &u0, const float2 &u1) {
-        return ff_to_double(ff_add(u0, ff_mul(f, ff_sub(u1, u0))));
+        return ff_add(u0, ff_mul(f, ff_sub(u1, u0)));
       };
       const float2 rxp = ff_from_double(Rhoi[cxp]), ryp = ff_from_double(Rhoi[cyp]),
                    rzp = ff_from_double(Rhoi[czp]);
-      ug = lerp(fx, uface(RUi[c0], r0, Rhoi[cxm]), uface(RUi[cxp], rxp, Rhoi[c0]));
-      vg = lerp(fy, uface(RUi[g.n + c0], r0, Rhoi[cym]), uface(RUi[g.n + cyp], ryp, Rhoi[c0]));
-      wg = lerp(fz, uface(RUi[2 * g.n + c0], r0, Rhoi[czm]),
-                uface(RUi[2 * g.n + czp], rzp, Rhoi[c0]));
+      gq[0] = lerp(fx, uface(RUi[c0], r0, Rhoi[cxm]), uface(RUi[cxp], rxp, Rhoi[c0]));
+      gq[1] = lerp(fy, uface(RUi[g.n + c0], r0, Rhoi[cym]), uface(RUi[g.n + cyp], ryp, Rhoi[c0]));
+      gq[2] = lerp(fz, uface(RUi[2 * g.n + c0], r0, Rhoi[czm]),
+                   uface(RUi[2 * g.n + czp], rzp, Rhoi[c0]));
     }
     // ---- update_position (particle.cpp:314-338) ----
     // (the mixed path, TU = float, accumulates with FMAs; the FP64 path keeps
@@ -132,10 +134,29 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     }
     // ---- update_velocity (particle.cpp:362-399) ----
     const double iTp = a.has_tau ? 1. / tau[p] : a.iTp;
-    const double rhs[3] = {(ug - ui) * iTp, (vg - vi) * iTp, (wg - wi) * iTp};
+    // RHS_u = (u_gas - u_int) / Tp; the mixed path forms it in pairs (within
+    // ~2^-44 of the FP64 value: the drag of a relaxing particle, a difference
+    // of close velocities, keeps its relative accuracy) with one FP64
+    // operation per component instead of four; rh: its FP32 value for the
+    // deposit payload
+    double rhs[3];
+    float rh[3];
+    if constexpr (kMixed) {
+      const float2 it2 = ff_from_double(iTp);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float2 r = ff_mul(ff_sub_sloppy(gq[d], ff_from_double(uint_[d])), it2);
+        rh[d] = r.x;
+        rhs[d] = ff_to_double(r);
+      }
+    } else {
+      rhs[0] = (ug - ui) * iTp;
+      rhs[1] = (vg - vi) * iTp;
+      rhs[2] = (wg - wi) * iTp;
+    }
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const double f = rhs[d] + a.gp[d];
+      const double f = (!kMixed || a.has_gp) ? rhs[d] + a.gp[d] : rhs[d];
       double np1 = kFma ? fma(a.dtpo, f, ps.np1_in[3 + d][p]) : ps.np1_in[3 + d][p] + a.dtpo * f;
       ps.np1[3 + d][p] = np1;
       ps.nw[3 + d][p] = (a.stage != 3) ? (kFma ? fma(a.dtpr, f, ps.b[3 + d][p])
@@ -153,7 +174,7 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
       key_t[p] = (int32_t)c0;
       if (kFma) {  // FP32 payload (mixed path): FP32 products of truncated copies
         const float xf = fx.x, yf = fy.x, zf = fz.x;
-        const float r0 = ff_hi(rhs[0]), r1 = ff_hi(rhs[1]), r2 = ff_hi(rhs[2]);
+        const float r0 = rh[0], r1 = rh[1], r2 = rh[2];
         pay_t[0 * np + p] = (TP)((1 - xf) * r0);
         pay_t[1 * np + p] = (TP)(xf * r0);
         pay_t[2 * np + p] = (TP)((1 - yf) * r1);
@@ -807,22 +828,26 @@ int pblocks(int64_t np) {
 }
 
 // sort `key` into perm / starts (deterministic cell-major, index-minor order)
-void sort_by_cell(tpm_ctx *c, const int32_t *key, int32_t *perm, int32_t *starts) {
+// with the momentum deposit's scratch set (mom) or the heat deposit's
+void sort_by_cell(tpm_ctx *c, const int32_t *key, int32_t *perm, int32_t *starts, bool mom) {
   const long long n = c->g.n;
-  TPM_CUDA_TRY(cudaMemsetAsync(c->counts, 0, sizeof(int32_t) * n, c->stream));
-  TPM_LAUNCH(c, "sort_hist", k_hist, pblocks(c->np), kThreads, 0, key, c->np, c->counts);
+  int32_t *counts = mom ? c->counts_t : c->counts;
+  int32_t *scan_blocks = mom ? c->scan_blocks_t : c->scan_blocks;
+  unsigned char *unsorted = mom ? c->unsorted_t : c->unsorted;
+  TPM_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int32_t) * n, c->stream));
+  TPM_LAUNCH(c, "sort_hist", k_hist, pblocks(c->np), kThreads, 0, key, c->np, counts);
   const int nchunks = (int)((n + kScanChunk - 1) / kScanChunk);
-  TPM_LAUNCH(c, "sort_scan_reduce", k_scan_reduce, nchunks, kScanThreads, 0, c->counts, n,
-             c->scan_blocks);
-  TPM_LAUNCH(c, "sort_scan_chunks", k_scan_chunks, 1, kScanThreads, 0, c->scan_blocks, nchunks);
-  TPM_LAUNCH(c, "sort_scan_apply", k_scan_apply, nchunks, kScanThreads, 0, c->counts, n,
-             c->scan_blocks, starts, (int32_t)c->np);
+  TPM_LAUNCH(c, "sort_scan_reduce", k_scan_reduce, nchunks, kScanThreads, 0, counts, n,
+             scan_blocks);
+  TPM_LAUNCH(c, "sort_scan_chunks", k_scan_chunks, 1, kScanThreads, 0, scan_blocks, nchunks);
+  TPM_LAUNCH(c, "sort_scan_apply", k_scan_apply, nchunks, kScanThreads, 0, counts, n,
+             scan_blocks, starts, (int32_t)c->np);
   TPM_LAUNCH(c, "sort_scatter", k_scatter, pblocks(c->np), kThreads, 0, key, c->np, starts,
-             c->counts, perm, c->unsorted);
+             counts, perm, unsorted);
   const long long nwords = (n + 15) / 16;
   TPM_LAUNCH(c, "sort_segsort", k_segsort,
              wave_blocks(c, reinterpret_cast<const void *>(k_segsort), kThreads, nwords, false),
-             kThreads, 0, nwords, starts, perm, reinterpret_cast<uint4 *>(c->unsorted),
+             kThreads, 0, nwords, starts, perm, reinterpret_cast<uint4 *>(unsorted),
              &c->dsc->crowded);
 }
 
@@ -910,6 +935,7 @@ void launch_particle_push(tpm_ctx *c, int s, bool np1_in_base) {
   a.stage = s;
   a.twc = c->p.TWC;
   a.has_tau = c->tau != nullptr;
+  a.has_gp = a.gp[0] != 0 || a.gp[1] != 0 || a.gp[2] != 0;
   if (c->p.precision == TPM_PREC_MIXED)
     TPM_LAUNCH(c, "particle_push", (k_push<float, float>), pblocks(c->np), kThreads, 0, c->g,
                pstate(c, np1_in_base), a, c->np, static_cast<const float *>(nullptr), c->RU_int,
@@ -932,17 +958,16 @@ void particle_deposit_momentum(tpm_ctx *c) {
       TPM_CUDA_TRY(cudaMemsetAsync(c->Fp, 0, sizeof(double) * 3 * c->g.n, c->stream));
     return;
   }
-  sort_by_cell(c, c->key_t, c->perm_t, c->starts_t);
+  sort_by_cell(c, c->key_t, c->perm_t, c->starts_t, true);
   if (mixed) {
-    // the 16 n corner-sum floats of the heat deposit hold these 6 n (the two
-    // deposits run one after the other)
+    // (its own scratch: it runs beside the heat deposit)
     TPM_LAUNCH(c, "deposit_momentum_cells", k_dep_mom_cells,
                cell_waves(c, k_dep_mom_cells, false), kThreads, 0,
                c->g, c->starts_t, c->perm_t, reinterpret_cast<const float *>(c->pay_t), c->np,
-               c->corner_sums);
+               c->mom_sums);
     TPM_LAUNCH(c, "deposit_momentum", k_dep_mom_faces, cell_waves(c, k_dep_mom_faces, false),
                kThreads, 0, c->g,
-               c->corner_sums, c->Fp32);
+               c->mom_sums, c->Fp32);
   } else {
     TPM_LAUNCH(c, "payload_gather_t", k_gather_payload<double>, pblocks(c->np), kThreads, 0, c->np,
                6, c->perm_t, c->pay_t, c->pay_t_s);
@@ -968,7 +993,7 @@ static void heat_deposit(tpm_ctx *c) {
   const bool mixed = c->p.precision == TPM_PREC_MIXED;
   const int nb = mixed ? cell_waves(c, k_dep_gather8, true)
                        : cell_waves(c, k_dep_sum8x2<double>, true);
-  sort_by_cell(c, c->key_r, c->perm_r[0], c->starts_r[0]);
+  sort_by_cell(c, c->key_r, c->perm_r[0], c->starts_r[0], false);
   double *parts = c->partials + kPartQ * kRedBlocks;
   if (mixed) {
     TPM_LAUNCH(c, "deposit_corner_sums", k_dep_corners, cell_waves(c, k_dep_corners, false),
