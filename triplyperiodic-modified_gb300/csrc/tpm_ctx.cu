@@ -857,6 +857,7 @@ int tpm_initialize(tpm_ctx *c) {
     }
     // grid.cpp:474 (Rho_face is recomputed from Rho_int where it is needed)
     // grid.cpp:481-484: initial particle heat coupling
+    c->counted_r = c->counted_t = false;  // (no push has counted the keys)
     tpm::particle_zero_fields(c);
     tpm::particle_init_heat(c);
     tpm::particle_reorder(c);
@@ -903,6 +904,7 @@ void resume_device(tpm_ctx *c) {
       TPM_CUDA_TRY(cudaMemcpyAsync(c->PS_int, c->PS, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
       tpm::launch_passive_scalar_face(c, c->PS);
     }
+    c->counted_r = c->counted_t = false;  // (no push has counted the keys)
     tpm::particle_resume(c);
     tpm::particle_reorder(c);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));

@@ -247,6 +247,9 @@ struct tpm_ctx {
   int32_t *counts = nullptr, *counts_t = nullptr;
   unsigned char *unsorted = nullptr, *unsorted_t = nullptr;
   int32_t *scan_blocks = nullptr, *scan_blocks_t = nullptr;
+  // the push has counted key_r / key_t into counts / counts_t (the next sort
+  // of each skips its histogram pass)
+  bool counted_r = false, counted_t = false;
   double *pay_t = nullptr, *pay_t_s = nullptr;          // 6*np
   double *pay_r = nullptr;  // 4*np: round-indexed fractions and heat rate, unsorted
   // mixed path: particles kept in cell order (particle_reorder).  pid[s] is the

@@ -51,17 +51,39 @@ struct PState {
   double *nw[7];
 };
 
+// a warp's keys (lanes in `live`) counted into their cells, one atomic per
+// distinct key (the counting sort's histogram; in cell order neighbouring
+// lanes share a cell)
+__device__ __forceinline__ void count_keys(unsigned live, bool mine, int32_t key,
+                                           int32_t *__restrict__ counts) {
+  if (mine) {
+    const int lane = threadIdx.x & 31;
+    const unsigned peers = __match_any_sync(live, key);
+    if (lane == __ffs(peers) - 1) atomicAdd(&counts[key], __popc(peers));
+  }
+}
+
 // TU: element type of the face velocity (FP32 copy on the mixed path);
-// TP: type of the momentum-deposit payload.
+// TP: type of the momentum-deposit payload.  cnt_t / cnt_r (when not null,
+// cleared): the per-cell counts of key_t / key_r, the two counting sorts'
+// histograms, formed here instead of by a pass over the keys.  A warp walks
+// the particles together (uniform trip count) for the counting.
 template <typename TU, typename TP>
-__global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__restrict__ U,
+__global__ void __launch_bounds__(kThreads, 4)
+k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__restrict__ U,
                        const double *__restrict__ RUi, const double *__restrict__ Rhoi,
                        const double *__restrict__ Tgas, double *__restrict__ rhs_t,
                        const double *__restrict__ tau, int32_t *__restrict__ key_t,
                        TP *__restrict__ pay_t, int32_t *__restrict__ key_r,
-                       TP *__restrict__ pay_r) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
-       p += (int64_t)gridDim.x * blockDim.x) {
+                       TP *__restrict__ pay_r, int32_t *__restrict__ cnt_t,
+                       int32_t *__restrict__ cnt_r) {
+  const int lane_ = threadIdx.x & 31;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane_; base < np;
+       base += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t p = base + lane_;
+  const unsigned live = __ballot_sync(0xffffffffu, p < np);
+  int32_t kt = 0, kr = 0;
+  if (p < np) {
     constexpr bool kMixed = sizeof(TU) == sizeof(float);
     const double xi = ps.in[0][p], yi = ps.in[1][p], zi = ps.in[2][p];
     const double ui = ps.in[3][p], vi = ps.in[4][p], wi = ps.in[5][p];
@@ -172,6 +194,7 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
     // ---- part2gas_velocity payload at x_int (particle.cpp:494-520) ----
     if (a.twc) {
       key_t[p] = (int32_t)c0;
+      kt = (int32_t)c0;
       if (kFma) {  // FP32 payload (mixed path): FP32 products of truncated copies
         const float xf = fx.x, yf = fy.x, zf = fz.x;
         const float r0 = rh[0], r1 = rh[1], r2 = rh[2];
@@ -291,7 +314,8 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
       rt = ff_f2d(sum) * a.iTth;
     }
     rhs_t[p] = rt;
-    key_r[p] = (int32_t)at(g, i1, j1, k1);
+    kr = (int32_t)at(g, i1, j1, k1);
+    key_r[p] = kr;
     if constexpr (kMixed) {  // the FP32 values the mixed deposit uses (x_l is one exactly)
       pay_r[0 * np + p] = ff_hi(x_l);
       pay_r[1 * np + p] = ff_hi(y_l);
@@ -303,6 +327,9 @@ __global__ void k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__re
       pay_r[2 * np + p] = z_l;
       pay_r[3 * np + p] = rt;
     }
+  }
+  if (cnt_t) count_keys(live, p < np, kt, cnt_t);
+  if (cnt_r) count_keys(live, p < np, kr, cnt_r);
   }
 }
 
@@ -834,8 +861,12 @@ void sort_by_cell(tpm_ctx *c, const int32_t *key, int32_t *perm, int32_t *starts
   int32_t *counts = mom ? c->counts_t : c->counts;
   int32_t *scan_blocks = mom ? c->scan_blocks_t : c->scan_blocks;
   unsigned char *unsorted = mom ? c->unsorted_t : c->unsorted;
-  TPM_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int32_t) * n, c->stream));
-  TPM_LAUNCH(c, "sort_hist", k_hist, pblocks(c->np), kThreads, 0, key, c->np, counts);
+  bool &counted = mom ? c->counted_t : c->counted_r;
+  if (!counted) {  // (after a push the histogram is already there)
+    TPM_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int32_t) * n, c->stream));
+    TPM_LAUNCH(c, "sort_hist", k_hist, pblocks(c->np), kThreads, 0, key, c->np, counts);
+  }
+  counted = false;
   const int nchunks = (int)((n + kScanChunk - 1) / kScanChunk);
   TPM_LAUNCH(c, "sort_scan_reduce", k_scan_reduce, nchunks, kScanThreads, 0, counts, n,
              scan_blocks);
@@ -936,16 +967,24 @@ void launch_particle_push(tpm_ctx *c, int s, bool np1_in_base) {
   a.twc = c->p.TWC;
   a.has_tau = c->tau != nullptr;
   a.has_gp = a.gp[0] != 0 || a.gp[1] != 0 || a.gp[2] != 0;
+  // the two sorts' histograms (the momentum deposit's only with two-way
+  // coupling) are counted by the push
+  const long long n = c->g.n;
+  TPM_CUDA_TRY(cudaMemsetAsync(c->counts, 0, sizeof(int32_t) * n, c->stream));
+  if (a.twc) TPM_CUDA_TRY(cudaMemsetAsync(c->counts_t, 0, sizeof(int32_t) * n, c->stream));
+  int32_t *cnt_t = a.twc ? c->counts_t : nullptr;
+  c->counted_t = a.twc != 0;
+  c->counted_r = true;
   if (c->p.precision == TPM_PREC_MIXED)
     TPM_LAUNCH(c, "particle_push", (k_push<float, float>), pblocks(c->np), kThreads, 0, c->g,
                pstate(c, np1_in_base), a, c->np, static_cast<const float *>(nullptr), c->RU_int,
                c->Rho_int, c->Tgas, c->rhs_t, c->tau, c->key_t,
                reinterpret_cast<float *>(c->pay_t), c->key_r,
-               reinterpret_cast<float *>(c->pay_r));
+               reinterpret_cast<float *>(c->pay_r), cnt_t, c->counts);
   else
     TPM_LAUNCH(c, "particle_push", (k_push<double, double>), pblocks(c->np), kThreads, 0, c->g,
                pstate(c, np1_in_base), a, c->np, c->U, nullptr, nullptr, c->Tgas, c->rhs_t, c->tau, c->key_t,
-               c->pay_t, c->key_r, c->pay_r);
+               c->pay_t, c->key_r, c->pay_r, cnt_t, c->counts);
 }
 
 // two-way momentum source at x_int (grid.cpp:877)
