@@ -69,7 +69,7 @@ __device__ __forceinline__ void count_keys(unsigned live, bool mine, int32_t key
 // histograms, formed here instead of by a pass over the keys.  A warp walks
 // the particles together (uniform trip count) for the counting.
 template <typename TU, typename TP>
-__global__ void __launch_bounds__(kThreads, sizeof(TU) == sizeof(float) ? 4 : 1)
+__global__ void __launch_bounds__(kThreads, sizeof(TU) == sizeof(float) ? 4 : 3)
 k_push(Grid g, PState ps, PushArgs a, int64_t np, const TU *__restrict__ U,
                        const double *__restrict__ RUi, const double *__restrict__ Rhoi,
                        const double *__restrict__ Tgas, double *__restrict__ rhs_t,
