@@ -693,12 +693,10 @@ k_fft_yz_tma(Grid g, FftPlan pl, const __grid_constant__ CUtensorMap map, int si
     mbar_init_fence();
     if ((int)blockIdx.x < ntiles) load(blockIdx.x, 0);
   }
-  // the twiddles in shared memory for all of the block's tiles (a block with
-  // one tile reads them from the plan: the copy would cost more than it saves)
-  const bool one_tile = (int)gridDim.x >= ntiles;
-  if (!one_tile)
-    for (int m = threadIdx.x; m < pl.n; m += blockDim.x) tw[m] = pl.tw32[m];
-  const float2 *tws = one_tile ? nullptr : tw;
+  // the plan's twiddles in shared memory (copied while the first tile loads:
+  // the stages then read them without an L1 round trip)
+  for (int m = threadIdx.x; m < pl.n; m += blockDim.x) tw[m] = pl.tw32[m];
+  const float2 *tws = tw;
   __syncthreads();
   // a transform ends in its input buffer after an even number of Stockham
   // stages (the z pass runs two transforms of the same plan): then the store
