@@ -39,9 +39,9 @@ FALLBACK_HBM_GBS = 6800.0
 # capture of every kernel of this bench's two profiled steps (the command is
 # in the summary of the capture)
 NCU_TRAFFIC = {
-    ("box256_p8e6_heated", True, "fft_x_fwd_resid"): 8.654e8,
-    ("box256_p8e6_heated", True, "particle_push"): 3.557e9,
-    ("box256_p8e6_heated", True, "rhs_momentum"): 2.009e9,
+    ("box256_p8e6_heated", True, "fft_x_fwd_resid"): 8.644e8,
+    ("box256_p8e6_heated", True, "particle_push"): 3.849e9,
+    ("box256_p8e6_heated", True, "rhs_momentum"): 2.007e9,
     ("box256_p8e6_heated", True, "poisson_rhs"): 1.279e9,
     ("box256_p8e6_heated", True, "rho_update"): 1.347e9,
     ("box256_p8e6_heated", False, "rhs_momentum"): 2.595e9,
