@@ -177,6 +177,19 @@ int tpm_load_state(tpm_ctx *ctx, const double *RU, const double *RU_int, const d
 int tpm_save_state(tpm_ctx *ctx, double *RU, double *RU_int, double *Rho, double *P,
                    double *const *part, double *rhs_t, tpm_scalars *scalars);
 
+/* tpm_load_state, one tpm_step and tpm_save_state in one call, with the same
+ * results bit for bit, the host transfers overlapping the step: RU and P go up
+ * while the resume and the first stage's particle stage run, the particles,
+ * their heat rates and Rho come down during the last stage's pressure solve.
+ * The inputs and outputs may be the same arrays.  Steps from a CUDA graph per
+ * piece when TPM_OPT_CUDA_GRAPH is on.  (Not in the reference: its state is
+ * host memory throughout.) */
+int tpm_step_state(tpm_ctx *ctx, const double *RU, const double *RU_int, const double *Rho,
+                   const double *P, const double *const *part, const double *rhs_t, double P0,
+                   double T_cur, int64_t num_timestep, double *RU_out, double *RU_int_out,
+                   double *Rho_out, double *P_out, double *const *part_out, double *rhs_t_out,
+                   tpm_scalars *scalars);
+
 /* Restart files in the reference's format, the set its Initial=1 branch reads
  * (grid.cpp:221-238, particle.cpp:939-989): Restart_RU.bin, Restart_Rho.bin,
  * Restart_P.bin (raw FP64, [Nz][Ny][Nx], RU as x,y,z blocks),

@@ -171,3 +171,39 @@ def test_batch_matches_boxes_run_alone(capi, prec):
         for box, want in zip(b.boxes, alone):
             assert_same(state(box), want)
         b.close()
+
+@pytest.mark.parametrize("prec,graph", [(P.PREC_FP64, False), (P.PREC_MIXED, False),
+                                        (P.PREC_MIXED, True)])
+def test_step_state_equals_load_step_save(capi, prec, graph):
+    """tpm_step_state (one call: load the host state, step, save it, the
+    transfers overlapping the step) gives the bits of tpm_load_state +
+    tpm_step + tpm_save_state, step after step, also in place; the context
+    then steps on as usual."""
+    import copy
+
+    p, s = case(prec=prec, dims=(32, 32, 32), npart=6000, seed=21, heat=0.4)
+    a = run(capi, p, s, 1)
+    st0 = a.download_state()
+    ref = copy.deepcopy(st0)
+    b = capi.Context(p, s.npart)
+    b.set_graph(graph)
+    for _ in range(3):
+        b.upload_state(ref)
+        b.step()
+        ref = b.download_state()
+    c = capi.Context(p, s.npart)
+    c.set_graph(graph)
+    cur = copy.deepcopy(st0)
+    for k in range(3):
+        cur = c.step_state(cur, out=cur if k else None)
+    for f in capi.Context.STATE_FIELDS:
+        assert np.array_equal(cur[f], ref[f]), f
+    for q in cur["part"]:
+        assert np.array_equal(cur["part"][q], ref["part"][q]), q
+    assert np.array_equal(cur["RHS_T"], ref["RHS_T"])
+    for k in ("P0", "T_cur", "num_timestep"):
+        assert cur["scalars"][k] == ref["scalars"][k], k
+    b.step()
+    c.step()
+    for f in ("RU", "RHO", "P", "C", "Q"):
+        assert np.array_equal(b.download_field(f), c.download_field(f)), f

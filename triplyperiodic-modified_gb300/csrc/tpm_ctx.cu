@@ -292,16 +292,24 @@ void aux_join(tpm_ctx *c, cudaEvent_t e) {
 // stream joins back before their results are used (push, Poisson RHS).
 // While per-kernel profiling is on, everything stays on one stream so that
 // each kernel's events time that kernel alone.
-void substep(tpm_ctx *c, int s) {
+//
+// A stage runs as its head (through the particle push) and its tail; a step
+// whose host transfers overlap it (tpm_step_state) captures them in separate
+// graphs, and then the head joins the auxiliary stream at its end so that
+// each captured piece holds whole fork/join pairs (join_aux).
+template <typename F>
+void beside_aux(tpm_ctx *c, int fork, F &&launch) {
+  if (c->prof_on) return launch();
+  aux_fork(c, c->fork_ev[fork]);
+  OnStream on(c, c->aux);
+  launch();
+}
+
+void stage_head(tpm_ctx *c, int s, bool join_aux) {
   refresh_rui32(c);
   const bool nb = c->np1_is_base;
   const bool par = !c->prof_on;
-  auto beside = [&](int fork, auto &&launch) {
-    if (!par) return launch();
-    aux_fork(c, c->fork_ev[fork]);
-    OnStream on(c, c->aux);
-    launch();
-  };
+  auto beside = [&](int fork, auto &&launch) { beside_aux(c, fork, launch); };
   tpm::launch_p0_update(c, s);
   const bool own_u = !tpm::face_velocity_in_rho_pass(c);
   if (own_u) {
@@ -315,6 +323,13 @@ void substep(tpm_ctx *c, int s) {
   if (par && own_u && (c->p.precision != TPM_PREC_MIXED || c->PS))
     TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join_ev[0], 0));
   tpm::launch_particle_push(c, s, nb);
+  if (par && join_aux) aux_join(c, c->join_ev[1]);
+}
+
+void stage_tail(tpm_ctx *c, int s) {
+  const bool nb = c->np1_is_base;
+  const bool par = !c->prof_on;
+  auto beside = [&](int fork, auto &&launch) { beside_aux(c, fork, launch); };
   beside(2, [&] {  // (F_p: the momentum deposit, then the RHS that reads it)
     tpm::particle_deposit_momentum(c);
     tpm::launch_rhs_momentum(c, s, nb);
@@ -332,8 +347,14 @@ void substep(tpm_ctx *c, int s) {
   c->np1_is_base = false;
 }
 
-// grid::TimeAdvance (grid.cpp:595-606): the step copies base = np1
-void time_advance(tpm_ctx *c) {
+void substep(tpm_ctx *c, int s) {
+  stage_head(c, s, false);
+  stage_tail(c, s);
+}
+
+// grid::TimeAdvance (grid.cpp:595-606): the step copies base = np1; the
+// particle reorder that follows may be left to the caller (reorder = false)
+void time_advance(tpm_ctx *c, bool reorder = true) {
   std::swap(c->Rho, c->Rho_np1);
   std::swap(c->PS, c->PS_np1);  // grid.cpp:598
   for (int q = 0; q < 7; ++q) std::swap(c->pq[0][q], c->pq[3][q]);
@@ -346,13 +367,13 @@ void time_advance(tpm_ctx *c) {
   c->stage_next = 0;
   c->ph_done = 0;
   c->p0_called = false;
-  tpm::particle_reorder(c);  // mixed path: cell order of the stage-3 positions
+  if (reorder) tpm::particle_reorder(c);  // mixed path: cell order of the stage-3 positions
 }
 
-void end_step(tpm_ctx *c) {
+void end_step(tpm_ctx *c, bool reorder = true) {
   // simulation.cpp:80 (RU_np1.make_mean_U0) then grid::TimeAdvance
   tpm::launch_mean_reset(c);
-  time_advance(c);
+  time_advance(c, reorder);
 }
 
 }  // namespace
@@ -362,6 +383,9 @@ namespace tpm {
 void step_param_update(tpm_ctx *c) { param_update(c); }
 void step_substep(tpm_ctx *c, int s) { substep(c, s); }
 void step_end(tpm_ctx *c) { end_step(c); }
+void step_stage_head(tpm_ctx *c, int s) { stage_head(c, s, true); }
+void step_stage_tail(tpm_ctx *c, int s) { stage_tail(c, s); }
+void step_end_no_reorder(tpm_ctx *c) { end_step(c, false); }
 
 void step_body(tpm_ctx *c) {
   for (int s = 0; s < 4; ++s) substep(c, s);
@@ -584,12 +608,16 @@ int tpm_destroy(tpm_ctx *c) {
       cudaEventDestroy(ev.second);
     }
   tpm::graphs_clear(c->graphs);
+  tpm::graphs_clear(c->piece_graphs);
   for (void *p : c->allocs) cudaFree(p);
   if (c->fft_mem) cudaFree(c->fft_mem);
   if (c->hsc) cudaFreeHost(c->hsc);
   if (c->stream) cudaStreamDestroy(c->stream);
   if (c->side) cudaStreamDestroy(c->side);
   if (c->aux) cudaStreamDestroy(c->aux);
+  if (c->io) cudaStreamDestroy(c->io);
+  for (cudaEvent_t e : c->io_ev)
+    if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : c->fork_ev)
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t e : c->join_ev)
@@ -611,6 +639,7 @@ int tpm_set_option(tpm_ctx *c, int option, int value) {
     if (option == TPM_OPT_FFT_TMA) {
       c->tma_y = c->tma_z = value != 0 && c->tma_fft;
       tpm::graphs_clear(c->graphs);  // launch shapes changed
+      tpm::graphs_clear(c->piece_graphs);
       return TPM_OK;
     }
     if (option == TPM_OPT_CUDA_GRAPH) {
@@ -816,6 +845,107 @@ int tpm_save_state(tpm_ctx *c, double *RU, double *RU_int, double *Rho, double *
       tpm::particles_to_host(c, rhs_t, c->rhs_t, 8);
     }
     pull_scalars(c);  // synchronises the copies above
+    if (sc) {
+      sc->P0 = c->hsc->P0;
+      sc->P0_int = c->hsc->P0_int;
+      sc->P0_new = c->hsc->P0_new;
+      sc->P0_np1 = c->hsc->P0;
+      sc->T_cur = c->T_cur;
+      sc->num_timestep = c->num_timestep;
+      sc->last_poisson_iterations = c->hsc->it;
+      sc->total_poisson_iterations = c->hsc->it_sum;
+      sc->last_poisson_error = c->p.epsilon > 0 ? c->last_err : c->hsc->err;
+      sc->max_abs_div = c->p.precision == TPM_PREC_MIXED ? c->hsc->max_div : -1.0;
+    }
+    return TPM_OK;
+  });
+}
+
+// tpm_load_state + tpm_step + tpm_save_state in one call, the transfers
+// overlapping the step: what the resume and the first stage's head read goes
+// up first on the step's stream; RU and P (first read in that stage's tail) go
+// up on a copy stream meanwhile; the particles, their heat rates and Rho,
+// final after the last stage's push, go down on the copy stream during that
+// stage's tail; RU, RU_int and P go down beside the particle reorder.  The
+// step runs as four captured pieces with the stream waits between them.
+int tpm_step_state(tpm_ctx *c, const double *RU, const double *RU_int, const double *Rho,
+                   const double *P, const double *const *part, const double *rhs_t, double P0,
+                   double T_cur, int64_t num_timestep, double *RU_out, double *RU_int_out,
+                   double *Rho_out, double *P_out, double *const *part_out, double *rhs_t_out,
+                   tpm_scalars *sc) {
+  return guarded(c, [&]() -> int {
+    if (!RU || !RU_int || !Rho || !P || !RU_out || !RU_int_out || !Rho_out || !P_out ||
+        (c->np > 0 && (!part || !rhs_t || !part_out || !rhs_t_out)))
+      return fail(c, TPM_ERR_ARG, "null buffer");
+    for (int q = 0; q < 7 && c->np > 0; ++q)
+      if (!part[q] || !part_out[q]) return fail(c, TPM_ERR_ARG, "null particle array");
+    if (c->stage_next || c->ph_done)
+      return fail(c, TPM_ERR_STATE, "a step is in progress through the substep or phase calls");
+    if (!c->io) {
+      TPM_CUDA_TRY(cudaStreamCreateWithFlags(&c->io, cudaStreamNonBlocking));
+      for (cudaEvent_t &e : c->io_ev)
+        TPM_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    const long long n = c->g.n;
+    const auto up = cudaMemcpyHostToDevice, down = cudaMemcpyDeviceToHost;
+    // 1. up on the step's stream: what the resume and stage 0's head read
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->Rho, Rho, sizeof(double) * n, up, c->stream));
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->RU_int, RU_int, sizeof(double) * 3 * n, up, c->stream));
+    if (c->np > 0) {
+      for (int q = 0; q < 7; ++q) tpm::particles_from_host(c, c->pq[0][q], part[q], 8);
+      tpm::particles_from_host(c, c->rhs_t, rhs_t, 8);
+    }
+    TPM_CUDA_TRY(cudaEventRecord(c->io_ev[0], c->stream));
+    // 2. up on the copy stream after them: RU and P
+    TPM_CUDA_TRY(cudaStreamWaitEvent(c->io, c->io_ev[0], 0));
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->RU, RU, sizeof(double) * 3 * n, up, c->io));
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->P, P, sizeof(double) * n, up, c->io));
+    TPM_CUDA_TRY(cudaEventRecord(c->io_ev[1], c->io));
+    pull_scalars(c);  // synchronises the step's stream (the copy stream goes on)
+    c->hsc->P0 = P0;
+    push_scalars(c);
+    c->T_cur = T_cur;
+    c->num_timestep = num_timestep;
+    tpm::resume_device(c);  // reads neither RU nor P
+    // 3. the step: stage 0's head, then (RU and P landed) up to stage 3's push
+    tpm::step_param_update(c);
+    tpm::run_piece(c, 1, false, [&] { tpm::step_stage_head(c, 0); });
+    TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->io_ev[1], 0));
+    tpm::run_piece(c, 2, false, [&] {
+      tpm::step_stage_tail(c, 0);
+      tpm::step_substep(c, 1);
+      tpm::step_substep(c, 2);
+      tpm::step_stage_head(c, 3);
+    });
+    TPM_CUDA_TRY(cudaEventRecord(c->io_ev[2], c->stream));
+    // 4. down on the copy stream during stage 3's tail: the particles (the np1
+    // set stage 3's push wrote, the base set after the step), their heat
+    // rates, and Rho (Rho_np1 after stage 3's density update)
+    {
+      TPM_CUDA_TRY(cudaStreamWaitEvent(c->io, c->io_ev[2], 0));
+      OnStream on(c, c->io);
+      if (c->np > 0) {
+        for (int q = 0; q < 7; ++q) tpm::particles_to_host(c, part_out[q], c->pq[3][q], 8);
+        tpm::particles_to_host(c, rhs_t_out, c->rhs_t, 8);
+      }
+      TPM_CUDA_TRY(cudaMemcpyAsync(Rho_out, c->Rho_np1, sizeof(double) * n, down, c->io));
+      TPM_CUDA_TRY(cudaEventRecord(c->io_ev[3], c->io));
+    }
+    tpm::run_piece(c, 3, true, [&] {
+      tpm::step_stage_tail(c, 3);
+      tpm::step_end_no_reorder(c);
+    });
+    TPM_CUDA_TRY(cudaEventRecord(c->io_ev[4], c->stream));
+    // 5. the reorder permutes what those copies read: after them
+    TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->io_ev[3], 0));
+    tpm::particle_reorder(c);
+    // 6. down on the copy stream beside the reorder: RU, RU_int and P
+    TPM_CUDA_TRY(cudaStreamWaitEvent(c->io, c->io_ev[4], 0));
+    TPM_CUDA_TRY(cudaMemcpyAsync(RU_out, c->RU, sizeof(double) * 3 * n, down, c->io));
+    TPM_CUDA_TRY(cudaMemcpyAsync(RU_int_out, c->RU_int, sizeof(double) * 3 * n, down, c->io));
+    TPM_CUDA_TRY(cudaMemcpyAsync(P_out, c->P, sizeof(double) * n, down, c->io));
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->io));
+    pull_scalars(c);
     if (sc) {
       sc->P0 = c->hsc->P0;
       sc->P0_int = c->hsc->P0_int;

@@ -42,6 +42,8 @@ HostState snapshot(const tpm_ctx *c) {
   h.q_parts = c->q_parts;
   h.np1_is_base = c->np1_is_base; h.rui32_stale = c->rui32_stale; h.stepped = c->stepped;
   h.store_div = c->store_div; h.div_every_stage = c->div_every_stage;
+  h.stage_next = c->stage_next; h.ph_done = (int)c->ph_done; h.p0_called = c->p0_called;
+  h.counted_r = c->counted_r; h.counted_t = c->counted_t;
   h.Iteration = c->Iteration;
   std::memcpy(h.pen, c->pen, sizeof(h.pen));
   h.A = c->A; h.gx = c->gx; h.gy = c->gy; h.gz = c->gz; h.I0 = c->I0;
@@ -57,6 +59,8 @@ void restore(tpm_ctx *c, const HostState &h) {
   c->PS = h.PS; c->PS_int = h.PS_int; c->PS_new = h.PS_new; c->PS_np1 = h.PS_np1;
   c->q_parts = h.q_parts;
   c->np1_is_base = h.np1_is_base; c->rui32_stale = h.rui32_stale; c->stepped = h.stepped;
+  c->stage_next = h.stage_next; c->ph_done = (unsigned)h.ph_done; c->p0_called = h.p0_called;
+  c->counted_r = h.counted_r; c->counted_t = h.counted_t;
 }
 
 bool same(const HostState &a, const HostState &b) { return std::memcmp(&a, &b, sizeof(a)) == 0; }
@@ -172,6 +176,65 @@ void step_any(tpm_ctx *c) {
     step_param_update(c);
     step_body(c);
   }
+}
+
+void run_piece(tpm_ctx *c, int piece, bool advances, const std::function<void()> &body) {
+  if (!c->graph_mode || c->prof_on) {
+    body();
+    return;
+  }
+  const HostState pre = snapshot(c);
+  GraphEntry *hit = nullptr;
+  for (GraphEntry &e : c->piece_graphs)
+    if (e.piece == piece && same(e.pre[0], pre)) {
+      hit = &e;
+      break;
+    }
+  if (hit) {
+    restore(c, hit->post[0]);
+    if (advances) {
+      c->T_cur += c->p.dt;  // grid::TimeAdvance (grid.cpp:604-605)
+      c->num_timestep++;
+    }
+    c->launches += hit->launches[0];
+    c->last_it = -1;
+  } else {
+    if (c->piece_graphs.size() >= 2 * kMaxGraphs) {
+      cudaGraphExecDestroy(c->piece_graphs.front().exec);
+      c->piece_graphs.erase(c->piece_graphs.begin());
+    }
+    GraphEntry e;
+    e.piece = piece;
+    e.pre = {pre};
+    const double t0 = c->T_cur;
+    const int64_t n0 = c->num_timestep, l0 = c->launches;
+    cudaGraph_t graph = nullptr;
+    TPM_CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      c->device_loop = true;
+      body();
+      c->device_loop = false;
+      TPM_CUDA_TRY(cudaStreamEndCapture(c->stream, &graph));
+    } catch (...) {
+      cudaGraph_t g2 = nullptr;
+      cudaStreamEndCapture(c->stream, &g2);
+      if (g2) cudaGraphDestroy(g2);
+      cudaGetLastError();
+      c->device_loop = false;
+      restore(c, pre);
+      c->T_cur = t0;
+      c->num_timestep = n0;
+      throw;
+    }
+    e.launches = {c->launches - l0};
+    cudaError_t err = cudaGraphInstantiate(&e.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    TPM_CUDA_TRY(err);
+    e.post = {snapshot(c)};
+    c->piece_graphs.push_back(std::move(e));
+    hit = &c->piece_graphs.back();
+  }
+  TPM_CUDA_TRY(cudaGraphLaunch(hit->exec, c->stream));
 }
 
 void graphs_clear(std::vector<GraphEntry> &cache) {
@@ -294,6 +357,7 @@ int tpm_autotune(tpm_ctx *c, int *pens_out) {
   return tpm::guarded(c, [&]() -> int {
     tpm::autotune(c);
     tpm::graphs_clear(c->graphs);  // launch shapes changed
+    tpm::graphs_clear(c->piece_graphs);
     if (pens_out)
       for (int d = 0; d < 3; ++d) {
         pens_out[d] = c->pen[d];
@@ -321,6 +385,7 @@ int tpm_set_fft_tiles(tpm_ctx *c, const int *tiles) {
       c->fthreads[d] = tiles[3 + d];
     }
     tpm::graphs_clear(c->graphs);  // launch shapes changed
+    tpm::graphs_clear(c->piece_graphs);
     return TPM_OK;
   });
 }

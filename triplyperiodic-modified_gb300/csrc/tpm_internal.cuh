@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <functional>
 #include <new>
 #include <string>
 #include <utility>
@@ -134,6 +135,7 @@ struct HostState {
   const double *tau;
   int q_parts;
   int np1_is_base, rui32_stale, stepped, store_div, div_every_stage;
+  int stage_next, ph_done, p0_called, counted_r, counted_t;  // (mid-step pieces)
   int Iteration;
   int pen[3];
   double A, gx, gy, gz, I0;
@@ -153,6 +155,7 @@ struct GraphEntry {
   std::vector<HostState> pre, post;
   std::vector<int64_t> launches;
   cudaGraphExec_t exec = nullptr;
+  int piece = 0;  // the piece of a split step (tpm_step_state), 0 for a whole step
 };
 
 }  // namespace tpm
@@ -293,6 +296,10 @@ struct tpm_ctx {
   // ---- CUDA graph replay of whole steps (tpm_graph.cu) ----
   bool graph_mode = false;
   std::vector<tpm::GraphEntry> graphs;
+  std::vector<tpm::GraphEntry> piece_graphs;  // the pieces of split steps
+  // tpm_step_state: its copy stream and the events between it and the step
+  cudaStream_t io = nullptr;
+  cudaEvent_t io_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 
   // ---- diagnostics (allocated on first use; tpm_diag.cu) ----
   double *diag_u = nullptr;      // 3n: face velocity RU/I_C2F(Rho) of the base state
@@ -392,6 +399,16 @@ void step_param_update(tpm_ctx *c);  // PARAM.update (params.cpp:80-86)
 void step_body(tpm_ctx *c);          // four substeps and the end of step
 void step_substep(tpm_ctx *c, int s); // one RK4 stage
 void step_end(tpm_ctx *c);           // make_mean_U0 and TimeAdvance
+// the pieces of a step whose host transfers overlap it: stage s's head
+// (through the push; joins the auxiliary stream at its end) and tail, and the
+// end of the step without the particle reorder (particle_reorder follows)
+void step_stage_head(tpm_ctx *c, int s);
+void step_stage_tail(tpm_ctx *c, int s);
+void step_end_no_reorder(tpm_ctx *c);
+// run `body` (one piece of a step, id `piece`) from a graph captured once per
+// host state, or eagerly when graphs are off or profiling is on; `advances`:
+// the piece ends the step (T_cur and num_timestep move on)
+void run_piece(tpm_ctx *c, int piece, bool advances, const std::function<void()> &body);
 void step_any(tpm_ctx *c);           // one step, replayed from a graph in graph mode
 void resume_device(tpm_ctx *c);      // tpm_resume without the status wrapper
 void graphs_clear(std::vector<GraphEntry> &cache);

@@ -48,6 +48,9 @@ SIGNATURES = {
     "tpm_resume": (_i, [_vp]),
     "tpm_load_state": (_i, [_vp, _dp, _dp, _dp, _dp, ctypes.POINTER(_dp), _dp, _d, _d, _i64]),
     "tpm_save_state": (_i, [_vp, _dp, _dp, _dp, _dp, ctypes.POINTER(_dp), _dp, _vp]),
+    "tpm_step_state": (_i, [_vp, _dp, _dp, _dp, _dp, ctypes.POINTER(_dp), _dp, ctypes.c_double,
+                            ctypes.c_double, ctypes.c_int64, _dp, _dp, _dp, _dp,
+                            ctypes.POINTER(_dp), _dp, _vp]),
     "tpm_statistics": (_i, [_vp, _vp]),
     "tpm_spectrum_shells": (_i, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
     "tpm_spectrum": (_i, [_vp, ctypes.POINTER(ctypes.c_double), _i]),
@@ -319,6 +322,35 @@ class Context:
         self._check(self.L.tpm_load_state(self.h, *[_dptr(a) for a in arrs], ptrs, _dptr(rhs_t),
                                           float(sc["P0"]), float(sc["T_cur"]),
                                           int(sc["num_timestep"])))
+
+    def step_state(self, st, out=None):
+        """One step of a host-resident state (tpm_step_state: load, step and
+        save in one call, the transfers overlapping the step); `out` (e.g. `st`
+        itself) receives the new state, in place when given."""
+        out = out if out is not None else {
+            **{f: np.empty(self._shape(f)) for f in self.STATE_FIELDS},
+            "part": {q: np.empty(self.npart) for q in inputs.PQ} if self.npart else None,
+            "RHS_T": np.empty(max(self.npart, 1)) if self.npart else None}
+        for f in self.STATE_FIELDS:
+            for d in (st, out):
+                a = d[f]
+                if not (a.flags["C_CONTIGUOUS"] and a.dtype == np.float64):
+                    raise ValueError(f"{f}: contiguous float64 arrays only")
+        if self.npart:
+            pin = (_dp * 7)(*[_dptr(st["part"][q]) for q in inputs.PQ])
+            pout = (_dp * 7)(*[_dptr(out["part"][q]) for q in inputs.PQ])
+            rin, rout = _dptr(st["RHS_T"]), _dptr(out["RHS_T"])
+        else:
+            pin = pout = None
+            rin = rout = _dptr(np.zeros(1))
+        sc_in = st["scalars"]
+        sc = TpmScalars()
+        self._check(self.L.tpm_step_state(
+            self.h, *[_dptr(st[f]) for f in self.STATE_FIELDS], pin, rin, float(sc_in["P0"]),
+            float(sc_in["T_cur"]), int(sc_in["num_timestep"]),
+            *[_dptr(out[f]) for f in self.STATE_FIELDS], pout, rout, ctypes.byref(sc)))
+        out["scalars"] = sc.as_dict()
+        return out
 
     def set_tau(self, tau):
         if tau is None:
