@@ -7,7 +7,11 @@ heated, two-way-coupled workload (the headline configuration).
 One JSON line on stdout (rank 0).  `value` is whole-job Mcell-steps/s with the
 state resident in HBM; `e2e` is the same metric through the C ABI with the
 step-boundary state round-tripped every step between pinned host buffers and
-the device (tpm_upload_* / tpm_resume / tpm_step / tpm_download_*).  With
+the device in one tpm_step_state call (its transfers overlapping the step;
+`three_calls` times tpm_load_state / tpm_step / tpm_save_state instead).  At
+one GPU the default run adds `ensemble48` and `adjoint64`: summaries of the
+48-box batched ensemble and of the 200-step discrete adjoint (each also runs
+alone with --workload; --no-extras skips them).  With
 --gpus N > 1 every rank runs an independent replica box (the path does not
 shard), and `value` sums the cells of all ranks over the slowest rank's time.
 `--impl reference` times the reference's CPU implementation of the path on
@@ -237,14 +241,15 @@ def time_gpu(p, s, steps, warmup, dist, device, tiles=None):
     return ctx, ms, n_it, launches, prof, clk.summary()
 
 
-def time_e2e(ctx, steps, warmup=1):
+def time_e2e(ctx, steps, warmup=3):
     """Same metric through the C ABI with host buffers: every step takes the
     step-boundary state from pinned host memory and returns it there.  Timed
     through tpm_step_state (load, step and save in one call, the transfers
     overlapping the step: the headline), and through the three calls
     tpm_load_state, tpm_step and tpm_save_state (their host-clock split
-    reported beside it).  `warmup` untimed rounds of each first (the first step
-    after a resume may capture its CUDA graphs)."""
+    reported beside it).  `warmup` untimed rounds of each first: the device
+    buffers alternate between two layouts from step to step, and the first
+    step in each captures its CUDA graphs."""
     import numpy as np
     import torch
 
@@ -645,7 +650,7 @@ def gpu_main(args):
         accuracy = mixed_accuracy_fresh(p64, s, (1, 10))
         accuracy["after_timed_run"] = after
     hctx = ctxs[head]
-    e2e_ms, h2d, d2h, e2e_split = time_e2e(hctx, max(1, min(args.steps, 5)))
+    e2e_ms, h2d, d2h, e2e_split = time_e2e(hctx, 2 * max(1, min(args.steps // 2, 3)))
     e2e_ms = max_over_ranks(e2e_ms, dist, "cuda")
     e2e_value = whole_job_rate(world, p64.ncell, 1, e2e_ms)
     r = res[head]
@@ -700,11 +705,24 @@ def gpu_main(args):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_port(args.workload)
     hctx.close()
+    if world == 1 and args.workload == WORKLOAD and args.grid is None and args.particles is None \
+            and not args.no_extras:
+        # the batched-ensemble and adjoint workloads at their default sizes,
+        # summarised in the same line (each also runs alone with --workload)
+        line["ensemble48"] = summary(ensemble_main(argparse.Namespace(steps=10, warmup=3)))
+        line["adjoint64"] = summary(adjoint_main(argparse.Namespace(steps=10, warmup=3)))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def summary(line):
+    keep = ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "dtype", "config",
+            "vs_sequential", "sequential_value", "adjoint_over_forward", "forward_ms_per_step",
+            "e2e", "gpu_launches", "clocks")
+    return {k: line[k] for k in keep if k in line}
 
 
 # ------------------------------------------------------ batched ensemble
@@ -786,8 +804,7 @@ def ensemble_main(args):
         "gpu_launches": int(g["launches"]),
         "clocks": g["clocks"],
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line
 
 
 ADJOINT = "adjoint64"
@@ -824,10 +841,12 @@ def adjoint_main(args):
     fwd = time.perf_counter() - t0
     c = fresh()
     torch.cuda.synchronize()
+    l0 = c.launch_count()
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         J, g, gA, gt = c.adjoint(horizon, checkpoint_every=20, w_tke=1.0, w_cvar=1.0)
         adj = time.perf_counter() - t0
+    launches = c.launch_count() - l0
     value = world * p.ncell * horizon / adj / 1e6
     line = {
         "metric": "adjoint Mcell-steps/s (forward + checkpointed recomputation + backward), "
@@ -845,10 +864,10 @@ def adjoint_main(args):
                                "dJ_dtau": gt},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": int(g.nbytes / horizon)},
+        "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    return line
 
 
 LONGRUN = "longrun256"
@@ -957,6 +976,8 @@ def main():
     ap.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the ensemble and adjoint summaries of the default run")
     ap.add_argument("--fft-tiles", type=lambda v: [int(t) for t in v.split(",")], default=None,
                     help="pencils x,y,z and threads x,y,z of the FFT passes instead of "
                          "autotuning them (one precision at a time)")
@@ -970,10 +991,10 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         reference_main(args)
-    elif args.workload == ENSEMBLE:
-        ensemble_main(args)
-    elif args.workload == ADJOINT:
-        adjoint_main(args)
+    elif args.workload in (ENSEMBLE, ADJOINT):
+        line = (ensemble_main if args.workload == ENSEMBLE else adjoint_main)(args)
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps(line), flush=True)
     elif args.workload == LONGRUN:
         longrun_main(args)
     else:
