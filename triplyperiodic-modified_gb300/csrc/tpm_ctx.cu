@@ -326,7 +326,8 @@ void stage_head(tpm_ctx *c, int s, bool join_aux) {
   if (par && join_aux) aux_join(c, c->join_ev[1]);
 }
 
-void stage_tail(tpm_ctx *c, int s) {
+// the tail through the Poisson solve (P final) ...
+void stage_tail_solve(tpm_ctx *c, int s) {
   const bool nb = c->np1_is_base;
   const bool par = !c->prof_on;
   auto beside = [&](int fork, auto &&launch) { beside_aux(c, fork, launch); };
@@ -340,11 +341,42 @@ void stage_tail(tpm_ctx *c, int s) {
   if (par) aux_join(c, c->join_ev[1]);
   tpm::launch_poisson_rhs(c, s, store_divergence(c, s));
   poisson_loop(c, c->Iteration, c->p.epsilon);
+}
+
+// ... and the projection (RU_int final after it)
+void stage_tail_project(tpm_ctx *c, int s) {
   tpm::launch_project(c, s);
   if (c->p.precision == TPM_PREC_MIXED && (s == 3 || c->div_every_stage))
     tpm::launch_div_residual(c, s);
   swap_stage(c);
   c->np1_is_base = false;
+}
+
+void stage_tail(tpm_ctx *c, int s) {
+  stage_tail_solve(c, s);
+  stage_tail_project(c, s);
+}
+
+// The tail as its particle deposits, which read neither the step's RU nor P
+// (a step whose transfers overlap it runs them while those land) ...
+void stage_tail_deposits(tpm_ctx *c, int s) {
+  const bool par = !c->prof_on;
+  auto beside = [&](int fork, auto &&launch) { beside_aux(c, fork, launch); };
+  beside(2, [&] { tpm::particle_deposit_momentum(c); });
+  tpm::particle_deposit_concentration(c);
+  tpm::particle_heat(c);
+  if (par) aux_join(c, c->join_ev[1]);
+}
+
+// ... and the rest of it (the same kernels as stage_tail, the momentum RHS on
+// the step's stream)
+void stage_tail_rest(tpm_ctx *c, int s) {
+  const bool nb = c->np1_is_base;
+  tpm::launch_rhs_momentum(c, s, nb);
+  if (c->PS) tpm::launch_passive_scalar(c, s, nb);  // simulation.cpp:65
+  tpm::launch_poisson_rhs(c, s, store_divergence(c, s));
+  poisson_loop(c, c->Iteration, c->p.epsilon);
+  stage_tail_project(c, s);
 }
 
 void substep(tpm_ctx *c, int s) {
@@ -385,6 +417,10 @@ void step_substep(tpm_ctx *c, int s) { substep(c, s); }
 void step_end(tpm_ctx *c) { end_step(c); }
 void step_stage_head(tpm_ctx *c, int s) { stage_head(c, s, true); }
 void step_stage_tail(tpm_ctx *c, int s) { stage_tail(c, s); }
+void step_stage_tail_solve(tpm_ctx *c, int s) { stage_tail_solve(c, s); }
+void step_stage_tail_deposits(tpm_ctx *c, int s) { stage_tail_deposits(c, s); }
+void step_stage_tail_rest(tpm_ctx *c, int s) { stage_tail_rest(c, s); }
+void step_stage_tail_project(tpm_ctx *c, int s) { stage_tail_project(c, s); }
 void step_end_no_reorder(tpm_ctx *c) { end_step(c, false); }
 
 void step_body(tpm_ctx *c) {
@@ -552,9 +588,10 @@ int tpm_create(const tpm_params *p, int64_t np, tpm_ctx **out) {
       c->reorder = true;
       c->pid = dalloc<int32_t>(c, np);
       c->pid2 = dalloc<int32_t>(c, np);
+      c->slot = dalloc<int32_t>(c, np);
       c->flag2 = dalloc<int32_t>(c, np);
       c->rhs_t2 = dalloc<double>(c, np);
-      c->pstage = dalloc<double>(c, np);
+      c->pstage = dalloc<double>(c, tpm::kStateArrays * (size_t)np);
       tpm::particles_reorder_init(c);
     }
     if (p->precision == TPM_PREC_MIXED) {
@@ -807,11 +844,9 @@ int tpm_load_state(tpm_ctx *c, const double *RU, const double *RU_int, const dou
     up(c->Rho, Rho, n);
     up(c->P, P, n);
     if (c->np > 0) {
-      for (int q = 0; q < 7; ++q) {
+      for (int q = 0; q < 7; ++q)
         if (!part[q]) return fail(c, TPM_ERR_ARG, "null particle array");
-        tpm::particles_from_host(c, c->pq[0][q], part[q], 8);
-      }
-      tpm::particles_from_host(c, c->rhs_t, rhs_t, 8);
+      tpm::particle_state_from_host(c, part, rhs_t);
     }
     pull_scalars(c);  // synchronises the copies above
     c->hsc->P0 = P0;
@@ -838,11 +873,11 @@ int tpm_save_state(tpm_ctx *c, double *RU, double *RU_int, double *Rho, double *
     down(Rho, c->Rho, n);
     down(P, c->P, n);
     if (c->np > 0) {
-      for (int q = 0; q < 7; ++q) {
+      for (int q = 0; q < 7; ++q)
         if (!part[q]) return fail(c, TPM_ERR_ARG, "null particle array");
-        tpm::particles_to_host(c, part[q], c->pq[0][q], 8);
-      }
-      tpm::particles_to_host(c, rhs_t, c->rhs_t, 8);
+      tpm::particle_state_index(c);
+      tpm::particle_state_stage_out(c, c->pq[0], c->rhs_t);
+      tpm::particle_state_copy_out(c, part, rhs_t, c->pq[0], c->rhs_t);
     }
     pull_scalars(c);  // synchronises the copies above
     if (sc) {
@@ -862,12 +897,16 @@ int tpm_save_state(tpm_ctx *c, double *RU, double *RU_int, double *Rho, double *
 }
 
 // tpm_load_state + tpm_step + tpm_save_state in one call, the transfers
-// overlapping the step: what the resume and the first stage's head read goes
-// up first on the step's stream; RU and P (first read in that stage's tail) go
-// up on a copy stream meanwhile; the particles, their heat rates and Rho,
-// final after the last stage's push, go down on the copy stream during that
-// stage's tail; RU, RU_int and P go down beside the particle reorder.  The
-// step runs as four captured pieces with the stream waits between them.
+// overlapping the step.  Up (one direction of the link, in this order): the
+// particle state, which the resume reads first, on the step's stream; then
+// Rho and RU_int (the first stage's head) and RU and P (its tail) on a copy
+// stream, the resume's particle work running meanwhile.  Down, on the copy
+// stream, each result once it is final: the particle state (permuted into the
+// caller's order on the step's stream) and Rho after the last stage's push,
+// then P after its Poisson solve, RU_int after its projection and RU after
+// the end of the step.  The step runs as seven captured pieces with the
+// stream waits between them; stage 0's particle deposits, which read neither
+// RU nor P, run while those two land.
 int tpm_step_state(tpm_ctx *c, const double *RU, const double *RU_int, const double *Rho,
                    const double *P, const double *const *part, const double *rhs_t, double P0,
                    double T_cur, int64_t num_timestep, double *RU_out, double *RU_int_out,
@@ -888,62 +927,65 @@ int tpm_step_state(tpm_ctx *c, const double *RU, const double *RU_int, const dou
     }
     const long long n = c->g.n;
     const auto up = cudaMemcpyHostToDevice, down = cudaMemcpyDeviceToHost;
-    // 1. up on the step's stream: what the resume and stage 0's head read
-    TPM_CUDA_TRY(cudaMemcpyAsync(c->Rho, Rho, sizeof(double) * n, up, c->stream));
-    TPM_CUDA_TRY(cudaMemcpyAsync(c->RU_int, RU_int, sizeof(double) * 3 * n, up, c->stream));
-    if (c->np > 0) {
-      for (int q = 0; q < 7; ++q) tpm::particles_from_host(c, c->pq[0][q], part[q], 8);
-      tpm::particles_from_host(c, c->rhs_t, rhs_t, 8);
-    }
-    TPM_CUDA_TRY(cudaEventRecord(c->io_ev[0], c->stream));
-    // 2. up on the copy stream after them: RU and P
-    TPM_CUDA_TRY(cudaStreamWaitEvent(c->io, c->io_ev[0], 0));
+    cudaEvent_t *ev = c->io_ev;
+    // the copy stream's next transfers wait for event e of the step's stream
+    auto io_after = [&](cudaEvent_t e) {
+      TPM_CUDA_TRY(cudaEventRecord(e, c->stream));
+      TPM_CUDA_TRY(cudaStreamWaitEvent(c->io, e, 0));
+    };
+    // 1. up: the particle state on the step's stream, then the fields on the
+    // copy stream (Rho and RU_int: ev[1]; RU and P: ev[2])
+    tpm::particle_state_copy_in(c, part, rhs_t);
+    io_after(ev[0]);
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->Rho, Rho, sizeof(double) * n, up, c->io));
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->RU_int, RU_int, sizeof(double) * 3 * n, up, c->io));
+    TPM_CUDA_TRY(cudaEventRecord(ev[1], c->io));
     TPM_CUDA_TRY(cudaMemcpyAsync(c->RU, RU, sizeof(double) * 3 * n, up, c->io));
     TPM_CUDA_TRY(cudaMemcpyAsync(c->P, P, sizeof(double) * n, up, c->io));
-    TPM_CUDA_TRY(cudaEventRecord(c->io_ev[1], c->io));
+    TPM_CUDA_TRY(cudaEventRecord(ev[2], c->io));
+    tpm::particle_state_stage_in(c);
     pull_scalars(c);  // synchronises the step's stream (the copy stream goes on)
     c->hsc->P0 = P0;
     push_scalars(c);
     c->T_cur = T_cur;
     c->num_timestep = num_timestep;
-    tpm::resume_device(c);  // reads neither RU nor P
-    // 3. the step: stage 0's head, then (RU and P landed) up to stage 3's push
+    tpm::resume_device(c, ev[1]);  // reads neither RU nor P
+    // 2. the step: stage 0's head, then (RU and P landed) up to stage 3's push
     tpm::step_param_update(c);
     tpm::run_piece(c, 1, false, [&] { tpm::step_stage_head(c, 0); });
-    TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->io_ev[1], 0));
-    tpm::run_piece(c, 2, false, [&] {
-      tpm::step_stage_tail(c, 0);
+    tpm::particle_state_index(c);  // (for step 3; the storage order holds until the reorder)
+    tpm::run_piece(c, 2, false, [&] { tpm::step_stage_tail_deposits(c, 0); });
+    TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, ev[2], 0));
+    tpm::run_piece(c, 6, false, [&] {
+      tpm::step_stage_tail_rest(c, 0);
       tpm::step_substep(c, 1);
       tpm::step_substep(c, 2);
       tpm::step_stage_head(c, 3);
     });
-    TPM_CUDA_TRY(cudaEventRecord(c->io_ev[2], c->stream));
-    // 4. down on the copy stream during stage 3's tail: the particles (the np1
-    // set stage 3's push wrote, the base set after the step), their heat
-    // rates, and Rho (Rho_np1 after stage 3's density update)
+    // 3. down: the particle state (the np1 set of stage 3's push, the base
+    // set after the step; in the caller's order) and Rho (Rho_np1 after
+    // stage 3's density update), during stage 3's tail
+    tpm::particle_state_stage_out(c, c->pq[3], c->rhs_t);
+    io_after(ev[3]);
     {
-      TPM_CUDA_TRY(cudaStreamWaitEvent(c->io, c->io_ev[2], 0));
       OnStream on(c, c->io);
-      if (c->np > 0) {
-        for (int q = 0; q < 7; ++q) tpm::particles_to_host(c, part_out[q], c->pq[3][q], 8);
-        tpm::particles_to_host(c, rhs_t_out, c->rhs_t, 8);
-      }
-      TPM_CUDA_TRY(cudaMemcpyAsync(Rho_out, c->Rho_np1, sizeof(double) * n, down, c->io));
-      TPM_CUDA_TRY(cudaEventRecord(c->io_ev[3], c->io));
+      tpm::particle_state_copy_out(c, part_out, rhs_t_out, c->pq[3], c->rhs_t);
     }
-    tpm::run_piece(c, 3, true, [&] {
-      tpm::step_stage_tail(c, 3);
-      tpm::step_end_no_reorder(c);
-    });
-    TPM_CUDA_TRY(cudaEventRecord(c->io_ev[4], c->stream));
-    // 5. the reorder permutes what those copies read: after them
-    TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->io_ev[3], 0));
-    tpm::particle_reorder(c);
-    // 6. down on the copy stream beside the reorder: RU, RU_int and P
-    TPM_CUDA_TRY(cudaStreamWaitEvent(c->io, c->io_ev[4], 0));
-    TPM_CUDA_TRY(cudaMemcpyAsync(RU_out, c->RU, sizeof(double) * 3 * n, down, c->io));
-    TPM_CUDA_TRY(cudaMemcpyAsync(RU_int_out, c->RU_int, sizeof(double) * 3 * n, down, c->io));
+    TPM_CUDA_TRY(cudaMemcpyAsync(Rho_out, c->Rho_np1, sizeof(double) * n, down, c->io));
+    // 4. stage 3's tail in three pieces, each of P, RU_int and RU going down
+    // once final
+    tpm::run_piece(c, 3, false, [&] { tpm::step_stage_tail_solve(c, 3); });
+    io_after(ev[4]);
     TPM_CUDA_TRY(cudaMemcpyAsync(P_out, c->P, sizeof(double) * n, down, c->io));
+    tpm::run_piece(c, 4, false, [&] { tpm::step_stage_tail_project(c, 3); });
+    io_after(ev[5]);
+    TPM_CUDA_TRY(cudaMemcpyAsync(RU_int_out, c->RU_int, sizeof(double) * 3 * n, down, c->io));
+    tpm::run_piece(c, 5, true, [&] { tpm::step_end_no_reorder(c); });
+    io_after(ev[6]);
+    TPM_CUDA_TRY(cudaMemcpyAsync(RU_out, c->RU, sizeof(double) * 3 * n, down, c->io));
+    // 5. the reorder (the staged copies no longer read the particle sets)
+    tpm::particle_reorder(c);
+    TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     TPM_CUDA_TRY(cudaStreamSynchronize(c->io));
     pull_scalars(c);
     if (sc) {
@@ -1011,12 +1053,11 @@ namespace tpm {
 
 // The step-boundary state (base copies, RU_int, P, Q, rhs_t, scalars) is on
 // the device; rebuild everything a step derives from it.
-void resume_device(tpm_ctx *c) {
+void resume_device(tpm_ctx *c, cudaEvent_t rho_ready) {
   {
     const long long n = c->g.n;
     // at a step boundary Rho_int == Rho, x_int == x (all particle copies
     // agree), P0_int == P0 and every np1 copy equals its base copy
-    TPM_CUDA_TRY(cudaMemcpyAsync(c->Rho_int, c->Rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
     for (int q = 0; q < 7 && c->np > 0; ++q)
       TPM_CUDA_TRY(cudaMemcpyAsync(c->pq[1][q], c->pq[0][q], sizeof(double) * c->np,
                                    cudaMemcpyDeviceToDevice, c->stream));
@@ -1030,13 +1071,15 @@ void resume_device(tpm_ctx *c) {
     c->stage_next = 0;
     c->ph_done = 0;
     c->p0_called = false;
+    c->counted_r = c->counted_t = false;  // (no push has counted the keys)
+    tpm::particle_resume(c);  // (the particles' heat rates and positions only)
+    tpm::particle_reorder(c);
+    if (rho_ready) TPM_CUDA_TRY(cudaStreamWaitEvent(c->stream, rho_ready, 0));
+    TPM_CUDA_TRY(cudaMemcpyAsync(c->Rho_int, c->Rho, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
     if (c->PS) {
       TPM_CUDA_TRY(cudaMemcpyAsync(c->PS_int, c->PS, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
       tpm::launch_passive_scalar_face(c, c->PS);
     }
-    c->counted_r = c->counted_t = false;  // (no push has counted the keys)
-    tpm::particle_resume(c);
-    tpm::particle_reorder(c);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     c->initialized = true;
     c->stepped = false;

@@ -258,9 +258,12 @@ struct tpm_ctx {
   // mixed path: particles kept in cell order (particle_reorder).  pid[s] is the
   // caller's index of the particle in storage slot s; host transfers of
   // per-particle data go through it.  pid2 / flag2 / rhs_t2 / tau2 take the
-  // permuted copies, pstage (np x 8 bytes) stages the caller-ordered arrays.
+  // permuted copies, pstage (kStateArrays slots of np doubles) stages the
+  // caller-ordered arrays (one array in its first slot, the particle state in
+  // all of them).
   bool reorder = false;
   int32_t *pid = nullptr, *pid2 = nullptr, *flag2 = nullptr;
+  int32_t *slot = nullptr;  // slot[i]: storage slot of caller particle i (particle_state_index)
   double *rhs_t2 = nullptr, *tau2 = nullptr, *pstage = nullptr;
   double *w8 = nullptr;  // 16*np corner weights (heat, concentration; sorted order)
   float *corner_sums = nullptr;  // mixed: 16*n per-source-cell corner sums (heat, conc.)
@@ -299,7 +302,7 @@ struct tpm_ctx {
   std::vector<tpm::GraphEntry> piece_graphs;  // the pieces of split steps
   // tpm_step_state: its copy stream and the events between it and the step
   cudaStream_t io = nullptr;
-  cudaEvent_t io_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  cudaEvent_t io_ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 
   // ---- diagnostics (allocated on first use; tpm_diag.cu) ----
   double *diag_u = nullptr;      // 3n: face velocity RU/I_C2F(Rho) of the base state
@@ -400,17 +403,26 @@ void step_body(tpm_ctx *c);          // four substeps and the end of step
 void step_substep(tpm_ctx *c, int s); // one RK4 stage
 void step_end(tpm_ctx *c);           // make_mean_U0 and TimeAdvance
 // the pieces of a step whose host transfers overlap it: stage s's head
-// (through the push; joins the auxiliary stream at its end) and tail, and the
-// end of the step without the particle reorder (particle_reorder follows)
+// (through the push; joins the auxiliary stream at its end) and tail, the
+// tail as two parts (through the Poisson solve, whose P is then final; the
+// projection, whose RU_int is then final) or as its particle deposits (which
+// read neither the step's RU nor P) and the rest, and the end of the step
+// without the particle reorder (particle_reorder follows)
 void step_stage_head(tpm_ctx *c, int s);
 void step_stage_tail(tpm_ctx *c, int s);
+void step_stage_tail_solve(tpm_ctx *c, int s);
+void step_stage_tail_project(tpm_ctx *c, int s);
+void step_stage_tail_deposits(tpm_ctx *c, int s);
+void step_stage_tail_rest(tpm_ctx *c, int s);
 void step_end_no_reorder(tpm_ctx *c);
 // run `body` (one piece of a step, id `piece`) from a graph captured once per
 // host state, or eagerly when graphs are off or profiling is on; `advances`:
 // the piece ends the step (T_cur and num_timestep move on)
 void run_piece(tpm_ctx *c, int piece, bool advances, const std::function<void()> &body);
 void step_any(tpm_ctx *c);           // one step, replayed from a graph in graph mode
-void resume_device(tpm_ctx *c);      // tpm_resume without the status wrapper
+// tpm_resume without the status wrapper; with rho_ready, the work that reads
+// Rho waits for that event (the particle work before it does not)
+void resume_device(tpm_ctx *c, cudaEvent_t rho_ready = nullptr);
 void graphs_clear(std::vector<GraphEntry> &cache);
 
 // ---- particles (tpm_particles.cu) ----
@@ -429,6 +441,23 @@ void particles_reorder_init(tpm_ctx *c);  // pid = identity (the caller order)
 // 8 or 4 bytes); plain copies unless c->reorder
 void particles_from_host(tpm_ctx *c, void *dev, const void *host, int elem);
 void particles_to_host(tpm_ctx *c, void *host, const void *dev, int elem);
+// The particle state (the base set's 7 quantities, then the heat rates) as
+// one transfer through kStateArrays staging slots of np doubles: copy_in
+// copies the caller's arrays into the slots back to back (directly into the
+// base set and rhs_t when the particles keep the caller's order) and
+// stage_in permutes the slots into storage with one kernel (from_host: both);
+// index forms slot (pid inverted) for the present storage order, after which
+// stage_out permutes storage (src, rhs_t) into the slots, and copy_out
+// copies the slots to the caller's arrays (directly from src and rhs_t_dev
+// when the particles keep the caller's order), each on the current stream.
+constexpr int kStateArrays = 8;
+void particle_state_copy_in(tpm_ctx *c, const double *const *part, const double *rhs_t);
+void particle_state_stage_in(tpm_ctx *c);
+void particle_state_from_host(tpm_ctx *c, const double *const *part, const double *rhs_t);
+void particle_state_index(tpm_ctx *c);
+void particle_state_stage_out(tpm_ctx *c, double *const *src, const double *rhs_t);
+void particle_state_copy_out(tpm_ctx *c, double *const *part, double *rhs_t,
+                             double *const *src, const double *rhs_t_dev);
 
 }  // namespace tpm
 

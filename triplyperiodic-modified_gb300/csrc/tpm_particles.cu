@@ -932,6 +932,13 @@ __global__ void k_to_caller(int64_t np, const int32_t *__restrict__ pid, const T
     out[pid[s]] = in[s];
 }
 
+// slot[i]: the storage slot of the caller's particle i (pid inverted)
+__global__ void k_slot_of(int64_t np, const int32_t *__restrict__ pid, int32_t *__restrict__ slot) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < np;
+       s += (int64_t)gridDim.x * blockDim.x)
+    slot[pid[s]] = (int32_t)s;
+}
+
 PState pstate(tpm_ctx *c, bool np1_in_base) {
   PState s;
   for (int q = 0; q < 7; ++q) {
@@ -1167,6 +1174,55 @@ void particles_from_host(tpm_ctx *c, void *dev, const void *host, int elem) {
   else
     TPM_LAUNCH(c, "from_caller", k_from_caller<int32_t>, pblocks(c->np), kThreads, 0, c->np, c->pid,
                reinterpret_cast<const int32_t *>(c->pstage), static_cast<int32_t *>(dev));
+}
+
+void particle_state_copy_in(tpm_ctx *c, const double *const *part, const double *rhs_t) {
+  if (c->np == 0) return;
+  const size_t bytes = sizeof(double) * c->np;
+  for (int k = 0; k < kStateArrays; ++k) {
+    const double *h = k < 7 ? part[k] : rhs_t;
+    double *d = c->reorder ? c->pstage + (size_t)k * c->np : (k < 7 ? c->pq[0][k] : c->rhs_t);
+    TPM_CUDA_TRY(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, c->stream));
+  }
+}
+
+// The permutations between the staging slots and storage are gathers, one
+// array per pass: the 64 MB source of an 8M-particle array stays in L2 while
+// its random reads land, where one pass over all eight arrays (or scattered
+// 8-byte stores, each rewriting a partial sector) goes to DRAM for each.
+void particle_state_stage_in(tpm_ctx *c) {
+  if (c->np == 0 || !c->reorder) return;
+  for (int k = 0; k < kStateArrays; ++k)
+    TPM_LAUNCH(c, "state_from_caller", k_from_caller<double>, pblocks(c->np), kThreads, 0, c->np,
+               c->pid, c->pstage + (size_t)k * c->np, k < 7 ? c->pq[0][k] : c->rhs_t);
+}
+
+void particle_state_from_host(tpm_ctx *c, const double *const *part, const double *rhs_t) {
+  particle_state_copy_in(c, part, rhs_t);
+  particle_state_stage_in(c);
+}
+
+void particle_state_index(tpm_ctx *c) {
+  if (c->np == 0 || !c->reorder) return;
+  TPM_LAUNCH(c, "slot_of", k_slot_of, pblocks(c->np), kThreads, 0, c->np, c->pid, c->slot);
+}
+
+void particle_state_stage_out(tpm_ctx *c, double *const *src, const double *rhs_t) {
+  if (c->np == 0 || !c->reorder) return;
+  for (int k = 0; k < kStateArrays; ++k)  // (slot[i] = s with pid[s] = i: a gather too)
+    TPM_LAUNCH(c, "state_to_caller", k_from_caller<double>, pblocks(c->np), kThreads, 0, c->np,
+               c->slot, k < 7 ? src[k] : rhs_t, c->pstage + (size_t)k * c->np);
+}
+
+void particle_state_copy_out(tpm_ctx *c, double *const *part, double *rhs_t,
+                             double *const *src, const double *rhs_t_dev) {
+  if (c->np == 0) return;
+  const size_t bytes = sizeof(double) * c->np;
+  for (int k = 0; k < kStateArrays; ++k) {
+    double *h = k < 7 ? part[k] : rhs_t;
+    const double *d = c->reorder ? c->pstage + (size_t)k * c->np : (k < 7 ? src[k] : rhs_t_dev);
+    TPM_CUDA_TRY(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, c->stream));
+  }
 }
 
 void particles_to_host(tpm_ctx *c, void *host, const void *dev, int elem) {
