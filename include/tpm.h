@@ -127,7 +127,11 @@ typedef struct tpm_scalars {
   int32_t total_poisson_iterations;  /* sum over all solves since create */
   double last_poisson_error;         /* max|dp| of the last iteration */
   double max_abs_div;                /* FP64 post-projection max|div u - divergence|
-                                        of the last stage (mixed path only; else -1) */
+                                        of the last stage (mixed path only; else -1).
+                                        At a step boundary it is evaluated on the first
+                                        read after the step (not inside the step); after
+                                        a field upload or an operator-level solve it
+                                        keeps the last evaluated value */
 } tpm_scalars;
 
 typedef struct tpm_ctx tpm_ctx;

@@ -172,16 +172,17 @@ def test_batch_matches_boxes_run_alone(capi, prec):
             assert_same(state(box), want)
         b.close()
 
-@pytest.mark.parametrize("prec,graph", [(P.PREC_FP64, False), (P.PREC_MIXED, False),
-                                        (P.PREC_MIXED, True)])
-def test_step_state_equals_load_step_save(capi, prec, graph):
+@pytest.mark.parametrize("prec,graph,npart", [(P.PREC_FP64, False, 6000),
+                                              (P.PREC_MIXED, False, 6000),
+                                              (P.PREC_MIXED, True, 6000), (P.PREC_MIXED, True, 0)])
+def test_step_state_equals_load_step_save(capi, prec, graph, npart):
     """tpm_step_state (one call: load the host state, step, save it, the
     transfers overlapping the step) gives the bits of tpm_load_state +
-    tpm_step + tpm_save_state, step after step, also in place; the context
-    then steps on as usual."""
+    tpm_step + tpm_save_state, step after step, also in place and without
+    particles; the context then steps on as usual."""
     import copy
 
-    p, s = case(prec=prec, dims=(32, 32, 32), npart=6000, seed=21, heat=0.4)
+    p, s = case(prec=prec, dims=(32, 32, 32), npart=npart, seed=21, heat=0.4)
     a = run(capi, p, s, 1)
     st0 = a.download_state()
     ref = copy.deepcopy(st0)
@@ -198,9 +199,12 @@ def test_step_state_equals_load_step_save(capi, prec, graph):
         cur = c.step_state(cur, out=cur if k else None)
     for f in capi.Context.STATE_FIELDS:
         assert np.array_equal(cur[f], ref[f]), f
-    for q in cur["part"]:
-        assert np.array_equal(cur["part"][q], ref["part"][q]), q
-    assert np.array_equal(cur["RHS_T"], ref["RHS_T"])
+    if npart:
+        for q in cur["part"]:
+            assert np.array_equal(cur["part"][q], ref["part"][q]), q
+        assert np.array_equal(cur["RHS_T"], ref["RHS_T"])
+    else:
+        assert cur["part"] is None and ref["part"] is None
     for k in ("P0", "T_cur", "num_timestep"):
         assert cur["scalars"][k] == ref["scalars"][k], k
     b.step()

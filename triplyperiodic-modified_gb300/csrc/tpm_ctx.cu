@@ -46,6 +46,22 @@ void pull_scalars(tpm_ctx *c) {
   TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
 }
 
+// The mixed path's post-projection residual of the last step, evaluated when
+// the scalars are first read after that step (a diagnostic: the reference's
+// step has none, so the step itself does not pay for it).  Its inputs - the
+// projected RU (RU_int after the stage swap), the last stage's C/d^2 pairs,
+// its divergence constraint and RHS mean - stay in place at the step
+// boundary until the next step's Poisson right-hand side.  Not after a resume
+// (no step yet) or after a call that overwrote them; queued before the read.
+void div_residual_on_read(tpm_ctx *c) {
+  if (c->p.precision != TPM_PREC_MIXED || c->div_every_stage || !c->stepped ||
+      !c->np1_is_base || c->stage_next != 0 || c->ph_done || c->div_dirty ||
+      c->div_eval_step == c->num_timestep)
+    return;
+  tpm::launch_div_residual(c, 3, c->RU_int);
+  c->div_eval_step = c->num_timestep;
+}
+
 // device field pointer and its length in doubles
 double *field_ptr(tpm_ctx *c, int f, long long *len, bool for_download) {
   const long long n = c->g.n;
@@ -90,6 +106,7 @@ void materialize_np1(tpm_ctx *c) {
 
 // PARAM.update (params.cpp:80-86)
 void param_update(tpm_ctx *c) {
+  c->div_dirty = false;  // (a step starts: its last stage forms fresh residual inputs)
   if (c->T_cur > c->p.threshold) {
     c->Iteration = c->p.Iteration2;
     c->A = c->p.A2;
@@ -346,8 +363,9 @@ void stage_tail_solve(tpm_ctx *c, int s) {
 // ... and the projection (RU_int final after it)
 void stage_tail_project(tpm_ctx *c, int s) {
   tpm::launch_project(c, s);
-  if (c->p.precision == TPM_PREC_MIXED && (s == 3 || c->div_every_stage))
-    tpm::launch_div_residual(c, s);
+  // (the last stage's residual is evaluated when the scalars are read)
+  if (c->p.precision == TPM_PREC_MIXED && c->div_every_stage)
+    tpm::launch_div_residual(c, s, c->RU_new);
   swap_stage(c);
   c->np1_is_base = false;
 }
@@ -697,6 +715,7 @@ int tpm_upload_field(tpm_ctx *c, int field, const double *host) {
     double *d = field_ptr(c, field, &len, false);
     if (!d) return fail(c, TPM_ERR_ARG, "unknown field id");
     if (field == TPM_FIELD_RU_INT || field == TPM_FIELD_RU) c->rui32_stale = true;
+    c->div_dirty = true;
     TPM_CUDA_TRY(cudaMemcpyAsync(d, host, sizeof(double) * len, cudaMemcpyHostToDevice, c->stream));
     if (field == TPM_FIELD_P)  // the next refinement solve starts cold
       TPM_CUDA_TRY(cudaMemsetAsync(&c->dsc->warm, 0, sizeof(int), c->stream));
@@ -804,6 +823,7 @@ int tpm_set_scalars(tpm_ctx *c, double P0, double T_cur, int64_t num_timestep) {
 int tpm_get_scalars(tpm_ctx *c, tpm_scalars *out) {
   return guarded(c, [&]() -> int {
     if (!out) return fail(c, TPM_ERR_ARG, "null output");
+    div_residual_on_read(c);
     pull_scalars(c);
     out->P0 = c->hsc->P0;
     out->P0_int = c->hsc->P0_int;
@@ -879,6 +899,7 @@ int tpm_save_state(tpm_ctx *c, double *RU, double *RU_int, double *Rho, double *
       tpm::particle_state_stage_out(c, c->pq[0], c->rhs_t);
       tpm::particle_state_copy_out(c, part, rhs_t, c->pq[0], c->rhs_t);
     }
+    div_residual_on_read(c);
     pull_scalars(c);  // synchronises the copies above
     if (sc) {
       sc->P0 = c->hsc->P0;
@@ -983,8 +1004,10 @@ int tpm_step_state(tpm_ctx *c, const double *RU, const double *RU_int, const dou
     tpm::run_piece(c, 5, true, [&] { tpm::step_end_no_reorder(c); });
     io_after(ev[6]);
     TPM_CUDA_TRY(cudaMemcpyAsync(RU_out, c->RU, sizeof(double) * 3 * n, down, c->io));
-    // 5. the reorder (the staged copies no longer read the particle sets)
+    // 5. the reorder (the staged copies no longer read the particle sets) and
+    // the step's divergence residual for the scalars
     tpm::particle_reorder(c);
+    div_residual_on_read(c);
     TPM_CUDA_TRY(cudaStreamSynchronize(c->stream));
     TPM_CUDA_TRY(cudaStreamSynchronize(c->io));
     pull_scalars(c);
@@ -1095,6 +1118,7 @@ int tpm_substep(tpm_ctx *c, int rk_stage) {
     if (!c->initialized) return fail(c, TPM_ERR_STATE, "tpm_initialize must come first");
     if (rk_stage < 0 || rk_stage > 3) return fail(c, TPM_ERR_ARG, "rk_stage must be 0..3");
     if (c->ph_done) return fail(c, TPM_ERR_STATE, "a stage is in progress through the phase calls");
+    if (rk_stage == 0) c->div_dirty = false;
     substep(c, rk_stage);
     return TPM_OK;
   });
@@ -1226,8 +1250,8 @@ int tpm_update_ru_wp(tpm_ctx *c, int k) {
   return guarded(c, [&]() -> int {
     if (int rc = phase_check(c, k, PH_RUWP, PH_SOLVE, "Update_RU_WP")) return rc;
     tpm::launch_project(c, k);
-    if (c->p.precision == TPM_PREC_MIXED && (k == 3 || c->div_every_stage))
-      tpm::launch_div_residual(c, k);
+    if (c->p.precision == TPM_PREC_MIXED && c->div_every_stage)
+      tpm::launch_div_residual(c, k, c->RU_new);
     c->ph_done |= PH_RUWP;
     return TPM_OK;
   });
@@ -1303,6 +1327,7 @@ int tpm_poisson_solve(tpm_ctx *c, const double *C3, double *P, const double *RHS
     c->hsc->warm = 0;      // and starts from the caller's P
     push_scalars(c);
     tpm::launch_center_coeff_from_C(c);
+    c->div_dirty = true;  // (C/d^2 and the RHS mean now belong to this solve)
     poisson_loop(c, max_iterations, epsilon);
     TPM_CUDA_TRY(cudaMemcpyAsync(P, c->P, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
     pull_scalars(c);

@@ -1719,9 +1719,9 @@ void launch_passive_scalar_face(tpm_ctx *c, const double *src) {
              c->PS_face);
 }
 
-void launch_div_residual(tpm_ctx *c, int s) {
+void launch_div_residual(tpm_ctx *c, int s, const double *RUn) {
   const int nb = cell_waves(c, k_div_residual, true);
-  TPM_LAUNCH(c, "div_residual", k_div_residual, nb, kThreads, 0, c->g, c->RU_new, c->Cs2,
+  TPM_LAUNCH(c, "div_residual", k_div_residual, nb, kThreads, 0, c->g, RUn, c->Cs2,
              c->divg, c->dsc, c->p.dt * kPre[s], c->partials + kPartDiv * kRedBlocks);
   TPM_LAUNCH(c, "finish_max_div", k_finish_max_div, 1, kThreads, 0,
              c->partials + kPartDiv * kRedBlocks, nb, c->dsc);

@@ -277,6 +277,13 @@ struct tpm_ctx {
 
   bool store_div = false;
   bool div_every_stage = false;
+  // The mixed path's post-projection residual of a step is evaluated when the
+  // scalars are first read after it (div_residual_on_read), from inputs that
+  // stay in place until the next step's Poisson right-hand side: the step
+  // count it was last evaluated at, and whether a call since the step has
+  // overwritten its inputs (a field upload, an operator-level solve).
+  int64_t div_eval_step = -1;
+  bool div_dirty = false;
   // mixed path: the face coefficients and the Poisson right-hand side in one
   // TMA-fed z-marching pass (grids of whole 32 x 8 tiles, Solver 0), with the
   // tensor maps of the arrays it reads
@@ -345,7 +352,7 @@ void particle_kernels_setup(tpm_ctx *c);  // tpm_particles.cu
 void launch_face_coeff(tpm_ctx *c);  // mixed path: C and C/d^2 pairs from Rho_new
 void launch_poisson_rhs(tpm_ctx *c, int stage, bool store_div);
 void launch_project(tpm_ctx *c, int stage);
-void launch_div_residual(tpm_ctx *c, int stage);
+void launch_div_residual(tpm_ctx *c, int stage, const double *RUn);
 void launch_mean_reset(tpm_ctx *c);
 void launch_passive_scalar(tpm_ctx *c, int stage, bool np1_in_base);  // grid.cpp:743-772
 void launch_passive_scalar_face(tpm_ctx *c, const double *src);      // PS_face = I_C2F(src)
