@@ -320,12 +320,18 @@ enum {
                             Poisson stopping test then runs on the device.
                             Results are bit-identical to eager stepping.  Not used
                             while profiling is on. */,
-  TPM_OPT_FFT_TMA = 4 /* mixed path: the y and z pencil passes take tiles of 8
+  TPM_OPT_FFT_TMA = 4, /* mixed path: the y and z pencil passes take tiles of 8
                          pencils moved by the TMA (1; the default where every
                          pencil has at most 256 points) or plain tiles (0).
                          tpm_autotune may turn either pass's TMA tiles off on a
                          grid where plain tiles are faster.  Results do not
                          depend on it.  (Not in the reference.) */
+  TPM_OPT_FUSED_DEPOSITS = 5 /* mixed path on grids of whole 32 x 8 column tiles:
+                                the heat/concentration and the momentum deposits
+                                each in one z-marching pass with the source
+                                cells' sums in shared memory (1, the default) or
+                                in two passes through HBM (0).  The same bits.
+                                (Not in the reference.) */
 };
 int tpm_set_option(tpm_ctx *ctx, int option, int value);
 

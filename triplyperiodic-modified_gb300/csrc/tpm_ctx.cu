@@ -701,6 +701,12 @@ int tpm_set_option(tpm_ctx *c, int option, int value) {
       c->graph_mode = value != 0;
       return TPM_OK;
     }
+    if (option == TPM_OPT_FUSED_DEPOSITS) {
+      c->dep_fused = value != 0;
+      tpm::graphs_clear(c->graphs);  // other kernels
+      tpm::graphs_clear(c->piece_graphs);
+      return TPM_OK;
+    }
     return fail(c, TPM_ERR_ARG, "unknown option");
   });
 }

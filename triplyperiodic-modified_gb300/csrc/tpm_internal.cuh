@@ -284,6 +284,7 @@ struct tpm_ctx {
   // overwritten its inputs (a field upload, an operator-level solve).
   int64_t div_eval_step = -1;
   bool div_dirty = false;
+  bool dep_fused = true;  // TPM_OPT_FUSED_DEPOSITS
   // mixed path: the face coefficients and the Poisson right-hand side in one
   // TMA-fed z-marching pass (grids of whole 32 x 8 tiles, Solver 0), with the
   // tensor maps of the arrays it reads

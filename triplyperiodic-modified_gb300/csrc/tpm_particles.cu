@@ -842,6 +842,229 @@ __global__ void k_dep_mom_faces(Grid g, const float *__restrict__ sums, float *_
   }
 }
 
+// The two mixed deposits in one z-marching pass each over whole 32 x 8 cell
+// tiles (the sums of a plane of source cells kept in shared memory instead of
+// written to and read back from HBM: 64 B + 64 B per cell for the heat and
+// concentration corners, 24 B + 24 B for the momentum), with the arithmetic
+// of the two-pass kernels above in the same order, so the same bits.  A block
+// takes work items (tile, chunk of kDepZ planes) blockIdx.x, + gridDim.x, ...;
+// the grid is at most one resident wave and kRedBlocks blocks (the heat
+// deposit's per-block sums of Q feed the P0 update).  Every source cell of a
+// plane (the tile and its halo) has its own thread, which walks its column of
+// source cells down the chunk with the loads of the next plane's cell range
+// and first particle in flight while the current plane is summed (the chain
+// starts -> perm -> payload would otherwise be paid in full at every plane).
+constexpr int kDX = 32, kDY = 8, kDepZ = 16, kDepThreads = 320;
+
+// A thread's column of source cells: the index range [s0, e0) of plane m's
+// cell and its first particle p0, with plane m + 1's range and first particle
+// and plane m + 2's range in flight.
+struct SrcColumn {
+  int32_t s0 = 0, e0 = 0, p0 = 0, s1 = 0, e1 = 0, p1 = 0, s2 = 0, e2 = 0;
+  __device__ __forceinline__ void range(const int32_t *__restrict__ starts, long long r,
+                                        int32_t &a, int32_t &b) {
+    a = starts[r];
+    b = starts[r + 1];
+  }
+};
+
+// the 8 + 8 corner sums of a source cell (particles [s0, e0), the first p0)
+// in slot order (k_dep_corners)
+__device__ __forceinline__ void corner_sums(const int32_t *__restrict__ perm,
+                                            const float *__restrict__ pay, int64_t np, int32_t s0,
+                                            int32_t e0, int32_t p0, float sq[8], float sc[8]) {
+#pragma unroll
+  for (int o = 0; o < 8; ++o) sq[o] = sc[o] = 0.f;
+  for (int32_t s = s0; s < e0; ++s) {
+    const int32_t p = s == s0 ? p0 : perm[s];
+    const float xl = pay[p], yl = pay[np + p], zl = pay[2 * np + p];
+    const float rt = pay[3 * np + p];
+    const float fx[2] = {xl, 1 - xl}, fy[2] = {yl, 1 - yl}, fz[2] = {zl, 1 - zl};
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+      for (int dx = 0; dx < 2; ++dx) {
+        const float fxy = fx[dx] * fy[dy];
+#pragma unroll
+        for (int dz = 0; dz < 2; ++dz) {
+          const int o = (dz * 2 + dy) * 2 + dx;
+          const float v = fxy * fz[dz];
+          sc[o] += v;
+          sq[o] += v * rt;
+        }
+      }
+  }
+}
+
+// Heat rate and concentration (k_dep_corners + k_dep_gather8): target cell
+// (i, j, k) adds the corners o = dz*4 + dy*2 + dx of source cells (i + dx,
+// j + dy, k + dz), o = 0..3 when source plane k is formed and 4..7 when plane
+// k + 1 is.  Threads 0-255 own the tile's cells (sources and targets),
+// threads 256-296 the sources of its upper x column and y row.
+__global__ void __launch_bounds__(kDepThreads)
+k_dep_heat_zm(Grid g, const int32_t *__restrict__ starts, const int32_t *__restrict__ perm,
+              const float *__restrict__ pay, int64_t np, double *__restrict__ Q,
+              double *__restrict__ C, double *__restrict__ partials) {
+  __shared__ float S[16][kDY + 1][kDX + 1];
+  __shared__ double sh[32];
+  const int tid = threadIdx.x, tx = tid % kDX, ty = tid / kDX;
+  const bool tgt = tid < kDX * kDY, src = tid < kDX * kDY + kDY + kDX + 1;
+  // this thread's source cell in the tile's (kDX + 1) x (kDY + 1) plane
+  const int h = tid - kDX * kDY;
+  const int sx = tgt ? tx : (h < kDY ? kDX : h - kDY), sy = tgt ? ty : (h < kDY ? h : kDY);
+  const int tilesx = g.nx / kDX, tilesy = g.ny / kDY, chunks = (g.nz + kDepZ - 1) / kDepZ;
+  const int items = tilesx * tilesy * chunks;
+  double bsum = 0;
+  for (int w = blockIdx.x; w < items; w += gridDim.x) {
+    const int bx = w % tilesx, by = (w / tilesx) % tilesy, bz = w / (tilesx * tilesy);
+    const int i0 = bx * kDX, j0 = by * kDY, k0 = bz * kDepZ, k1 = min(k0 + kDepZ, g.nz);
+    const int is = i0 + sx == g.nx ? 0 : i0 + sx, js = j0 + sy == g.ny ? 0 : j0 + sy;
+    auto cell = [&](int m) { return at(g, is, js, m >= g.nz ? m - g.nz : m); };
+    SrcColumn q;
+    if (src) {
+      q.range(starts, cell(k0), q.s0, q.e0);
+      if (k0 + 1 <= k1) q.range(starts, cell(k0 + 1), q.s1, q.e1);
+      if (q.s0 < q.e0) q.p0 = perm[q.s0];
+    }
+    float aq = 0.f, ac = 0.f;
+    for (int m = k0; m <= k1; ++m) {
+      if (src) {  // in flight: plane m + 1's first particle, plane m + 2's range
+        q.p1 = q.s1 < q.e1 ? perm[q.s1] : 0;
+        q.s2 = q.e2 = 0;
+        if (m + 2 <= k1) q.range(starts, cell(m + 2), q.s2, q.e2);
+        float sq[8], sc[8];
+        corner_sums(perm, pay, np, q.s0, q.e0, q.p0, sq, sc);
+#pragma unroll
+        for (int o = 0; o < 8; ++o) {
+          S[o][sy][sx] = sq[o];
+          S[8 + o][sy][sx] = sc[o];
+        }
+      }
+      __syncthreads();
+      if (tgt && m > k0) {  // target plane m - 1: the corners of source plane m (dz = 1)
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+          for (int dx = 0; dx < 2; ++dx) {
+            const int o = (2 + dy) * 2 + dx;
+            aq += S[o][ty + dy][tx + dx];
+            ac += S[8 + o][ty + dy][tx + dx];
+          }
+        const long long c = at(g, i0 + tx, j0 + ty, m - 1);
+        const double qd = ff_f2d(aq);
+        Q[c] = qd;
+        C[c] = ff_f2d(ac);
+        bsum += qd;
+      }
+      if (tgt && m < k1) {  // target plane m: the corners of source plane m (dz = 0)
+        aq = 0.f;
+        ac = 0.f;
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+          for (int dx = 0; dx < 2; ++dx) {
+            const int o = dy * 2 + dx;
+            aq += S[o][ty + dy][tx + dx];
+            ac += S[8 + o][ty + dy][tx + dx];
+          }
+      }
+      q.s0 = q.s1; q.e0 = q.e1; q.p0 = q.p1; q.s1 = q.s2; q.e1 = q.e2;
+      __syncthreads();  // (the plane's sums are rewritten next)
+    }
+  }
+  const double b = block_sum(bsum, sh);
+  if (tid == 0) partials[blockIdx.x] = b;
+}
+
+// Two-way momentum source on the faces (k_dep_mom_cells + k_dep_mom_faces):
+// face d of cell c takes the upper sum of cell c - e_d plus the lower sum of
+// cell c.  Threads 0-255 own the tile's cells; threads 256-263 form the upper
+// x sums of the column below the tile in x and threads 264-295 the upper y
+// sums of the row below it in y, through shared memory; the upper z sum of a
+// thread's own cell stays in a register for the plane above.  The walk starts
+// one plane below the chunk (that plane's upper z sums).
+__global__ void __launch_bounds__(kDepThreads)
+k_dep_mom_zm(Grid g, const int32_t *__restrict__ starts, const int32_t *__restrict__ perm,
+             const float *__restrict__ pay, int64_t np, float *__restrict__ Fp) {
+  __shared__ float hxs[kDY][kDX + 1], hys[kDY + 1][kDX];
+  const int tid = threadIdx.x, tx = tid % kDX, ty = tid / kDX;
+  const bool own = tid < kDX * kDY, src = tid < kDX * kDY + kDY + kDX;
+  const int h = tid - kDX * kDY;
+  const int tilesx = g.nx / kDX, tilesy = g.ny / kDY, chunks = (g.nz + kDepZ - 1) / kDepZ;
+  const int items = tilesx * tilesy * chunks;
+  for (int w = blockIdx.x; w < items; w += gridDim.x) {
+    const int bx = w % tilesx, by = (w / tilesx) % tilesy, bz = w / (tilesx * tilesy);
+    const int i0 = bx * kDX, j0 = by * kDY, k0 = bz * kDepZ, k1 = min(k0 + kDepZ, g.nz);
+    const int il = i0 == 0 ? g.nx - 1 : i0 - 1, jl = j0 == 0 ? g.ny - 1 : j0 - 1;
+    const int is = own ? i0 + tx : (h < kDY ? il : i0 + h - kDY);
+    const int js = own ? j0 + ty : (h < kDY ? j0 + h : jl);
+    const int f1 = h < kDY ? 1 : 3;  // the one sum a halo cell gives
+    auto cell = [&](int m) { return at(g, is, js, m < 0 ? m + g.nz : m); };
+    SrcColumn q;
+    if (src) {
+      q.range(starts, cell(k0 - 1), q.s0, q.e0);
+      q.range(starts, cell(k0), q.s1, q.e1);
+      if (q.s0 < q.e0) q.p0 = perm[q.s0];
+    }
+    float hz = 0.f;
+    for (int m = k0 - 1; m < k1; ++m) {
+      float acc[6];
+#pragma unroll
+      for (int f = 0; f < 6; ++f) acc[f] = 0.f;
+      if (src) {
+        q.p1 = q.s1 < q.e1 ? perm[q.s1] : 0;
+        q.s2 = q.e2 = 0;
+        if (m + 2 < k1) q.range(starts, cell(m + 2), q.s2, q.e2);
+        if (own) {
+          for (int32_t s = q.s0; s < q.e0; ++s) {
+            const int32_t p = s == q.s0 ? q.p0 : perm[s];
+#pragma unroll
+            for (int f = 0; f < 6; ++f) acc[f] += pay[f * np + p];
+          }
+        } else {
+          float a1 = 0.f;
+          for (int32_t s = q.s0; s < q.e0; ++s) a1 += pay[f1 * np + (s == q.s0 ? q.p0 : perm[s])];
+          acc[f1] = a1;
+        }
+      }
+      q.s0 = q.s1; q.e0 = q.e1; q.p0 = q.p1; q.s1 = q.s2; q.e1 = q.e2;
+      if (m < k0) {  // the plane below the chunk: its upper z sums only
+        hz = acc[5];
+        continue;
+      }
+      if (own) {
+        hxs[ty][tx + 1] = acc[1];
+        hys[ty + 1][tx] = acc[3];
+      } else if (src) {
+        if (h < kDY)
+          hxs[h][0] = acc[1];
+        else
+          hys[0][h - kDY] = acc[3];
+      }
+      __syncthreads();
+      if (own) {
+        const long long c = at(g, i0 + tx, j0 + ty, m);
+        Fp[c] = hxs[ty][tx] + acc[0];
+        Fp[g.n + c] = hys[ty][tx] + acc[2];
+        Fp[2 * g.n + c] = hz + acc[4];
+        hz = acc[5];
+      }
+      __syncthreads();  // (the plane's sums are rewritten next)
+    }
+  }
+}
+
+// the fused deposits run on whole tiles with at most kRedBlocks blocks
+static bool dep_fused(const tpm_ctx *c) {
+  return c->g.nx % kDX == 0 && c->g.ny % kDY == 0 && c->dep_fused;
+}
+static int dep_blocks(tpm_ctx *c, const void *kernel) {
+  const long long items = (long long)(c->g.nx / kDX) * (c->g.ny / kDY) *
+                          ((c->g.nz + kDepZ - 1) / kDepZ);
+  const int b = wave_blocks(c, kernel, kDepThreads, items * kDepThreads, true);
+  return b < 1 ? 1 : b;
+}
+
 // wave_blocks for a cell kernel of this file (kThreads per block)
 template <typename K>
 int cell_waves(tpm_ctx *c, K *kernel, bool reduces) {
@@ -1005,7 +1228,11 @@ void particle_deposit_momentum(tpm_ctx *c) {
     return;
   }
   sort_by_cell(c, c->key_t, c->perm_t, c->starts_t, true);
-  if (mixed) {
+  if (mixed && dep_fused(c)) {
+    TPM_LAUNCH(c, "deposit_momentum", k_dep_mom_zm,
+               dep_blocks(c, reinterpret_cast<const void *>(k_dep_mom_zm)), kDepThreads, 0, c->g,
+               c->starts_t, c->perm_t, reinterpret_cast<const float *>(c->pay_t), c->np, c->Fp32);
+  } else if (mixed) {
     // (its own scratch: it runs beside the heat deposit)
     TPM_LAUNCH(c, "deposit_momentum_cells", k_dep_mom_cells,
                cell_waves(c, k_dep_mom_cells, false), kThreads, 0,
@@ -1037,11 +1264,17 @@ void particle_deposit_concentration(tpm_ctx *c) {
 // and the concentration of these positions into C_next
 static void heat_deposit(tpm_ctx *c) {
   const bool mixed = c->p.precision == TPM_PREC_MIXED;
-  const int nb = mixed ? cell_waves(c, k_dep_gather8, true)
-                       : cell_waves(c, k_dep_sum8x2<double>, true);
+  const bool fused = mixed && dep_fused(c);
+  const int nb = fused ? dep_blocks(c, reinterpret_cast<const void *>(k_dep_heat_zm))
+                 : mixed ? cell_waves(c, k_dep_gather8, true)
+                         : cell_waves(c, k_dep_sum8x2<double>, true);
   sort_by_cell(c, c->key_r, c->perm_r[0], c->starts_r[0], false);
   double *parts = c->partials + kPartQ * kRedBlocks;
-  if (mixed) {
+  if (fused) {
+    TPM_LAUNCH(c, "deposit_heat_conc", k_dep_heat_zm, nb, kDepThreads, 0, c->g, c->starts_r[0],
+               c->perm_r[0], reinterpret_cast<const float *>(c->pay_r), c->np, c->Q, c->C_next,
+               parts);
+  } else if (mixed) {
     TPM_LAUNCH(c, "deposit_corner_sums", k_dep_corners, cell_waves(c, k_dep_corners, false),
                kThreads, 0, c->g, c->starts_r[0], c->perm_r[0],
                reinterpret_cast<const float *>(c->pay_r), c->np, c->corner_sums);
@@ -1106,6 +1339,8 @@ void particle_kernels_setup(tpm_ctx *c) {
   cell_waves(c, k_dep_gather8, true);
   cell_waves(c, k_dep_sum8x2<double>, true);
   cell_waves(c, k_dep_corners, false);
+  dep_blocks(c, reinterpret_cast<const void *>(k_dep_heat_zm));
+  dep_blocks(c, reinterpret_cast<const void *>(k_dep_mom_zm));
 }
 
 // Continuation from a caller-held state: the given heat rates at x_int give

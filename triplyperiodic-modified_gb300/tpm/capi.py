@@ -26,6 +26,7 @@ OPT_STORE_DIVERGENCE = 1
 OPT_DIV_RESIDUAL_EVERY_STAGE = 2
 OPT_CUDA_GRAPH = 3
 OPT_FFT_TMA = 4
+OPT_FUSED_DEPOSITS = 5
 STATUS = {0: "TPM_OK", -1: "TPM_ERR_ARG", -2: "TPM_ERR_CUDA", -3: "TPM_ERR_TIMEOUT",
           -4: "TPM_ERR_NONFINITE", -5: "TPM_ERR_UNSUPPORTED", -6: "TPM_ERR_STATE",
           -7: "TPM_ERR_NOMEM"}
