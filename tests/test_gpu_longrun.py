@@ -1,4 +1,4 @@
-"""Long runs compared on the statistics the flow is judged by: TKE,
+"""Long runs compared on the statistics that characterise the flow: TKE,
 dissipation rate, energy spectrum and particle radial distribution function,
 within 2 %, GPU (FP64 and mixed) against the oracle over 100 RK4 steps of the
 32^3 box with 10^4 particles (the CPU-runnable workload).
