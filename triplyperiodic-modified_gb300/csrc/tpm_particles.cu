@@ -530,7 +530,10 @@ __global__ void k_scan_apply(int32_t *__restrict__ counts, long long n,
 // Lanes of a warp with equal keys take consecutive slots in lane order, that
 // is in particle order; only a cell whose particles arrive from more than one
 // warp (a group smaller than the cell's count) can end up out of order, and
-// only such cells are flagged for k_segsort.
+// only such cells are flagged for k_segsort.  A group that is the whole cell
+// (the usual case for particles kept in cell order) starts at the cell's
+// first slot without touching its cursor (the cursors are cleared before
+// every histogram).
 __global__ void k_scatter(const int32_t *__restrict__ key, int64_t np,
                           const int32_t *__restrict__ starts, int32_t *__restrict__ cursor,
                           int32_t *__restrict__ perm, unsigned char *__restrict__ unsorted) {
@@ -545,9 +548,9 @@ __global__ void k_scatter(const int32_t *__restrict__ key, int64_t np,
       const unsigned peers = __match_any_sync(live, k);
       const int leader = __ffs(peers) - 1;
       int32_t first = 0;
-      if (lane == leader) {
+      if (lane == leader && __popc(peers) != starts[k + 1] - starts[k]) {
         first = atomicAdd(&cursor[k], __popc(peers));
-        if (__popc(peers) != starts[k + 1] - starts[k]) unsorted[k] = 1;
+        unsorted[k] = 1;
       }
       first = __shfl_sync(live, first, leader);
       const int32_t slot = starts[k] + first + __popc(peers & ((1u << lane) - 1u));
