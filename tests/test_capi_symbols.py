@@ -30,6 +30,18 @@ def test_header_and_binding_agree():
     assert set(declared_functions()) == set(capi.SIGNATURES)
 
 
+def test_option_and_field_ids_match_the_header():
+    """The harness's option and field ids are the header's enum values."""
+    from tpm import capi
+
+    text = re.sub(r"/\*.*?\*/", "", open(os.path.join(REPO, "include", "tpm.h")).read(), flags=re.S)
+    opts = {m.group(1): int(m.group(2)) for m in re.finditer(r"\bTPM_OPT_([A-Z_0-9]+)\s*=\s*(\d+)", text)}
+    assert opts and opts == {n[4:]: v for n, v in vars(capi).items() if n.startswith("OPT_")}
+    body = re.search(r"TPM_FIELD_RU\s*=\s*0,(.*?)TPM_FIELD_COUNT", text, re.S).group(1)
+    names = ["RU"] + re.findall(r"TPM_FIELD_([A-Z_0-9]+)", body)
+    assert {n: i for i, n in enumerate(names)} == capi.FIELD
+
+
 def test_library_exports_every_declared_symbol(lib):
     for name in declared_functions():
         assert hasattr(lib, name), name
