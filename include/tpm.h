@@ -182,12 +182,15 @@ int tpm_save_state(tpm_ctx *ctx, double *RU, double *RU_int, double *Rho, double
                    double *const *part, double *rhs_t, tpm_scalars *scalars);
 
 /* tpm_load_state, one tpm_step and tpm_save_state in one call, with the same
- * results bit for bit, the host transfers overlapping the step: RU and P go up
- * while the resume and the first stage's particle stage run, the particles,
- * their heat rates and Rho come down during the last stage's pressure solve.
- * The inputs and outputs may be the same arrays.  Steps from a CUDA graph per
- * piece when TPM_OPT_CUDA_GRAPH is on.  (Not in the reference: its state is
- * host memory throughout.) */
+ * results bit for bit, the host transfers overlapping the step: the particle
+ * state goes up first, then Rho and RU_int while the resume's particle work
+ * runs, then RU and P while the first stage's head and particle deposits run;
+ * the particles, their heat rates and Rho come down during the last stage's
+ * pressure solve, and P, RU_int and RU each as soon as it is final.  The
+ * inputs and outputs may be the same arrays (pinned host memory gives the
+ * link's full rate).  Steps from a CUDA graph per piece when
+ * TPM_OPT_CUDA_GRAPH is on.  (Not in the reference: its state is host memory
+ * throughout.) */
 int tpm_step_state(tpm_ctx *ctx, const double *RU, const double *RU_int, const double *Rho,
                    const double *P, const double *const *part, const double *rhs_t, double P0,
                    double T_cur, int64_t num_timestep, double *RU_out, double *RU_int_out,
