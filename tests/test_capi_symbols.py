@@ -101,3 +101,15 @@ def test_create_rejects_out_of_scope_options_before_touching_the_device(lib):
     rc = lib.tpm_create(ctypes.byref(bad.to_c()), 10, ctypes.byref(h))
     assert rc == -1
     lib.tpm_destroy(h)
+
+
+def test_null_context_state_and_option_calls_fail_cleanly(lib):
+    """The host-state entry points and the options refuse a null context
+    with TPM_ERR_ARG before touching any buffer or device."""
+    n = None
+    assert lib.tpm_step_state(n, n, n, n, n, n, n, 0.0, 0.0, 0, n, n, n, n, n, n, n) == -1
+    assert lib.tpm_load_state(n, n, n, n, n, n, n, 0.0, 0.0, 0) == -1
+    assert lib.tpm_save_state(n, n, n, n, n, n, n, n) == -1
+    for opt in range(1, 6):
+        assert lib.tpm_set_option(n, opt, 1) == -1
+    assert lib.tpm_last_error(None) == b"null context"
